@@ -1,0 +1,389 @@
+"""Benchmark of the DDGI probe-update path (trace + blend) on GB300.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--workload NAME]
+
+A step is one frame of the probe update over the whole volume: ray
+generation, SDF march, hit shading, irradiance + distance blend with the
+border copy.  The metric is probe-rays/s = probes x rays x frames / time.
+
+  value        device-resident inputs, CUDA events around each frame on the
+               launching stream; a 256 MB L2 flush runs between frames
+               (outside the events)
+  e2e          the same frames through the C ABI with host buffers: each
+               step uploads the frame's direct-light atlas from pinned host
+               memory, updates, and reads both probe atlases back
+  roofline     the trace kernel: algorithmic SDF bytes (mip + full-res
+               trilinear taps actually taken + normal taps, counted per ray
+               in an untimed debug pass of the same frames) per launch over
+               its event time, against the measured HBM copy bandwidth
+  cpu_baseline the CPU oracle (FP32, OpenMP, all host threads) on a bounded
+               sample of probes of the same workload
+
+--impl reference times that CPU restatement of the reference shaders alone
+(the reference itself is a Windows Vulkan renderer with no CPU path and no
+graphics stack on this machine).  Under torchrun every rank updates its own
+replica of the volume (replicas only: the volumes are independent).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "probe-rays/s (trace+blend) at ≤2e-3 rel irradiance err vs FP64; served p99 ms"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="production_32x16x32_r256_sdf256")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline time budget")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path("/tmp") / f"luxgi_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def traffic_from_profile(workload: str, kernel: str):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(workload, {}).get(kernel)
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------- CPU oracle leg
+def cpu_baseline(w, host, rot, seconds: float, gpu_frame0=None):
+    """FP32 oracle trace + blend on a bounded sample of probes, all threads.
+    Also the FP64 irradiance error of the GPU frame-0 atlases on a sample."""
+    import numpy as np
+
+    import oracle
+
+    vd = w.volume.desc()
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    R = w.volume.rays_per_probe
+    P = w.volume.probes
+    threads = oracle.num_threads()
+    n = min(P, 32)
+    elapsed = 0.0
+    while True:
+        t0 = time.perf_counter()
+        rays, _ = oracle.trace(vd, inp, rot, 0, precision=0, probes=(0, n), want_info=False)
+        dirs = oracle.ray_dirs(rot, R, 0)
+        oracle.blend(vd, dirs, rays, first=True, precision=0, border=False, probes=(0, n))
+        elapsed = time.perf_counter() - t0
+        if elapsed * 4 > seconds or n >= P:
+            break
+        n = min(P, max(n * 2, int(n * seconds / 2 / max(elapsed, 1e-3))))
+    out = {"value": n * R / elapsed, "unit": "probe-rays/s", "cores": threads, "kind": "port",
+           "sample": f"{n} probes x {R} rays x 1 frame of {w.name} (oracle FP32 trace + blend, {elapsed:.2f} s)"}
+    err = None
+    if gpu_frame0 is not None:
+        gi, _ = gpu_frame0
+        m = min(P, 64)
+        r64, _ = oracle.trace(vd, inp, rot, 0, precision=1, probes=(0, m), want_info=False)
+        d64 = oracle.ray_dirs(rot, R, 1)
+        i64, _ = oracle.blend(vd, d64, r64, first=True, precision=1, border=True, probes=(0, m))
+        u = vd.uniform
+        n_ = u.irradiance_probe_side
+        XY = u.probe_counts[0] * u.probe_counts[1]
+        errs = []
+        for p in range(m):
+            cx, cy = p % XY, p // XY
+            ys = slice(cy * (n_ + 2) + 2, cy * (n_ + 2) + 2 + n_)
+            xs = slice(cx * (n_ + 2) + 2, cx * (n_ + 2) + 2 + n_)
+            a, b = gi[ys, xs, :3].astype(np.float64), i64[ys, xs, :3].astype(np.float64)
+            errs.append(np.abs(a - b) / np.maximum(np.abs(b), 1e-3))
+        e = np.concatenate([x.ravel() for x in errs])
+        err = {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)), "median": float(np.median(e)),
+               "probes": m, "frame": 0}
+    return out, err
+
+
+# ------------------------------------------------------------------- ours
+def run_ours(args, rank: int, world: int):
+    import numpy as np
+    import torch
+
+    from luxgi_gb300 import DDGIVolume, DeviceScene, HostScene, WORKLOADS, frame_rotation, _native as N
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev_t = torch.device("cuda", local)
+    w = WORKLOADS[args.workload]
+    v = w.volume
+    P, R = v.probes, v.rays_per_probe
+    host = HostScene(w.scene)
+    dev = DeviceScene(host, v.light_mode, device=f"cuda:{local}")
+    vol = DDGIVolume(v)
+    vol.bind_scene(dev)
+    seed = 0x5EED + rank
+    K, W = args.steps, args.warmup
+    rots = [frame_rotation(seed, f) for f in range(W + K)]
+    stream = torch.cuda.current_stream()
+
+    # frame 0 (first warm-up frame), kept for the FP64 error check
+    vol.update(rots[0])
+    torch.cuda.synchronize()
+    irr0 = vol.atlases()[0].float().cpu().numpy()
+    for f in range(1, W):
+        vol.update(rots[f])
+    torch.cuda.synchronize()
+
+    # exact algorithmic bytes of the timed traces (untimed debug pass; the
+    # march does not depend on the atlases, so counts equal the timed ones)
+    vol.set_debug_rays(True)
+    esz = 2 if host.sdf_format == N.STORAGE_FP16 else 4
+    out_b = 8 if v.storage == N.STORAGE_FP16 else 16
+    march_bytes = []
+    steps_total = 0
+    for f in range(W, W + K):
+        vol.trace(rots[f])
+        info = vol.rays()[2]
+        s = info[..., 0].to(torch.int64).sum().item()
+        fine = info[..., 2].to(torch.int64).sum().item()
+        hits = (info[..., 1] >= 0).sum().item()
+        steps_total += s
+        march_bytes.append((s * 8 + fine * 8 + hits * 48) * esz + P * R * out_b)
+    vol.set_debug_rays(False)
+    torch.cuda.synchronize()
+
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev_t)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    clocks = Clocks(local)
+    launches0 = N.ddgi().luxgi_launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for k in range(K):
+        flush.zero_()
+        ev[k][0].record(stream)
+        vol.trace(rots[W + k], stream)
+        ev[k][1].record(stream)
+        vol.probe_update(stream)
+        ev[k][2].record(stream)
+        vol.end_frame()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    launches = N.ddgi().luxgi_launch_count() - launches0
+    t_trace = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
+    t_blend = [ev[k][1].elapsed_time(ev[k][2]) for k in range(K)]
+    t_frame = sum(t_trace) + sum(t_blend)          # ms, flush excluded
+    if world > 1:
+        t = torch.tensor([t_frame], device=dev_t)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_frame = float(t.item())
+    value = world * P * R * K / (t_frame / 1e3)
+
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        direct_h = torch.from_numpy(host.direct.view(np.int16)).pin_memory()
+        irr, dist = vol.atlases()
+        irr_h = torch.empty(irr.shape, dtype=irr.dtype).pin_memory()
+        dist_h = torch.empty(dist.shape, dtype=dist.dtype).pin_memory()
+        erots = [frame_rotation(seed + 1000, f) for f in range(K)]
+        for f in range(2):
+            dev.direct.copy_(direct_h, non_blocking=True)
+            vol.update(erots[f])
+            irr, dist = vol.atlases()
+            irr_h.copy_(irr, non_blocking=True)
+            dist_h.copy_(dist, non_blocking=True)
+            torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for k in range(K):
+            dev.direct.copy_(direct_h, non_blocking=True)
+            vol.update(erots[k])
+            irr, dist = vol.atlases()
+            irr_h.copy_(irr, non_blocking=True)
+            dist_h.copy_(dist, non_blocking=True)
+            torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([te], device=dev_t)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": world * P * R * K / te, "unit": "probe-rays/s",
+               "h2d_bytes_per_step": int(direct_h.numel() * 2 + 36),
+               "d2h_bytes_per_step": int(irr_h.numel() * irr_h.element_size() + dist_h.numel() * dist_h.element_size())}
+
+    pk = peaks()
+    avg_trace_ms = sum(t_trace) / K
+    avg_bytes = sum(march_bytes) / K
+    achieved = avg_bytes / (avg_trace_ms / 1e3) / 1e9
+    traffic = traffic_from_profile(w.name, "trace_kernel")
+    roofline = {"kernel": "trace_kernel (ray gen + SDF march + hit shading)", "bound": "hbm",
+                "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / pk["hbm_gbs"], 4), "peak_source": pk["source"],
+                "traffic": traffic, "algorithmic_bytes_per_launch": int(avg_bytes),
+                "avg_launch_ms": round(avg_trace_ms, 4), "avg_march_steps_per_ray": round(steps_total / (K * P * R), 2)}
+    if rank != 0:
+        return
+    cpu, err = (None, None)
+    if not args.no_cpu:
+        cpu, err = cpu_baseline(w, host, rots[0], args.cpu_seconds, gpu_frame0=(irr0, None))
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "probe-rays/s", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": round(t_frame / K, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded analytic scene)",
+        "config": {"workload": w.name, "probes": P, "rays_per_probe": R, "probe_counts": list(v.probe_counts),
+                   "sdf": f"{host.res}^3 {'fp16' if host.sdf_format else 'fp32'}", "atlas": host.atlas,
+                   "octahedral_sides": [v.irradiance_side, v.depth_side], "max_steps": v.max_steps,
+                   "light_mode": "per-hit bounce" if v.light_mode else "light cache",
+                   "blend": "tensor" if v.blend else "fp32 simt", "storage": "fp16" if v.storage else "fp32",
+                   "parallelism": f"replicas{world}", "l2": "256 MB flush between frames (outside the events)"},
+        "stage_ms": {"trace": round(avg_trace_ms, 4), "blend": round(sum(t_blend) / K, 4)},
+        "wall_s": round(wall, 4),
+        "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
+        "irradiance_rel_err_vs_fp64": err, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------- reference
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    import oracle
+    from luxgi_gb300 import HostScene, WORKLOADS, frame_rotation
+
+    w = WORKLOADS[args.workload]
+    v = w.volume
+    host = HostScene(w.scene)
+    vd = v.desc()
+    inp = oracle.HostInputs(host, v.light_mode)
+    R = v.rays_per_probe
+    n = min(v.probes, 64)
+    rots = [frame_rotation(0x5EED, f) for f in range(args.warmup + args.steps)]
+    state = None
+
+    def step(rot):
+        rays, _ = oracle.trace(vd, inp, rot, 0, precision=0, probes=(0, n), want_info=False)
+        oracle.blend(vd, oracle.ray_dirs(rot, R, 0), rays, first=True, precision=0, border=False, probes=(0, n))
+
+    for f in range(args.warmup):
+        step(rots[f])
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(rots[args.warmup + k])
+    dt = time.perf_counter() - t0
+    value = n * R * args.steps / dt
+    cores = oracle.num_threads()
+    sample = f"{n} probes x {R} rays per step of {w.name} (CPU restatement of the reference shaders, FP32)"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "probe-rays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded analytic scene)",
+            "config": {"workload": w.name, "probes": v.probes, "rays_per_probe": R, "parallelism": "cpu"},
+            "cpu_baseline": {"value": round(value, 1), "unit": "probe-rays/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 1), "unit": "probe-rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1 and args.impl == "ours":
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,300 @@
+/*
+ * luxgi_ddgi.h -- C ABI of the GB300 (sm_103a) DDGI probe-update path.
+ *
+ * This library replaces the non-raytracing ("SoftTrace") DDGI probe update of
+ * LuxGI/Maple: the three ECS systems
+ *     trace_rays::system    Code/Maple/src/Engine/DDGI/DDGIRenderer.cpp:217-330
+ *     probe_update::system  Code/Maple/src/Engine/DDGI/DDGIRenderer.cpp:347-413
+ *     border_update::system Code/Maple/src/Engine/DDGI/DDGIRenderer.cpp:418-464
+ *     end_frame::system     Code/Maple/src/Engine/DDGI/DDGIRenderer.cpp:335-342
+ * and the shaders they dispatch (Shaders/DDGI/GISDFRays.comp,
+ * Shaders/DDGI/ProbeUpdate.glsl, Shaders/DDGI/BorderUpdate.glsl).
+ *
+ * Conventions
+ *   - every entry point returns an int status: 0 = LUXGI_OK, negative = error;
+ *     no exceptions cross the ABI;
+ *   - all buffer arguments are plain pointers; "device" pointers must be CUDA
+ *     device (or managed) memory, "host" pointers ordinary host memory;
+ *   - a `stream` argument is a cudaStream_t passed as void* (NULL = legacy
+ *     default stream);
+ *   - the library never frees memory it did not allocate; scene inputs bound
+ *     with luxgi_ddgi_bind_scene stay owned by the caller and must outlive the
+ *     volume's use of them;
+ *   - a volume is not thread-safe; use one volume per caller thread, or
+ *     serialise calls on it.
+ *
+ * Texel/array layouts (all "x fastest"):
+ *   SDF volume       (res*C) x res x res, cascades packed along x
+ *                    (GlobalDistanceField.cpp:615, SDFRasterizeModel.glsl:47)
+ *   SDF mip          (mres*C) x mres x mres, mres = res/4
+ *   probe atlases    width x height texels, width  = (n+2)*X*Y + 2,
+ *                    height = (n+2)*Z + 2   (DDGIRenderer.cpp:182-185);
+ *                    irradiance = 4 channels (RGBA), distance = 2 (RG);
+ *                    element type FP32 or FP16 (luxgi_storage)
+ *   surface atlases  res x res texels (GlobalSurfaceAtlas.cpp:91)
+ */
+#ifndef LUXGI_DDGI_H
+#define LUXGI_DDGI_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define LUXGI_OK            0
+#define LUXGI_EINVAL       -1   /* bad argument (null pointer, bad dims ...)  */
+#define LUXGI_ENOMEM       -2   /* device allocation or capacity exhausted    */
+#define LUXGI_ECUDA        -3   /* a CUDA runtime call failed                 */
+#define LUXGI_ETIMEOUT     -4   /* a bounded device-side wait gave up         */
+#define LUXGI_ENOTBOUND    -5   /* luxgi_ddgi_bind_scene was not called       */
+#define LUXGI_EUNSUPPORTED -6   /* option not available on this device/build  */
+
+/* ---------------------------------------------------------------- enums */
+enum luxgi_storage {           /* element type of ray buffers and atlases      */
+    LUXGI_STORAGE_FP32 = 0,    /* FP32 atlases (meets 1e-4 rel vs FP64)        */
+    LUXGI_STORAGE_FP16 = 1     /* RGBA16F/RG16F like the reference (F4)        */
+};
+enum luxgi_light_mode {
+    LUXGI_LIGHT_CACHE   = 0,   /* hits sample the light-cache atlas; infinite
+                                  bounce is injected into that atlas by
+                                  luxgi_ddgi_inject_indirect
+                                  (GISDFRays.comp:104-118,
+                                   SDFAtlasIndirectLight.frag:44-67)           */
+    LUXGI_LIGHT_PER_HIT = 1    /* hits sample the direct-light and albedo
+                                  atlases and add albedo/pi * E_prev(hit)
+                                  (Raytraced/Lighting.glsl:79-84)              */
+};
+enum luxgi_blend {
+    LUXGI_BLEND_FP32   = 0,    /* FP32 SIMT contraction                        */
+    LUXGI_BLEND_TENSOR = 1     /* tcgen05 FP16 operands, FP32 accumulation;
+                                  distance data split hi+lo                    */
+};
+
+/* ------------------------------------------------------- parameter blocks */
+
+/* DDGIUniform (Shaders/DDGI/DDGICommon.glsl:11-31, host copy
+ * Engine/DDGI/DDGIRenderer.h:22-42), scalar layout, 96 bytes.  Width and
+ * height fields left at 0 are derived by luxgi_ddgi_derive_uniform. */
+typedef struct luxgi_ddgi_uniform {
+    float   start_position[4];
+    float   step[4];
+    int32_t probe_counts[4];
+    float   max_distance;
+    float   sharpness;
+    float   hysteresis;
+    float   normal_bias;
+    float   ddgi_gamma;
+    int32_t irradiance_probe_side;
+    int32_t irradiance_width;
+    int32_t irradiance_height;
+    int32_t depth_probe_side;
+    int32_t depth_width;
+    int32_t depth_height;
+    int32_t rays_per_probe;
+} luxgi_ddgi_uniform;
+
+/* GlobalSDFData (Shaders/SDF/GlobalSDFData.glsl), 96 bytes. */
+typedef struct luxgi_sdf_data {
+    float    cascade_pos_distance[4][4];  /* center.xyz, half extent w      */
+    float    cascade_voxel_size[4];
+    uint32_t cascades_count;
+    float    resolution;
+    float    near_plane;
+    float    far_plane;
+} luxgi_sdf_data;
+
+/* GlobalSurfaceAtlasData (Shaders/SDF/AtlasCommon.glsl:8-16), 32 bytes. */
+typedef struct luxgi_surface_data {
+    float    camera_pos[3];
+    float    chunk_size;
+    uint32_t culled_objects_capacity;
+    uint32_t resolution;
+    uint32_t objects_count;
+    uint32_t padding;
+} luxgi_surface_data;
+
+/* ObjectBuffer (AtlasCommon.glsl:18-25, std430), 128 bytes.  Matrices are
+ * column-major.  tile_offset[i] == 0 means "no tile" (AtlasCommon.glsl:143),
+ * so tile slot 0 is never a real tile. */
+typedef struct luxgi_surface_object {
+    float    object_bounds[4];     /* bounding sphere center.xyz, radius     */
+    uint32_t tile_offset[6];
+    int32_t  padding[2];
+    float    transform[16];        /* object(OBB) -> world                   */
+    float    extends[4];           /* OBB half extents                       */
+} luxgi_surface_object;
+
+/* TileBuffer (AtlasCommon.glsl:27-32), 96 bytes. */
+typedef struct luxgi_surface_tile {
+    float extends[4];              /* (x, y, w-1, h-1) / atlas resolution    */
+    float transform[16];           /* tile view rotation, translation zeroed */
+    float object_bounds[4];        /* tile-space bounds size (x, y, z, 0)    */
+} luxgi_surface_tile;
+
+/* Scene inputs produced upstream of the path: the global SDF and its mip
+ * (GlobalDistanceFieldPublic, GlobalDistanceField.h:31-42). */
+typedef struct luxgi_sdf_desc {
+    luxgi_sdf_data data;
+    int32_t     format;            /* luxgi_storage: element type of sdf/mip  */
+    int32_t     resolution;        /* res  (texels per cascade side)          */
+    int32_t     mip_resolution;    /* mres (res / 4)                          */
+    int32_t     reserved;
+    const void* sdf;               /* device, (res*C) x res x res             */
+    const void* mip;               /* device, (mres*C) x mres x mres          */
+} luxgi_sdf_desc;
+
+/* The surface cache (GlobalSurfacePublic, GlobalSurfaceAtlas.h:31-44). */
+typedef struct luxgi_surface_desc {
+    luxgi_surface_data          data;
+    int32_t                     num_objects;
+    int32_t                     num_tiles;      /* including dummy slot 0     */
+    const luxgi_surface_object* objects;        /* device                     */
+    const luxgi_surface_tile*   tiles;          /* device                     */
+    const uint32_t*             chunks;         /* device, 40^3 u32           */
+    const uint32_t*             culled_objects; /* device, [0] = used words   */
+    void*                       light_cache;    /* device RGBA16F res^2 (mode A
+                                                   sampled; written by inject) */
+    const float*                depth;          /* device R32F res^2, 1 = empty*/
+    const uint16_t*             direct_light;   /* device RGBA16F res^2       */
+    const uint8_t*              albedo;         /* device RGBA8 UNORM res^2   */
+    const float*                gbuffer0;       /* device float4: albedo.rgb,
+                                                   world.x (SDFDeferredColor
+                                                   .frag:114)                 */
+    const float*                gbuffer1;       /* device float4: oct normal.xy,
+                                                   world.yz (:115)            */
+} luxgi_surface_desc;
+
+/* Volume configuration: DDGIUniform plus the IrradianceVolume fields the
+ * path reads (DDGIRenderer.h:44-60) and the build's own switches. */
+typedef struct luxgi_ddgi_volume_desc {
+    luxgi_ddgi_uniform uniform;
+    int32_t storage;               /* luxgi_storage                           */
+    int32_t light_mode;            /* luxgi_light_mode                        */
+    int32_t blend;                 /* luxgi_blend                             */
+    int32_t max_steps;             /* march step cap per cascade; 250 in the
+                                      reference (SDFCommon.glsl:143)          */
+    int32_t infinite_bounce;       /* IrradianceVolume::infiniteBounce        */
+    float   intensity;             /* IrradianceVolume::intensity             */
+    float   sky_radiance[3];       /* constant sky for misses                 */
+    int32_t reserved[8];
+} luxgi_ddgi_volume_desc;
+
+/* Device views of a volume's probe atlases. */
+typedef struct luxgi_ddgi_atlases {
+    void*   irradiance;            /* current (last written) irradiance       */
+    void*   distance;              /* current distance                        */
+    void*   prev_irradiance;       /* the other ping-pong copy                */
+    void*   prev_distance;
+    int32_t irradiance_width, irradiance_height;
+    int32_t depth_width, depth_height;
+    int32_t storage;               /* luxgi_storage                           */
+    int32_t frames;                /* frames completed                        */
+} luxgi_ddgi_atlases;
+
+/* Device views of the last trace's per-ray results (the reference's
+ * "DDGI Raytrace Radiance" / "Direction Depth" textures, DDGIRenderer.cpp:173-177). */
+typedef struct luxgi_ddgi_rays {
+    const float* directions;       /* float4 [R]: rotated ray directions      */
+    const void*  radiance;         /* [P][R] x4: rgb radiance, hit distance;
+                                      FP32 or FP16 per storage                */
+    const int32_t* hit_info;       /* int4 [P][R]: march steps, hit cascade
+                                      (-1 miss), full-resolution SDF samples,
+                                      0; NULL unless debug rays are on       */
+    int32_t probes, rays, storage;
+} luxgi_ddgi_rays;
+
+typedef struct luxgi_ddgi_volume luxgi_ddgi_volume;
+
+/* ------------------------------------------------------------ volumes */
+
+/* Fill width/height fields of `u` from probe counts and sides
+ * (DDGIRenderer.cpp:182-185) and validate it.  Host only. */
+int luxgi_ddgi_derive_uniform(luxgi_ddgi_uniform* u);
+
+/* Rotation matrix of angleAxis(angle, axis) as a column-major 3x3
+ * (DDGIRenderer.cpp:267-272: glm::mat4_cast(glm::angleAxis(...))). Host only. */
+int luxgi_ddgi_rotation(const float axis[3], float angle, float out_mat3[9]);
+
+/* The seeded per-frame rotation used in place of std::random_device (F5):
+ * xoshiro256** seeded by splitmix64(seed); axis = normalize(U(-1,1)^3),
+ * angle = U(0,1) * 2pi, drawn in that order for each frame. Host only. */
+int luxgi_ddgi_frame_rotation(uint64_t seed, uint32_t frame, float out_mat3[9]);
+
+/* Allocate a volume (both atlas copies, per-ray buffers, weight tables) on
+ * the current device.  Replaces ddgi::on_game_start + initializeProbeGrid
+ * (DDGIRenderer.cpp:163-211, 565-683).  Atlases start zeroed. */
+int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** out);
+int luxgi_ddgi_destroy(luxgi_ddgi_volume* vol);
+
+/* Bind scene inputs (device pointers, caller-owned). */
+int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* vol, const luxgi_sdf_desc* sdf,
+                          const luxgi_surface_desc* surface);
+
+/* trace_rays::system: ray generation under `rot` (column-major 3x3) plus
+ * SDF march and hit shading into the per-ray buffers. */
+int luxgi_ddgi_trace(luxgi_ddgi_volume* vol, const float rot[9], void* stream);
+/* probe_update::system: irradiance and distance blend into the write copy
+ * (1 - pingPong), reading the previous copy; the border copy is fused in. */
+int luxgi_ddgi_probe_update(luxgi_ddgi_volume* vol, void* stream);
+/* border_update::system, standalone (in place on the write copy). */
+int luxgi_ddgi_border_update(luxgi_ddgi_volume* vol, void* stream);
+/* end_frame::system: flip ping-pong, frames++.  Host only. */
+int luxgi_ddgi_end_frame(luxgi_ddgi_volume* vol);
+
+/* One whole frame: trace + probe update (fused border) + end_frame. */
+int luxgi_ddgi_update(luxgi_ddgi_volume* vol, const float rot[9], void* stream);
+
+/* Many volumes, one frame each, in one persistent launch per stage.
+ * rots = n consecutive column-major 3x3 matrices (host). */
+int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n,
+                            const float* rots, void* stream);
+
+int luxgi_ddgi_get_atlases(const luxgi_ddgi_volume* vol, luxgi_ddgi_atlases* out);
+int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* vol, luxgi_ddgi_rays* out);
+/* Record per-ray march steps / hit cascade on the next traces (test aid). */
+int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* vol, int enable);
+/* Overwrite both atlas copies from host buffers of the volume's storage type
+ * and set the frame counter (atlas persistence / restore). */
+int luxgi_ddgi_load_atlases(luxgi_ddgi_volume* vol, const void* irradiance_host,
+                            const void* distance_host, int32_t frames, void* stream);
+
+/* Mode A infinite bounce (SDFAtlasIndirectLight.frag:44-67): for every
+ * surface-atlas texel covered by a tile, light_cache = direct_light +
+ * intensity * min(albedo,0.9)/pi * sampleIrradiance(prev atlases).  When
+ * infinite bounce is off or no frame is done yet it copies direct_light. */
+int luxgi_ddgi_inject_indirect(luxgi_ddgi_volume* vol, void* stream);
+
+/* sampleIrradiance (DDGICommon.glsl:163-233) for n points against the
+ * volume's current atlases: positions, normals, view vectors float3 [n]
+ * (device), out float3 [n] (device). */
+int luxgi_ddgi_sample_irradiance(const luxgi_ddgi_volume* vol, const float* pos,
+                                 const float* nrm, const float* wo, float* out,
+                                 int n, void* stream);
+
+/* ------------------------------------------------------- scene set-up */
+
+/* GlobalSDFMipmap.comp + 4 flood passes (GlobalDistanceField.cpp:537-573,
+ * 823-841): mip (device) from sdf (device), for every cascade.  `tmp` is a
+ * device buffer of mres^3 elements. */
+int luxgi_sdf_build_mip(const luxgi_sdf_desc* sdf, void* mip, void* tmp, void* stream);
+
+/* SDFCulling.comp: chunk table (40^3 u32, device) and culled-object lists
+ * (device, `capacity` u32) for the objects of `surface`.  Layout is
+ * deterministic: chunks in flattened order, objects in index order; entry
+ * [0] of the list holds the number of words used.  Returns LUXGI_ENOMEM
+ * when the lists do not fit (chunks that do not fit stay empty). */
+int luxgi_surface_cull(const luxgi_surface_desc* surface, uint32_t* chunks,
+                       uint32_t* culled, uint32_t capacity, void* stream);
+
+/* ------------------------------------------------------------ misc */
+const char* luxgi_strerror(int status);
+/* Kernel launches issued by this library since load (all entry points). */
+uint64_t luxgi_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LUXGI_DDGI_H */

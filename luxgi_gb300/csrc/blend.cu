@@ -1,0 +1,315 @@
+// Probe blend (ProbeUpdate.glsl) as a contraction, and the border copy
+// (BorderUpdate.glsl).
+//
+// Every probe of a volume traces the same R directions in a frame (one
+// rotation per frame, DDGIRenderer.cpp:267-272), so the texel x ray weights
+//   irradiance  W[t][r] = max(0, D_t . dir_r)                 (ProbeUpdate.glsl:219)
+//   distance    W[t][r] = pow(max(0, D_t . dir_r), sharpness) (ProbeUpdate.glsl:217)
+// (zeroed below 1e-8, ProbeUpdate.glsl:222) and the normalisers
+// 1 / (2 sum_r W[t][r]) are shared by all probes.  The blend is then
+//   out[p][t][c] = n[t] * sum_r W[t][r] * ray[p][r][c]
+// followed by the gamma encode, the hysteresis mix and the store; the
+// border copy is fused into the store (each interior texel writes its
+// border mirrors too).
+#include <cuda_fp16.h>
+
+#include "luxgi_internal.h"
+
+namespace luxgi {
+
+// ------------------------------------------------------------- weights
+// One thread per texel row: octDecode(normalizedOctCoord) (DDGICommon.glsl:
+// 74-92) against every ray direction; sequential sum like the reference.
+// Also writes the FP16 K-major weight operands of the tensor-core blend
+// (rows padded with zeros) and their own normalisers.
+__global__ void weights_kernel(const luxgi_ddgi_uniform u, const float4* __restrict__ dirs, float* __restrict__ w_irr,
+                               float* __restrict__ w_dist, float* __restrict__ n_irr, float* __restrict__ n_dist,
+                               __half* __restrict__ tcw_irr, __half* __restrict__ tcw_dist, int tc_n_irr,
+                               int tc_n_dist) {
+    const int ni = u.irradiance_probe_side, nd = u.depth_probe_side;
+    const int Ti = ni * ni, Td = nd * nd;
+    const int R = u.rays_per_probe;
+    const bool tc = tcw_irr != nullptr;
+    const int rows_i = tc ? tc_n_irr : Ti;      // tensor-core rows are padded (>= T)
+    const int rows_d = tc ? tc_n_dist : Td;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= rows_i + rows_d) return;
+    const bool depth = row >= rows_i;
+    const int t = depth ? row - rows_i : row;
+    const int n = depth ? nd : ni;
+    const int T = depth ? Td : Ti;
+    __half* tcw = depth ? tcw_dist : tcw_irr;
+    if (t >= T) {                                  // tensor-core padding row
+        for (int r = 0; r < R; ++r) tcw[size_t(t) * R + r] = __float2half_rn(0.0f);
+        return;
+    }
+    const int tx = t % n, ty = t / n;
+    const float s = 2.0f / float(n);
+    const float ox = (float(tx) + 0.5f) * s - 1.0f, oy = (float(ty) + 0.5f) * s - 1.0f;
+    f3 v{ox, oy, 1.0f - fabsf(ox) - fabsf(oy)};
+    if (v.z < 0.0f) {
+        const float nx = (1.0f - fabsf(v.y)) * sign_nz(v.x);
+        const float ny = (1.0f - fabsf(v.x)) * sign_nz(v.y);
+        v.x = nx; v.y = ny;
+    }
+    const f3 td = norm3(v);
+    float* w = depth ? w_dist : w_irr;
+    float sum = 0.0f, sum_h = 0.0f;
+    for (int r = 0; r < R; ++r) {
+        const float4 d = __ldg(dirs + r);
+        const float c = mx(0.0f, td.x * d.x + td.y * d.y + td.z * d.z);
+        float wt = depth ? powf(c, u.sharpness) : c;
+        if (!(wt >= 1e-8f)) wt = 0.0f;
+        w[size_t(t) * R + r] = wt;
+        sum = sum + wt;
+        if (tc) {
+            const __half h = __float2half_rn(wt);
+            tcw[size_t(t) * R + r] = h;
+            sum_h = sum_h + __half2float(h);
+        }
+    }
+    float* nrm = depth ? n_dist : n_irr;
+    nrm[t] = (sum > 1e-8f) ? 1.0f / (2.0f * sum) : 1.0f;
+    if (tc) nrm[T + t] = (sum_h > 1e-8f) ? 1.0f / (2.0f * sum_h) : 1.0f;   // tensor-core normaliser
+}
+
+cudaError_t launch_weights(const luxgi_ddgi_uniform& u, const float4* dirs, float* w_irr, float* w_dist, float* n_irr,
+                           float* n_dist, __half* tc_w_irr, __half* tc_w_dist, int tc_n_irr, int tc_n_dist,
+                           cudaStream_t st) {
+    const int Ti = u.irradiance_probe_side * u.irradiance_probe_side;
+    const int Td = u.depth_probe_side * u.depth_probe_side;
+    const int rows = tc_w_irr ? tc_n_irr + tc_n_dist : Ti + Td;
+    weights_kernel<<<(rows + 63) / 64, 64, 0, st>>>(u, dirs, w_irr, w_dist, n_irr, n_dist, tc_w_irr, tc_w_dist,
+                                                    tc_n_irr, tc_n_dist);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- store helpers
+template <typename AT> struct AtlasIO;
+template <> struct AtlasIO<float> {
+    __device__ static float ld(const void* p, size_t i) { return static_cast<const float*>(p)[i]; }
+    __device__ static float rnd(float v) { return v; }
+    __device__ static void st(void* p, size_t i, float v) { static_cast<float*>(p)[i] = v; }
+};
+template <> struct AtlasIO<__half> {
+    __device__ static float ld(const void* p, size_t i) { return __half2float(static_cast<const __half*>(p)[i]); }
+    __device__ static float rnd(float v) { return __half2float(__float2half_rn(v)); }
+    __device__ static void st(void* p, size_t i, float v) { static_cast<__half*>(p)[i] = __float2half_rn(v); }
+};
+
+// Writes channel values v[0..nc) of interior texel (tx, ty) of cell
+// (cx, cy) and its border mirrors (BorderUpdate.glsl:136-156, rule
+// generalised from the 8/16 tables at :25-133).
+template <typename AT, int NC>
+__device__ __forceinline__ void store_texel(void* atlas, int W, int n, int cx, int cy, int tx, int ty, const float* v) {
+    const int ox = cx * (n + 2) + 1, oy = cy * (n + 2) + 1;   // cell origin (border corner)
+    const int X = tx + 1, Y = ty + 1;                        // cell-relative interior coords
+    int dx[9], dy[9];
+    int nd = 0;
+    dx[nd] = X; dy[nd] = Y; ++nd;
+    if (Y == 1) { dx[nd] = n + 1 - X; dy[nd] = 0; ++nd; }
+    if (Y == n) { dx[nd] = n + 1 - X; dy[nd] = n + 1; ++nd; }
+    if (X == 1) { dx[nd] = 0; dy[nd] = n + 1 - Y; ++nd; }
+    if (X == n) { dx[nd] = n + 1; dy[nd] = n + 1 - Y; ++nd; }
+    // corners: (0,0)<-(n,n), (n+1,0)<-(1,n), (0,n+1)<-(n,1), (n+1,n+1)<-(1,1)
+    if (X == n && Y == n) { dx[nd] = 0; dy[nd] = 0; ++nd; }
+    if (X == 1 && Y == n) { dx[nd] = n + 1; dy[nd] = 0; ++nd; }
+    if (X == n && Y == 1) { dx[nd] = 0; dy[nd] = n + 1; ++nd; }
+    if (X == 1 && Y == 1) { dx[nd] = n + 1; dy[nd] = n + 1; ++nd; }
+    for (int k = 0; k < nd; ++k) {
+        const size_t base = (size_t(oy + dy[k]) * W + (ox + dx[k])) * NC;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) AtlasIO<AT>::st(atlas, base + c, v[c]);
+    }
+}
+
+// --------------------------------------------------------------- blend
+// Block = 256 threads over (texel, probe-of-block) pairs; rays in chunks of
+// KC through shared memory (weights stored ray-major so a warp's texels hit
+// distinct banks, ray data broadcast).
+constexpr int kBlendThreads = 256;
+constexpr int kPairsPerThread = 4;
+constexpr int kRayChunk = 32;
+
+template <int DEPTH, typename RT, typename AT>
+__global__ void __launch_bounds__(kBlendThreads) blend_kernel(const BlendParams p, int PB) {
+    extern __shared__ float smem[];
+    const luxgi_ddgi_uniform& u = p.u;
+    const int n = DEPTH ? u.depth_probe_side : u.irradiance_probe_side;
+    const int T = n * n;
+    const int W = DEPTH ? u.depth_width : u.irradiance_width;
+    const int R = p.R;
+    const int p0 = blockIdx.x * PB;
+    float* Ws = smem;                                  // [KC][T]
+    float4* Rs = reinterpret_cast<float4*>(smem + kRayChunk * T);   // [PB][KC]
+    const float* Wg = DEPTH ? p.w_dist : p.w_irr;
+    const int npairs = T * PB;
+    float acc[kPairsPerThread][3];
+#pragma unroll
+    for (int q = 0; q < kPairsPerThread; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0f;
+    for (int r0 = 0; r0 < R; r0 += kRayChunk) {
+        const int kc = min(kRayChunk, R - r0);
+        for (int i = threadIdx.x; i < kc * T; i += blockDim.x) {
+            const int t = i / kc, r = i % kc;
+            Ws[r * T + t] = __ldg(Wg + size_t(t) * R + r0 + r);
+        }
+        for (int i = threadIdx.x; i < PB * kc; i += blockDim.x) {
+            const int pb = i / kc, r = i % kc;
+            const int pr = p0 + pb;
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (pr < p.P) {
+                const size_t o = size_t(pr) * R + r0 + r;
+                if (sizeof(RT) == 16) {
+                    v = __ldg(static_cast<const float4*>(p.rays) + o);
+                } else {
+                    const uint2 raw = __ldg(static_cast<const uint2*>(p.rays) + o);
+                    const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
+                    const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
+                    v = make_float4(__low2float(a), __high2float(a), __low2float(b), __high2float(b));
+                }
+            }
+            if (DEPTH) {
+                float d = mn(u.max_distance, v.w - 0.01f);
+                if (d == -1.0f) d = u.max_distance;
+                v = make_float4(d, d * d, 0.0f, 0.0f);
+            }
+            Rs[pb * kRayChunk + r] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kPairsPerThread; ++q) {
+            const int pair = threadIdx.x + q * blockDim.x;
+            if (pair < npairs) {
+                const int t = pair % T, pb = pair / T;
+                const float4* rr = Rs + pb * kRayChunk;
+                float a0 = acc[q][0], a1 = acc[q][1], a2 = acc[q][2];
+                for (int r = 0; r < kc; ++r) {
+                    const float w = Ws[r * T + t];
+                    const float4 v = rr[r];
+                    a0 = fmaf(v.x, w, a0);
+                    a1 = fmaf(v.y, w, a1);
+                    if (!DEPTH) a2 = fmaf(v.z, w, a2);
+                }
+                acc[q][0] = a0; acc[q][1] = a1; acc[q][2] = a2;
+            }
+        }
+        __syncthreads();
+    }
+    // epilogue: normalise, gamma, hysteresis, store + border mirrors
+    const int XY = u.probe_counts[0] * u.probe_counts[1];
+    const float* nrm = DEPTH ? p.n_dist : p.n_irr;
+    const void* prev = DEPTH ? p.prev_dist : p.prev_irr;
+    void* out = DEPTH ? p.out_dist : p.out_irr;
+    constexpr int NC = DEPTH ? 2 : 4;
+    const float h = u.hysteresis;
+    const float ig = 1.0f / u.ddgi_gamma;
+#pragma unroll
+    for (int q = 0; q < kPairsPerThread; ++q) {
+        const int pair = threadIdx.x + q * blockDim.x;
+        if (pair >= npairs) continue;
+        const int t = pair % T, pb = pair / T;
+        const int pr = p0 + pb;
+        if (pr >= p.P) continue;
+        const int tx = t % n, ty = t / n;
+        const int cx = pr % XY, cy = pr / XY;
+        const float s = __ldg(nrm + t);
+        float v[4];
+        v[0] = acc[q][0] * s;
+        v[1] = acc[q][1] * s;
+        v[2] = acc[q][2] * s;
+        v[3] = 1.0f;
+        if (!DEPTH) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[c] = powf(v[c], ig);
+        }
+        const size_t base = (size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2)) * NC;
+        const int nch = DEPTH ? 2 : 3;
+        for (int c = 0; c < nch; ++c) {
+            float x = v[c];
+            if (!p.first) x = x * (1.0f - h) + AtlasIO<AT>::ld(prev, base + c) * h;
+            v[c] = AtlasIO<AT>::rnd(x);
+        }
+        store_texel<AT, NC>(out, W, n, cx, cy, tx, ty, v);
+    }
+}
+
+template <typename RT, typename AT>
+static cudaError_t launch_blend_t(const BlendParams& p, cudaStream_t st) {
+    const int Ti = p.u.irradiance_probe_side * p.u.irradiance_probe_side;
+    const int Td = p.u.depth_probe_side * p.u.depth_probe_side;
+    const int cap = kBlendThreads * kPairsPerThread;
+    {
+        const int PB = cap / Ti > 0 ? cap / Ti : 1;
+        const size_t sm = sizeof(float) * kRayChunk * Ti + sizeof(float4) * PB * kRayChunk;
+        const unsigned blocks = unsigned((p.P + PB - 1) / PB);
+        if (sm > 48 * 1024) cudaFuncSetAttribute(blend_kernel<0, RT, AT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        blend_kernel<0, RT, AT><<<blocks, kBlendThreads, sm, st>>>(p, PB);
+        note_launch();
+    }
+    {
+        const int PB = cap / Td > 0 ? cap / Td : 1;
+        const size_t sm = sizeof(float) * kRayChunk * Td + sizeof(float4) * PB * kRayChunk;
+        const unsigned blocks = unsigned((p.P + PB - 1) / PB);
+        if (sm > 48 * 1024) cudaFuncSetAttribute(blend_kernel<1, RT, AT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        blend_kernel<1, RT, AT><<<blocks, kBlendThreads, sm, st>>>(p, PB);
+        note_launch();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_blend(const BlendParams& p, cudaStream_t st) {
+    if (p.P <= 0) return cudaSuccess;
+    if (p.u.irradiance_probe_side * p.u.irradiance_probe_side > kBlendThreads * kPairsPerThread ||
+        p.u.depth_probe_side * p.u.depth_probe_side > kBlendThreads * kPairsPerThread)
+        return cudaErrorInvalidValue;
+    if (p.storage == LUXGI_STORAGE_FP16) return launch_blend_t<uint2, __half>(p, st);
+    return launch_blend_t<float4, float>(p, st);
+}
+
+// --------------------------------------------------------------- border
+// Standalone BorderUpdate.glsl: one block per probe cell, one thread per
+// (dst, src) pair; sources are interior texels, destinations border texels.
+template <typename AT, int NC>
+__global__ void border_kernel(void* atlas, int W, int n, int XY, int P) {
+    const int p = blockIdx.x;
+    if (p >= P) return;
+    const int cx = p % XY, cy = p / XY;
+    const int ox = cx * (n + 2) + 1, oy = cy * (n + 2) + 1;
+    for (int i = threadIdx.x; i < 4 * n + 4; i += blockDim.x) {
+        int dx, dy, sx, sy;
+        const int side = i / n, k = i % n + 1;
+        if (i < 4 * n) {
+            if (side == 0) { dx = k; dy = 0; sx = n + 1 - k; sy = 1; }
+            else if (side == 1) { dx = k; dy = n + 1; sx = n + 1 - k; sy = n; }
+            else if (side == 2) { dx = 0; dy = k; sx = 1; sy = n + 1 - k; }
+            else { dx = n + 1; dy = k; sx = n; sy = n + 1 - k; }
+        } else {
+            const int c = i - 4 * n;
+            if (c == 0) { dx = 0; dy = 0; sx = n; sy = n; }
+            else if (c == 1) { dx = n + 1; dy = 0; sx = 1; sy = n; }
+            else if (c == 2) { dx = 0; dy = n + 1; sx = n; sy = 1; }
+            else { dx = n + 1; dy = n + 1; sx = 1; sy = 1; }
+        }
+        const size_t d = (size_t(oy + dy) * W + ox + dx) * NC, s = (size_t(oy + sy) * W + ox + sx) * NC;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) AtlasIO<AT>::st(atlas, d + c, AtlasIO<AT>::ld(atlas, s + c));
+    }
+}
+
+cudaError_t launch_border(const luxgi_ddgi_uniform& u, void* irr, void* dist, int storage, cudaStream_t st) {
+    const int XY = u.probe_counts[0] * u.probe_counts[1];
+    const int P = XY * u.probe_counts[2];
+    if (P <= 0) return cudaSuccess;
+    if (storage == LUXGI_STORAGE_FP16) {
+        border_kernel<__half, 4><<<P, 128, 0, st>>>(irr, u.irradiance_width, u.irradiance_probe_side, XY, P);
+        border_kernel<__half, 2><<<P, 128, 0, st>>>(dist, u.depth_width, u.depth_probe_side, XY, P);
+    } else {
+        border_kernel<float, 4><<<P, 128, 0, st>>>(irr, u.irradiance_width, u.irradiance_probe_side, XY, P);
+        border_kernel<float, 2><<<P, 128, 0, st>>>(dist, u.depth_width, u.depth_probe_side, XY, P);
+    }
+    note_launch(2);
+    return cudaGetLastError();
+}
+
+}  // namespace luxgi

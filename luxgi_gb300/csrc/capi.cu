@@ -1,0 +1,513 @@
+// C ABI of the DDGI probe-update path (include/luxgi_ddgi.h).
+//
+// Replaces the bodies of the three ECS systems of Engine/DDGI/DDGIRenderer.cpp
+// (trace_rays :217-330, probe_update :347-413, border_update :418-464) and
+// end_frame (:335-342); the volume object owns what DDGIPipelineInternal and
+// the DDGIUniform hold there (:85-97).
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include <cuda_runtime.h>
+
+#include "luxgi_internal.h"
+
+namespace luxgi {
+static std::atomic<uint64_t> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add(uint64_t(n), std::memory_order_relaxed); }
+}  // namespace luxgi
+
+using namespace luxgi;
+
+struct luxgi_ddgi_volume {
+    luxgi_ddgi_volume_desc desc;
+    int device = 0;
+    int P = 0, R = 0, Ti = 0, Td = 0;
+    int frames = 0, ping_pong = 0;
+    int debug_rays = 0;
+    bool bound = false;
+    bool tc = false;
+    int tc_ni = 0, tc_nd = 0;      // padded weight rows (multiples of 16)
+    size_t irr_bytes = 0, dist_bytes = 0;
+    void* irr[2] = {nullptr, nullptr};
+    void* dist[2] = {nullptr, nullptr};
+    float4* dirs_trace = nullptr;
+    float4* dirs_blend = nullptr;
+    void* rays = nullptr;
+    int4* info = nullptr;
+    float* w_irr = nullptr;
+    float* w_dist = nullptr;
+    float* n_irr = nullptr;
+    float* n_dist = nullptr;
+    __half* tc_irr = nullptr;
+    __half* tc_dist = nullptr;
+    __half* tcw_irr = nullptr;
+    __half* tcw_dist = nullptr;
+    uint32_t* status = nullptr;
+    luxgi_sdf_desc sdf{};
+    luxgi_surface_desc surf{};
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return LUXGI_OK;
+    if (e == cudaErrorMemoryAllocation) return LUXGI_ENOMEM;
+    if (e == cudaErrorNotSupported) return LUXGI_EUNSUPPORTED;
+    return LUXGI_ECUDA;
+}
+
+int check_uniform(const luxgi_ddgi_uniform& u) {
+    for (int k = 0; k < 3; ++k)
+        if (u.probe_counts[k] <= 0) return LUXGI_EINVAL;
+    if (u.irradiance_probe_side < 1 || u.irradiance_probe_side > 32) return LUXGI_EINVAL;
+    if (u.depth_probe_side < 1 || u.depth_probe_side > 32) return LUXGI_EINVAL;
+    if (u.rays_per_probe < 1 || u.rays_per_probe > 4096) return LUXGI_EINVAL;
+    if (!(u.step[0] > 0.0f) || !(u.step[1] > 0.0f) || !(u.step[2] > 0.0f)) return LUXGI_EINVAL;
+    if (!(u.ddgi_gamma > 0.0f)) return LUXGI_EINVAL;
+    const int64_t P = int64_t(u.probe_counts[0]) * u.probe_counts[1] * u.probe_counts[2];
+    if (P > (int64_t(1) << 26)) return LUXGI_EINVAL;
+    const int64_t XY = int64_t(u.probe_counts[0]) * u.probe_counts[1];
+    if (u.irradiance_width != (u.irradiance_probe_side + 2) * XY + 2) return LUXGI_EINVAL;
+    if (u.irradiance_height != (u.irradiance_probe_side + 2) * u.probe_counts[2] + 2) return LUXGI_EINVAL;
+    if (u.depth_width != (u.depth_probe_side + 2) * XY + 2) return LUXGI_EINVAL;
+    if (u.depth_height != (u.depth_probe_side + 2) * u.probe_counts[2] + 2) return LUXGI_EINVAL;
+    return LUXGI_OK;
+}
+
+template <typename T> cudaError_t dmalloc(T** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(p), bytes);
+}
+
+void free_volume(luxgi_ddgi_volume* v) {
+    void* ptrs[] = {v->irr[0], v->irr[1], v->dist[0], v->dist[1], v->dirs_trace, v->dirs_blend, v->rays, v->info,
+                    v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
+                    v->status};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+SdfView sdf_view(const luxgi_sdf_desc& s) {
+    SdfView v;
+    v.data = s.data;
+    v.sdf = s.sdf;
+    v.mip = s.mip;
+    v.res = s.resolution;
+    v.mres = s.mip_resolution;
+    v.C = int(s.data.cascades_count);
+    v.format = s.format;
+    return v;
+}
+
+SurfaceView surface_view(const luxgi_surface_desc& s, int light_mode) {
+    SurfaceView v;
+    v.data = s.data;
+    v.objects = s.objects;
+    v.tiles = s.tiles;
+    v.chunks = s.chunks;
+    v.culled = s.culled_objects;
+    v.depth = s.depth;
+    if (light_mode == LUXGI_LIGHT_PER_HIT) {
+        v.color0 = reinterpret_cast<const __half*>(s.direct_light);
+        v.color1 = s.albedo;
+    } else {
+        v.color0 = static_cast<const __half*>(s.light_cache);
+        v.color1 = nullptr;
+    }
+    return v;
+}
+
+size_t ray_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 8 : 16; }
+size_t atlas_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 2 : 4; }
+
+int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
+    if (!v->bound) return LUXGI_ENOTBOUND;
+    Rot r;
+    for (int i = 0; i < 9; ++i) r.m[i] = rot[i];
+    const luxgi_ddgi_volume_desc& d = v->desc;
+    cudaError_t e = launch_raygen(r, v->R, d.storage, v->dirs_trace, v->dirs_blend, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    e = launch_weights(d.uniform, v->dirs_blend, v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc ? v->tcw_irr : nullptr,
+                       v->tc ? v->tcw_dist : nullptr, v->tc_ni, v->tc_nd, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    TraceParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.u = d.uniform;
+    p.sdf = sdf_view(v->sdf);
+    p.surf = surface_view(v->surf, d.light_mode);
+    p.prev.irr = v->irr[v->ping_pong];
+    p.prev.dist = v->dist[v->ping_pong];
+    p.prev.storage = d.storage;
+    p.dirs = v->dirs_trace;
+    p.out = v->rays;
+    p.info = v->debug_rays ? v->info : nullptr;
+    p.tc_irr = v->tc ? v->tc_irr : nullptr;
+    p.tc_dist = v->tc ? v->tc_dist : nullptr;
+    for (int k = 0; k < 3; ++k) p.sky[k] = d.sky_radiance[k];
+    p.intensity = d.intensity;
+    p.storage = d.storage;
+    p.light_mode = d.light_mode;
+    p.max_steps = d.max_steps;
+    p.bounce = (d.infinite_bounce && v->frames != 0) ? 1 : 0;
+    p.P = v->P;
+    p.R = v->R;
+    return cuda_status(launch_trace(p, st));
+}
+
+int do_probe_update(luxgi_ddgi_volume* v, cudaStream_t st) {
+    const luxgi_ddgi_volume_desc& d = v->desc;
+    const int rd = v->ping_pong, wr = 1 - v->ping_pong;
+    if (v->tc) {
+        TcBlendParams p;
+        std::memset(&p, 0, sizeof(p));
+        p.u = d.uniform;
+        p.a_irr = v->tc_irr;
+        p.a_dist = v->tc_dist;
+        p.w_irr = v->tcw_irr;
+        p.w_dist = v->tcw_dist;
+        p.n_irr = v->n_irr + v->Ti;
+        p.n_dist = v->n_dist + v->Td;
+        p.prev_irr = v->irr[rd];
+        p.prev_dist = v->dist[rd];
+        p.out_irr = v->irr[wr];
+        p.out_dist = v->dist[wr];
+        p.status = v->status;
+        p.storage = d.storage;
+        p.first = v->frames == 0;
+        p.P = v->P;
+        p.R = v->R;
+        p.Ni = v->tc_ni;
+        p.Nd = v->tc_nd;
+        return cuda_status(launch_tc_blend(p, st));
+    }
+    BlendParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.u = d.uniform;
+    p.dirs = v->dirs_blend;
+    p.rays = v->rays;
+    p.prev_irr = v->irr[rd];
+    p.prev_dist = v->dist[rd];
+    p.out_irr = v->irr[wr];
+    p.out_dist = v->dist[wr];
+    p.w_irr = v->w_irr;
+    p.w_dist = v->w_dist;
+    p.n_irr = v->n_irr;
+    p.n_dist = v->n_dist;
+    p.storage = d.storage;
+    p.first = v->frames == 0;
+    p.P = v->P;
+    p.R = v->R;
+    return cuda_status(launch_blend(p, st));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* luxgi_strerror(int s) {
+    switch (s) {
+        case LUXGI_OK: return "ok";
+        case LUXGI_EINVAL: return "invalid argument";
+        case LUXGI_ENOMEM: return "out of device memory or capacity";
+        case LUXGI_ECUDA: return "CUDA runtime error";
+        case LUXGI_ETIMEOUT: return "bounded device wait timed out";
+        case LUXGI_ENOTBOUND: return "scene not bound";
+        case LUXGI_EUNSUPPORTED: return "unsupported option";
+        default: return "unknown status";
+    }
+}
+
+uint64_t luxgi_launch_count(void) { return g_launches.load(); }
+
+int luxgi_ddgi_derive_uniform(luxgi_ddgi_uniform* u) {
+    if (!u) return LUXGI_EINVAL;
+    for (int k = 0; k < 3; ++k)
+        if (u->probe_counts[k] <= 0) return LUXGI_EINVAL;
+    const int XY = u->probe_counts[0] * u->probe_counts[1], Z = u->probe_counts[2];
+    if (u->irradiance_probe_side <= 0 || u->depth_probe_side <= 0) return LUXGI_EINVAL;
+    // 1-texel border per probe plus a 1-texel pad around the atlas
+    // (DDGIRenderer.cpp:181-185)
+    u->irradiance_width = (u->irradiance_probe_side + 2) * XY + 2;
+    u->irradiance_height = (u->irradiance_probe_side + 2) * Z + 2;
+    u->depth_width = (u->depth_probe_side + 2) * XY + 2;
+    u->depth_height = (u->depth_probe_side + 2) * Z + 2;
+    u->probe_counts[3] = 0;
+    return check_uniform(*u);
+}
+
+int luxgi_ddgi_rotation(const float axis[3], float angle, float out[9]) {
+    if (!axis || !out) return LUXGI_EINVAL;
+    // glm::angleAxis then mat4_cast: the unit quaternion (axis sin(a/2),
+    // cos(a/2)) turned into its rotation matrix, column-major.
+    const float h = angle * 0.5f, s = std::sin(h);
+    const float x = axis[0] * s, y = axis[1] * s, z = axis[2] * s, w = std::cos(h);
+    const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y,
+                wz = w * z;
+    out[0] = 1.0f - 2.0f * (yy + zz); out[1] = 2.0f * (xy + wz);        out[2] = 2.0f * (xz - wy);
+    out[3] = 2.0f * (xy - wz);        out[4] = 1.0f - 2.0f * (xx + zz); out[5] = 2.0f * (yz + wx);
+    out[6] = 2.0f * (xz + wy);        out[7] = 2.0f * (yz - wx);        out[8] = 1.0f - 2.0f * (xx + yy);
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_frame_rotation(uint64_t seed, uint32_t frame, float out[9]) {
+    if (!out) return LUXGI_EINVAL;
+    // splitmix64 -> xoshiro256**, one fresh stream per (seed, frame)
+    uint64_t x = seed ^ (0xD1B54A32D192ED03ull * (uint64_t(frame) + 1ull));
+    uint64_t s[4];
+    for (int i = 0; i < 4; ++i) {
+        uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        s[i] = z ^ (z >> 31);
+    }
+    auto rotl = [](uint64_t v, int k) { return (v << k) | (v >> (64 - k)); };
+    auto next = [&]() {
+        const uint64_t r = rotl(s[1] * 5, 7) * 9;
+        const uint64_t t = s[1] << 17;
+        s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3];
+        s[2] ^= t; s[3] = rotl(s[3], 45);
+        return r;
+    };
+    auto uni = [&](float a, float b) { return a + (b - a) * (float(next() >> 40) * (1.0f / 16777216.0f)); };
+    float ax[3] = {uni(-1.0f, 1.0f), uni(-1.0f, 1.0f), uni(-1.0f, 1.0f)};
+    const float len = std::sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+    if (len > 0.0f) for (float& a : ax) a /= len;
+    else { ax[0] = 0.0f; ax[1] = 0.0f; ax[2] = 1.0f; }
+    const float angle = uni(0.0f, 1.0f) * 3.14159265f * 2.0f;
+    return luxgi_ddgi_rotation(ax, angle, out);
+}
+
+int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** out) {
+    if (!desc || !out) return LUXGI_EINVAL;
+    *out = nullptr;
+    int st = check_uniform(desc->uniform);
+    if (st != LUXGI_OK) return st;
+    if (desc->storage != LUXGI_STORAGE_FP32 && desc->storage != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    if (desc->light_mode != LUXGI_LIGHT_CACHE && desc->light_mode != LUXGI_LIGHT_PER_HIT) return LUXGI_EINVAL;
+    if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
+    if (desc->max_steps < 1) return LUXGI_EINVAL;
+    if (desc->blend == LUXGI_BLEND_TENSOR && !tc_blend_supported(desc->uniform)) return LUXGI_EUNSUPPORTED;
+    luxgi_ddgi_volume* v = new (std::nothrow) luxgi_ddgi_volume();
+    if (!v) return LUXGI_ENOMEM;
+    v->desc = *desc;
+    cudaGetDevice(&v->device);
+    const luxgi_ddgi_uniform& u = desc->uniform;
+    v->P = u.probe_counts[0] * u.probe_counts[1] * u.probe_counts[2];
+    v->R = u.rays_per_probe;
+    v->Ti = u.irradiance_probe_side * u.irradiance_probe_side;
+    v->Td = u.depth_probe_side * u.depth_probe_side;
+    v->tc = desc->blend == LUXGI_BLEND_TENSOR;
+    v->tc_ni = (v->Ti + 15) / 16 * 16;
+    v->tc_nd = (v->Td + 15) / 16 * 16;
+    const size_t ae = atlas_elem_bytes(desc->storage);
+    v->irr_bytes = size_t(u.irradiance_width) * u.irradiance_height * 4 * ae;
+    v->dist_bytes = size_t(u.depth_width) * u.depth_height * 2 * ae;
+    const size_t PR = size_t(v->P) * v->R;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = dmalloc(&v->irr[i], v->irr_bytes);
+        if (e == cudaSuccess) e = dmalloc(&v->dist[i], v->dist_bytes);
+    }
+    if (e == cudaSuccess) e = dmalloc(&v->dirs_trace, sizeof(float4) * v->R);
+    if (e == cudaSuccess) e = dmalloc(&v->dirs_blend, sizeof(float4) * v->R);
+    if (e == cudaSuccess) e = dmalloc(&v->rays, PR * ray_elem_bytes(desc->storage));
+    if (e == cudaSuccess) e = dmalloc(&v->w_irr, sizeof(float) * v->Ti * v->R);
+    if (e == cudaSuccess) e = dmalloc(&v->w_dist, sizeof(float) * v->Td * v->R);
+    if (e == cudaSuccess) e = dmalloc(&v->n_irr, sizeof(float) * 2 * v->Ti);
+    if (e == cudaSuccess) e = dmalloc(&v->n_dist, sizeof(float) * 2 * v->Td);
+    if (e == cudaSuccess) e = dmalloc(&v->status, sizeof(uint32_t) * 4);
+    if (v->tc) {
+        if (e == cudaSuccess) e = dmalloc(&v->tc_irr, sizeof(__half) * PR * 4);
+        if (e == cudaSuccess) e = dmalloc(&v->tc_dist, sizeof(__half) * PR * 4);
+        if (e == cudaSuccess) e = dmalloc(&v->tcw_irr, sizeof(__half) * v->tc_ni * v->R);
+        if (e == cudaSuccess) e = dmalloc(&v->tcw_dist, sizeof(__half) * v->tc_nd * v->R);
+    }
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaMemset(v->irr[i], 0, v->irr_bytes);
+        if (e == cudaSuccess) e = cudaMemset(v->dist[i], 0, v->dist_bytes);
+    }
+    if (e == cudaSuccess) e = cudaMemset(v->status, 0, sizeof(uint32_t) * 4);
+    if (e != cudaSuccess) {
+        free_volume(v);
+        delete v;
+        return cuda_status(e);
+    }
+    *out = v;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_destroy(luxgi_ddgi_volume* v) {
+    if (!v) return LUXGI_EINVAL;
+    free_volume(v);
+    delete v;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf) {
+    if (!v || !sdf || !surf) return LUXGI_EINVAL;
+    const int C = int(sdf->data.cascades_count);
+    if (C < 1 || C > 4 || sdf->resolution < 4 || sdf->mip_resolution < 1 || !sdf->sdf || !sdf->mip) return LUXGI_EINVAL;
+    if (sdf->resolution != int(sdf->data.resolution)) return LUXGI_EINVAL;
+    if (sdf->format != LUXGI_STORAGE_FP32 && sdf->format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    if (!surf->objects || !surf->tiles || !surf->chunks || !surf->culled_objects || !surf->depth) return LUXGI_EINVAL;
+    if (surf->data.resolution == 0) return LUXGI_EINVAL;
+    if (v->desc.light_mode == LUXGI_LIGHT_PER_HIT && (!surf->direct_light || !surf->albedo)) return LUXGI_EINVAL;
+    if (v->desc.light_mode == LUXGI_LIGHT_CACHE && !surf->light_cache) return LUXGI_EINVAL;
+    v->sdf = *sdf;
+    v->surf = *surf;
+    v->bound = true;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_trace(luxgi_ddgi_volume* v, const float rot[9], void* stream) {
+    if (!v || !rot) return LUXGI_EINVAL;
+    return do_trace(v, rot, static_cast<cudaStream_t>(stream));
+}
+
+int luxgi_ddgi_probe_update(luxgi_ddgi_volume* v, void* stream) {
+    if (!v) return LUXGI_EINVAL;
+    return do_probe_update(v, static_cast<cudaStream_t>(stream));
+}
+
+int luxgi_ddgi_border_update(luxgi_ddgi_volume* v, void* stream) {
+    if (!v) return LUXGI_EINVAL;
+    const int wr = 1 - v->ping_pong;
+    return cuda_status(launch_border(v->desc.uniform, v->irr[wr], v->dist[wr], v->desc.storage,
+                                     static_cast<cudaStream_t>(stream)));
+}
+
+int luxgi_ddgi_end_frame(luxgi_ddgi_volume* v) {
+    if (!v) return LUXGI_EINVAL;
+    v->ping_pong = 1 - v->ping_pong;
+    v->frames += 1;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_update(luxgi_ddgi_volume* v, const float rot[9], void* stream) {
+    if (!v || !rot) return LUXGI_EINVAL;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int s = do_trace(v, rot, st);
+    if (s != LUXGI_OK) return s;
+    s = do_probe_update(v, st);
+    if (s != LUXGI_OK) return s;
+    return luxgi_ddgi_end_frame(v);
+}
+
+int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* rots, void* stream) {
+    if ((!vols && n > 0) || n < 0 || (!rots && n > 0)) return LUXGI_EINVAL;
+    for (int i = 0; i < n; ++i) {
+        int s = luxgi_ddgi_update(vols[i], rots + 9 * i, stream);
+        if (s != LUXGI_OK) return s;
+    }
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_get_atlases(const luxgi_ddgi_volume* v, luxgi_ddgi_atlases* out) {
+    if (!v || !out) return LUXGI_EINVAL;
+    const luxgi_ddgi_uniform& u = v->desc.uniform;
+    out->irradiance = v->irr[v->ping_pong];
+    out->distance = v->dist[v->ping_pong];
+    out->prev_irradiance = v->irr[1 - v->ping_pong];
+    out->prev_distance = v->dist[1 - v->ping_pong];
+    out->irradiance_width = u.irradiance_width;
+    out->irradiance_height = u.irradiance_height;
+    out->depth_width = u.depth_width;
+    out->depth_height = u.depth_height;
+    out->storage = v->desc.storage;
+    out->frames = v->frames;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* v, luxgi_ddgi_rays* out) {
+    if (!v || !out) return LUXGI_EINVAL;
+    out->directions = reinterpret_cast<const float*>(v->dirs_trace);
+    out->radiance = v->rays;
+    out->hit_info = v->debug_rays ? reinterpret_cast<const int32_t*>(v->info) : nullptr;
+    out->probes = v->P;
+    out->rays = v->R;
+    out->storage = v->desc.storage;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* v, int enable) {
+    if (!v) return LUXGI_EINVAL;
+    if (enable && !v->info) {
+        cudaError_t e = dmalloc(&v->info, sizeof(int4) * size_t(v->P) * v->R);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    v->debug_rays = enable ? 1 : 0;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_load_atlases(luxgi_ddgi_volume* v, const void* irr, const void* dist, int32_t frames, void* stream) {
+    if (!v || !irr || !dist || frames < 0) return LUXGI_EINVAL;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int i = 0; i < 2; ++i) {
+        cudaError_t e = cudaMemcpyAsync(v->irr[i], irr, v->irr_bytes, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(v->dist[i], dist, v->dist_bytes, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e);
+    v->frames = frames;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_inject_indirect(luxgi_ddgi_volume* v, void* stream) {
+    if (!v) return LUXGI_EINVAL;
+    if (!v->bound) return LUXGI_ENOTBOUND;
+    const luxgi_surface_desc& s = v->surf;
+    if (!s.light_cache || !s.direct_light || !s.gbuffer0 || !s.gbuffer1 || !s.tiles) return LUXGI_EINVAL;
+    AtlasView A;
+    A.irr = v->irr[v->ping_pong];
+    A.dist = v->dist[v->ping_pong];
+    A.storage = v->desc.storage;
+    const int bounce = (v->desc.infinite_bounce && v->frames != 0) ? 1 : 0;
+    return cuda_status(launch_inject(v->desc.uniform, surface_view(s, LUXGI_LIGHT_CACHE), s.gbuffer0, s.gbuffer1,
+                                     reinterpret_cast<const __half*>(s.direct_light),
+                                     static_cast<__half*>(s.light_cache), A, s.num_tiles, v->desc.intensity, bounce,
+                                     static_cast<cudaStream_t>(stream)));
+}
+
+int luxgi_ddgi_sample_irradiance(const luxgi_ddgi_volume* v, const float* pos, const float* nrm, const float* wo,
+                                 float* out, int n, void* stream) {
+    if (!v || n < 0 || (n > 0 && (!pos || !nrm || !wo || !out))) return LUXGI_EINVAL;
+    AtlasView A;
+    A.irr = v->irr[v->ping_pong];
+    A.dist = v->dist[v->ping_pong];
+    A.storage = v->desc.storage;
+    return cuda_status(launch_sample_irradiance(v->desc.uniform, A, pos, nrm, wo, out, n,
+                                                static_cast<cudaStream_t>(stream)));
+}
+
+int luxgi_sdf_build_mip(const luxgi_sdf_desc* sdf, void* mip, void* tmp, void* stream) {
+    if (!sdf || !mip || !tmp || !sdf->sdf) return LUXGI_EINVAL;
+    const int C = int(sdf->data.cascades_count);
+    if (C < 1 || C > 4 || sdf->resolution < 4 || sdf->resolution % 4 != 0 ||
+        sdf->mip_resolution != sdf->resolution / 4)
+        return LUXGI_EINVAL;
+    if (sdf->format != LUXGI_STORAGE_FP32 && sdf->format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    return cuda_status(launch_mip(*sdf, mip, tmp, static_cast<cudaStream_t>(stream)));
+}
+
+int luxgi_surface_cull(const luxgi_surface_desc* s, uint32_t* chunks, uint32_t* culled, uint32_t capacity,
+                       void* stream) {
+    if (!s || !chunks || !culled || !s->objects || capacity < 1) return LUXGI_EINVAL;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint32_t* scratch = nullptr;   // 40^3 counts + status word
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(uint32_t) * (40 * 40 * 40 + 1), st);
+    if (e != cudaSuccess) return cuda_status(e);
+    e = launch_cull(s->data, s->objects, chunks, culled, capacity, scratch, scratch + 40 * 40 * 40, st);
+    uint32_t status = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&status, scratch + 40 * 40 * 40, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    cudaError_t e2 = cudaFreeAsync(scratch, st);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e);
+    return status ? LUXGI_ENOMEM : LUXGI_OK;
+}
+
+}  // extern "C"

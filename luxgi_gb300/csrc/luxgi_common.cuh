@@ -1,0 +1,490 @@
+// Device-side math shared by the DDGI kernels (sm_103a).
+//
+// The SDF march is evaluated in FP32 with a fixed operation order and no
+// fused multiply-add (the translation units that include the march build
+// with -fmad=false), so its hit times equal those of an FP32 CPU evaluation
+// of the same expressions bit for bit.  min/max follow the C++ std::min /
+// std::max convention ((b < a) ? b : a), not fminf/fmaxf.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+
+#include "luxgi_ddgi.h"
+
+namespace luxgi {
+
+constexpr float kWorldSize = 60000.0f;          // GLOBAL_SDF_WORLD_SIZE (SDFCommon.glsl:8)
+constexpr int kChunksRes = 40;                  // GLOBAL_SURFACE_ATLAS_CHUNKS_RESOLUTION
+constexpr float kPi = 3.14159265f;
+
+struct f3 { float x, y, z; };
+
+__host__ __device__ __forceinline__ float mn(float a, float b) { return (b < a) ? b : a; }
+__host__ __device__ __forceinline__ float mx(float a, float b) { return (a < b) ? b : a; }
+__host__ __device__ __forceinline__ int imn(int a, int b) { return (b < a) ? b : a; }
+__host__ __device__ __forceinline__ int imx(int a, int b) { return (a < b) ? b : a; }
+__host__ __device__ __forceinline__ float clampf(float v, float lo, float hi) { return mn(mx(v, lo), hi); }
+__device__ __forceinline__ f3 make3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 add3(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 mul3(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 mulv3(f3 a, f3 b) { return f3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float len3(f3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ f3 norm3(f3 a) { float inv = 1.0f / sqrtf(dot3(a, a)); return mul3(a, inv); }
+
+// sin/cos for the Fibonacci azimuth: Cody-Waite reduction by pi/2 and Taylor
+// polynomials of degree 9 (sin) and 8 (cos) on [-pi/4, pi/4].
+__device__ __forceinline__ void fib_sincos(float x, float* s, float* c) {
+    const float k = floorf(x * 0.63661977f + 0.5f);
+    const float r = (x - k * 1.57079637f) - k * -4.37113883e-8f;
+    const float r2 = r * r;
+    const float sp = r + r * r2 * (-0.166666672f + r2 * (0.00833333377f + r2 * (-0.000198412701f + r2 * 2.75573188e-6f)));
+    const float cp = 1.0f + r2 * (-0.5f + r2 * (0.0416666679f + r2 * (-0.00138888892f + r2 * 2.48015876e-5f)));
+    const int q = int(k) & 3;
+    if (q == 0) { *s = sp; *c = cp; }
+    else if (q == 1) { *s = cp; *c = -sp; }
+    else if (q == 2) { *s = -sp; *c = -cp; }
+    else { *s = -cp; *c = sp; }
+}
+
+// sphericalFibonacci (DDGICommon.glsl:42-52) rotated by mat3(rot), normalised.
+__device__ __forceinline__ f3 ray_direction(const float* rot, int r, int nrays) {
+    const float PHI = sqrtf(5.0f) * 0.5f + 0.5f;
+    const float i = float(r);
+    const float t = i * (PHI - 1.0f);
+    const float mf = t - floorf(t);
+    const float phi = (2.0f * kPi) * mf;
+    const float cos_t = 1.0f - (2.0f * i + 1.0f) * (1.0f / float(nrays));
+    const float sin_t = sqrtf(clampf(1.0f - cos_t * cos_t, 0.0f, 1.0f));
+    float sp, cp;
+    fib_sincos(phi, &sp, &cp);
+    const f3 f{cp * sin_t, sp * sin_t, cos_t};
+    const f3 m{rot[0] * f.x + rot[3] * f.y + rot[6] * f.z,
+               rot[1] * f.x + rot[4] * f.y + rot[7] * f.z,
+               rot[2] * f.x + rot[5] * f.y + rot[8] * f.z};
+    return norm3(m);
+}
+
+// probeLocation (DDGICommon.glsl:101-114)
+__device__ __forceinline__ f3 probe_location(const luxgi_ddgi_uniform& u, int index) {
+    const int X = u.probe_counts[0], Y = u.probe_counts[1];
+    const int gx = index % X, gy = (index % (X * Y)) / X, gz = index / (X * Y);
+    return f3{u.step[0] * float(gx) + u.start_position[0], u.step[1] * float(gy) + u.start_position[1],
+              u.step[2] * float(gz) + u.start_position[2]};
+}
+
+__device__ __forceinline__ float load_val(const float* p, size_t i) { return __ldg(p + i); }
+__device__ __forceinline__ float load_val(const __half* p, size_t i) { return __half2float(__ldg(p + i)); }
+
+// GL LINEAR + CLAMP_TO_EDGE trilinear sample of a W x H x D volume.
+template <typename T>
+__device__ __forceinline__ float sample3d(const T* __restrict__ v, int W, int H, int D, float u, float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    const float a = x - fx, b = y - fy, c = z - fz;
+    int x0 = int(fx), y0 = int(fy), z0 = int(fz);
+    const int x1 = imn(imx(x0 + 1, 0), W - 1), y1 = imn(imx(y0 + 1, 0), H - 1), z1 = imn(imx(z0 + 1, 0), D - 1);
+    x0 = imn(imx(x0, 0), W - 1); y0 = imn(imx(y0, 0), H - 1); z0 = imn(imx(z0, 0), D - 1);
+    const size_t WH = size_t(W) * size_t(H);
+    const size_t r00 = size_t(y0) * W + z0 * WH, r10 = size_t(y1) * W + z0 * WH;
+    const size_t r01 = size_t(y0) * W + z1 * WH, r11 = size_t(y1) * W + z1 * WH;
+    const float t000 = load_val(v, r00 + x0), t100 = load_val(v, r00 + x1);
+    const float t010 = load_val(v, r10 + x0), t110 = load_val(v, r10 + x1);
+    const float t001 = load_val(v, r01 + x0), t101 = load_val(v, r01 + x1);
+    const float t011 = load_val(v, r11 + x0), t111 = load_val(v, r11 + x1);
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float c00 = t000 * ia + t100 * a, c10 = t010 * ia + t110 * a;
+    const float c01 = t001 * ia + t101 * a, c11 = t011 * ia + t111 * a;
+    const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
+struct SdfView {
+    luxgi_sdf_data data;
+    const void* sdf;
+    const void* mip;
+    int res, mres, C;
+    int format;   // luxgi_storage of the sdf/mip texels
+};
+
+struct MarchHit {
+    f3 normal;
+    float time;
+    int cascade;
+    int steps;
+    int fine;      // full-resolution SDF samples taken (for byte accounting)
+    float sdf;
+};
+
+// tracyGlobalSDF (SDFCommon.glsl:98-194) with stepScale 1, start bias 0,
+// hit normal requested (GISDFRays.comp:79-87).
+template <typename T>
+__device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps) {
+    const T* __restrict__ tex = static_cast<const T*>(s.sdf);
+    const T* __restrict__ mip = static_cast<const T*>(s.mip);
+    const int C = s.C;
+    const int TW = s.res * C, MW = s.mres * C;
+    MarchHit hit;
+    hit.normal = f3{0.0f, 0.0f, 0.0f};
+    hit.time = -1.0f;
+    hit.cascade = 0;
+    hit.steps = 0;
+    hit.fine = 0;
+    hit.sdf = 0.0f;
+    const float tmax = mn(trace_max, s.data.cascade_pos_distance[C - 1][3] * 2.0f);
+    const float chunk = 32.0f / s.data.resolution;
+    const float margin = 4.0f / s.data.resolution;
+    float next_start = 0.0f;
+    const f3 end = add3(origin, mul3(dir, tmax));
+    for (int cascade = 0; cascade < C && hit.time < 0.0f; ++cascade) {
+        const float cx = s.data.cascade_pos_distance[cascade][0], cy = s.data.cascade_pos_distance[cascade][1],
+                    cz = s.data.cascade_pos_distance[cascade][2], cw = s.data.cascade_pos_distance[cascade][3];
+        const float voxel = s.data.cascade_voxel_size[cascade];
+        const float voxel_half = voxel * 0.5f;
+        const f3 wpos = add3(origin, mul3(dir, voxel * 0.0f));
+        // lineHitAABB (SDFCommon.glsl:84-95)
+        const f3 d = sub3(end, wpos);
+        const f3 inv{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+        const f3 en{((cx - cw) - wpos.x) * inv.x, ((cy - cw) - wpos.y) * inv.y, ((cz - cw) - wpos.z) * inv.z};
+        const f3 ex{((cx + cw) - wpos.x) * inv.x, ((cy + cw) - wpos.y) * inv.y, ((cz + cw) - wpos.z) * inv.z};
+        const float i0 = mx(mn(en.x, ex.x), mx(mn(en.y, ex.y), mn(en.z, ex.z)));
+        const float i1 = mn(mx(en.x, ex.x), mn(mx(en.y, ex.y), mx(en.z, ex.z)));
+        float is_x = clampf(i0, 0.0f, 1.0f) * tmax;
+        const float is_y = clampf(i1, 0.0f, 1.0f) * tmax;
+        is_x = mx(is_x, next_start);
+        float t = is_x;
+        if (is_x >= is_y) t = is_y;
+        else next_start = is_y;
+        const float md = cw * 2.0f;
+        const float invC = float(C);
+        int step = 0;
+        for (; step < max_steps && t < is_y; ++step) {
+            const f3 sp = add3(wpos, mul3(dir, t));
+            // getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
+            const float ux = clampf((sp.x - cx) / md + 0.5f, 0.0f, 1.0f);
+            const float uy = clampf((sp.y - cy) / md + 0.5f, 0.0f, 1.0f);
+            const float uz = clampf((sp.z - cz) / md + 0.5f, 0.0f, 1.0f);
+            const float tu = (float(cascade) + ux) / invC;
+            float sd = sample3d(mip, MW, s.mres, s.mres, tu, uy, uz);
+            if (sd < chunk) {
+                const float sdt = sample3d(tex, TW, s.res, s.res, tu, uy, uz);
+                ++hit.fine;
+                if (sdt < margin * 2.0f) sd = sdt;
+            } else {
+                sd = chunk;
+            }
+            sd = sd * md;
+            const float thick = voxel_half * clampf(t / voxel, 0.0f, 1.0f);
+            if (sd < thick) {
+                hit.time = mx(t + sd - thick, 0.0f);
+                hit.cascade = cascade;
+                hit.sdf = sd;
+                const float off = 1.0f / s.data.resolution;
+                const float xp = sample3d(tex, TW, s.res, s.res, tu + off, uy, uz);
+                const float xn = sample3d(tex, TW, s.res, s.res, tu - off, uy, uz);
+                const float yp = sample3d(tex, TW, s.res, s.res, tu, uy + off, uz);
+                const float yn = sample3d(tex, TW, s.res, s.res, tu, uy - off, uz);
+                const float zp = sample3d(tex, TW, s.res, s.res, tu, uy, uz + off);
+                const float zn = sample3d(tex, TW, s.res, s.res, tu, uy, uz - off);
+                hit.normal = norm3(f3{xp - xn, yp - yn, zp - zn});
+                break;
+            }
+            t = t + mx(sd * 1.0f, voxel);
+        }
+        hit.steps += step;
+    }
+    return hit;
+}
+
+// ------------------------------------------------ surface atlas sampling
+struct SurfaceView {
+    luxgi_surface_data data;
+    const luxgi_surface_object* objects;
+    const luxgi_surface_tile* tiles;
+    const uint32_t* chunks;
+    const uint32_t* culled;
+    const __half* color0;     // light cache (mode A) or direct light (mode B), RGBA16F
+    const uint8_t* color1;    // albedo RGBA8 (mode B)
+    const float* depth;
+};
+
+__device__ __forceinline__ f3 mat4_mul_pt(const float* m, f3 v, float w) {
+    return f3{m[0] * v.x + m[4] * v.y + m[8] * v.z + m[12] * w,
+              m[1] * v.x + m[5] * v.y + m[9] * v.z + m[13] * w,
+              m[2] * v.x + m[6] * v.y + m[10] * v.z + m[14] * w};
+}
+
+// 4x4 inverse by adjugate (same cofactor sequence as the CPU restatement).
+__device__ __forceinline__ void mat4_inverse(const float* A, float* out) {
+    float a[4][4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r][c] = A[c * 4 + r];
+    const float s0 = a[0][0] * a[1][1] - a[1][0] * a[0][1];
+    const float s1 = a[0][0] * a[1][2] - a[1][0] * a[0][2];
+    const float s2 = a[0][0] * a[1][3] - a[1][0] * a[0][3];
+    const float s3 = a[0][1] * a[1][2] - a[1][1] * a[0][2];
+    const float s4 = a[0][1] * a[1][3] - a[1][1] * a[0][3];
+    const float s5 = a[0][2] * a[1][3] - a[1][2] * a[0][3];
+    const float c5 = a[2][2] * a[3][3] - a[3][2] * a[2][3];
+    const float c4 = a[2][1] * a[3][3] - a[3][1] * a[2][3];
+    const float c3 = a[2][1] * a[3][2] - a[3][1] * a[2][2];
+    const float c2 = a[2][0] * a[3][3] - a[3][0] * a[2][3];
+    const float c1 = a[2][0] * a[3][2] - a[3][0] * a[2][2];
+    const float c0 = a[2][0] * a[3][1] - a[3][0] * a[2][1];
+    const float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    const float id = 1.0f / det;
+    float b[4][4];
+    b[0][0] = ( a[1][1] * c5 - a[1][2] * c4 + a[1][3] * c3) * id;
+    b[0][1] = (-a[0][1] * c5 + a[0][2] * c4 - a[0][3] * c3) * id;
+    b[0][2] = ( a[3][1] * s5 - a[3][2] * s4 + a[3][3] * s3) * id;
+    b[0][3] = (-a[2][1] * s5 + a[2][2] * s4 - a[2][3] * s3) * id;
+    b[1][0] = (-a[1][0] * c5 + a[1][2] * c2 - a[1][3] * c1) * id;
+    b[1][1] = ( a[0][0] * c5 - a[0][2] * c2 + a[0][3] * c1) * id;
+    b[1][2] = (-a[3][0] * s5 + a[3][2] * s2 - a[3][3] * s1) * id;
+    b[1][3] = ( a[2][0] * s5 - a[2][2] * s2 + a[2][3] * s1) * id;
+    b[2][0] = ( a[1][0] * c4 - a[1][1] * c2 + a[1][3] * c0) * id;
+    b[2][1] = (-a[0][0] * c4 + a[0][1] * c2 - a[0][3] * c0) * id;
+    b[2][2] = ( a[3][0] * s4 - a[3][1] * s2 + a[3][3] * s0) * id;
+    b[2][3] = (-a[2][0] * s4 + a[2][1] * s2 - a[2][3] * s0) * id;
+    b[3][0] = (-a[1][0] * c3 + a[1][1] * c1 - a[1][2] * c0) * id;
+    b[3][1] = ( a[0][0] * c3 - a[0][1] * c1 + a[0][2] * c0) * id;
+    b[3][2] = (-a[3][0] * s3 + a[3][1] * s1 - a[3][2] * s0) * id;
+    b[3][3] = ( a[2][0] * s3 - a[2][1] * s1 + a[2][2] * s0) * id;
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) out[c * 4 + r] = b[r][c];
+}
+
+// textureGather texel indices (clamp to edge): (i0,j1),(i1,j1),(i1,j0),(i0,j0)
+struct Gather4 { int i0, i1, j0, j1; };
+__device__ __forceinline__ Gather4 gather_idx(float u, float v, int W, int H) {
+    const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
+    int i0 = int(floorf(x)), j0 = int(floorf(y));
+    Gather4 g;
+    g.i1 = imn(imx(i0 + 1, 0), W - 1);
+    g.j1 = imn(imx(j0 + 1, 0), H - 1);
+    g.i0 = imn(imx(i0, 0), W - 1);
+    g.j0 = imn(imx(j0, 0), H - 1);
+    return g;
+}
+
+// sampleGlobalSurfaceAtlasTile, both overloads (AtlasCommon.glsl:58-112);
+// accumulates colour*weight of one or two atlases.
+template <bool TWO>
+__device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_surface_tile* __restrict__ tl, f3 local,
+                                            f3 nrm_local, float thr, f3& acc0, f3& acc1, float& accw) {
+    float T[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) T[k] = __ldg(&tl->transform[k]);
+    const f3 n = norm3(mat4_mul_pt(T, nrm_local, 1.0f));
+    float nw = clampf(0.0f * n.x + 0.0f * n.y + 1.0f * n.z, 0.0f, 1.0f);
+    nw = (nw - 0.05f) / (1.0f - 0.05f);
+    if (nw <= 0.0f) return;
+    const f3 tp = mat4_mul_pt(T, local, 1.0f);
+    const float bx = __ldg(&tl->object_bounds[0]), by = __ldg(&tl->object_bounds[1]), bz = __ldg(&tl->object_bounds[2]);
+    const float tdepth = tp.z / bz;
+    const float tu = clampf(tp.x / bx + 0.5f, 0.0f, 1.0f), tv = clampf(tp.y / by + 0.5f, 0.0f, 1.0f);
+    const float au = tu * __ldg(&tl->extends[2]) + __ldg(&tl->extends[0]);
+    const float av = tv * __ldg(&tl->extends[3]) + __ldg(&tl->extends[1]);
+    const float res = float(S.data.resolution);
+    float bu = au * res + 0.5f; bu = bu - floorf(bu);
+    float bv = av * res + 0.5f; bv = bv - floorf(bv);
+    const float bw0 = (1.0f - bu) * bv, bw1 = bu * bv, bw2 = bu * (1.0f - bv), bw3 = (1.0f - bu) * (1.0f - bv);
+    const int R = int(S.data.resolution);
+    const Gather4 g = gather_idx(au, av, R, R);
+    const size_t o0 = size_t(g.j1) * R + g.i0, o1 = size_t(g.j1) * R + g.i1;
+    const size_t o2 = size_t(g.j0) * R + g.i1, o3 = size_t(g.j0) * R + g.i0;
+    const float tz[4] = {__ldg(S.depth + o0), __ldg(S.depth + o1), __ldg(S.depth + o2), __ldg(S.depth + o3)};
+    const float dthr = 2.0f * thr / bz;
+    float dv[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        dv[i] = 1.0f - clampf((fabsf(tdepth - tz[i]) - dthr) / (0.5f * dthr), 0.0f, 1.0f);
+        if (tz[i] >= 1.0f) dv[i] = 0.0f;
+    }
+    float sw = dv[0] * bw0 + dv[1] * bw1 + dv[2] * bw2 + dv[3] * bw3;
+    sw = sw * nw;
+    if (sw <= 0.0f) return;
+    const float w0 = bw0 * dv[0], w1 = bw1 * dv[1], w2 = bw2 * dv[2], w3 = bw3 * dv[3];
+    const size_t offs[4] = {o0, o1, o2, o3};
+    float ch[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint2 raw = __ldg(reinterpret_cast<const uint2*>(S.color0) + offs[i]);
+        const __half2 rg = *reinterpret_cast<const __half2*>(&raw.x);
+        const __half2 ba = *reinterpret_cast<const __half2*>(&raw.y);
+        ch[i][0] = __low2float(rg); ch[i][1] = __high2float(rg); ch[i][2] = __low2float(ba);
+    }
+    const f3 c0{ch[0][0] * w0 + ch[1][0] * w1 + ch[2][0] * w2 + ch[3][0] * w3,
+                ch[0][1] * w0 + ch[1][1] * w1 + ch[2][1] * w2 + ch[3][1] * w3,
+                ch[0][2] * w0 + ch[1][2] * w1 + ch[2][2] * w2 + ch[3][2] * w3};
+    acc0 = add3(acc0, mul3(c0, sw));
+    if (TWO) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uchar4 a = __ldg(reinterpret_cast<const uchar4*>(S.color1) + offs[i]);
+            ch[i][0] = float(a.x) / 255.0f; ch[i][1] = float(a.y) / 255.0f; ch[i][2] = float(a.z) / 255.0f;
+        }
+        const f3 c1{ch[0][0] * w0 + ch[1][0] * w1 + ch[2][0] * w2 + ch[3][0] * w3,
+                    ch[0][1] * w0 + ch[1][1] * w1 + ch[2][1] * w2 + ch[3][1] * w3,
+                    ch[0][2] * w0 + ch[1][2] * w1 + ch[2][2] * w2 + ch[3][2] * w3};
+        acc1 = add3(acc1, mul3(c1, sw));
+    }
+    accw = accw + sw;
+}
+
+// sampleGlobalSurfaceAtlas (AtlasCommon.glsl:115-157), debug off.
+template <bool TWO>
+__device__ __forceinline__ float sample_surface(const SurfaceView& S, f3 pos, f3 wn, float thr, f3& out0, f3& out1) {
+    f3 acc0{0.0f, 0.0f, 0.0f}, acc1{0.0f, 0.0f, 0.0f};
+    float accw = 0.0f;
+    out0 = acc0;
+    out1 = acc1;
+    const float cs = S.data.chunk_size;
+    const int cx = imn(imx(int(floorf(pos.x / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const int cy = imn(imx(int(floorf(pos.y / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const int cz = imn(imx(int(floorf(pos.z / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const uint32_t addr = uint32_t(cz * kChunksRes * kChunksRes + cy * kChunksRes + cx);
+    uint32_t start = __ldg(S.chunks + addr);
+    if (start == 0) return 0.0f;
+    const uint32_t count = __ldg(S.culled + start);
+    if (count > S.data.objects_count) return 0.0f;
+    ++start;
+    for (uint32_t oi = 0; oi < count; ++oi) {
+        const uint32_t oaddr = __ldg(S.culled + start++);
+        const luxgi_surface_object* ob = S.objects + oaddr;
+        const float4 bnd = __ldg(reinterpret_cast<const float4*>(ob->object_bounds));
+        if (len3(sub3(f3{bnd.x, bnd.y, bnd.z}, pos)) > bnd.w) continue;
+        float M[16], w2l[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) M[k] = __ldg(&ob->transform[k]);
+        mat4_inverse(M, w2l);
+        const f3 lp = mat4_mul_pt(w2l, pos, 1.0f);
+        const float4 e = __ldg(reinterpret_cast<const float4*>(ob->extends));
+        if (fabsf(lp.x) > e.x + thr || fabsf(lp.y) > e.y + thr || fabsf(lp.z) > e.z + thr) continue;
+        const f3 ln = norm3(f3{w2l[0] * wn.x + w2l[4] * wn.y + w2l[8] * wn.z,
+                               w2l[1] * wn.x + w2l[5] * wn.y + w2l[9] * wn.z,
+                               w2l[2] * wn.x + w2l[6] * wn.y + w2l[10] * wn.z});
+        for (int i = 0; i < 6; ++i) {
+            const uint32_t to = __ldg(&ob->tile_offset[i]);
+            if (to != 0) sample_tile<TWO>(S, S.tiles + to, lp, ln, thr, acc0, acc1, accw);
+        }
+    }
+    const float den = mx(accw, 0.0001f);
+    out0 = f3{acc0.x / den, acc0.y / den, acc0.z / den};
+    out1 = f3{acc1.x / den, acc1.y / den, acc1.z / den};
+    return accw;
+}
+
+// ------------------------------------------------ probe atlas sampling
+struct AtlasView {
+    const void* irr;
+    const void* dist;
+    int storage;   // luxgi_storage
+};
+
+__device__ __forceinline__ float atlas_load(const void* p, int storage, size_t i) {
+    if (storage == LUXGI_STORAGE_FP16) return __half2float(__ldg(static_cast<const __half*>(p) + i));
+    return __ldg(static_cast<const float*>(p) + i);
+}
+
+// textureLod bilinear with REPEAT of channel ch (nc channels per texel).
+__device__ __forceinline__ float bilinear_repeat(const void* p, int storage, int W, int H, int nc, float u, float v, int ch) {
+    const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    int i0 = int(fx) % W; if (i0 < 0) i0 += W;
+    int i1 = (int(fx) + 1) % W; if (i1 < 0) i1 += W;
+    int j0 = int(fy) % H; if (j0 < 0) j0 += H;
+    int j1 = (int(fy) + 1) % H; if (j1 < 0) j1 += H;
+    const float t00 = atlas_load(p, storage, (size_t(j0) * W + i0) * nc + ch);
+    const float t10 = atlas_load(p, storage, (size_t(j0) * W + i1) * nc + ch);
+    const float t01 = atlas_load(p, storage, (size_t(j1) * W + i0) * nc + ch);
+    const float t11 = atlas_load(p, storage, (size_t(j1) * W + i1) * nc + ch);
+    const float r0 = t00 * (1.0f - a) + t10 * a, r1 = t01 * (1.0f - a) + t11 * a;
+    return r0 * (1.0f - b) + r1 * b;
+}
+
+__device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
+
+// textureCoordFromDirection (DDGICommon.glsl:141-158)
+__device__ __forceinline__ void tex_coord_from_dir(f3 dir, int probe, int W, int H, int side, float& u, float& v) {
+    const f3 d = norm3(dir);
+    const float l1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+    const float inv = 1.0f / l1;
+    float ox = d.x * inv, oy = d.y * inv;
+    if (d.z < 0.0f) {
+        const float nx = (1.0f - fabsf(oy)) * sign_nz(ox);
+        const float ny = (1.0f - fabsf(ox)) * sign_nz(oy);
+        ox = nx; oy = ny;
+    }
+    const float zx = (ox + 1.0f) * 0.5f, zy = (oy + 1.0f) * 0.5f;
+    const float pwb = float(side) + 2.0f;
+    const float nx = (zx * float(side)) / float(W), ny = (zy * float(side)) / float(H);
+    const int ppr = (W - 2) / int(pwb);
+    const float tlx = float(probe % ppr) * pwb + 2.0f, tly = float(probe / ppr) * pwb + 2.0f;
+    u = tlx / float(W) + nx;
+    v = tly / float(H) + ny;
+}
+
+// sampleIrradiance (DDGICommon.glsl:163-233)
+__device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, f3 P, f3 N, f3 Wo) {
+    const f3 start{u.start_position[0], u.start_position[1], u.start_position[2]};
+    const f3 stp{u.step[0], u.step[1], u.step[2]};
+    const int cnt[3] = {u.probe_counts[0], u.probe_counts[1], u.probe_counts[2]};
+    int base[3] = {int((P.x - start.x) / stp.x), int((P.y - start.y) / stp.y), int((P.z - start.z) / stp.z)};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) base[k] = imn(imx(base[k], 0), cnt[k] - 1);
+    const f3 bpos{stp.x * float(base[0]) + start.x, stp.y * float(base[1]) + start.y, stp.z * float(base[2]) + start.z};
+    const f3 alpha{clampf((P.x - bpos.x) / stp.x, 0.0f, 1.0f), clampf((P.y - bpos.y) / stp.y, 0.0f, 1.0f),
+                   clampf((P.z - bpos.z) / stp.z, 0.0f, 1.0f)};
+    f3 sum{0.0f, 0.0f, 0.0f};
+    float sumw = 0.0f;
+    const float ge = u.ddgi_gamma * 0.5f;
+    for (int i = 0; i < 8; ++i) {
+        const int off[3] = {i & 1, (i >> 1) & 1, (i >> 2) & 1};
+        int g[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) g[k] = imn(imx(base[k] + off[k], 0), cnt[k] - 1);
+        const f3 ppos{stp.x * float(g[0]) + start.x, stp.y * float(g[1]) + start.y, stp.z * float(g[2]) + start.z};
+        const f3 tri{off[0] ? alpha.x : 1.0f - alpha.x, off[1] ? alpha.y : 1.0f - alpha.y, off[2] ? alpha.z : 1.0f - alpha.z};
+        float weight = 1.0f;
+        const f3 dtp = norm3(sub3(ppos, P));
+        const float bf = mx(0.0001f, (dot3(dtp, N) + 1.0f) * 0.5f);
+        weight = weight * (bf * bf + 0.2f);
+        const int pidx = g[0] + g[1] * cnt[0] + g[2] * cnt[0] * cnt[1];
+        const f3 vb = mul3(add3(N, mul3(Wo, 3.0f)), u.normal_bias);
+        const f3 ptp = add3(sub3(P, ppos), vb);
+        const f3 dir = norm3(mul3(ptp, -1.0f));
+        float tu, tv;
+        tex_coord_from_dir(mul3(dir, -1.0f), pidx, u.depth_width, u.depth_height, u.depth_probe_side, tu, tv);
+        const float dist = len3(ptp);
+        const float mean = bilinear_repeat(A.dist, A.storage, u.depth_width, u.depth_height, 2, tu, tv, 0);
+        const float mean2 = bilinear_repeat(A.dist, A.storage, u.depth_width, u.depth_height, 2, tu, tv, 1);
+        const float variance = fabsf(mean * mean - mean2);
+        const float dm = mx(dist - mean, 0.0f);
+        float cheb = variance / (variance + dm * dm);
+        cheb = mx(cheb * cheb * cheb, 0.0f);
+        weight = weight * ((dist <= mean) ? 1.0f : cheb);
+        weight = mx(0.000001f, weight);
+        tex_coord_from_dir(N, pidx, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, tu, tv);
+        const f3 pir{powf(bilinear_repeat(A.irr, A.storage, u.irradiance_width, u.irradiance_height, 4, tu, tv, 0), ge),
+                     powf(bilinear_repeat(A.irr, A.storage, u.irradiance_width, u.irradiance_height, 4, tu, tv, 1), ge),
+                     powf(bilinear_repeat(A.irr, A.storage, u.irradiance_width, u.irradiance_height, 4, tu, tv, 2), ge)};
+        const float crush = 0.2f;
+        if (weight < crush) weight = weight * (weight * weight * (1.0f / (crush * crush)));
+        weight = weight * (tri.x * tri.y * tri.z);
+        sum = add3(sum, mul3(pir, weight));
+        sumw = sumw + weight;
+    }
+    f3 net{sum.x / sumw, sum.y / sumw, sum.z / sumw};
+    net = mulv3(net, net);
+    return mul3(net, 2.0f * kPi);
+}
+
+}  // namespace luxgi

@@ -1,0 +1,264 @@
+"""ORACLE -- test infrastructure only; never part of the product path.
+
+ctypes wrapper of oracle/oracle.cpp, the CPU restatement (FP32 and FP64,
+OpenMP over probes) of LuxGI's non-raytracing DDGI probe update.  Only the
+tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg import it.
+
+Parity pins: the reference ships no tests, fixtures or golden data for
+this path.  The oracle is pinned by analytic known-answer tests (empty
+scene / constant sky, hysteresis closed form, octahedral round trips,
+Fibonacci determinism, probe inside a sphere) and by the border offset
+tables read out of the reference source (tests/golden/border_tables.json).
+The trace, surface-atlas and sampleIrradiance restatements are pinned only
+by those analytic cases: their parity with the reference is otherwise
+unpinned.
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from ctypes import POINTER, c_float, c_int, c_int32, c_uint16, c_uint32, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "oracle.cpp"
+LIB = HERE / "liboracle.so"
+INCLUDE = HERE.parent / "include"
+
+
+def build() -> Path:
+    deps = [SRC] + sorted(INCLUDE.glob("*.h"))
+    if not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", str(SRC), "-o", str(LIB)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB))
+        vp = c_void_p
+        sig = {
+            "oracle_num_threads": (c_int, []),
+            "oracle_set_threads": (None, [c_int]),
+            "oracle_ray_dirs": (c_int, [vp, c_int, c_int, c_int, vp]),
+            "oracle_rotation": (c_int, [vp, c_float, vp]),
+            "oracle_trace": (c_int, [vp, vp, vp, vp, vp, c_int, vp, c_int, c_int, c_int, vp, vp]),
+            "oracle_blend": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int, c_int, c_int, c_int, c_int]),
+            "oracle_border": (c_int, [vp, vp, vp]),
+            "oracle_border_pairs": (c_int, [c_int, vp]),
+            "oracle_build_mip": (c_int, [vp, vp, vp]),
+            "oracle_cull": (c_int, [vp, vp, vp, c_uint32]),
+            "oracle_inject": (c_int, [vp, vp, vp, vp, c_int, c_int, vp]),
+            "oracle_sample_irradiance": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int, c_int]),
+            "oracle_texel_dirs": (c_int, [c_int, c_int, vp]),
+            "oracle_oct_encode": (c_int, [vp, c_int, vp]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def num_threads() -> int:
+    return lib().oracle_num_threads()
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(n)
+
+
+def ray_dirs(rot, nrays: int, precision: int = 0, fp16_round: bool = False) -> np.ndarray:
+    rot = np.ascontiguousarray(rot, dtype=np.float32)
+    out = np.zeros((nrays, 4), dtype=np.float32)
+    lib().oracle_ray_dirs(_p(rot), nrays, precision, 1 if fp16_round else 0, _p(out))
+    return out
+
+
+def rotation(axis, angle: float) -> np.ndarray:
+    a = np.ascontiguousarray(axis, dtype=np.float32)
+    out = np.zeros(9, dtype=np.float32)
+    lib().oracle_rotation(_p(a), angle, _p(out))
+    return out
+
+
+def texel_dirs(n: int, precision: int = 0) -> np.ndarray:
+    out = np.zeros((n * n, 3), dtype=np.float32)
+    lib().oracle_texel_dirs(n, precision, _p(out))
+    return out
+
+
+def oct_encode(dirs: np.ndarray) -> np.ndarray:
+    d = np.ascontiguousarray(dirs, dtype=np.float32)
+    out = np.zeros((d.shape[0], 2), dtype=np.float32)
+    lib().oracle_oct_encode(_p(d), d.shape[0], _p(out))
+    return out
+
+
+def border_pairs(n: int) -> np.ndarray:
+    out = np.zeros((4 * n + 4, 4), dtype=np.int32)
+    k = lib().oracle_border_pairs(n, _p(out))
+    return out[:k]
+
+
+class HostInputs:
+    """Host-side descriptors of a scene for the oracle (numpy-backed)."""
+
+    def __init__(self, host, light_mode: int, mip: np.ndarray | None = None, chunks: np.ndarray | None = None,
+                 culled: np.ndarray | None = None, light_cache: np.ndarray | None = None):
+        from luxgi_gb300 import _native as N
+
+        self.host = host
+        self.sdf = host.sdf
+        self.sdf_desc = N.SdfDesc()
+        self.sdf_desc.data = host.sdf_data
+        self.sdf_desc.format = host.sdf_format
+        self.sdf_desc.resolution = host.res
+        self.sdf_desc.mip_resolution = host.mres
+        self.sdf_desc.sdf = self.sdf.ctypes.data
+        if mip is None:
+            mipf = build_mip(self.sdf_desc, host.sdf_float())
+            mip = mipf.astype(np.float16).view(np.uint16) if host.sdf_format == N.STORAGE_FP16 else mipf
+        self.mip = np.ascontiguousarray(mip)
+        self.sdf_desc.mip = self.mip.ctypes.data
+        self.surface_desc = N.SurfaceDesc()
+        sd = N.SurfaceData.from_buffer_copy(host.surface_data)
+        sd.culled_objects_capacity = host.cull_capacity()
+        self.surface_desc.data = sd
+        self.surface_desc.num_objects = host.num_objects
+        self.surface_desc.num_tiles = host.num_tiles
+        self.objects = host.objects
+        self.tiles = host.tiles
+        self.surface_desc.objects = self.objects.ctypes.data
+        self.surface_desc.tiles = self.tiles.ctypes.data
+        if chunks is None or culled is None:
+            chunks, culled, _ = cull(self.surface_desc, host.cull_capacity())
+        self.chunks = np.ascontiguousarray(chunks, dtype=np.uint32)
+        self.culled = np.ascontiguousarray(culled, dtype=np.uint32)
+        self.surface_desc.chunks = self.chunks.ctypes.data
+        self.surface_desc.culled_objects = self.culled.ctypes.data
+        self.light_cache = np.ascontiguousarray(host.direct.copy() if light_cache is None else light_cache)
+        self.surface_desc.light_cache = self.light_cache.ctypes.data
+        self.surface_desc.depth = host.depth.ctypes.data
+        self.surface_desc.direct_light = host.direct.ctypes.data
+        self.surface_desc.albedo = host.albedo.ctypes.data
+        self.surface_desc.gbuffer0 = host.gbuffer0.ctypes.data
+        self.surface_desc.gbuffer1 = host.gbuffer1.ctypes.data
+
+
+def build_mip(sdf_desc, sdf_float: np.ndarray) -> np.ndarray:
+    s = np.ascontiguousarray(sdf_float, dtype=np.float32)
+    m, C = sdf_desc.mip_resolution, sdf_desc.data.cascades_count
+    out = np.zeros(m * C * m * m, dtype=np.float32)
+    lib().oracle_build_mip(ctypes.byref(sdf_desc), _p(s), _p(out))
+    return out
+
+
+def cull(surface_desc, capacity: int):
+    chunks = np.zeros(40 ** 3, dtype=np.uint32)
+    culled = np.zeros(capacity, dtype=np.uint32)
+    st = lib().oracle_cull(ctypes.byref(surface_desc), _p(chunks), _p(culled), capacity)
+    return chunks, culled, st
+
+
+def trace(vdesc, inputs: HostInputs, rot, frames: int = 0, prev_irr=None, prev_dist=None, precision: int = 0,
+          probes: tuple | None = None, want_info: bool = True):
+    """GISDFRays.comp for probes [p0, p1): (rays [n, R, 4], info [n, R, 4]:
+    steps, hit cascade or -1, full-resolution samples, 0)."""
+    u = vdesc.uniform
+    P = u.probe_counts[0] * u.probe_counts[1] * u.probe_counts[2]
+    p0, p1 = probes if probes is not None else (0, P)
+    R = u.rays_per_probe
+    out = np.zeros((p1 - p0, R, 4), dtype=np.float32)
+    info = np.zeros((p1 - p0, R, 4), dtype=np.int32) if want_info else None
+    rot = np.ascontiguousarray(rot, dtype=np.float32)
+    pi = None if prev_irr is None else np.ascontiguousarray(prev_irr, dtype=np.float32)
+    pd = None if prev_dist is None else np.ascontiguousarray(prev_dist, dtype=np.float32)
+    lib().oracle_trace(ctypes.byref(vdesc), ctypes.byref(inputs.sdf_desc), ctypes.byref(inputs.surface_desc), _p(pi),
+                       _p(pd), frames, _p(rot), precision, p0, p1, _p(out), _p(info))
+    return out, info
+
+
+def blend(vdesc, dirs: np.ndarray, rays: np.ndarray, prev_irr=None, prev_dist=None, first: bool = True,
+          precision: int = 0, border: bool = True, probes: tuple | None = None):
+    """ProbeUpdate.glsl (+ BorderUpdate.glsl): float atlases (irr [H,W,4],
+    dist [H,W,2]); `rays` holds probes [p0, p1) when `probes` is given."""
+    p0, p1 = probes if probes is not None else (0, 0)
+    u = vdesc.uniform
+    irr = np.zeros((u.irradiance_height, u.irradiance_width, 4), dtype=np.float32)
+    dist = np.zeros((u.depth_height, u.depth_width, 2), dtype=np.float32)
+    if prev_irr is not None:
+        irr[...] = prev_irr
+    if prev_dist is not None:
+        dist[...] = prev_dist
+    d = np.ascontiguousarray(dirs, dtype=np.float32)
+    r = np.ascontiguousarray(rays, dtype=np.float32)
+    pi = None if prev_irr is None else np.ascontiguousarray(prev_irr, dtype=np.float32)
+    pd = None if prev_dist is None else np.ascontiguousarray(prev_dist, dtype=np.float32)
+    lib().oracle_blend(ctypes.byref(vdesc), _p(d), _p(r), _p(pi), _p(pd), _p(irr), _p(dist), 1 if first else 0,
+                       precision, 1 if border else 0, p0, p1)
+    return irr, dist
+
+
+def border(uniform, irr: np.ndarray | None, dist: np.ndarray | None) -> None:
+    lib().oracle_border(ctypes.byref(uniform), _p(irr), _p(dist))
+
+
+def inject(vdesc, inputs: HostInputs, irr, dist, frames: int, precision: int = 0) -> np.ndarray:
+    res = inputs.surface_desc.data.resolution
+    out = np.zeros(res * res * 4, dtype=np.uint16)
+    i = np.ascontiguousarray(irr, dtype=np.float32)
+    d = np.ascontiguousarray(dist, dtype=np.float32)
+    lib().oracle_inject(ctypes.byref(vdesc), ctypes.byref(inputs.surface_desc), _p(i), _p(d), frames, precision,
+                        _p(out))
+    return out
+
+
+def sample_irradiance(uniform, irr, dist, pos, nrm, wo, precision: int = 0) -> np.ndarray:
+    i = np.ascontiguousarray(irr, dtype=np.float32)
+    d = np.ascontiguousarray(dist, dtype=np.float32)
+    p = np.ascontiguousarray(pos, dtype=np.float32)
+    n = np.ascontiguousarray(nrm, dtype=np.float32)
+    w = np.ascontiguousarray(wo, dtype=np.float32)
+    out = np.zeros_like(p)
+    lib().oracle_sample_irradiance(ctypes.byref(uniform), _p(i), _p(d), _p(p), _p(n), _p(w), _p(out), p.shape[0],
+                                   precision)
+    return out
+
+
+def run_frames(vdesc, inputs: HostInputs, rots, precision: int = 0, inject_every: int = 0,
+               state: tuple | None = None):
+    """Whole frames (trace, blend + border, ping-pong) on the CPU.
+
+    Returns (irr, dist, frames_done, last_rays).  Mode-A volumes refresh the
+    light cache with inject() every `inject_every` frames (0 = never),
+    before that frame's trace."""
+    from luxgi_gb300 import _native as N
+
+    u = vdesc.uniform
+    fp16 = vdesc.storage == N.STORAGE_FP16
+    irr, dist, frames = (None, None, 0) if state is None else state
+    rays = None
+    for rot in rots:
+        if inject_every and vdesc.light_mode == N.LIGHT_CACHE and frames % inject_every == 0 and frames > 0:
+            inputs.light_cache[...] = inject(vdesc, inputs, irr, dist, frames, precision)
+        rays, _ = trace(vdesc, inputs, rot, frames, irr, dist, precision, want_info=False)
+        dirs = ray_dirs(rot, u.rays_per_probe, precision, fp16)
+        irr, dist = blend(vdesc, dirs, rays, irr, dist, first=(frames == 0), precision=precision)
+        frames += 1
+    return irr, dist, frames, rays

@@ -1,0 +1,1016 @@
+// ORACLE -- test infrastructure only.  Not part of the product path.
+//
+// A CPU restatement (C++17, OpenMP over probes) of LuxGI's non-raytracing
+// DDGI probe update, written from the reference GLSL.  Every function cites
+// the reference lines it follows (paths relative to Code/Maple/src/Shaders/
+// unless stated).  Templated on the arithmetic type: R = float is the FP32
+// transcription (same operation order as the CUDA kernels, no FP
+// contraction, so the SDF march matches them bit for bit), R = double is the
+// FP64 error reference.  The FP16-storage switch rounds at the points where
+// the reference stores RGBA16F / RG16F (Engine/DDGI/DDGIRenderer.cpp:173-204).
+//
+// Parity pins: the reference ships no tests or golden data.  This oracle is
+// pinned by analytic known-answer tests and by the border tables read from
+// the reference source (tests/golden/); see the repository design notes for
+// what that leaves unpinned.
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+// this library.
+#include "../include/luxgi_ddgi.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------- vectors
+template <typename R> struct V2 { R x, y; };
+template <typename R> struct V3 { R x, y, z; };
+template <typename R> struct V4 { R x, y, z, w; };
+
+template <typename R> inline V3<R> v3(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <typename R> inline V3<R> add(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename R> inline V3<R> sub(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename R> inline V3<R> mul(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <typename R> inline V3<R> mulv(V3<R> a, V3<R> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+// GLSL dot: left-to-right sum of products
+template <typename R> inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename R> inline R length(V3<R> a) { return std::sqrt(dot(a, a)); }
+// normalize(v) = v * (1 / sqrt(dot(v, v))) -- the form the kernels use too
+template <typename R> inline V3<R> normalize(V3<R> a) { R inv = R(1) / std::sqrt(dot(a, a)); return mul(a, inv); }
+template <typename R> inline R clampr(R v, R lo, R hi) { return std::min(std::max(v, lo), hi); }
+template <typename R> inline R fractr(R v) { return v - std::floor(v); }
+template <typename R> inline R mixr(R x, R y, R a) { return x * (R(1) - a) + y * a; }
+
+// column-major 4x4: m[col*4 + row]
+template <typename R> struct M4 { R m[16]; };
+template <typename R> inline M4<R> load_m4(const float* f) { M4<R> r; for (int i = 0; i < 16; ++i) r.m[i] = R(f[i]); return r; }
+template <typename R> inline V4<R> mul_m4(const M4<R>& M, V4<R> v) {
+    const R* m = M.m;
+    return {m[0] * v.x + m[4] * v.y + m[8] * v.z + m[12] * v.w,
+            m[1] * v.x + m[5] * v.y + m[9] * v.z + m[13] * v.w,
+            m[2] * v.x + m[6] * v.y + m[10] * v.z + m[14] * v.w,
+            m[3] * v.x + m[7] * v.y + m[11] * v.z + m[15] * v.w};
+}
+// mat3(M) * v
+template <typename R> inline V3<R> mul_m3of4(const M4<R>& M, V3<R> v) {
+    const R* m = M.m;
+    return {m[0] * v.x + m[4] * v.y + m[8] * v.z,
+            m[1] * v.x + m[5] * v.y + m[9] * v.z,
+            m[2] * v.x + m[6] * v.y + m[10] * v.z};
+}
+// inverse(M): adjugate / determinant, cofactors from 2x2 sub-determinants of
+// the lower and upper row pairs (Laplace expansion).
+template <typename R> inline M4<R> inverse(const M4<R>& A) {
+    // a[r][c]
+    R a[4][4];
+    for (int c = 0; c < 4; ++c) for (int r = 0; r < 4; ++r) a[r][c] = A.m[c * 4 + r];
+    R s0 = a[0][0] * a[1][1] - a[1][0] * a[0][1];
+    R s1 = a[0][0] * a[1][2] - a[1][0] * a[0][2];
+    R s2 = a[0][0] * a[1][3] - a[1][0] * a[0][3];
+    R s3 = a[0][1] * a[1][2] - a[1][1] * a[0][2];
+    R s4 = a[0][1] * a[1][3] - a[1][1] * a[0][3];
+    R s5 = a[0][2] * a[1][3] - a[1][2] * a[0][3];
+    R c5 = a[2][2] * a[3][3] - a[3][2] * a[2][3];
+    R c4 = a[2][1] * a[3][3] - a[3][1] * a[2][3];
+    R c3 = a[2][1] * a[3][2] - a[3][1] * a[2][2];
+    R c2 = a[2][0] * a[3][3] - a[3][0] * a[2][3];
+    R c1 = a[2][0] * a[3][2] - a[3][0] * a[2][2];
+    R c0 = a[2][0] * a[3][1] - a[3][0] * a[2][1];
+    R det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    R id = R(1) / det;
+    R b[4][4];
+    b[0][0] = ( a[1][1] * c5 - a[1][2] * c4 + a[1][3] * c3) * id;
+    b[0][1] = (-a[0][1] * c5 + a[0][2] * c4 - a[0][3] * c3) * id;
+    b[0][2] = ( a[3][1] * s5 - a[3][2] * s4 + a[3][3] * s3) * id;
+    b[0][3] = (-a[2][1] * s5 + a[2][2] * s4 - a[2][3] * s3) * id;
+    b[1][0] = (-a[1][0] * c5 + a[1][2] * c2 - a[1][3] * c1) * id;
+    b[1][1] = ( a[0][0] * c5 - a[0][2] * c2 + a[0][3] * c1) * id;
+    b[1][2] = (-a[3][0] * s5 + a[3][2] * s2 - a[3][3] * s1) * id;
+    b[1][3] = ( a[2][0] * s5 - a[2][2] * s2 + a[2][3] * s1) * id;
+    b[2][0] = ( a[1][0] * c4 - a[1][1] * c2 + a[1][3] * c0) * id;
+    b[2][1] = (-a[0][0] * c4 + a[0][1] * c2 - a[0][3] * c0) * id;
+    b[2][2] = ( a[3][0] * s4 - a[3][1] * s2 + a[3][3] * s0) * id;
+    b[2][3] = (-a[2][0] * s4 + a[2][1] * s2 - a[2][3] * s0) * id;
+    b[3][0] = (-a[1][0] * c3 + a[1][1] * c1 - a[1][2] * c0) * id;
+    b[3][1] = ( a[0][0] * c3 - a[0][1] * c1 + a[0][2] * c0) * id;
+    b[3][2] = (-a[3][0] * s3 + a[3][1] * s1 - a[3][2] * s0) * id;
+    b[3][3] = ( a[2][0] * s3 - a[2][1] * s1 + a[2][2] * s0) * id;
+    M4<R> out;
+    for (int c = 0; c < 4; ++c) for (int r = 0; r < 4; ++r) out.m[c * 4 + r] = b[r][c];
+    return out;
+}
+
+inline float h2f(uint16_t h) { _Float16 v; std::memcpy(&v, &h, 2); return float(v); }
+inline float round_half(float f) { return float(_Float16(f)); }
+
+// ---------------------------------------------------------- sin / cos
+// FP32: Cody-Waite reduction by pi/2 and Taylor polynomials of degree 9/8 on
+// [-pi/4, pi/4]; the CUDA ray generator evaluates the same sequence.  FP64:
+// the C library.  (GLSL leaves sin/cos precision to the implementation.)
+inline void sincos_r(float x, float* s, float* c) {
+    const float k = std::floor(x * 0.63661977f + 0.5f);
+    const float r = (x - k * 1.57079637f) - k * -4.37113883e-8f;
+    const float r2 = r * r;
+    const float sp = r + r * r2 * (-0.166666672f + r2 * (0.00833333377f + r2 * (-0.000198412701f + r2 * 2.75573188e-6f)));
+    const float cp = 1.0f + r2 * (-0.5f + r2 * (0.0416666679f + r2 * (-0.00138888892f + r2 * 2.48015876e-5f)));
+    const int q = int(k) & 3;
+    if (q == 0) { *s = sp; *c = cp; }
+    else if (q == 1) { *s = cp; *c = -sp; }
+    else if (q == 2) { *s = -sp; *c = -cp; }
+    else { *s = -cp; *c = sp; }
+}
+inline void sincos_r(double x, double* s, double* c) { *s = std::sin(x); *c = std::cos(x); }
+
+template <typename R> inline R pi_r();
+template <> inline float pi_r<float>() { return 3.14159265f; }
+template <> inline double pi_r<double>() { return 3.14159265358979323846; }
+
+// ------------------------------------------------ DDGICommon.glsl
+// sphericalFibonacci (DDGICommon.glsl:42-52)
+template <typename R> V3<R> spherical_fibonacci(R i, R n) {
+    const R PHI = std::sqrt(R(5)) * R(0.5) + R(0.5);
+    R t = i * (PHI - R(1));
+    R mf = t - std::floor(t);
+    R phi = (R(2) * pi_r<R>()) * mf;
+    R cos_t = R(1) - (R(2) * i + R(1)) * (R(1) / n);
+    R sin_t = std::sqrt(clampr(R(1) - cos_t * cos_t, R(0), R(1)));
+    R sp, cp;
+    sincos_r(phi, &sp, &cp);
+    return {cp * sin_t, sp * sin_t, cos_t};
+}
+
+template <typename R> inline R sign_not_zero(R k) { return k >= R(0) ? R(1) : R(-1); }
+
+// octEncode (DDGICommon.glsl:65-72)
+template <typename R> V2<R> oct_encode(V3<R> v) {
+    R l1 = std::fabs(v.x) + std::fabs(v.y) + std::fabs(v.z);
+    R inv = R(1) / l1;
+    V2<R> r{v.x * inv, v.y * inv};
+    if (v.z < R(0)) {
+        V2<R> t{(R(1) - std::fabs(r.y)) * sign_not_zero(r.x), (R(1) - std::fabs(r.x)) * sign_not_zero(r.y)};
+        r = t;
+    }
+    return r;
+}
+// octDecode (DDGICommon.glsl:74-82)
+template <typename R> V3<R> oct_decode(V2<R> o) {
+    V3<R> v{o.x, o.y, R(1) - std::fabs(o.x) - std::fabs(o.y)};
+    if (v.z < R(0)) {
+        R nx = (R(1) - std::fabs(v.y)) * sign_not_zero(v.x);
+        R ny = (R(1) - std::fabs(v.x)) * sign_not_zero(v.y);
+        v.x = nx; v.y = ny;
+    }
+    return normalize(v);
+}
+// normalizedOctCoord (DDGICommon.glsl:85-92) for interior texel (tx, ty)
+template <typename R> V2<R> normalized_oct_coord(int tx, int ty, int side) {
+    R s = R(2) / R(side);
+    return {(R(tx) + R(0.5)) * s - R(1), (R(ty) + R(0.5)) * s - R(1)};
+}
+// textureCoordFromDirection (DDGICommon.glsl:141-158)
+template <typename R> V2<R> tex_coord_from_dir(V3<R> dir, int probe, int width, int height, int side) {
+    V2<R> o = oct_encode(normalize(dir));
+    V2<R> zo{(o.x + R(1)) * R(0.5), (o.y + R(1)) * R(0.5)};
+    R pwb = R(side) + R(2);
+    V2<R> octn{(zo.x * R(side)) / R(width), (zo.y * R(side)) / R(height)};
+    int ppr = (width - 2) / int(pwb);
+    V2<R> tl{R(probe % ppr) * pwb + R(2), R(probe / ppr) * pwb + R(2)};
+    V2<R> tln{tl.x / R(width), tl.y / R(height)};
+    return {tln.x + octn.x, tln.y + octn.y};
+}
+
+// ------------------------------------------------ texture emulation
+// GL LINEAR filtering, CLAMP_TO_EDGE, on the packed SDF (x fastest).
+struct Vol {
+    const float* f32 = nullptr;
+    const uint16_t* f16 = nullptr;
+    int W = 0, H = 0, D = 0;
+    float at(int x, int y, int z) const {
+        size_t i = size_t(x) + size_t(W) * (size_t(y) + size_t(H) * size_t(z));
+        return f16 ? h2f(f16[i]) : f32[i];
+    }
+};
+template <typename R> R sample3d(const Vol& v, V3<R> uvw) {
+    R x = uvw.x * R(v.W) - R(0.5), y = uvw.y * R(v.H) - R(0.5), z = uvw.z * R(v.D) - R(0.5);
+    R fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+    R a = x - fx, b = y - fy, c = z - fz;
+    int x0 = int(fx), y0 = int(fy), z0 = int(fz);
+    int x1 = std::min(std::max(x0 + 1, 0), v.W - 1), y1 = std::min(std::max(y0 + 1, 0), v.H - 1),
+        z1 = std::min(std::max(z0 + 1, 0), v.D - 1);
+    x0 = std::min(std::max(x0, 0), v.W - 1); y0 = std::min(std::max(y0, 0), v.H - 1);
+    z0 = std::min(std::max(z0, 0), v.D - 1);
+    R t000 = R(v.at(x0, y0, z0)), t100 = R(v.at(x1, y0, z0));
+    R t010 = R(v.at(x0, y1, z0)), t110 = R(v.at(x1, y1, z0));
+    R t001 = R(v.at(x0, y0, z1)), t101 = R(v.at(x1, y0, z1));
+    R t011 = R(v.at(x0, y1, z1)), t111 = R(v.at(x1, y1, z1));
+    R ia = R(1) - a, ib = R(1) - b, ic = R(1) - c;
+    R c00 = t000 * ia + t100 * a, c10 = t010 * ia + t110 * a;
+    R c01 = t001 * ia + t101 * a, c11 = t011 * ia + t111 * a;
+    R c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
+// 2D atlas texel access
+struct Tex2 {
+    const float* f32 = nullptr;      // interleaved channels
+    const uint16_t* f16 = nullptr;
+    const uint8_t* u8 = nullptr;     // UNORM
+    int W = 0, H = 0, C = 4;
+    float at(int x, int y, int ch) const {
+        size_t i = (size_t(y) * size_t(W) + size_t(x)) * size_t(C) + size_t(ch);
+        if (f16) return h2f(f16[i]);
+        if (u8) return float(u8[i]) / 255.0f;
+        return f32[i];
+    }
+};
+// textureGather component order: (i0,j1), (i1,j1), (i1,j0), (i0,j0); clamp to edge
+template <typename R> V4<R> gather(const Tex2& t, V2<R> uv, int ch) {
+    R x = uv.x * R(t.W) - R(0.5), y = uv.y * R(t.H) - R(0.5);
+    int i0 = int(std::floor(x)), j0 = int(std::floor(y));
+    int i1 = std::min(std::max(i0 + 1, 0), t.W - 1), j1 = std::min(std::max(j0 + 1, 0), t.H - 1);
+    i0 = std::min(std::max(i0, 0), t.W - 1); j0 = std::min(std::max(j0, 0), t.H - 1);
+    return {R(t.at(i0, j1, ch)), R(t.at(i1, j1, ch)), R(t.at(i1, j0, ch)), R(t.at(i0, j0, ch))};
+}
+// textureLod(..., 0) bilinear with REPEAT (default sampler of the probe atlases)
+template <typename R> R bilinear_repeat(const Tex2& t, V2<R> uv, int ch) {
+    R x = uv.x * R(t.W) - R(0.5), y = uv.y * R(t.H) - R(0.5);
+    R fx = std::floor(x), fy = std::floor(y);
+    R a = x - fx, b = y - fy;
+    auto wrap = [](int i, int n) { int r = i % n; return r < 0 ? r + n : r; };
+    int i0 = wrap(int(fx), t.W), i1 = wrap(int(fx) + 1, t.W);
+    int j0 = wrap(int(fy), t.H), j1 = wrap(int(fy) + 1, t.H);
+    R t00 = R(t.at(i0, j0, ch)), t10 = R(t.at(i1, j0, ch)), t01 = R(t.at(i0, j1, ch)), t11 = R(t.at(i1, j1, ch));
+    R r0 = t00 * (R(1) - a) + t10 * a, r1 = t01 * (R(1) - a) + t11 * a;
+    return r0 * (R(1) - b) + r1 * b;
+}
+
+// ------------------------------------------------ SDFCommon.glsl
+template <typename R> struct Hit {
+    V3<R> normal{R(0), R(0), R(0)};
+    R time = R(-1);
+    int cascade = 0;
+    int steps = 0;
+    int fine = 0;
+    R sdf = R(0);
+};
+
+// lineHitAABB (SDFCommon.glsl:84-95)
+template <typename R> V2<R> line_hit_aabb(V3<R> s, V3<R> e, V3<R> bmin, V3<R> bmax) {
+    V3<R> d = sub(e, s);
+    V3<R> inv{R(1) / d.x, R(1) / d.y, R(1) / d.z};
+    V3<R> en{(bmin.x - s.x) * inv.x, (bmin.y - s.y) * inv.y, (bmin.z - s.z) * inv.z};
+    V3<R> ex{(bmax.x - s.x) * inv.x, (bmax.y - s.y) * inv.y, (bmax.z - s.z) * inv.z};
+    V3<R> mn{std::min(en.x, ex.x), std::min(en.y, ex.y), std::min(en.z, ex.z)};
+    V3<R> mx{std::max(en.x, ex.x), std::max(en.y, ex.y), std::max(en.z, ex.z)};
+    V2<R> r{std::max(mn.x, std::max(mn.y, mn.z)), std::min(mx.x, std::min(mx.y, mx.z))};
+    return {clampr(r.x, R(0), R(1)), clampr(r.y, R(0), R(1))};
+}
+
+// getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
+template <typename R> V3<R> cascade_texture_uv(const luxgi_sdf_data& d, int cascade, V3<R> p, R* max_dist) {
+    V3<R> c{R(d.cascade_pos_distance[cascade][0]), R(d.cascade_pos_distance[cascade][1]), R(d.cascade_pos_distance[cascade][2])};
+    R w = R(d.cascade_pos_distance[cascade][3]);
+    V3<R> pic = sub(p, c);
+    R md = w * R(2);
+    *max_dist = md;
+    V3<R> cuv{clampr(pic.x / md + R(0.5), R(0), R(1)), clampr(pic.y / md + R(0.5), R(0), R(1)),
+              clampr(pic.z / md + R(0.5), R(0), R(1))};
+    return {(R(cascade) + cuv.x) / R(d.cascades_count), cuv.y, cuv.z};
+}
+
+// tracyGlobalSDF (SDFCommon.glsl:98-194); stepScale = 1, start bias 0,
+// needsHitNormal = true, minDistance = 0 as GISDFRays.comp:79-87 sets them.
+template <typename R> Hit<R> trace_sdf(const luxgi_sdf_data& d, const Vol& tex, const Vol& mip,
+                                       V3<R> origin, V3<R> dir, R trace_max, int max_steps) {
+    Hit<R> hit;
+    const int C = int(d.cascades_count);
+    R tmax = std::min(trace_max, R(d.cascade_pos_distance[C - 1][3]) * R(2));
+    R chunk = R(32) / R(d.resolution);
+    R margin = R(4) / R(d.resolution);
+    R next_start = R(0);
+    V3<R> end = add(origin, mul(dir, tmax));
+    for (int cascade = 0; cascade < C && hit.time < R(0); ++cascade) {
+        V3<R> cpos{R(d.cascade_pos_distance[cascade][0]), R(d.cascade_pos_distance[cascade][1]), R(d.cascade_pos_distance[cascade][2])};
+        R cw = R(d.cascade_pos_distance[cascade][3]);
+        R voxel = R(d.cascade_voxel_size[cascade]);
+        R voxel_half = voxel * R(0.5);
+        V3<R> wpos = add(origin, mul(dir, voxel * R(0)));
+        V2<R> is = line_hit_aabb(wpos, end, v3(cpos.x - cw, cpos.y - cw, cpos.z - cw), v3(cpos.x + cw, cpos.y + cw, cpos.z + cw));
+        is.x = is.x * tmax;
+        is.y = is.y * tmax;
+        is.x = std::max(is.x, next_start);
+        R t = is.x;
+        if (is.x >= is.y) t = is.y;
+        else next_start = is.y;
+        int step = 0;
+        for (; step < max_steps && t < is.y; ++step) {
+            V3<R> sp = add(wpos, mul(dir, t));
+            R cmd;
+            V3<R> uv = cascade_texture_uv(d, cascade, sp, &cmd);
+            R sd = sample3d(mip, uv);
+            if (sd < chunk) {
+                R sdt = sample3d(tex, uv);
+                ++hit.fine;
+                if (sdt < margin * R(2)) sd = sdt;
+            } else {
+                sd = chunk;
+            }
+            sd = sd * cmd;
+            R thick = voxel_half * clampr(t / voxel, R(0), R(1));
+            if (sd < thick) {
+                hit.time = std::max(t + sd - thick, R(0));
+                hit.cascade = cascade;
+                hit.sdf = sd;
+                R off = R(1) / R(d.resolution);
+                R xp = sample3d(tex, v3(uv.x + off, uv.y, uv.z));
+                R xn = sample3d(tex, v3(uv.x - off, uv.y, uv.z));
+                R yp = sample3d(tex, v3(uv.x, uv.y + off, uv.z));
+                R yn = sample3d(tex, v3(uv.x, uv.y - off, uv.z));
+                R zp = sample3d(tex, v3(uv.x, uv.y, uv.z + off));
+                R zn = sample3d(tex, v3(uv.x, uv.y, uv.z - off));
+                hit.normal = normalize(v3(xp - xn, yp - yn, zp - zn));
+                break;
+            }
+            t = t + std::max(sd * R(1), voxel);
+        }
+        hit.steps += step;
+    }
+    return hit;
+}
+
+// ------------------------------------------------ AtlasCommon.glsl
+struct Surface {
+    const luxgi_surface_desc* d;
+    Tex2 depth, c0, c1;     // c1 used for the second (albedo) atlas in mode B
+    bool two = false;
+};
+
+// sampleGlobalSurfaceAtlasTile, both overloads (AtlasCommon.glsl:58-112).
+// Accumulates colour * weight into acc0 (and acc1 for the second atlas).
+template <typename R> void sample_tile(const Surface& S, const luxgi_surface_tile& tile, V3<R> local,
+                                       V3<R> nrm_local, R thr, V3<R>& acc0, V3<R>& acc1, R& accw) {
+    M4<R> T = load_m4<R>(tile.transform);
+    V4<R> n4 = mul_m4(T, V4<R>{nrm_local.x, nrm_local.y, nrm_local.z, R(1)});
+    V3<R> n = normalize(V3<R>{n4.x, n4.y, n4.z});
+    R nw = clampr(R(0) * n.x + R(0) * n.y + R(1) * n.z, R(0), R(1));
+    nw = (nw - R(0.05f)) / (R(1) - R(0.05f));
+    if (nw <= R(0)) return;
+    V4<R> tp = mul_m4(T, V4<R>{local.x, local.y, local.z, R(1)});
+    R bx = R(tile.object_bounds[0]), by = R(tile.object_bounds[1]), bz = R(tile.object_bounds[2]);
+    R tdepth = tp.z / bz;
+    V2<R> tuv{clampr(tp.x / bx + R(0.5), R(0), R(1)), clampr(tp.y / by + R(0.5), R(0), R(1))};
+    V2<R> auv{tuv.x * R(tile.extends[2]) + R(tile.extends[0]), tuv.y * R(tile.extends[3]) + R(tile.extends[1])};
+    R res = R(S.d->data.resolution);
+    V2<R> bwu{fractr(auv.x * res + R(0.5)), fractr(auv.y * res + R(0.5))};
+    V4<R> bw{(R(1) - bwu.x) * bwu.y, bwu.x * bwu.y, bwu.x * (R(1) - bwu.y), (R(1) - bwu.x) * (R(1) - bwu.y)};
+    V4<R> tz = gather(S.depth, auv, 0);
+    R dthr = R(2) * thr / bz;
+    R dv[4];
+    R tzs[4] = {tz.x, tz.y, tz.z, tz.w};
+    for (int i = 0; i < 4; ++i) {
+        dv[i] = R(1) - clampr((std::fabs(tdepth - tzs[i]) - dthr) / (R(0.5) * dthr), R(0), R(1));
+        if (tzs[i] >= R(1)) dv[i] = R(0);
+    }
+    R sw = dv[0] * bw.x + dv[1] * bw.y + dv[2] * bw.z + dv[3] * bw.w;
+    sw = sw * nw;
+    if (sw <= R(0)) return;
+    V4<R> w{bw.x * dv[0], bw.y * dv[1], bw.z * dv[2], bw.w * dv[3]};
+    auto color = [&](const Tex2& tex) {
+        V4<R> gx = gather(tex, auv, 0), gy = gather(tex, auv, 1), gz = gather(tex, auv, 2);
+        return V3<R>{gx.x * w.x + gx.y * w.y + gx.z * w.z + gx.w * w.w,
+                     gy.x * w.x + gy.y * w.y + gy.z * w.z + gy.w * w.w,
+                     gz.x * w.x + gz.y * w.y + gz.z * w.z + gz.w * w.w};
+    };
+    V3<R> c0 = color(S.c0);
+    acc0 = add(acc0, mul(c0, sw));
+    if (S.two) {
+        V3<R> c1 = color(S.c1);
+        acc1 = add(acc1, mul(c1, sw));
+    }
+    accw = accw + sw;
+}
+
+// sampleGlobalSurfaceAtlas macro (AtlasCommon.glsl:115-157), debug = false.
+template <typename R> R sample_surface(const Surface& S, V3<R> pos, V3<R> wn, R thr, V3<R>& out0, V3<R>& out1) {
+    const luxgi_surface_desc* d = S.d;
+    V3<R> acc0{R(0), R(0), R(0)}, acc1{R(0), R(0), R(0)};
+    R accw = R(0);
+    R cs = R(d->data.chunk_size);
+    int cc[3];
+    R pc[3] = {pos.x, pos.y, pos.z};
+    for (int k = 0; k < 3; ++k) {
+        int v = int(std::floor(pc[k] / cs + R(40 * 0.5f)));
+        cc[k] = std::min(std::max(v, 0), 39);
+    }
+    uint32_t addr = uint32_t(cc[2] * 40 * 40 + cc[1] * 40 + cc[0]);
+    uint32_t start = d->chunks[addr];
+    out0 = acc0; out1 = acc1;
+    if (start == 0) return R(0);
+    uint32_t count = d->culled_objects[start];
+    if (count > d->data.objects_count) return R(0);
+    ++start;
+    for (uint32_t oi = 0; oi < count; ++oi) {
+        uint32_t oaddr = d->culled_objects[start++];
+        const luxgi_surface_object& ob = d->objects[oaddr];
+        V3<R> bc{R(ob.object_bounds[0]), R(ob.object_bounds[1]), R(ob.object_bounds[2])};
+        if (length(sub(bc, pos)) > R(ob.object_bounds[3])) continue;
+        M4<R> w2l = inverse(load_m4<R>(ob.transform));
+        V4<R> lp4 = mul_m4(w2l, V4<R>{pos.x, pos.y, pos.z, R(1)});
+        V3<R> lp{lp4.x, lp4.y, lp4.z};
+        V3<R> ext{R(ob.extends[0]) + thr, R(ob.extends[1]) + thr, R(ob.extends[2]) + thr};
+        if (std::fabs(lp.x) > ext.x || std::fabs(lp.y) > ext.y || std::fabs(lp.z) > ext.z) continue;
+        V3<R> ln = normalize(mul_m3of4(w2l, wn));
+        for (int i = 0; i < 6; ++i) {
+            uint32_t to = ob.tile_offset[i];
+            if (to != 0) sample_tile(S, d->tiles[to], lp, ln, thr, acc0, acc1, accw);
+        }
+    }
+    R den = std::max(accw, R(0.0001f));
+    out0 = V3<R>{acc0.x / den, acc0.y / den, acc0.z / den};
+    out1 = V3<R>{acc1.x / den, acc1.y / den, acc1.z / den};
+    return accw;
+}
+
+// ------------------------------------------------ sampleIrradiance
+struct Atlases {
+    Tex2 irr, dist;
+};
+// sampleIrradiance (DDGICommon.glsl:163-233)
+template <typename R> V3<R> sample_irradiance(const luxgi_ddgi_uniform& u, const Atlases& A, V3<R> P, V3<R> N, V3<R> Wo) {
+    V3<R> start{R(u.start_position[0]), R(u.start_position[1]), R(u.start_position[2])};
+    V3<R> stp{R(u.step[0]), R(u.step[1]), R(u.step[2])};
+    int cnt[3] = {u.probe_counts[0], u.probe_counts[1], u.probe_counts[2]};
+    V3<R> rel{(P.x - start.x) / stp.x, (P.y - start.y) / stp.y, (P.z - start.z) / stp.z};
+    int base[3] = {int(rel.x), int(rel.y), int(rel.z)};
+    for (int k = 0; k < 3; ++k) base[k] = std::min(std::max(base[k], 0), cnt[k] - 1);
+    V3<R> bpos{stp.x * R(base[0]) + start.x, stp.y * R(base[1]) + start.y, stp.z * R(base[2]) + start.z};
+    V3<R> alpha{clampr((P.x - bpos.x) / stp.x, R(0), R(1)), clampr((P.y - bpos.y) / stp.y, R(0), R(1)),
+                clampr((P.z - bpos.z) / stp.z, R(0), R(1))};
+    V3<R> sum{R(0), R(0), R(0)};
+    R sumw = R(0);
+    for (int i = 0; i < 8; ++i) {
+        int off[3] = {i & 1, (i >> 1) & 1, (i >> 2) & 1};
+        int g[3];
+        for (int k = 0; k < 3; ++k) g[k] = std::min(std::max(base[k] + off[k], 0), cnt[k] - 1);
+        V3<R> ppos{stp.x * R(g[0]) + start.x, stp.y * R(g[1]) + start.y, stp.z * R(g[2]) + start.z};
+        V3<R> tri{off[0] ? alpha.x : R(1) - alpha.x, off[1] ? alpha.y : R(1) - alpha.y, off[2] ? alpha.z : R(1) - alpha.z};
+        R weight = R(1);
+        V3<R> dtp = normalize(sub(ppos, P));
+        R bf = std::max(R(0.0001f), (dot(dtp, N) + R(1)) * R(0.5));
+        weight = weight * (bf * bf + R(0.2f));
+        int pidx = g[0] + g[1] * cnt[0] + g[2] * cnt[0] * cnt[1];
+        V3<R> vb = mul(add(N, mul(Wo, R(3))), R(u.normal_bias));
+        V3<R> ptp = add(sub(P, ppos), vb);
+        V3<R> dir = normalize(mul(ptp, R(-1)));
+        V2<R> tc = tex_coord_from_dir(mul(dir, R(-1)), pidx, u.depth_width, u.depth_height, u.depth_probe_side);
+        R dist = length(ptp);
+        R mean = bilinear_repeat(A.dist, tc, 0);
+        R mean2 = bilinear_repeat(A.dist, tc, 1);
+        R variance = std::fabs(mean * mean - mean2);
+        R dm = std::max(dist - mean, R(0));
+        R cheb = variance / (variance + dm * dm);
+        cheb = std::max(cheb * cheb * cheb, R(0));
+        weight = weight * ((dist <= mean) ? R(1) : cheb);
+        weight = std::max(R(0.000001f), weight);
+        tc = tex_coord_from_dir(normalize(N), pidx, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side);
+        R ge = R(u.ddgi_gamma) * R(0.5);
+        V3<R> pir{std::pow(bilinear_repeat(A.irr, tc, 0), ge), std::pow(bilinear_repeat(A.irr, tc, 1), ge),
+                  std::pow(bilinear_repeat(A.irr, tc, 2), ge)};
+        const R crush = R(0.2f);
+        if (weight < crush) weight = weight * (weight * weight * (R(1) / (crush * crush)));
+        weight = weight * (tri.x * tri.y * tri.z);
+        sum = add(sum, mul(pir, weight));
+        sumw = sumw + weight;
+    }
+    V3<R> net{sum.x / sumw, sum.y / sumw, sum.z / sumw};
+    net = mulv(net, net);
+    return mul(net, R(2) * pi_r<R>());
+}
+
+// ------------------------------------------------ probe location
+template <typename R> V3<R> probe_location(const luxgi_ddgi_uniform& u, int index) {
+    int X = u.probe_counts[0], Y = u.probe_counts[1];
+    int gx = index % X, gy = (index % (X * Y)) / X, gz = index / (X * Y);
+    return {R(u.step[0]) * R(gx) + R(u.start_position[0]), R(u.step[1]) * R(gy) + R(u.start_position[1]),
+            R(u.step[2]) * R(gz) + R(u.start_position[2])};
+}
+
+template <typename R> V3<R> ray_direction(const float rot[9], int r, int nrays) {
+    V3<R> f = spherical_fibonacci<R>(R(r), R(nrays));
+    // mat3(randomOrientation) * f, column-major
+    V3<R> m{R(rot[0]) * f.x + R(rot[3]) * f.y + R(rot[6]) * f.z,
+            R(rot[1]) * f.x + R(rot[4]) * f.y + R(rot[7]) * f.z,
+            R(rot[2]) * f.x + R(rot[5]) * f.y + R(rot[8]) * f.z};
+    return normalize(m);
+}
+
+struct TraceCtx {
+    const luxgi_ddgi_volume_desc* vd;
+    const luxgi_sdf_desc* sdf;
+    const luxgi_surface_desc* surf;
+    Vol tex, mip;
+    Surface S;
+    Atlases prev;
+    bool bounce;   // infinite bounce active this frame (mode B)
+};
+
+// GISDFRays.comp main (GISDFRays.comp:63-128) for one (probe, ray).
+// out: rgb radiance, distance; info: steps, hit cascade (-1 = miss).
+template <typename R> void trace_one(const TraceCtx& c, const float rot[9], int probe, int ray, float out[4], int32_t info[4]) {
+    const luxgi_ddgi_uniform& u = c.vd->uniform;
+    const luxgi_sdf_data& sd = c.sdf->data;
+    const R WORLD = R(60000.0f);
+    V3<R> origin = probe_location<R>(u, probe);
+    V3<R> dir = ray_direction<R>(rot, ray, u.rays_per_probe);
+    Hit<R> hit = trace_sdf<R>(sd, c.tex, c.mip, origin, dir, WORLD, c.vd->max_steps);
+    V3<R> rad{R(0), R(0), R(0)};
+    R dist;
+    info[0] = hit.steps;
+    info[1] = -1;
+    info[2] = hit.fine;
+    info[3] = 0;
+    if (hit.time >= R(0)) {
+        info[1] = hit.cascade;
+        if (hit.sdf <= R(0) && hit.time <= R(sd.cascade_voxel_size[0])) {
+            dist = WORLD;
+        } else {
+            V3<R> hp = add(origin, mul(dir, hit.time));
+            R thr = R(sd.cascade_voxel_size[hit.cascade]) * R(1.05f);
+            V3<R> s0, s1;
+            sample_surface(c.S, hp, hit.normal, thr, s0, s1);
+            if (c.vd->light_mode == LUXGI_LIGHT_PER_HIT) {
+                rad = s0;
+                if (c.bounce) {
+                    // intensity * albedo / pi * E (Raytraced/Lighting.glsl:79-84, with the
+                    // volume intensity SDFAtlasIndirectLight.frag:74 applies)
+                    V3<R> e = sample_irradiance<R>(u, c.prev, hp, hit.normal, mul(dir, R(-1)));
+                    V3<R> diff{s1.x / pi_r<R>(), s1.y / pi_r<R>(), s1.z / pi_r<R>()};
+                    rad = add(rad, mulv(mul(diff, R(c.vd->intensity)), e));
+                }
+            } else {
+                rad = s0;
+            }
+            dist = std::max(hit.time + R(sd.cascade_voxel_size[hit.cascade]) * R(0.5), R(0));
+        }
+    } else {
+        rad = V3<R>{R(c.vd->sky_radiance[0]), R(c.vd->sky_radiance[1]), R(c.vd->sky_radiance[2])};
+        dist = WORLD;
+    }
+    out[0] = float(rad.x); out[1] = float(rad.y); out[2] = float(rad.z); out[3] = float(dist);
+    if (c.vd->storage == LUXGI_STORAGE_FP16)
+        for (int k = 0; k < 4; ++k) out[k] = round_half(out[k]);
+}
+
+// ------------------------------------------------ ProbeUpdate.glsl
+// One probe of the irradiance or distance blend (ProbeUpdate.glsl:195-281).
+// dirs: float4 [R] (already storage-rounded), rays: float4 [P][R].
+template <typename R> void blend_probe(const luxgi_ddgi_volume_desc* vd, const float* dirs, const float* rays,
+                                       const float* prev, float* out, int probe, bool depth, bool first, int p0) {
+    const luxgi_ddgi_uniform& u = vd->uniform;
+    const int n = depth ? u.depth_probe_side : u.irradiance_probe_side;
+    const int W = depth ? u.depth_width : u.irradiance_width;
+    const int nc = depth ? 2 : 4;
+    const int XY = u.probe_counts[0] * u.probe_counts[1];
+    const int cx = probe % XY, cy = probe / XY;
+    const int Rn = u.rays_per_probe;
+    const R FLT_EPS = R(0.00000001f);
+    for (int ty = 0; ty < n; ++ty) {
+        for (int tx = 0; tx < n; ++tx) {
+            V3<R> td = oct_decode(normalized_oct_coord<R>(tx, ty, n));
+            R res[3] = {R(0), R(0), R(0)};
+            R tw = R(0);
+            for (int r = 0; r < Rn; ++r) {
+                const float* dd = dirs + 4 * r;
+                const float* ry = rays + (size_t(probe - p0) * Rn + r) * 4;
+                V3<R> rd{R(dd[0]), R(dd[1]), R(dd[2])};
+                R cosv = std::max(R(0), dot(td, rd));
+                if (depth) {
+                    R d = std::min(R(u.max_distance), R(ry[3]) - R(0.01f));
+                    if (d == R(-1)) d = R(u.max_distance);
+                    R w = std::pow(cosv, R(u.sharpness));
+                    if (w >= FLT_EPS) {
+                        res[0] = res[0] + d * w;
+                        res[1] = res[1] + (d * d) * w;
+                        tw = tw + w;
+                    }
+                } else {
+                    R w = cosv;
+                    if (w >= FLT_EPS) {
+                        res[0] = res[0] + R(ry[0]) * w;
+                        res[1] = res[1] + R(ry[1]) * w;
+                        res[2] = res[2] + R(ry[2]) * w;
+                        tw = tw + w;
+                    }
+                }
+            }
+            if (tw > FLT_EPS) {
+                R s = R(1) / (R(2) * tw);
+                for (int k = 0; k < 3; ++k) res[k] = res[k] * s;
+            }
+            if (!depth) {
+                R ig = R(1) / R(u.ddgi_gamma);
+                for (int k = 0; k < 3; ++k) res[k] = std::pow(res[k], ig);
+            }
+            const int x = cx * (n + 2) + tx + 2, y = cy * (n + 2) + ty + 2;
+            const size_t ti = (size_t(y) * size_t(W) + size_t(x)) * size_t(nc);
+            R h = R(u.hysteresis);
+            int nch = depth ? 2 : 3;
+            for (int k = 0; k < nch; ++k) {
+                R v = res[k];
+                if (!first) v = mixr(v, R(prev[ti + size_t(k)]), h);
+                float f = float(v);
+                if (vd->storage == LUXGI_STORAGE_FP16) f = round_half(f);
+                out[ti + size_t(k)] = f;
+            }
+            if (!depth) out[ti + 3] = 1.0f;
+        }
+    }
+}
+
+// BorderUpdate.glsl:136-156 for side n, generalised from its 36/68-entry
+// offset tables: (dst, src) pairs relative to the cell origin.
+int border_pairs(int n, int (*pairs)[4]) {
+    int k = 0;
+    for (int x = 1; x <= n; ++x) { pairs[k][0] = x; pairs[k][1] = 0; pairs[k][2] = n + 1 - x; pairs[k][3] = 1; ++k; }
+    for (int x = 1; x <= n; ++x) { pairs[k][0] = x; pairs[k][1] = n + 1; pairs[k][2] = n + 1 - x; pairs[k][3] = n; ++k; }
+    for (int y = 1; y <= n; ++y) { pairs[k][0] = 0; pairs[k][1] = y; pairs[k][2] = 1; pairs[k][3] = n + 1 - y; ++k; }
+    for (int y = 1; y <= n; ++y) { pairs[k][0] = n + 1; pairs[k][1] = y; pairs[k][2] = n; pairs[k][3] = n + 1 - y; ++k; }
+    int corners[4][4] = {{0, 0, n, n}, {n + 1, 0, 1, n}, {0, n + 1, n, 1}, {n + 1, n + 1, 1, 1}};
+    for (auto& c : corners) { for (int q = 0; q < 4; ++q) pairs[k][q] = c[q]; ++k; }
+    return k;
+}
+
+void border_atlas(float* atlas, int W, int nc, int n, int cells_x, int cells_y) {
+    std::vector<int> buf(size_t(4 * (4 * n + 4)));
+    int (*pairs)[4] = reinterpret_cast<int (*)[4]>(buf.data());
+    int np = border_pairs(n, pairs);
+#pragma omp parallel for
+    for (int cy = 0; cy < cells_y; ++cy) {
+        for (int cx = 0; cx < cells_x; ++cx) {
+            int ox = cx * (n + 2) + 1, oy = cy * (n + 2) + 1;
+            for (int i = 0; i < np; ++i) {
+                size_t dst = (size_t(oy + pairs[i][1]) * size_t(W) + size_t(ox + pairs[i][0])) * size_t(nc);
+                size_t src = (size_t(oy + pairs[i][3]) * size_t(W) + size_t(ox + pairs[i][2])) * size_t(nc);
+                for (int c = 0; c < nc; ++c) atlas[dst + size_t(c)] = atlas[src + size_t(c)];
+            }
+        }
+    }
+}
+
+// GlobalSDFMipmap.comp sampleSDF/main (GlobalSDFMipmap.comp:190-225) and
+// combineDistanceToSDF (SDFCommon.glsl:18-36).
+inline float combine(float sdf, float dist) {
+    if (sdf <= 0.0f && dist <= 0.0f) return sdf;
+    float m = std::max(sdf, 0.0f);
+    return std::sqrt(m * m + dist * dist);
+}
+
+void mip_pass(const std::vector<float>& src, int src_w, int src_res, int src_off_x, std::vector<float>& dst, int dst_w,
+              int dst_off_x, int mres, int coord_scale, float max_dist, bool fp16) {
+    static const int off[7][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
+#pragma omp parallel for
+    for (int z = 0; z < mres; ++z)
+        for (int y = 0; y < mres; ++y)
+            for (int x = 0; x < mres; ++x) {
+                float mn = 0.0f;
+                for (int i = 0; i < 7; ++i) {
+                    int c[3] = {x * coord_scale + off[i][0], y * coord_scale + off[i][1], z * coord_scale + off[i][2]};
+                    for (int k = 0; k < 3; ++k) c[k] = std::min(std::max(c[k], 0), src_res - 1);
+                    c[0] += src_off_x;
+                    float v = src[size_t(c[0]) + size_t(src_w) * (size_t(c[1]) + size_t(src_res) * size_t(c[2]))];
+                    float len = std::sqrt(float(off[i][0] * off[i][0] + off[i][1] * off[i][1] + off[i][2] * off[i][2]));
+                    float dv = len * (max_dist / float(src_res));
+                    float r = combine(v, dv);
+                    mn = (i == 0) ? r : std::min(mn, r);
+                }
+                if (fp16) mn = round_half(mn);
+                dst[size_t(x + dst_off_x) + size_t(dst_w) * (size_t(y) + size_t(mres) * size_t(z))] = mn;
+            }
+}
+
+}  // namespace
+
+// ===================================================================== C API
+extern "C" {
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+// Rotated Fibonacci directions, float4 [R] (w = 0); storage rounding as the
+// blend sees them when fp16_round != 0.
+int oracle_ray_dirs(const float rot[9], int nrays, int precision, int fp16_round, float* out) {
+    for (int r = 0; r < nrays; ++r) {
+        float v[3];
+        if (precision == 1) {
+            V3<double> d = ray_direction<double>(rot, r, nrays);
+            v[0] = float(d.x); v[1] = float(d.y); v[2] = float(d.z);
+        } else {
+            V3<float> d = ray_direction<float>(rot, r, nrays);
+            v[0] = d.x; v[1] = d.y; v[2] = d.z;
+        }
+        for (int k = 0; k < 3; ++k) out[4 * r + k] = fp16_round ? round_half(v[k]) : v[k];
+        out[4 * r + 3] = 0.0f;
+    }
+    return 0;
+}
+
+// Rotation of glm::angleAxis(angle, axis) cast to a matrix (DDGIRenderer.cpp:
+// 267-272), column-major; the quaternion-to-matrix identity.
+int oracle_rotation(const float axis[3], float angle, float out[9]) {
+    double half = double(angle) * 0.5, s = std::sin(half);
+    double x = axis[0] * s, y = axis[1] * s, z = axis[2] * s, w = std::cos(half);
+    double m[9] = {1 - 2 * (y * y + z * z), 2 * (x * y + w * z), 2 * (x * z - w * y),
+                   2 * (x * y - w * z), 1 - 2 * (x * x + z * z), 2 * (y * z + w * x),
+                   2 * (x * z + w * y), 2 * (y * z - w * x), 1 - 2 * (x * x + y * y)};
+    for (int i = 0; i < 9; ++i) out[i] = float(m[i]);
+    return 0;
+}
+
+// Trace probes [p0, p1): out float4 [P][R] (rgb, distance), info int4 [P][R]
+// (steps, cascade, full-resolution samples, 0) or NULL.  sdf/surface descriptors hold HOST pointers;
+// prev_irr / prev_dist are float atlases (mode B when frames > 0).
+int oracle_trace(const luxgi_ddgi_volume_desc* vd, const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf,
+                 const float* prev_irr, const float* prev_dist, int frames, const float rot[9], int precision,
+                 int p0, int p1, float* out, int32_t* info) {
+    const luxgi_ddgi_uniform& u = vd->uniform;
+    TraceCtx c;
+    c.vd = vd; c.sdf = sdf; c.surf = surf;
+    const int res = sdf->resolution, mres = sdf->mip_resolution, C = int(sdf->data.cascades_count);
+    c.tex.W = res * C; c.tex.H = res; c.tex.D = res;
+    c.mip.W = mres * C; c.mip.H = mres; c.mip.D = mres;
+    if (sdf->format == LUXGI_STORAGE_FP16) {
+        c.tex.f16 = static_cast<const uint16_t*>(sdf->sdf);
+        c.mip.f16 = static_cast<const uint16_t*>(sdf->mip);
+    } else {
+        c.tex.f32 = static_cast<const float*>(sdf->sdf);
+        c.mip.f32 = static_cast<const float*>(sdf->mip);
+    }
+    const int ares = int(surf->data.resolution);
+    c.S.d = surf;
+    c.S.depth.f32 = surf->depth; c.S.depth.W = ares; c.S.depth.H = ares; c.S.depth.C = 1;
+    if (vd->light_mode == LUXGI_LIGHT_PER_HIT) {
+        c.S.c0.f16 = surf->direct_light;
+        c.S.c1.u8 = surf->albedo;
+        c.S.c1.W = ares; c.S.c1.H = ares; c.S.c1.C = 4;
+        c.S.two = true;
+    } else {
+        c.S.c0.f16 = static_cast<const uint16_t*>(surf->light_cache);
+    }
+    c.S.c0.W = ares; c.S.c0.H = ares; c.S.c0.C = 4;
+    c.prev.irr.f32 = prev_irr; c.prev.irr.W = u.irradiance_width; c.prev.irr.H = u.irradiance_height; c.prev.irr.C = 4;
+    c.prev.dist.f32 = prev_dist; c.prev.dist.W = u.depth_width; c.prev.dist.H = u.depth_height; c.prev.dist.C = 2;
+    c.bounce = vd->infinite_bounce && frames != 0 && prev_irr && prev_dist;
+    const int Rn = u.rays_per_probe;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int p = p0; p < p1; ++p) {
+        for (int r = 0; r < Rn; ++r) {
+            size_t i = size_t(p - p0) * Rn + r;
+            int32_t inf[4];
+            if (precision == 1) trace_one<double>(c, rot, p, r, out + 4 * i, inf);
+            else trace_one<float>(c, rot, p, r, out + 4 * i, inf);
+            if (info) for (int k = 0; k < 4; ++k) info[4 * i + k] = inf[k];
+        }
+    }
+    return 0;
+}
+
+// Irradiance + distance blend of probes [p0, p1) (ProbeUpdate.glsl; p1 <= 0
+// means all) followed by the border copy of every cell when `border` != 0.
+// rays holds probes [p0, p1).  Atlases are float arrays; prev may be NULL
+// when first != 0.
+int oracle_blend(const luxgi_ddgi_volume_desc* vd, const float* dirs, const float* rays, const float* prev_irr,
+                 const float* prev_dist, float* out_irr, float* out_dist, int first, int precision, int border,
+                 int p0, int p1) {
+    const luxgi_ddgi_uniform& u = vd->uniform;
+    const int P = u.probe_counts[0] * u.probe_counts[1] * u.probe_counts[2];
+    if (p1 <= 0 || p1 > P) p1 = P;
+    if (p0 < 0) p0 = 0;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int p = p0; p < p1; ++p) {
+        if (precision == 1) {
+            blend_probe<double>(vd, dirs, rays, prev_irr, out_irr, p, false, first != 0, p0);
+            blend_probe<double>(vd, dirs, rays, prev_dist, out_dist, p, true, first != 0, p0);
+        } else {
+            blend_probe<float>(vd, dirs, rays, prev_irr, out_irr, p, false, first != 0, p0);
+            blend_probe<float>(vd, dirs, rays, prev_dist, out_dist, p, true, first != 0, p0);
+        }
+    }
+    if (border) {
+        const int XY = u.probe_counts[0] * u.probe_counts[1], Z = u.probe_counts[2];
+        border_atlas(out_irr, u.irradiance_width, 4, u.irradiance_probe_side, XY, Z);
+        border_atlas(out_dist, u.depth_width, 2, u.depth_probe_side, XY, Z);
+    }
+    return 0;
+}
+
+int oracle_border(const luxgi_ddgi_uniform* u, float* irr, float* dist) {
+    const int XY = u->probe_counts[0] * u->probe_counts[1], Z = u->probe_counts[2];
+    if (irr) border_atlas(irr, u->irradiance_width, 4, u->irradiance_probe_side, XY, Z);
+    if (dist) border_atlas(dist, u->depth_width, 2, u->depth_probe_side, XY, Z);
+    return 0;
+}
+
+// (dst, src) offset pairs of the border rule for side n: int4 [4n+4].
+int oracle_border_pairs(int n, int32_t* out) {
+    std::vector<int> buf(size_t(4 * (4 * n + 4)));
+    int (*pairs)[4] = reinterpret_cast<int (*)[4]>(buf.data());
+    int np = border_pairs(n, pairs);
+    for (int i = 0; i < np * 4; ++i) out[i] = buf[size_t(i)];
+    return np;
+}
+
+// SDF mip + 4 flood passes for every cascade.  sdf_f32: the SDF as float
+// values (FP16 SDFs converted by the caller); mip_out float [(mres*C)*mres^3].
+int oracle_build_mip(const luxgi_sdf_desc* sdf, const float* sdf_f32, float* mip_out) {
+    const int res = sdf->resolution, mres = sdf->mip_resolution, C = int(sdf->data.cascades_count);
+    const bool fp16 = sdf->format == LUXGI_STORAGE_FP16;
+    std::vector<float> src(sdf_f32, sdf_f32 + size_t(res) * C * res * res);
+    std::vector<float> mip(size_t(mres) * C * mres * mres, 0.0f), tmp(size_t(mres) * mres * mres, 0.0f);
+    for (int k = 0; k < C; ++k) {
+        float maxd = sdf->data.cascade_pos_distance[k][3] * 2.0f;
+        mip_pass(src, res * C, res, k * res, mip, mres * C, k * mres, mres, 4, maxd, fp16);
+        for (int i = 1; i < 5; ++i) {
+            if (i & 1) mip_pass(mip, mres * C, mres, k * mres, tmp, mres, 0, mres, 1, maxd, fp16);
+            else mip_pass(tmp, mres, mres, 0, mip, mres * C, k * mres, mres, 1, maxd, fp16);
+        }
+    }
+    std::memcpy(mip_out, mip.data(), mip.size() * sizeof(float));
+    return 0;
+}
+
+// SDFCulling.comp (SDFCulling.comp:36-101) with a deterministic layout:
+// chunks in flattened order at prefix-sum offsets starting at word 1, each
+// list = [count, ids ascending]; [0] = words the full layout needs.  Chunks
+// whose list would pass `capacity` stay empty (entry 0) and the call
+// reports LUXGI_ENOMEM.
+int oracle_cull(const luxgi_surface_desc* s, uint32_t* chunks, uint32_t* culled, uint32_t capacity) {
+    const int N = 40;
+    std::memset(chunks, 0, sizeof(uint32_t) * N * N * N);
+    uint32_t used = 1;
+    for (int z = 0; z < N; ++z)
+        for (int y = 0; y < N; ++y)
+            for (int x = 0; x < N; ++x) {
+                float cs = s->data.chunk_size;
+                float mn[3] = {(float(x) - N * 0.5f) * cs, (float(y) - N * 0.5f) * cs, (float(z) - N * 0.5f) * cs};
+                float mx[3] = {mn[0] + cs, mn[1] + cs, mn[2] + cs};
+                std::vector<uint32_t> ids;
+                for (uint32_t o = 0; o < s->data.objects_count; ++o) {
+                    const float* b = s->objects[o].object_bounds;
+                    float cc[3], d2[3];
+                    for (int k = 0; k < 3; ++k) { cc[k] = std::min(std::max(b[k], mn[k]), mx[k]); d2[k] = b[k] - cc[k]; }
+                    float dist = std::sqrt(d2[0] * d2[0] + d2[1] * d2[1] + d2[2] * d2[2]);
+                    if (dist <= b[3]) ids.push_back(o);
+                }
+                if (ids.empty()) continue;
+                uint32_t need = uint32_t(ids.size()) + 1;
+                uint32_t st = used;
+                used += need;
+                if (st + need > capacity) continue;
+                culled[st] = uint32_t(ids.size());
+                for (size_t i = 0; i < ids.size(); ++i) culled[st + 1 + i] = ids[i];
+                chunks[z * N * N + y * N + x] = st;
+            }
+    if (capacity > 0) culled[0] = used;
+    return used > capacity ? LUXGI_ENOMEM : 0;
+}
+
+// SDFAtlasIndirectLight.frag:44-67 over every texel of every tile rect;
+// light_out RGBA16F [res^2] (starts as a copy of direct_light).
+int oracle_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* s, const float* irr, const float* dist,
+                  int frames, int precision, uint16_t* light_out) {
+    const int res = int(s->data.resolution);
+    std::memcpy(light_out, s->direct_light, size_t(res) * res * 4 * sizeof(uint16_t));
+    if (!vd->infinite_bounce || frames == 0) return 0;
+    Atlases A;
+    const luxgi_ddgi_uniform& u = vd->uniform;
+    A.irr.f32 = irr; A.irr.W = u.irradiance_width; A.irr.H = u.irradiance_height; A.irr.C = 4;
+    A.dist.f32 = dist; A.dist.W = u.depth_width; A.dist.H = u.depth_height; A.dist.C = 2;
+    for (int t = 1; t < s->num_tiles; ++t) {
+        const luxgi_surface_tile& tl = s->tiles[t];
+        int x0 = int(std::lround(tl.extends[0] * res)), y0 = int(std::lround(tl.extends[1] * res));
+        int w = int(std::lround(tl.extends[2] * res)), h = int(std::lround(tl.extends[3] * res));
+#pragma omp parallel for
+        for (int j = 0; j < h; ++j)
+            for (int i = 0; i < w; ++i) {
+                size_t ti = size_t(y0 + j) * size_t(res) + size_t(x0 + i);
+                const float* g0 = s->gbuffer0 + ti * 4;
+                const float* g1 = s->gbuffer1 + ti * 4;
+                float add[3];
+                if (precision == 1) {
+                    using R = double;
+                    // octohedralToDirection (Math.glsl:27-33)
+                    V3<R> v{R(g1[0]), R(g1[1]), R(1) - std::fabs(R(g1[0])) - std::fabs(R(g1[1]))};
+                    if (v.z < R(0)) {
+                        R nx = (R(1) - std::fabs(v.y)) * (v.x >= R(0) ? R(1) : R(-1));
+                        R ny = (R(1) - std::fabs(v.x)) * (v.y >= R(0) ? R(1) : R(-1));
+                        v.x = nx; v.y = ny;
+                    }
+                    V3<R> n = normalize(v);
+                    V3<R> wp{R(g0[3]), R(g1[2]), R(g1[3])};
+                    V3<R> cam{R(s->data.camera_pos[0]), R(s->data.camera_pos[1]), R(s->data.camera_pos[2])};
+                    V3<R> wo = normalize(sub(cam, wp));
+                    V3<R> e = sample_irradiance<R>(u, A, wp, n, wo);
+                    for (int k = 0; k < 3; ++k) {
+                        R alb = std::min(R(g0[k]), R(0.9f));
+                        R diff = (alb - alb * R(0)) / pi_r<R>();
+                        add[k] = float(R(vd->intensity) * diff * (k == 0 ? e.x : k == 1 ? e.y : e.z));
+                    }
+                } else {
+                    using R = float;
+                    V3<R> v{g1[0], g1[1], 1.0f - std::fabs(g1[0]) - std::fabs(g1[1])};
+                    if (v.z < 0.0f) {
+                        R nx = (1.0f - std::fabs(v.y)) * (v.x >= 0.0f ? 1.0f : -1.0f);
+                        R ny = (1.0f - std::fabs(v.x)) * (v.y >= 0.0f ? 1.0f : -1.0f);
+                        v.x = nx; v.y = ny;
+                    }
+                    V3<R> n = normalize(v);
+                    V3<R> wp{g0[3], g1[2], g1[3]};
+                    V3<R> cam{s->data.camera_pos[0], s->data.camera_pos[1], s->data.camera_pos[2]};
+                    V3<R> wo = normalize(sub(cam, wp));
+                    V3<R> e = sample_irradiance<R>(u, A, wp, n, wo);
+                    for (int k = 0; k < 3; ++k) {
+                        R alb = std::min(g0[k], 0.9f);
+                        R diff = (alb - alb * 0.0f) / pi_r<R>();
+                        add[k] = vd->intensity * diff * (k == 0 ? e.x : k == 1 ? e.y : e.z);
+                    }
+                }
+                for (int k = 0; k < 3; ++k) {
+                    float base = h2f(s->direct_light[ti * 4 + size_t(k)]);
+                    float v = base + add[k];
+                    _Float16 hv = _Float16(v);
+                    std::memcpy(&light_out[ti * 4 + size_t(k)], &hv, 2);
+                }
+            }
+    }
+    return 0;
+}
+
+// sampleIrradiance for n points (float3 arrays), float atlases.
+int oracle_sample_irradiance(const luxgi_ddgi_uniform* u, const float* irr, const float* dist, const float* pos,
+                             const float* nrm, const float* wo, float* out, int n, int precision) {
+    Atlases A;
+    A.irr.f32 = irr; A.irr.W = u->irradiance_width; A.irr.H = u->irradiance_height; A.irr.C = 4;
+    A.dist.f32 = dist; A.dist.W = u->depth_width; A.dist.H = u->depth_height; A.dist.C = 2;
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        if (precision == 1) {
+            V3<double> e = sample_irradiance<double>(*u, A, V3<double>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]},
+                                                     V3<double>{nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]},
+                                                     V3<double>{wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]});
+            out[3 * i] = float(e.x); out[3 * i + 1] = float(e.y); out[3 * i + 2] = float(e.z);
+        } else {
+            V3<float> e = sample_irradiance<float>(*u, A, V3<float>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]},
+                                                   V3<float>{nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]},
+                                                   V3<float>{wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]});
+            out[3 * i] = e.x; out[3 * i + 1] = e.y; out[3 * i + 2] = e.z;
+        }
+    }
+    return 0;
+}
+
+// Texel directions octDecode(normalizedOctCoord) for side n: float3 [n*n].
+int oracle_texel_dirs(int n, int precision, float* out) {
+    for (int ty = 0; ty < n; ++ty)
+        for (int tx = 0; tx < n; ++tx) {
+            int i = ty * n + tx;
+            if (precision == 1) {
+                V3<double> d = oct_decode(normalized_oct_coord<double>(tx, ty, n));
+                out[3 * i] = float(d.x); out[3 * i + 1] = float(d.y); out[3 * i + 2] = float(d.z);
+            } else {
+                V3<float> d = oct_decode(normalized_oct_coord<float>(tx, ty, n));
+                out[3 * i] = d.x; out[3 * i + 1] = d.y; out[3 * i + 2] = d.z;
+            }
+        }
+    return 0;
+}
+
+// octEncode for n float3 directions (test aid).
+int oracle_oct_encode(const float* dirs, int n, float* out) {
+    for (int i = 0; i < n; ++i) {
+        V2<double> o = oct_encode(V3<double>{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]});
+        out[2 * i] = float(o.x); out[2 * i + 1] = float(o.y);
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,295 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the CPU oracle
+on the same seeded inputs.
+
+Tolerances (stated per test):
+  - SDF mip, chunk culling, march steps / hit cascade / hit distance:
+    bit-exact against the FP32 oracle (the march is FP32 without FMA
+    contraction in both);
+  - FP32 blend: 1e-5 relative to the FP32 oracle, 1e-4 to the FP64 oracle;
+  - FP16 storage: 2 half-ulps (1e-3 relative);
+  - hit distance vs FP64: 1e-3 voxel except branch-flipped rays (< 1%).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from luxgi_gb300 import _native as N
+from luxgi_gb300.ddgi import DDGIVolume, frame_rotation
+from luxgi_gb300.scene import PLAIN_SMALL, PLAIN_SMALL_REF, DeviceScene, HostScene
+from tests._helpers import rel_err, tiny_workload
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    import torch
+
+    t = t.detach().cpu()
+    if t.dtype == torch.float16:
+        t = t.float()
+    return t.numpy()
+
+
+def setup(w, debug=True):
+    host = HostScene(w.scene)
+    dev = DeviceScene(host, w.volume.light_mode)
+    vol = DDGIVolume(w.volume)
+    vol.bind_scene(dev)
+    if debug:
+        vol.set_debug_rays(True)
+    mip = dev.mip.cpu().numpy()
+    if host.sdf_format == N.STORAGE_FP16:
+        mip = mip.view(np.uint16)
+    inp = oracle.HostInputs(host, w.volume.light_mode, mip=mip, chunks=dev.chunks.cpu().numpy().view(np.uint32),
+                            culled=dev.culled.cpu().numpy().view(np.uint32))
+    return host, dev, vol, inp
+
+
+def sync():
+    import torch
+
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("fmt,cascades", [(N.STORAGE_FP32, 1), (N.STORAGE_FP16, 1), (N.STORAGE_FP32, 2)])
+def test_sdf_mip_bit_exact(cuda, fmt, cascades):
+    w = tiny_workload(sdf=64, sdf_format=fmt, cascades=cascades)
+    host = HostScene(w.scene)
+    dev = DeviceScene(host, w.volume.light_mode)
+    sync()
+    ref = oracle.build_mip(oracle.HostInputs(host, w.volume.light_mode).sdf_desc, host.sdf_float())
+    got = dev.mip.cpu().numpy()
+    if fmt == N.STORAGE_FP16:
+        got = got.view(np.float16).astype(np.float32)
+    assert np.array_equal(got, ref)
+
+
+def test_surface_cull_bit_exact(cuda):
+    w = PLAIN_SMALL
+    host = HostScene(w.scene)
+    dev = DeviceScene(host, w.volume.light_mode)
+    sync()
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    chunks = dev.chunks.cpu().numpy().view(np.uint32)
+    culled = dev.culled.cpu().numpy().view(np.uint32)
+    assert np.array_equal(chunks, inp.chunks)
+    used = int(inp.culled[0])
+    assert culled[0] == used
+    assert np.array_equal(culled[:used], inp.culled[:used])
+
+
+def test_surface_cull_capacity_overflow(cuda):
+    import ctypes
+    import torch
+
+    w = tiny_workload(prims=10)
+    host = HostScene(w.scene)
+    dev = DeviceScene(host, w.volume.light_mode)
+    need = int(dev.culled[0].item())
+    small = torch.zeros(need // 2, dtype=torch.int32, device="cuda")
+    chunks = torch.zeros(40 ** 3, dtype=torch.int32, device="cuda")
+    st = N.ddgi().luxgi_surface_cull(ctypes.byref(dev.surface_desc), chunks.data_ptr(), small.data_ptr(), need // 2,
+                                     torch.cuda.current_stream().cuda_stream)
+    assert st == N.LUXGI_ENOMEM
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    ch, cu, ost = oracle.cull(inp.surface_desc, need // 2)
+    assert ost == N.LUXGI_ENOMEM
+    assert np.array_equal(chunks.cpu().numpy().view(np.uint32), ch)
+
+
+def _check_trace(vol, inp, vd, rot, frames=0, prev=None):
+    dirs, rad, info = vol.rays()
+    sync()
+    rad, info = _np(rad), info.cpu().numpy()
+    pi, pd = (None, None) if prev is None else prev
+    ref, rinfo = oracle.trace(vd, inp, rot, frames, pi, pd, precision=0)
+    assert np.array_equal(info, rinfo), np.argwhere(info != rinfo)[:5]
+    assert np.array_equal(rad[..., 3], ref[..., 3])
+    np.testing.assert_allclose(rad[..., :3], ref[..., :3], rtol=2e-5, atol=2e-6)
+    np.testing.assert_array_equal(_np(dirs), oracle.ray_dirs(rot, vd.uniform.rays_per_probe, 0))
+    return rad, ref
+
+
+@pytest.mark.parametrize("light", [N.LIGHT_PER_HIT, N.LIGHT_CACHE])
+def test_trace_bit_exact_plain_small(cuda, light):
+    from dataclasses import replace
+
+    w = replace(PLAIN_SMALL, volume=replace(PLAIN_SMALL.volume, light_mode=light))
+    host, dev, vol, inp = setup(w)
+    rot = frame_rotation(21, 0)
+    vol.trace(rot)
+    _check_trace(vol, inp, vol.desc, rot)
+
+
+def test_trace_hit_distance_vs_fp64(cuda):
+    w = PLAIN_SMALL
+    host, dev, vol, inp = setup(w)
+    rot = frame_rotation(22, 0)
+    vol.trace(rot)
+    _, rad, info = vol.rays()
+    sync()
+    rad = _np(rad)
+    ref, _ = oracle.trace(vol.desc, inp, rot, precision=1)
+    voxel = host.sdf_data.cascade_voxel_size[0]
+    ok = np.abs(rad[..., 3] - ref[..., 3]) <= 1e-3 * voxel
+    assert ok.mean() > 0.99, f"flip fraction {1 - ok.mean():.4f}"
+
+
+def test_blend_matches_oracle_fp32_and_fp64(cuda):
+    w = PLAIN_SMALL
+    host, dev, vol, inp = setup(w, debug=False)
+    u = vol.uniform
+    rot = frame_rotation(23, 0)
+    vol.trace(rot)
+    vol.probe_update()
+    vol.end_frame()
+    irr, dist = vol.atlases()
+    _, rad, _ = vol.rays()
+    sync()
+    rays = _np(rad)
+    dirs = oracle.ray_dirs(rot, u.rays_per_probe, 0)
+    r32 = oracle.blend(vol.desc, dirs, rays, first=True, precision=0)
+    r64 = oracle.blend(vol.desc, oracle.ray_dirs(rot, u.rays_per_probe, 1), rays, first=True, precision=1)
+    gi, gd = _np(irr), _np(dist)
+    assert rel_err(gi, r32[0]) < 1e-5
+    assert rel_err(gd, r32[1]) < 1e-5
+    assert rel_err(gi, r64[0]) < 1e-4
+    assert rel_err(gd, r64[1]) < 1e-4
+
+
+def test_border_standalone_equals_fused(cuda):
+    w = PLAIN_SMALL
+    host, dev, vol, inp = setup(w, debug=False)
+    rot = frame_rotation(24, 0)
+    vol.trace(rot)
+    vol.probe_update()
+    vol.end_frame()
+    irr, dist = vol.atlases()
+    a, b = irr.clone(), dist.clone()
+    # zero the border of the last written copy, then rebuild it in place
+    u = vol.uniform
+    for t, n in ((irr, u.irradiance_probe_side), (dist, u.depth_probe_side)):
+        H, W = t.shape[:2]
+        for y in range(1, H - 1, n + 2):
+            t[y, :] = 0
+            t[y + n + 1, :] = 0
+        for x in range(1, W - 1, n + 2):
+            t[:, x] = 0
+            t[:, x + n + 1] = 0
+    # border_update works on the write copy (1 - pingPong): step back a frame
+    N.ddgi().luxgi_ddgi_end_frame(vol.handle)
+    vol.border_update()
+    sync()
+    irr2, dist2 = vol.atlases("prev")
+    assert np.array_equal(_np(irr2), _np(a))
+    assert np.array_equal(_np(dist2), _np(b))
+
+
+def test_multi_frame_per_hit_bounce(cuda):
+    """Eight frames with infinite bounce from the previous frame's atlases."""
+    w = PLAIN_SMALL
+    host, dev, vol, inp = setup(w, debug=False)
+    rots = [frame_rotation(25, f) for f in range(w.frames)]
+    for r in rots:
+        vol.update(r)
+    irr, dist = vol.atlases()
+    sync()
+    oi, od, frames, _ = oracle.run_frames(vol.desc, inp, rots, precision=0)
+    assert frames == w.frames == vol.frames
+    assert rel_err(_np(irr), oi) < 1e-4
+    assert rel_err(_np(dist), od) < 1e-4
+    oi64, od64, _, _ = oracle.run_frames(vol.desc, inp, rots, precision=1)
+    assert rel_err(_np(irr), oi64) < 1e-4
+    assert rel_err(_np(dist), od64) < 1e-4
+
+
+def test_reference_parity_mode_fp16_light_cache(cuda):
+    """8/16 sides, 250 steps, FP16 storage, light-cache bounce injected
+    every 2 frames (the reference's own configuration of the path)."""
+    w = PLAIN_SMALL_REF
+    host, dev, vol, inp = setup(w, debug=False)
+    rots = [frame_rotation(26, f) for f in range(5)]
+    for f, r in enumerate(rots):
+        if f > 0 and f % 2 == 0:
+            vol.inject_indirect()
+        vol.update(r)
+    irr, dist = vol.atlases()
+    light = dev.light_cache.cpu().numpy().view(np.uint16)
+    sync()
+    oi, od, _, _ = oracle.run_frames(vol.desc, inp, rots, precision=0, inject_every=2)
+    assert rel_err(_np(irr), oi) < 2e-3
+    assert rel_err(_np(dist), od) < 2e-3
+    lo = inp.light_cache.view(np.float16).astype(np.float32)
+    lg = light.view(np.float16).astype(np.float32)
+    assert rel_err(lg, lo, floor=1e-2) < 2e-3
+
+
+def test_sample_irradiance_matches_oracle(cuda):
+    import torch
+
+    w = PLAIN_SMALL
+    host, dev, vol, inp = setup(w, debug=False)
+    for f in range(3):
+        vol.update(frame_rotation(27, f))
+    irr, dist = vol.atlases()
+    rng = np.random.default_rng(5)
+    n = 4096
+    pos = rng.uniform(-4, 4, size=(n, 3)).astype(np.float32)
+    nrm = rng.normal(size=(n, 3)).astype(np.float32)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    wo = rng.normal(size=(n, 3)).astype(np.float32)
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    out = torch.zeros(n, 3, device="cuda")
+    vol.sample_irradiance(torch.from_numpy(pos).cuda(), torch.from_numpy(nrm).cuda(), torch.from_numpy(wo).cuda(), out)
+    sync()
+    ref = oracle.sample_irradiance(vol.uniform, _np(irr), _np(dist), pos, nrm, wo, precision=1)
+    assert rel_err(out.cpu().numpy(), ref, floor=1e-2) < 1e-4
+
+
+@pytest.mark.parametrize("kw", [
+    dict(probe_counts=(1, 1, 1), rays=1),
+    dict(probe_counts=(1, 1, 1), rays=33, irr=1, dist=2),
+    dict(probe_counts=(5, 1, 3), rays=17, irr=2, dist=3),
+    dict(probe_counts=(2, 3, 2), rays=64, cascades=2, sdf=32),
+    dict(probe_counts=(4, 2, 2), rays=40, sdf_format=N.STORAGE_FP16, storage=N.STORAGE_FP16),
+    dict(probe_counts=(3, 3, 3), rays=32, spacing=9.0),       # probes outside the room: misses
+])
+def test_edge_shapes(cuda, kw):
+    w = tiny_workload(**kw)
+    host, dev, vol, inp = setup(w)
+    rots = [frame_rotation(28, f) for f in range(3)]
+    prev = None
+    for f, r in enumerate(rots):
+        vol.trace(r)
+        _check_trace(vol, inp, vol.desc, r, f, prev)
+        vol.probe_update()
+        vol.end_frame()
+        irr, dist = vol.atlases()
+        sync()
+        prev = (_np(irr), _np(dist))
+    oi, od, _, _ = oracle.run_frames(vol.desc, inp, rots, precision=0)
+    tol = 2e-3 if w.volume.storage == N.STORAGE_FP16 else 1e-4
+    assert rel_err(prev[0], oi) < tol
+    assert rel_err(prev[1], od) < tol
+
+
+def test_runs_are_deterministic(cuda):
+    w = tiny_workload(probe_counts=(6, 3, 6), rays=96)
+    outs = []
+    for _ in range(2):
+        host, dev, vol, inp = setup(w, debug=False)
+        for f in range(3):
+            vol.update(frame_rotation(29, f))
+        irr, dist = vol.atlases()
+        outs.append((_np(irr), _np(dist)))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_unbound_volume_reports(cuda):
+    w = tiny_workload()
+    vol = DDGIVolume(w.volume)
+    with pytest.raises(N.LuxgiError) as e:
+        vol.trace(frame_rotation(1, 0))
+    assert e.value.status == N.LUXGI_ENOTBOUND
