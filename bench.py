@@ -215,6 +215,7 @@ def run_ours(args, rank: int, world: int):
     out_b = 8 if v.storage == N.STORAGE_FP16 else 16
     march_bytes = []
     steps_total = 0
+    fine_total = 0
     for f in range(W, W + K):
         vol.trace(rots[f])
         info = vol.rays()[2]
@@ -222,6 +223,7 @@ def run_ours(args, rank: int, world: int):
         fine = info[..., 2].to(torch.int64).sum().item()
         hits = (info[..., 1] >= 0).sum().item()
         steps_total += s
+        fine_total += fine
         march_bytes.append((s * 8 + fine * 8 + hits * 48) * esz + P * R * out_b)
     vol.set_debug_rays(False)
     torch.cuda.synchronize()
@@ -301,7 +303,8 @@ def run_ours(args, rank: int, world: int):
                 "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_source": pk["source"],
                 "traffic": traffic, "algorithmic_bytes_per_launch": int(avg_bytes),
-                "avg_launch_ms": round(avg_trace_ms, 4), "avg_march_steps_per_ray": round(steps_total / (K * P * R), 2)}
+                "avg_launch_ms": round(avg_trace_ms, 4), "avg_march_steps_per_ray": round(steps_total / (K * P * R), 2),
+                "avg_fine_samples_per_ray": round(fine_total / (K * P * R), 2)}
     if rank != 0:
         return
     cpu, err = (None, None)

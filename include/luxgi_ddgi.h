@@ -254,6 +254,10 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n,
 
 int luxgi_ddgi_get_atlases(const luxgi_ddgi_volume* vol, luxgi_ddgi_atlases* out);
 int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* vol, luxgi_ddgi_rays* out);
+/* Synchronise `stream` and read the volume's device status word: returns
+ * LUXGI_ETIMEOUT (and clears the word) when a bounded device-side wait of
+ * the tensor-core blend gave up since the last check, else LUXGI_OK. */
+int luxgi_ddgi_check_status(luxgi_ddgi_volume* vol, void* stream);
 /* Record per-ray march steps / hit cascade on the next traces (test aid). */
 int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* vol, int enable);
 /* Overwrite both atlas copies from host buffers of the volume's storage type

@@ -134,6 +134,7 @@ DDGI_API = [
     ("luxgi_ddgi_update_batch", c_int, [POINTER(c_void_p), c_int, POINTER(c_float), c_void_p]),
     ("luxgi_ddgi_get_atlases", c_int, [c_void_p, POINTER(Atlases)]),
     ("luxgi_ddgi_get_rays", c_int, [c_void_p, POINTER(Rays)]),
+    ("luxgi_ddgi_check_status", c_int, [c_void_p, c_void_p]),
     ("luxgi_ddgi_set_debug_rays", c_int, [c_void_p, c_int]),
     ("luxgi_ddgi_load_atlases", c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     ("luxgi_ddgi_inject_indirect", c_int, [c_void_p, c_void_p]),

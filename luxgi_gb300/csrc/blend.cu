@@ -234,28 +234,34 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(const BlendParams 
     }
 }
 
+// Probes per block: enough (texel, probe) pairs for every thread, at most
+// 32 probes (their ray chunk is 16 KB of shared memory).
+constexpr int kMaxProbesPerBlock = 32;
+
+template <int DEPTH, typename RT, typename AT>
+static cudaError_t launch_blend_kind(const BlendParams& p, int T, cudaStream_t st) {
+    const int cap = kBlendThreads * kPairsPerThread;
+    int PB = cap / T;
+    PB = PB < 1 ? 1 : (PB > kMaxProbesPerBlock ? kMaxProbesPerBlock : PB);
+    const size_t sm = sizeof(float) * kRayChunk * T + sizeof(float4) * PB * kRayChunk;
+    const unsigned blocks = unsigned((p.P + PB - 1) / PB);
+    if (sm > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(blend_kernel<DEPTH, RT, AT>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        if (e != cudaSuccess) return e;
+    }
+    blend_kernel<DEPTH, RT, AT><<<blocks, kBlendThreads, sm, st>>>(p, PB);
+    note_launch();
+    return cudaGetLastError();
+}
+
 template <typename RT, typename AT>
 static cudaError_t launch_blend_t(const BlendParams& p, cudaStream_t st) {
     const int Ti = p.u.irradiance_probe_side * p.u.irradiance_probe_side;
     const int Td = p.u.depth_probe_side * p.u.depth_probe_side;
-    const int cap = kBlendThreads * kPairsPerThread;
-    {
-        const int PB = cap / Ti > 0 ? cap / Ti : 1;
-        const size_t sm = sizeof(float) * kRayChunk * Ti + sizeof(float4) * PB * kRayChunk;
-        const unsigned blocks = unsigned((p.P + PB - 1) / PB);
-        if (sm > 48 * 1024) cudaFuncSetAttribute(blend_kernel<0, RT, AT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-        blend_kernel<0, RT, AT><<<blocks, kBlendThreads, sm, st>>>(p, PB);
-        note_launch();
-    }
-    {
-        const int PB = cap / Td > 0 ? cap / Td : 1;
-        const size_t sm = sizeof(float) * kRayChunk * Td + sizeof(float4) * PB * kRayChunk;
-        const unsigned blocks = unsigned((p.P + PB - 1) / PB);
-        if (sm > 48 * 1024) cudaFuncSetAttribute(blend_kernel<1, RT, AT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-        blend_kernel<1, RT, AT><<<blocks, kBlendThreads, sm, st>>>(p, PB);
-        note_launch();
-    }
-    return cudaGetLastError();
+    const cudaError_t e = launch_blend_kind<0, RT, AT>(p, Ti, st);
+    if (e != cudaSuccess) return e;
+    return launch_blend_kind<1, RT, AT>(p, Td, st);
 }
 
 cudaError_t launch_blend(const BlendParams& p, cudaStream_t st) {

@@ -1,11 +1,450 @@
-// Tensor-core (tcgen05) probe blend.  Placeholder until the kernel lands:
-// the volume reports LUXGI_EUNSUPPORTED for the tensor blend.
+// Tensor-core probe blend (tcgen05, sm_103a).
+//
+// The blend of ProbeUpdate.glsl is a contraction with a weight matrix shared
+// by every probe of a volume (see blend.cu):
+//     D[(p,c)][t] = sum_k A[(p,c)][k] * B[t][k]
+// A = per-ray data of 128 (probe, channel) rows, FP16, K-major:
+//     irradiance  rows (p, r|g|b|0), K = R rays
+//     distance    rows (p, d|d^2),   K = 2R: the value split hi + lo
+//                 (FP16 hi, FP16 residual) so the sums keep ~FP32 accuracy
+// B = weights W[t][r] in FP16, K-major, N = texels padded to 16; for the
+//     distance the same B block multiplies the hi and the lo half of A.
+// D accumulates in TMEM (FP32).  One CTA per SM, persistent over M tiles:
+//   warp 0      TMA producer (cp.async.bulk.tensor, 128B swizzle, 16 KB stages)
+//   warp 1      TMEM allocator + single-thread tcgen05.mma issuer
+//   warps 2..5  epilogue: tcgen05.ld, normalise, gamma, hysteresis, store
+//               with the border mirrors
+// The accumulator is double buffered in TMEM so the epilogue of one tile
+// overlaps the MMAs of the next.  Every mbarrier wait is bounded by a clock
+// budget; on expiry the kernel raises *status, stops issuing work, drains
+// what it issued and frees its TMEM.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
 #include "luxgi_internal.h"
 
 namespace luxgi {
 
-bool tc_blend_supported(const luxgi_ddgi_uniform&) { return false; }
+namespace {
 
-cudaError_t launch_tc_blend(const TcBlendParams&, cudaStream_t) { return cudaErrorNotSupported; }
+constexpr int kStages = 5;
+constexpr int kKBlock = 64;                 // halves per 128-byte swizzle row
+constexpr int kStageBytes = 128 * 128;      // 128 rows x 128 bytes
+constexpr int kThreads = 192;
+constexpr long long kWaitCycles = 4000000000LL;   // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false when the clock budget ran out or another role gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= uint64_t((addr & 0x3FFFF) >> 4);
+    d |= uint64_t(1) << 16;                 // leading byte offset (unused with 128B swizzle)
+    d |= uint64_t(1024 >> 4) << 32;         // stride byte offset
+    d |= uint64_t(1) << 46;                 // version
+    d |= uint64_t(2) << 61;                 // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor of kind::f16: D = F32, A = B = F16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | (0u << 7) | (0u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <typename AT> __device__ __forceinline__ float ld_atlas(const void* p, size_t i);
+template <> __device__ __forceinline__ float ld_atlas<float>(const void* p, size_t i) {
+    return static_cast<const float*>(p)[i];
+}
+template <> __device__ __forceinline__ float ld_atlas<__half>(const void* p, size_t i) {
+    return __half2float(static_cast<const __half*>(p)[i]);
+}
+template <typename AT> __device__ __forceinline__ void st_atlas(void* p, size_t i, float v);
+template <> __device__ __forceinline__ void st_atlas<float>(void* p, size_t i, float v) { static_cast<float*>(p)[i] = v; }
+template <> __device__ __forceinline__ void st_atlas<__half>(void* p, size_t i, float v) {
+    static_cast<__half*>(p)[i] = __float2half_rn(v);
+}
+
+struct TcArgs {
+    luxgi_ddgi_uniform u;
+    const float* norm;        // [N] tensor-core normalisers (1 / (2 sum w_fp16))
+    const void* prev;
+    void* out;
+    uint32_t* status;
+    int first, P, R, N, T, side, W, nc;   // nc: atlas channels (4 irradiance, 2 distance)
+    int rows_per_probe;                   // 4 irradiance, 2 distance
+    int kb_a;                             // K blocks of A per tile
+    int kb_b;                             // K blocks of B (ceil(R / 64))
+    int lo_offset;                        // column of the lo half in A (distance), 0 otherwise
+    int tiles;
+};
+
+// Writes one channel of interior texel (tx, ty) of cell (cx, cy) and its
+// border mirrors (BorderUpdate.glsl:136-156).
+template <typename AT>
+__device__ __forceinline__ void store_channel(void* atlas, int W, int nc, int n, int cx, int cy, int tx, int ty, int c,
+                                              float v) {
+    const int ox = cx * (n + 2) + 1, oy = cy * (n + 2) + 1;
+    const int X = tx + 1, Y = ty + 1;
+    auto put = [&](int x, int y) { st_atlas<AT>(atlas, (size_t(oy + y) * W + (ox + x)) * nc + c, v); };
+    put(X, Y);
+    if (Y == 1) put(n + 1 - X, 0);
+    if (Y == n) put(n + 1 - X, n + 1);
+    if (X == 1) put(0, n + 1 - Y);
+    if (X == n) put(n + 1, n + 1 - Y);
+    if (X == n && Y == n) put(0, 0);
+    if (X == 1 && Y == n) put(n + 1, 0);
+    if (X == n && Y == 1) put(0, n + 1);
+    if (X == 1 && Y == 1) put(n + 1, n + 1);
+}
+
+template <bool DIST, typename AT>
+__global__ void __launch_bounds__(kThreads, 1)
+tc_blend_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs g) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // 1024-byte aligned carve-out: B blocks, A stages, then barriers
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int b_block_bytes = g.N * 128;
+    uint8_t* smem_b = base;
+    uint8_t* smem_a = smem_b + g.kb_b * b_block_bytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_a + kStages * kStageBytes);
+    uint64_t* full = bars;                       // [kStages]
+    uint64_t* empty = bars + kStages;            // [kStages]
+    uint64_t* bfull = bars + 2 * kStages;        // [1]
+    uint64_t* tfull = bars + 2 * kStages + 1;    // [2]
+    uint64_t* tempty = bars + 2 * kStages + 3;   // [2]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 5);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t tmem_cols = (2 * g.N <= 32) ? 32 : (2 * g.N <= 64) ? 64 : (2 * g.N <= 128) ? 128 : (2 * g.N <= 256) ? 256 : 512;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(bfull, 1);
+        mbar_init(&tfull[0], 1);
+        mbar_init(&tfull[1], 1);
+        mbar_init(&tempty[0], 128);
+        mbar_init(&tempty[1], 128);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(tmem_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+    const uint32_t idesc = idesc_f16(128, g.N);
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            mbar_expect_tx(bfull, uint32_t(g.kb_b * b_block_bytes));
+            for (int kb = 0; kb < g.kb_b; ++kb) tma_load_2d(smem_b + kb * b_block_bytes, &map_b, bfull, kb * kKBlock, 0);
+            int stage = 0;
+            uint32_t phase = 0;
+            uint32_t pending[kStages];
+            for (int s = 0; s < kStages; ++s) pending[s] = 0xFFFFFFFFu;
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < g.tiles && ok; tile += gridDim.x) {
+                for (int kb = 0; kb < g.kb_a && ok; ++kb) {
+                    ok = mbar_wait(&empty[stage], phase ^ 1u, abort_flag);
+                    if (!ok) break;
+                    const int x = (kb < g.kb_b) ? kb * kKBlock : g.lo_offset + (kb - g.kb_b) * kKBlock;
+                    mbar_expect_tx(&full[stage], kStageBytes);
+                    tma_load_2d(smem_a + stage * kStageBytes, &map_a, &full[stage], x, tile * 128);
+                    pending[stage] = phase;
+                    if (++stage == kStages) { stage = 0; phase ^= 1u; }
+                }
+            }
+            if (!ok) {
+                // drain the loads this thread issued before giving up
+                for (int s = 0; s < kStages; ++s) {
+                    if (pending[s] == 0xFFFFFFFFu) continue;
+                    const long long t0 = clock64();
+                    while (!mbar_try_wait(&full[s], pending[s]) && clock64() - t0 < kWaitCycles) {}
+                }
+                const long long t0 = clock64();
+                while (!mbar_try_wait(bfull, 0) && clock64() - t0 < kWaitCycles) {}
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            bool ok = mbar_wait(bfull, 0, abort_flag);
+            int stage = 0;
+            uint32_t phase = 0;
+            int it = 0;
+            for (int tile = blockIdx.x; tile < g.tiles && ok; tile += gridDim.x, ++it) {
+                const int acc = it & 1;
+                const uint32_t use = uint32_t(it >> 1);
+                ok = mbar_wait(&tempty[acc], (use & 1u) ^ 1u, abort_flag);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t d_tmem = tmem_base + uint32_t(acc * g.N);
+                for (int kb = 0; kb < g.kb_a && ok; ++kb) {
+                    ok = mbar_wait(&full[stage], phase, abort_flag);
+                    if (!ok) break;
+                    tc_fence_after();
+                    const int bk = (kb < g.kb_b) ? kb : kb - g.kb_b;
+                    const uint32_t a_addr = smem_u32(smem_a + stage * kStageBytes);
+                    const uint32_t b_addr = smem_u32(smem_b + bk * b_block_bytes);
+#pragma unroll
+                    for (int k = 0; k < kKBlock / 16; ++k) {
+                        mma_f16(d_tmem, smem_desc(a_addr + k * 32), smem_desc(b_addr + k * 32), idesc,
+                                (kb > 0 || k > 0) ? 1u : 0u);
+                    }
+                    mma_commit(&empty[stage]);
+                    if (++stage == kStages) { stage = 0; phase ^= 1u; }
+                }
+                if (ok) mma_commit(&tfull[acc]);
+            }
+        }
+    } else {
+        // ------------------------------------------------ epilogue
+        const int q = warp & 3;                 // TMEM lane quadrant of this warp
+        const int row = q * 32 + lane;          // accumulator row = (probe, channel)
+        const luxgi_ddgi_uniform& u = g.u;
+        const int XY = u.probe_counts[0] * u.probe_counts[1];
+        const int n = g.side;
+        const float h = u.hysteresis;
+        const float ig = 1.0f / u.ddgi_gamma;
+        const int probes_per_tile = 128 / g.rows_per_probe;
+        int it = 0;
+        bool ok = true;
+        for (int tile = blockIdx.x; tile < g.tiles; tile += gridDim.x, ++it) {
+            const int acc = it & 1;
+            const uint32_t use = uint32_t(it >> 1);
+            ok = mbar_wait(&tfull[acc], use & 1u, abort_flag);
+            if (!ok) break;
+            tc_fence_after();
+            const int p = tile * probes_per_tile + row / g.rows_per_probe;
+            const int c = row % g.rows_per_probe;
+            const bool live = p < g.P && (DIST || c < 3);
+            const int cx = p % XY, cy = p / XY;
+            for (int c0 = 0; c0 < g.N; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * g.N + c0), v);
+                if (!live) continue;
+#pragma unroll 4
+                for (int j = 0; j < 16; ++j) {
+                    const int t = c0 + j;
+                    if (t >= g.T) break;
+                    const int tx = t % n, ty = t / n;
+                    float x = v[j] * __ldg(g.norm + t);
+                    if (!DIST) x = powf(x, ig);
+                    const size_t ti = (size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2)) * g.nc + c;
+                    if (!g.first) x = x * (1.0f - h) + ld_atlas<AT>(g.prev, ti) * h;
+                    store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, tx, ty, c, x);
+                }
+            }
+            if (!DIST && p < g.P && c == 3) {
+                // alpha = 1 (ProbeUpdate.glsl:279) for every texel of the cell
+                for (int t = 0; t < g.T; ++t) store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, t % n, t / n, 3, 1.0f);
+            }
+            tc_fence_before();
+            mbar_arrive(&tempty[acc]);
+        }
+        (void)ok;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(tmem_cols));
+    }
+    if (threadIdx.x == 0 && *abort_flag) atomicOr(g.status, 1u);
+}
+
+// ------------------------------------------------------------ host side
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+bool make_map(CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t rows, uint32_t box_inner, uint32_t box_rows) {
+    EncodeTiled fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {inner, rows};
+    cuuint64_t strides[1] = {inner * 2};
+    cuuint32_t box[2] = {box_inner, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <bool DIST, typename AT>
+cudaError_t launch_one(const TcBlendParams& p, cudaStream_t st) {
+    const luxgi_ddgi_uniform& u = p.u;
+    TcArgs g;
+    g.u = u;
+    g.first = p.first;
+    g.P = p.P;
+    g.R = p.R;
+    g.side = DIST ? u.depth_probe_side : u.irradiance_probe_side;
+    g.T = g.side * g.side;
+    g.N = DIST ? p.Nd : p.Ni;
+    g.W = DIST ? u.depth_width : u.irradiance_width;
+    g.nc = DIST ? 2 : 4;
+    g.rows_per_probe = DIST ? 2 : 4;
+    g.kb_b = (p.R + kKBlock - 1) / kKBlock;
+    g.kb_a = DIST ? 2 * g.kb_b : g.kb_b;
+    g.lo_offset = DIST ? p.R : 0;
+    g.norm = DIST ? p.n_dist : p.n_irr;
+    g.prev = DIST ? p.prev_dist : p.prev_irr;
+    g.out = DIST ? p.out_dist : p.out_irr;
+    g.status = p.status;
+    const int64_t rows = int64_t(p.P) * g.rows_per_probe;
+    g.tiles = int((rows + 127) / 128);
+    CUtensorMap ma, mb;
+    const uint64_t a_inner = DIST ? uint64_t(2) * p.R : uint64_t(p.R);
+    if (!make_map(&ma, DIST ? static_cast<const void*>(p.a_dist) : static_cast<const void*>(p.a_irr), a_inner,
+                  uint64_t(rows), kKBlock, 128))
+        return cudaErrorNotSupported;
+    if (!make_map(&mb, DIST ? static_cast<const void*>(p.w_dist) : static_cast<const void*>(p.w_irr), uint64_t(p.R),
+                  uint64_t(g.N), kKBlock, uint32_t(g.N)))
+        return cudaErrorNotSupported;
+    const size_t smem = 1024 + size_t(g.kb_b) * g.N * 128 + size_t(kStages) * kStageBytes + 256;
+    auto kern = tc_blend_kernel<DIST, AT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    const int grid = g.tiles < num_sms() ? g.tiles : num_sms();
+    kern<<<grid, kThreads, smem, st>>>(ma, mb, g);
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool tc_blend_supported(const luxgi_ddgi_uniform& u) {
+    const int R = u.rays_per_probe;
+    if (R % 16 != 0 || R < 16) return false;
+    const int ni = u.irradiance_probe_side * u.irradiance_probe_side;
+    const int nd = u.depth_probe_side * u.depth_probe_side;
+    const int Ni = (ni + 15) / 16 * 16, Nd = (nd + 15) / 16 * 16;
+    if (Ni > 256 || Nd > 256) return false;      // one UMMA N, one TMA box
+    const int kb = (R + kKBlock - 1) / kKBlock;
+    const size_t smem = 1024 + size_t(kb) * (Nd > Ni ? Nd : Ni) * 128 + size_t(kStages) * kStageBytes + 256;
+    return smem <= 227 * 1024 && encode_fn() != nullptr;
+}
+
+cudaError_t launch_tc_blend(const TcBlendParams& p, cudaStream_t st) {
+    if (p.P <= 0) return cudaSuccess;
+    if (!tc_blend_supported(p.u)) return cudaErrorNotSupported;
+    cudaError_t e;
+    if (p.storage == LUXGI_STORAGE_FP16) {
+        e = launch_one<false, __half>(p, st);
+        if (e == cudaSuccess) e = launch_one<true, __half>(p, st);
+    } else {
+        e = launch_one<false, float>(p, st);
+        if (e == cudaSuccess) e = launch_one<true, float>(p, st);
+    }
+    return e;
+}
 
 }  // namespace luxgi

@@ -432,6 +432,19 @@ int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* v, luxgi_ddgi_rays* out) {
     return LUXGI_OK;
 }
 
+int luxgi_ddgi_check_status(luxgi_ddgi_volume* v, void* stream) {
+    if (!v) return LUXGI_EINVAL;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint32_t word = 0;
+    cudaError_t e = cudaMemcpyAsync(&word, v->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (word == 0) return LUXGI_OK;
+    e = cudaMemsetAsync(v->status, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? LUXGI_ETIMEOUT : cuda_status(e);
+}
+
 int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* v, int enable) {
     if (!v) return LUXGI_EINVAL;
     if (enable && !v->info) {

@@ -49,12 +49,24 @@ __device__ __forceinline__ void fib_sincos(float x, float* s, float* c) {
     else { *s = -cp; *c = sp; }
 }
 
+// madfrac(i, PHI - 1) of sphericalFibonacci in compensated FP32: PHI - 1 as
+// a hi + lo pair and the product i * hi split exactly with one FMA, so the
+// azimuth keeps ~1e-7 rad at any ray index (plain FP32 loses ~2^-24 * i turns).
+__host__ __device__ __forceinline__ float fib_frac(float i) {
+    const float c_hi = 0.618034005165100098f;      // float(PHI - 1)
+    const float c_lo = -1.64152047e-8f;            // (PHI - 1) - c_hi
+    const float p = i * c_hi;
+    const float e = fmaf(i, c_hi, -p);             // exact low part of i * c_hi
+    float m = (p - floorf(p)) + (e + i * c_lo);
+    if (m >= 1.0f) m = m - 1.0f;
+    if (m < 0.0f) m = m + 1.0f;
+    return m;
+}
+
 // sphericalFibonacci (DDGICommon.glsl:42-52) rotated by mat3(rot), normalised.
 __device__ __forceinline__ f3 ray_direction(const float* rot, int r, int nrays) {
-    const float PHI = sqrtf(5.0f) * 0.5f + 0.5f;
     const float i = float(r);
-    const float t = i * (PHI - 1.0f);
-    const float mf = t - floorf(t);
+    const float mf = fib_frac(i);
     const float phi = (2.0f * kPi) * mf;
     const float cos_t = 1.0f - (2.0f * i + 1.0f) * (1.0f / float(nrays));
     const float sin_t = sqrtf(clampf(1.0f - cos_t * cos_t, 0.0f, 1.0f));

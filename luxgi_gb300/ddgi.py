@@ -82,6 +82,10 @@ class DDGIVolume:
                 "bind_scene")
         self.scene = scene
 
+    def check_status(self, stream=None) -> None:
+        """Raises LuxgiError(LUXGI_ETIMEOUT) if a bounded device wait gave up."""
+        N.check(N.ddgi().luxgi_ddgi_check_status(self._h, _stream(stream)), "check_status")
+
     def set_debug_rays(self, on: bool = True) -> None:
         N.check(N.ddgi().luxgi_ddgi_set_debug_rays(self._h, 1 if on else 0), "set_debug_rays")
 

@@ -157,6 +157,12 @@ def scaled(w: Workload, probe_counts=None, rays=None, sdf_resolution=None, atlas
     return replace(w, name=name or w.name + "_scaled", volume=v, scene=s)
 
 
+# The production scene with an eighth of the probes (16x8x16 at 3.8 m):
+# the case ncu captures are taken on (a few hundred MB on the device).
+PRODUCTION_PROFILE = scaled(PRODUCTION, probe_counts=(16, 8, 16), name="production_16x8x16_r256_sdf256")
+WORKLOADS[PRODUCTION_PROFILE.name] = PRODUCTION_PROFILE
+
+
 # --------------------------------------------------------------- host scene
 class HostScene:
     """Scene arrays on the host (numpy), copied out of libluxgi_scene."""

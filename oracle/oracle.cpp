@@ -133,11 +133,29 @@ template <> inline float pi_r<float>() { return 3.14159265f; }
 template <> inline double pi_r<double>() { return 3.14159265358979323846; }
 
 // ------------------------------------------------ DDGICommon.glsl
+// madfrac(i, PHI - 1) (DDGICommon.glsl:46-47).  FP64: direct.  FP32:
+// compensated -- PHI - 1 as a hi + lo float pair, the product i * hi split
+// exactly by one FMA -- so FP32 directions stay within ~1e-7 of FP64 at any
+// ray index (the plain FP32 product loses ~2^-24 * i turns).
+inline double fib_frac(double i) {
+    const double PHI = std::sqrt(5.0) * 0.5 + 0.5;
+    double t = i * (PHI - 1.0);
+    return t - std::floor(t);
+}
+inline float fib_frac(float i) {
+    const float c_hi = 0.618034005165100098f;
+    const float c_lo = -1.64152047e-8f;
+    const float p = i * c_hi;
+    const float e = std::fmaf(i, c_hi, -p);
+    float m = (p - std::floor(p)) + (e + i * c_lo);
+    if (m >= 1.0f) m = m - 1.0f;
+    if (m < 0.0f) m = m + 1.0f;
+    return m;
+}
+
 // sphericalFibonacci (DDGICommon.glsl:42-52)
 template <typename R> V3<R> spherical_fibonacci(R i, R n) {
-    const R PHI = std::sqrt(R(5)) * R(0.5) + R(0.5);
-    R t = i * (PHI - R(1));
-    R mf = t - std::floor(t);
+    R mf = fib_frac(i);
     R phi = (R(2) * pi_r<R>()) * mf;
     R cos_t = R(1) - (R(2) * i + R(1)) * (R(1) / n);
     R sin_t = std::sqrt(clampr(R(1) - cos_t * cos_t, R(0), R(1)));

@@ -293,3 +293,50 @@ def test_unbound_volume_reports(cuda):
     with pytest.raises(N.LuxgiError) as e:
         vol.trace(frame_rotation(1, 0))
     assert e.value.status == N.LUXGI_ENOTBOUND
+
+
+# ------------------------------------------------------------ tensor-core blend
+# Tolerance: 2e-3 relative to the FP64 oracle (FP16 operands, FP32
+# accumulation; the distance data split hi + lo).
+@pytest.mark.parametrize("sides,rays", [((6, 14), 256), ((8, 16), 128), ((6, 14), 288), ((8, 16), 64)])
+def test_tensor_blend_vs_fp64(cuda, sides, rays):
+    from dataclasses import replace
+
+    w = tiny_workload(probe_counts=(7, 3, 5), rays=rays, irr=sides[0], dist=sides[1], blend=N.BLEND_TENSOR)
+    host, dev, vol, inp = setup(w, debug=False)
+    u = vol.uniform
+    rots = [frame_rotation(31, f) for f in range(3)]
+    prev = None
+    for f, r in enumerate(rots):
+        vol.trace(r)
+        _, rad, _ = vol.rays()
+        sync()
+        rays_np = _np(rad)
+        vol.probe_update()
+        vol.end_frame()
+        vol.check_status()
+        irr, dist = vol.atlases()
+        sync()
+        pi, pd = (None, None) if prev is None else prev
+        ref = oracle.blend(vol.desc, oracle.ray_dirs(r, u.rays_per_probe, 1), rays_np, pi, pd, first=(f == 0),
+                           precision=1)
+        gi, gd = _np(irr), _np(dist)
+        assert rel_err(gi, ref[0]) < 2e-3
+        assert rel_err(gd, ref[1]) < 2e-3
+        prev = (gi, gd)
+
+
+def test_tensor_blend_matches_fp32_blend_on_plain_small(cuda):
+    from dataclasses import replace
+
+    outs = {}
+    for blend in (N.BLEND_FP32, N.BLEND_TENSOR):
+        w = replace(PLAIN_SMALL, volume=replace(PLAIN_SMALL.volume, blend=blend))
+        host, dev, vol, inp = setup(w, debug=False)
+        for f in range(4):
+            vol.update(frame_rotation(32, f))
+        vol.check_status()
+        irr, dist = vol.atlases()
+        outs[blend] = (_np(irr), _np(dist))
+    assert rel_err(outs[N.BLEND_TENSOR][0], outs[N.BLEND_FP32][0]) < 2e-3
+    assert rel_err(outs[N.BLEND_TENSOR][1], outs[N.BLEND_FP32][1]) < 2e-3
