@@ -5,13 +5,15 @@ OpenMP over probes) of LuxGI's non-raytracing DDGI probe update.  Only the
 tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg import it.
 
 Parity pins: the reference ships no tests, fixtures or golden data for
-this path.  The oracle is pinned by analytic known-answer tests (empty
-scene / constant sky, hysteresis closed form, octahedral round trips,
-Fibonacci determinism, probe inside a sphere) and by the border offset
-tables read out of the reference source (tests/golden/border_tables.json).
-The trace, surface-atlas and sampleIrradiance restatements are pinned only
-by those analytic cases: their parity with the reference is otherwise
-unpinned.
+this path.  The oracle is pinned three ways:
+  - against the reference's own code: its GLSL function libraries
+    (DDGICommon.glsl, SDFCommon.glsl, AtlasCommon.glsl, Math.glsl,
+    Random.glsl) compiled as C++ into oracle/_ref/libref.so by
+    oracle/build_ref.py (tests/test_reference_pin.py);
+  - by the border offset tables read out of the reference source
+    (tests/golden/border_tables.json);
+  - by analytic known-answer tests (empty scene / constant sky, hysteresis
+    closed form, octahedral round trips, Fibonacci, probe inside a sphere).
 """
 from __future__ import annotations
 
@@ -262,3 +264,100 @@ def run_frames(vdesc, inputs: HostInputs, rots, precision: int = 0, inject_every
         irr, dist = blend(vdesc, dirs, rays, irr, dist, first=(frames == 0), precision=precision)
         frames += 1
     return irr, dist, frames, rays
+
+
+# ------------------------------------------------------------------ reference
+# oracle/_ref/libref.so: the reference's own GLSL function libraries compiled
+# as C++ (oracle/build_ref.py); present only where the reference checkout is.
+_ref = None
+
+
+def ref_lib():
+    """The compiled reference library, or None when it cannot be built here."""
+    global _ref
+    if _ref is None:
+        from . import build_ref
+
+        path = build_ref.build()
+        if path is None or not Path(path).exists():
+            return None
+        L = ctypes.CDLL(str(path))
+        vp = c_void_p
+        sig = {
+            "ref_trace": (c_int, [vp, vp, vp, vp, vp, c_int, vp, c_int, c_int, vp, vp, vp]),
+            "ref_blend": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int]),
+            "ref_mip": (c_int, [vp, vp, vp]),
+            "ref_cull": (c_int, [vp, vp, vp, c_uint32]),
+            "ref_sample_irradiance": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int]),
+            "ref_ray_dirs": (c_int, [vp, c_int, vp]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _ref = L
+    return _ref
+
+
+def ref_ray_dirs(rot, nrays: int) -> np.ndarray:
+    rot = np.ascontiguousarray(rot, dtype=np.float32)
+    out = np.zeros((nrays, 4), dtype=np.float32)
+    ref_lib().ref_ray_dirs(_p(rot), nrays, _p(out))
+    return out
+
+
+def ref_trace(vdesc, inputs: HostInputs, rot, frames: int = 0, prev_irr=None, prev_dist=None,
+              probes: tuple | None = None, dirs: np.ndarray | None = None):
+    """GISDFRays.comp through the reference's compiled functions; `dirs`
+    (float4 [R]) overrides the ray directions."""
+    u = vdesc.uniform
+    dd = None if dirs is None else np.ascontiguousarray(dirs, dtype=np.float32)
+    P = u.probe_counts[0] * u.probe_counts[1] * u.probe_counts[2]
+    p0, p1 = probes if probes is not None else (0, P)
+    R = u.rays_per_probe
+    out = np.zeros((p1 - p0, R, 4), dtype=np.float32)
+    info = np.zeros((p1 - p0, R, 2), dtype=np.int32)
+    rot = np.ascontiguousarray(rot, dtype=np.float32)
+    pi = None if prev_irr is None else np.ascontiguousarray(prev_irr, dtype=np.float32)
+    pd = None if prev_dist is None else np.ascontiguousarray(prev_dist, dtype=np.float32)
+    ref_lib().ref_trace(ctypes.byref(vdesc), ctypes.byref(inputs.sdf_desc), ctypes.byref(inputs.surface_desc), _p(pi),
+                        _p(pd), frames, _p(rot), p0, p1, _p(out), _p(info), _p(dd))
+    return out, info
+
+
+def ref_blend(vdesc, dirs, rays, prev_irr=None, prev_dist=None, first: bool = True):
+    u = vdesc.uniform
+    irr = np.zeros((u.irradiance_height, u.irradiance_width, 4), dtype=np.float32)
+    dist = np.zeros((u.depth_height, u.depth_width, 2), dtype=np.float32)
+    d = np.ascontiguousarray(dirs, dtype=np.float32)
+    r = np.ascontiguousarray(rays, dtype=np.float32)
+    pi = None if prev_irr is None else np.ascontiguousarray(prev_irr, dtype=np.float32)
+    pd = None if prev_dist is None else np.ascontiguousarray(prev_dist, dtype=np.float32)
+    ref_lib().ref_blend(ctypes.byref(vdesc), _p(d), _p(r), _p(pi), _p(pd), _p(irr), _p(dist), 1 if first else 0)
+    return irr, dist
+
+
+def ref_mip(sdf_desc, sdf_float: np.ndarray) -> np.ndarray:
+    s = np.ascontiguousarray(sdf_float, dtype=np.float32)
+    m, C = sdf_desc.mip_resolution, sdf_desc.data.cascades_count
+    out = np.zeros(m * C * m * m, dtype=np.float32)
+    ref_lib().ref_mip(ctypes.byref(sdf_desc), _p(s), _p(out))
+    return out
+
+
+def ref_cull(surface_desc, capacity: int):
+    chunks = np.zeros(40 ** 3, dtype=np.uint32)
+    culled = np.zeros(capacity, dtype=np.uint32)
+    st = ref_lib().ref_cull(ctypes.byref(surface_desc), _p(chunks), _p(culled), capacity)
+    return chunks, culled, st
+
+
+def ref_sample_irradiance(uniform, irr, dist, pos, nrm, wo) -> np.ndarray:
+    i = np.ascontiguousarray(irr, dtype=np.float32)
+    d = np.ascontiguousarray(dist, dtype=np.float32)
+    p = np.ascontiguousarray(pos, dtype=np.float32)
+    n = np.ascontiguousarray(nrm, dtype=np.float32)
+    w = np.ascontiguousarray(wo, dtype=np.float32)
+    out = np.zeros_like(p)
+    ref_lib().ref_sample_irradiance(ctypes.byref(uniform), _p(i), _p(d), _p(p), _p(n), _p(w), _p(out), p.shape[0])
+    return out

@@ -16,6 +16,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 typedef unsigned int uint;
 
@@ -37,19 +38,29 @@ inline float f_log(float x) { return __builtin_logf(x); }
 
 template <typename T, int N> struct gvec;
 
-// Swizzle proxy over the parent's storage (union member of gvec).
+// Swizzle proxy over the parent's storage (union member of gvec).  Member
+// bodies are instantiated on use, after gvec is complete.
 template <typename T, int N, int... I> struct Swz {
     T e[N];
     static constexpr int L = sizeof...(I);
-    inline operator gvec<T, L>() const;
-    inline Swz& operator=(const gvec<T, L>& v);
-    inline Swz& operator=(const Swz& o);
-    inline Swz& operator+=(const gvec<T, L>& v);
-    inline Swz& operator-=(const gvec<T, L>& v);
-    inline Swz& operator*=(const gvec<T, L>& v);
-    inline Swz& operator/=(const gvec<T, L>& v);
-    inline Swz& operator*=(T s);
-    inline Swz& operator/=(T s);
+    operator gvec<T, L>() const {
+        gvec<T, L> v;
+        int k = 0;
+        ((v.e[k++] = e[I]), ...);
+        return v;
+    }
+    Swz& operator=(const gvec<T, L>& v) {
+        int k = 0;
+        ((e[I] = v.e[k++]), ...);
+        return *this;
+    }
+    Swz& operator=(const Swz& o) { return *this = gvec<T, L>(o); }
+    Swz& operator+=(const gvec<T, L>& v) { int k = 0; ((e[I] = e[I] + v.e[k++]), ...); return *this; }
+    Swz& operator-=(const gvec<T, L>& v) { int k = 0; ((e[I] = e[I] - v.e[k++]), ...); return *this; }
+    Swz& operator*=(const gvec<T, L>& v) { int k = 0; ((e[I] = e[I] * v.e[k++]), ...); return *this; }
+    Swz& operator/=(const gvec<T, L>& v) { int k = 0; ((e[I] = e[I] / v.e[k++]), ...); return *this; }
+    Swz& operator*=(T s) { ((e[I] = e[I] * s), ...); return *this; }
+    Swz& operator/=(T s) { ((e[I] = e[I] / s), ...); return *this; }
 };
 
 #define SWZ(...) Swz<T, N, __VA_ARGS__>
@@ -65,7 +76,7 @@ template <typename T> struct gvec<T, 2> {
     gvec() : e{T(0), T(0)} {}
     explicit gvec(T s) : e{s, s} {}
     gvec(T a, T b) : e{a, b} {}
-    template <typename U> explicit gvec(const gvec<U, 2>& o) : e{T(o.e[0]), T(o.e[1])} {}
+    template <typename U> gvec(const gvec<U, 2>& o) : e{T(o.e[0]), T(o.e[1])} {}
     template <typename U> explicit gvec(const gvec<U, 3>& o) : e{T(o.e[0]), T(o.e[1])} {}
     template <typename U> explicit gvec(const gvec<U, 4>& o) : e{T(o.e[0]), T(o.e[1])} {}
     gvec(const gvec& o) { std::memcpy(e, o.e, sizeof(e)); }
@@ -117,40 +128,6 @@ template <typename T> struct gvec<T, 4> {
 
 #undef SWZ
 
-template <typename T, int N, int... I> Swz<T, N, I...>::operator gvec<T, sizeof...(I)>() const {
-    gvec<T, sizeof...(I)> v;
-    int k = 0;
-    ((v.e[k++] = e[I]), ...);
-    return v;
-}
-template <typename T, int N, int... I> Swz<T, N, I...>& Swz<T, N, I...>::operator=(const gvec<T, sizeof...(I)>& v) {
-    int k = 0;
-    ((e[I] = v.e[k++]), ...);
-    return *this;
-}
-template <typename T, int N, int... I> Swz<T, N, I...>& Swz<T, N, I...>::operator=(const Swz& o) {
-    return *this = gvec<T, sizeof...(I)>(o);
-}
-#define SWZ_COMPOUND(OP)                                                                                   \
-    template <typename T, int N, int... I>                                                                 \
-    Swz<T, N, I...>& Swz<T, N, I...>::operator OP##=(const gvec<T, sizeof...(I)>& v) {                     \
-        int k = 0;                                                                                         \
-        ((e[I] = e[I] OP v.e[k++]), ...);                                                                  \
-        return *this;                                                                                      \
-    }
-SWZ_COMPOUND(+)
-SWZ_COMPOUND(-)
-SWZ_COMPOUND(*)
-SWZ_COMPOUND(/)
-template <typename T, int N, int... I> Swz<T, N, I...>& Swz<T, N, I...>::operator*=(T s) {
-    ((e[I] = e[I] * s), ...);
-    return *this;
-}
-template <typename T, int N, int... I> Swz<T, N, I...>& Swz<T, N, I...>::operator/=(T s) {
-    ((e[I] = e[I] / s), ...);
-    return *this;
-}
-
 typedef gvec<float, 2> vec2;
 typedef gvec<float, 3> vec3;
 typedef gvec<float, 4> vec4;
@@ -201,7 +178,10 @@ F1(cos, glslc::f_cos(x))
 F1(exp, glslc::f_exp(x))
 F1(log, glslc::f_log(x))
 F1(sign, x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f))
-inline int abs(int x) { return x < 0 ? -x : x; }
+// integer overloads only match integer arguments exactly, so that e.g.
+// clamp(float, 0, 1) picks the float overload as GLSL does
+template <typename I> using only_int = std::enable_if_t<std::is_same_v<I, int> || std::is_same_v<I, uint>, int>;
+template <typename I, only_int<I> = 0> inline I abs(I x) { return x < 0 ? -x : x; }
 
 #define F2(NAME, EXPR)                                                                            \
     inline float NAME(float x, float y) { return EXPR; }                                        \
@@ -217,10 +197,12 @@ F2(max, x < y ? y : x)
 F2(pow, glslc::f_pow(x, y))
 F2(mod, x - y * glslc::f_floor(x / y))
 F2(step, x > y ? 0.0f : 1.0f)   // step(edge = x, v = y): 0 if v < edge
-inline int min(int x, int y) { return y < x ? y : x; }
-inline int max(int x, int y) { return x < y ? y : x; }
-inline uint min(uint x, uint y) { return y < x ? y : x; }
-inline uint max(uint x, uint y) { return x < y ? y : x; }
+inline vec2 step(float edge, const vec2& v) { return vec2(v.e[0] < edge ? 0.0f : 1.0f, v.e[1] < edge ? 0.0f : 1.0f); }
+inline vec3 step(float edge, const vec3& v) {
+    return vec3(v.e[0] < edge ? 0.0f : 1.0f, v.e[1] < edge ? 0.0f : 1.0f, v.e[2] < edge ? 0.0f : 1.0f);
+}
+template <typename I, only_int<I> = 0> inline I min(I x, I y) { return y < x ? y : x; }
+template <typename I, only_int<I> = 0> inline I max(I x, I y) { return x < y ? y : x; }
 
 inline float clamp(float v, float lo, float hi) { return min(max(v, lo), hi); }
 inline vec2 clamp(const vec2& v, float lo, float hi) { return min(max(v, lo), hi); }
@@ -228,7 +210,7 @@ inline vec3 clamp(const vec3& v, float lo, float hi) { return min(max(v, lo), hi
 inline vec4 clamp(const vec4& v, float lo, float hi) { return min(max(v, lo), hi); }
 inline vec2 clamp(const vec2& v, const vec2& lo, const vec2& hi) { return min(max(v, lo), hi); }
 inline vec3 clamp(const vec3& v, const vec3& lo, const vec3& hi) { return min(max(v, lo), hi); }
-inline int clamp(int v, int lo, int hi) { return min(max(v, lo), hi); }
+template <typename I, only_int<I> = 0> inline I clamp(I v, I lo, I hi) { return min(max(v, lo), hi); }
 inline ivec3 clamp(const ivec3& v, const ivec3& lo, const ivec3& hi) {
     ivec3 r;
     for (int i = 0; i < 3; ++i) r.e[i] = min(max(v.e[i], lo.e[i]), hi.e[i]);

@@ -10,9 +10,10 @@
 // the reference stores RGBA16F / RG16F (Engine/DDGI/DDGIRenderer.cpp:173-204).
 //
 // Parity pins: the reference ships no tests or golden data.  This oracle is
-// pinned by analytic known-answer tests and by the border tables read from
-// the reference source (tests/golden/); see the repository design notes for
-// what that leaves unpinned.
+// pinned against the reference's own GLSL function libraries compiled as
+// C++ (oracle/build_ref.py, oracle/ref_harness.cpp), by the border tables
+// read from the reference source (tests/golden/) and by analytic
+// known-answer tests.
 //
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
 // this library.

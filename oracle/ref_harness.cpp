@@ -1,0 +1,308 @@
+// ORACLE -- test infrastructure only.
+//
+// Host harness around the reference's own GLSL function libraries, compiled
+// as C++ (see oracle/build_ref.py).  Every computation below is a call into
+// the reference functions -- sphericalFibonacci, probeLocation,
+// tracyGlobalSDF, getHitPosition, getGlobalSurfaceAtlasThreshold, the
+// sampleGlobalSurfaceAtlas macro, sampleIrradiance, octDecode,
+// normalizedOctCoord, getProbeId, combineDistanceToSDF, boxIntersectsSphere,
+// flattenId -- glued together the way the shader entry points do:
+//   ref_trace  GISDFRays.comp:63-128
+//   ref_blend  ProbeUpdate.glsl:182-281
+//   ref_mip    GlobalSDFMipmap.comp:190-226 and GlobalDistanceField.cpp:537-573
+//   ref_cull   SDFCulling.comp:262-327 (deterministic list placement)
+// The entry-point bodies are restated because they declare Vulkan
+// resources (images, SSBOs, push constants) that do not compile as C++.
+#include "glsl_compat.h"
+
+#include "DDGI/DDGICommon.glsl"
+#include "SDF/SDFCommon.glsl"
+#include "SDF/AtlasCommon.glsl"
+
+#include <vector>
+
+#include "luxgi_ddgi.h"
+
+static_assert(sizeof(DDGIUniform) == sizeof(luxgi_ddgi_uniform), "DDGIUniform layout");
+static_assert(sizeof(GlobalSDFData) == sizeof(luxgi_sdf_data), "GlobalSDFData layout");
+static_assert(sizeof(GlobalSurfaceAtlasData) == sizeof(luxgi_surface_data), "GlobalSurfaceAtlasData layout");
+static_assert(sizeof(ObjectBuffer) == sizeof(luxgi_surface_object), "ObjectBuffer layout");
+static_assert(sizeof(TileBuffer) == sizeof(luxgi_surface_tile), "TileBuffer layout");
+
+namespace {
+
+template <typename T, typename S> T as(const S& s) {
+    T t;
+    std::memcpy(static_cast<void*>(&t), &s, sizeof(T));
+    return t;
+}
+
+sampler3D volume(const void* p, int fmt, int W, int H, int D) {
+    sampler3D s;
+    if (fmt == LUXGI_STORAGE_FP16) s.f16 = static_cast<const uint16_t*>(p);
+    else s.f32 = static_cast<const float*>(p);
+    s.W = W; s.H = H; s.D = D;
+    return s;
+}
+
+sampler2D tex2d(const float* f32, const uint16_t* f16, const uint8_t* u8, int W, int H, int C, bool repeat) {
+    sampler2D s;
+    s.f32 = f32; s.f16 = f16; s.u8 = u8;
+    s.W = W; s.H = H; s.C = C;
+    s.repeat = repeat;
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+// GISDFRays.comp main for probes [p0, p1): out float4 [n][R] (rgb, distance),
+// info int2 [n][R] (steps, hit cascade or -1).  Mode B adds
+// intensity * albedo/pi * sampleIrradiance(previous atlases) at hits
+// (Raytraced/Lighting.glsl:79-84 with the volume intensity).
+// `dirs` (float4 [R], optional) replaces the rotated sphericalFibonacci
+// directions, so march and shading can be compared on identical rays.
+int ref_trace(const luxgi_ddgi_volume_desc* vd, const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf,
+              const float* prev_irr, const float* prev_dist, int frames, const float rot9[9], int p0, int p1,
+              float* out, int32_t* info, const float* dirs) {
+    const DDGIUniform ddgi = as<DDGIUniform>(vd->uniform);
+    const GlobalSDFData sd = as<GlobalSDFData>(sdf->data);
+    const GlobalSurfaceAtlasData ad = as<GlobalSurfaceAtlasData>(surf->data);
+    const int C = int(sdf->data.cascades_count), res = sdf->resolution, mres = sdf->mip_resolution;
+    const sampler3D tex = volume(sdf->sdf, sdf->format, res * C, res, res);
+    const sampler3D mip = volume(sdf->mip, sdf->format, mres * C, mres, mres);
+    const int A = int(surf->data.resolution);
+    const sampler2D depthS = tex2d(surf->depth, nullptr, nullptr, A, A, 1, false);
+    const bool per_hit = vd->light_mode == LUXGI_LIGHT_PER_HIT;
+    const sampler2D colorS = per_hit ? tex2d(nullptr, surf->direct_light, nullptr, A, A, 4, false)
+                                     : tex2d(nullptr, static_cast<const uint16_t*>(surf->light_cache), nullptr, A, A, 4, false);
+    const sampler2D albedoS = tex2d(nullptr, nullptr, surf->albedo, A, A, 4, false);
+    const sampler2D irrS = tex2d(prev_irr, nullptr, nullptr, ddgi.irradianceTextureWidth, ddgi.irradianceTextureHeight, 4, true);
+    const sampler2D distS = tex2d(prev_dist, nullptr, nullptr, ddgi.depthTextureWidth, ddgi.depthTextureHeight, 2, true);
+    const ObjectBuffer* objects = reinterpret_cast<const ObjectBuffer*>(surf->objects);
+    const TileBuffer* tiles = reinterpret_cast<const TileBuffer*>(surf->tiles);
+    const uint* chunks = surf->chunks;
+    const uint* cull = surf->culled_objects;
+    const bool bounce = per_hit && vd->infinite_bounce && frames != 0 && prev_irr && prev_dist;
+    mat3 orientation(vec3(rot9[0], rot9[1], rot9[2]), vec3(rot9[3], rot9[4], rot9[5]), vec3(rot9[6], rot9[7], rot9[8]));
+    const int R = ddgi.raysPerProbe;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int probeId = p0; probeId < p1; ++probeId) {
+        for (int rayId = 0; rayId < R; ++rayId) {
+            vec3 rayOrigin = probeLocation(ddgi, probeId);
+            vec3 direction = dirs ? vec3(dirs[4 * rayId], dirs[4 * rayId + 1], dirs[4 * rayId + 2])
+                                  : normalize(orientation * sphericalFibonacci(float(rayId), float(ddgi.raysPerProbe)));
+            GlobalSDFTrace trace;
+            trace.worldPosition = rayOrigin;
+            trace.worldDirection = direction;
+            trace.minDistance = 0;
+            trace.maxDistance = GLOBAL_SDF_WORLD_SIZE;
+            trace.stepScale = 1.f;
+            trace.needsHitNormal = true;
+            GlobalSDFHit hit = tracyGlobalSDF(sd, tex, mip, trace, 0);
+            vec4 radiance = vec4(0);
+            if (isHit(hit)) {
+                if (hit.hitSDF <= 0.0f && hit.hitTime <= sd.cascadeVoxelSize[0]) {
+                    radiance = vec4(0, 0, 0, GLOBAL_SDF_WORLD_SIZE);
+                } else {
+                    vec3 hitPosition = getHitPosition(hit, trace);
+                    float surfaceThreshold = getGlobalSurfaceAtlasThreshold(sd, hit);
+                    vec4 surfaceColor;
+                    sampleGlobalSurfaceAtlas(surfaceColor, ad, chunks, cull, objects, tiles, depthS, colorS,
+                                             getHitPosition(hit, trace), hit.hitNormal, surfaceThreshold, false);
+                    radiance = vec4(vec3(surfaceColor.rgb), hit.hitTime);
+                    if (bounce) {
+                        vec4 albedo;
+                        sampleGlobalSurfaceAtlas(albedo, ad, chunks, cull, objects, tiles, depthS, albedoS,
+                                                 hitPosition, hit.hitNormal, surfaceThreshold, false);
+                        vec3 diffuseColor = (vec3(albedo.rgb) - vec3(albedo.rgb) * 0.0f) / PI;
+                        vec3 e = sampleIrradiance(ddgi, hitPosition, hit.hitNormal, -direction, irrS, distS);
+                        radiance.rgb += vd->intensity * diffuseColor * e;
+                    }
+                    radiance.w = max(radiance.w + sd.cascadeVoxelSize[hit.hitCascade] * 0.5f, 0);
+                }
+            } else {
+                radiance = vec4(vd->sky_radiance[0], vd->sky_radiance[1], vd->sky_radiance[2], GLOBAL_SDF_WORLD_SIZE);
+            }
+            const size_t i = size_t(probeId - p0) * R + rayId;
+            out[4 * i + 0] = radiance.x;
+            out[4 * i + 1] = radiance.y;
+            out[4 * i + 2] = radiance.z;
+            out[4 * i + 3] = radiance.w;
+            if (info) {
+                info[2 * i] = int32_t(hit.stepsCount);
+                info[2 * i + 1] = isHit(hit) ? int32_t(hit.hitCascade) : -1;
+            }
+        }
+    }
+    return 0;
+}
+
+// ProbeUpdate.glsl main for both atlases.  dirs float4 [R], rays float4
+// [P][R] (rgb, distance); atlases float, prev may be NULL when first.
+int ref_blend(const luxgi_ddgi_volume_desc* vd, const float* dirs, const float* rays, const float* prev_irr,
+              const float* prev_dist, float* out_irr, float* out_dist, int first) {
+    const DDGIUniform ddgi = as<DDGIUniform>(vd->uniform);
+    const int XY = ddgi.probeCounts.x * ddgi.probeCounts.y, Z = ddgi.probeCounts.z;
+    const float FLT_EPS = 0.00000001;
+    for (int depth = 0; depth < 2; ++depth) {
+        const int n = depth ? ddgi.depthProbeSideLength : ddgi.irradianceProbeSideLength;
+        const int W = depth ? ddgi.depthTextureWidth : ddgi.irradianceTextureWidth;
+        const int nc = depth ? 2 : 4;
+        const float* prev = depth ? prev_dist : prev_irr;
+        float* outp = depth ? out_dist : out_irr;
+#pragma omp parallel for collapse(2)
+        for (int gy = 0; gy < Z; ++gy)
+            for (int gx = 0; gx < XY; ++gx)
+                for (int ly = 0; ly < n; ++ly)
+                    for (int lx = 0; lx < n; ++lx) {
+                        // gl_GlobalInvocationID = workgroup * local size + local id
+                        const ivec2 currentCoord = ivec2(gx * n + lx, gy * n + ly) + (ivec2(gx, gy) * ivec2(2)) + ivec2(2);
+                        const int relativeProbeId = getProbeId(vec2(currentCoord), W, n);
+                        vec3 result = vec3(0.0f);
+                        float totalWeight = 0.0f;
+                        vec3 texelDirection = octDecode(normalizedOctCoord(currentCoord, n));
+                        for (int r = 0; r < ddgi.raysPerProbe; ++r) {
+                            const float* dd = dirs + 4 * r;
+                            const float* ry = rays + (size_t(relativeProbeId) * ddgi.raysPerProbe + r) * 4;
+                            vec3 rayDirection = vec3(dd[0], dd[1], dd[2]);
+                            float weight = 0.0f;
+                            if (depth) {
+                                float rayProbeDistance = min(ddgi.maxDistance, ry[3] - 0.01f);
+                                if (rayProbeDistance == -1.0f) rayProbeDistance = ddgi.maxDistance;
+                                weight = pow(max(0.0, dot(texelDirection, rayDirection)), ddgi.sharpness);
+                                if (weight >= FLT_EPS) {
+                                    result += vec3(rayProbeDistance * weight, square(rayProbeDistance) * weight, 0.0);
+                                    totalWeight += weight;
+                                }
+                            } else {
+                                vec3 rayHitRadiance = vec3(ry[0], ry[1], ry[2]);
+                                weight = max(0.0, dot(texelDirection, rayDirection));
+                                if (weight >= FLT_EPS) {
+                                    result += vec3(rayHitRadiance * weight);
+                                    totalWeight += weight;
+                                }
+                            }
+                        }
+                        if (totalWeight > FLT_EPS) result *= 1.f / (2 * totalWeight);
+                        const size_t ti = (size_t(currentCoord.y) * W + size_t(currentCoord.x)) * nc;
+                        vec3 prevResult = vec3(0.0f);
+                        if (!first) {
+                            prevResult.x = prev[ti];
+                            prevResult.y = prev[ti + 1];
+                            if (!depth) prevResult.z = prev[ti + 2];
+                        }
+                        if (!depth) result.rgb = pow(vec3(result.rgb), vec3(1.0f / ddgi.ddgiGamma));
+                        if (!first) result = mix(result, prevResult, ddgi.hysteresis);
+                        outp[ti] = result.x;
+                        outp[ti + 1] = result.y;
+                        if (!depth) {
+                            outp[ti + 2] = result.z;
+                            outp[ti + 3] = 1.0f;
+                        }
+                    }
+    }
+    return 0;
+}
+
+// GlobalSDFMipmap.comp main + the four fillFlood passes, every cascade.
+int ref_mip(const luxgi_sdf_desc* s, const float* sdf, float* mip_out) {
+    const int res = s->resolution, mres = s->mip_resolution, C = int(s->data.cascades_count);
+    std::vector<float> mip(size_t(mres) * C * mres * mres, 1.0f), tmp(size_t(mres) * mres * mres, 1.0f);
+    const ivec3 coords[6] = {ivec3(1, 0, 0), ivec3(0, 1, 0), ivec3(0, 0, 1), ivec3(-1, 0, 0), ivec3(0, -1, 0), ivec3(0, 0, -1)};
+    auto pass = [&](const float* src, int srcW, int srcRes, int scale, int offX, float* dst, int dstW, int dstOffX,
+                    float maxDistance) {
+        auto sampleSDF = [&](ivec3 voxelCoordMip, ivec3 offset) {
+            voxelCoordMip = clamp(voxelCoordMip * scale + offset, ivec3(0), ivec3(srcRes - 1));
+            voxelCoordMip.x += offX;
+            float result = src[size_t(voxelCoordMip.x) + size_t(srcW) * (size_t(voxelCoordMip.y) + size_t(srcRes) * voxelCoordMip.z)];
+            float distanceToVoxel = length(offset) * (maxDistance / float(srcRes));
+            return combineDistanceToSDF(result, distanceToVoxel);
+        };
+        for (int z = 0; z < mres; ++z)
+            for (int y = 0; y < mres; ++y)
+                for (int x = 0; x < mres; ++x) {
+                    ivec3 uvw = ivec3(x, y, z);
+                    float minDistance = sampleSDF(uvw, ivec3(0, 0, 0));
+                    for (int i = 0; i < 6; i++) minDistance = min(minDistance, sampleSDF(uvw, coords[i]));
+                    if (s->format == LUXGI_STORAGE_FP16) minDistance = float(_Float16(minDistance));
+                    dst[size_t(x + dstOffX) + size_t(dstW) * (size_t(y) + size_t(mres) * z)] = minDistance;
+                }
+    };
+    for (int k = 0; k < C; ++k) {
+        const float maxd = s->data.cascade_pos_distance[k][3] * 2.0f;
+        pass(sdf, res * C, res, 4, k * res, mip.data(), mres * C, k * mres, maxd);
+        for (int i = 1; i < 5; ++i) {
+            if (i & 1) pass(mip.data(), mres * C, mres, 1, k * mres, tmp.data(), mres, 0, maxd);
+            else pass(tmp.data(), mres, mres, 1, 0, mip.data(), mres * C, k * mres, maxd);
+        }
+    }
+    std::memcpy(mip_out, mip.data(), mip.size() * sizeof(float));
+    return 0;
+}
+
+// SDFCulling.comp main: for every chunk, the objects whose bounding sphere
+// touches the chunk box.  Lists are written in flattened chunk order at
+// prefix-sum offsets from word 1 (the reference appends them with an
+// atomic counter in arbitrary order; the per-chunk contents are the same).
+int ref_cull(const luxgi_surface_desc* s, uint32_t* chunks, uint32_t* culled, uint32_t capacity) {
+    const GlobalSurfaceAtlasData data = as<GlobalSurfaceAtlasData>(s->data);
+    const ObjectBuffer* objects = reinterpret_cast<const ObjectBuffer*>(s->objects);
+    const int NC = GLOBAL_SURFACE_ATLAS_CHUNKS_RESOLUTION;
+    std::memset(chunks, 0, sizeof(uint32_t) * NC * NC * NC);
+    uint32_t used = 1;
+    for (int z = 0; z < NC; ++z)
+        for (int y = 0; y < NC; ++y)
+            for (int x = 0; x < NC; ++x) {
+                ivec3 chunkCoord = ivec3(x, y, z);
+                uint chunkAddress = flattenId(chunkCoord);
+                vec3 chunkMin = (vec3(chunkCoord) - (GLOBAL_SURFACE_ATLAS_CHUNKS_RESOLUTION * 0.5f)) * data.chunkSize;
+                vec3 chunkMax = chunkMin + data.chunkSize;
+                std::vector<uint32_t> ids;
+                for (uint objectIndex = 0; objectIndex < data.objectsCount; objectIndex++) {
+                    ObjectBuffer obj = objects[objectIndex];
+                    if (boxIntersectsSphere(chunkMin, chunkMax, vec3(obj.objectBounds.xyz), obj.objectBounds.w))
+                        ids.push_back(objectIndex);
+                }
+                if (ids.empty()) continue;
+                const uint32_t need = uint32_t(ids.size()) + 1, st = used;
+                used += need;
+                if (st + need > capacity) continue;
+                culled[st] = uint32_t(ids.size());
+                for (size_t i = 0; i < ids.size(); ++i) culled[st + 1 + i] = ids[i];
+                chunks[chunkAddress] = st;
+            }
+    if (capacity > 0) culled[0] = used;
+    return used > capacity ? LUXGI_ENOMEM : 0;
+}
+
+// sampleIrradiance for n points (float3) against float atlases.
+int ref_sample_irradiance(const luxgi_ddgi_uniform* u, const float* irr, const float* dist, const float* pos,
+                          const float* nrm, const float* wo, float* out, int n) {
+    const DDGIUniform ddgi = as<DDGIUniform>(*u);
+    const sampler2D irrS = tex2d(irr, nullptr, nullptr, ddgi.irradianceTextureWidth, ddgi.irradianceTextureHeight, 4, true);
+    const sampler2D distS = tex2d(dist, nullptr, nullptr, ddgi.depthTextureWidth, ddgi.depthTextureHeight, 2, true);
+#pragma omp parallel for
+    for (int i = 0; i < n; ++i) {
+        vec3 e = sampleIrradiance(ddgi, vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]),
+                                  vec3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]),
+                                  vec3(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), irrS, distS);
+        out[3 * i] = e.x;
+        out[3 * i + 1] = e.y;
+        out[3 * i + 2] = e.z;
+    }
+    return 0;
+}
+
+// sphericalFibonacci under a rotation (GISDFRays.comp:73), float4 [R].
+int ref_ray_dirs(const float rot9[9], int R, float* out) {
+    mat3 orientation(vec3(rot9[0], rot9[1], rot9[2]), vec3(rot9[3], rot9[4], rot9[5]), vec3(rot9[6], rot9[7], rot9[8]));
+    for (int r = 0; r < R; ++r) {
+        vec3 d = normalize(orientation * sphericalFibonacci(float(r), float(R)));
+        out[4 * r] = d.x; out[4 * r + 1] = d.y; out[4 * r + 2] = d.z; out[4 * r + 3] = 0.0f;
+    }
+    return 0;
+}
+
+}  // extern "C"

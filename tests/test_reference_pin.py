@@ -1,0 +1,151 @@
+"""Pins the CPU oracle to the reference's own code: the GLSL function
+libraries of the reference (DDGICommon.glsl, SDFCommon.glsl,
+AtlasCommon.glsl, Math.glsl, Random.glsl) compiled as C++ by
+oracle/build_ref.py, driven the way the shader entry points drive them
+(oracle/ref_harness.cpp).  Runs on the host; skipped where the reference
+checkout is absent (the compiled library cannot be rebuilt there).
+
+Tolerances: mip and culling bit-exact; with identical ray directions the
+march takes the same steps and hits within 1e-3 voxel, radiance within
+1e-3 relative (p99 1e-5); blend 1e-5 relative; sampleIrradiance 1e-4.
+"""
+from __future__ import annotations
+
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+import oracle
+from luxgi_gb300 import _native as N
+from luxgi_gb300.ddgi import frame_rotation
+from luxgi_gb300.scene import PLAIN_SMALL, HostScene
+from tests._helpers import rel_err, tiny_workload
+
+
+@pytest.fixture(scope="module")
+def ref():
+    lib = oracle.ref_lib()
+    if lib is None:
+        pytest.skip("reference checkout not available: compiled reference library absent")
+    return lib
+
+
+@pytest.mark.parametrize("fmt,cascades", [(N.STORAGE_FP32, 1), (N.STORAGE_FP16, 1), (N.STORAGE_FP32, 2)])
+def test_mip_equals_reference(ref, fmt, cascades):
+    w = tiny_workload(sdf=64, sdf_format=fmt, cascades=cascades)
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    a = oracle.ref_mip(inp.sdf_desc, host.sdf_float())
+    b = oracle.build_mip(inp.sdf_desc, host.sdf_float())
+    assert np.array_equal(a, b)
+
+
+def test_cull_equals_reference(ref):
+    host = HostScene(PLAIN_SMALL.scene)
+    inp = oracle.HostInputs(host, PLAIN_SMALL.volume.light_mode)
+    ch, cu, st = oracle.ref_cull(inp.surface_desc, host.cull_capacity())
+    assert st == 0
+    assert np.array_equal(ch, inp.chunks) and np.array_equal(cu, inp.culled)
+
+
+def test_ray_directions_vs_reference(ref):
+    for f in range(3):
+        rot = frame_rotation(40, f)
+        r = oracle.ref_ray_dirs(rot, 256)          # the reference formula in plain FP32
+        d64 = oracle.ray_dirs(rot, 256, precision=1)
+        d32 = oracle.ray_dirs(rot, 256, precision=0)
+        assert np.max(np.abs(r - d64)) < 5e-5       # plain FP32 madfrac loses ~2^-24 * i turns
+        assert np.max(np.abs(d32 - d64)) < 2e-6     # the compensated evaluation does not
+
+
+def _trace_pair(w, frames=0, prev=None, seed=41):
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    vd = w.volume.desc()
+    rot = frame_rotation(seed, frames)
+    dirs = oracle.ray_dirs(rot, vd.uniform.rays_per_probe, 0)
+    pi, pd = (None, None) if prev is None else prev
+    a, ia = oracle.ref_trace(vd, inp, rot, frames, pi, pd, dirs=dirs)
+    b, ib = oracle.trace(vd, inp, rot, frames, pi, pd, precision=0)
+    return host, a, ia, b, ib
+
+
+@pytest.mark.parametrize("light", [N.LIGHT_PER_HIT, N.LIGHT_CACHE])
+def test_trace_matches_reference_functions(ref, light):
+    w = replace(PLAIN_SMALL, volume=replace(PLAIN_SMALL.volume, light_mode=light))
+    host, a, ia, b, ib = _trace_pair(w)
+    voxel = host.sdf_data.cascade_voxel_size[0]
+    assert np.array_equal(ia[..., 0], ib[..., 0])            # march steps
+    assert np.array_equal(ia[..., 1], ib[..., 1])            # hit cascade / miss
+    assert np.all(np.abs(a[..., 3] - b[..., 3]) <= 1e-3 * voxel)
+    rel = np.abs(a[..., :3] - b[..., :3]) / np.maximum(np.abs(b[..., :3]), 1e-3)
+    assert rel.max() < 1e-3 and np.quantile(rel, 0.99) < 1e-5
+
+
+def test_trace_two_cascades_matches_reference(ref):
+    w = tiny_workload(probe_counts=(4, 3, 4), rays=96, sdf=64, cascades=2, room=24.0, prims=10, steps=250)
+    host, a, ia, b, ib = _trace_pair(w)
+    assert (ia[..., 1] >= 0).any() and (ia[..., 1] == 1).any()   # both cascades used
+    same = (ia[..., 0] == ib[..., 0]) & (ia[..., 1] == ib[..., 1])
+    assert same.mean() > 0.999
+    voxel = host.sdf_data.cascade_voxel_size[1]
+    assert (np.abs(a[..., 3] - b[..., 3]) <= 1e-3 * voxel)[same].all()
+
+
+def test_trace_bounce_matches_reference(ref):
+    """Per-hit bounce (frame > 0) through the reference's sampleIrradiance."""
+    w = PLAIN_SMALL
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    rots = [frame_rotation(42, f) for f in range(2)]
+    irr, dist, frames, _ = oracle.run_frames(w.volume.desc(), inp, rots, precision=0)
+    host2, a, ia, b, ib = _trace_pair(w, frames=frames, prev=(irr, dist), seed=42)
+    assert np.array_equal(ia, ib[..., :2])
+    rel = np.abs(a[..., :3] - b[..., :3]) / np.maximum(np.abs(b[..., :3]), 1e-3)
+    assert rel.max() < 2e-3 and np.quantile(rel, 0.99) < 1e-5
+
+
+@pytest.mark.parametrize("sides", [(6, 14), (8, 16)])
+def test_blend_matches_reference(ref, sides):
+    w = tiny_workload(probe_counts=(5, 2, 3), rays=128, irr=sides[0], dist=sides[1])
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    vd = w.volume.desc()
+    prev = None
+    for f in range(3):
+        rot = frame_rotation(43, f)
+        rays, _ = oracle.trace(vd, inp, rot, f, *(prev or (None, None)), precision=0, want_info=False)
+        dirs = oracle.ray_dirs(rot, vd.uniform.rays_per_probe, 0)
+        pi, pd = prev or (None, None)
+        a = oracle.ref_blend(vd, dirs, rays, pi, pd, first=(f == 0))
+        b = oracle.blend(vd, dirs, rays, pi, pd, first=(f == 0), precision=0, border=False)
+        u = vd.uniform
+        for k, n in ((0, u.irradiance_probe_side), (1, u.depth_probe_side)):
+            # interiors only: the reference writes borders in a separate pass
+            H, W = a[k].shape[:2]
+            m = np.zeros((H, W), dtype=bool)
+            for cy in range(u.probe_counts[2]):
+                for cx in range(u.probe_counts[0] * u.probe_counts[1]):
+                    m[cy * (n + 2) + 2: cy * (n + 2) + 2 + n, cx * (n + 2) + 2: cx * (n + 2) + 2 + n] = True
+            assert rel_err(a[k][m], b[k][m]) < 1e-5
+        prev = oracle.blend(vd, dirs, rays, pi, pd, first=(f == 0), precision=0, border=True)
+
+
+def test_sample_irradiance_matches_reference(ref):
+    w = PLAIN_SMALL
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    rots = [frame_rotation(44, f) for f in range(3)]
+    irr, dist, _, _ = oracle.run_frames(w.volume.desc(), inp, rots, precision=0)
+    rng = np.random.default_rng(8)
+    n = 2000
+    pos = rng.uniform(-4, 4, size=(n, 3)).astype(np.float32)
+    nrm = rng.normal(size=(n, 3)).astype(np.float32)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    wo = rng.normal(size=(n, 3)).astype(np.float32)
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    u = w.volume.uniform()
+    a = oracle.ref_sample_irradiance(u, irr, dist, pos, nrm, wo)
+    b = oracle.sample_irradiance(u, irr, dist, pos, nrm, wo, precision=0)
+    assert rel_err(a, b, floor=1e-2) < 1e-4
