@@ -179,7 +179,11 @@ typedef struct luxgi_ddgi_volume_desc {
     int32_t infinite_bounce;       /* IrradianceVolume::infiniteBounce        */
     float   intensity;             /* IrradianceVolume::intensity             */
     float   sky_radiance[3];       /* constant sky for misses                 */
-    int32_t reserved[8];
+    int32_t march_variant;         /* tuning: 0 = default, 1 = occupancy-bound
+                                      march (64 registers), 2 = latency-bound
+                                      march (no register bound); results are
+                                      identical, only speed differs          */
+    int32_t reserved[7];
 } luxgi_ddgi_volume_desc;
 
 /* Device views of a volume's probe atlases. */

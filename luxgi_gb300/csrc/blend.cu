@@ -18,29 +18,31 @@
 namespace luxgi {
 
 // ------------------------------------------------------------- weights
-// One thread per texel row: octDecode(normalizedOctCoord) (DDGICommon.glsl:
-// 74-92) against every ray direction; sequential sum like the reference.
-// Also writes the FP16 K-major weight operands of the tensor-core blend
-// (rows padded with zeros) and their own normalisers.
-__global__ void weights_kernel(const luxgi_ddgi_uniform u, const float4* __restrict__ dirs, float* __restrict__ w_irr,
-                               float* __restrict__ w_dist, float* __restrict__ n_irr, float* __restrict__ n_dist,
-                               __half* __restrict__ tcw_irr, __half* __restrict__ tcw_dist, int tc_n_irr,
-                               int tc_n_dist) {
+// One block per texel row, threads over rays: octDecode(normalizedOctCoord)
+// (DDGICommon.glsl:74-92) against every ray direction.  The row sum is a
+// fixed-order tree reduction (deterministic).  Also writes the FP16 K-major
+// weight operands of the tensor-core blend (rows padded with zeros) and
+// their own normalisers.
+constexpr int kWeightThreads = 128;
+
+__global__ void __launch_bounds__(kWeightThreads) weights_kernel(
+    const luxgi_ddgi_uniform u, const float4* __restrict__ dirs, float* __restrict__ w_irr, float* __restrict__ w_dist,
+    float* __restrict__ n_irr, float* __restrict__ n_dist, __half* __restrict__ tcw_irr, __half* __restrict__ tcw_dist,
+    int tc_n_irr, int tc_n_dist) {
+    __shared__ float red[2][kWeightThreads];
     const int ni = u.irradiance_probe_side, nd = u.depth_probe_side;
     const int Ti = ni * ni, Td = nd * nd;
     const int R = u.rays_per_probe;
     const bool tc = tcw_irr != nullptr;
     const int rows_i = tc ? tc_n_irr : Ti;      // tensor-core rows are padded (>= T)
-    const int rows_d = tc ? tc_n_dist : Td;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= rows_i + rows_d) return;
+    const int row = blockIdx.x;
     const bool depth = row >= rows_i;
     const int t = depth ? row - rows_i : row;
     const int n = depth ? nd : ni;
     const int T = depth ? Td : Ti;
     __half* tcw = depth ? tcw_dist : tcw_irr;
     if (t >= T) {                                  // tensor-core padding row
-        for (int r = 0; r < R; ++r) tcw[size_t(t) * R + r] = __float2half_rn(0.0f);
+        for (int r = threadIdx.x; r < R; r += blockDim.x) tcw[size_t(t) * R + r] = __float2half_rn(0.0f);
         return;
     }
     const int tx = t % n, ty = t / n;
@@ -55,7 +57,7 @@ __global__ void weights_kernel(const luxgi_ddgi_uniform u, const float4* __restr
     const f3 td = norm3(v);
     float* w = depth ? w_dist : w_irr;
     float sum = 0.0f, sum_h = 0.0f;
-    for (int r = 0; r < R; ++r) {
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
         const float4 d = __ldg(dirs + r);
         const float c = mx(0.0f, td.x * d.x + td.y * d.y + td.z * d.z);
         float wt = depth ? powf(c, u.sharpness) : c;
@@ -68,9 +70,23 @@ __global__ void weights_kernel(const luxgi_ddgi_uniform u, const float4* __restr
             sum_h = sum_h + __half2float(h);
         }
     }
-    float* nrm = depth ? n_dist : n_irr;
-    nrm[t] = (sum > 1e-8f) ? 1.0f / (2.0f * sum) : 1.0f;
-    if (tc) nrm[T + t] = (sum_h > 1e-8f) ? 1.0f / (2.0f * sum_h) : 1.0f;   // tensor-core normaliser
+    red[0][threadIdx.x] = sum;
+    red[1][threadIdx.x] = sum_h;
+    __syncthreads();
+    for (int k = kWeightThreads / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + k];
+            red[1][threadIdx.x] += red[1][threadIdx.x + k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        float* nrm = depth ? n_dist : n_irr;
+        sum = red[0][0];
+        sum_h = red[1][0];
+        nrm[t] = (sum > 1e-8f) ? 1.0f / (2.0f * sum) : 1.0f;
+        if (tc) nrm[T + t] = (sum_h > 1e-8f) ? 1.0f / (2.0f * sum_h) : 1.0f;   // tensor-core normaliser
+    }
 }
 
 cudaError_t launch_weights(const luxgi_ddgi_uniform& u, const float4* dirs, float* w_irr, float* w_dist, float* n_irr,
@@ -79,7 +95,7 @@ cudaError_t launch_weights(const luxgi_ddgi_uniform& u, const float4* dirs, floa
     const int Ti = u.irradiance_probe_side * u.irradiance_probe_side;
     const int Td = u.depth_probe_side * u.depth_probe_side;
     const int rows = tc_w_irr ? tc_n_irr + tc_n_dist : Ti + Td;
-    weights_kernel<<<(rows + 63) / 64, 64, 0, st>>>(u, dirs, w_irr, w_dist, n_irr, n_dist, tc_w_irr, tc_w_dist,
+    weights_kernel<<<rows, kWeightThreads, 0, st>>>(u, dirs, w_irr, w_dist, n_irr, n_dist, tc_w_irr, tc_w_dist,
                                                     tc_n_irr, tc_n_dist);
     note_launch();
     return cudaGetLastError();

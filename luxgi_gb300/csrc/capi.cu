@@ -45,6 +45,11 @@ struct luxgi_ddgi_volume {
     __half* tcw_irr = nullptr;
     __half* tcw_dist = nullptr;
     uint32_t* status = nullptr;
+    float4* hit_t = nullptr;       // march records: time, normal
+    int* hit_c = nullptr;          // march records: cascade / -1 miss / -2 inside
+    float* w2l = nullptr;          // per-object inverse transforms of the bound scene
+    int w2l_cap = 0;
+    bool w2l_dirty = true;
     luxgi_sdf_desc sdf{};
     luxgi_surface_desc surf{};
 };
@@ -85,7 +90,7 @@ template <typename T> cudaError_t dmalloc(T** p, size_t bytes) {
 void free_volume(luxgi_ddgi_volume* v) {
     void* ptrs[] = {v->irr[0], v->irr[1], v->dist[0], v->dist[1], v->dirs_trace, v->dirs_blend, v->rays, v->info,
                     v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
-                    v->status};
+                    v->status, v->hit_t, v->hit_c, v->w2l};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -102,10 +107,11 @@ SdfView sdf_view(const luxgi_sdf_desc& s) {
     return v;
 }
 
-SurfaceView surface_view(const luxgi_surface_desc& s, int light_mode) {
+SurfaceView surface_view(const luxgi_surface_desc& s, int light_mode, const float* w2l = nullptr) {
     SurfaceView v;
     v.data = s.data;
     v.objects = s.objects;
+    v.w2l = w2l;
     v.tiles = s.tiles;
     v.chunks = s.chunks;
     v.culled = s.culled_objects;
@@ -133,11 +139,18 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     e = launch_weights(d.uniform, v->dirs_blend, v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc ? v->tcw_irr : nullptr,
                        v->tc ? v->tcw_dist : nullptr, v->tc_ni, v->tc_nd, st);
     if (e != cudaSuccess) return cuda_status(e);
+    if (v->w2l_dirty) {
+        e = launch_world_to_local(v->surf.objects, int(v->surf.data.objects_count), v->w2l, st);
+        if (e != cudaSuccess) return cuda_status(e);
+        v->w2l_dirty = false;
+    }
     TraceParams p;
     std::memset(&p, 0, sizeof(p));
     p.u = d.uniform;
     p.sdf = sdf_view(v->sdf);
-    p.surf = surface_view(v->surf, d.light_mode);
+    p.surf = surface_view(v->surf, d.light_mode, v->w2l);
+    p.hit_t = v->hit_t;
+    p.hit_c = v->hit_c;
     p.prev.irr = v->irr[v->ping_pong];
     p.prev.dist = v->dist[v->ping_pong];
     p.prev.storage = d.storage;
@@ -151,6 +164,7 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     p.storage = d.storage;
     p.light_mode = d.light_mode;
     p.max_steps = d.max_steps;
+    p.march_variant = d.march_variant;
     p.bounce = (d.infinite_bounce && v->frames != 0) ? 1 : 0;
     p.P = v->P;
     p.R = v->R;
@@ -289,6 +303,7 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->light_mode != LUXGI_LIGHT_CACHE && desc->light_mode != LUXGI_LIGHT_PER_HIT) return LUXGI_EINVAL;
     if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
     if (desc->max_steps < 1) return LUXGI_EINVAL;
+    if (desc->march_variant < 0 || desc->march_variant > 2) return LUXGI_EINVAL;
     if (desc->blend == LUXGI_BLEND_TENSOR && !tc_blend_supported(desc->uniform)) return LUXGI_EUNSUPPORTED;
     luxgi_ddgi_volume* v = new (std::nothrow) luxgi_ddgi_volume();
     if (!v) return LUXGI_ENOMEM;
@@ -319,6 +334,8 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (e == cudaSuccess) e = dmalloc(&v->n_irr, sizeof(float) * 2 * v->Ti);
     if (e == cudaSuccess) e = dmalloc(&v->n_dist, sizeof(float) * 2 * v->Td);
     if (e == cudaSuccess) e = dmalloc(&v->status, sizeof(uint32_t) * 4);
+    if (e == cudaSuccess) e = dmalloc(&v->hit_t, sizeof(float4) * PR);
+    if (e == cudaSuccess) e = dmalloc(&v->hit_c, sizeof(int) * PR);
     if (v->tc) {
         if (e == cudaSuccess) e = dmalloc(&v->tc_irr, sizeof(__half) * PR * 4);
         if (e == cudaSuccess) e = dmalloc(&v->tc_dist, sizeof(__half) * PR * 4);
@@ -356,6 +373,16 @@ int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const
     if (surf->data.resolution == 0) return LUXGI_EINVAL;
     if (v->desc.light_mode == LUXGI_LIGHT_PER_HIT && (!surf->direct_light || !surf->albedo)) return LUXGI_EINVAL;
     if (v->desc.light_mode == LUXGI_LIGHT_CACHE && !surf->light_cache) return LUXGI_EINVAL;
+    const int nobj = int(surf->data.objects_count);
+    if (nobj > v->w2l_cap) {
+        if (v->w2l) cudaFree(v->w2l);
+        v->w2l = nullptr;
+        v->w2l_cap = 0;
+        const cudaError_t e = dmalloc(&v->w2l, sizeof(float) * 16 * size_t(nobj));
+        if (e != cudaSuccess) return cuda_status(e);
+        v->w2l_cap = nobj;
+    }
+    v->w2l_dirty = true;
     v->sdf = *sdf;
     v->surf = *surf;
     v->bound = true;

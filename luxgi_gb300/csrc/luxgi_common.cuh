@@ -121,6 +121,21 @@ struct SdfView {
     int format;   // luxgi_storage of the sdf/mip texels
 };
 
+// Hit normal: central differences of the full-resolution SDF at +-1/res in
+// packed texture coordinates (SDFCommon.glsl:174-183).  Kept out of line so
+// the march loop's register budget does not carry its 48 taps.
+template <typename T>
+__device__ __noinline__ f3 sdf_normal(const T* __restrict__ tex, int TW, int res, float tu, float uy, float uz,
+                                      float off) {
+    const float xp = sample3d(tex, TW, res, res, tu + off, uy, uz);
+    const float xn = sample3d(tex, TW, res, res, tu - off, uy, uz);
+    const float yp = sample3d(tex, TW, res, res, tu, uy + off, uz);
+    const float yn = sample3d(tex, TW, res, res, tu, uy - off, uz);
+    const float zp = sample3d(tex, TW, res, res, tu, uy, uz + off);
+    const float zn = sample3d(tex, TW, res, res, tu, uy, uz - off);
+    return norm3(f3{xp - xn, yp - yn, zp - zn});
+}
+
 struct MarchHit {
     f3 normal;
     float time;
@@ -179,9 +194,12 @@ __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 di
             const float uy = clampf((sp.y - cy) / md + 0.5f, 0.0f, 1.0f);
             const float uz = clampf((sp.z - cz) / md + 0.5f, 0.0f, 1.0f);
             const float tu = (float(cascade) + ux) / invC;
+            // the full-resolution taps are issued together with the mip taps
+            // (one memory round trip per step); their value is used only
+            // where SDFCommon.glsl:150-158 samples the full-resolution SDF
             float sd = sample3d(mip, MW, s.mres, s.mres, tu, uy, uz);
+            const float sdt = sample3d(tex, TW, s.res, s.res, tu, uy, uz);
             if (sd < chunk) {
-                const float sdt = sample3d(tex, TW, s.res, s.res, tu, uy, uz);
                 ++hit.fine;
                 if (sdt < margin * 2.0f) sd = sdt;
             } else {
@@ -193,14 +211,7 @@ __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 di
                 hit.time = mx(t + sd - thick, 0.0f);
                 hit.cascade = cascade;
                 hit.sdf = sd;
-                const float off = 1.0f / s.data.resolution;
-                const float xp = sample3d(tex, TW, s.res, s.res, tu + off, uy, uz);
-                const float xn = sample3d(tex, TW, s.res, s.res, tu - off, uy, uz);
-                const float yp = sample3d(tex, TW, s.res, s.res, tu, uy + off, uz);
-                const float yn = sample3d(tex, TW, s.res, s.res, tu, uy - off, uz);
-                const float zp = sample3d(tex, TW, s.res, s.res, tu, uy, uz + off);
-                const float zn = sample3d(tex, TW, s.res, s.res, tu, uy, uz - off);
-                hit.normal = norm3(f3{xp - xn, yp - yn, zp - zn});
+                hit.normal = sdf_normal(tex, TW, s.res, tu, uy, uz, 1.0f / s.data.resolution);
                 break;
             }
             t = t + mx(sd * 1.0f, voxel);
@@ -214,6 +225,7 @@ __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 di
 struct SurfaceView {
     luxgi_surface_data data;
     const luxgi_surface_object* objects;
+    const float* w2l;         // [objects][16] inverse(object.transform), precomputed; or nullptr
     const luxgi_surface_tile* tiles;
     const uint32_t* chunks;
     const uint32_t* culled;
@@ -372,10 +384,22 @@ __device__ __forceinline__ float sample_surface(const SurfaceView& S, f3 pos, f3
         const luxgi_surface_object* ob = S.objects + oaddr;
         const float4 bnd = __ldg(reinterpret_cast<const float4*>(ob->object_bounds));
         if (len3(sub3(f3{bnd.x, bnd.y, bnd.z}, pos)) > bnd.w) continue;
-        float M[16], w2l[16];
+        float w2l[16];
+        if (S.w2l) {
+            // inverse(object.transform), computed once per scene by the same
+            // mat4_inverse (AtlasCommon.glsl:134 recomputes it per ray)
+            const float4* src = reinterpret_cast<const float4*>(S.w2l + size_t(oaddr) * 16);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) M[k] = __ldg(&ob->transform[k]);
-        mat4_inverse(M, w2l);
+            for (int k = 0; k < 4; ++k) {
+                const float4 c = __ldg(src + k);
+                w2l[4 * k] = c.x; w2l[4 * k + 1] = c.y; w2l[4 * k + 2] = c.z; w2l[4 * k + 3] = c.w;
+            }
+        } else {
+            float M[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) M[k] = __ldg(&ob->transform[k]);
+            mat4_inverse(M, w2l);
+        }
         const f3 lp = mat4_mul_pt(w2l, pos, 1.0f);
         const float4 e = __ldg(reinterpret_cast<const float4*>(ob->extends));
         if (fabsf(lp.x) > e.x + thr || fabsf(lp.y) > e.y + thr || fabsf(lp.z) > e.z + thr) continue;

@@ -20,6 +20,8 @@ struct TraceParams {
     SurfaceView surf;
     AtlasView prev;          // previous-frame atlases (mode B bounce)
     const float4* dirs;      // [R] exact FP32 directions
+    float4* hit_t;           // [P][R] march result: hit time, normal xyz
+    int* hit_c;              // [P][R] hit cascade, -1 miss, -2 inside (GISDFRays.comp:93)
     void* out;               // [P][R] x4 radiance rgb + distance (FP32 or FP16)
     int4* info;              // [P][R] steps, cascade (-1 miss), fine samples, 0; or nullptr
     // tensor-core blend operands (nullptr unless the tensor blend is on)
@@ -28,6 +30,7 @@ struct TraceParams {
     float sky[3];
     float intensity;
     int storage, light_mode, max_steps, bounce;
+    int march_variant;
     int P, R;
 };
 
@@ -49,6 +52,7 @@ struct BlendParams {
 cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace, float4* dirs_blend,
                           cudaStream_t st);
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t st);
+cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 cudaError_t launch_weights(const luxgi_ddgi_uniform& u, const float4* dirs, float* w_irr, float* w_dist,
                            float* n_irr, float* n_dist, __half* tc_w_irr, __half* tc_w_dist, int tc_n_irr,
                            int tc_n_dist, cudaStream_t st);

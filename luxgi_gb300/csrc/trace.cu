@@ -33,12 +33,13 @@ cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace
     return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------- trace
+// ---------------------------------------------------------------- march
 // One thread per (probe, ray); consecutive threads take consecutive probes
 // with the same ray index, so a warp marches 32 parallel rays from
-// neighbouring probes through nearby SDF texels.
-template <typename SdfT, int MODE>
-__global__ void __launch_bounds__(128) trace_kernel(const TraceParams p) {
+// neighbouring probes through nearby SDF texels.  The march is the whole
+// kernel (no shading code): small, low register count, high occupancy.
+template <typename SdfT, int MIN_BLOCKS>
+__global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = int64_t(p.P) * p.R;
     if (idx >= total) return;
@@ -48,35 +49,59 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceParams p) {
     const f3 dir{d4.x, d4.y, d4.z};
     const f3 origin = probe_location(p.u, probe);
     const MarchHit hit = march_sdf<SdfT>(p.sdf, origin, dir, kWorldSize, p.max_steps);
-    f3 rad{0.0f, 0.0f, 0.0f};
-    float dist;
+    int cls = -1;                                          // miss
     if (hit.time >= 0.0f) {
-        if (hit.sdf <= 0.0f && hit.time <= p.sdf.data.cascade_voxel_size[0]) {
-            dist = kWorldSize;
-        } else {
-            const f3 hp = add3(origin, mul3(dir, hit.time));
-            const float vs = p.sdf.data.cascade_voxel_size[hit.cascade];
-            const float thr = vs * 1.05f;
-            f3 s0, s1;
-            if (MODE == LUXGI_LIGHT_PER_HIT) {
-                sample_surface<true>(p.surf, hp, hit.normal, thr, s0, s1);
-                rad = s0;
-                if (p.bounce) {
-                    const f3 e = sample_irradiance(p.u, p.prev, hp, hit.normal, mul3(dir, -1.0f));
-                    const f3 diff{s1.x / kPi, s1.y / kPi, s1.z / kPi};
-                    rad = add3(rad, mulv3(mul3(diff, p.intensity), e));
-                }
-            } else {
-                sample_surface<false>(p.surf, hp, hit.normal, thr, s0, s1);
-                rad = s0;
-            }
-            dist = mx(hit.time + vs * 0.5f, 0.0f);
-        }
-    } else {
-        rad = f3{p.sky[0], p.sky[1], p.sky[2]};
-        dist = kWorldSize;
+        // GISDFRays.comp:93: a hit at the probe from inside a surface
+        cls = (hit.sdf <= 0.0f && hit.time <= p.sdf.data.cascade_voxel_size[0]) ? -2 : hit.cascade;
     }
     const size_t o = size_t(probe) * p.R + ray;
+    p.hit_t[o] = make_float4(hit.time, hit.normal.x, hit.normal.y, hit.normal.z);
+    p.hit_c[o] = cls;
+    if (p.info) p.info[o] = make_int4(hit.steps, hit.time >= 0.0f ? hit.cascade : -1, hit.fine, 0);
+}
+
+// ---------------------------------------------------------------- shade
+// Hit classification and shading of GISDFRays.comp:89-127 from the march
+// records: sky for misses, zero for rays starting inside geometry, the
+// surface-cache sample (and, per hit, the previous frame's irradiance) for
+// hits; writes the per-ray radiance + distance and the tensor-core operands.
+template <int MODE>
+__global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = int64_t(p.P) * p.R;
+    if (idx >= total) return;
+    const int probe = int(idx % p.P);
+    const int ray = int(idx / p.P);
+    const size_t o = size_t(probe) * p.R + ray;
+    const float4 h = p.hit_t[o];
+    const int cls = p.hit_c[o];
+    f3 rad{0.0f, 0.0f, 0.0f};
+    float dist = kWorldSize;
+    if (cls == -1) {
+        rad = f3{p.sky[0], p.sky[1], p.sky[2]};
+    } else if (cls >= 0) {
+        const float4 d4 = __ldg(p.dirs + ray);
+        const f3 dir{d4.x, d4.y, d4.z};
+        const f3 origin = probe_location(p.u, probe);
+        const f3 nrm{h.y, h.z, h.w};
+        const f3 hp = add3(origin, mul3(dir, h.x));
+        const float vs = p.sdf.data.cascade_voxel_size[cls];
+        const float thr = vs * 1.05f;
+        f3 s0, s1;
+        if (MODE == LUXGI_LIGHT_PER_HIT) {
+            sample_surface<true>(p.surf, hp, nrm, thr, s0, s1);
+            rad = s0;
+            if (p.bounce) {
+                const f3 e = sample_irradiance(p.u, p.prev, hp, nrm, mul3(dir, -1.0f));
+                const f3 diff{s1.x / kPi, s1.y / kPi, s1.z / kPi};
+                rad = add3(rad, mulv3(mul3(diff, p.intensity), e));
+            }
+        } else {
+            sample_surface<false>(p.surf, hp, nrm, thr, s0, s1);
+            rad = s0;
+        }
+        dist = mx(h.x + vs * 0.5f, 0.0f);
+    }
     if (p.storage == LUXGI_STORAGE_FP16) {
         const __half2 rg = __floats2half2_rn(rad.x, rad.y);
         const __half2 bd = __floats2half2_rn(rad.z, dist);
@@ -89,7 +114,6 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceParams p) {
     } else {
         reinterpret_cast<float4*>(p.out)[o] = make_float4(rad.x, rad.y, rad.z, dist);
     }
-    if (p.info) p.info[o] = make_int4(hit.steps, hit.time >= 0.0f ? hit.cascade : -1, hit.fine, 0);
     if (p.tc_irr) {
         // tensor-core operands: radiance rows and the blend's per-ray depth
         // split into FP16 hi + lo (ProbeUpdate.glsl:204-207)
@@ -115,16 +139,43 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceParams p) {
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
     const int64_t total = int64_t(p.P) * p.R;
     if (total <= 0) return cudaSuccess;
-    const int threads = 128;
-    const unsigned blocks = unsigned((total + threads - 1) / threads);
-    const bool sdf16 = p.sdf.format == LUXGI_STORAGE_FP16;
-    if (p.light_mode == LUXGI_LIGHT_PER_HIT) {
-        if (sdf16) trace_kernel<__half, LUXGI_LIGHT_PER_HIT><<<blocks, threads, 0, st>>>(p);
-        else trace_kernel<float, LUXGI_LIGHT_PER_HIT><<<blocks, threads, 0, st>>>(p);
+    const unsigned mblocks = unsigned((total + 255) / 256);
+    // variant 1 bounds the march to 64 registers (4 blocks of 256 per SM),
+    // variant 2 lets it keep all 16 taps of a step in flight
+    const bool bounded = p.march_variant != 2;
+    if (p.sdf.format == LUXGI_STORAGE_FP16) {
+        if (bounded) march_kernel<__half, 4><<<mblocks, 256, 0, st>>>(p);
+        else march_kernel<__half, 1><<<mblocks, 256, 0, st>>>(p);
     } else {
-        if (sdf16) trace_kernel<__half, LUXGI_LIGHT_CACHE><<<blocks, threads, 0, st>>>(p);
-        else trace_kernel<float, LUXGI_LIGHT_CACHE><<<blocks, threads, 0, st>>>(p);
+        if (bounded) march_kernel<float, 4><<<mblocks, 256, 0, st>>>(p);
+        else march_kernel<float, 1><<<mblocks, 256, 0, st>>>(p);
     }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const unsigned sblocks = unsigned((total + 127) / 128);
+    if (p.light_mode == LUXGI_LIGHT_PER_HIT) shade_kernel<LUXGI_LIGHT_PER_HIT><<<sblocks, 128, 0, st>>>(p);
+    else shade_kernel<LUXGI_LIGHT_CACHE><<<sblocks, 128, 0, st>>>(p);
+    note_launch(2);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- world-to-local
+// inverse(object.transform) for every object (AtlasCommon.glsl:134), once
+// per bound scene instead of once per ray and object.
+__global__ void world_to_local_kernel(const luxgi_surface_object* __restrict__ objs, int n, float* __restrict__ w2l) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float M[16], inv[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) M[k] = objs[i].transform[k];
+    mat4_inverse(M, inv);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) w2l[size_t(i) * 16 + k] = inv[k];
+}
+
+cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    world_to_local_kernel<<<(n + 127) / 128, 128, 0, st>>>(objs, n, w2l);
     note_launch();
     return cudaGetLastError();
 }

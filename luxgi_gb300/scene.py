@@ -53,6 +53,7 @@ class VolumeSpec:
     infinite_bounce: bool = True
     intensity: float = 1.0
     sky: tuple = (0.5, 0.6, 0.8)
+    march_variant: int = 0
 
     @property
     def probes(self) -> int:
@@ -89,6 +90,7 @@ class VolumeSpec:
         d.intensity = self.intensity
         for k in range(3):
             d.sky_radiance[k] = self.sky[k]
+        d.march_variant = self.march_variant
         return d
 
 
