@@ -50,6 +50,13 @@ struct luxgi_ddgi_volume {
     float* w2l = nullptr;          // per-object inverse transforms of the bound scene
     int w2l_cap = 0;
     bool w2l_dirty = true;
+    uint32_t* shade_chunks = nullptr;   // shading lists (subset of the reference lists)
+    uint32_t* shade_culled = nullptr;
+    uint32_t* shade_scratch = nullptr;  // 40^3 counts + status
+    uint32_t shade_cap = 0;
+    void* sdf_quad = nullptr;           // quad-packed copies for march variants 3, 4
+    void* mip_quad = nullptr;
+    size_t sdf_quad_bytes = 0, mip_quad_bytes = 0;
     luxgi_sdf_desc sdf{};
     luxgi_surface_desc surf{};
 };
@@ -90,7 +97,8 @@ template <typename T> cudaError_t dmalloc(T** p, size_t bytes) {
 void free_volume(luxgi_ddgi_volume* v) {
     void* ptrs[] = {v->irr[0], v->irr[1], v->dist[0], v->dist[1], v->dirs_trace, v->dirs_blend, v->rays, v->info,
                     v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
-                    v->status, v->hit_t, v->hit_c, v->w2l};
+                    v->status, v->hit_t, v->hit_c, v->w2l, v->shade_chunks, v->shade_culled, v->shade_scratch,
+                    v->sdf_quad, v->mip_quad};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -142,6 +150,22 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     if (v->w2l_dirty) {
         e = launch_world_to_local(v->surf.objects, int(v->surf.data.objects_count), v->w2l, st);
         if (e != cudaSuccess) return cuda_status(e);
+        float thr = 0.0f;   // largest surface threshold (SDFCommon.glsl:196-199)
+        for (int k = 0; k < int(v->sdf.data.cascades_count); ++k)
+            thr = std::fmax(thr, v->sdf.data.cascade_voxel_size[k] * 1.05f);
+        e = launch_shade_lists(v->surf.data, v->surf.objects, v->surf.chunks, v->surf.culled_objects, thr,
+                               v->shade_chunks, v->shade_culled, v->shade_cap, v->shade_scratch,
+                               v->shade_scratch + 40 * 40 * 40, st);
+        if (e != cudaSuccess) return cuda_status(e);
+        const int C = int(v->sdf.data.cascades_count), res = v->sdf.resolution, mres = v->sdf.mip_resolution;
+        if (v->mip_quad) {
+            e = launch_quad_pack(v->sdf.mip, mres * C, mres, mres, v->sdf.format, v->mip_quad, st);
+            if (e != cudaSuccess) return cuda_status(e);
+        }
+        if (v->sdf_quad) {
+            e = launch_quad_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st);
+            if (e != cudaSuccess) return cuda_status(e);
+        }
         v->w2l_dirty = false;
     }
     TraceParams p;
@@ -149,6 +173,10 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     p.u = d.uniform;
     p.sdf = sdf_view(v->sdf);
     p.surf = surface_view(v->surf, d.light_mode, v->w2l);
+    p.surf.chunks = v->shade_chunks;
+    p.surf.culled = v->shade_culled;
+    p.sdf.sdf_quad = v->sdf_quad;
+    p.sdf.mip_quad = v->mip_quad;
     p.hit_t = v->hit_t;
     p.hit_c = v->hit_c;
     p.prev.irr = v->irr[v->ping_pong];
@@ -303,7 +331,7 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->light_mode != LUXGI_LIGHT_CACHE && desc->light_mode != LUXGI_LIGHT_PER_HIT) return LUXGI_EINVAL;
     if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
     if (desc->max_steps < 1) return LUXGI_EINVAL;
-    if (desc->march_variant < 0 || desc->march_variant > 2) return LUXGI_EINVAL;
+    if (desc->march_variant < 0 || desc->march_variant > 4) return LUXGI_EINVAL;
     if (desc->blend == LUXGI_BLEND_TENSOR && !tc_blend_supported(desc->uniform)) return LUXGI_EUNSUPPORTED;
     luxgi_ddgi_volume* v = new (std::nothrow) luxgi_ddgi_volume();
     if (!v) return LUXGI_ENOMEM;
@@ -381,6 +409,48 @@ int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const
         const cudaError_t e = dmalloc(&v->w2l, sizeof(float) * 16 * size_t(nobj));
         if (e != cudaSuccess) return cuda_status(e);
         v->w2l_cap = nobj;
+    }
+    // shading lists are a subset of the reference lists: the same capacity
+    // (or the worst case when the descriptor does not state it) always fits
+    uint32_t cap = surf->data.culled_objects_capacity;
+    if (cap == 0) cap = 1u + 40u * 40u * 40u * uint32_t(nobj + 1);
+    if (cap > v->shade_cap) {
+        if (v->shade_culled) cudaFree(v->shade_culled);
+        v->shade_culled = nullptr;
+        v->shade_cap = 0;
+        const cudaError_t e = dmalloc(&v->shade_culled, sizeof(uint32_t) * size_t(cap));
+        if (e != cudaSuccess) return cuda_status(e);
+        v->shade_cap = cap;
+    }
+    if (!v->shade_chunks) {
+        cudaError_t e = dmalloc(&v->shade_chunks, sizeof(uint32_t) * 40 * 40 * 40);
+        if (e == cudaSuccess) e = dmalloc(&v->shade_scratch, sizeof(uint32_t) * (40 * 40 * 40 + 1));
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    // quad-packed SDF copies for the march variants that read them
+    const int mv = v->desc.march_variant;
+    const size_t mq = (mv == 3 || mv == 4) ? quad_bytes(sdf->mip_resolution * C, sdf->mip_resolution,
+                                                         sdf->mip_resolution, sdf->format) : 0;
+    const size_t sq = (mv == 4) ? quad_bytes(sdf->resolution * C, sdf->resolution, sdf->resolution, sdf->format) : 0;
+    if (mq != v->mip_quad_bytes) {
+        if (v->mip_quad) cudaFree(v->mip_quad);
+        v->mip_quad = nullptr;
+        v->mip_quad_bytes = 0;
+        if (mq) {
+            const cudaError_t e = dmalloc(&v->mip_quad, mq);
+            if (e != cudaSuccess) return cuda_status(e);
+            v->mip_quad_bytes = mq;
+        }
+    }
+    if (sq != v->sdf_quad_bytes) {
+        if (v->sdf_quad) cudaFree(v->sdf_quad);
+        v->sdf_quad = nullptr;
+        v->sdf_quad_bytes = 0;
+        if (sq) {
+            const cudaError_t e = dmalloc(&v->sdf_quad, sq);
+            if (e != cudaSuccess) return cuda_status(e);
+            v->sdf_quad_bytes = sq;
+        }
     }
     v->w2l_dirty = true;
     v->sdf = *sdf;

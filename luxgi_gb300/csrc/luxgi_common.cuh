@@ -113,26 +113,72 @@ __device__ __forceinline__ float sample3d(const T* __restrict__ v, int W, int H,
     return c0 * ic + c1 * c;
 }
 
+// Quad-packed volume: texel (x, y, z) for x in [-1, W-1], y in [-1, H-1]
+// holds (v[x, y], v[x+1, y], v[x, y+1], v[x+1, y+1]) of plane z with the
+// indices clamped to the volume, at [z][y + 1][x + 1] of a (W+1) x (H+1) x D
+// array.  A GL trilinear sample with clamp-to-edge needs two of them (planes
+// z0 and z1) and reads exactly the values of the eight-tap form.
+template <typename T> struct Quad;
+template <> struct Quad<float> { using type = float4; };
+template <> struct Quad<__half> { using type = uint2; };
+
+__device__ __forceinline__ void quad_vals(const float4& q, float* o) { o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.w; }
+__device__ __forceinline__ void quad_vals(const uint2& q, float* o) {
+    const __half2 a = *reinterpret_cast<const __half2*>(&q.x);
+    const __half2 b = *reinterpret_cast<const __half2*>(&q.y);
+    o[0] = __low2float(a); o[1] = __high2float(a); o[2] = __low2float(b); o[3] = __high2float(b);
+}
+
+template <typename T>
+__device__ __forceinline__ float sample3d_quad(const typename Quad<T>::type* __restrict__ q, int W, int H, int D, float u,
+                                               float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    const float a = x - fx, b = y - fy, c = z - fz;
+    const int qx = imn(imx(int(fx), -1), W - 1) + 1, qy = imn(imx(int(fy), -1), H - 1) + 1;
+    const int z0 = imn(imx(int(fz), 0), D - 1), z1 = imn(imx(int(fz) + 1, 0), D - 1);
+    const size_t QW = size_t(W) + 1, QWH = QW * (size_t(H) + 1);
+    float p0[4], p1[4];
+    quad_vals(__ldg(q + size_t(z0) * QWH + size_t(qy) * QW + qx), p0);
+    quad_vals(__ldg(q + size_t(z1) * QWH + size_t(qy) * QW + qx), p1);
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float c00 = p0[0] * ia + p0[1] * a, c10 = p0[2] * ia + p0[3] * a;
+    const float c01 = p1[0] * ia + p1[1] * a, c11 = p1[2] * ia + p1[3] * a;
+    const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
 struct SdfView {
     luxgi_sdf_data data;
     const void* sdf;
     const void* mip;
+    const void* sdf_quad;   // quad-packed copies (march variants 3, 4) or nullptr
+    const void* mip_quad;
     int res, mres, C;
     int format;   // luxgi_storage of the sdf/mip texels
 };
 
+// One GL trilinear sample of the full-resolution or mip volume, from the
+// plain layout or from its quad-packed copy (same values either way).
+template <typename T, bool QUAD>
+__device__ __forceinline__ float sample_vol(const void* plain, const void* quad, int W, int H, int D, float u, float v,
+                                            float w) {
+    if (QUAD) return sample3d_quad<T>(static_cast<const typename Quad<T>::type*>(quad), W, H, D, u, v, w);
+    return sample3d(static_cast<const T*>(plain), W, H, D, u, v, w);
+}
+
 // Hit normal: central differences of the full-resolution SDF at +-1/res in
 // packed texture coordinates (SDFCommon.glsl:174-183).  Kept out of line so
-// the march loop's register budget does not carry its 48 taps.
-template <typename T>
-__device__ __noinline__ f3 sdf_normal(const T* __restrict__ tex, int TW, int res, float tu, float uy, float uz,
+// the march loop's register budget does not carry its taps.
+template <typename T, bool QUAD>
+__device__ __noinline__ f3 sdf_normal(const void* tex, const void* texq, int TW, int res, float tu, float uy, float uz,
                                       float off) {
-    const float xp = sample3d(tex, TW, res, res, tu + off, uy, uz);
-    const float xn = sample3d(tex, TW, res, res, tu - off, uy, uz);
-    const float yp = sample3d(tex, TW, res, res, tu, uy + off, uz);
-    const float yn = sample3d(tex, TW, res, res, tu, uy - off, uz);
-    const float zp = sample3d(tex, TW, res, res, tu, uy, uz + off);
-    const float zn = sample3d(tex, TW, res, res, tu, uy, uz - off);
+    const float xp = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu + off, uy, uz);
+    const float xn = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu - off, uy, uz);
+    const float yp = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy + off, uz);
+    const float yn = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy - off, uz);
+    const float zp = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy, uz + off);
+    const float zn = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy, uz - off);
     return norm3(f3{xp - xn, yp - yn, zp - zn});
 }
 
@@ -146,11 +192,10 @@ struct MarchHit {
 };
 
 // tracyGlobalSDF (SDFCommon.glsl:98-194) with stepScale 1, start bias 0,
-// hit normal requested (GISDFRays.comp:79-87).
-template <typename T>
+// hit normal requested (GISDFRays.comp:79-87).  QMIP / QTEX select the
+// quad-packed copies of the mip / full-resolution volume.
+template <typename T, bool QMIP = false, bool QTEX = false>
 __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps) {
-    const T* __restrict__ tex = static_cast<const T*>(s.sdf);
-    const T* __restrict__ mip = static_cast<const T*>(s.mip);
     const int C = s.C;
     const int TW = s.res * C, MW = s.mres * C;
     MarchHit hit;
@@ -197,8 +242,8 @@ __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 di
             // the full-resolution taps are issued together with the mip taps
             // (one memory round trip per step); their value is used only
             // where SDFCommon.glsl:150-158 samples the full-resolution SDF
-            float sd = sample3d(mip, MW, s.mres, s.mres, tu, uy, uz);
-            const float sdt = sample3d(tex, TW, s.res, s.res, tu, uy, uz);
+            float sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
+            const float sdt = sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz);
             if (sd < chunk) {
                 ++hit.fine;
                 if (sdt < margin * 2.0f) sd = sdt;
@@ -211,7 +256,7 @@ __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 di
                 hit.time = mx(t + sd - thick, 0.0f);
                 hit.cascade = cascade;
                 hit.sdf = sd;
-                hit.normal = sdf_normal(tex, TW, s.res, tu, uy, uz, 1.0f / s.data.resolution);
+                hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, tu, uy, uz, 1.0f / s.data.resolution);
                 break;
             }
             t = t + mx(sd * 1.0f, voxel);
@@ -446,6 +491,53 @@ __device__ __forceinline__ float bilinear_repeat(const void* p, int storage, int
     return r0 * (1.0f - b) + r1 * b;
 }
 
+// All NC channels of one atlas texel in one load (NC = 4 irradiance, 2 distance).
+template <int NC>
+__device__ __forceinline__ void atlas_texel(const void* p, int storage, size_t texel, float* out) {
+    if (storage == LUXGI_STORAGE_FP16) {
+        if (NC == 4) {
+            const uint2 raw = __ldg(static_cast<const uint2*>(p) + texel);
+            const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
+            const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
+            out[0] = __low2float(a); out[1] = __high2float(a); out[2] = __low2float(b); out[3] = __high2float(b);
+        } else {
+            const __half2 a = __ldg(static_cast<const __half2*>(p) + texel);
+            out[0] = __low2float(a); out[1] = __high2float(a);
+        }
+    } else {
+        if (NC == 4) {
+            const float4 v = __ldg(static_cast<const float4*>(p) + texel);
+            out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
+        } else {
+            const float2 v = __ldg(static_cast<const float2*>(p) + texel);
+            out[0] = v.x; out[1] = v.y;
+        }
+    }
+}
+
+// textureLod bilinear with REPEAT, all NC channels (same per-channel
+// arithmetic as bilinear_repeat).
+template <int NC>
+__device__ __forceinline__ void bilinear_repeat_v(const void* p, int storage, int W, int H, float u, float v, float* out) {
+    const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    int i0 = int(fx) % W; if (i0 < 0) i0 += W;
+    int i1 = (int(fx) + 1) % W; if (i1 < 0) i1 += W;
+    int j0 = int(fy) % H; if (j0 < 0) j0 += H;
+    int j1 = (int(fy) + 1) % H; if (j1 < 0) j1 += H;
+    float t00[NC], t10[NC], t01[NC], t11[NC];
+    atlas_texel<NC>(p, storage, size_t(j0) * W + i0, t00);
+    atlas_texel<NC>(p, storage, size_t(j0) * W + i1, t10);
+    atlas_texel<NC>(p, storage, size_t(j1) * W + i0, t01);
+    atlas_texel<NC>(p, storage, size_t(j1) * W + i1, t11);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const float r0 = t00[c] * (1.0f - a) + t10[c] * a, r1 = t01[c] * (1.0f - a) + t11[c] * a;
+        out[c] = r0 * (1.0f - b) + r1 * b;
+    }
+}
+
 __device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
 
 // textureCoordFromDirection (DDGICommon.glsl:141-158)
@@ -500,8 +592,10 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         float tu, tv;
         tex_coord_from_dir(mul3(dir, -1.0f), pidx, u.depth_width, u.depth_height, u.depth_probe_side, tu, tv);
         const float dist = len3(ptp);
-        const float mean = bilinear_repeat(A.dist, A.storage, u.depth_width, u.depth_height, 2, tu, tv, 0);
-        const float mean2 = bilinear_repeat(A.dist, A.storage, u.depth_width, u.depth_height, 2, tu, tv, 1);
+        float mm[2];
+        bilinear_repeat_v<2>(A.dist, A.storage, u.depth_width, u.depth_height, tu, tv, mm);
+        const float mean = mm[0];
+        const float mean2 = mm[1];
         const float variance = fabsf(mean * mean - mean2);
         const float dm = mx(dist - mean, 0.0f);
         float cheb = variance / (variance + dm * dm);
@@ -509,9 +603,9 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         weight = weight * ((dist <= mean) ? 1.0f : cheb);
         weight = mx(0.000001f, weight);
         tex_coord_from_dir(N, pidx, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, tu, tv);
-        const f3 pir{powf(bilinear_repeat(A.irr, A.storage, u.irradiance_width, u.irradiance_height, 4, tu, tv, 0), ge),
-                     powf(bilinear_repeat(A.irr, A.storage, u.irradiance_width, u.irradiance_height, 4, tu, tv, 1), ge),
-                     powf(bilinear_repeat(A.irr, A.storage, u.irradiance_width, u.irradiance_height, 4, tu, tv, 2), ge)};
+        float ir[4];
+        bilinear_repeat_v<4>(A.irr, A.storage, u.irradiance_width, u.irradiance_height, tu, tv, ir);
+        const f3 pir{powf(ir[0], ge), powf(ir[1], ge), powf(ir[2], ge)};
         const float crush = 0.2f;
         if (weight < crush) weight = weight * (weight * weight * (1.0f / (crush * crush)));
         weight = weight * (tri.x * tri.y * tri.z);

@@ -158,4 +158,90 @@ cudaError_t launch_cull(const luxgi_surface_data& d, const luxgi_surface_object*
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------- shading lists
+// Per chunk, the objects of the reference list (SDFCulling.comp) that a
+// surface-atlas lookup from inside the chunk can actually accept: the
+// sampler (AtlasCommon.glsl:132-138) skips an object unless the point lies
+// within its box grown by the surface threshold, so an object whose grown
+// box misses the chunk contributes nothing there and is left out.  Edge
+// chunks extend to infinity outwards (lookups clamp into them).  Same
+// layout as the reference lists; the contributions summed in the sampler
+// are unchanged, only fewer objects are visited.
+__device__ __forceinline__ bool shade_candidate(const luxgi_surface_data& d, const luxgi_surface_object* objs, int c,
+                                                uint32_t o, float thr) {
+    const int x = c % kChunksRes, y = (c / kChunksRes) % kChunksRes, z = c / (kChunksRes * kChunksRes);
+    const float cs = d.chunk_size;
+    const int cc[3] = {x, y, z};
+    const float* M = objs[o].transform;
+    const float* e = objs[o].extends;
+    const float slack = 1e-3f * cs;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        // world AABB of the object box [-(e+thr), e+thr] (column-major M)
+        const float h = fabsf(M[0 * 4 + k]) * (e[0] + thr) + fabsf(M[1 * 4 + k]) * (e[1] + thr) +
+                        fabsf(M[2 * 4 + k]) * (e[2] + thr) + slack;
+        const float lo = M[12 + k] - h, hi = M[12 + k] + h;
+        const float cmin = (cc[k] == 0) ? -INFINITY : (float(cc[k]) - kChunksRes * 0.5f) * cs - slack;
+        const float cmax = (cc[k] == kChunksRes - 1) ? INFINITY : (float(cc[k]) - kChunksRes * 0.5f + 1.0f) * cs + slack;
+        if (hi < cmin || lo > cmax) return false;
+    }
+    return true;
+}
+
+__global__ void shade_list_count_kernel(const luxgi_surface_data d, const luxgi_surface_object* __restrict__ objs,
+                                        const uint32_t* __restrict__ ref_chunks, const uint32_t* __restrict__ ref_culled,
+                                        float thr, uint32_t* __restrict__ need) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= kChunks) return;
+    const uint32_t st = ref_chunks[c];
+    uint32_t n = 0;
+    if (st != 0) {
+        const uint32_t cnt = ref_culled[st];
+        if (cnt <= d.objects_count)
+            for (uint32_t i = 0; i < cnt; ++i) n += shade_candidate(d, objs, c, ref_culled[st + 1 + i], thr) ? 1u : 0u;
+    }
+    need[c] = n ? n + 1 : 0;
+}
+
+__global__ void shade_list_fill_kernel(const luxgi_surface_data d, const luxgi_surface_object* __restrict__ objs,
+                                       const uint32_t* __restrict__ ref_chunks, const uint32_t* __restrict__ ref_culled,
+                                       float thr, const uint32_t* __restrict__ start, uint32_t* __restrict__ chunks,
+                                       uint32_t* __restrict__ culled, uint32_t capacity) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= kChunks) return;
+    const uint32_t rs = ref_chunks[c];
+    const uint32_t at = start[c];
+    uint32_t n = 0;
+    if (rs != 0) {
+        const uint32_t cnt = ref_culled[rs];
+        if (cnt <= d.objects_count)
+            for (uint32_t i = 0; i < cnt; ++i) n += shade_candidate(d, objs, c, ref_culled[rs + 1 + i], thr) ? 1u : 0u;
+    }
+    if (n == 0 || at + n + 1 > capacity) {
+        chunks[c] = 0;
+        return;
+    }
+    culled[at] = n;
+    uint32_t k = at + 1;
+    const uint32_t cnt = ref_culled[rs];
+    for (uint32_t i = 0; i < cnt; ++i) {
+        const uint32_t o = ref_culled[rs + 1 + i];
+        if (shade_candidate(d, objs, c, o, thr)) culled[k++] = o;
+    }
+    chunks[c] = at;
+}
+
+cudaError_t launch_shade_lists(const luxgi_surface_data& d, const luxgi_surface_object* objects,
+                               const uint32_t* ref_chunks, const uint32_t* ref_culled, float thr, uint32_t* chunks,
+                               uint32_t* culled, uint32_t capacity, uint32_t* d_counts, uint32_t* d_status,
+                               cudaStream_t st) {
+    const int threads = 128, blocks = (kChunks + threads - 1) / threads;
+    shade_list_count_kernel<<<blocks, threads, 0, st>>>(d, objects, ref_chunks, ref_culled, thr, d_counts);
+    cull_scan_kernel<<<1, kScanThreads, 0, st>>>(d_counts, culled, capacity, d_status);
+    shade_list_fill_kernel<<<blocks, threads, 0, st>>>(d, objects, ref_chunks, ref_culled, thr, d_counts, chunks, culled,
+                                                       capacity);
+    note_launch(3);
+    return cudaGetLastError();
+}
+
 }  // namespace luxgi

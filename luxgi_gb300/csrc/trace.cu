@@ -2,6 +2,8 @@
 // mode-A light-cache injection (SDFAtlasIndirectLight.frag) and batched
 // sampleIrradiance.  Built with -fmad=false: the march must reproduce the
 // FP32 CPU restatement bit for bit.
+#include <algorithm>
+
 #include <cuda_fp16.h>
 
 #include "luxgi_internal.h"
@@ -38,7 +40,7 @@ cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace
 // with the same ray index, so a warp marches 32 parallel rays from
 // neighbouring probes through nearby SDF texels.  The march is the whole
 // kernel (no shading code): small, low register count, high occupancy.
-template <typename SdfT, int MIN_BLOCKS>
+template <typename SdfT, int MIN_BLOCKS, bool QMIP, bool QTEX>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = int64_t(p.P) * p.R;
@@ -48,7 +50,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParam
     const float4 d4 = __ldg(p.dirs + ray);
     const f3 dir{d4.x, d4.y, d4.z};
     const f3 origin = probe_location(p.u, probe);
-    const MarchHit hit = march_sdf<SdfT>(p.sdf, origin, dir, kWorldSize, p.max_steps);
+    const MarchHit hit = march_sdf<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps);
     int cls = -1;                                          // miss
     if (hit.time >= 0.0f) {
         // GISDFRays.comp:93: a hit at the probe from inside a surface
@@ -140,15 +142,27 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
     const int64_t total = int64_t(p.P) * p.R;
     if (total <= 0) return cudaSuccess;
     const unsigned mblocks = unsigned((total + 255) / 256);
-    // variant 1 bounds the march to 64 registers (4 blocks of 256 per SM),
-    // variant 2 lets it keep all 16 taps of a step in flight
-    const bool bounded = p.march_variant != 2;
-    if (p.sdf.format == LUXGI_STORAGE_FP16) {
-        if (bounded) march_kernel<__half, 4><<<mblocks, 256, 0, st>>>(p);
-        else march_kernel<__half, 1><<<mblocks, 256, 0, st>>>(p);
-    } else {
-        if (bounded) march_kernel<float, 4><<<mblocks, 256, 0, st>>>(p);
-        else march_kernel<float, 1><<<mblocks, 256, 0, st>>>(p);
+    // variants: 1 plain layout, 64 registers (4 blocks of 256 per SM);
+    // 2 plain layout, no register bound; 3 quad-packed mip; 4 quad-packed
+    // mip and full-resolution volume.  All produce identical results.
+    const bool h = p.sdf.format == LUXGI_STORAGE_FP16;
+    switch (p.march_variant) {
+        case 2:
+            if (h) march_kernel<__half, 1, false, false><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 1, false, false><<<mblocks, 256, 0, st>>>(p);
+            break;
+        case 3:
+            if (h) march_kernel<__half, 4, true, false><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 4, true, false><<<mblocks, 256, 0, st>>>(p);
+            break;
+        case 4:
+            if (h) march_kernel<__half, 4, true, true><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 4, true, true><<<mblocks, 256, 0, st>>>(p);
+            break;
+        default:
+            if (h) march_kernel<__half, 4, false, false><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 4, false, false><<<mblocks, 256, 0, st>>>(p);
+            break;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -176,6 +190,46 @@ __global__ void world_to_local_kernel(const luxgi_surface_object* __restrict__ o
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     world_to_local_kernel<<<(n + 127) / 128, 128, 0, st>>>(objs, n, w2l);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ quad pack
+// Quad-packed copy of a W x H x D volume (see Quad / sample3d_quad).
+template <typename T>
+__global__ void quad_pack_kernel(const T* __restrict__ src, int W, int H, int D, typename Quad<T>::type* __restrict__ dst) {
+    const int64_t QW = int64_t(W) + 1, QH = int64_t(H) + 1;
+    const int64_t n = QW * QH * D;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const int qx = int(i % QW), qy = int((i / QW) % QH), z = int(i / (QW * QH));
+        const int x0 = imn(imx(qx - 1, 0), W - 1), x1 = imn(imx(qx, 0), W - 1);
+        const int y0 = imn(imx(qy - 1, 0), H - 1), y1 = imn(imx(qy, 0), H - 1);
+        const size_t pz = size_t(z) * W * H;
+        const T a = src[pz + size_t(y0) * W + x0], b = src[pz + size_t(y0) * W + x1];
+        const T c = src[pz + size_t(y1) * W + x0], d = src[pz + size_t(y1) * W + x1];
+        if constexpr (sizeof(T) == 4) {
+            dst[i] = make_float4(a, b, c, d);
+        } else {
+            __half2 ab = __halves2half2(a, b), cd = __halves2half2(c, d);
+            uint2 q;
+            q.x = *reinterpret_cast<const uint32_t*>(&ab);
+            q.y = *reinterpret_cast<const uint32_t*>(&cd);
+            dst[i] = q;
+        }
+    }
+}
+
+size_t quad_bytes(int W, int H, int D, int format) {
+    return (size_t(W) + 1) * (size_t(H) + 1) * size_t(D) * (format == LUXGI_STORAGE_FP16 ? 8 : 16);
+}
+
+cudaError_t launch_quad_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st) {
+    const int64_t n = (int64_t(W) + 1) * (int64_t(H) + 1) * D;
+    const unsigned blocks = unsigned(std::min<int64_t>((n + 255) / 256, 65535));
+    if (format == LUXGI_STORAGE_FP16)
+        quad_pack_kernel<__half><<<blocks, 256, 0, st>>>(static_cast<const __half*>(src), W, H, D, static_cast<uint2*>(dst));
+    else
+        quad_pack_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(src), W, H, D, static_cast<float4*>(dst));
     note_launch();
     return cudaGetLastError();
 }
