@@ -51,6 +51,8 @@ extern "C" {
 #define LUXGI_ETIMEOUT     -4   /* a bounded device-side wait gave up         */
 #define LUXGI_ENOTBOUND    -5   /* luxgi_ddgi_bind_scene was not called       */
 #define LUXGI_EUNSUPPORTED -6   /* option not available on this device/build  */
+#define LUXGI_ESCRATCH     -7   /* input too large for the static scratch of
+                                   luxgi_sdf_build_mip_noalloc               */
 
 /* ---------------------------------------------------------------- enums */
 enum luxgi_storage {           /* element type of ray buffers and atlases      */
@@ -288,6 +290,24 @@ int luxgi_ddgi_sample_irradiance(const luxgi_ddgi_volume* vol, const float* pos,
  * 823-841): mip (device) from sdf (device), for every cascade.  `tmp` is a
  * device buffer of mres^3 elements. */
 int luxgi_sdf_build_mip(const luxgi_sdf_desc* sdf, void* mip, void* tmp, void* stream);
+
+/* luxgi_sdf_build_mip for callers that cannot allocate device memory: an
+ * engine that hands every byte of device memory out of its own fixed-budget
+ * pool, or a frame loop that must not call cudaMalloc (it can synchronise
+ * the device and stall the render thread).  No counterpart in the
+ * reference: there the mip build's scratch is an engine-owned texture.
+ * The flood-fill scratch plane lives in a 1 MiB static device array inside
+ * the library (held by every GPU that loads the library until the process
+ * exits), so the caller passes only the SDF and the mip.  Limit: mres^3
+ * texels of the SDF's element type must fit in 1 MiB -- a mip of up to 64^3
+ * FP32 texels (SDF resolution <= 256) or 80^3 FP16 texels; larger inputs
+ * return LUXGI_ESCRATCH before anything runs.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All
+ * calls share the one array, so calls that overlap on the GPU (e.g. on two
+ * streams) race; every scratch texel is written before it is read, so no
+ * state carries over between calls.  Allocates nothing. */
+int luxgi_sdf_build_mip_noalloc(const luxgi_sdf_desc* sdf, void* mip, void* stream);
 
 /* SDFCulling.comp: chunk table (40^3 u32, device) and culled-object lists
  * (device, `capacity` u32) for the objects of `surface`.  Layout is

@@ -20,6 +20,7 @@ LUXGI_ECUDA = -3
 LUXGI_ETIMEOUT = -4
 LUXGI_ENOTBOUND = -5
 LUXGI_EUNSUPPORTED = -6
+LUXGI_ESCRATCH = -7
 
 STORAGE_FP32 = 0
 STORAGE_FP16 = 1
@@ -140,6 +141,7 @@ DDGI_API = [
     ("luxgi_ddgi_inject_indirect", c_int, [c_void_p, c_void_p]),
     ("luxgi_ddgi_sample_irradiance", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("luxgi_sdf_build_mip", c_int, [POINTER(SdfDesc), c_void_p, c_void_p, c_void_p]),
+    ("luxgi_sdf_build_mip_noalloc", c_int, [POINTER(SdfDesc), c_void_p, c_void_p]),
     ("luxgi_surface_cull", c_int, [POINTER(SurfaceDesc), c_void_p, c_void_p, c_uint32, c_void_p]),
     ("luxgi_strerror", ctypes.c_char_p, [c_int]),
     ("luxgi_launch_count", c_uint64, []),

@@ -258,6 +258,7 @@ const char* luxgi_strerror(int s) {
         case LUXGI_ETIMEOUT: return "bounded device wait timed out";
         case LUXGI_ENOTBOUND: return "scene not bound";
         case LUXGI_EUNSUPPORTED: return "unsupported option";
+        case LUXGI_ESCRATCH: return "input exceeds the 1 MiB static scratch of luxgi_sdf_build_mip_noalloc";
         default: return "unknown status";
     }
 }

@@ -2,6 +2,8 @@
 // the four flood passes of GlobalDistanceField.cpp:537-573) and the surface
 // chunk culling (SDFCulling.comp).  Built with -fmad=false so the mip and
 // the sphere-vs-chunk tests equal their FP32 CPU restatement bit for bit.
+#include <mutex>
+
 #include <cuda_fp16.h>
 
 #include "luxgi_internal.h"
@@ -244,4 +246,57 @@ cudaError_t launch_shade_lists(const luxgi_surface_data& d, const luxgi_surface_
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------- no-alloc mip build
+// Scratch of luxgi_sdf_build_mip_noalloc: the flood-fill ping-pong plane
+// (mres^3 texels) in a static device array, so the call allocates nothing.
+// 1 MiB holds a 64^3 FP32 or an 80^3 FP16 plane.  Every GPU that loads the
+// library holds it until the process exits.
+static constexpr size_t kMipScratchBytes = size_t(1) << 20;
+static __device__ __align__(256) unsigned char g_mip_scratch[kMipScratchBytes];
+
+namespace {
+constexpr int kMaxScratchDevices = 128;
+std::mutex g_mip_scratch_mu;
+void* g_mip_scratch_addr[kMaxScratchDevices] = {};
+
+// Device address of g_mip_scratch on the current device.  Host code cannot
+// name the array directly (its host symbol is only a stand-in), so the first
+// call on each device looks the address up with that device current and
+// caches it.
+cudaError_t mip_scratch_address(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxScratchDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_mip_scratch_mu);
+    if (!g_mip_scratch_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_mip_scratch);
+        if (e != cudaSuccess) return e;
+        g_mip_scratch_addr[dev] = p;
+    }
+    *out = g_mip_scratch_addr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
 }  // namespace luxgi
+
+extern "C" int luxgi_sdf_build_mip_noalloc(const luxgi_sdf_desc* sdf, void* mip, void* stream) {
+    using namespace luxgi;
+    if (!sdf || !mip || !sdf->sdf) return LUXGI_EINVAL;
+    const int C = int(sdf->data.cascades_count);
+    if (C < 1 || C > 4 || sdf->resolution < 4 || sdf->resolution % 4 != 0 ||
+        sdf->mip_resolution != sdf->resolution / 4)
+        return LUXGI_EINVAL;
+    if (sdf->format != LUXGI_STORAGE_FP32 && sdf->format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    const size_t m = size_t(sdf->mip_resolution);
+    const size_t need = m * m * m * (sdf->format == LUXGI_STORAGE_FP16 ? 2 : 4);
+    if (need > kMipScratchBytes) return LUXGI_ESCRATCH;
+    void* tmp = nullptr;
+    cudaError_t e = mip_scratch_address(&tmp);
+    if (e == cudaSuccess) e = launch_mip(*sdf, mip, tmp, static_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess) return LUXGI_OK;
+    return e == cudaErrorMemoryAllocation ? LUXGI_ENOMEM : LUXGI_ECUDA;
+}
+
