@@ -181,10 +181,12 @@ typedef struct luxgi_ddgi_volume_desc {
     int32_t infinite_bounce;       /* IrradianceVolume::infiniteBounce        */
     float   intensity;             /* IrradianceVolume::intensity             */
     float   sky_radiance[3];       /* constant sky for misses                 */
-    int32_t march_variant;         /* tuning: 0 = default, 1 = occupancy-bound
-                                      march (64 registers), 2 = latency-bound
-                                      march (no register bound); results are
-                                      identical, only speed differs          */
+    int32_t march_variant;         /* tuning, results identical, speed differs:
+                                      0 default (= 1); 1 plain SDF layout,
+                                      64-register march; 2 plain, no register
+                                      bound; 3 quad-packed mip; 4 quad-packed
+                                      mip + SDF (4x SDF memory); 5 quad-packed
+                                      mip + pair-packed SDF (2x SDF memory)  */
     int32_t reserved[7];
 } luxgi_ddgi_volume_desc;
 

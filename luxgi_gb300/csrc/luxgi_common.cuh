@@ -148,37 +148,73 @@ __device__ __forceinline__ float sample3d_quad(const typename Quad<T>::type* __r
     return c0 * ic + c1 * c;
 }
 
+// Pair-packed volume: texel (x, y, z) for x in [-1, W-1] holds
+// (v[x, y, z], v[x+1, y, z]) with x clamped, at [z][y][x + 1] of a
+// (W+1) x H x D array: a trilinear sample is four paired loads.
+template <typename T> struct Pair;
+template <> struct Pair<float> { using type = float2; };
+template <> struct Pair<__half> { using type = __half2; };
+__device__ __forceinline__ void pair_vals(const float2& q, float* o) { o[0] = q.x; o[1] = q.y; }
+__device__ __forceinline__ void pair_vals(const __half2& q, float* o) { o[0] = __low2float(q); o[1] = __high2float(q); }
+
+template <typename T>
+__device__ __forceinline__ float sample3d_pair(const typename Pair<T>::type* __restrict__ q, int W, int H, int D, float u,
+                                               float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    const float a = x - fx, b = y - fy, c = z - fz;
+    const int px = imn(imx(int(fx), -1), W - 1) + 1;
+    const int y0 = imn(imx(int(fy), 0), H - 1), y1 = imn(imx(int(fy) + 1, 0), H - 1);
+    const int z0 = imn(imx(int(fz), 0), D - 1), z1 = imn(imx(int(fz) + 1, 0), D - 1);
+    const size_t PW = size_t(W) + 1, PWH = PW * size_t(H);
+    float r00[2], r10[2], r01[2], r11[2];
+    pair_vals(__ldg(q + size_t(z0) * PWH + size_t(y0) * PW + px), r00);
+    pair_vals(__ldg(q + size_t(z0) * PWH + size_t(y1) * PW + px), r10);
+    pair_vals(__ldg(q + size_t(z1) * PWH + size_t(y0) * PW + px), r01);
+    pair_vals(__ldg(q + size_t(z1) * PWH + size_t(y1) * PW + px), r11);
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float c00 = r00[0] * ia + r00[1] * a, c10 = r10[0] * ia + r10[1] * a;
+    const float c01 = r01[0] * ia + r01[1] * a, c11 = r11[0] * ia + r11[1] * a;
+    const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
+// Volume layouts a march variant reads
+enum VolLayout { kPlain = 0, kQuad = 1, kPair = 2 };
+
 struct SdfView {
     luxgi_sdf_data data;
     const void* sdf;
     const void* mip;
-    const void* sdf_quad;   // quad-packed copies (march variants 3, 4) or nullptr
-    const void* mip_quad;
+    const void* sdf_quad;   // packed copy of the full-resolution volume (quad or
+                            // pair layout, march variants 4 / 5) or nullptr
+    const void* mip_quad;   // quad-packed mip (variants 3-5) or nullptr
     int res, mres, C;
     int format;   // luxgi_storage of the sdf/mip texels
 };
 
 // One GL trilinear sample of the full-resolution or mip volume, from the
 // plain layout or from its quad-packed copy (same values either way).
-template <typename T, bool QUAD>
-__device__ __forceinline__ float sample_vol(const void* plain, const void* quad, int W, int H, int D, float u, float v,
+template <typename T, int LAYOUT>
+__device__ __forceinline__ float sample_vol(const void* plain, const void* packed, int W, int H, int D, float u, float v,
                                             float w) {
-    if (QUAD) return sample3d_quad<T>(static_cast<const typename Quad<T>::type*>(quad), W, H, D, u, v, w);
+    if (LAYOUT == kQuad) return sample3d_quad<T>(static_cast<const typename Quad<T>::type*>(packed), W, H, D, u, v, w);
+    if (LAYOUT == kPair) return sample3d_pair<T>(static_cast<const typename Pair<T>::type*>(packed), W, H, D, u, v, w);
     return sample3d(static_cast<const T*>(plain), W, H, D, u, v, w);
 }
 
 // Hit normal: central differences of the full-resolution SDF at +-1/res in
 // packed texture coordinates (SDFCommon.glsl:174-183).  Kept out of line so
 // the march loop's register budget does not carry its taps.
-template <typename T, bool QUAD>
+template <typename T, int LAYOUT>
 __device__ __noinline__ f3 sdf_normal(const void* tex, const void* texq, int TW, int res, float tu, float uy, float uz,
                                       float off) {
-    const float xp = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu + off, uy, uz);
-    const float xn = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu - off, uy, uz);
-    const float yp = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy + off, uz);
-    const float yn = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy - off, uz);
-    const float zp = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy, uz + off);
-    const float zn = sample_vol<T, QUAD>(tex, texq, TW, res, res, tu, uy, uz - off);
+    const float xp = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu + off, uy, uz);
+    const float xn = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu - off, uy, uz);
+    const float yp = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy + off, uz);
+    const float yn = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy - off, uz);
+    const float zp = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy, uz + off);
+    const float zn = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy, uz - off);
     return norm3(f3{xp - xn, yp - yn, zp - zn});
 }
 
@@ -193,8 +229,8 @@ struct MarchHit {
 
 // tracyGlobalSDF (SDFCommon.glsl:98-194) with stepScale 1, start bias 0,
 // hit normal requested (GISDFRays.comp:79-87).  QMIP / QTEX select the
-// quad-packed copies of the mip / full-resolution volume.
-template <typename T, bool QMIP = false, bool QTEX = false>
+// layouts (VolLayout) read for the mip / full-resolution volume.
+template <typename T, int QMIP = kPlain, int QTEX = kPlain>
 __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps) {
     const int C = s.C;
     const int TW = s.res * C, MW = s.mres * C;
@@ -540,27 +576,49 @@ __device__ __forceinline__ void bilinear_repeat_v(const void* p, int storage, in
 
 __device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
 
-// textureCoordFromDirection (DDGICommon.glsl:141-158)
-__device__ __forceinline__ void tex_coord_from_dir(f3 dir, int probe, int W, int H, int side, float& u, float& v) {
+// textureCoordFromDirection (DDGICommon.glsl:141-158), split into its
+// direction part (octEncode of the normalised direction, scaled to texture
+// units) and its probe part (the cell's top-left corner); tex_coord_from_dir
+// adds them exactly as the shader does.
+__device__ __forceinline__ void oct_texel_offset(f3 dir, int W, int H, int side, float& nx, float& ny) {
     const f3 d = norm3(dir);
     const float l1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
     const float inv = 1.0f / l1;
     float ox = d.x * inv, oy = d.y * inv;
     if (d.z < 0.0f) {
-        const float nx = (1.0f - fabsf(oy)) * sign_nz(ox);
-        const float ny = (1.0f - fabsf(ox)) * sign_nz(oy);
-        ox = nx; oy = ny;
+        const float tx = (1.0f - fabsf(oy)) * sign_nz(ox);
+        const float ty = (1.0f - fabsf(ox)) * sign_nz(oy);
+        ox = tx; oy = ty;
     }
     const float zx = (ox + 1.0f) * 0.5f, zy = (oy + 1.0f) * 0.5f;
+    nx = (zx * float(side)) / float(W);
+    ny = (zy * float(side)) / float(H);
+}
+
+__device__ __forceinline__ void probe_texel_origin(int probe, int W, int H, int side, float nx, float ny, float& u,
+                                                   float& v) {
     const float pwb = float(side) + 2.0f;
-    const float nx = (zx * float(side)) / float(W), ny = (zy * float(side)) / float(H);
     const int ppr = (W - 2) / int(pwb);
     const float tlx = float(probe % ppr) * pwb + 2.0f, tly = float(probe / ppr) * pwb + 2.0f;
     u = tlx / float(W) + nx;
     v = tly / float(H) + ny;
 }
 
-// sampleIrradiance (DDGICommon.glsl:163-233)
+__device__ __forceinline__ void tex_coord_from_dir(f3 dir, int probe, int W, int H, int side, float& u, float& v) {
+    float nx, ny;
+    oct_texel_offset(dir, W, H, side, nx, ny);
+    probe_texel_origin(probe, W, H, side, nx, ny, u, v);
+}
+
+// pow(x, e) of the irradiance decode; x*x*sqrt(x) for the default gamma
+// (e = 2.5), within 1.5 ulp of powf
+__device__ __forceinline__ float pow_decode(float x, float e) {
+    return (e == 2.5f) ? x * x * sqrtf(x) : powf(x, e);
+}
+
+// sampleIrradiance (DDGICommon.glsl:163-233).  The normal-bias vector and
+// the octahedral coordinate of N are the same for the 8 cage probes and are
+// computed once.
 __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, f3 P, f3 N, f3 Wo) {
     const f3 start{u.start_position[0], u.start_position[1], u.start_position[2]};
     const f3 stp{u.step[0], u.step[1], u.step[2]};
@@ -574,6 +632,10 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
     f3 sum{0.0f, 0.0f, 0.0f};
     float sumw = 0.0f;
     const float ge = u.ddgi_gamma * 0.5f;
+    const f3 vb = mul3(add3(N, mul3(Wo, 3.0f)), u.normal_bias);
+    float nnx, nny;
+    // textureCoordFromDirection(normalize(N), ...) (DDGICommon.glsl:213)
+    oct_texel_offset(norm3(N), u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny);
     for (int i = 0; i < 8; ++i) {
         const int off[3] = {i & 1, (i >> 1) & 1, (i >> 2) & 1};
         int g[3];
@@ -586,7 +648,6 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         const float bf = mx(0.0001f, (dot3(dtp, N) + 1.0f) * 0.5f);
         weight = weight * (bf * bf + 0.2f);
         const int pidx = g[0] + g[1] * cnt[0] + g[2] * cnt[0] * cnt[1];
-        const f3 vb = mul3(add3(N, mul3(Wo, 3.0f)), u.normal_bias);
         const f3 ptp = add3(sub3(P, ppos), vb);
         const f3 dir = norm3(mul3(ptp, -1.0f));
         float tu, tv;
@@ -602,10 +663,10 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         cheb = mx(cheb * cheb * cheb, 0.0f);
         weight = weight * ((dist <= mean) ? 1.0f : cheb);
         weight = mx(0.000001f, weight);
-        tex_coord_from_dir(N, pidx, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, tu, tv);
+        probe_texel_origin(pidx, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny, tu, tv);
         float ir[4];
         bilinear_repeat_v<4>(A.irr, A.storage, u.irradiance_width, u.irradiance_height, tu, tv, ir);
-        const f3 pir{powf(ir[0], ge), powf(ir[1], ge), powf(ir[2], ge)};
+        const f3 pir{pow_decode(ir[0], ge), pow_decode(ir[1], ge), pow_decode(ir[2], ge)};
         const float crush = 0.2f;
         if (weight < crush) weight = weight * (weight * weight * (1.0f / (crush * crush)));
         weight = weight * (tri.x * tri.y * tri.z);

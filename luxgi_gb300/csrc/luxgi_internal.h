@@ -55,6 +55,8 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 size_t quad_bytes(int W, int H, int D, int format);
 cudaError_t launch_quad_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);
+size_t pair_bytes(int W, int H, int D, int format);
+cudaError_t launch_pair_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);
 cudaError_t launch_shade_lists(const luxgi_surface_data& d, const luxgi_surface_object* objects,
                                const uint32_t* ref_chunks, const uint32_t* ref_culled, float thr, uint32_t* chunks,
                                uint32_t* culled, uint32_t capacity, uint32_t* d_counts, uint32_t* d_status,

@@ -40,7 +40,7 @@ cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace
 // with the same ray index, so a warp marches 32 parallel rays from
 // neighbouring probes through nearby SDF texels.  The march is the whole
 // kernel (no shading code): small, low register count, high occupancy.
-template <typename SdfT, int MIN_BLOCKS, bool QMIP, bool QTEX>
+template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = int64_t(p.P) * p.R;
@@ -144,24 +144,29 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
     const unsigned mblocks = unsigned((total + 255) / 256);
     // variants: 1 plain layout, 64 registers (4 blocks of 256 per SM);
     // 2 plain layout, no register bound; 3 quad-packed mip; 4 quad-packed
-    // mip and full-resolution volume.  All produce identical results.
+    // mip and full-resolution volume; 5 quad-packed mip, pair-packed
+    // full-resolution volume.  All produce identical results.
     const bool h = p.sdf.format == LUXGI_STORAGE_FP16;
     switch (p.march_variant) {
         case 2:
-            if (h) march_kernel<__half, 1, false, false><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 1, false, false><<<mblocks, 256, 0, st>>>(p);
+            if (h) march_kernel<__half, 1, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 1, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
             break;
         case 3:
-            if (h) march_kernel<__half, 4, true, false><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 4, true, false><<<mblocks, 256, 0, st>>>(p);
+            if (h) march_kernel<__half, 4, kQuad, kPlain><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 4, kQuad, kPlain><<<mblocks, 256, 0, st>>>(p);
             break;
         case 4:
-            if (h) march_kernel<__half, 4, true, true><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 4, true, true><<<mblocks, 256, 0, st>>>(p);
+            if (h) march_kernel<__half, 4, kQuad, kQuad><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 4, kQuad, kQuad><<<mblocks, 256, 0, st>>>(p);
+            break;
+        case 5:
+            if (h) march_kernel<__half, 4, kQuad, kPair><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 4, kQuad, kPair><<<mblocks, 256, 0, st>>>(p);
             break;
         default:
-            if (h) march_kernel<__half, 4, false, false><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 4, false, false><<<mblocks, 256, 0, st>>>(p);
+            if (h) march_kernel<__half, 4, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
+            else march_kernel<float, 4, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
             break;
     }
     cudaError_t e = cudaGetLastError();
@@ -230,6 +235,36 @@ cudaError_t launch_quad_pack(const void* src, int W, int H, int D, int format, v
         quad_pack_kernel<__half><<<blocks, 256, 0, st>>>(static_cast<const __half*>(src), W, H, D, static_cast<uint2*>(dst));
     else
         quad_pack_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(src), W, H, D, static_cast<float4*>(dst));
+    note_launch();
+    return cudaGetLastError();
+}
+
+// Pair-packed copy of a W x H x D volume (see Pair / sample3d_pair).
+template <typename T>
+__global__ void pair_pack_kernel(const T* __restrict__ src, int W, int H, int D, typename Pair<T>::type* __restrict__ dst) {
+    const int64_t PW = int64_t(W) + 1;
+    const int64_t n = PW * H * D;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const int px = int(i % PW);
+        const int64_t row = i / PW;                      // y + H * z
+        const int x0 = imn(imx(px - 1, 0), W - 1), x1 = imn(imx(px, 0), W - 1);
+        const T a = src[size_t(row) * W + x0], b = src[size_t(row) * W + x1];
+        if constexpr (sizeof(T) == 4) dst[i] = make_float2(a, b);
+        else dst[i] = __halves2half2(a, b);
+    }
+}
+
+size_t pair_bytes(int W, int H, int D, int format) {
+    return (size_t(W) + 1) * size_t(H) * size_t(D) * (format == LUXGI_STORAGE_FP16 ? 4 : 8);
+}
+
+cudaError_t launch_pair_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st) {
+    const int64_t n = (int64_t(W) + 1) * H * D;
+    const unsigned blocks = unsigned(std::min<int64_t>((n + 255) / 256, 65535));
+    if (format == LUXGI_STORAGE_FP16)
+        pair_pack_kernel<__half><<<blocks, 256, 0, st>>>(static_cast<const __half*>(src), W, H, D, static_cast<__half2*>(dst));
+    else
+        pair_pack_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(src), W, H, D, static_cast<float2*>(dst));
     note_launch();
     return cudaGetLastError();
 }
