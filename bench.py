@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline time budget")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--march-variant", type=int, default=None, help="override the volume's march variant (0-2)")
+    ap.add_argument("--march-variant", type=int, default=None, help="override the volume's march variant (0-5)")
+    ap.add_argument("--shade-variant", type=int, default=None, help="override the volume's shade variant (1,2,4,8)")
     return ap.parse_args()
 
 
@@ -190,10 +191,12 @@ def run_ours(args, rank: int, world: int):
     torch.cuda.set_device(local)
     dev_t = torch.device("cuda", local)
     w = WORKLOADS[args.workload]
-    if args.march_variant is not None:
-        from dataclasses import replace
+    from dataclasses import replace
 
+    if args.march_variant is not None:
         w = replace(w, volume=replace(w.volume, march_variant=args.march_variant))
+    if args.shade_variant is not None:
+        w = replace(w, volume=replace(w.volume, shade_variant=args.shade_variant))
     v = w.volume
     P, R = v.probes, v.rays_per_probe
     host = HostScene(w.scene)

@@ -187,7 +187,10 @@ typedef struct luxgi_ddgi_volume_desc {
                                       bound; 3 quad-packed mip; 4 quad-packed
                                       mip + SDF (4x SDF memory); 5 quad-packed
                                       mip + pair-packed SDF (2x SDF memory)  */
-    int32_t reserved[7];
+    int32_t shade_variant;         /* tuning, results identical: cage probes of
+                                      sampleIrradiance per loop iteration
+                                      (0 default = 1; 1, 2, 4 or 8)          */
+    int32_t reserved[6];
 } luxgi_ddgi_volume_desc;
 
 /* Device views of a volume's probe atlases. */

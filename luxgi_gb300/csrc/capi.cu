@@ -195,6 +195,7 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     p.light_mode = d.light_mode;
     p.max_steps = d.max_steps;
     p.march_variant = d.march_variant;
+    p.shade_variant = d.shade_variant;
     p.bounce = (d.infinite_bounce && v->frames != 0) ? 1 : 0;
     p.P = v->P;
     p.R = v->R;
@@ -335,6 +336,9 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
     if (desc->max_steps < 1) return LUXGI_EINVAL;
     if (desc->march_variant < 0 || desc->march_variant > 5) return LUXGI_EINVAL;
+    if (desc->shade_variant != 0 && desc->shade_variant != 1 && desc->shade_variant != 2 &&
+        desc->shade_variant != 4 && desc->shade_variant != 8)
+        return LUXGI_EINVAL;
     if (desc->blend == LUXGI_BLEND_TENSOR && !tc_blend_supported(desc->uniform)) return LUXGI_EUNSUPPORTED;
     luxgi_ddgi_volume* v = new (std::nothrow) luxgi_ddgi_volume();
     if (!v) return LUXGI_ENOMEM;

@@ -619,6 +619,7 @@ __device__ __forceinline__ float pow_decode(float x, float e) {
 // sampleIrradiance (DDGICommon.glsl:163-233).  The normal-bias vector and
 // the octahedral coordinate of N are the same for the 8 cage probes and are
 // computed once.
+template <int UNROLL = 1>
 __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, f3 P, f3 N, f3 Wo) {
     const f3 start{u.start_position[0], u.start_position[1], u.start_position[2]};
     const f3 stp{u.step[0], u.step[1], u.step[2]};
@@ -636,6 +637,9 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
     float nnx, nny;
     // textureCoordFromDirection(normalize(N), ...) (DDGICommon.glsl:213)
     oct_texel_offset(norm3(N), u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny);
+    // UNROLL cage probes per iteration overlap their texel fetches; the sums
+    // still accumulate in probe order 0..7
+#pragma unroll UNROLL
     for (int i = 0; i < 8; ++i) {
         const int off[3] = {i & 1, (i >> 1) & 1, (i >> 2) & 1};
         int g[3];

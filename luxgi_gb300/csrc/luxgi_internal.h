@@ -31,6 +31,7 @@ struct TraceParams {
     float intensity;
     int storage, light_mode, max_steps, bounce;
     int march_variant;
+    int shade_variant;
     int P, R;
 };
 

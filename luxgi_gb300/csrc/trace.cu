@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParam
 // records: sky for misses, zero for rays starting inside geometry, the
 // surface-cache sample (and, per hit, the previous frame's irradiance) for
 // hits; writes the per-ray radiance + distance and the tensor-core operands.
-template <int MODE>
+template <int MODE, int UNROLL>
 __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t total = int64_t(p.P) * p.R;
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
             sample_surface<true>(p.surf, hp, nrm, thr, s0, s1);
             rad = s0;
             if (p.bounce) {
-                const f3 e = sample_irradiance(p.u, p.prev, hp, nrm, mul3(dir, -1.0f));
+                const f3 e = sample_irradiance<UNROLL>(p.u, p.prev, hp, nrm, mul3(dir, -1.0f));
                 const f3 diff{s1.x / kPi, s1.y / kPi, s1.z / kPi};
                 rad = add3(rad, mulv3(mul3(diff, p.intensity), e));
             }
@@ -172,8 +172,16 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const unsigned sblocks = unsigned((total + 127) / 128);
-    if (p.light_mode == LUXGI_LIGHT_PER_HIT) shade_kernel<LUXGI_LIGHT_PER_HIT><<<sblocks, 128, 0, st>>>(p);
-    else shade_kernel<LUXGI_LIGHT_CACHE><<<sblocks, 128, 0, st>>>(p);
+    if (p.light_mode == LUXGI_LIGHT_PER_HIT) {
+        switch (p.shade_variant) {
+            case 2: shade_kernel<LUXGI_LIGHT_PER_HIT, 2><<<sblocks, 128, 0, st>>>(p); break;
+            case 4: shade_kernel<LUXGI_LIGHT_PER_HIT, 4><<<sblocks, 128, 0, st>>>(p); break;
+            case 8: shade_kernel<LUXGI_LIGHT_PER_HIT, 8><<<sblocks, 128, 0, st>>>(p); break;
+            default: shade_kernel<LUXGI_LIGHT_PER_HIT, 1><<<sblocks, 128, 0, st>>>(p); break;
+        }
+    } else {
+        shade_kernel<LUXGI_LIGHT_CACHE, 1><<<sblocks, 128, 0, st>>>(p);   // no per-hit bounce
+    }
     note_launch(2);
     return cudaGetLastError();
 }

@@ -54,6 +54,7 @@ class VolumeSpec:
     intensity: float = 1.0
     sky: tuple = (0.5, 0.6, 0.8)
     march_variant: int = 0
+    shade_variant: int = 0
 
     @property
     def probes(self) -> int:
@@ -91,6 +92,7 @@ class VolumeSpec:
         for k in range(3):
             d.sky_radiance[k] = self.sky[k]
         d.march_variant = self.march_variant
+        d.shade_variant = self.shade_variant
         return d
 
 

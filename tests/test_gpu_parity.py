@@ -361,3 +361,21 @@ def test_march_variants_bit_identical(cuda, fmt):
         outs.append((rad, info.cpu().numpy()))
     for rad, info in outs[1:]:
         assert np.array_equal(rad, outs[0][0]) and np.array_equal(info, outs[0][1])
+
+
+def test_shade_variants_bit_identical(cuda):
+    """Unrolling the cage-probe loop of sampleIrradiance changes scheduling
+    only: the per-hit bounce radiance is identical for every shade variant."""
+    from dataclasses import replace
+
+    outs = []
+    for sv in (1, 2, 4, 8):
+        w = replace(PLAIN_SMALL, volume=replace(PLAIN_SMALL.volume, shade_variant=sv))
+        host, dev, vol, inp = setup(w, debug=False)
+        for f in range(2):
+            vol.update(frame_rotation(51, f))
+        vol.trace(frame_rotation(51, 2))                 # frame 2: bounce on
+        _, rad, _ = vol.rays()
+        outs.append(_np(rad))
+    for r in outs[1:]:
+        assert np.array_equal(r, outs[0])
