@@ -186,7 +186,9 @@ typedef struct luxgi_ddgi_volume_desc {
                                       64-register march; 2 plain, no register
                                       bound; 3 quad-packed mip; 4 quad-packed
                                       mip + SDF (4x SDF memory); 5 quad-packed
-                                      mip + pair-packed SDF (2x SDF memory)  */
+                                      mip + pair-packed SDF (2x SDF memory);
+                                      6-9 as 2-5 with the pooled march (warps
+                                      refill finished lanes from a ray pool) */
     int32_t shade_variant;         /* tuning, results identical: cage probes of
                                       sampleIrradiance per loop iteration
                                       (0 default = 1; 1, 2, 4 or 8)          */

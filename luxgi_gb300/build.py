@@ -25,7 +25,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose FP32 arithmetic must match the CPU restatement bit
 # for bit are built without FMA contraction
 NO_FMAD = {"trace.cu", "setup.cu"}
-CUDA_SOURCES = ["trace.cu", "blend.cu", "blend_tc.cu", "setup.cu", "capi.cu"]
+# shading is compared with the restatement by tolerance: approximate
+# division and square root
+FAST_DIV = {"shade.cu"}
+CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "capi.cu"]
 
 
 def nvcc() -> str:
@@ -68,6 +71,8 @@ def build_cuda(verbose: bool = False) -> Path:
                    "-I", str(CSRC), "-c", str(s), "-o", str(o)]
             if src in NO_FMAD:
                 cmd.insert(1, "-fmad=false")
+            if src in FAST_DIV:
+                cmd[1:1] = ["-prec-div=false", "-prec-sqrt=false"]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

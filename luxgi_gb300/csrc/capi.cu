@@ -163,7 +163,7 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
             if (e != cudaSuccess) return cuda_status(e);
         }
         if (v->sdf_quad) {
-            e = (v->desc.march_variant == 5)
+            e = (v->desc.march_variant == 5 || v->desc.march_variant == 9)
                     ? launch_pair_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st)
                     : launch_quad_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st);
             if (e != cudaSuccess) return cuda_status(e);
@@ -335,7 +335,7 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->light_mode != LUXGI_LIGHT_CACHE && desc->light_mode != LUXGI_LIGHT_PER_HIT) return LUXGI_EINVAL;
     if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
     if (desc->max_steps < 1) return LUXGI_EINVAL;
-    if (desc->march_variant < 0 || desc->march_variant > 5) return LUXGI_EINVAL;
+    if (desc->march_variant < 0 || desc->march_variant > 9) return LUXGI_EINVAL;
     if (desc->shade_variant != 0 && desc->shade_variant != 1 && desc->shade_variant != 2 &&
         desc->shade_variant != 4 && desc->shade_variant != 8)
         return LUXGI_EINVAL;
@@ -435,12 +435,14 @@ int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const
         if (e != cudaSuccess) return cuda_status(e);
     }
     // quad-packed SDF copies for the march variants that read them
+    // (variants 3-5 per-ray threads, 7-9 the pooled march with the same layouts)
     const int mv = v->desc.march_variant;
-    const size_t mq = (mv >= 3) ? quad_bytes(sdf->mip_resolution * C, sdf->mip_resolution, sdf->mip_resolution,
-                                             sdf->format) : 0;
-    const size_t sq = (mv == 4)   ? quad_bytes(sdf->resolution * C, sdf->resolution, sdf->resolution, sdf->format)
-                      : (mv == 5) ? pair_bytes(sdf->resolution * C, sdf->resolution, sdf->resolution, sdf->format)
-                                  : 0;
+    const int layout = mv >= 6 ? mv - 4 : mv;          // 6..9 -> 2..5
+    const size_t mq = (layout >= 3) ? quad_bytes(sdf->mip_resolution * C, sdf->mip_resolution, sdf->mip_resolution,
+                                                 sdf->format) : 0;
+    const size_t sq = (layout == 4)   ? quad_bytes(sdf->resolution * C, sdf->resolution, sdf->resolution, sdf->format)
+                      : (layout == 5) ? pair_bytes(sdf->resolution * C, sdf->resolution, sdf->resolution, sdf->format)
+                                      : 0;
     if (mq != v->mip_quad_bytes) {
         if (v->mip_quad) cudaFree(v->mip_quad);
         v->mip_quad = nullptr;

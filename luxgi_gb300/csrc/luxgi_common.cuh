@@ -384,8 +384,15 @@ template <bool TWO>
 __device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_surface_tile* __restrict__ tl, f3 local,
                                             f3 nrm_local, float thr, f3& acc0, f3& acc1, float& accw) {
     float T[16];
+    {
+        // 96-byte tile records: the matrix sits at a 16-byte-aligned offset
+        const float4* src = reinterpret_cast<const float4*>(tl->transform);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) T[k] = __ldg(&tl->transform[k]);
+        for (int k = 0; k < 4; ++k) {
+            const float4 c = __ldg(src + k);
+            T[4 * k] = c.x; T[4 * k + 1] = c.y; T[4 * k + 2] = c.z; T[4 * k + 3] = c.w;
+        }
+    }
     const f3 n = norm3(mat4_mul_pt(T, nrm_local, 1.0f));
     float nw = clampf(0.0f * n.x + 0.0f * n.y + 1.0f * n.z, 0.0f, 1.0f);
     nw = (nw - 0.05f) / (1.0f - 0.05f);

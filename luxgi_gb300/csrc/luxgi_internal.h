@@ -53,6 +53,7 @@ struct BlendParams {
 cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace, float4* dirs_blend,
                           cudaStream_t st);
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t st);
+cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 size_t quad_bytes(int W, int H, int D, int format);
 cudaError_t launch_quad_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);

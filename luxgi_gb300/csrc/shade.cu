@@ -1,0 +1,108 @@
+// Hit shading of the march records (GISDFRays.comp:89-127): the
+// surface-cache sample and the per-hit infinite bounce.  This translation
+// unit builds with approximate division and square root and with FMA
+// contraction (-prec-div=false -prec-sqrt=false -fmad=true): shading is
+// compared with the CPU restatement by tolerance (2e-5 relative), while the
+// march, whose hit test must reproduce the restatement's branches bit for
+// bit, stays in trace.cu with IEEE arithmetic.
+#include <cuda_fp16.h>
+
+#include "luxgi_internal.h"
+
+namespace luxgi {
+
+// ---------------------------------------------------------------- shade
+// Hit classification and shading of GISDFRays.comp:89-127 from the march
+// records: sky for misses, zero for rays starting inside geometry, the
+// surface-cache sample (and, per hit, the previous frame's irradiance) for
+// hits; writes the per-ray radiance + distance and the tensor-core operands.
+template <int MODE, int UNROLL>
+__global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = int64_t(p.P) * p.R;
+    if (idx >= total) return;
+    const int probe = int(idx % p.P);
+    const int ray = int(idx / p.P);
+    const size_t o = size_t(probe) * p.R + ray;
+    const float4 h = p.hit_t[o];
+    const int cls = p.hit_c[o];
+    f3 rad{0.0f, 0.0f, 0.0f};
+    float dist = kWorldSize;
+    if (cls == -1) {
+        rad = f3{p.sky[0], p.sky[1], p.sky[2]};
+    } else if (cls >= 0) {
+        const float4 d4 = __ldg(p.dirs + ray);
+        const f3 dir{d4.x, d4.y, d4.z};
+        const f3 origin = probe_location(p.u, probe);
+        const f3 nrm{h.y, h.z, h.w};
+        const f3 hp = add3(origin, mul3(dir, h.x));
+        const float vs = p.sdf.data.cascade_voxel_size[cls];
+        const float thr = vs * 1.05f;
+        f3 s0, s1;
+        if (MODE == LUXGI_LIGHT_PER_HIT) {
+            sample_surface<true>(p.surf, hp, nrm, thr, s0, s1);
+            rad = s0;
+            if (p.bounce) {
+                const f3 e = sample_irradiance<UNROLL>(p.u, p.prev, hp, nrm, mul3(dir, -1.0f));
+                const f3 diff{s1.x / kPi, s1.y / kPi, s1.z / kPi};
+                rad = add3(rad, mulv3(mul3(diff, p.intensity), e));
+            }
+        } else {
+            sample_surface<false>(p.surf, hp, nrm, thr, s0, s1);
+            rad = s0;
+        }
+        dist = mx(h.x + vs * 0.5f, 0.0f);
+    }
+    if (p.storage == LUXGI_STORAGE_FP16) {
+        const __half2 rg = __floats2half2_rn(rad.x, rad.y);
+        const __half2 bd = __floats2half2_rn(rad.z, dist);
+        uint2 raw;
+        raw.x = *reinterpret_cast<const uint32_t*>(&rg);
+        raw.y = *reinterpret_cast<const uint32_t*>(&bd);
+        reinterpret_cast<uint2*>(p.out)[o] = raw;
+        rad = f3{__low2float(rg), __high2float(rg), __low2float(bd)};
+        dist = __high2float(bd);
+    } else {
+        reinterpret_cast<float4*>(p.out)[o] = make_float4(rad.x, rad.y, rad.z, dist);
+    }
+    if (p.tc_irr) {
+        // tensor-core operands: radiance rows and the blend's per-ray depth
+        // split into FP16 hi + lo (ProbeUpdate.glsl:204-207)
+        __half* a = p.tc_irr + size_t(probe) * 4 * p.R + ray;
+        a[0] = __float2half_rn(rad.x);
+        a[p.R] = __float2half_rn(rad.y);
+        a[2 * p.R] = __float2half_rn(rad.z);
+        a[3 * p.R] = __float2half_rn(0.0f);
+        float dd = mn(p.u.max_distance, dist - 0.01f);
+        if (dd == -1.0f) dd = p.u.max_distance;
+        const float d2 = dd * dd;
+        const __half dh = __float2half_rn(dd), d2h = __float2half_rn(d2);
+        const __half dl = __float2half_rn(dd - __half2float(dh));
+        const __half d2l = __float2half_rn(d2 - __half2float(d2h));
+        __half* b = p.tc_dist + size_t(probe) * 4 * p.R;
+        b[ray] = dh;
+        b[p.R + ray] = dl;
+        b[2 * p.R + ray] = d2h;
+        b[3 * p.R + ray] = d2l;
+    }
+}
+
+cudaError_t launch_shade(const TraceParams& p, cudaStream_t st) {
+    const int64_t total = int64_t(p.P) * p.R;
+    if (total <= 0) return cudaSuccess;
+    const unsigned sblocks = unsigned((total + 127) / 128);
+    if (p.light_mode == LUXGI_LIGHT_PER_HIT) {
+        switch (p.shade_variant) {
+            case 2: shade_kernel<LUXGI_LIGHT_PER_HIT, 2><<<sblocks, 128, 0, st>>>(p); break;
+            case 4: shade_kernel<LUXGI_LIGHT_PER_HIT, 4><<<sblocks, 128, 0, st>>>(p); break;
+            case 8: shade_kernel<LUXGI_LIGHT_PER_HIT, 8><<<sblocks, 128, 0, st>>>(p); break;
+            default: shade_kernel<LUXGI_LIGHT_PER_HIT, 1><<<sblocks, 128, 0, st>>>(p); break;
+        }
+    } else {
+        shade_kernel<LUXGI_LIGHT_CACHE, 1><<<sblocks, 128, 0, st>>>(p);   // no per-hit bounce
+    }
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace luxgi

@@ -62,85 +62,168 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParam
     if (p.info) p.info[o] = make_int4(hit.steps, hit.time >= 0.0f ? hit.cascade : -1, hit.fine, 0);
 }
 
-// ---------------------------------------------------------------- shade
-// Hit classification and shading of GISDFRays.comp:89-127 from the march
-// records: sky for misses, zero for rays starting inside geometry, the
-// surface-cache sample (and, per hit, the previous frame's irradiance) for
-// hits; writes the per-ray radiance + distance and the tensor-core operands.
-template <int MODE, int UNROLL>
-__global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
-    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+// ------------------------------------------------------- pooled march
+// Warp-cooperative step scheduling: each warp owns a pool of 32 * POOL
+// consecutive rays; a lane whose ray ends takes the next one from the pool
+// at once, so lanes do not idle while the warp's longest ray finishes.  The
+// per-ray arithmetic is exactly march_sdf's (SDFCommon.glsl:98-194), kept
+// as a small state machine: a cascade set-up phase and a step phase.
+template <typename SdfT, int QMIP, int QTEX, int POOL>
+__global__ void __launch_bounds__(256, 4) march_pool_kernel(const TraceParams p) {
+    const SdfView& s = p.sdf;
+    const int lane = threadIdx.x & 31;
     const int64_t total = int64_t(p.P) * p.R;
-    if (idx >= total) return;
-    const int probe = int(idx % p.P);
-    const int ray = int(idx / p.P);
-    const size_t o = size_t(probe) * p.R + ray;
-    const float4 h = p.hit_t[o];
-    const int cls = p.hit_c[o];
-    f3 rad{0.0f, 0.0f, 0.0f};
-    float dist = kWorldSize;
-    if (cls == -1) {
-        rad = f3{p.sky[0], p.sky[1], p.sky[2]};
-    } else if (cls >= 0) {
+    const int64_t wbase = ((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * (32 * POOL);
+    const int64_t wend = wbase + 32 * POOL < total ? wbase + 32 * POOL : total;
+    const int C = s.C;
+    const int TW = s.res * C, MW = s.mres * C;
+    const float tmax = mn(kWorldSize, s.data.cascade_pos_distance[C - 1][3] * 2.0f);
+    const float chunk = 32.0f / s.data.resolution;
+    const float margin = 4.0f / s.data.resolution;
+    // lane state
+    int64_t cur = wbase + lane;
+    bool has = cur < wend;
+    f3 origin{0.0f, 0.0f, 0.0f}, dir{0.0f, 0.0f, 0.0f}, end{0.0f, 0.0f, 0.0f};
+    float t = 0.0f, is_y = 0.0f, next_start = 0.0f;
+    int cascade = 0, step = 0, steps = 0, fine = 0;
+    bool setup = true;
+    auto begin_ray = [&](int64_t idx) {
+        const int probe = int(idx % p.P), ray = int(idx / p.P);
         const float4 d4 = __ldg(p.dirs + ray);
-        const f3 dir{d4.x, d4.y, d4.z};
-        const f3 origin = probe_location(p.u, probe);
-        const f3 nrm{h.y, h.z, h.w};
-        const f3 hp = add3(origin, mul3(dir, h.x));
-        const float vs = p.sdf.data.cascade_voxel_size[cls];
-        const float thr = vs * 1.05f;
-        f3 s0, s1;
-        if (MODE == LUXGI_LIGHT_PER_HIT) {
-            sample_surface<true>(p.surf, hp, nrm, thr, s0, s1);
-            rad = s0;
-            if (p.bounce) {
-                const f3 e = sample_irradiance<UNROLL>(p.u, p.prev, hp, nrm, mul3(dir, -1.0f));
-                const f3 diff{s1.x / kPi, s1.y / kPi, s1.z / kPi};
-                rad = add3(rad, mulv3(mul3(diff, p.intensity), e));
+        dir = f3{d4.x, d4.y, d4.z};
+        origin = probe_location(p.u, probe);
+        end = add3(origin, mul3(dir, tmax));
+        next_start = 0.0f;
+        cascade = 0;
+        steps = 0;
+        fine = 0;
+        setup = true;
+    };
+    auto finish_ray = [&](int64_t idx, float time, int hc, float hsdf, f3 nrm) {
+        const int probe = int(idx % p.P), ray = int(idx / p.P);
+        int cls = -1;
+        if (time >= 0.0f) cls = (hsdf <= 0.0f && time <= s.data.cascade_voxel_size[0]) ? -2 : hc;
+        const size_t o = size_t(probe) * p.R + ray;
+        p.hit_t[o] = make_float4(time, nrm.x, nrm.y, nrm.z);
+        p.hit_c[o] = cls;
+        if (p.info) p.info[o] = make_int4(steps, time >= 0.0f ? hc : -1, fine, 0);
+    };
+    if (has) begin_ray(cur);
+    int handed = 32;                                  // rays of the pool taken so far (warp-uniform)
+    while (__any_sync(0xffffffffu, has)) {
+        if (has) {
+            const float cx = s.data.cascade_pos_distance[cascade < C ? cascade : 0][0];
+            const float cy = s.data.cascade_pos_distance[cascade < C ? cascade : 0][1];
+            const float cz = s.data.cascade_pos_distance[cascade < C ? cascade : 0][2];
+            const float cw = s.data.cascade_pos_distance[cascade < C ? cascade : 0][3];
+            const float voxel = s.data.cascade_voxel_size[cascade < C ? cascade : 0];
+            const f3 wpos = add3(origin, mul3(dir, voxel * 0.0f));
+            if (setup) {
+                if (cascade >= C) {
+                    finish_ray(cur, -1.0f, 0, 0.0f, f3{0.0f, 0.0f, 0.0f});     // left every cascade: miss
+                    has = false;
+                } else {
+                    // lineHitAABB (SDFCommon.glsl:84-95) and the cascade entry
+                    const f3 d = sub3(end, wpos);
+                    const f3 inv{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+                    const f3 en{((cx - cw) - wpos.x) * inv.x, ((cy - cw) - wpos.y) * inv.y, ((cz - cw) - wpos.z) * inv.z};
+                    const f3 ex{((cx + cw) - wpos.x) * inv.x, ((cy + cw) - wpos.y) * inv.y, ((cz + cw) - wpos.z) * inv.z};
+                    const float i0 = mx(mn(en.x, ex.x), mx(mn(en.y, ex.y), mn(en.z, ex.z)));
+                    const float i1 = mn(mx(en.x, ex.x), mn(mx(en.y, ex.y), mx(en.z, ex.z)));
+                    float is_x = clampf(i0, 0.0f, 1.0f) * tmax;
+                    is_y = clampf(i1, 0.0f, 1.0f) * tmax;
+                    is_x = mx(is_x, next_start);
+                    t = is_x;
+                    if (is_x >= is_y) t = is_y;
+                    else next_start = is_y;
+                    step = 0;
+                    setup = false;
+                }
             }
-        } else {
-            sample_surface<false>(p.surf, hp, nrm, thr, s0, s1);
-            rad = s0;
+            if (has && !setup) {
+                if (step < p.max_steps && t < is_y) {
+                    const float md = cw * 2.0f;
+                    const f3 sp = add3(wpos, mul3(dir, t));
+                    const float ux = clampf((sp.x - cx) / md + 0.5f, 0.0f, 1.0f);
+                    const float uy = clampf((sp.y - cy) / md + 0.5f, 0.0f, 1.0f);
+                    const float uz = clampf((sp.z - cz) / md + 0.5f, 0.0f, 1.0f);
+                    const float tu = (float(cascade) + ux) / float(C);
+                    float sd = sample_vol<SdfT, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
+                    const float sdt = sample_vol<SdfT, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz);
+                    if (sd < chunk) {
+                        ++fine;
+                        if (sdt < margin * 2.0f) sd = sdt;
+                    } else {
+                        sd = chunk;
+                    }
+                    sd = sd * md;
+                    const float thick = (voxel * 0.5f) * clampf(t / voxel, 0.0f, 1.0f);
+                    if (sd < thick) {
+                        const float time = mx(t + sd - thick, 0.0f);
+                        const f3 nrm = sdf_normal<SdfT, QTEX>(s.sdf, s.sdf_quad, TW, s.res, tu, uy, uz,
+                                                             1.0f / s.data.resolution);
+                        steps += step;
+                        finish_ray(cur, time, cascade, sd, nrm);
+                        has = false;
+                    } else {
+                        t = t + mx(sd * 1.0f, voxel);
+                        ++step;
+                    }
+                } else {
+                    steps += step;                     // this cascade is done
+                    ++cascade;
+                    setup = true;
+                }
+            }
         }
-        dist = mx(h.x + vs * 0.5f, 0.0f);
-    }
-    if (p.storage == LUXGI_STORAGE_FP16) {
-        const __half2 rg = __floats2half2_rn(rad.x, rad.y);
-        const __half2 bd = __floats2half2_rn(rad.z, dist);
-        uint2 raw;
-        raw.x = *reinterpret_cast<const uint32_t*>(&rg);
-        raw.y = *reinterpret_cast<const uint32_t*>(&bd);
-        reinterpret_cast<uint2*>(p.out)[o] = raw;
-        rad = f3{__low2float(rg), __high2float(rg), __low2float(bd)};
-        dist = __high2float(bd);
-    } else {
-        reinterpret_cast<float4*>(p.out)[o] = make_float4(rad.x, rad.y, rad.z, dist);
-    }
-    if (p.tc_irr) {
-        // tensor-core operands: radiance rows and the blend's per-ray depth
-        // split into FP16 hi + lo (ProbeUpdate.glsl:204-207)
-        __half* a = p.tc_irr + size_t(probe) * 4 * p.R + ray;
-        a[0] = __float2half_rn(rad.x);
-        a[p.R] = __float2half_rn(rad.y);
-        a[2 * p.R] = __float2half_rn(rad.z);
-        a[3 * p.R] = __float2half_rn(0.0f);
-        float dd = mn(p.u.max_distance, dist - 0.01f);
-        if (dd == -1.0f) dd = p.u.max_distance;
-        const float d2 = dd * dd;
-        const __half dh = __float2half_rn(dd), d2h = __float2half_rn(d2);
-        const __half dl = __float2half_rn(dd - __half2float(dh));
-        const __half d2l = __float2half_rn(d2 - __half2float(d2h));
-        __half* b = p.tc_dist + size_t(probe) * 4 * p.R;
-        b[ray] = dh;
-        b[p.R + ray] = dl;
-        b[2 * p.R + ray] = d2h;
-        b[3 * p.R + ray] = d2l;
+        // refill finished lanes from the warp's pool
+        const unsigned need = __ballot_sync(0xffffffffu, !has);
+        const int avail = 32 * POOL - handed;
+        if (need && avail > 0) {
+            const int rank = __popc(need & ((1u << lane) - 1u));
+            if (!has && rank < avail) {
+                cur = wbase + handed + rank;
+                has = cur < wend;
+                if (has) begin_ray(cur);
+            }
+            const int taken = __popc(need);
+            handed += taken < avail ? taken : avail;
+        }
     }
 }
 
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
     const int64_t total = int64_t(p.P) * p.R;
     if (total <= 0) return cudaSuccess;
+    if (p.march_variant >= 6) {
+        // pooled march: 8 rays per lane, 8 warps per block
+        constexpr int POOL = 8;
+        const int64_t warps = (total + 32 * POOL - 1) / (32 * POOL);
+        const unsigned pblocks = unsigned((warps + 7) / 8);
+        const bool h = p.sdf.format == LUXGI_STORAGE_FP16;
+        switch (p.march_variant) {
+            case 7:
+                if (h) march_pool_kernel<__half, kQuad, kPlain, POOL><<<pblocks, 256, 0, st>>>(p);
+                else march_pool_kernel<float, kQuad, kPlain, POOL><<<pblocks, 256, 0, st>>>(p);
+                break;
+            case 8:
+                if (h) march_pool_kernel<__half, kQuad, kQuad, POOL><<<pblocks, 256, 0, st>>>(p);
+                else march_pool_kernel<float, kQuad, kQuad, POOL><<<pblocks, 256, 0, st>>>(p);
+                break;
+            case 9:
+                if (h) march_pool_kernel<__half, kQuad, kPair, POOL><<<pblocks, 256, 0, st>>>(p);
+                else march_pool_kernel<float, kQuad, kPair, POOL><<<pblocks, 256, 0, st>>>(p);
+                break;
+            default:
+                if (h) march_pool_kernel<__half, kPlain, kPlain, POOL><<<pblocks, 256, 0, st>>>(p);
+                else march_pool_kernel<float, kPlain, kPlain, POOL><<<pblocks, 256, 0, st>>>(p);
+                break;
+        }
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        note_launch();
+        return launch_shade(p, st);
+    }
     const unsigned mblocks = unsigned((total + 255) / 256);
     // variants: 1 plain layout, 64 registers (4 blocks of 256 per SM);
     // 2 plain layout, no register bound; 3 quad-packed mip; 4 quad-packed
@@ -171,19 +254,7 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const unsigned sblocks = unsigned((total + 127) / 128);
-    if (p.light_mode == LUXGI_LIGHT_PER_HIT) {
-        switch (p.shade_variant) {
-            case 2: shade_kernel<LUXGI_LIGHT_PER_HIT, 2><<<sblocks, 128, 0, st>>>(p); break;
-            case 4: shade_kernel<LUXGI_LIGHT_PER_HIT, 4><<<sblocks, 128, 0, st>>>(p); break;
-            case 8: shade_kernel<LUXGI_LIGHT_PER_HIT, 8><<<sblocks, 128, 0, st>>>(p); break;
-            default: shade_kernel<LUXGI_LIGHT_PER_HIT, 1><<<sblocks, 128, 0, st>>>(p); break;
-        }
-    } else {
-        shade_kernel<LUXGI_LIGHT_CACHE, 1><<<sblocks, 128, 0, st>>>(p);   // no per-hit bounce
-    }
-    note_launch(2);
-    return cudaGetLastError();
+    return launch_shade(p, st);
 }
 
 // ------------------------------------------------------- world-to-local

@@ -351,7 +351,7 @@ def test_march_variants_bit_identical(cuda, fmt):
 
     base = tiny_workload(probe_counts=(6, 3, 5), rays=64, sdf=64, sdf_format=fmt, cascades=2, room=20.0, prims=10)
     outs = []
-    for mv in (1, 2, 3, 4, 5):
+    for mv in (1, 2, 3, 4, 5, 6, 7, 8, 9):
         w = replace(base, volume=replace(base.volume, march_variant=mv))
         host, dev, vol, inp = setup(w)
         rot = frame_rotation(50, 0)
