@@ -182,7 +182,7 @@ typedef struct luxgi_ddgi_volume_desc {
     float   intensity;             /* IrradianceVolume::intensity             */
     float   sky_radiance[3];       /* constant sky for misses                 */
     int32_t march_variant;         /* tuning, results identical, speed differs:
-                                      0 default (= 1); 1 plain SDF layout,
+                                      0 default (= 4); 1 plain SDF layout,
                                       64-register march; 2 plain, no register
                                       bound; 3 quad-packed mip; 4 quad-packed
                                       mip + SDF (4x SDF memory); 5 quad-packed

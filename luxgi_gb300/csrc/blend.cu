@@ -25,22 +25,18 @@ namespace luxgi {
 // their own normalisers.
 constexpr int kWeightThreads = 128;
 
-__global__ void __launch_bounds__(kWeightThreads) weights_kernel(
-    const luxgi_ddgi_uniform u, const float4* __restrict__ dirs, float* __restrict__ w_irr, float* __restrict__ w_dist,
-    float* __restrict__ n_irr, float* __restrict__ n_dist, __half* __restrict__ tcw_irr, __half* __restrict__ tcw_dist,
-    int tc_n_irr, int tc_n_dist) {
-    __shared__ float red[2][kWeightThreads];
+__device__ __forceinline__ void weights_row(const BlendParams& p, int row, float (*red)[kWeightThreads]) {
+    const luxgi_ddgi_uniform& u = p.u;
     const int ni = u.irradiance_probe_side, nd = u.depth_probe_side;
     const int Ti = ni * ni, Td = nd * nd;
-    const int R = u.rays_per_probe;
-    const bool tc = tcw_irr != nullptr;
-    const int rows_i = tc ? tc_n_irr : Ti;      // tensor-core rows are padded (>= T)
-    const int row = blockIdx.x;
+    const int R = p.R;
+    const bool tc = p.tcw_irr != nullptr;
+    const int rows_i = tc ? p.tc_ni : Ti;       // tensor-core rows are padded (>= T)
     const bool depth = row >= rows_i;
     const int t = depth ? row - rows_i : row;
     const int n = depth ? nd : ni;
     const int T = depth ? Td : Ti;
-    __half* tcw = depth ? tcw_dist : tcw_irr;
+    __half* tcw = depth ? p.tcw_dist : p.tcw_irr;
     if (t >= T) {                                  // tensor-core padding row
         for (int r = threadIdx.x; r < R; r += blockDim.x) tcw[size_t(t) * R + r] = __float2half_rn(0.0f);
         return;
@@ -55,7 +51,8 @@ __global__ void __launch_bounds__(kWeightThreads) weights_kernel(
         v.x = nx; v.y = ny;
     }
     const f3 td = norm3(v);
-    float* w = depth ? w_dist : w_irr;
+    float* w = depth ? p.w_dist : p.w_irr;
+    const float4* dirs = p.dirs;
     float sum = 0.0f, sum_h = 0.0f;
     for (int r = threadIdx.x; r < R; r += blockDim.x) {
         const float4 d = __ldg(dirs + r);
@@ -81,7 +78,7 @@ __global__ void __launch_bounds__(kWeightThreads) weights_kernel(
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        float* nrm = depth ? n_dist : n_irr;
+        float* nrm = depth ? p.n_dist : p.n_irr;
         sum = red[0][0];
         sum_h = red[1][0];
         nrm[t] = (sum > 1e-8f) ? 1.0f / (2.0f * sum) : 1.0f;
@@ -89,14 +86,34 @@ __global__ void __launch_bounds__(kWeightThreads) weights_kernel(
     }
 }
 
-cudaError_t launch_weights(const luxgi_ddgi_uniform& u, const float4* dirs, float* w_irr, float* w_dist, float* n_irr,
-                           float* n_dist, __half* tc_w_irr, __half* tc_w_dist, int tc_n_irr, int tc_n_dist,
-                           cudaStream_t st) {
-    const int Ti = u.irradiance_probe_side * u.irradiance_probe_side;
-    const int Td = u.depth_probe_side * u.depth_probe_side;
-    const int rows = tc_w_irr ? tc_n_irr + tc_n_dist : Ti + Td;
-    weights_kernel<<<rows, kWeightThreads, 0, st>>>(u, dirs, w_irr, w_dist, n_irr, n_dist, tc_w_irr, tc_w_dist,
-                                                    tc_n_irr, tc_n_dist);
+__global__ void __launch_bounds__(kWeightThreads) weights_kernel(const BlendParams p) {
+    __shared__ float red[2][kWeightThreads];
+    weights_row(p, int(blockIdx.x), red);
+}
+
+__global__ void __launch_bounds__(kWeightThreads)
+    weights_batch_kernel(const BlendParams* __restrict__ vp, const int* __restrict__ starts, int n) {
+    __shared__ float red[2][kWeightThreads];
+    const int v = batch_volume(starts, n, int(blockIdx.x));
+    weights_row(vp[v], int(blockIdx.x) - __ldg(starts + v), red);
+}
+
+// Rows of the weights launch of one volume (texels, or padded tensor-core rows).
+int weight_rows(const BlendParams& p) {
+    const int Ti = p.u.irradiance_probe_side * p.u.irradiance_probe_side;
+    const int Td = p.u.depth_probe_side * p.u.depth_probe_side;
+    return p.tcw_irr ? p.tc_ni + p.tc_nd : Ti + Td;
+}
+
+cudaError_t launch_weights(const BlendParams& p, cudaStream_t st) {
+    weights_kernel<<<weight_rows(p), kWeightThreads, 0, st>>>(p);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weights_batch(const BlendParams* vp, const int* starts, int n, int blocks, cudaStream_t st) {
+    if (blocks <= 0) return cudaSuccess;
+    weights_batch_kernel<<<blocks, kWeightThreads, 0, st>>>(vp, starts, n);
     note_launch();
     return cudaGetLastError();
 }
@@ -149,14 +166,13 @@ constexpr int kPairsPerThread = 4;
 constexpr int kRayChunk = 32;
 
 template <int DEPTH, typename RT, typename AT>
-__global__ void __launch_bounds__(kBlendThreads) blend_kernel(const BlendParams p, int PB) {
-    extern __shared__ float smem[];
+__device__ __forceinline__ void blend_block(const BlendParams& p, int PB, int block, float* smem) {
     const luxgi_ddgi_uniform& u = p.u;
     const int n = DEPTH ? u.depth_probe_side : u.irradiance_probe_side;
     const int T = n * n;
     const int W = DEPTH ? u.depth_width : u.irradiance_width;
     const int R = p.R;
-    const int p0 = blockIdx.x * PB;
+    const int p0 = block * PB;
     float* Ws = smem;                                  // [KC][T]
     float4* Rs = reinterpret_cast<float4*>(smem + kRayChunk * T);   // [PB][KC]
     const float* Wg = DEPTH ? p.w_dist : p.w_irr;
@@ -250,16 +266,83 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(const BlendParams 
     }
 }
 
+template <int DEPTH, typename RT, typename AT>
+__global__ void __launch_bounds__(kBlendThreads) blend_kernel(const BlendParams p, int PB) {
+    extern __shared__ __align__(16) float smem[];
+    blend_block<DEPTH, RT, AT>(p, PB, int(blockIdx.x), smem);
+}
+
 // Probes per block: enough (texel, probe) pairs for every thread, at most
-// 32 probes (their ray chunk is 16 KB of shared memory).
+// pb_cap (32 at most: their ray chunk is 16 KB of shared memory).
 constexpr int kMaxProbesPerBlock = 32;
+
+__host__ __device__ __forceinline__ int blend_probes_per_block(int T, int pb_cap) {
+    int PB = kBlendThreads * kPairsPerThread / T;
+    return PB < 1 ? 1 : (PB > pb_cap ? pb_cap : PB);
+}
+
+// Batched: the volume's probes-per-block follows from its texel count and
+// the launch's cap; parameters staged in shared memory once per block.
+template <int DEPTH, typename RT, typename AT>
+__global__ void __launch_bounds__(kBlendThreads)
+    blend_batch_kernel(const BlendParams* __restrict__ vp, const int* __restrict__ starts, int n, int pb_cap) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ __align__(16) uint32_t sp[sizeof(BlendParams) / 4];
+    const int v = batch_volume(starts, n, int(blockIdx.x));
+    const BlendParams& p = stage_params(vp + v, sp);
+    const int side = DEPTH ? p.u.depth_probe_side : p.u.irradiance_probe_side;
+    blend_block<DEPTH, RT, AT>(p, blend_probes_per_block(side * side, pb_cap), int(blockIdx.x) - __ldg(starts + v),
+                               smem);
+}
+
+size_t blend_smem_bytes(int T, int PB) { return sizeof(float) * kRayChunk * T + sizeof(float4) * PB * kRayChunk; }
+
+int blend_blocks(const BlendParams& p, bool depth, int pb_cap) {
+    const int side = depth ? p.u.depth_probe_side : p.u.irradiance_probe_side;
+    const int PB = blend_probes_per_block(side * side, pb_cap);
+    return (p.P + PB - 1) / PB;
+}
+
+size_t blend_smem(const BlendParams& p, bool depth, int pb_cap) {
+    const int side = depth ? p.u.depth_probe_side : p.u.irradiance_probe_side;
+    return blend_smem_bytes(side * side, blend_probes_per_block(side * side, pb_cap));
+}
+
+template <int DEPTH, typename RT, typename AT>
+static cudaError_t launch_blend_batch_kind(const BlendParams* vp, const int* starts, int n, int blocks, size_t sm,
+                                           int pb_cap, cudaStream_t st) {
+    if (blocks <= 0) return cudaSuccess;
+    if (sm > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(blend_batch_kernel<DEPTH, RT, AT>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        if (e != cudaSuccess) return e;
+    }
+    blend_batch_kernel<DEPTH, RT, AT><<<blocks, kBlendThreads, sm, st>>>(vp, starts, n, pb_cap);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_blend_batch(const BlendParams* vp, const int* starts_irr, int blocks_irr, size_t smem_irr,
+                               const int* starts_dist, int blocks_dist, size_t smem_dist, int n, int pb_cap,
+                               int storage, cudaStream_t st) {
+    if (pb_cap < 1 || pb_cap > kMaxProbesPerBlock) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if (storage == LUXGI_STORAGE_FP16) {
+        e = launch_blend_batch_kind<0, uint2, __half>(vp, starts_irr, n, blocks_irr, smem_irr, pb_cap, st);
+        if (e == cudaSuccess)
+            e = launch_blend_batch_kind<1, uint2, __half>(vp, starts_dist, n, blocks_dist, smem_dist, pb_cap, st);
+    } else {
+        e = launch_blend_batch_kind<0, float4, float>(vp, starts_irr, n, blocks_irr, smem_irr, pb_cap, st);
+        if (e == cudaSuccess)
+            e = launch_blend_batch_kind<1, float4, float>(vp, starts_dist, n, blocks_dist, smem_dist, pb_cap, st);
+    }
+    return e;
+}
 
 template <int DEPTH, typename RT, typename AT>
 static cudaError_t launch_blend_kind(const BlendParams& p, int T, cudaStream_t st) {
-    const int cap = kBlendThreads * kPairsPerThread;
-    int PB = cap / T;
-    PB = PB < 1 ? 1 : (PB > kMaxProbesPerBlock ? kMaxProbesPerBlock : PB);
-    const size_t sm = sizeof(float) * kRayChunk * T + sizeof(float4) * PB * kRayChunk;
+    const int PB = blend_probes_per_block(T, kMaxProbesPerBlock);
+    const size_t sm = blend_smem_bytes(T, PB);
     const unsigned blocks = unsigned((p.P + PB - 1) / PB);
     if (sm > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(blend_kernel<DEPTH, RT, AT>,

@@ -18,6 +18,8 @@
 // overlaps the MMAs of the next.  Every mbarrier wait is bounded by a clock
 // budget; on expiry the kernel raises *status, stops issuing work, drains
 // what it issued and frees its TMEM.
+#include <cstring>
+
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -174,8 +176,7 @@ __device__ __forceinline__ void store_channel(void* atlas, int W, int nc, int n,
 }
 
 template <bool DIST, typename AT>
-__global__ void __launch_bounds__(kThreads, 1)
-tc_blend_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs g) {
+__device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CUtensorMap& map_b, const TcArgs& g) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte aligned carve-out: B blocks, A stages, then barriers
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -338,6 +339,22 @@ tc_blend_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
     if (threadIdx.x == 0 && *abort_flag) atomicOr(g.status, 1u);
 }
 
+template <bool DIST, typename AT>
+__global__ void __launch_bounds__(kThreads, 1)
+tc_blend_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs g) {
+    tc_blend_body<DIST, AT>(map_a, map_b, g);
+}
+
+// Same kernel with the per-frame arguments (ping-pong atlases, first-frame
+// flag) read from device memory, so that a captured graph replays it frame
+// after frame while the host rewrites the arguments.
+template <bool DIST, typename AT>
+__global__ void __launch_bounds__(kThreads, 1)
+tc_blend_dyn_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                    const TcArgs* __restrict__ gd) {
+    tc_blend_body<DIST, AT>(map_a, map_b, *gd);
+}
+
 // ------------------------------------------------------------ host side
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -378,10 +395,10 @@ int num_sms() {
     return n;
 }
 
-template <bool DIST, typename AT>
-cudaError_t launch_one(const TcBlendParams& p, cudaStream_t st) {
+template <bool DIST>
+void fill_args(const TcBlendParams& p, TcArgs& g) {
     const luxgi_ddgi_uniform& u = p.u;
-    TcArgs g;
+    std::memset(&g, 0, sizeof(g));
     g.u = u;
     g.first = p.first;
     g.P = p.P;
@@ -401,20 +418,50 @@ cudaError_t launch_one(const TcBlendParams& p, cudaStream_t st) {
     g.status = p.status;
     const int64_t rows = int64_t(p.P) * g.rows_per_probe;
     g.tiles = int((rows + 127) / 128);
-    CUtensorMap ma, mb;
+}
+
+// Tensor maps, shared memory and grid of one blend kind of one volume.
+template <bool DIST>
+bool plan_kind(const TcBlendParams& p, CUtensorMap& ma, CUtensorMap& mb, size_t& smem, int& grid) {
+    TcArgs g;
+    fill_args<DIST>(p, g);
+    const int64_t rows = int64_t(p.P) * g.rows_per_probe;
     const uint64_t a_inner = DIST ? uint64_t(2) * p.R : uint64_t(p.R);
     if (!make_map(&ma, DIST ? static_cast<const void*>(p.a_dist) : static_cast<const void*>(p.a_irr), a_inner,
                   uint64_t(rows), kKBlock, 128))
-        return cudaErrorNotSupported;
+        return false;
     if (!make_map(&mb, DIST ? static_cast<const void*>(p.w_dist) : static_cast<const void*>(p.w_irr), uint64_t(p.R),
                   uint64_t(g.N), kKBlock, uint32_t(g.N)))
-        return cudaErrorNotSupported;
-    const size_t smem = 1024 + size_t(g.kb_b) * g.N * 128 + size_t(kStages) * kStageBytes + 256;
+        return false;
+    smem = 1024 + size_t(g.kb_b) * g.N * 128 + size_t(kStages) * kStageBytes + 256;
+    grid = g.tiles < num_sms() ? g.tiles : num_sms();
+    return true;
+}
+
+template <bool DIST, typename AT>
+cudaError_t launch_one(const TcBlendParams& p, cudaStream_t st) {
+    TcArgs g;
+    fill_args<DIST>(p, g);
+    CUtensorMap ma, mb;
+    size_t smem = 0;
+    int grid = 0;
+    if (!plan_kind<DIST>(p, ma, mb, smem, grid)) return cudaErrorNotSupported;
     auto kern = tc_blend_kernel<DIST, AT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    const int grid = g.tiles < num_sms() ? g.tiles : num_sms();
     kern<<<grid, kThreads, smem, st>>>(ma, mb, g);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <bool DIST, typename AT>
+cudaError_t launch_dyn(const TcPlan& plan, const void* d_args, cudaStream_t st) {
+    const int k = DIST ? 1 : 0;
+    auto kern = tc_blend_dyn_kernel<DIST, AT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(plan.smem[k]));
+    if (e != cudaSuccess) return e;
+    kern<<<plan.grid[k], kThreads, plan.smem[k], st>>>(plan.ma[k], plan.mb[k],
+                                                      static_cast<const TcArgs*>(d_args) + k);
     note_launch();
     return cudaGetLastError();
 }
@@ -431,6 +478,32 @@ bool tc_blend_supported(const luxgi_ddgi_uniform& u) {
     const int kb = (R + kKBlock - 1) / kKBlock;
     const size_t smem = 1024 + size_t(kb) * (Nd > Ni ? Nd : Ni) * 128 + size_t(kStages) * kStageBytes + 256;
     return smem <= 227 * 1024 && encode_fn() != nullptr;
+}
+
+size_t tc_args_bytes() { return sizeof(TcArgs); }
+
+void tc_fill_args(const TcBlendParams& p, void* out) {
+    TcArgs* g = static_cast<TcArgs*>(out);
+    fill_args<false>(p, g[0]);
+    fill_args<true>(p, g[1]);
+}
+
+bool tc_plan(const TcBlendParams& p, TcPlan& plan) {
+    if (p.P <= 0 || !tc_blend_supported(p.u)) return false;
+    return plan_kind<false>(p, plan.ma[0], plan.mb[0], plan.smem[0], plan.grid[0]) &&
+           plan_kind<true>(p, plan.ma[1], plan.mb[1], plan.smem[1], plan.grid[1]);
+}
+
+cudaError_t launch_tc_blend_dyn(const TcPlan& plan, int storage, const void* d_args, cudaStream_t st) {
+    cudaError_t e;
+    if (storage == LUXGI_STORAGE_FP16) {
+        e = launch_dyn<false, __half>(plan, d_args, st);
+        if (e == cudaSuccess) e = launch_dyn<true, __half>(plan, d_args, st);
+    } else {
+        e = launch_dyn<false, float>(plan, d_args, st);
+        if (e == cudaSuccess) e = launch_dyn<true, float>(plan, d_args, st);
+    }
+    return e;
 }
 
 cudaError_t launch_tc_blend(const TcBlendParams& p, cudaStream_t st) {

@@ -11,7 +11,7 @@
 
 #include <cuda_runtime.h>
 
-#include "luxgi_internal.h"
+#include "luxgi_volume.h"
 
 namespace luxgi {
 static std::atomic<uint64_t> g_launches{0};
@@ -20,55 +20,15 @@ void note_launch(int n) { g_launches.fetch_add(uint64_t(n), std::memory_order_re
 
 using namespace luxgi;
 
-struct luxgi_ddgi_volume {
-    luxgi_ddgi_volume_desc desc;
-    int device = 0;
-    int P = 0, R = 0, Ti = 0, Td = 0;
-    int frames = 0, ping_pong = 0;
-    int debug_rays = 0;
-    bool bound = false;
-    bool tc = false;
-    int tc_ni = 0, tc_nd = 0;      // padded weight rows (multiples of 16)
-    size_t irr_bytes = 0, dist_bytes = 0;
-    void* irr[2] = {nullptr, nullptr};
-    void* dist[2] = {nullptr, nullptr};
-    float4* dirs_trace = nullptr;
-    float4* dirs_blend = nullptr;
-    void* rays = nullptr;
-    int4* info = nullptr;
-    float* w_irr = nullptr;
-    float* w_dist = nullptr;
-    float* n_irr = nullptr;
-    float* n_dist = nullptr;
-    __half* tc_irr = nullptr;
-    __half* tc_dist = nullptr;
-    __half* tcw_irr = nullptr;
-    __half* tcw_dist = nullptr;
-    uint32_t* status = nullptr;
-    float4* hit_t = nullptr;       // march records: time, normal
-    int* hit_c = nullptr;          // march records: cascade / -1 miss / -2 inside
-    float* w2l = nullptr;          // per-object inverse transforms of the bound scene
-    int w2l_cap = 0;
-    bool w2l_dirty = true;
-    uint32_t* shade_chunks = nullptr;   // shading lists (subset of the reference lists)
-    uint32_t* shade_culled = nullptr;
-    uint32_t* shade_scratch = nullptr;  // 40^3 counts + status
-    uint32_t shade_cap = 0;
-    void* sdf_quad = nullptr;           // quad-packed copies for march variants 3, 4
-    void* mip_quad = nullptr;
-    size_t sdf_quad_bytes = 0, mip_quad_bytes = 0;
-    luxgi_sdf_desc sdf{};
-    luxgi_surface_desc surf{};
-};
 
-namespace {
-
-int cuda_status(cudaError_t e) {
+int luxgi::cuda_status(cudaError_t e) {
     if (e == cudaSuccess) return LUXGI_OK;
     if (e == cudaErrorMemoryAllocation) return LUXGI_ENOMEM;
     if (e == cudaErrorNotSupported) return LUXGI_EUNSUPPORTED;
     return LUXGI_ECUDA;
 }
+
+namespace {
 
 int check_uniform(const luxgi_ddgi_uniform& u) {
     for (int k = 0; k < 3; ++k)
@@ -137,41 +97,75 @@ SurfaceView surface_view(const luxgi_surface_desc& s, int light_mode, const floa
 size_t ray_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 8 : 16; }
 size_t atlas_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 2 : 4; }
 
-int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
-    if (!v->bound) return LUXGI_ENOTBOUND;
-    Rot r;
-    for (int i = 0; i < 9; ++i) r.m[i] = rot[i];
-    const luxgi_ddgi_volume_desc& d = v->desc;
-    cudaError_t e = launch_raygen(r, v->R, d.storage, v->dirs_trace, v->dirs_blend, st);
-    if (e != cudaSuccess) return cuda_status(e);
-    e = launch_weights(d.uniform, v->dirs_blend, v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc ? v->tcw_irr : nullptr,
-                       v->tc ? v->tcw_dist : nullptr, v->tc_ni, v->tc_nd, st);
-    if (e != cudaSuccess) return cuda_status(e);
-    if (v->w2l_dirty) {
-        e = launch_world_to_local(v->surf.objects, int(v->surf.data.objects_count), v->w2l, st);
-        if (e != cudaSuccess) return cuda_status(e);
-        float thr = 0.0f;   // largest surface threshold (SDFCommon.glsl:196-199)
-        for (int k = 0; k < int(v->sdf.data.cascades_count); ++k)
-            thr = std::fmax(thr, v->sdf.data.cascade_voxel_size[k] * 1.05f);
-        e = launch_shade_lists(v->surf.data, v->surf.objects, v->surf.chunks, v->surf.culled_objects, thr,
-                               v->shade_chunks, v->shade_culled, v->shade_cap, v->shade_scratch,
-                               v->shade_scratch + 40 * 40 * 40, st);
-        if (e != cudaSuccess) return cuda_status(e);
-        const int C = int(v->sdf.data.cascades_count), res = v->sdf.resolution, mres = v->sdf.mip_resolution;
-        if (v->mip_quad) {
-            e = launch_quad_pack(v->sdf.mip, mres * C, mres, mres, v->sdf.format, v->mip_quad, st);
+}  // namespace
+
+int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
+    // quad-packed SDF copies for the march variants that read them
+    // (variants 3-5 per-ray threads, 7-9 the pooled march with the same layouts)
+    const luxgi_sdf_desc& sdf = v->sdf;
+    const int C = int(sdf.data.cascades_count);
+    const int mv = v->desc.march_variant;
+    const int layout = mv >= 6 ? mv - 4 : mv;          // 6..9 -> 2..5
+    const size_t mq = (layout >= 3) ? quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution,
+                                                 sdf.format) : 0;
+    const size_t sq = (layout == 4)   ? quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format)
+                      : (layout == 5) ? pair_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format)
+                                      : 0;
+    if (mq != v->mip_quad_bytes) {
+        if (v->mip_quad) cudaFree(v->mip_quad);
+        v->mip_quad = nullptr;
+        v->mip_quad_bytes = 0;
+        if (mq) {
+            const cudaError_t e = dmalloc(&v->mip_quad, mq);
             if (e != cudaSuccess) return cuda_status(e);
+            v->mip_quad_bytes = mq;
         }
-        if (v->sdf_quad) {
-            e = (v->desc.march_variant == 5 || v->desc.march_variant == 9)
-                    ? launch_pair_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st)
-                    : launch_quad_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st);
-            if (e != cudaSuccess) return cuda_status(e);
-        }
-        v->w2l_dirty = false;
     }
-    TraceParams p;
+    if (sq != v->sdf_quad_bytes) {
+        if (v->sdf_quad) cudaFree(v->sdf_quad);
+        v->sdf_quad = nullptr;
+        v->sdf_quad_bytes = 0;
+        if (sq) {
+            const cudaError_t e = dmalloc(&v->sdf_quad, sq);
+            if (e != cudaSuccess) return cuda_status(e);
+            v->sdf_quad_bytes = sq;
+        }
+    }
+    v->w2l_dirty = true;
+    return LUXGI_OK;
+}
+
+int luxgi::volume_prepare(luxgi_ddgi_volume* v, cudaStream_t st) {
+    if (!v->bound) return LUXGI_ENOTBOUND;
+    if (!v->w2l_dirty) return LUXGI_OK;
+    cudaError_t e = launch_world_to_local(v->surf.objects, int(v->surf.data.objects_count), v->w2l, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    float thr = 0.0f;   // largest surface threshold (SDFCommon.glsl:196-199)
+    for (int k = 0; k < int(v->sdf.data.cascades_count); ++k)
+        thr = std::fmax(thr, v->sdf.data.cascade_voxel_size[k] * 1.05f);
+    e = launch_shade_lists(v->surf.data, v->surf.objects, v->surf.chunks, v->surf.culled_objects, thr,
+                           v->shade_chunks, v->shade_culled, v->shade_cap, v->shade_scratch,
+                           v->shade_scratch + 40 * 40 * 40, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    const int C = int(v->sdf.data.cascades_count), res = v->sdf.resolution, mres = v->sdf.mip_resolution;
+    if (v->mip_quad) {
+        e = launch_quad_pack(v->sdf.mip, mres * C, mres, mres, v->sdf.format, v->mip_quad, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    if (v->sdf_quad) {
+        e = (v->desc.march_variant == 5 || v->desc.march_variant == 9)
+                ? launch_pair_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st)
+                : launch_quad_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    v->w2l_dirty = false;
+    return LUXGI_OK;
+}
+
+void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], TraceParams& p) {
+    const luxgi_ddgi_volume_desc& d = v->desc;
     std::memset(&p, 0, sizeof(p));
+    for (int i = 0; i < 9; ++i) p.rot.m[i] = rot[i];
     p.u = d.uniform;
     p.sdf = sdf_view(v->sdf);
     p.surf = surface_view(v->surf, d.light_mode, v->w2l);
@@ -185,6 +179,7 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     p.prev.dist = v->dist[v->ping_pong];
     p.prev.storage = d.storage;
     p.dirs = v->dirs_trace;
+    p.dirs_blend = v->dirs_blend;
     p.out = v->rays;
     p.info = v->debug_rays ? v->info : nullptr;
     p.tc_irr = v->tc ? v->tc_irr : nullptr;
@@ -199,36 +194,35 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     p.bounce = (d.infinite_bounce && v->frames != 0) ? 1 : 0;
     p.P = v->P;
     p.R = v->R;
-    return cuda_status(launch_trace(p, st));
 }
 
-int do_probe_update(luxgi_ddgi_volume* v, cudaStream_t st) {
+void luxgi::volume_tc_params(const luxgi_ddgi_volume* v, TcBlendParams& p) {
     const luxgi_ddgi_volume_desc& d = v->desc;
     const int rd = v->ping_pong, wr = 1 - v->ping_pong;
-    if (v->tc) {
-        TcBlendParams p;
-        std::memset(&p, 0, sizeof(p));
-        p.u = d.uniform;
-        p.a_irr = v->tc_irr;
-        p.a_dist = v->tc_dist;
-        p.w_irr = v->tcw_irr;
-        p.w_dist = v->tcw_dist;
-        p.n_irr = v->n_irr + v->Ti;
-        p.n_dist = v->n_dist + v->Td;
-        p.prev_irr = v->irr[rd];
-        p.prev_dist = v->dist[rd];
-        p.out_irr = v->irr[wr];
-        p.out_dist = v->dist[wr];
-        p.status = v->status;
-        p.storage = d.storage;
-        p.first = v->frames == 0;
-        p.P = v->P;
-        p.R = v->R;
-        p.Ni = v->tc_ni;
-        p.Nd = v->tc_nd;
-        return cuda_status(launch_tc_blend(p, st));
-    }
-    BlendParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.u = d.uniform;
+    p.a_irr = v->tc_irr;
+    p.a_dist = v->tc_dist;
+    p.w_irr = v->tcw_irr;
+    p.w_dist = v->tcw_dist;
+    p.n_irr = v->n_irr + v->Ti;
+    p.n_dist = v->n_dist + v->Td;
+    p.prev_irr = v->irr[rd];
+    p.prev_dist = v->dist[rd];
+    p.out_irr = v->irr[wr];
+    p.out_dist = v->dist[wr];
+    p.status = v->status;
+    p.storage = d.storage;
+    p.first = v->frames == 0;
+    p.P = v->P;
+    p.R = v->R;
+    p.Ni = v->tc_ni;
+    p.Nd = v->tc_nd;
+}
+
+void luxgi::volume_blend_params(const luxgi_ddgi_volume* v, BlendParams& p) {
+    const luxgi_ddgi_volume_desc& d = v->desc;
+    const int rd = v->ping_pong, wr = 1 - v->ping_pong;
     std::memset(&p, 0, sizeof(p));
     p.u = d.uniform;
     p.dirs = v->dirs_blend;
@@ -241,10 +235,41 @@ int do_probe_update(luxgi_ddgi_volume* v, cudaStream_t st) {
     p.w_dist = v->w_dist;
     p.n_irr = v->n_irr;
     p.n_dist = v->n_dist;
+    p.tcw_irr = v->tc ? v->tcw_irr : nullptr;
+    p.tcw_dist = v->tc ? v->tcw_dist : nullptr;
+    p.tc_ni = v->tc_ni;
+    p.tc_nd = v->tc_nd;
     p.storage = d.storage;
     p.first = v->frames == 0;
     p.P = v->P;
     p.R = v->R;
+}
+
+namespace {
+
+int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
+    if (!v->bound) return LUXGI_ENOTBOUND;
+    TraceParams p;
+    volume_trace_params(v, rot, p);
+    BlendParams b;
+    volume_blend_params(v, b);
+    cudaError_t e = launch_raygen(p.rot, v->R, v->desc.storage, v->dirs_trace, v->dirs_blend, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    e = launch_weights(b, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    const int s = volume_prepare(v, st);
+    if (s != LUXGI_OK) return s;
+    return cuda_status(launch_trace(p, st));
+}
+
+int do_probe_update(luxgi_ddgi_volume* v, cudaStream_t st) {
+    if (v->tc) {
+        TcBlendParams p;
+        volume_tc_params(v, p);
+        return cuda_status(launch_tc_blend(p, st));
+    }
+    BlendParams p;
+    volume_blend_params(v, p);
     return cuda_status(launch_blend(p, st));
 }
 
@@ -343,6 +368,9 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     luxgi_ddgi_volume* v = new (std::nothrow) luxgi_ddgi_volume();
     if (!v) return LUXGI_ENOMEM;
     v->desc = *desc;
+    // defaults: the variants measured fastest on the production workload
+    if (v->desc.march_variant == 0) v->desc.march_variant = 4;
+    if (v->desc.shade_variant == 0) v->desc.shade_variant = 1;
     cudaGetDevice(&v->device);
     const luxgi_ddgi_uniform& u = desc->uniform;
     v->P = u.probe_counts[0] * u.probe_counts[1] * u.probe_counts[2];
@@ -434,38 +462,11 @@ int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const
         if (e == cudaSuccess) e = dmalloc(&v->shade_scratch, sizeof(uint32_t) * (40 * 40 * 40 + 1));
         if (e != cudaSuccess) return cuda_status(e);
     }
-    // quad-packed SDF copies for the march variants that read them
-    // (variants 3-5 per-ray threads, 7-9 the pooled march with the same layouts)
-    const int mv = v->desc.march_variant;
-    const int layout = mv >= 6 ? mv - 4 : mv;          // 6..9 -> 2..5
-    const size_t mq = (layout >= 3) ? quad_bytes(sdf->mip_resolution * C, sdf->mip_resolution, sdf->mip_resolution,
-                                                 sdf->format) : 0;
-    const size_t sq = (layout == 4)   ? quad_bytes(sdf->resolution * C, sdf->resolution, sdf->resolution, sdf->format)
-                      : (layout == 5) ? pair_bytes(sdf->resolution * C, sdf->resolution, sdf->resolution, sdf->format)
-                                      : 0;
-    if (mq != v->mip_quad_bytes) {
-        if (v->mip_quad) cudaFree(v->mip_quad);
-        v->mip_quad = nullptr;
-        v->mip_quad_bytes = 0;
-        if (mq) {
-            const cudaError_t e = dmalloc(&v->mip_quad, mq);
-            if (e != cudaSuccess) return cuda_status(e);
-            v->mip_quad_bytes = mq;
-        }
-    }
-    if (sq != v->sdf_quad_bytes) {
-        if (v->sdf_quad) cudaFree(v->sdf_quad);
-        v->sdf_quad = nullptr;
-        v->sdf_quad_bytes = 0;
-        if (sq) {
-            const cudaError_t e = dmalloc(&v->sdf_quad, sq);
-            if (e != cudaSuccess) return cuda_status(e);
-            v->sdf_quad_bytes = sq;
-        }
-    }
-    v->w2l_dirty = true;
     v->sdf = *sdf;
     v->surf = *surf;
+    const int st = volume_alloc_packs(v);
+    if (st != LUXGI_OK) return st;
+    v->w2l_dirty = true;
     v->bound = true;
     return LUXGI_OK;
 }

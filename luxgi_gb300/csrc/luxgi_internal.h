@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "luxgi_ddgi.h"
@@ -15,11 +16,13 @@ void note_launch(int n = 1);
 struct Rot { float m[9]; };
 
 struct TraceParams {
+    Rot rot;                 // frame rotation of the ray directions
     luxgi_ddgi_uniform u;
     SdfView sdf;
     SurfaceView surf;
     AtlasView prev;          // previous-frame atlases (mode B bounce)
     const float4* dirs;      // [R] exact FP32 directions
+    float4* dirs_blend;      // [R] directions as the blend reads them (raygen output)
     float4* hit_t;           // [P][R] march result: hit time, normal xyz
     int* hit_c;              // [P][R] hit cascade, -1 miss, -2 inside (GISDFRays.comp:93)
     void* out;               // [P][R] x4 radiance rgb + distance (FP32 or FP16)
@@ -43,15 +46,50 @@ struct BlendParams {
     const void* prev_dist;
     void* out_irr;
     void* out_dist;
-    const float* w_irr;      // [Ti][R] cut weights
-    const float* w_dist;     // [Td][R]
-    const float* n_irr;      // [Ti] 1/(2 sum w) or 1
-    const float* n_dist;     // [Td]
+    float* w_irr;            // [Ti][R] cut weights
+    float* w_dist;           // [Td][R]
+    float* n_irr;            // [Ti] 1/(2 sum w) or 1 (then the tensor-core normalisers)
+    float* n_dist;           // [Td]
+    __half* tcw_irr;         // [tc_ni][R] FP16 tensor-core weights, or nullptr
+    __half* tcw_dist;        // [tc_nd][R]
+    int tc_ni, tc_nd;        // tensor-core weight rows (texels padded to 16)
     int storage, first, P, R;
 };
 
 cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace, float4* dirs_blend,
                           cudaStream_t st);
+
+// ------------------------------------------------------- batched launches
+// One launch covers many volumes: block b belongs to volume v when
+// starts[v] <= b < starts[v + 1] (starts has n + 1 entries, starts[0] = 0),
+// and the volume's parameters are vp[v] in device memory.
+__device__ __forceinline__ int batch_volume(const int* __restrict__ starts, int n, int b) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(starts + mid) <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Copies one parameter block to shared memory (all threads of the block
+// take part) and returns it there.
+template <typename T>
+__device__ __forceinline__ const T& stage_params(const T* __restrict__ src, uint32_t* dst) {
+    static_assert(sizeof(T) % 4 == 0, "parameter blocks are word multiples");
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+    for (int i = threadIdx.x; i < int(sizeof(T) / 4); i += blockDim.x) dst[i] = __ldg(s + i);
+    __syncthreads();
+    return *reinterpret_cast<const T*>(dst);
+}
+
+cudaError_t launch_raygen_batch(const TraceParams* vp, const int* starts, int n, int blocks, cudaStream_t st);
+// variant 1-5 as TraceParams::march_variant; tpb 128 or 256 rays a block
+cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, int blocks, int variant, int tpb,
+                               int sdf_format, cudaStream_t st);
+cudaError_t launch_shade_batch(const TraceParams* vp, const int* starts, int n, int blocks, int light_mode,
+                               int shade_variant, cudaStream_t st);
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
@@ -63,10 +101,17 @@ cudaError_t launch_shade_lists(const luxgi_surface_data& d, const luxgi_surface_
                                const uint32_t* ref_chunks, const uint32_t* ref_culled, float thr, uint32_t* chunks,
                                uint32_t* culled, uint32_t capacity, uint32_t* d_counts, uint32_t* d_status,
                                cudaStream_t st);
-cudaError_t launch_weights(const luxgi_ddgi_uniform& u, const float4* dirs, float* w_irr, float* w_dist,
-                           float* n_irr, float* n_dist, __half* tc_w_irr, __half* tc_w_dist, int tc_n_irr,
-                           int tc_n_dist, cudaStream_t st);
+cudaError_t launch_weights(const BlendParams& p, cudaStream_t st);
 cudaError_t launch_blend(const BlendParams& p, cudaStream_t st);
+// batched weights / blend (block-to-volume maps as above); pb_cap bounds the
+// probes a blend block takes (1-32)
+int weight_rows(const BlendParams& p);
+int blend_blocks(const BlendParams& p, bool depth, int pb_cap);
+size_t blend_smem(const BlendParams& p, bool depth, int pb_cap);
+cudaError_t launch_weights_batch(const BlendParams* vp, const int* starts, int n, int blocks, cudaStream_t st);
+cudaError_t launch_blend_batch(const BlendParams* vp, const int* starts_irr, int blocks_irr, size_t smem_irr,
+                               const int* starts_dist, int blocks_dist, size_t smem_dist, int n, int pb_cap,
+                               int storage, cudaStream_t st);
 cudaError_t launch_border(const luxgi_ddgi_uniform& u, void* irr, void* dist, int storage, cudaStream_t st);
 cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const float* gb0, const float* gb1,
                           const __half* direct, __half* light, const AtlasView& A, int num_tiles, float intensity,
@@ -97,5 +142,19 @@ struct TcBlendParams {
 };
 cudaError_t launch_tc_blend(const TcBlendParams& p, cudaStream_t st);
 bool tc_blend_supported(const luxgi_ddgi_uniform& u);
+
+// Graph-replayable form: tensor maps, shared memory and grids fixed per
+// volume (index 0 irradiance, 1 distance); the per-frame kernel arguments
+// (two blocks of tc_args_bytes(), filled by tc_fill_args) live in device
+// memory at d_args.
+struct TcPlan {
+    CUtensorMap ma[2], mb[2];
+    size_t smem[2];
+    int grid[2];
+};
+bool tc_plan(const TcBlendParams& p, TcPlan& plan);
+size_t tc_args_bytes();
+void tc_fill_args(const TcBlendParams& p, void* out);
+cudaError_t launch_tc_blend_dyn(const TcPlan& plan, int storage, const void* d_args, cudaStream_t st);
 
 }  // namespace luxgi

@@ -1,0 +1,66 @@
+// The volume object behind luxgi_ddgi_volume* (C ABI) and the helpers the
+// single-volume and batched entry points share.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "luxgi_internal.h"
+
+// Everything the reference keeps in DDGIPipelineInternal + DDGIUniform
+// (Engine/DDGI/DDGIRenderer.cpp:85-97) plus the scene-derived caches.
+struct luxgi_ddgi_volume {
+    luxgi_ddgi_volume_desc desc;
+    int device = 0;
+    int P = 0, R = 0, Ti = 0, Td = 0;
+    int frames = 0, ping_pong = 0;
+    int debug_rays = 0;
+    bool bound = false;
+    bool tc = false;
+    int tc_ni = 0, tc_nd = 0;      // padded weight rows (multiples of 16)
+    size_t irr_bytes = 0, dist_bytes = 0;
+    void* irr[2] = {nullptr, nullptr};
+    void* dist[2] = {nullptr, nullptr};
+    float4* dirs_trace = nullptr;
+    float4* dirs_blend = nullptr;
+    void* rays = nullptr;
+    int4* info = nullptr;
+    float* w_irr = nullptr;
+    float* w_dist = nullptr;
+    float* n_irr = nullptr;
+    float* n_dist = nullptr;
+    __half* tc_irr = nullptr;
+    __half* tc_dist = nullptr;
+    __half* tcw_irr = nullptr;
+    __half* tcw_dist = nullptr;
+    uint32_t* status = nullptr;
+    float4* hit_t = nullptr;       // march records: time, normal
+    int* hit_c = nullptr;          // march records: cascade / -1 miss / -2 inside
+    float* w2l = nullptr;          // per-object inverse transforms of the bound scene
+    int w2l_cap = 0;
+    bool w2l_dirty = true;
+    uint32_t* shade_chunks = nullptr;   // shading lists (subset of the reference lists)
+    uint32_t* shade_culled = nullptr;
+    uint32_t* shade_scratch = nullptr;  // 40^3 counts + status
+    uint32_t shade_cap = 0;
+    void* sdf_quad = nullptr;           // quad-packed copies for march variants 3, 4
+    void* mip_quad = nullptr;
+    size_t sdf_quad_bytes = 0, mip_quad_bytes = 0;
+    luxgi_sdf_desc sdf{};
+    luxgi_surface_desc surf{};
+};
+
+
+namespace luxgi {
+
+int cuda_status(cudaError_t e);
+// Scene-derived caches (world-to-local, shading lists, packed SDF copies)
+// for the first trace after a bind or a variant change.
+int volume_prepare(luxgi_ddgi_volume* v, cudaStream_t st);
+// Per-frame kernel parameters of a volume in its current state.
+void volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], TraceParams& p);
+void volume_blend_params(const luxgi_ddgi_volume* v, BlendParams& p);
+void volume_tc_params(const luxgi_ddgi_volume* v, TcBlendParams& p);
+// (Re)allocates the packed SDF copies the volume's march variant reads.
+int volume_alloc_packs(luxgi_ddgi_volume* v);
+
+}  // namespace luxgi

@@ -13,10 +13,8 @@ namespace luxgi {
 // --------------------------------------------------------------- raygen
 // sphericalFibonacci under the frame rotation (GISDFRays.comp:73); one
 // direction per ray index, shared by every probe of the volume.
-__global__ void raygen_kernel(Rot rot, int R, int storage, float4* __restrict__ dirs_trace,
-                              float4* __restrict__ dirs_blend) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
+__device__ __forceinline__ void raygen_ray(const Rot& rot, int R, int storage, float4* __restrict__ dirs_trace,
+                                           float4* __restrict__ dirs_blend, int r) {
     const f3 d = ray_direction(rot.m, r, R);
     dirs_trace[r] = make_float4(d.x, d.y, d.z, 0.0f);
     if (storage == LUXGI_STORAGE_FP16) {
@@ -28,9 +26,33 @@ __global__ void raygen_kernel(Rot rot, int R, int storage, float4* __restrict__ 
     }
 }
 
+__global__ void raygen_kernel(Rot rot, int R, int storage, float4* __restrict__ dirs_trace,
+                              float4* __restrict__ dirs_blend) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    raygen_ray(rot, R, storage, dirs_trace, dirs_blend, r);
+}
+
+// Batched: blocks of 128 rays, volume found from the block index.
+__global__ void __launch_bounds__(128) raygen_batch_kernel(const TraceParams* __restrict__ vp,
+                                                          const int* __restrict__ starts, int n) {
+    const int v = batch_volume(starts, n, int(blockIdx.x));
+    const TraceParams& p = vp[v];
+    const int r = (int(blockIdx.x) - __ldg(starts + v)) * 128 + int(threadIdx.x);
+    if (r >= p.R) return;
+    raygen_ray(p.rot, p.R, p.storage, const_cast<float4*>(p.dirs), p.dirs_blend, r);
+}
+
 cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace, float4* dirs_blend,
                           cudaStream_t st) {
     raygen_kernel<<<(R + 127) / 128, 128, 0, st>>>(rot, R, storage, dirs_trace, dirs_blend);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raygen_batch(const TraceParams* vp, const int* starts, int n, int blocks, cudaStream_t st) {
+    if (blocks <= 0) return cudaSuccess;
+    raygen_batch_kernel<<<blocks, 128, 0, st>>>(vp, starts, n);
     note_launch();
     return cudaGetLastError();
 }
@@ -40,11 +62,8 @@ cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace
 // with the same ray index, so a warp marches 32 parallel rays from
 // neighbouring probes through nearby SDF texels.  The march is the whole
 // kernel (no shading code): small, low register count, high occupancy.
-template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX>
-__global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParams p) {
-    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int64_t total = int64_t(p.P) * p.R;
-    if (idx >= total) return;
+template <typename SdfT, int QMIP, int QTEX>
+__device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
     const int probe = int(idx % p.P);
     const int ray = int(idx / p.P);
     const float4 d4 = __ldg(p.dirs + ray);
@@ -60,6 +79,27 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParam
     p.hit_t[o] = make_float4(hit.time, hit.normal.x, hit.normal.y, hit.normal.z);
     p.hit_c[o] = cls;
     if (p.info) p.info[o] = make_int4(hit.steps, hit.time >= 0.0f ? hit.cascade : -1, hit.fine, 0);
+}
+
+template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX>
+__global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParams p) {
+    const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= int64_t(p.P) * p.R) return;
+    march_ray<SdfT, QMIP, QTEX>(p, idx);
+}
+
+// Batched march over many volumes: TPB rays per block, the volume's
+// parameters staged in shared memory once per block.  Same per-ray code as
+// march_kernel, hence the same results.
+template <typename SdfT, int TPB, int MIN_BLOCKS, int QMIP, int QTEX>
+__global__ void __launch_bounds__(TPB, MIN_BLOCKS)
+    march_batch_kernel(const TraceParams* __restrict__ vp, const int* __restrict__ starts, int n) {
+    __shared__ __align__(16) uint32_t sp[sizeof(TraceParams) / 4];
+    const int v = batch_volume(starts, n, int(blockIdx.x));
+    const TraceParams& p = stage_params(vp + v, sp);
+    const int64_t idx = int64_t(int(blockIdx.x) - __ldg(starts + v)) * TPB + threadIdx.x;
+    if (idx >= int64_t(p.P) * p.R) return;
+    march_ray<SdfT, QMIP, QTEX>(p, idx);
 }
 
 // ------------------------------------------------------- pooled march
@@ -254,7 +294,37 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    note_launch();
     return launch_shade(p, st);
+}
+
+template <typename SdfT, int TPB, int MINB>
+static void march_batch_variant(int variant, unsigned blocks, const TraceParams* vp, const int* starts, int n,
+                                cudaStream_t st) {
+    switch (variant) {
+        case 2: march_batch_kernel<SdfT, TPB, 1, kPlain, kPlain><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
+        case 3: march_batch_kernel<SdfT, TPB, MINB, kQuad, kPlain><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
+        case 4: march_batch_kernel<SdfT, TPB, MINB, kQuad, kQuad><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
+        case 5: march_batch_kernel<SdfT, TPB, MINB, kQuad, kPair><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
+        default: march_batch_kernel<SdfT, TPB, MINB, kPlain, kPlain><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
+    }
+}
+
+cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, int blocks, int variant, int tpb,
+                               int sdf_format, cudaStream_t st) {
+    if (blocks <= 0) return cudaSuccess;
+    if (variant < 1 || variant > 5 || (tpb != 128 && tpb != 256)) return cudaErrorInvalidValue;
+    const bool h = sdf_format == LUXGI_STORAGE_FP16;
+    // bounded variants keep 64 registers a thread (1024 resident threads per SM)
+    if (tpb == 128) {
+        if (h) march_batch_variant<__half, 128, 8>(variant, unsigned(blocks), vp, starts, n, st);
+        else march_batch_variant<float, 128, 8>(variant, unsigned(blocks), vp, starts, n, st);
+    } else {
+        if (h) march_batch_variant<__half, 256, 4>(variant, unsigned(blocks), vp, starts, n, st);
+        else march_batch_variant<float, 256, 4>(variant, unsigned(blocks), vp, starts, n, st);
+    }
+    note_launch();
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------- world-to-local
