@@ -336,6 +336,135 @@ def run_ours(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------- batch
+def run_batch(args, rank: int, world: int):
+    """Batching form: 48 uneven volumes, each with its own FP16 SDF scene,
+    tensor-core blend.  `value` is the batched, graph-replayed, autotuned
+    form; `sequential` the same volumes as 48 plain luxgi_ddgi_update calls
+    per frame on the same GPU."""
+    import numpy as np
+    import torch
+
+    from luxgi_gb300 import DDGIBatch, DDGIVolume, DeviceScene, HostScene, frame_rotation, _native as N
+    from luxgi_gb300.scene import batch_workloads
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev_t = torch.device("cuda", local)
+    count = int(args.workload[len("batch"):] or 48)
+    t0 = time.perf_counter()
+    ws = batch_workloads(count)
+    vols, scenes = [], []
+    for w in ws:
+        host = HostScene(w.scene)
+        dev = DeviceScene(host, w.volume.light_mode, device=f"cuda:{local}")
+        v = DDGIVolume(w.volume)
+        v.bind_scene(dev)
+        scenes.append((host, dev))
+        vols.append(v)
+    setup_s = time.perf_counter() - t0
+    n = len(vols)
+    pr = sum(w.volume.probes * w.volume.rays_per_probe for w in ws)
+    K, W = args.steps, args.warmup
+    seed = 0x5EED + rank
+    rots = [np.stack([frame_rotation(seed + i, f) for i in range(n)]) for f in range(W + K)]
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev_t)
+
+    def timed(step, frames):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in frames]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for (e0, e1), f in zip(ev, frames):
+            flush.zero_()
+            e0.record(stream)
+            step(f)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+        if world > 1:
+            t = torch.tensor([ms], device=dev_t)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    def seq_step(f):
+        for v, r in zip(vols, rots[f]):
+            v.update(r, stream)
+
+    for f in range(W):
+        seq_step(f)
+    seq_ms = timed(seq_step, range(W, W + K))
+
+    batch = DDGIBatch(vols)
+    t0 = time.perf_counter()
+    tuning = batch.autotune(frames=3)
+    tune_s = time.perf_counter() - t0
+
+    def batch_step(f):
+        batch.update(rots[f], stream)
+
+    for f in range(W):
+        batch_step(f)
+    clocks = Clocks(local)
+    launches0 = N.ddgi().luxgi_launch_count()
+    clocks.start()
+    b_ms = timed(batch_step, range(W, W + K))
+    clk = clocks.stop()
+    launches = N.ddgi().luxgi_launch_count() - launches0
+    value = world * pr * K / (b_ms / 1e3)
+    seq_value = world * pr * K / (seq_ms / 1e3)
+
+    # e2e: rotations from the host, every volume's atlases read back to
+    # pinned host memory each frame
+    e2e = None
+    if not args.no_e2e:
+        views = [v.atlases() for v in vols]
+        hosts = [(torch.empty(i.shape, dtype=i.dtype).pin_memory(), torch.empty(d.shape, dtype=d.dtype).pin_memory())
+                 for i, d in views]
+
+        def e2e_step(f):
+            batch.update(rots[f], stream)
+            for v, (ih, dh) in zip(vols, hosts):
+                i, d = v.atlases()
+                ih.copy_(i, non_blocking=True)
+                dh.copy_(d, non_blocking=True)
+            torch.cuda.synchronize()
+
+        for f in range(2):
+            e2e_step(f)
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for f in range(W, W + K):
+            e2e_step(f)
+        te = time.perf_counter() - t0
+        d2h = sum(ih.numel() * ih.element_size() + dh.numel() * dh.element_size() for ih, dh in hosts)
+        e2e = {"value": world * pr * K / te, "unit": "probe-rays/s", "h2d_bytes_per_step": 36 * n,
+               "d2h_bytes_per_step": int(d2h)}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "probe-rays/s", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": round(b_ms / K, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 march, fp16 tensor-core blend operands, fp32 accumulate",
+        "data": "synthetic (seeded analytic scenes, one per volume)",
+        "config": {"workload": f"batch{n}_uneven_fp16sdf_tensorblend", "volumes": n, "probe_rays_per_frame": pr,
+                   "probes": sum(w.volume.probes for w in ws),
+                   "rays_per_probe": sorted({w.volume.rays_per_probe for w in ws}),
+                   "sdf": sorted({w.scene.sdf_resolution for w in ws}),
+                   "atlas": sorted({w.scene.atlas_resolution for w in ws}), "parallelism": f"replicas{world}",
+                   "l2": "256 MB flush between frames (outside the events)"},
+        "sequential": {"value": round(seq_value, 1), "ms_per_step": round(seq_ms / K, 4),
+                       "what": f"{n} luxgi_ddgi_update calls per frame, same volumes and GPU"},
+        "speedup_vs_sequential": round(value / seq_value, 3),
+        "autotune": tuning, "autotune_s": round(tune_s, 2), "setup_s": round(setup_s, 2),
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # -------------------------------------------------------------- reference
 def run_reference(args, rank: int, world: int):
     if rank != 0:
@@ -388,6 +517,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload.startswith("batch"):
+        run_batch(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1 and args.impl == "ours":

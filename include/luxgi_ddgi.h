@@ -260,10 +260,63 @@ int luxgi_ddgi_end_frame(luxgi_ddgi_volume* vol);
 /* One whole frame: trace + probe update (fused border) + end_frame. */
 int luxgi_ddgi_update(luxgi_ddgi_volume* vol, const float rot[9], void* stream);
 
-/* Many volumes, one frame each, in one persistent launch per stage.
- * rots = n consecutive column-major 3x3 matrices (host). */
+/* Many volumes, one frame each.  rots = n consecutive column-major 3x3
+ * matrices (host).  Volumes that share storage, light mode, blend kind, SDF
+ * format and a per-ray march variant (1-5) run together, one launch per
+ * stage for the group; the rest run one after another.  A volume may appear
+ * once.  The reference dispatches every volume separately
+ * (DDGIRenderer.cpp:217-464); this call replaces a loop over those
+ * dispatches.  For repeated frames of the same volumes luxgi_ddgi_batch_*
+ * below adds graph replay and tuning. */
 int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n,
                             const float* rots, void* stream);
+
+/* ------------------------------------------------ batched volume sets
+ * A fixed set of volumes (uneven probe grids and ray counts) updated
+ * together, frame after frame: raygen, weights, march, shade and the FP32
+ * blend are each one launch over all volumes (blocks find their volume by
+ * a block-offset table); the tensor-core blend is one launch pair per
+ * volume on parallel graph branches.  The frame is captured once as a CUDA
+ * graph and replayed; the per-frame arguments (rotations, ping-pong
+ * atlases, first-frame and bounce flags) are written to pinned host memory
+ * and copied in by the graph.  Results equal luxgi_ddgi_update of each
+ * volume alone.  No reference counterpart. */
+typedef struct luxgi_ddgi_batch luxgi_ddgi_batch;
+
+typedef struct luxgi_ddgi_batch_tuning {
+    int32_t march_variant;   /* 1-5, as luxgi_ddgi_volume_desc.march_variant  */
+    int32_t march_threads;   /* rays per march block: 128 or 256              */
+    int32_t shade_variant;   /* 1, 2, 4 or 8                                  */
+    int32_t blend_probes;    /* cap on probes per FP32-blend block, 1-32      */
+    int32_t use_graph;       /* 1 capture + replay a CUDA graph, 0 launch     */
+    int32_t reserved[3];
+    float frame_ms;          /* frame time measured by the autotuner, else 0  */
+} luxgi_ddgi_batch_tuning;
+
+/* All volumes bound, on the current device, with the same storage, light
+ * mode, blend kind and SDF format; none twice.  tuning may be NULL (march
+ * variant 4, 256 rays a block, shade variant 1, 32 probes, graph on).  The
+ * batch sets every volume's march and shade variant to its own (reallocating
+ * the packed SDF copies the variant reads).  Volumes must outlive the batch
+ * and must not be destroyed, re-created or updated concurrently with it. */
+int luxgi_ddgi_batch_create(luxgi_ddgi_volume* const* vols, int n,
+                            const luxgi_ddgi_batch_tuning* tuning,
+                            luxgi_ddgi_batch** out);
+/* One frame of every volume; rots = n column-major 3x3 matrices (host).
+ * Consecutive frames of one batch must be ordered on the GPU (same stream,
+ * or synchronised).  Host-side end_frame of every volume included. */
+int luxgi_ddgi_batch_update(luxgi_ddgi_batch* batch, const float* rots, void* stream);
+/* Times `frames` frames (after 2 warm-up frames) of each candidate tuning
+ * (march variant x rays per block, then shade variant, then blend probes)
+ * with CUDA events on `stream`, applies the fastest and writes it to *best
+ * (may be NULL).  Every volume's atlases, frame count and ping-pong are saved
+ * before and restored after, so results are unchanged by tuning.  Rotations
+ * of the timed frames come from luxgi_ddgi_frame_rotation(seed 0). */
+int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* batch, int frames, void* stream,
+                              luxgi_ddgi_batch_tuning* best);
+int luxgi_ddgi_batch_get_tuning(const luxgi_ddgi_batch* batch, luxgi_ddgi_batch_tuning* out);
+int luxgi_ddgi_batch_set_tuning(luxgi_ddgi_batch* batch, const luxgi_ddgi_batch_tuning* tuning);
+int luxgi_ddgi_batch_destroy(luxgi_ddgi_batch* batch);
 
 int luxgi_ddgi_get_atlases(const luxgi_ddgi_volume* vol, luxgi_ddgi_atlases* out);
 int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* vol, luxgi_ddgi_rays* out);

@@ -5,10 +5,10 @@ the work; this package is the host-side mirror of the reference's DDGI volume
 interface plus the seeded synthetic scene inputs.
 """
 from . import _native
-from .ddgi import DDGIVolume, frame_rotation, rotation, update_batch
+from .ddgi import DDGIBatch, DDGIVolume, frame_rotation, rotation, update_batch
 from .scene import (PLAIN_SMALL, PLAIN_SMALL_REF, PRECISION, PRODUCTION, WORKLOADS, DeviceScene, HostScene,
                     SceneSpec, VolumeSpec, Workload, scaled)
 
-__all__ = ["DDGIVolume", "DeviceScene", "HostScene", "SceneSpec", "VolumeSpec", "Workload", "WORKLOADS",
+__all__ = ["DDGIBatch", "DDGIVolume", "DeviceScene", "HostScene", "SceneSpec", "VolumeSpec", "Workload", "WORKLOADS",
            "PLAIN_SMALL", "PLAIN_SMALL_REF", "PRODUCTION", "PRECISION", "frame_rotation", "rotation",
            "update_batch", "scaled", "_native"]

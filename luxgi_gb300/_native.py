@@ -92,6 +92,11 @@ class Rays(ctypes.Structure):
                 ("rays", c_int32), ("storage", c_int32)]
 
 
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("march_variant", c_int32), ("march_threads", c_int32), ("shade_variant", c_int32),
+                ("blend_probes", c_int32), ("use_graph", c_int32), ("reserved", c_int32 * 3), ("frame_ms", c_float)]
+
+
 class SceneConfig(ctypes.Structure):
     _fields_ = [("seed", c_uint64), ("room_size", c_float), ("wall_thickness", c_float), ("num_primitives", c_int32),
                 ("sphere_radius", c_float * 2), ("box_half_extent", c_float * 2), ("sdf_resolution", c_int32),
@@ -134,6 +139,12 @@ DDGI_API = [
     ("luxgi_ddgi_end_frame", c_int, [c_void_p]),
     ("luxgi_ddgi_update", c_int, [c_void_p, POINTER(c_float), c_void_p]),
     ("luxgi_ddgi_update_batch", c_int, [POINTER(c_void_p), c_int, POINTER(c_float), c_void_p]),
+    ("luxgi_ddgi_batch_create", c_int, [POINTER(c_void_p), c_int, POINTER(BatchTuning), POINTER(c_void_p)]),
+    ("luxgi_ddgi_batch_update", c_int, [c_void_p, POINTER(c_float), c_void_p]),
+    ("luxgi_ddgi_batch_autotune", c_int, [c_void_p, c_int, c_void_p, POINTER(BatchTuning)]),
+    ("luxgi_ddgi_batch_get_tuning", c_int, [c_void_p, POINTER(BatchTuning)]),
+    ("luxgi_ddgi_batch_set_tuning", c_int, [c_void_p, POINTER(BatchTuning)]),
+    ("luxgi_ddgi_batch_destroy", c_int, [c_void_p]),
     ("luxgi_ddgi_get_atlases", c_int, [c_void_p, POINTER(Atlases)]),
     ("luxgi_ddgi_get_rays", c_int, [c_void_p, POINTER(Rays)]),
     ("luxgi_ddgi_check_status", c_int, [c_void_p, c_void_p]),

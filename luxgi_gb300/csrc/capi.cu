@@ -505,15 +505,6 @@ int luxgi_ddgi_update(luxgi_ddgi_volume* v, const float rot[9], void* stream) {
     return luxgi_ddgi_end_frame(v);
 }
 
-int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* rots, void* stream) {
-    if ((!vols && n > 0) || n < 0 || (!rots && n > 0)) return LUXGI_EINVAL;
-    for (int i = 0; i < n; ++i) {
-        int s = luxgi_ddgi_update(vols[i], rots + 9 * i, stream);
-        if (s != LUXGI_OK) return s;
-    }
-    return LUXGI_OK;
-}
-
 int luxgi_ddgi_get_atlases(const luxgi_ddgi_volume* v, luxgi_ddgi_atlases* out) {
     if (!v || !out) return LUXGI_EINVAL;
     const luxgi_ddgi_uniform& u = v->desc.uniform;

@@ -168,3 +168,68 @@ def update_batch(volumes, rots, stream=None) -> None:
     r = np.ascontiguousarray(np.asarray(rots, dtype=np.float32).reshape(n, 9))
     N.check(N.ddgi().luxgi_ddgi_update_batch(hs, n, r.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), _stream(stream)),
             "update_batch")
+
+
+class DDGIBatch:
+    """A fixed set of volumes updated together frame after frame
+    (luxgi_ddgi_batch_*): one launch per stage over all volumes, replayed
+    as a CUDA graph.  The volumes must stay alive while the batch exists."""
+
+    def __init__(self, volumes, tuning: dict | None = None):
+        self.volumes = list(volumes)
+        n = len(self.volumes)
+        hs = (ctypes.c_void_p * n)(*[v.handle.value for v in self.volumes])
+        t = None
+        if tuning is not None:
+            t = N.BatchTuning()
+            for k, v in {**self.default_tuning(), **tuning}.items():
+                setattr(t, k, v)
+        h = ctypes.c_void_p()
+        N.check(N.ddgi().luxgi_ddgi_batch_create(hs, n, ctypes.byref(t) if t is not None else None, ctypes.byref(h)),
+                "batch_create")
+        self._h = h
+
+    @staticmethod
+    def default_tuning() -> dict:
+        return {"march_variant": 4, "march_threads": 256, "shade_variant": 1, "blend_probes": 32, "use_graph": 1}
+
+    def update(self, rots, stream=None) -> None:
+        r = np.ascontiguousarray(np.asarray(rots, dtype=np.float32).reshape(len(self.volumes), 9))
+        N.check(N.ddgi().luxgi_ddgi_batch_update(self._h, r.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                 _stream(stream)), "batch_update")
+
+    def autotune(self, frames: int = 3, stream=None) -> dict:
+        t = N.BatchTuning()
+        N.check(N.ddgi().luxgi_ddgi_batch_autotune(self._h, frames, _stream(stream), ctypes.byref(t)),
+                "batch_autotune")
+        return self._as_dict(t)
+
+    @property
+    def tuning(self) -> dict:
+        t = N.BatchTuning()
+        N.check(N.ddgi().luxgi_ddgi_batch_get_tuning(self._h, ctypes.byref(t)), "batch_get_tuning")
+        return self._as_dict(t)
+
+    @tuning.setter
+    def tuning(self, values: dict) -> None:
+        t = N.BatchTuning()
+        for k, v in {**self.tuning, **values}.items():
+            setattr(t, k, v)
+        N.check(N.ddgi().luxgi_ddgi_batch_set_tuning(self._h, ctypes.byref(t)), "batch_set_tuning")
+
+    @staticmethod
+    def _as_dict(t) -> dict:
+        return {"march_variant": t.march_variant, "march_threads": t.march_threads, "shade_variant": t.shade_variant,
+                "blend_probes": t.blend_probes, "use_graph": t.use_graph, "frame_ms": t.frame_ms}
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            N.ddgi().luxgi_ddgi_batch_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

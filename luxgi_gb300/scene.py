@@ -167,6 +167,36 @@ PRODUCTION_PROFILE = scaled(PRODUCTION, probe_counts=(16, 8, 16), name="producti
 WORKLOADS[PRODUCTION_PROFILE.name] = PRODUCTION_PROFILE
 
 
+# Batching form: many volumes of uneven size, each with its own scene.  Grid
+# dims log-uniform per axis from 4x4x4 to 32x16x32, rays per probe from
+# {64, 128, 192, 256, 288}, FP16 SDF of 64^3-256^3 (multiples of 32; the room
+# grows with it at a 0.25 m voxel), surface-cache atlas of 512^2-2048^2,
+# tensor-core blend.
+BATCH_RAYS = (64, 128, 192, 256, 288)
+
+
+def batch_workloads(count: int = 48, seed: int = SEED0 + 4, max_counts=(32, 16, 32), min_counts=(4, 4, 4),
+                    sdf_range=(64, 256), atlas_range=(512, 2048), blend: int = N.BLEND_TENSOR,
+                    storage: int = N.STORAGE_FP32, max_steps: int = 128) -> list[Workload]:
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        counts = tuple(int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+                       for lo, hi in zip(min_counts, max_counts))
+        rays = int(rng.choice(BATCH_RAYS))
+        res = int(round(math.exp(rng.uniform(math.log(sdf_range[0]), math.log(sdf_range[1]))) / 32.0)) * 32
+        res = min(max(res, sdf_range[0]), sdf_range[1])
+        atlas = int(2 ** round(rng.uniform(math.log2(atlas_range[0]), math.log2(atlas_range[1]))))
+        room = 0.25 * res
+        prims = max(4, int(round(12 * (res / 64.0) ** 1.5)))
+        spacing = 0.8 * room / max(counts)
+        v = VolumeSpec(counts, spacing, rays, max_steps=max_steps, light_mode=N.LIGHT_PER_HIT, blend=blend,
+                       storage=storage)
+        sc = SceneSpec(seed * 1000 + i, room, 0.25 * room / 16.0, prims, res, atlas, sdf_format=N.STORAGE_FP16)
+        out.append(Workload(f"batch{count}_v{i:02d}", v, sc, 16))
+    return out
+
+
 # --------------------------------------------------------------- host scene
 class HostScene:
     """Scene arrays on the host (numpy), copied out of libluxgi_scene."""

@@ -1,0 +1,177 @@
+"""Batched updates of many volumes (luxgi_ddgi_update_batch and the
+luxgi_ddgi_batch_* objects) against the same volumes updated alone.
+
+The batched kernels run the per-ray and per-texel code of the single-volume
+kernels from the same translation units, so with the same march and shade
+variant every atlas texel must match bit for bit: FP32 and tensor-core
+blend, graph replay and direct launches.  Where the autotuner picks a
+different shade variant the shading differs only by its approximate
+division (1e-4 relative, as in test_gpu_parity).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from luxgi_gb300 import _native as N
+from luxgi_gb300.ddgi import DDGIBatch, DDGIVolume, frame_rotation, update_batch
+from luxgi_gb300.scene import DeviceScene, HostScene, batch_workloads
+from tests._helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    import torch
+
+    t = t.detach().cpu()
+    if t.dtype == torch.float16:
+        t = t.float()
+    return t.numpy()
+
+
+def _pairs(blend, storage=N.STORAGE_FP32, n=5, seed=11):
+    """n uneven small volumes, each with its own scene, twice: (alone, batched)."""
+    ws = batch_workloads(count=n, seed=seed, max_counts=(7, 4, 6), min_counts=(2, 2, 2), sdf_range=(32, 64),
+                         atlas_range=(256, 512), blend=blend, storage=storage, max_steps=48)
+    scenes, alone, batched = [], [], []
+    for w in ws:
+        host = HostScene(w.scene)
+        dev = DeviceScene(host, w.volume.light_mode)
+        a, b = DDGIVolume(w.volume), DDGIVolume(w.volume)
+        a.bind_scene(dev)
+        b.bind_scene(dev)
+        scenes.append((host, dev))
+        alone.append(a)
+        batched.append(b)
+    return scenes, alone, batched
+
+
+def _rots(n, frame):
+    return np.stack([frame_rotation(0xBA7C + i, frame) for i in range(n)])
+
+
+def _assert_same(alone, batched, exact=True):
+    import torch
+
+    torch.cuda.synchronize()
+    for a, b in zip(alone, batched):
+        assert a.frames == b.frames
+        for x, y in zip(a.atlases(), b.atlases()):
+            x, y = _np(x), _np(y)
+            if exact:
+                np.testing.assert_array_equal(x, y)
+            else:
+                assert rel_err(y, x) <= 1e-4
+
+
+@pytest.mark.parametrize("blend", [N.BLEND_FP32, N.BLEND_TENSOR])
+@pytest.mark.parametrize("use_graph", [1, 0])
+def test_batch_equals_single(cuda, blend, use_graph):
+    _, alone, batched = _pairs(blend)
+    batch = DDGIBatch(batched, {"use_graph": use_graph})
+    n = len(alone)
+    for f in range(3):
+        rots = _rots(n, f)
+        for v, r in zip(alone, rots):
+            v.update(r)
+        batch.update(rots)
+        _assert_same(alone, batched)
+
+
+def test_batch_fp16_storage_and_tuning_knobs(cuda):
+    _, alone, batched = _pairs(N.BLEND_FP32, storage=N.STORAGE_FP16, n=4, seed=12)
+    batch = DDGIBatch(batched, {"march_variant": 5, "march_threads": 128, "blend_probes": 8})
+    n = len(alone)
+    for f in range(2):
+        rots = _rots(n, f)
+        for v, r in zip(alone, rots):
+            v.update(r)
+        batch.update(rots)
+    # march variants are bit-identical and the shade variant is the same
+    _assert_same(alone, batched)
+
+
+def test_update_batch_groups_and_falls_back(cuda):
+    _, alone, batched = _pairs(N.BLEND_FP32, n=4, seed=13)
+    _, alone16, batched16 = _pairs(N.BLEND_FP32, storage=N.STORAGE_FP16, n=2, seed=14)
+    vols_a = alone + alone16
+    vols_b = batched + batched16
+    n = len(vols_a)
+    for f in range(3):
+        rots = _rots(n, f)
+        for v, r in zip(vols_a, rots):
+            v.update(r)
+        update_batch(vols_b, rots)
+        _assert_same(vols_a, vols_b)
+
+
+def test_batch_autotune_keeps_state(cuda):
+    import torch
+
+    _, alone, batched = _pairs(N.BLEND_FP32, n=4, seed=15)
+    batch = DDGIBatch(batched)
+    n = len(alone)
+    for f in range(2):
+        rots = _rots(n, f)
+        for v, r in zip(alone, rots):
+            v.update(r)
+        batch.update(rots)
+    torch.cuda.synchronize()
+    before = [[_np(t).copy() for t in v.atlases("current") + v.atlases("prev")] for v in batched]
+    frames = [v.frames for v in batched]
+    best = batch.autotune(frames=1)
+    assert best["frame_ms"] > 0.0
+    assert best == batch.tuning
+    torch.cuda.synchronize()
+    after = [[_np(t) for t in v.atlases("current") + v.atlases("prev")] for v in batched]
+    assert [v.frames for v in batched] == frames
+    for x, y in zip(before, after):
+        for p, q in zip(x, y):
+            np.testing.assert_array_equal(p, q)
+    rots = _rots(n, 2)
+    for v, r in zip(alone, rots):
+        v.update(r)
+    batch.update(rots)
+    _assert_same(alone, batched, exact=best["shade_variant"] == 1)
+
+
+def test_batch_rejects_incompatible(cuda):
+    _, _, b32 = _pairs(N.BLEND_FP32, n=2, seed=16)
+    _, _, b16 = _pairs(N.BLEND_FP32, storage=N.STORAGE_FP16, n=1, seed=17)
+    with pytest.raises(N.LuxgiError) as e:
+        DDGIBatch(b32 + b16)
+    assert e.value.status == N.LUXGI_EINVAL
+    with pytest.raises(N.LuxgiError) as e:
+        DDGIBatch([b32[0], b32[0]])
+    assert e.value.status == N.LUXGI_EINVAL
+    with pytest.raises(N.LuxgiError) as e:
+        DDGIBatch(b32, {"march_variant": 7})
+    assert e.value.status == N.LUXGI_EINVAL
+    ws = batch_workloads(count=1, seed=18, max_counts=(3, 3, 3), min_counts=(2, 2, 2), sdf_range=(32, 32),
+                         atlas_range=(256, 256), blend=N.BLEND_FP32)
+    unbound = DDGIVolume(ws[0].volume)
+    with pytest.raises(N.LuxgiError) as e:
+        DDGIBatch([b32[0], unbound])
+    assert e.value.status == N.LUXGI_ENOTBOUND
+    with pytest.raises(N.LuxgiError) as e:
+        update_batch([b32[0], b32[0]], _rots(2, 0))
+    assert e.value.status == N.LUXGI_EINVAL
+
+
+@pytest.mark.parametrize("blend", [N.BLEND_FP32, N.BLEND_TENSOR])
+def test_batch_launch_count(cuda, blend):
+    import torch
+
+    _, _, batched = _pairs(blend, n=3, seed=19)
+    batch = DDGIBatch(batched)
+    lib = N.ddgi()
+    batch.update(_rots(3, 0))          # captures the graph of argument block 0
+    batch.update(_rots(3, 1))          # and of block 1
+    torch.cuda.synchronize()
+    c0 = lib.luxgi_launch_count()
+    batch.update(_rots(3, 2))
+    torch.cuda.synchronize()
+    per_frame = lib.luxgi_launch_count() - c0
+    # raygen, weights, march, shade + blend: 2 FP32 launches, or 2 per volume
+    assert per_frame == (6 if blend == N.BLEND_FP32 else 4 + 2 * 3)
