@@ -6,9 +6,10 @@ interface plus the seeded synthetic scene inputs.
 """
 from . import _native
 from .ddgi import DDGIBatch, DDGIVolume, frame_rotation, rotation, update_batch
+from .serve import Server
 from .scene import (PLAIN_SMALL, PLAIN_SMALL_REF, PRECISION, PRODUCTION, WORKLOADS, DeviceScene, HostScene,
                     SceneSpec, VolumeSpec, Workload, scaled)
 
 __all__ = ["DDGIBatch", "DDGIVolume", "DeviceScene", "HostScene", "SceneSpec", "VolumeSpec", "Workload", "WORKLOADS",
            "PLAIN_SMALL", "PLAIN_SMALL_REF", "PRODUCTION", "PRECISION", "frame_rotation", "rotation",
-           "update_batch", "scaled", "_native"]
+           "update_batch", "scaled", "Server", "_native"]

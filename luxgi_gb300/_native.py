@@ -97,6 +97,28 @@ class BatchTuning(ctypes.Structure):
                 ("blend_probes", c_int32), ("use_graph", c_int32), ("reserved", c_int32 * 3), ("frame_ms", c_float)]
 
 
+class ServerDesc(ctypes.Structure):
+    _fields_ = [("memory_budget", c_uint64), ("executor", c_int32), ("max_group", c_int32),
+                ("max_inflight", c_int32), ("reserved0", c_int32), ("tuning", BatchTuning), ("sim_rate", ctypes.c_double),
+                ("sim_admit_s", ctypes.c_double), ("reserved", c_int32 * 4)]
+
+
+class SessionScene(ctypes.Structure):
+    _fields_ = [("sdf", SdfDesc), ("surface", SurfaceDesc), ("atlas_resolution", c_int32), ("reserved", c_int32 * 3)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, c_uint64) for n in ("submitted", "completed", "pending", "inflight_groups", "admissions",
+                                        "evictions", "rejected", "resident_sessions", "resident_bytes",
+                                        "peak_resident_bytes", "groups", "probe_rays", "max_overlap")] + \
+               [(n, ctypes.c_double) for n in ("mean_group", "latency_ms_p50", "latency_ms_p95", "latency_ms_p99",
+                                               "latency_ms_mean", "latency_ms_max", "wall_s")]
+
+
+SERVE_EXEC_CUDA = 0
+SERVE_EXEC_SIM = 1
+
+
 class SceneConfig(ctypes.Structure):
     _fields_ = [("seed", c_uint64), ("room_size", c_float), ("wall_thickness", c_float), ("num_primitives", c_int32),
                 ("sphere_radius", c_float * 2), ("box_half_extent", c_float * 2), ("sdf_resolution", c_int32),
@@ -159,6 +181,21 @@ DDGI_API = [
     ("luxgi_launch_count", c_uint64, []),
 ]
 
+SERVE_API = [
+    ("luxgi_server_create", c_int, [POINTER(ServerDesc), POINTER(c_void_p)]),
+    ("luxgi_server_destroy", c_int, [c_void_p]),
+    ("luxgi_server_add_session", c_int, [c_void_p, POINTER(VolumeDesc), POINTER(SessionScene), POINTER(c_int32)]),
+    ("luxgi_server_session_bytes", c_int, [c_void_p, c_int32, POINTER(c_uint64)]),
+    ("luxgi_server_submit", c_int, [c_void_p, c_int32, POINTER(c_float), POINTER(c_uint64)]),
+    ("luxgi_server_drain", c_int, [c_void_p, ctypes.c_double]),
+    ("luxgi_server_run_poisson", c_int, [c_void_p, POINTER(c_int32), c_int, ctypes.c_double, ctypes.c_double,
+                                         c_uint64]),
+    ("luxgi_server_stats_get", c_int, [c_void_p, POINTER(ServerStats), c_int]),
+    ("luxgi_server_touch", c_int, [c_void_p, c_int32]),
+    ("luxgi_server_session_atlases", c_int, [c_void_p, c_int32, POINTER(Atlases)]),
+    ("luxgi_server_session_state", c_int, [c_void_p, c_int32, POINTER(c_int32), POINTER(c_int32)]),
+]
+
 SCENE_API = [
     ("luxgi_scene_build", c_int, [POINTER(SceneConfig), POINTER(c_void_p)]),
     ("luxgi_scene_view_get", c_int, [c_void_p, POINTER(SceneView)]),
@@ -189,7 +226,7 @@ _scene = None
 def ddgi() -> ctypes.CDLL:
     global _ddgi
     if _ddgi is None:
-        _ddgi = _load("libluxgi_ddgi.so", DDGI_API)
+        _ddgi = _load("libluxgi_ddgi.so", DDGI_API + SERVE_API)
     return _ddgi
 
 

@@ -28,7 +28,7 @@ NO_FMAD = {"trace.cu", "setup.cu"}
 # shading is compared with the restatement by tolerance: approximate
 # division and square root
 FAST_DIV = {"shade.cu"}
-CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "capi.cu", "batch.cu"]
+CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "capi.cu", "batch.cu", "server.cu"]
 
 
 def nvcc() -> str:

@@ -16,32 +16,15 @@
 
 #include <cuda_runtime.h>
 
-#include "luxgi_volume.h"
+#include "luxgi_batch.h"
 
 using namespace luxgi;
 
-namespace {
+namespace luxgi {
 
 constexpr int kForkStreams = 4;   // parallel graph branches of the per-volume tensor-core blend
 
-size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
-
-enum Stage { kRaygen, kWeights, kMarch, kShade, kBlendI, kBlendD, kNumStages };
-
-// What a set of volumes needs to run one frame as batched launches.
-struct Plan {
-    std::vector<luxgi_ddgi_volume*> vols;
-    luxgi_ddgi_batch_tuning t{};
-    int n = 0;
-    int storage = 0, light_mode = 0, sdf_format = 0;
-    bool tc = false;
-    // per-frame argument block: TraceParams[n], BlendParams[n], 2 x TcArgs[n]
-    size_t off_trace = 0, off_blend = 0, off_tc = 0, tc_bytes = 0, arg_bytes = 0;
-    std::vector<int> starts;            // [kNumStages][n + 1] block offsets
-    int blocks[kNumStages] = {};
-    size_t smem_i = 0, smem_d = 0;      // dynamic shared memory of the FP32 blend
-    std::vector<TcPlan> tcp;            // tensor-core blend maps, one per volume
-};
+static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 int compat_check(luxgi_ddgi_volume* const* vols, int n) {
     if (n < 1 || !vols) return LUXGI_EINVAL;
@@ -234,6 +217,10 @@ void end_frame_all(const Plan& P) {
         v->frames += 1;
     }
 }
+
+}  // namespace luxgi
+
+namespace {
 
 // One frame of a compatible group through direct batched launches, with
 // transient stream-ordered device buffers.

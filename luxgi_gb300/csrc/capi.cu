@@ -99,6 +99,32 @@ size_t atlas_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 2 
 
 }  // namespace
 
+uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,
+                                    const luxgi_surface_desc& surf) {
+    // mirrors the allocations of luxgi_ddgi_create and luxgi_ddgi_bind_scene
+    const luxgi_ddgi_uniform& u = d.uniform;
+    const uint64_t P = uint64_t(u.probe_counts[0]) * u.probe_counts[1] * u.probe_counts[2];
+    const uint64_t R = uint64_t(u.rays_per_probe), PR = P * R;
+    const uint64_t Ti = uint64_t(u.irradiance_probe_side) * u.irradiance_probe_side;
+    const uint64_t Td = uint64_t(u.depth_probe_side) * u.depth_probe_side;
+    const uint64_t ae = atlas_elem_bytes(d.storage);
+    uint64_t b = 2 * (uint64_t(u.irradiance_width) * u.irradiance_height * 4 * ae +
+                      uint64_t(u.depth_width) * u.depth_height * 2 * ae);
+    b += 2 * 16 * R + PR * ray_elem_bytes(d.storage) + 4 * (Ti + Td) * R + 8 * (Ti + Td) + 16 + PR * (16 + 4);
+    if (d.blend == LUXGI_BLEND_TENSOR) b += PR * 16 + 2 * ((Ti + 15) / 16 * 16 + (Td + 15) / 16 * 16) * R;
+    const uint64_t nobj = surf.data.objects_count;
+    uint64_t cap = surf.data.culled_objects_capacity;
+    if (cap == 0) cap = 1 + 40ull * 40 * 40 * (nobj + 1);
+    b += 64 * nobj + 4 * cap + 4 * (2 * 40ull * 40 * 40 + 1);
+    const int C = int(sdf.data.cascades_count);
+    const int mv = d.march_variant == 0 ? 4 : d.march_variant;
+    const int layout = mv >= 6 ? mv - 4 : mv;
+    if (layout >= 3) b += quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
+    if (layout == 4) b += quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
+    if (layout == 5) b += pair_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
+    return b;
+}
+
 int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
     // quad-packed SDF copies for the march variants that read them
     // (variants 3-5 per-ray threads, 7-9 the pooled march with the same layouts)

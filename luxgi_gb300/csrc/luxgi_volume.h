@@ -62,5 +62,9 @@ void volume_blend_params(const luxgi_ddgi_volume* v, BlendParams& p);
 void volume_tc_params(const luxgi_ddgi_volume* v, TcBlendParams& p);
 // (Re)allocates the packed SDF copies the volume's march variant reads.
 int volume_alloc_packs(luxgi_ddgi_volume* v);
+// Device bytes a volume of description d allocates once bound to the scene
+// (luxgi_ddgi_create + luxgi_ddgi_bind_scene; debug ray records excluded).
+uint64_t volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,
+                             const luxgi_surface_desc& surf);
 
 }  // namespace luxgi

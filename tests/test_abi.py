@@ -23,7 +23,8 @@ def _declared(header: Path) -> set[str]:
     return set(re.findall(r"\b(luxgi_\w+)\s*\(", text)) - {"luxgi_ddgi_volume", "luxgi_scene"}
 
 
-@pytest.mark.parametrize("header,lib", [("luxgi_ddgi.h", "libluxgi_ddgi.so"), ("luxgi_scene.h", "libluxgi_scene.so")])
+@pytest.mark.parametrize("header,lib", [("luxgi_ddgi.h", "libluxgi_ddgi.so"), ("luxgi_serve.h", "libluxgi_ddgi.so"),
+                                        ("luxgi_scene.h", "libluxgi_scene.so")])
 def test_library_exports_every_declared_symbol(header, lib):
     names = _declared(ROOT / "include" / header)
     assert names
@@ -35,6 +36,8 @@ def test_library_exports_every_declared_symbol(header, lib):
 def test_ctypes_mirror_covers_header():
     names = _declared(ROOT / "include" / "luxgi_ddgi.h")
     assert names == {n for n, _, _ in N.DDGI_API}
+    names = _declared(ROOT / "include" / "luxgi_serve.h")
+    assert names == {n for n, _, _ in N.SERVE_API}
     names = _declared(ROOT / "include" / "luxgi_scene.h")
     assert names == {n for n, _, _ in N.SCENE_API}
 
@@ -45,6 +48,8 @@ def test_struct_sizes():
     assert ctypes.sizeof(N.SurfaceData) == 32
     assert ctypes.sizeof(N.SurfaceObject) == 128    # std430 ObjectBuffer
     assert ctypes.sizeof(N.SurfaceTile) == 96
+    assert ctypes.sizeof(N.BatchTuning) == 36
+    assert ctypes.sizeof(N.ServerDesc) == 8 + 16 + 36 + 4 + 16 + 16
 
 
 def test_derive_uniform_reference_layout():
