@@ -287,7 +287,8 @@ typedef struct luxgi_ddgi_batch_tuning {
     int32_t march_variant;   /* 1-5, as luxgi_ddgi_volume_desc.march_variant  */
     int32_t march_threads;   /* rays per march block: 128 or 256              */
     int32_t shade_variant;   /* 1, 2, 4 or 8                                  */
-    int32_t blend_probes;    /* cap on probes per FP32-blend block, 1-32      */
+    int32_t blend_probes;    /* probes per thread of the FP32-blend register
+                                tile (x 4 texels): 1, 2 or 4                 */
     int32_t use_graph;       /* 1 capture + replay a CUDA graph, 0 launch     */
     int32_t reserved[3];
     float frame_ms;          /* frame time measured by the autotuner, else 0  */
@@ -295,7 +296,7 @@ typedef struct luxgi_ddgi_batch_tuning {
 
 /* All volumes bound, on the current device, with the same storage, light
  * mode, blend kind and SDF format; none twice.  tuning may be NULL (march
- * variant 4, 256 rays a block, shade variant 1, 32 probes, graph on).  The
+ * variant 4, 256 rays a block, shade variant 1, 2 blend probes, graph on).  The
  * batch sets every volume's march and shade variant to its own (reallocating
  * the packed SDF copies the variant reads).  Volumes must outlive the batch
  * and must not be destroyed, re-created or updated concurrently with it. */
@@ -307,7 +308,7 @@ int luxgi_ddgi_batch_create(luxgi_ddgi_volume* const* vols, int n,
  * or synchronised).  Host-side end_frame of every volume included. */
 int luxgi_ddgi_batch_update(luxgi_ddgi_batch* batch, const float* rots, void* stream);
 /* Times `frames` frames (after 2 warm-up frames) of each candidate tuning
- * (march variant x rays per block, then shade variant, then blend probes)
+ * (march variant x rays per block, then shade variant, then blend tile)
  * with CUDA events on `stream`, applies the fastest and writes it to *best
  * (may be NULL).  Every volume's atlases, frame count and ping-pong are saved
  * before and restored after, so results are unchanged by tuning.  Rotations

@@ -45,7 +45,7 @@ int compat_check(luxgi_ddgi_volume* const* vols, int n) {
 bool tuning_valid(const luxgi_ddgi_batch_tuning& t) {
     return t.march_variant >= 1 && t.march_variant <= 5 && (t.march_threads == 128 || t.march_threads == 256) &&
            (t.shade_variant == 1 || t.shade_variant == 2 || t.shade_variant == 4 || t.shade_variant == 8) &&
-           t.blend_probes >= 1 && t.blend_probes <= 32 && (t.use_graph == 0 || t.use_graph == 1);
+           (t.blend_probes == 1 || t.blend_probes == 2 || t.blend_probes == 4) && (t.use_graph == 0 || t.use_graph == 1);
 }
 
 luxgi_ddgi_batch_tuning default_tuning() {
@@ -54,7 +54,7 @@ luxgi_ddgi_batch_tuning default_tuning() {
     t.march_variant = 4;
     t.march_threads = 256;
     t.shade_variant = 1;
-    t.blend_probes = 32;
+    t.blend_probes = 2;
     t.use_graph = 1;
     return t;
 }
@@ -581,7 +581,7 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
         return cs;
     };
     // coordinate descent: march variant x rays per block, then shade
-    // variant, then the FP32 blend's probes per block
+    // variant, then the FP32 blend's probes per thread
     for (int mv = 1; mv <= 5; ++mv) {
         for (int tpb : {128, 256}) {
             luxgi_ddgi_batch_tuning c = best;
@@ -597,7 +597,7 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
         if (c.shade_variant != best.shade_variant) consider(c);
     }
     if (!b->plan.tc) {
-        for (int pb : {8, 16, 32}) {
+        for (int pb : {1, 2, 4}) {
             luxgi_ddgi_batch_tuning c = best;
             c.blend_probes = pb;
             if (c.blend_probes != best.blend_probes) consider(c);

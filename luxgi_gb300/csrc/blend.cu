@@ -17,6 +17,12 @@
 
 namespace luxgi {
 
+// Texels per thread of the FP32 blend tile; the FP32 weight rows are stored
+// ray-major, [R][Tp] with Tp = T rounded up to whole tiles (padding zero).
+constexpr int kTexelTile = 4;
+
+__host__ __device__ __forceinline__ int blend_row_pitch(int T) { return (T + kTexelTile - 1) / kTexelTile * kTexelTile; }
+
 // ------------------------------------------------------------- weights
 // One block per texel row, threads over rays: octDecode(normalizedOctCoord)
 // (DDGICommon.glsl:74-92) against every ray direction.  The row sum is a
@@ -52,6 +58,7 @@ __device__ __forceinline__ void weights_row(const BlendParams& p, int row, float
     }
     const f3 td = norm3(v);
     float* w = depth ? p.w_dist : p.w_irr;
+    const int Tp = blend_row_pitch(T);          // ray-major rows, padded to whole texel tiles
     const float4* dirs = p.dirs;
     float sum = 0.0f, sum_h = 0.0f;
     for (int r = threadIdx.x; r < R; r += blockDim.x) {
@@ -59,7 +66,7 @@ __device__ __forceinline__ void weights_row(const BlendParams& p, int row, float
         const float c = mx(0.0f, td.x * d.x + td.y * d.y + td.z * d.z);
         float wt = depth ? powf(c, u.sharpness) : c;
         if (!(wt >= 1e-8f)) wt = 0.0f;
-        w[size_t(t) * R + r] = wt;
+        w[size_t(r) * Tp + t] = wt;
         sum = sum + wt;
         if (tc) {
             const __half h = __float2half_rn(wt);
@@ -158,33 +165,75 @@ __device__ __forceinline__ void store_texel(void* atlas, int W, int n, int cx, i
 }
 
 // --------------------------------------------------------------- blend
-// Block = 256 threads over (texel, probe-of-block) pairs; rays in chunks of
-// KC through shared memory (weights stored ray-major so a warp's texels hit
-// distinct banks, ray data broadcast).
+// Register-tiled contraction: a block takes PB probes and every texel of
+// one atlas; each thread owns a tile of kTexelTile consecutive texels x PP
+// probes (x 3 or 2 channels) in registers.  Rays go through shared memory
+// in chunks of kRayChunk: the weights chunk [r][texel] (copied as float4 from
+// the ray-major weight rows) and the ray chunk [r][probe] (rgb, or the
+// clamped distance and its square).  Per ray a thread loads one float4 of
+// weights and PP ray values and issues kTexelTile x PP x channels FMAs.  Each
+// accumulator sums its rays in ascending order with fmaf, as the
+// restatement does.
 constexpr int kBlendThreads = 256;
-constexpr int kPairsPerThread = 4;
 constexpr int kRayChunk = 32;
+constexpr int kMaxProbesPerBlock = 128;
 
-template <int DEPTH, typename RT, typename AT>
-__device__ __forceinline__ void blend_block(const BlendParams& p, int PB, int block, float* smem) {
+struct BlendShape {
+    int TG;   // texel groups (threads along texels)
+    int PG;   // probe groups (threads along probes)
+    int PB;   // probes per block
+};
+
+__host__ __device__ __forceinline__ BlendShape blend_shape(int T, int PP) {
+    BlendShape s;
+    s.TG = (T + kTexelTile - 1) / kTexelTile;
+    int pg = kBlendThreads / s.TG;
+    const int cap = kMaxProbesPerBlock / PP;
+    s.PG = pg < 1 ? 1 : (pg > cap ? cap : pg);
+    s.PB = s.PG * PP;
+    return s;
+}
+
+__host__ __device__ __forceinline__ size_t blend_smem_bytes(int T, int PP, bool depth) {
+    const BlendShape s = blend_shape(T, PP);
+    return sizeof(float) * kRayChunk * (s.TG * kTexelTile) + size_t(depth ? 8 : 16) * kRayChunk * s.PB;
+}
+
+template <bool DEPTH> struct RayVal;
+template <> struct RayVal<false> { using type = float4; };
+template <> struct RayVal<true> { using type = float2; };
+
+template <int DEPTH, typename RT, typename AT, int PP>
+__device__ __forceinline__ void blend_block(const BlendParams& p, int block, float* smem) {
+    using RV = typename RayVal<DEPTH != 0>::type;
+    constexpr int NC_ACC = DEPTH ? 2 : 3;
     const luxgi_ddgi_uniform& u = p.u;
     const int n = DEPTH ? u.depth_probe_side : u.irradiance_probe_side;
     const int T = n * n;
     const int W = DEPTH ? u.depth_width : u.irradiance_width;
     const int R = p.R;
+    const BlendShape sh = blend_shape(T, PP);
+    const int Tp = sh.TG * kTexelTile;
+    const int PB = sh.PB;
     const int p0 = block * PB;
-    float* Ws = smem;                                  // [KC][T]
-    float4* Rs = reinterpret_cast<float4*>(smem + kRayChunk * T);   // [PB][KC]
-    const float* Wg = DEPTH ? p.w_dist : p.w_irr;
-    const int npairs = T * PB;
-    float acc[kPairsPerThread][3];
+    float* Ws = smem;                                               // [kRayChunk][Tp]
+    RV* Rs = reinterpret_cast<RV*>(smem + kRayChunk * Tp);          // [kRayChunk][PB]
+    const float* Wg = DEPTH ? p.w_dist : p.w_irr;                   // [R][Tp]
+    const int tg = int(threadIdx.x) % sh.TG, pg = int(threadIdx.x) / sh.TG;
+    const bool active = pg < sh.PG;
+    float acc[PP][kTexelTile][NC_ACC];
 #pragma unroll
-    for (int q = 0; q < kPairsPerThread; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0f;
+    for (int j = 0; j < PP; ++j)
+#pragma unroll
+        for (int k = 0; k < kTexelTile; ++k)
+#pragma unroll
+            for (int c = 0; c < NC_ACC; ++c) acc[j][k][c] = 0.0f;
     for (int r0 = 0; r0 < R; r0 += kRayChunk) {
         const int kc = min(kRayChunk, R - r0);
-        for (int i = threadIdx.x; i < kc * T; i += blockDim.x) {
-            const int t = i / kc, r = i % kc;
-            Ws[r * T + t] = __ldg(Wg + size_t(t) * R + r0 + r);
+        {
+            const float4* src = reinterpret_cast<const float4*>(Wg + size_t(r0) * Tp);
+            float4* dst = reinterpret_cast<float4*>(Ws);
+            for (int i = threadIdx.x; i < kc * Tp / 4; i += blockDim.x) dst[i] = __ldg(src + i);
         }
         for (int i = threadIdx.x; i < PB * kc; i += blockDim.x) {
             const int pb = i / kc, r = i % kc;
@@ -201,33 +250,37 @@ __device__ __forceinline__ void blend_block(const BlendParams& p, int PB, int bl
                     v = make_float4(__low2float(a), __high2float(a), __low2float(b), __high2float(b));
                 }
             }
-            if (DEPTH) {
+            if constexpr (DEPTH) {
                 float d = mn(u.max_distance, v.w - 0.01f);
                 if (d == -1.0f) d = u.max_distance;
-                v = make_float4(d, d * d, 0.0f, 0.0f);
+                Rs[r * PB + pb] = make_float2(d, d * d);
+            } else {
+                Rs[r * PB + pb] = v;
             }
-            Rs[pb * kRayChunk + r] = v;
         }
         __syncthreads();
+        if (active) {
+            const float* wrow = Ws + tg * kTexelTile;
+            const RV* rrow = Rs + pg * PP;
+#pragma unroll 2
+            for (int r = 0; r < kc; ++r) {
+                const float4 w4 = *reinterpret_cast<const float4*>(wrow + r * Tp);
+                const float w[kTexelTile] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
-        for (int q = 0; q < kPairsPerThread; ++q) {
-            const int pair = threadIdx.x + q * blockDim.x;
-            if (pair < npairs) {
-                const int t = pair % T, pb = pair / T;
-                const float4* rr = Rs + pb * kRayChunk;
-                float a0 = acc[q][0], a1 = acc[q][1], a2 = acc[q][2];
-                for (int r = 0; r < kc; ++r) {
-                    const float w = Ws[r * T + t];
-                    const float4 v = rr[r];
-                    a0 = fmaf(v.x, w, a0);
-                    a1 = fmaf(v.y, w, a1);
-                    if (!DEPTH) a2 = fmaf(v.z, w, a2);
+                for (int j = 0; j < PP; ++j) {
+                    const RV v = rrow[r * PB + j];
+#pragma unroll
+                    for (int k = 0; k < kTexelTile; ++k) {
+                        acc[j][k][0] = fmaf(v.x, w[k], acc[j][k][0]);
+                        acc[j][k][1] = fmaf(v.y, w[k], acc[j][k][1]);
+                        if constexpr (!DEPTH) acc[j][k][2] = fmaf(v.z, w[k], acc[j][k][2]);
+                    }
                 }
-                acc[q][0] = a0; acc[q][1] = a1; acc[q][2] = a2;
             }
         }
         __syncthreads();
     }
+    if (!active) return;
     // epilogue: normalise, gamma, hysteresis, store + border mirrors
     const int XY = u.probe_counts[0] * u.probe_counts[1];
     const float* nrm = DEPTH ? p.n_dist : p.n_irr;
@@ -237,139 +290,149 @@ __device__ __forceinline__ void blend_block(const BlendParams& p, int PB, int bl
     const float h = u.hysteresis;
     const float ig = 1.0f / u.ddgi_gamma;
 #pragma unroll
-    for (int q = 0; q < kPairsPerThread; ++q) {
-        const int pair = threadIdx.x + q * blockDim.x;
-        if (pair >= npairs) continue;
-        const int t = pair % T, pb = pair / T;
-        const int pr = p0 + pb;
+    for (int j = 0; j < PP; ++j) {
+        const int pr = p0 + pg * PP + j;
         if (pr >= p.P) continue;
-        const int tx = t % n, ty = t / n;
         const int cx = pr % XY, cy = pr / XY;
-        const float s = __ldg(nrm + t);
-        float v[4];
-        v[0] = acc[q][0] * s;
-        v[1] = acc[q][1] * s;
-        v[2] = acc[q][2] * s;
-        v[3] = 1.0f;
-        if (!DEPTH) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) v[c] = powf(v[c], ig);
+        for (int k = 0; k < kTexelTile; ++k) {
+            const int t = tg * kTexelTile + k;
+            if (t >= T) continue;
+            const int tx = t % n, ty = t / n;
+            const float s = __ldg(nrm + t);
+            float v[4];
+            v[0] = acc[j][k][0] * s;
+            v[1] = acc[j][k][1] * s;
+            v[2] = DEPTH ? 0.0f : acc[j][k][NC_ACC - 1] * s;
+            v[3] = 1.0f;
+            if (!DEPTH) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) v[c] = powf(v[c], ig);
+            }
+            const size_t base = (size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2)) * NC;
+            const int nch = DEPTH ? 2 : 3;
+            for (int c = 0; c < nch; ++c) {
+                float x = v[c];
+                if (!p.first) x = x * (1.0f - h) + AtlasIO<AT>::ld(prev, base + c) * h;
+                v[c] = AtlasIO<AT>::rnd(x);
+            }
+            store_texel<AT, NC>(out, W, n, cx, cy, tx, ty, v);
         }
-        const size_t base = (size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2)) * NC;
-        const int nch = DEPTH ? 2 : 3;
-        for (int c = 0; c < nch; ++c) {
-            float x = v[c];
-            if (!p.first) x = x * (1.0f - h) + AtlasIO<AT>::ld(prev, base + c) * h;
-            v[c] = AtlasIO<AT>::rnd(x);
-        }
-        store_texel<AT, NC>(out, W, n, cx, cy, tx, ty, v);
     }
 }
 
-template <int DEPTH, typename RT, typename AT>
-__global__ void __launch_bounds__(kBlendThreads) blend_kernel(const BlendParams p, int PB) {
+template <int DEPTH, typename RT, typename AT, int PP>
+__global__ void __launch_bounds__(kBlendThreads) blend_kernel(const BlendParams p) {
     extern __shared__ __align__(16) float smem[];
-    blend_block<DEPTH, RT, AT>(p, PB, int(blockIdx.x), smem);
+    blend_block<DEPTH, RT, AT, PP>(p, int(blockIdx.x), smem);
 }
 
-// Probes per block: enough (texel, probe) pairs for every thread, at most
-// pb_cap (32 at most: their ray chunk is 16 KB of shared memory).
-constexpr int kMaxProbesPerBlock = 32;
-
-__host__ __device__ __forceinline__ int blend_probes_per_block(int T, int pb_cap) {
-    int PB = kBlendThreads * kPairsPerThread / T;
-    return PB < 1 ? 1 : (PB > pb_cap ? pb_cap : PB);
-}
-
-// Batched: the volume's probes-per-block follows from its texel count and
-// the launch's cap; parameters staged in shared memory once per block.
-template <int DEPTH, typename RT, typename AT>
+// Batched: every volume of the launch uses the same probes-per-thread PP;
+// its probes per block follow from its texel count.  Parameters staged in
+// shared memory once per block.
+template <int DEPTH, typename RT, typename AT, int PP>
 __global__ void __launch_bounds__(kBlendThreads)
-    blend_batch_kernel(const BlendParams* __restrict__ vp, const int* __restrict__ starts, int n, int pb_cap) {
+    blend_batch_kernel(const BlendParams* __restrict__ vp, const int* __restrict__ starts, int n) {
     extern __shared__ __align__(16) float smem[];
     __shared__ __align__(16) uint32_t sp[sizeof(BlendParams) / 4];
     const int v = batch_volume(starts, n, int(blockIdx.x));
     const BlendParams& p = stage_params(vp + v, sp);
-    const int side = DEPTH ? p.u.depth_probe_side : p.u.irradiance_probe_side;
-    blend_block<DEPTH, RT, AT>(p, blend_probes_per_block(side * side, pb_cap), int(blockIdx.x) - __ldg(starts + v),
-                               smem);
+    blend_block<DEPTH, RT, AT, PP>(p, int(blockIdx.x) - __ldg(starts + v), smem);
 }
 
-size_t blend_smem_bytes(int T, int PB) { return sizeof(float) * kRayChunk * T + sizeof(float4) * PB * kRayChunk; }
+static int blend_side(const BlendParams& p, bool depth) {
+    return depth ? p.u.depth_probe_side : p.u.irradiance_probe_side;
+}
 
-int blend_blocks(const BlendParams& p, bool depth, int pb_cap) {
-    const int side = depth ? p.u.depth_probe_side : p.u.irradiance_probe_side;
-    const int PB = blend_probes_per_block(side * side, pb_cap);
+int blend_blocks(const BlendParams& p, bool depth, int pp) {
+    const int side = blend_side(p, depth);
+    const int PB = blend_shape(side * side, pp).PB;
     return (p.P + PB - 1) / PB;
 }
 
-size_t blend_smem(const BlendParams& p, bool depth, int pb_cap) {
-    const int side = depth ? p.u.depth_probe_side : p.u.irradiance_probe_side;
-    return blend_smem_bytes(side * side, blend_probes_per_block(side * side, pb_cap));
+size_t blend_smem(const BlendParams& p, bool depth, int pp) {
+    const int side = blend_side(p, depth);
+    return blend_smem_bytes(side * side, pp, depth);
 }
 
-template <int DEPTH, typename RT, typename AT>
-static cudaError_t launch_blend_batch_kind(const BlendParams* vp, const int* starts, int n, int blocks, size_t sm,
-                                           int pb_cap, cudaStream_t st) {
+// Probes per thread of a single-volume launch: the largest tile that still
+// gives every SM two blocks.
+static int auto_pp(const BlendParams& p, bool depth) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    for (int pp : {4, 2})
+        if (blend_blocks(p, depth, pp) >= 2 * sms) return pp;
+    return 1;
+}
+
+template <int DEPTH, typename RT, typename AT, int PP>
+static cudaError_t launch_kind_pp(const void* vp, const int* starts, int n, int blocks, size_t sm, bool batch,
+                                  cudaStream_t st) {
     if (blocks <= 0) return cudaSuccess;
-    if (sm > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(blend_batch_kernel<DEPTH, RT, AT>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-        if (e != cudaSuccess) return e;
+    if (batch) {
+        auto k = blend_batch_kernel<DEPTH, RT, AT, PP>;
+        if (sm > 48 * 1024) {
+            const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+            if (e != cudaSuccess) return e;
+        }
+        k<<<blocks, kBlendThreads, sm, st>>>(static_cast<const BlendParams*>(vp), starts, n);
+    } else {
+        auto k = blend_kernel<DEPTH, RT, AT, PP>;
+        if (sm > 48 * 1024) {
+            const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+            if (e != cudaSuccess) return e;
+        }
+        k<<<blocks, kBlendThreads, sm, st>>>(*static_cast<const BlendParams*>(vp));
     }
-    blend_batch_kernel<DEPTH, RT, AT><<<blocks, kBlendThreads, sm, st>>>(vp, starts, n, pb_cap);
     note_launch();
     return cudaGetLastError();
-}
-
-cudaError_t launch_blend_batch(const BlendParams* vp, const int* starts_irr, int blocks_irr, size_t smem_irr,
-                               const int* starts_dist, int blocks_dist, size_t smem_dist, int n, int pb_cap,
-                               int storage, cudaStream_t st) {
-    if (pb_cap < 1 || pb_cap > kMaxProbesPerBlock) return cudaErrorInvalidValue;
-    cudaError_t e;
-    if (storage == LUXGI_STORAGE_FP16) {
-        e = launch_blend_batch_kind<0, uint2, __half>(vp, starts_irr, n, blocks_irr, smem_irr, pb_cap, st);
-        if (e == cudaSuccess)
-            e = launch_blend_batch_kind<1, uint2, __half>(vp, starts_dist, n, blocks_dist, smem_dist, pb_cap, st);
-    } else {
-        e = launch_blend_batch_kind<0, float4, float>(vp, starts_irr, n, blocks_irr, smem_irr, pb_cap, st);
-        if (e == cudaSuccess)
-            e = launch_blend_batch_kind<1, float4, float>(vp, starts_dist, n, blocks_dist, smem_dist, pb_cap, st);
-    }
-    return e;
 }
 
 template <int DEPTH, typename RT, typename AT>
-static cudaError_t launch_blend_kind(const BlendParams& p, int T, cudaStream_t st) {
-    const int PB = blend_probes_per_block(T, kMaxProbesPerBlock);
-    const size_t sm = blend_smem_bytes(T, PB);
-    const unsigned blocks = unsigned((p.P + PB - 1) / PB);
-    if (sm > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(blend_kernel<DEPTH, RT, AT>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
-        if (e != cudaSuccess) return e;
+static cudaError_t launch_kind(const void* vp, const int* starts, int n, int blocks, size_t sm, int pp, bool batch,
+                               cudaStream_t st) {
+    switch (pp) {
+        case 1: return launch_kind_pp<DEPTH, RT, AT, 1>(vp, starts, n, blocks, sm, batch, st);
+        case 2: return launch_kind_pp<DEPTH, RT, AT, 2>(vp, starts, n, blocks, sm, batch, st);
+        case 4: return launch_kind_pp<DEPTH, RT, AT, 4>(vp, starts, n, blocks, sm, batch, st);
+        default: return cudaErrorInvalidValue;
     }
-    blend_kernel<DEPTH, RT, AT><<<blocks, kBlendThreads, sm, st>>>(p, PB);
-    note_launch();
-    return cudaGetLastError();
-}
-
-template <typename RT, typename AT>
-static cudaError_t launch_blend_t(const BlendParams& p, cudaStream_t st) {
-    const int Ti = p.u.irradiance_probe_side * p.u.irradiance_probe_side;
-    const int Td = p.u.depth_probe_side * p.u.depth_probe_side;
-    const cudaError_t e = launch_blend_kind<0, RT, AT>(p, Ti, st);
-    if (e != cudaSuccess) return e;
-    return launch_blend_kind<1, RT, AT>(p, Td, st);
 }
 
 cudaError_t launch_blend(const BlendParams& p, cudaStream_t st) {
     if (p.P <= 0) return cudaSuccess;
-    if (p.u.irradiance_probe_side * p.u.irradiance_probe_side > kBlendThreads * kPairsPerThread ||
-        p.u.depth_probe_side * p.u.depth_probe_side > kBlendThreads * kPairsPerThread)
-        return cudaErrorInvalidValue;
-    if (p.storage == LUXGI_STORAGE_FP16) return launch_blend_t<uint2, __half>(p, st);
-    return launch_blend_t<float4, float>(p, st);
+    const int ppi = auto_pp(p, false), ppd = auto_pp(p, true);
+    const int bi = blend_blocks(p, false, ppi), bd = blend_blocks(p, true, ppd);
+    const size_t si = blend_smem(p, false, ppi), sd = blend_smem(p, true, ppd);
+    cudaError_t e;
+    if (p.storage == LUXGI_STORAGE_FP16) {
+        e = launch_kind<0, uint2, __half>(&p, nullptr, 1, bi, si, ppi, false, st);
+        if (e == cudaSuccess) e = launch_kind<1, uint2, __half>(&p, nullptr, 1, bd, sd, ppd, false, st);
+    } else {
+        e = launch_kind<0, float4, float>(&p, nullptr, 1, bi, si, ppi, false, st);
+        if (e == cudaSuccess) e = launch_kind<1, float4, float>(&p, nullptr, 1, bd, sd, ppd, false, st);
+    }
+    return e;
+}
+
+cudaError_t launch_blend_batch(const BlendParams* vp, const int* starts_irr, int blocks_irr, size_t smem_irr,
+                               const int* starts_dist, int blocks_dist, size_t smem_dist, int n, int pp,
+                               int storage, cudaStream_t st) {
+    if (pp != 1 && pp != 2 && pp != 4) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if (storage == LUXGI_STORAGE_FP16) {
+        e = launch_kind<0, uint2, __half>(vp, starts_irr, n, blocks_irr, smem_irr, pp, true, st);
+        if (e == cudaSuccess) e = launch_kind<1, uint2, __half>(vp, starts_dist, n, blocks_dist, smem_dist, pp, true, st);
+    } else {
+        e = launch_kind<0, float4, float>(vp, starts_irr, n, blocks_irr, smem_irr, pp, true, st);
+        if (e == cudaSuccess) e = launch_kind<1, float4, float>(vp, starts_dist, n, blocks_dist, smem_dist, pp, true, st);
+    }
+    return e;
 }
 
 // --------------------------------------------------------------- border

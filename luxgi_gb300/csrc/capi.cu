@@ -110,7 +110,8 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
     const uint64_t ae = atlas_elem_bytes(d.storage);
     uint64_t b = 2 * (uint64_t(u.irradiance_width) * u.irradiance_height * 4 * ae +
                       uint64_t(u.depth_width) * u.depth_height * 2 * ae);
-    b += 2 * 16 * R + PR * ray_elem_bytes(d.storage) + 4 * (Ti + Td) * R + 8 * (Ti + Td) + 16 + PR * (16 + 4);
+    b += 2 * 16 * R + PR * ray_elem_bytes(d.storage) + 4 * ((Ti + 3) / 4 * 4 + (Td + 3) / 4 * 4) * R + 8 * (Ti + Td) + 16 +
+         PR * (16 + 4);
     if (d.blend == LUXGI_BLEND_TENSOR) b += PR * 16 + 2 * ((Ti + 15) / 16 * 16 + (Td + 15) / 16 * 16) * R;
     const uint64_t nobj = surf.data.objects_count;
     uint64_t cap = surf.data.culled_objects_capacity;
@@ -220,6 +221,10 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.bounce = (d.infinite_bounce && v->frames != 0) ? 1 : 0;
     p.P = v->P;
     p.R = v->R;
+    p.index32 = (uint64_t(v->P) * uint64_t(v->R)) < (uint64_t(1) << 32) ? 1 : 0;
+    p.div_p = make_fastdiv(uint32_t(v->P));
+    p.div_x = make_fastdiv(uint32_t(d.uniform.probe_counts[0]));
+    p.div_xy = make_fastdiv(uint32_t(d.uniform.probe_counts[0]) * uint32_t(d.uniform.probe_counts[1]));
 }
 
 void luxgi::volume_tc_params(const luxgi_ddgi_volume* v, TcBlendParams& p) {
@@ -418,8 +423,13 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (e == cudaSuccess) e = dmalloc(&v->dirs_trace, sizeof(float4) * v->R);
     if (e == cudaSuccess) e = dmalloc(&v->dirs_blend, sizeof(float4) * v->R);
     if (e == cudaSuccess) e = dmalloc(&v->rays, PR * ray_elem_bytes(desc->storage));
-    if (e == cudaSuccess) e = dmalloc(&v->w_irr, sizeof(float) * v->Ti * v->R);
-    if (e == cudaSuccess) e = dmalloc(&v->w_dist, sizeof(float) * v->Td * v->R);
+    // FP32 weights: ray-major rows padded to whole texel tiles, padding zero
+    const size_t wi_bytes = sizeof(float) * size_t((v->Ti + 3) / 4 * 4) * v->R;
+    const size_t wd_bytes = sizeof(float) * size_t((v->Td + 3) / 4 * 4) * v->R;
+    if (e == cudaSuccess) e = dmalloc(&v->w_irr, wi_bytes);
+    if (e == cudaSuccess) e = dmalloc(&v->w_dist, wd_bytes);
+    if (e == cudaSuccess) e = cudaMemset(v->w_irr, 0, wi_bytes);
+    if (e == cudaSuccess) e = cudaMemset(v->w_dist, 0, wd_bytes);
     if (e == cudaSuccess) e = dmalloc(&v->n_irr, sizeof(float) * 2 * v->Ti);
     if (e == cudaSuccess) e = dmalloc(&v->n_dist, sizeof(float) * 2 * v->Td);
     if (e == cudaSuccess) e = dmalloc(&v->status, sizeof(uint32_t) * 4);

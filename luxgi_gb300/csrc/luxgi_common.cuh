@@ -80,6 +80,40 @@ __device__ __forceinline__ f3 ray_direction(const float* rot, int r, int nrays) 
 }
 
 // probeLocation (DDGICommon.glsl:101-114)
+// Division by a run-time invariant d >= 1 as multiply-high and shift
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, theorem 4.2): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (mulhi(n, m) + n) >> l for
+// every 32-bit n.  Exact, so it replaces '/' and '%' without changing results.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    uint32_t l = 0;
+    while ((uint64_t(1) << l) < d) ++l;
+    f.s = l;
+    f.m = uint32_t(((uint64_t(1) << 32) * ((uint64_t(1) << l) - d)) / d + 1);
+    return f;
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return uint32_t((uint64_t(__umulhi(n, f.m)) + n) >> f.s);
+}
+
+// probeLocation with the grid index split by precomputed divisors of X and X*Y.
+__device__ __forceinline__ f3 probe_location(const luxgi_ddgi_uniform& u, uint32_t index, const FastDiv& div_x,
+                                             const FastDiv& div_xy) {
+    const uint32_t gz = fdiv(index, div_xy);
+    const uint32_t rem = index - gz * div_xy.d;
+    const uint32_t gy = fdiv(rem, div_x);
+    const uint32_t gx = rem - gy * div_x.d;
+    return f3{u.step[0] * float(int(gx)) + u.start_position[0], u.step[1] * float(int(gy)) + u.start_position[1],
+              u.step[2] * float(int(gz)) + u.start_position[2]};
+}
+
 __device__ __forceinline__ f3 probe_location(const luxgi_ddgi_uniform& u, int index) {
     const int X = u.probe_counts[0], Y = u.probe_counts[1];
     const int gx = index % X, gy = (index % (X * Y)) / X, gz = index / (X * Y);
@@ -517,15 +551,24 @@ __device__ __forceinline__ float atlas_load(const void* p, int storage, size_t i
     return __ldg(static_cast<const float*>(p) + i);
 }
 
+// GL REPEAT of texel index i over n texels: i mod n in [0, n).  The texel
+// coordinates of the probe atlases stay within one period of the atlas, so
+// the remainder is almost never needed.
+__device__ __forceinline__ int wrap_repeat(int i, int n) {
+    if (i >= 0 && i < n) return i;
+    if (i < 0 && i >= -n) return i + n;
+    if (i >= n && i < 2 * n) return i - n;
+    const int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
 // textureLod bilinear with REPEAT of channel ch (nc channels per texel).
 __device__ __forceinline__ float bilinear_repeat(const void* p, int storage, int W, int H, int nc, float u, float v, int ch) {
     const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
     const float fx = floorf(x), fy = floorf(y);
     const float a = x - fx, b = y - fy;
-    int i0 = int(fx) % W; if (i0 < 0) i0 += W;
-    int i1 = (int(fx) + 1) % W; if (i1 < 0) i1 += W;
-    int j0 = int(fy) % H; if (j0 < 0) j0 += H;
-    int j1 = (int(fy) + 1) % H; if (j1 < 0) j1 += H;
+    const int i0 = wrap_repeat(int(fx), W), i1 = wrap_repeat(int(fx) + 1, W);
+    const int j0 = wrap_repeat(int(fy), H), j1 = wrap_repeat(int(fy) + 1, H);
     const float t00 = atlas_load(p, storage, (size_t(j0) * W + i0) * nc + ch);
     const float t10 = atlas_load(p, storage, (size_t(j0) * W + i1) * nc + ch);
     const float t01 = atlas_load(p, storage, (size_t(j1) * W + i0) * nc + ch);
@@ -565,10 +608,8 @@ __device__ __forceinline__ void bilinear_repeat_v(const void* p, int storage, in
     const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
     const float fx = floorf(x), fy = floorf(y);
     const float a = x - fx, b = y - fy;
-    int i0 = int(fx) % W; if (i0 < 0) i0 += W;
-    int i1 = (int(fx) + 1) % W; if (i1 < 0) i1 += W;
-    int j0 = int(fy) % H; if (j0 < 0) j0 += H;
-    int j1 = (int(fy) + 1) % H; if (j1 < 0) j1 += H;
+    const int i0 = wrap_repeat(int(fx), W), i1 = wrap_repeat(int(fx) + 1, W);
+    const int j0 = wrap_repeat(int(fy), H), j1 = wrap_repeat(int(fy) + 1, H);
     float t00[NC], t10[NC], t01[NC], t11[NC];
     atlas_texel<NC>(p, storage, size_t(j0) * W + i0, t00);
     atlas_texel<NC>(p, storage, size_t(j0) * W + i1, t10);
@@ -607,6 +648,16 @@ __device__ __forceinline__ void probe_texel_origin(int probe, int W, int H, int 
     const float pwb = float(side) + 2.0f;
     const int ppr = (W - 2) / int(pwb);
     const float tlx = float(probe % ppr) * pwb + 2.0f, tly = float(probe / ppr) * pwb + 2.0f;
+    u = tlx / float(W) + nx;
+    v = tly / float(H) + ny;
+}
+
+// The same for a probe given by its atlas cell (cx, cy) = (probe mod X*Y,
+// probe div X*Y): the atlas holds X*Y cells per row, (W - 2) / (side + 2).
+__device__ __forceinline__ void cell_texel_origin(int cx, int cy, int W, int H, int side, float nx, float ny, float& u,
+                                                  float& v) {
+    const float pwb = float(side) + 2.0f;
+    const float tlx = float(cx) * pwb + 2.0f, tly = float(cy) * pwb + 2.0f;
     u = tlx / float(W) + nx;
     v = tly / float(H) + ny;
 }
@@ -658,11 +709,16 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         const f3 dtp = norm3(sub3(ppos, P));
         const float bf = mx(0.0001f, (dot3(dtp, N) + 1.0f) * 0.5f);
         weight = weight * (bf * bf + 0.2f);
-        const int pidx = g[0] + g[1] * cnt[0] + g[2] * cnt[0] * cnt[1];
+        // probe index g0 + g1 X + g2 X Y sits in atlas cell (g0 + g1 X, g2)
+        const int cell_x = g[0] + g[1] * cnt[0], cell_y = g[2];
         const f3 ptp = add3(sub3(P, ppos), vb);
         const f3 dir = norm3(mul3(ptp, -1.0f));
         float tu, tv;
-        tex_coord_from_dir(mul3(dir, -1.0f), pidx, u.depth_width, u.depth_height, u.depth_probe_side, tu, tv);
+        {
+            float ox, oy;
+            oct_texel_offset(mul3(dir, -1.0f), u.depth_width, u.depth_height, u.depth_probe_side, ox, oy);
+            cell_texel_origin(cell_x, cell_y, u.depth_width, u.depth_height, u.depth_probe_side, ox, oy, tu, tv);
+        }
         const float dist = len3(ptp);
         float mm[2];
         bilinear_repeat_v<2>(A.dist, A.storage, u.depth_width, u.depth_height, tu, tv, mm);
@@ -674,7 +730,8 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         cheb = mx(cheb * cheb * cheb, 0.0f);
         weight = weight * ((dist <= mean) ? 1.0f : cheb);
         weight = mx(0.000001f, weight);
-        probe_texel_origin(pidx, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny, tu, tv);
+        cell_texel_origin(cell_x, cell_y, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny, tu,
+                          tv);
         float ir[4];
         bilinear_repeat_v<4>(A.irr, A.storage, u.irradiance_width, u.irradiance_height, tu, tv, ir);
         const f3 pir{pow_decode(ir[0], ge), pow_decode(ir[1], ge), pow_decode(ir[2], ge)};

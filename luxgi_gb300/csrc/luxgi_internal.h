@@ -36,7 +36,21 @@ struct TraceParams {
     int march_variant;
     int shade_variant;
     int P, R;
+    int index32;             // P * R < 2^32: (probe, ray) from a 32-bit index
+    FastDiv div_p, div_x, div_xy;   // divisors P, X, X * Y
 };
+
+// (probe, ray) of linear work index idx = ray * P + probe.
+__device__ __forceinline__ void probe_ray(const TraceParams& p, int64_t idx, int& probe, int& ray) {
+    if (p.index32) {
+        const uint32_t r = fdiv(uint32_t(idx), p.div_p);
+        ray = int(r);
+        probe = int(uint32_t(idx) - r * p.div_p.d);
+    } else {
+        ray = int(idx / p.P);
+        probe = int(idx - int64_t(ray) * p.P);
+    }
+}
 
 struct BlendParams {
     luxgi_ddgi_uniform u;
@@ -46,8 +60,8 @@ struct BlendParams {
     const void* prev_dist;
     void* out_irr;
     void* out_dist;
-    float* w_irr;            // [Ti][R] cut weights
-    float* w_dist;           // [Td][R]
+    float* w_irr;            // [R][Ti rounded up to 4] cut weights, ray-major
+    float* w_dist;           // [R][Td rounded up to 4]
     float* n_irr;            // [Ti] 1/(2 sum w) or 1 (then the tensor-core normalisers)
     float* n_dist;           // [Td]
     __half* tcw_irr;         // [tc_ni][R] FP16 tensor-core weights, or nullptr
@@ -103,14 +117,14 @@ cudaError_t launch_shade_lists(const luxgi_surface_data& d, const luxgi_surface_
                                cudaStream_t st);
 cudaError_t launch_weights(const BlendParams& p, cudaStream_t st);
 cudaError_t launch_blend(const BlendParams& p, cudaStream_t st);
-// batched weights / blend (block-to-volume maps as above); pb_cap bounds the
-// probes a blend block takes (1-32)
+// batched weights / blend (block-to-volume maps as above); pp = probes per
+// thread of the FP32 blend tile (1, 2 or 4)
 int weight_rows(const BlendParams& p);
-int blend_blocks(const BlendParams& p, bool depth, int pb_cap);
-size_t blend_smem(const BlendParams& p, bool depth, int pb_cap);
+int blend_blocks(const BlendParams& p, bool depth, int pp);
+size_t blend_smem(const BlendParams& p, bool depth, int pp);
 cudaError_t launch_weights_batch(const BlendParams* vp, const int* starts, int n, int blocks, cudaStream_t st);
 cudaError_t launch_blend_batch(const BlendParams* vp, const int* starts_irr, int blocks_irr, size_t smem_irr,
-                               const int* starts_dist, int blocks_dist, size_t smem_dist, int n, int pb_cap,
+                               const int* starts_dist, int blocks_dist, size_t smem_dist, int n, int pp,
                                int storage, cudaStream_t st);
 cudaError_t launch_border(const luxgi_ddgi_uniform& u, void* irr, void* dist, int storage, cudaStream_t st);
 cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const float* gb0, const float* gb1,

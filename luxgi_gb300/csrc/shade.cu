@@ -18,8 +18,8 @@ namespace luxgi {
 // hits; writes the per-ray radiance + distance and the tensor-core operands.
 template <int MODE, int UNROLL>
 __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
-    const int probe = int(idx % p.P);
-    const int ray = int(idx / p.P);
+    int probe, ray;
+    probe_ray(p, idx, probe, ray);
     const size_t o = size_t(probe) * p.R + ray;
     const float4 h = p.hit_t[o];
     const int cls = p.hit_c[o];
@@ -30,7 +30,7 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
     } else if (cls >= 0) {
         const float4 d4 = __ldg(p.dirs + ray);
         const f3 dir{d4.x, d4.y, d4.z};
-        const f3 origin = probe_location(p.u, probe);
+        const f3 origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
         const f3 nrm{h.y, h.z, h.w};
         const f3 hp = add3(origin, mul3(dir, h.x));
         const float vs = p.sdf.data.cascade_voxel_size[cls];

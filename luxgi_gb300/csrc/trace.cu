@@ -64,11 +64,11 @@ cudaError_t launch_raygen_batch(const TraceParams* vp, const int* starts, int n,
 // kernel (no shading code): small, low register count, high occupancy.
 template <typename SdfT, int QMIP, int QTEX>
 __device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
-    const int probe = int(idx % p.P);
-    const int ray = int(idx / p.P);
+    int probe, ray;
+    probe_ray(p, idx, probe, ray);
     const float4 d4 = __ldg(p.dirs + ray);
     const f3 dir{d4.x, d4.y, d4.z};
-    const f3 origin = probe_location(p.u, probe);
+    const f3 origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
     const MarchHit hit = march_sdf<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps);
     int cls = -1;                                          // miss
     if (hit.time >= 0.0f) {
@@ -128,10 +128,11 @@ __global__ void __launch_bounds__(256, 4) march_pool_kernel(const TraceParams p)
     int cascade = 0, step = 0, steps = 0, fine = 0;
     bool setup = true;
     auto begin_ray = [&](int64_t idx) {
-        const int probe = int(idx % p.P), ray = int(idx / p.P);
+        int probe, ray;
+        probe_ray(p, idx, probe, ray);
         const float4 d4 = __ldg(p.dirs + ray);
         dir = f3{d4.x, d4.y, d4.z};
-        origin = probe_location(p.u, probe);
+        origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
         end = add3(origin, mul3(dir, tmax));
         next_start = 0.0f;
         cascade = 0;
@@ -140,7 +141,8 @@ __global__ void __launch_bounds__(256, 4) march_pool_kernel(const TraceParams p)
         setup = true;
     };
     auto finish_ray = [&](int64_t idx, float time, int hc, float hsdf, f3 nrm) {
-        const int probe = int(idx % p.P), ray = int(idx / p.P);
+        int probe, ray;
+        probe_ray(p, idx, probe, ray);
         int cls = -1;
         if (time >= 0.0f) cls = (hsdf <= 0.0f && time <= s.data.cascade_voxel_size[0]) ? -2 : hc;
         const size_t o = size_t(probe) * p.R + ray;

@@ -191,7 +191,7 @@ class DDGIBatch:
 
     @staticmethod
     def default_tuning() -> dict:
-        return {"march_variant": 4, "march_threads": 256, "shade_variant": 1, "blend_probes": 32, "use_graph": 1}
+        return {"march_variant": 4, "march_threads": 256, "shade_variant": 1, "blend_probes": 2, "use_graph": 1}
 
     def update(self, rots, stream=None) -> None:
         r = np.ascontiguousarray(np.asarray(rots, dtype=np.float32).reshape(len(self.volumes), 9))

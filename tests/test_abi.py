@@ -159,3 +159,23 @@ def test_scene_cards_follow_tile_convention():
             R = M[:3, :3]
             np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-6)
             np.testing.assert_allclose(tiles[t, 20:23], 2 * np.abs(R @ e), rtol=1e-6)
+
+
+def test_fastdiv_formula_exact():
+    """The multiply-high division the kernels use for probe / ray indices
+    (FastDiv in luxgi_common.cuh): (mulhi(n, m) + n) >> l == n // d."""
+    rng = np.random.default_rng(5)
+    divisors = [1, 2, 3, 5, 7, 8, 12, 255, 256, 1000, 16384, 131072, 65535, 65537, (1 << 26), (1 << 26) - 1,
+                (1 << 31) + 1, (1 << 32) - 1]
+    ns = np.concatenate([rng.integers(0, 1 << 32, 2000, dtype=np.uint64),
+                         np.array([0, 1, (1 << 32) - 1, (1 << 31), (1 << 31) - 1], dtype=np.uint64)])
+    for d in divisors:
+        l = 0
+        while (1 << l) < d:
+            l += 1
+        m = ((1 << 32) * ((1 << l) - d)) // d + 1
+        assert 0 < m < (1 << 32) or (d & (d - 1)) == 0
+        for n in ns.tolist() + [d - 1, d, d + 1, 2 * d - 1]:
+            n &= (1 << 32) - 1
+            q = (((n * m) >> 32) + n) >> l
+            assert q == n // d, (d, n)

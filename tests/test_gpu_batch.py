@@ -87,7 +87,7 @@ def test_batch_equals_single(cuda, blend, use_graph):
 
 def test_batch_fp16_storage_and_tuning_knobs(cuda):
     _, alone, batched = _pairs(N.BLEND_FP32, storage=N.STORAGE_FP16, n=4, seed=12)
-    batch = DDGIBatch(batched, {"march_variant": 5, "march_threads": 128, "blend_probes": 8})
+    batch = DDGIBatch(batched, {"march_variant": 5, "march_threads": 128, "blend_probes": 4})
     n = len(alone)
     for f in range(2):
         rots = _rots(n, f)
