@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--march-variant", type=int, default=None, help="override the volume's march variant (0-5)")
     ap.add_argument("--shade-variant", type=int, default=None, help="override the volume's shade variant (1,2,4,8)")
+    ap.add_argument("--ray-order", type=int, default=None, help="override the volume's ray order (0, 1)")
+    ap.add_argument("--march-budget", type=int, default=None, help="override the volume's march budget (-1 one pass)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serve200: length of the timed Poisson run")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serve200: requests per second, all sessions")
     ap.add_argument("--serve-budget-gb", type=float, default=120.0, help="serve200: device-memory budget")
@@ -200,6 +202,10 @@ def run_ours(args, rank: int, world: int):
         w = replace(w, volume=replace(w.volume, march_variant=args.march_variant))
     if args.shade_variant is not None:
         w = replace(w, volume=replace(w.volume, shade_variant=args.shade_variant))
+    if args.ray_order is not None:
+        w = replace(w, volume=replace(w.volume, ray_order=args.ray_order))
+    if args.march_budget is not None:
+        w = replace(w, volume=replace(w.volume, march_budget=args.march_budget))
     v = w.volume
     P, R = v.probes, v.rays_per_probe
     host = HostScene(w.scene)

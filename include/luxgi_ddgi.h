@@ -192,7 +192,20 @@ typedef struct luxgi_ddgi_volume_desc {
     int32_t shade_variant;         /* tuning, results identical: cage probes of
                                       sampleIrradiance per loop iteration
                                       (0 default = 1; 1, 2, 4 or 8)          */
-    int32_t reserved[6];
+    int32_t ray_order;             /* tuning, results identical: order of the
+                                      (probe, ray) work of march and shade.
+                                      0 every probe for ray 0, then ray 1 ...;
+                                      1 tiles of 256 consecutive probes, all
+                                      rays of a tile before the next (a warp
+                                      is 32 probes with one ray either way).
+                                      The pooled march variants use 0.       */
+    int32_t march_budget;          /* tuning, results identical: > 0 the march
+                                      runs every ray for at most this many
+                                      steps, queues the unfinished ones and
+                                      resumes them with full warps (twice,
+                                      then to the end); 0 (default) or -1 one
+                                      pass.  Per-ray variants 1-5.           */
+    int32_t reserved[4];
 } luxgi_ddgi_volume_desc;
 
 /* Device views of a volume's probe atlases. */
@@ -290,7 +303,8 @@ typedef struct luxgi_ddgi_batch_tuning {
     int32_t blend_probes;    /* probes per thread of the FP32-blend register
                                 tile (x 4 texels): 1, 2 or 4                 */
     int32_t use_graph;       /* 1 capture + replay a CUDA graph, 0 launch     */
-    int32_t reserved[3];
+    int32_t march_budget;    /* as luxgi_ddgi_volume_desc.march_budget        */
+    int32_t reserved[2];
     float frame_ms;          /* frame time measured by the autotuner, else 0  */
 } luxgi_ddgi_batch_tuning;
 

@@ -45,7 +45,8 @@ int compat_check(luxgi_ddgi_volume* const* vols, int n) {
 bool tuning_valid(const luxgi_ddgi_batch_tuning& t) {
     return t.march_variant >= 1 && t.march_variant <= 5 && (t.march_threads == 128 || t.march_threads == 256) &&
            (t.shade_variant == 1 || t.shade_variant == 2 || t.shade_variant == 4 || t.shade_variant == 8) &&
-           (t.blend_probes == 1 || t.blend_probes == 2 || t.blend_probes == 4) && (t.use_graph == 0 || t.use_graph == 1);
+           (t.blend_probes == 1 || t.blend_probes == 2 || t.blend_probes == 4) && (t.use_graph == 0 || t.use_graph == 1) &&
+           t.march_budget >= -1;
 }
 
 luxgi_ddgi_batch_tuning default_tuning() {
@@ -56,7 +57,22 @@ luxgi_ddgi_batch_tuning default_tuning() {
     t.shade_variant = 1;
     t.blend_probes = 2;
     t.use_graph = 1;
+    t.march_budget = 0;
     return t;
+}
+
+size_t plan_queue_bytes(const Plan& P) {
+    return P.budget > 0 ? sizeof(int4) * 2 * (size_t(P.qa_cap) + P.qb_cap) + 16 : 0;
+}
+
+void plan_set_queues(Plan& P, void* dev) {
+    if (P.budget <= 0 || !dev) {
+        P.q = nullptr;
+        P.qcount = nullptr;
+        return;
+    }
+    P.q = static_cast<int4*>(dev);
+    P.qcount = reinterpret_cast<uint32_t*>(P.q + 2 * (size_t(P.qa_cap) + P.qb_cap));
 }
 
 // Gives every volume the plan's march and shade variant (the packed SDF
@@ -91,11 +107,16 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
     P.starts.assign(size_t(kNumStages) * (n + 1), 0);
     int64_t acc[kNumStages] = {};
     if (P.tc) P.tcp.resize(n);
+    P.budget = 1 << 30;
     for (int i = 0; i < n; ++i) {
         const luxgi_ddgi_volume* v = vols[i];
         BlendParams b;
         volume_blend_params(v, b);
-        const int64_t PR = int64_t(v->P) * v->R;
+        const int64_t PR = trace_work(v->P, v->R, (v->desc.ray_order == 1 && v->desc.march_variant < 6) ? 1 : 0);
+        luxgi_ddgi_volume_desc vd = v->desc;
+        vd.march_budget = t.march_budget;
+        P.budget = std::min(P.budget, march_budget_for(vd, PR, int(v->sdf.data.cascades_count)));
+        P.work += PR;
         int64_t cnt[kNumStages];
         cnt[kRaygen] = (v->R + 127) / 128;
         cnt[kWeights] = weight_rows(b);
@@ -121,6 +142,13 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         P.starts[size_t(s) * (n + 1) + n] = int(acc[s]);
         P.blocks[s] = int(acc[s]);
     }
+    // the batch's queue entries hold 32-bit work indices per volume; the
+    // counters hold the whole batch's
+    if (P.work >= (int64_t(1) << 32)) P.budget = 0;
+    if (P.budget > 0) {
+        P.qa_cap = march_qa_cap(P.work);
+        P.qb_cap = march_qb_cap(P.work);
+    }
     return LUXGI_OK;
 }
 
@@ -131,6 +159,14 @@ void plan_fill(const Plan& P, const float* rots, uint8_t* host) {
     for (int i = 0; i < P.n; ++i) {
         const luxgi_ddgi_volume* v = P.vols[i];
         volume_trace_params(v, rots + 9 * i, tp[i]);
+        tp[i].budget1 = P.q ? P.budget : 0;
+        tp[i].budget2 = P.budget;
+        tp[i].qa = P.q;
+        tp[i].qb = P.q ? P.q + 2 * size_t(P.qa_cap) : nullptr;
+        tp[i].qcount = P.qcount;
+        tp[i].qa_cap = P.qa_cap;
+        tp[i].qb_cap = P.qb_cap;
+        tp[i].vol = i;
         volume_blend_params(v, bp[i]);
         if (P.tc) {
             TcBlendParams t;
@@ -176,7 +212,7 @@ cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cud
     if (e == cudaSuccess) e = launch_weights_batch(bp, d_starts + kWeights * n1, n, P.blocks[kWeights], st);
     if (e == cudaSuccess)
         e = launch_march_batch(tp, d_starts + kMarch * n1, n, P.blocks[kMarch], P.t.march_variant,
-                               P.t.march_threads, P.sdf_format, st);
+                               P.t.march_threads, P.sdf_format, P.q ? 1 : 0, P.qcount, st);
     if (e == cudaSuccess)
         e = launch_shade_batch(tp, d_starts + kShade * n1, n, P.blocks[kShade], P.light_mode, P.t.shade_variant, st);
     if (e != cudaSuccess) return e;
@@ -228,6 +264,7 @@ int run_group(luxgi_ddgi_volume* const* vols, int n, const float* rots, cudaStre
     luxgi_ddgi_batch_tuning t = default_tuning();
     t.march_variant = vols[0]->desc.march_variant;
     t.shade_variant = vols[0]->desc.shade_variant;
+    t.march_budget = vols[0]->desc.march_budget;
     t.use_graph = 0;
     Plan P;
     int s = plan_build(P, vols, n, t);
@@ -235,11 +272,13 @@ int run_group(luxgi_ddgi_volume* const* vols, int n, const float* rots, cudaStre
     s = prepare_all(P, st);
     if (s != LUXGI_OK) return s;
     std::vector<uint8_t> host(P.arg_bytes + P.starts.size() * sizeof(int));
+    const size_t qoff = align16(host.size());
+    uint8_t* dev = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&dev), qoff + plan_queue_bytes(P), st);
+    if (e != cudaSuccess) return cuda_status(e);
+    plan_set_queues(P, dev + qoff);
     plan_fill(P, rots, host.data());
     std::memcpy(host.data() + P.arg_bytes, P.starts.data(), P.starts.size() * sizeof(int));
-    uint8_t* dev = nullptr;
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&dev), host.size(), st);
-    if (e != cudaSuccess) return cuda_status(e);
     // pageable source: the copy has taken the bytes when the call returns
     e = cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = plan_launch(P, dev, reinterpret_cast<const int*>(dev + P.arg_bytes), st, nullptr);
@@ -258,7 +297,8 @@ struct luxgi_ddgi_batch {
     uint8_t* host[2] = {nullptr, nullptr};   // pinned per-frame argument blocks (double buffered)
     uint8_t* dev_args = nullptr;
     int* dev_starts = nullptr;
-    size_t dev_args_cap = 0, dev_starts_cap = 0, host_cap = 0;
+    void* dev_q = nullptr;                   // march compaction queues
+    size_t dev_args_cap = 0, dev_starts_cap = 0, host_cap = 0, dev_q_cap = 0;
     cudaStream_t cap = nullptr;              // capture stream
     Fork fork;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
@@ -299,6 +339,7 @@ void release(luxgi_ddgi_batch* b) {
     }
     if (b->dev_args) cudaFree(b->dev_args);
     if (b->dev_starts) cudaFree(b->dev_starts);
+    if (b->dev_q) cudaFree(b->dev_q);
     if (b->cap) cudaStreamDestroy(b->cap);
     fork_destroy(b->fork);
 }
@@ -314,6 +355,16 @@ int replan(luxgi_ddgi_batch* b, const luxgi_ddgi_batch_tuning& t) {
     if (s != LUXGI_OK) return s;
     s = plan_build(b->plan, vols.data(), int(vols.size()), t);
     if (s != LUXGI_OK) return s;
+    const size_t qb = plan_queue_bytes(b->plan);
+    if (qb > b->dev_q_cap) {
+        if (b->dev_q) cudaFree(b->dev_q);
+        b->dev_q = nullptr;
+        b->dev_q_cap = 0;
+        e = cudaMalloc(&b->dev_q, qb);
+        if (e != cudaSuccess) return cuda_status(e);
+        b->dev_q_cap = qb;
+    }
+    plan_set_queues(b->plan, b->dev_q);
     const Plan& P = b->plan;
     if (P.arg_bytes > b->host_cap) {
         for (int k = 0; k < 2; ++k) {
@@ -509,7 +560,8 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* 
             for (int j = i + 1; j < n; ++j) {
                 const luxgi_ddgi_volume* c = vols[j];
                 if (done[j] || !c->bound || c->desc.march_variant != mv ||
-                    c->desc.shade_variant != a->desc.shade_variant || c->desc.storage != a->desc.storage ||
+                    c->desc.shade_variant != a->desc.shade_variant || c->desc.march_budget != a->desc.march_budget ||
+                    c->desc.storage != a->desc.storage ||
                     c->desc.light_mode != a->desc.light_mode || c->tc != a->tc || c->sdf.format != a->sdf.format ||
                     c->device != a->device)
                     continue;
@@ -580,8 +632,9 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
         }
         return cs;
     };
-    // coordinate descent: march variant x rays per block, then shade
-    // variant, then the FP32 blend's probes per thread
+    // coordinate descent: march variant x rays per block, then the march
+    // compaction budget, then shade variant, then the FP32 blend's probes
+    // per thread
     for (int mv = 1; mv <= 5; ++mv) {
         for (int tpb : {128, 256}) {
             luxgi_ddgi_batch_tuning c = best;
@@ -590,6 +643,12 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
             c.use_graph = 1;
             consider(c);
         }
+    }
+    for (int mb : {0, 6, 8, 12}) {
+        luxgi_ddgi_batch_tuning c = best;
+        c.march_budget = mb;
+        const int cur = best.march_budget < 0 ? 0 : best.march_budget;
+        if (mb != cur) consider(c);
     }
     for (int sv : {1, 2, 4}) {
         luxgi_ddgi_batch_tuning c = best;

@@ -58,13 +58,13 @@ void free_volume(luxgi_ddgi_volume* v) {
     void* ptrs[] = {v->irr[0], v->irr[1], v->dist[0], v->dist[1], v->dirs_trace, v->dirs_blend, v->rays, v->info,
                     v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
                     v->status, v->hit_t, v->hit_c, v->w2l, v->shade_chunks, v->shade_culled, v->shade_scratch,
-                    v->sdf_quad, v->mip_quad};
+                    v->sdf_quad, v->mip_quad, v->mq, v->mq_count, v->cell_min};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
 
 SdfView sdf_view(const luxgi_sdf_desc& s) {
-    SdfView v;
+    SdfView v{};
     v.data = s.data;
     v.sdf = s.sdf;
     v.mip = s.mip;
@@ -99,6 +99,14 @@ size_t atlas_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 2 
 
 }  // namespace
 
+int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int cascades) {
+    const int mv = d.march_variant == 0 ? 4 : d.march_variant;
+    if (d.march_budget < 0 || mv >= 6) return 0;
+    // queue entries hold 32-bit work indices and 16-bit step totals
+    if (work >= (int64_t(1) << 32) || int64_t(cascades) * d.max_steps >= 65536) return 0;
+    return d.march_budget == 0 ? 0 : d.march_budget;   // default: one pass
+}
+
 uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,
                                     const luxgi_surface_desc& surf) {
     // mirrors the allocations of luxgi_ddgi_create and luxgi_ddgi_bind_scene
@@ -123,6 +131,7 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
     if (layout >= 3) b += quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
     if (layout == 4) b += quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
     if (layout == 5) b += pair_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
+    if (mv < 6) b += cell_min_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution);
     return b;
 }
 
@@ -158,6 +167,18 @@ int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
             v->sdf_quad_bytes = sq;
         }
     }
+    // cell minima for every per-ray march variant (the pooled march reads none)
+    const size_t cb = (mv >= 6) ? 0 : cell_min_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution);
+    if (cb != v->cell_min_bytes) {
+        if (v->cell_min) cudaFree(v->cell_min);
+        v->cell_min = nullptr;
+        v->cell_min_bytes = 0;
+        if (cb) {
+            const cudaError_t e = dmalloc(&v->cell_min, cb);
+            if (e != cudaSuccess) return cuda_status(e);
+            v->cell_min_bytes = cb;
+        }
+    }
     v->w2l_dirty = true;
     return LUXGI_OK;
 }
@@ -177,6 +198,10 @@ int luxgi::volume_prepare(luxgi_ddgi_volume* v, cudaStream_t st) {
     const int C = int(v->sdf.data.cascades_count), res = v->sdf.resolution, mres = v->sdf.mip_resolution;
     if (v->mip_quad) {
         e = launch_quad_pack(v->sdf.mip, mres * C, mres, mres, v->sdf.format, v->mip_quad, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    if (v->cell_min) {
+        e = launch_cell_min(v->sdf.sdf, res * C, res, res, v->sdf.format, v->cell_min, st);
         if (e != cudaSuccess) return cuda_status(e);
     }
     if (v->sdf_quad) {
@@ -200,6 +225,9 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.surf.culled = v->shade_culled;
     p.sdf.sdf_quad = v->sdf_quad;
     p.sdf.mip_quad = v->mip_quad;
+    p.sdf.cell_min = v->cell_min;
+    p.sdf.cw = (v->sdf.resolution * int(v->sdf.data.cascades_count) + kCellSide - 1) / kCellSide;
+    p.sdf.ch = (v->sdf.resolution + kCellSide - 1) / kCellSide;
     p.hit_t = v->hit_t;
     p.hit_c = v->hit_c;
     p.prev.irr = v->irr[v->ping_pong];
@@ -221,8 +249,20 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.bounce = (d.infinite_bounce && v->frames != 0) ? 1 : 0;
     p.P = v->P;
     p.R = v->R;
-    p.index32 = (uint64_t(v->P) * uint64_t(v->R)) < (uint64_t(1) << 32) ? 1 : 0;
+    p.order = (d.ray_order == 1 && d.march_variant < 6) ? 1 : 0;
+    p.work = trace_work(v->P, v->R, p.order);
+    p.index32 = p.work < (int64_t(1) << 32) ? 1 : 0;
     p.div_p = make_fastdiv(uint32_t(v->P));
+    p.div_r = make_fastdiv(uint32_t(v->R));
+    const int budget = v->mq ? march_budget_for(d, p.work, int(v->sdf.data.cascades_count)) : 0;
+    p.budget1 = budget;
+    p.budget2 = budget;
+    p.qa = v->mq;
+    p.qb = v->mq ? v->mq + 2 * size_t(v->mqa_cap) : nullptr;
+    p.qcount = v->mq_count;
+    p.qa_cap = v->mqa_cap;
+    p.qb_cap = v->mqb_cap;
+    p.vol = 0;
     p.div_x = make_fastdiv(uint32_t(d.uniform.probe_counts[0]));
     p.div_xy = make_fastdiv(uint32_t(d.uniform.probe_counts[0]) * uint32_t(d.uniform.probe_counts[1]));
 }
@@ -280,6 +320,21 @@ namespace {
 
 int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     if (!v->bound) return LUXGI_ENOTBOUND;
+    const int order = (v->desc.ray_order == 1 && v->desc.march_variant < 6) ? 1 : 0;
+    const int64_t work = trace_work(v->P, v->R, order);
+    if (!v->mq && march_budget_for(v->desc, work, int(v->sdf.data.cascades_count)) > 0) {
+        // queues of the compacted march, made on the first trace that needs them
+        const uint32_t ca = march_qa_cap(work), cb = march_qb_cap(work);
+        cudaError_t e = dmalloc(&v->mq, sizeof(int4) * 2 * (size_t(ca) + cb));
+        if (e == cudaSuccess) e = dmalloc(&v->mq_count, 2 * sizeof(uint32_t));
+        if (e != cudaSuccess) {
+            if (v->mq) cudaFree(v->mq);
+            v->mq = nullptr;
+            return cuda_status(e);
+        }
+        v->mqa_cap = ca;
+        v->mqb_cap = cb;
+    }
     TraceParams p;
     volume_trace_params(v, rot, p);
     BlendParams b;
@@ -392,6 +447,8 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
     if (desc->max_steps < 1) return LUXGI_EINVAL;
     if (desc->march_variant < 0 || desc->march_variant > 9) return LUXGI_EINVAL;
+    if (desc->ray_order != 0 && desc->ray_order != 1) return LUXGI_EINVAL;
+    if (desc->march_budget < -1) return LUXGI_EINVAL;
     if (desc->shade_variant != 0 && desc->shade_variant != 1 && desc->shade_variant != 2 &&
         desc->shade_variant != 4 && desc->shade_variant != 8)
         return LUXGI_EINVAL;

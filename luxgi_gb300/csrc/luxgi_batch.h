@@ -23,7 +23,18 @@ struct Plan {
     int blocks[kNumStages] = {};
     size_t smem_i = 0, smem_d = 0;      // dynamic shared memory of the FP32 blend
     std::vector<TcPlan> tcp;            // tensor-core blend maps, one per volume
+    // march compaction shared by the plan's volumes (budget 0: one pass)
+    int budget = 0;
+    int64_t work = 0;                   // march work items of all volumes
+    uint32_t qa_cap = 0, qb_cap = 0;
+    int4* q = nullptr;                  // device queues + counters (plan_set_queues)
+    uint32_t* qcount = nullptr;
 };
+
+// Device bytes of the plan's march queues and counters (0 without compaction),
+// and binding them to a device region of that size (16-byte aligned).
+size_t plan_queue_bytes(const Plan& P);
+void plan_set_queues(Plan& P, void* dev);
 
 int compat_check(luxgi_ddgi_volume* const* vols, int n);
 bool tuning_valid(const luxgi_ddgi_batch_tuning& t);

@@ -34,6 +34,27 @@ __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y
 __device__ __forceinline__ float len3(f3 a) { return sqrtf(dot3(a, a)); }
 __device__ __forceinline__ f3 norm3(f3 a) { float inv = 1.0f / sqrtf(dot3(a, a)); return mul3(a, inv); }
 
+// x / d for a divisor fixed over a loop.  When d is a power of two (with a
+// normal reciprocal) x * (1 / d) is the same real number as x / d and both
+// round it once, so the multiply gives the IEEE quotient bit for bit;
+// otherwise the division itself runs.
+struct ExactDiv {
+    float d, inv;
+    bool pow2;
+};
+
+__device__ __forceinline__ ExactDiv exact_div(float d) {
+    ExactDiv e;
+    const uint32_t b = __float_as_uint(d);
+    const uint32_t ex = (b >> 23) & 0xFFu;
+    e.d = d;
+    e.pow2 = (b & 0x7FFFFFu) == 0u && ex >= 2u && ex <= 252u;
+    e.inv = e.pow2 ? 1.0f / d : 0.0f;
+    return e;
+}
+
+__device__ __forceinline__ float xdiv(float x, const ExactDiv& e) { return e.pow2 ? x * e.inv : x / e.d; }
+
 // sin/cos for the Fibonacci azimuth: Cody-Waite reduction by pi/2 and Taylor
 // polynomials of degree 9 (sin) and 8 (cos) on [-pi/4, pi/4].
 __device__ __forceinline__ void fib_sincos(float x, float* s, float* c) {
@@ -223,9 +244,31 @@ struct SdfView {
     const void* sdf_quad;   // packed copy of the full-resolution volume (quad or
                             // pair layout, march variants 4 / 5) or nullptr
     const void* mip_quad;   // quad-packed mip (variants 3-5) or nullptr
+    // Conservative cell minima of the full-resolution volume: cell (i, j, k)
+    // holds the minimum texel over [4i, 4i+4] x [4j, 4j+4] x [4k, 4k+4]
+    // (clamped), every texel a trilinear footprint whose lower corner lies in
+    // the cell can read.  nullptr: not built.
+    const float* cell_min;
+    int cw, ch;             // cells along x (packed cascades) and y
     int res, mres, C;
     int format;   // luxgi_storage of the sdf/mip texels
 };
+
+constexpr int kCellSide = 4;
+
+// True when the trilinear full-resolution sample at packed texture
+// coordinates (u, v, w) is certainly >= thr: every texel it interpolates is
+// >= the cell minimum, and a convex combination of values >= m > 0 computed
+// in FP32 is >= m (1 - 2^-20); the caller's thr carries that margin.
+__device__ __forceinline__ bool fine_sample_at_least(const SdfView& s, float u, float v, float w, float thr) {
+    const int W = s.res * s.C, H = s.res, D = s.res;
+    const int x0 = imn(imx(int(floorf(u * float(W) - 0.5f)), 0), W - 1);
+    const int y0 = imn(imx(int(floorf(v * float(H) - 0.5f)), 0), H - 1);
+    const int z0 = imn(imx(int(floorf(w * float(D) - 0.5f)), 0), D - 1);
+    const float m = __ldg(s.cell_min + (size_t(z0 / kCellSide) * s.ch + size_t(y0 / kCellSide)) * s.cw +
+                          size_t(x0 / kCellSide));
+    return m >= thr;
+}
 
 // One GL trilinear sample of the full-resolution or mip volume, from the
 // plain layout or from its quad-packed copy (same values either way).
@@ -261,78 +304,135 @@ struct MarchHit {
     float sdf;
 };
 
+// Where a ray's march stands between calls of march_run: the cascade (and
+// whether its entry was computed), the step within it, the march distance
+// t, the cascade's exit distance, the next cascade's start, and the step and
+// full-resolution sample totals.  Everything else is recomputed from the
+// ray's origin and direction.
+struct MarchState {
+    int cascade;
+    int in_cascade;
+    int step;
+    float t, is_y, next_start;
+    int steps, fine;
+};
+
+__device__ __forceinline__ void march_state_init(MarchState& m) {
+    m.cascade = 0;
+    m.in_cascade = 0;
+    m.step = 0;
+    m.t = 0.0f;
+    m.is_y = 0.0f;
+    m.next_start = 0.0f;
+    m.steps = 0;
+    m.fine = 0;
+}
+
 // tracyGlobalSDF (SDFCommon.glsl:98-194) with stepScale 1, start bias 0,
-// hit normal requested (GISDFRays.comp:79-87).  QMIP / QTEX select the
-// layouts (VolLayout) read for the mip / full-resolution volume.
+// hit normal requested (GISDFRays.comp:79-87), run for at most `budget`
+// steps: returns true with `hit` filled when the march ended (hit, or every
+// cascade left), false when the budget ran out first (m holds the state to
+// resume from).  Resuming performs exactly the arithmetic of an unbroken
+// march.  QMIP / QTEX select the layouts (VolLayout) read for the mip /
+// full-resolution volume.
 template <typename T, int QMIP = kPlain, int QTEX = kPlain>
-__device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps) {
+__device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps,
+                                          MarchState& m, int budget, MarchHit& hit) {
     const int C = s.C;
     const int TW = s.res * C, MW = s.mres * C;
-    MarchHit hit;
-    hit.normal = f3{0.0f, 0.0f, 0.0f};
-    hit.time = -1.0f;
-    hit.cascade = 0;
-    hit.steps = 0;
-    hit.fine = 0;
-    hit.sdf = 0.0f;
     const float tmax = mn(trace_max, s.data.cascade_pos_distance[C - 1][3] * 2.0f);
     const float chunk = 32.0f / s.data.resolution;
     const float margin = 4.0f / s.data.resolution;
-    float next_start = 0.0f;
+    // cell minimum at or above this: the full-resolution value is >= 2 margin
+    // and unused (SDFCommon.glsl:150-158), so its taps need not be read
+    const float skip_thr = (margin * 2.0f) * 1.001f;
     const f3 end = add3(origin, mul3(dir, tmax));
-    for (int cascade = 0; cascade < C && hit.time < 0.0f; ++cascade) {
+    for (; m.cascade < C; ++m.cascade) {
+        const int cascade = m.cascade;
         const float cx = s.data.cascade_pos_distance[cascade][0], cy = s.data.cascade_pos_distance[cascade][1],
                     cz = s.data.cascade_pos_distance[cascade][2], cw = s.data.cascade_pos_distance[cascade][3];
         const float voxel = s.data.cascade_voxel_size[cascade];
         const float voxel_half = voxel * 0.5f;
         const f3 wpos = add3(origin, mul3(dir, voxel * 0.0f));
-        // lineHitAABB (SDFCommon.glsl:84-95)
-        const f3 d = sub3(end, wpos);
-        const f3 inv{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-        const f3 en{((cx - cw) - wpos.x) * inv.x, ((cy - cw) - wpos.y) * inv.y, ((cz - cw) - wpos.z) * inv.z};
-        const f3 ex{((cx + cw) - wpos.x) * inv.x, ((cy + cw) - wpos.y) * inv.y, ((cz + cw) - wpos.z) * inv.z};
-        const float i0 = mx(mn(en.x, ex.x), mx(mn(en.y, ex.y), mn(en.z, ex.z)));
-        const float i1 = mn(mx(en.x, ex.x), mn(mx(en.y, ex.y), mx(en.z, ex.z)));
-        float is_x = clampf(i0, 0.0f, 1.0f) * tmax;
-        const float is_y = clampf(i1, 0.0f, 1.0f) * tmax;
-        is_x = mx(is_x, next_start);
-        float t = is_x;
-        if (is_x >= is_y) t = is_y;
-        else next_start = is_y;
+        if (!m.in_cascade) {
+            // lineHitAABB (SDFCommon.glsl:84-95)
+            const f3 d = sub3(end, wpos);
+            const f3 inv{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+            const f3 en{((cx - cw) - wpos.x) * inv.x, ((cy - cw) - wpos.y) * inv.y, ((cz - cw) - wpos.z) * inv.z};
+            const f3 ex{((cx + cw) - wpos.x) * inv.x, ((cy + cw) - wpos.y) * inv.y, ((cz + cw) - wpos.z) * inv.z};
+            const float i0 = mx(mn(en.x, ex.x), mx(mn(en.y, ex.y), mn(en.z, ex.z)));
+            const float i1 = mn(mx(en.x, ex.x), mn(mx(en.y, ex.y), mx(en.z, ex.z)));
+            float is_x = clampf(i0, 0.0f, 1.0f) * tmax;
+            m.is_y = clampf(i1, 0.0f, 1.0f) * tmax;
+            is_x = mx(is_x, m.next_start);
+            m.t = is_x;
+            if (is_x >= m.is_y) m.t = m.is_y;
+            else m.next_start = m.is_y;
+            m.step = 0;
+            m.in_cascade = 1;
+        }
         const float md = cw * 2.0f;
-        const float invC = float(C);
-        int step = 0;
-        for (; step < max_steps && t < is_y; ++step) {
+        const ExactDiv div_md = exact_div(md), div_c = exact_div(float(C)), div_voxel = exact_div(voxel);
+        float t = m.t;
+        int step = m.step;
+        for (; step < max_steps && t < m.is_y; ++step) {
+            if (budget <= 0) {
+                m.t = t;
+                m.step = step;
+                return false;
+            }
+            --budget;
             const f3 sp = add3(wpos, mul3(dir, t));
             // getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
-            const float ux = clampf((sp.x - cx) / md + 0.5f, 0.0f, 1.0f);
-            const float uy = clampf((sp.y - cy) / md + 0.5f, 0.0f, 1.0f);
-            const float uz = clampf((sp.z - cz) / md + 0.5f, 0.0f, 1.0f);
-            const float tu = (float(cascade) + ux) / invC;
+            const float ux = clampf(xdiv(sp.x - cx, div_md) + 0.5f, 0.0f, 1.0f);
+            const float uy = clampf(xdiv(sp.y - cy, div_md) + 0.5f, 0.0f, 1.0f);
+            const float uz = clampf(xdiv(sp.z - cz, div_md) + 0.5f, 0.0f, 1.0f);
+            const float tu = xdiv(float(cascade) + ux, div_c);
             // the full-resolution taps are issued together with the mip taps
-            // (one memory round trip per step); their value is used only
-            // where SDFCommon.glsl:150-158 samples the full-resolution SDF
+            // (one memory round trip per step) unless the cell minima show
+            // their value cannot be used; it is used only where
+            // SDFCommon.glsl:150-158 samples the full-resolution SDF
+            const bool need_fine = !s.cell_min || !fine_sample_at_least(s, tu, uy, uz, skip_thr);
             float sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
-            const float sdt = sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz);
+            const float sdt = need_fine ? sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz) : 1.0f;
             if (sd < chunk) {
-                ++hit.fine;
+                ++m.fine;
                 if (sdt < margin * 2.0f) sd = sdt;
             } else {
                 sd = chunk;
             }
             sd = sd * md;
-            const float thick = voxel_half * clampf(t / voxel, 0.0f, 1.0f);
+            const float thick = voxel_half * clampf(xdiv(t, div_voxel), 0.0f, 1.0f);
             if (sd < thick) {
                 hit.time = mx(t + sd - thick, 0.0f);
                 hit.cascade = cascade;
                 hit.sdf = sd;
                 hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, tu, uy, uz, 1.0f / s.data.resolution);
-                break;
+                hit.steps = m.steps + step;
+                hit.fine = m.fine;
+                return true;
             }
             t = t + mx(sd * 1.0f, voxel);
         }
-        hit.steps += step;
+        m.steps += step;
+        m.in_cascade = 0;
     }
+    hit.normal = f3{0.0f, 0.0f, 0.0f};
+    hit.time = -1.0f;
+    hit.cascade = 0;
+    hit.sdf = 0.0f;
+    hit.steps = m.steps;
+    hit.fine = m.fine;
+    return true;
+}
+
+// The whole march in one call.
+template <typename T, int QMIP = kPlain, int QTEX = kPlain>
+__device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps) {
+    MarchState m;
+    march_state_init(m);
+    MarchHit hit;
+    march_run<T, QMIP, QTEX>(s, origin, dir, trace_max, max_steps, m, 0x7FFFFFFF, hit);
     return hit;
 }
 

@@ -36,12 +36,47 @@ struct TraceParams {
     int march_variant;
     int shade_variant;
     int P, R;
-    int index32;             // P * R < 2^32: (probe, ray) from a 32-bit index
-    FastDiv div_p, div_x, div_xy;   // divisors P, X, X * Y
+    int order;               // ray order: 0 ray-major over all probes, 1 probe tiles (kProbeTile)
+    int index32;             // work < 2^32: (probe, ray) from a 32-bit index
+    int64_t work;            // march / shade work items (P * R, or whole tiles x R)
+    FastDiv div_p, div_r, div_x, div_xy;   // divisors P, R, X, X * Y
+    // march compaction: pass 1 marches every ray for at most budget1 steps
+    // and queues the unfinished ones (qa); pass 2 resumes them for budget2
+    // more (unfinished into qb); pass 3 finishes qb.  budget1 == 0: one pass.
+    int4* qa;                // [qa_cap][2] suspended marches
+    int4* qb;                // [qb_cap][2]
+    uint32_t* qcount;        // [0] entries pushed to qa, [1] to qb
+    uint32_t qa_cap, qb_cap;
+    int budget1, budget2;
+    int vol;                 // this volume's index in a batched launch (queue entries)
 };
 
-// (probe, ray) of linear work index idx = ray * P + probe.
-__device__ __forceinline__ void probe_ray(const TraceParams& p, int64_t idx, int& probe, int& ray) {
+constexpr int kProbeTile = 256;
+
+// Work items of the march and shade launches of a volume in ray order `order`.
+inline int64_t trace_work(int P, int R, int order) {
+    if (order == 1) return (int64_t(P) + kProbeTile - 1) / kProbeTile * kProbeTile * R;
+    return int64_t(P) * R;
+}
+
+// (probe, ray) of work item idx; false for the padding of the last tile.
+//   order 0: idx = ray * P + probe
+//   order 1: idx = (tile * R + ray) * kProbeTile + j, probe = tile * kProbeTile + j
+__device__ __forceinline__ bool probe_ray(const TraceParams& p, int64_t idx, int& probe, int& ray) {
+    if (p.order == 1) {
+        const int64_t tr = idx / kProbeTile;
+        const int j = int(idx % kProbeTile);
+        int64_t tile;
+        if (p.index32) {
+            tile = fdiv(uint32_t(tr), p.div_r);
+        } else {
+            tile = tr / p.R;
+        }
+        ray = int(tr - tile * p.R);
+        const int64_t pr = tile * kProbeTile + j;
+        probe = int(pr);
+        return pr < p.P;
+    }
     if (p.index32) {
         const uint32_t r = fdiv(uint32_t(idx), p.div_p);
         ray = int(r);
@@ -50,6 +85,7 @@ __device__ __forceinline__ void probe_ray(const TraceParams& p, int64_t idx, int
         ray = int(idx / p.P);
         probe = int(idx - int64_t(ray) * p.P);
     }
+    return true;
 }
 
 struct BlendParams {
@@ -99,15 +135,23 @@ __device__ __forceinline__ const T& stage_params(const T* __restrict__ src, uint
 }
 
 cudaError_t launch_raygen_batch(const TraceParams* vp, const int* starts, int n, int blocks, cudaStream_t st);
-// variant 1-5 as TraceParams::march_variant; tpb 128 or 256 rays a block
+// Suspended-march queue capacities for `work` work items (entries of 32 B).
+inline uint32_t march_qa_cap(int64_t work) { return uint32_t((work * 3 + 4) / 5); }
+inline uint32_t march_qb_cap(int64_t work) { return uint32_t((work + 4) / 5); }
+// variant 1-5 as TraceParams::march_variant; tpb 128 or 256 rays a block.
+// With compaction (budget1 > 0 in the parameter blocks) the batch shares the
+// queues q (two int4 per entry, capacities qa_cap / qb_cap, counters qcount)
+// and the resume passes follow the first.
 cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, int blocks, int variant, int tpb,
-                               int sdf_format, cudaStream_t st);
+                               int sdf_format, int compact, uint32_t* qcount, cudaStream_t st);
 cudaError_t launch_shade_batch(const TraceParams* vp, const int* starts, int n, int blocks, int light_mode,
                                int shade_variant, cudaStream_t st);
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 size_t quad_bytes(int W, int H, int D, int format);
+size_t cell_min_bytes(int W, int H, int D);
+cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, float* dst, cudaStream_t st);
 cudaError_t launch_quad_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);
 size_t pair_bytes(int W, int H, int D, int format);
 cudaError_t launch_pair_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);

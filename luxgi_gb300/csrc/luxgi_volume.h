@@ -47,6 +47,11 @@ struct luxgi_ddgi_volume {
     size_t sdf_quad_bytes = 0, mip_quad_bytes = 0;
     luxgi_sdf_desc sdf{};
     luxgi_surface_desc surf{};
+    float* cell_min = nullptr;          // conservative cell minima of the full-resolution SDF
+    size_t cell_min_bytes = 0;
+    int4* mq = nullptr;                 // suspended-march queues (march compaction)
+    uint32_t* mq_count = nullptr;
+    uint32_t mqa_cap = 0, mqb_cap = 0;
 };
 
 
@@ -62,6 +67,10 @@ void volume_blend_params(const luxgi_ddgi_volume* v, BlendParams& p);
 void volume_tc_params(const luxgi_ddgi_volume* v, TcBlendParams& p);
 // (Re)allocates the packed SDF copies the volume's march variant reads.
 int volume_alloc_packs(luxgi_ddgi_volume* v);
+// Steps of the first march pass with compaction for a volume whose work is
+// `work` items and whose march variant / budget / step cap are those of d;
+// 0 when the march runs in one pass.
+int march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int cascades);
 // Device bytes a volume of description d allocates once bound to the scene
 // (luxgi_ddgi_create + luxgi_ddgi_bind_scene; debug ray records excluded).
 uint64_t volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,

@@ -121,6 +121,7 @@ luxgi_ddgi_batch_tuning server_tuning(const luxgi_server_desc& d) {
     if (d.tuning.march_threads) t.march_threads = d.tuning.march_threads;
     if (d.tuning.shade_variant) t.shade_variant = d.tuning.shade_variant;
     if (d.tuning.blend_probes) t.blend_probes = d.tuning.blend_probes;
+    t.march_budget = d.tuning.march_budget;
     t.use_graph = 0;
     return t;
 }
@@ -278,7 +279,8 @@ int cuda_launch(luxgi_server* S, Slot& sl, const std::vector<Session*>& members)
     int s = plan_build(P, vols.data(), int(vols.size()), S->tuning);
     if (s != LUXGI_OK) return s;
     const size_t sb = P.starts.size() * sizeof(int);
-    const size_t need = P.arg_bytes + sb;
+    const size_t qoff = (P.arg_bytes + sb + 15) & ~size_t(15);
+    const size_t need = qoff + plan_queue_bytes(P);
     if (need > sl.cap) {
         if (sl.host) cudaFreeHost(sl.host);
         if (sl.dev) cudaFree(sl.dev);
@@ -293,9 +295,10 @@ int cuda_launch(luxgi_server* S, Slot& sl, const std::vector<Session*>& members)
     }
     s = prepare_all(P, sl.st);
     if (s != LUXGI_OK) return s;
+    plan_set_queues(P, sl.dev + qoff);
     plan_fill(P, rots.data(), sl.host);
     std::memcpy(sl.host + P.arg_bytes, P.starts.data(), sb);
-    cudaError_t e = cudaMemcpyAsync(sl.dev, sl.host, need, cudaMemcpyHostToDevice, sl.st);
+    cudaError_t e = cudaMemcpyAsync(sl.dev, sl.host, P.arg_bytes + sb, cudaMemcpyHostToDevice, sl.st);
     if (e == cudaSuccess) e = plan_launch(P, sl.dev, reinterpret_cast<const int*>(sl.dev + P.arg_bytes), sl.st, nullptr);
     if (e == cudaSuccess) e = cudaEventRecord(sl.ev, sl.st);
     if (e != cudaSuccess) return cuda_status(e);

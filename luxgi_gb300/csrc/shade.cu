@@ -19,7 +19,7 @@ namespace luxgi {
 template <int MODE, int UNROLL>
 __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
     int probe, ray;
-    probe_ray(p, idx, probe, ray);
+    if (!probe_ray(p, idx, probe, ray)) return;
     const size_t o = size_t(probe) * p.R + ray;
     const float4 h = p.hit_t[o];
     const int cls = p.hit_c[o];
@@ -87,7 +87,7 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
 template <int MODE, int UNROLL>
 __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= int64_t(p.P) * p.R) return;
+    if (idx >= p.work) return;
     shade_ray<MODE, UNROLL>(p, idx);
 }
 
@@ -100,12 +100,12 @@ __global__ void __launch_bounds__(128)
     const int v = batch_volume(starts, n, int(blockIdx.x));
     const TraceParams& p = stage_params(vp + v, sp);
     const int64_t idx = int64_t(int(blockIdx.x) - __ldg(starts + v)) * 128 + threadIdx.x;
-    if (idx >= int64_t(p.P) * p.R) return;
+    if (idx >= p.work) return;
     shade_ray<MODE, UNROLL>(p, idx);
 }
 
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st) {
-    const int64_t total = int64_t(p.P) * p.R;
+    const int64_t total = p.work;
     if (total <= 0) return cudaSuccess;
     const unsigned sblocks = unsigned((total + 127) / 128);
     if (p.light_mode == LUXGI_LIGHT_PER_HIT) {

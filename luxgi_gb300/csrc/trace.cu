@@ -62,14 +62,7 @@ cudaError_t launch_raygen_batch(const TraceParams* vp, const int* starts, int n,
 // with the same ray index, so a warp marches 32 parallel rays from
 // neighbouring probes through nearby SDF texels.  The march is the whole
 // kernel (no shading code): small, low register count, high occupancy.
-template <typename SdfT, int QMIP, int QTEX>
-__device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
-    int probe, ray;
-    probe_ray(p, idx, probe, ray);
-    const float4 d4 = __ldg(p.dirs + ray);
-    const f3 dir{d4.x, d4.y, d4.z};
-    const f3 origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
-    const MarchHit hit = march_sdf<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps);
+__device__ __forceinline__ void write_march(const TraceParams& p, int probe, int ray, const MarchHit& hit) {
     int cls = -1;                                          // miss
     if (hit.time >= 0.0f) {
         // GISDFRays.comp:93: a hit at the probe from inside a surface
@@ -81,11 +74,111 @@ __device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
     if (p.info) p.info[o] = make_int4(hit.steps, hit.time >= 0.0f ? hit.cascade : -1, hit.fine, 0);
 }
 
+// Suspended-march queue entry: (work item, volume, cascade | in-cascade << 7
+// | step << 8, steps | fine << 16), (t, exit, next start, 0).
+__device__ __forceinline__ void encode_march(int64_t idx, int vol, const MarchState& m, int4& a, float4& b) {
+    a = make_int4(int(uint32_t(idx)), vol, m.cascade | (m.in_cascade << 7) | (m.step << 8), m.steps | (m.fine << 16));
+    b = make_float4(m.t, m.is_y, m.next_start, 0.0f);
+}
+
+__device__ __forceinline__ void decode_march(const int4& a, const float4& b, int64_t& idx, int& vol, MarchState& m) {
+    idx = int64_t(uint32_t(a.x));
+    vol = a.y;
+    m.cascade = a.z & 0x7F;
+    m.in_cascade = (a.z >> 7) & 1;
+    m.step = int(uint32_t(a.z) >> 8);
+    m.steps = a.w & 0xFFFF;
+    m.fine = int(uint32_t(a.w) >> 16);
+    m.t = b.x;
+    m.is_y = b.y;
+    m.next_start = b.z;
+}
+
+// Appends the suspended marches of the calling lanes that want it, one
+// atomic per group of converged lanes.  False where the queue is full (the
+// lane then finishes its march in place).
+__device__ __forceinline__ bool enqueue_march(int4* q, uint32_t* count, uint32_t cap, bool want, int64_t idx, int vol,
+                                              const MarchState& m) {
+    const unsigned act = __activemask();
+    const unsigned ball = __ballot_sync(act, want);
+    if (!ball) return false;
+    const int lane = int(threadIdx.x) & 31;
+    const int leader = __ffs(ball) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, uint32_t(__popc(ball)));
+    base = __shfl_sync(act, base, leader);
+    if (!want) return false;
+    const uint32_t slot = base + uint32_t(__popc(ball & ((1u << lane) - 1u)));
+    if (slot >= cap) return false;
+    int4 ea;
+    float4 eb;
+    encode_march(idx, vol, m, ea, eb);
+    q[2 * size_t(slot)] = ea;
+    reinterpret_cast<float4*>(q)[2 * size_t(slot) + 1] = eb;
+    return true;
+}
+
+// One work item: the whole march, or (compaction) at most budget1 steps
+// with the rest queued.
+template <typename SdfT, int QMIP, int QTEX>
+__device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
+    int probe, ray;
+    const bool valid = probe_ray(p, idx, probe, ray);
+    MarchState m;
+    march_state_init(m);
+    MarchHit hit;
+    bool done = true;
+    if (valid) {
+        const float4 d4 = __ldg(p.dirs + ray);
+        const f3 dir{d4.x, d4.y, d4.z};
+        const f3 origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
+        done = march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m,
+                                           p.budget1 > 0 ? p.budget1 : 0x7FFFFFFF, hit);
+        if (p.budget1 > 0 && enqueue_march(p.qa, p.qcount, p.qa_cap, !done, idx, p.vol, m)) return;
+        if (!done) march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m, 0x7FFFFFFF, hit);
+        write_march(p, probe, ray, hit);
+    }
+}
+
+// Resumes queued marches: pass 2 (FINAL false) reads qa, runs budget2 more
+// steps and queues the unfinished into qb; pass 3 (FINAL) finishes qb.
+// Persistent blocks walk the queue.  vp: batched parameter blocks indexed
+// by each entry's volume, or nullptr (then p).
+template <typename SdfT, int QMIP, int QTEX, bool FINAL>
+__device__ __forceinline__ void march_resume(const TraceParams& p0, const TraceParams* __restrict__ vp) {
+    const int4* in = FINAL ? p0.qb : p0.qa;
+    const uint32_t n = min(__ldg(p0.qcount + (FINAL ? 1 : 0)), FINAL ? p0.qb_cap : p0.qa_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int64_t idx;
+        int vol;
+        MarchState m;
+        decode_march(__ldg(in + 2 * size_t(i)), __ldg(reinterpret_cast<const float4*>(in) + 2 * size_t(i) + 1), idx,
+                     vol, m);
+        const TraceParams& p = vp ? vp[vol] : p0;
+        int probe, ray;
+        probe_ray(p, idx, probe, ray);
+        const float4 d4 = __ldg(p.dirs + ray);
+        const f3 dir{d4.x, d4.y, d4.z};
+        const f3 origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
+        MarchHit hit;
+        bool done = march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m,
+                                                FINAL ? 0x7FFFFFFF : p.budget2, hit);
+        if (!FINAL && enqueue_march(p0.qb, p0.qcount + 1, p0.qb_cap, !done, idx, vol, m)) continue;
+        if (!done) march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m, 0x7FFFFFFF, hit);
+        write_march(p, probe, ray, hit);
+    }
+}
+
 template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= int64_t(p.P) * p.R) return;
+    if (idx >= p.work) return;
     march_ray<SdfT, QMIP, QTEX>(p, idx);
+}
+
+template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX, bool FINAL>
+__global__ void __launch_bounds__(256, MIN_BLOCKS) march_resume_kernel(const TraceParams p) {
+    march_resume<SdfT, QMIP, QTEX, FINAL>(p, nullptr);
 }
 
 // Batched march over many volumes: TPB rays per block, the volume's
@@ -98,8 +191,15 @@ __global__ void __launch_bounds__(TPB, MIN_BLOCKS)
     const int v = batch_volume(starts, n, int(blockIdx.x));
     const TraceParams& p = stage_params(vp + v, sp);
     const int64_t idx = int64_t(int(blockIdx.x) - __ldg(starts + v)) * TPB + threadIdx.x;
-    if (idx >= int64_t(p.P) * p.R) return;
+    if (idx >= p.work) return;
     march_ray<SdfT, QMIP, QTEX>(p, idx);
+}
+
+// Resume passes of a batch: every volume's parameter block names the same
+// queues; entries carry their volume.
+template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX, bool FINAL>
+__global__ void __launch_bounds__(256, MIN_BLOCKS) march_resume_batch_kernel(const TraceParams* __restrict__ vp) {
+    march_resume<SdfT, QMIP, QTEX, FINAL>(vp[0], vp);
 }
 
 // ------------------------------------------------------- pooled march
@@ -234,8 +334,39 @@ __global__ void __launch_bounds__(256, 4) march_pool_kernel(const TraceParams p)
     }
 }
 
+static unsigned resume_blocks() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return unsigned(sms * 4);
+}
+
+// One march variant: pass 1 over every work item, then (compaction) the two
+// resume passes over the queued rays.
+template <typename SdfT, int MINB, int QMIP, int QTEX>
+static cudaError_t launch_march_variant(const TraceParams& p, cudaStream_t st) {
+    const unsigned mblocks = unsigned((p.work + 255) / 256);
+    if (p.budget1 > 0) {
+        const cudaError_t e = cudaMemsetAsync(p.qcount, 0, 2 * sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+    }
+    march_kernel<SdfT, MINB, QMIP, QTEX><<<mblocks, 256, 0, st>>>(p);
+    note_launch();
+    if (p.budget1 > 0) {
+        const unsigned rb = resume_blocks();
+        march_resume_kernel<SdfT, MINB, QMIP, QTEX, false><<<rb, 256, 0, st>>>(p);
+        march_resume_kernel<SdfT, MINB, QMIP, QTEX, true><<<rb, 256, 0, st>>>(p);
+        note_launch(2);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
-    const int64_t total = int64_t(p.P) * p.R;
+    const int64_t total = p.work;
     if (total <= 0) return cudaSuccess;
     if (p.march_variant >= 6) {
         // pooled march: 8 rays per lane, 8 warps per block
@@ -266,66 +397,65 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
         note_launch();
         return launch_shade(p, st);
     }
-    const unsigned mblocks = unsigned((total + 255) / 256);
     // variants: 1 plain layout, 64 registers (4 blocks of 256 per SM);
     // 2 plain layout, no register bound; 3 quad-packed mip; 4 quad-packed
     // mip and full-resolution volume; 5 quad-packed mip, pair-packed
     // full-resolution volume.  All produce identical results.
     const bool h = p.sdf.format == LUXGI_STORAGE_FP16;
+    cudaError_t e;
     switch (p.march_variant) {
-        case 2:
-            if (h) march_kernel<__half, 1, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 1, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
-            break;
-        case 3:
-            if (h) march_kernel<__half, 4, kQuad, kPlain><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 4, kQuad, kPlain><<<mblocks, 256, 0, st>>>(p);
-            break;
-        case 4:
-            if (h) march_kernel<__half, 4, kQuad, kQuad><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 4, kQuad, kQuad><<<mblocks, 256, 0, st>>>(p);
-            break;
-        case 5:
-            if (h) march_kernel<__half, 4, kQuad, kPair><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 4, kQuad, kPair><<<mblocks, 256, 0, st>>>(p);
-            break;
-        default:
-            if (h) march_kernel<__half, 4, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
-            else march_kernel<float, 4, kPlain, kPlain><<<mblocks, 256, 0, st>>>(p);
-            break;
+        case 2: e = h ? launch_march_variant<__half, 1, kPlain, kPlain>(p, st) : launch_march_variant<float, 1, kPlain, kPlain>(p, st); break;
+        case 3: e = h ? launch_march_variant<__half, 4, kQuad, kPlain>(p, st) : launch_march_variant<float, 4, kQuad, kPlain>(p, st); break;
+        case 4: e = h ? launch_march_variant<__half, 4, kQuad, kQuad>(p, st) : launch_march_variant<float, 4, kQuad, kQuad>(p, st); break;
+        case 5: e = h ? launch_march_variant<__half, 4, kQuad, kPair>(p, st) : launch_march_variant<float, 4, kQuad, kPair>(p, st); break;
+        default: e = h ? launch_march_variant<__half, 4, kPlain, kPlain>(p, st) : launch_march_variant<float, 4, kPlain, kPlain>(p, st); break;
     }
-    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    note_launch();
     return launch_shade(p, st);
+}
+
+template <typename SdfT, int TPB, int MINB, int QMIP, int QTEX>
+static void march_batch_launch(unsigned blocks, const TraceParams* vp, const int* starts, int n, bool compact,
+                               cudaStream_t st) {
+    march_batch_kernel<SdfT, TPB, MINB, QMIP, QTEX><<<blocks, TPB, 0, st>>>(vp, starts, n);
+    if (compact) {
+        constexpr int RMINB = MINB == 1 ? 1 : 4;   // resume kernels run 256-thread blocks
+        const unsigned rb = resume_blocks();
+        march_resume_batch_kernel<SdfT, RMINB, QMIP, QTEX, false><<<rb, 256, 0, st>>>(vp);
+        march_resume_batch_kernel<SdfT, RMINB, QMIP, QTEX, true><<<rb, 256, 0, st>>>(vp);
+    }
 }
 
 template <typename SdfT, int TPB, int MINB>
 static void march_batch_variant(int variant, unsigned blocks, const TraceParams* vp, const int* starts, int n,
-                                cudaStream_t st) {
+                                bool compact, cudaStream_t st) {
     switch (variant) {
-        case 2: march_batch_kernel<SdfT, TPB, 1, kPlain, kPlain><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
-        case 3: march_batch_kernel<SdfT, TPB, MINB, kQuad, kPlain><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
-        case 4: march_batch_kernel<SdfT, TPB, MINB, kQuad, kQuad><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
-        case 5: march_batch_kernel<SdfT, TPB, MINB, kQuad, kPair><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
-        default: march_batch_kernel<SdfT, TPB, MINB, kPlain, kPlain><<<blocks, TPB, 0, st>>>(vp, starts, n); break;
+        case 2: march_batch_launch<SdfT, TPB, 1, kPlain, kPlain>(blocks, vp, starts, n, compact, st); break;
+        case 3: march_batch_launch<SdfT, TPB, MINB, kQuad, kPlain>(blocks, vp, starts, n, compact, st); break;
+        case 4: march_batch_launch<SdfT, TPB, MINB, kQuad, kQuad>(blocks, vp, starts, n, compact, st); break;
+        case 5: march_batch_launch<SdfT, TPB, MINB, kQuad, kPair>(blocks, vp, starts, n, compact, st); break;
+        default: march_batch_launch<SdfT, TPB, MINB, kPlain, kPlain>(blocks, vp, starts, n, compact, st); break;
     }
 }
 
 cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, int blocks, int variant, int tpb,
-                               int sdf_format, cudaStream_t st) {
+                               int sdf_format, int compact, uint32_t* qcount, cudaStream_t st) {
     if (blocks <= 0) return cudaSuccess;
     if (variant < 1 || variant > 5 || (tpb != 128 && tpb != 256)) return cudaErrorInvalidValue;
+    if (compact) {
+        const cudaError_t e = cudaMemsetAsync(qcount, 0, 2 * sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+    }
     const bool h = sdf_format == LUXGI_STORAGE_FP16;
     // bounded variants keep 64 registers a thread (1024 resident threads per SM)
     if (tpb == 128) {
-        if (h) march_batch_variant<__half, 128, 8>(variant, unsigned(blocks), vp, starts, n, st);
-        else march_batch_variant<float, 128, 8>(variant, unsigned(blocks), vp, starts, n, st);
+        if (h) march_batch_variant<__half, 128, 8>(variant, unsigned(blocks), vp, starts, n, compact != 0, st);
+        else march_batch_variant<float, 128, 8>(variant, unsigned(blocks), vp, starts, n, compact != 0, st);
     } else {
-        if (h) march_batch_variant<__half, 256, 4>(variant, unsigned(blocks), vp, starts, n, st);
-        else march_batch_variant<float, 256, 4>(variant, unsigned(blocks), vp, starts, n, st);
+        if (h) march_batch_variant<__half, 256, 4>(variant, unsigned(blocks), vp, starts, n, compact != 0, st);
+        else march_batch_variant<float, 256, 4>(variant, unsigned(blocks), vp, starts, n, compact != 0, st);
     }
-    note_launch();
+    note_launch(compact ? 3 : 1);
     return cudaGetLastError();
 }
 
@@ -346,6 +476,43 @@ __global__ void world_to_local_kernel(const luxgi_surface_object* __restrict__ o
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     world_to_local_kernel<<<(n + 127) / 128, 128, 0, st>>>(objs, n, w2l);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ cell minima
+// Cell (i, j, k) of a W x H x D volume: min over texels [4i, 4i+4] x
+// [4j, 4j+4] x [4k, 4k+4] clamped to the volume (every texel of a trilinear
+// footprint whose clamped lower corner lies in the cell).
+template <typename T>
+__global__ void cell_min_kernel(const T* __restrict__ src, int W, int H, int D, int cw, int ch, int cd,
+                                float* __restrict__ dst) {
+    const int64_t n = int64_t(cw) * ch * cd;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const int cx = int(i % cw), cy = int((i / cw) % ch), cz = int(i / (int64_t(cw) * ch));
+        float m = 3.0e38f;
+        for (int z = cz * kCellSide; z <= imn(cz * kCellSide + kCellSide, D - 1); ++z)
+            for (int y = cy * kCellSide; y <= imn(cy * kCellSide + kCellSide, H - 1); ++y)
+                for (int x = cx * kCellSide; x <= imn(cx * kCellSide + kCellSide, W - 1); ++x)
+                    m = mn(m, load_val(src, (size_t(z) * H + y) * W + x));
+        dst[i] = m;
+    }
+}
+
+size_t cell_min_bytes(int W, int H, int D) {
+    return sizeof(float) * size_t((W + kCellSide - 1) / kCellSide) * ((H + kCellSide - 1) / kCellSide) *
+           ((D + kCellSide - 1) / kCellSide);
+}
+
+cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, float* dst, cudaStream_t st) {
+    const int cw = (W + kCellSide - 1) / kCellSide, ch = (H + kCellSide - 1) / kCellSide;
+    const int cd = (D + kCellSide - 1) / kCellSide;
+    const int64_t n = int64_t(cw) * ch * cd;
+    const unsigned blocks = unsigned(std::min<int64_t>((n + 255) / 256, 4096));
+    if (format == LUXGI_STORAGE_FP16)
+        cell_min_kernel<__half><<<blocks, 256, 0, st>>>(static_cast<const __half*>(src), W, H, D, cw, ch, cd, dst);
+    else
+        cell_min_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(src), W, H, D, cw, ch, cd, dst);
     note_launch();
     return cudaGetLastError();
 }

@@ -55,6 +55,8 @@ class VolumeSpec:
     sky: tuple = (0.5, 0.6, 0.8)
     march_variant: int = 0
     shade_variant: int = 0
+    ray_order: int = 0
+    march_budget: int = 0
 
     @property
     def probes(self) -> int:
@@ -93,6 +95,8 @@ class VolumeSpec:
             d.sky_radiance[k] = self.sky[k]
         d.march_variant = self.march_variant
         d.shade_variant = self.shade_variant
+        d.ray_order = self.ray_order
+        d.march_budget = self.march_budget
         return d
 
 

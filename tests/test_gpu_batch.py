@@ -180,4 +180,5 @@ def test_batch_launch_count(cuda, blend):
     torch.cuda.synchronize()
     per_frame = lib.luxgi_launch_count() - c0
     # raygen, weights, march, shade + blend: 2 FP32 launches, or 2 per volume
-    assert per_frame == (6 if blend == N.BLEND_FP32 else 4 + 2 * 3)
+    # (the default march is one pass)
+    assert per_frame == 4 + (2 if blend == N.BLEND_FP32 else 2 * 3)

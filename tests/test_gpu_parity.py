@@ -368,6 +368,29 @@ def test_march_variants_bit_identical(cuda, fmt):
         assert np.array_equal(rad, outs[0][0]) and np.array_equal(info, outs[0][1])
 
 
+@pytest.mark.parametrize("fmt", [N.STORAGE_FP32, N.STORAGE_FP16])
+def test_march_compaction_and_ray_order_bit_identical(cuda, fmt):
+    """Suspending marches after a step budget and resuming them from the
+    queues (budgets 1, 2, 8; budget 1 overflows the queues, whose rays then
+    finish in place), and the tiled ray order, give exactly the one-pass
+    results, and those equal the FP32 oracle."""
+    from dataclasses import replace
+
+    base = tiny_workload(probe_counts=(7, 3, 5), rays=64, sdf=64, sdf_format=fmt, cascades=2, room=20.0, prims=10)
+    outs = []
+    for mv, budget, order in ((4, -1, 0), (4, 1, 0), (4, 2, 0), (4, 8, 0), (3, 2, 1), (5, 8, 1), (1, -1, 1)):
+        w = replace(base, volume=replace(base.volume, march_variant=mv, march_budget=budget, ray_order=order))
+        host, dev, vol, inp = setup(w)
+        rot = frame_rotation(51, 0)
+        vol.trace(rot)
+        rad, ref = _check_trace(vol, inp, vol.desc, rot)
+        _, _, info = vol.rays()
+        outs.append((rad, info.cpu().numpy()))
+    assert outs[0][1][..., 0].max() > 8          # some rays outlast the budgets
+    for rad, info in outs[1:]:
+        assert np.array_equal(rad, outs[0][0]) and np.array_equal(info, outs[0][1])
+
+
 def test_shade_variants_consistent(cuda):
     """Unrolling the cage-probe loop of sampleIrradiance changes scheduling
     (and where FMAs contract): the per-hit bounce radiance of every shade
