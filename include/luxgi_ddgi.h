@@ -333,6 +333,15 @@ int luxgi_ddgi_batch_get_tuning(const luxgi_ddgi_batch* batch, luxgi_ddgi_batch_
 int luxgi_ddgi_batch_set_tuning(luxgi_ddgi_batch* batch, const luxgi_ddgi_batch_tuning* tuning);
 int luxgi_ddgi_batch_destroy(luxgi_ddgi_batch* batch);
 
+/* Per-stage timing: with timing on, every trace / probe update records CUDA
+ * events on its stream between its stages; luxgi_ddgi_stage_times waits for
+ * the last frame's events and writes its milliseconds: [0] ray generation,
+ * weights and scene set-up, [1] march (all passes), [2] hit shading,
+ * [3] probe update (0 when none followed the trace).  Entry points also
+ * push NVTX ranges (no cost without a profiler attached). */
+int luxgi_ddgi_set_stage_timing(luxgi_ddgi_volume* vol, int enable);
+int luxgi_ddgi_stage_times(luxgi_ddgi_volume* vol, float out[4]);
+
 int luxgi_ddgi_get_atlases(const luxgi_ddgi_volume* vol, luxgi_ddgi_atlases* out);
 int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* vol, luxgi_ddgi_rays* out);
 /* Synchronise `stream` and read the volume's device status word: returns

@@ -168,6 +168,8 @@ DDGI_API = [
     ("luxgi_ddgi_batch_get_tuning", c_int, [c_void_p, POINTER(BatchTuning)]),
     ("luxgi_ddgi_batch_set_tuning", c_int, [c_void_p, POINTER(BatchTuning)]),
     ("luxgi_ddgi_batch_destroy", c_int, [c_void_p]),
+    ("luxgi_ddgi_set_stage_timing", c_int, [c_void_p, c_int]),
+    ("luxgi_ddgi_stage_times", c_int, [c_void_p, POINTER(c_float)]),
     ("luxgi_ddgi_get_atlases", c_int, [c_void_p, POINTER(Atlases)]),
     ("luxgi_ddgi_get_rays", c_int, [c_void_p, POINTER(Rays)]),
     ("luxgi_ddgi_check_status", c_int, [c_void_p, c_void_p]),

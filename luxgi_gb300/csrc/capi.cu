@@ -10,6 +10,7 @@
 #include <new>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "luxgi_volume.h"
 
@@ -339,24 +340,44 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     volume_trace_params(v, rot, p);
     BlendParams b;
     volume_blend_params(v, b);
+    nvtxRangePushA("luxgi_ddgi_trace");
+    auto mark = [&](int i) { if (v->stage_timing) cudaEventRecord(v->stage_ev[i], st); };
+    mark(0);
+    v->stage_blend_recorded = false;
     cudaError_t e = launch_raygen(p.rot, v->R, v->desc.storage, v->dirs_trace, v->dirs_blend, st);
-    if (e != cudaSuccess) return cuda_status(e);
-    e = launch_weights(b, st);
-    if (e != cudaSuccess) return cuda_status(e);
-    const int s = volume_prepare(v, st);
-    if (s != LUXGI_OK) return s;
-    return cuda_status(launch_trace(p, st));
+    if (e == cudaSuccess) e = launch_weights(b, st);
+    int s = e == cudaSuccess ? volume_prepare(v, st) : cuda_status(e);
+    if (s == LUXGI_OK) {
+        mark(1);
+        s = cuda_status(launch_march(p, st));
+    }
+    if (s == LUXGI_OK) {
+        mark(2);
+        s = cuda_status(launch_shade(p, st));
+        mark(3);
+    }
+    nvtxRangePop();
+    return s;
 }
 
 int do_probe_update(luxgi_ddgi_volume* v, cudaStream_t st) {
+    nvtxRangePushA("luxgi_ddgi_probe_update");
+    cudaError_t e;
     if (v->tc) {
         TcBlendParams p;
         volume_tc_params(v, p);
-        return cuda_status(launch_tc_blend(p, st));
+        e = launch_tc_blend(p, st);
+    } else {
+        BlendParams p;
+        volume_blend_params(v, p);
+        e = launch_blend(p, st);
     }
-    BlendParams p;
-    volume_blend_params(v, p);
-    return cuda_status(launch_blend(p, st));
+    if (e == cudaSuccess && v->stage_timing) {
+        e = cudaEventRecord(v->stage_ev[4], st);
+        v->stage_blend_recorded = true;
+    }
+    nvtxRangePop();
+    return cuda_status(e);
 }
 
 }  // namespace
@@ -514,6 +535,8 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
 
 int luxgi_ddgi_destroy(luxgi_ddgi_volume* v) {
     if (!v) return LUXGI_EINVAL;
+    for (cudaEvent_t& ev : v->stage_ev)
+        if (ev) cudaEventDestroy(ev);
     free_volume(v);
     delete v;
     return LUXGI_OK;
@@ -636,6 +659,28 @@ int luxgi_ddgi_check_status(luxgi_ddgi_volume* v, void* stream) {
     e = cudaMemsetAsync(v->status, 0, sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     return e == cudaSuccess ? LUXGI_ETIMEOUT : cuda_status(e);
+}
+
+int luxgi_ddgi_set_stage_timing(luxgi_ddgi_volume* v, int enable) {
+    if (!v) return LUXGI_EINVAL;
+    if (enable && !v->stage_ev[0]) {
+        for (cudaEvent_t& ev : v->stage_ev) {
+            const cudaError_t e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return cuda_status(e);
+        }
+    }
+    v->stage_timing = enable != 0;
+    return LUXGI_OK;
+}
+
+int luxgi_ddgi_stage_times(luxgi_ddgi_volume* v, float out[4]) {
+    if (!v || !out) return LUXGI_EINVAL;
+    if (!v->stage_timing) return LUXGI_EINVAL;
+    cudaError_t e = cudaEventSynchronize(v->stage_blend_recorded ? v->stage_ev[4] : v->stage_ev[3]);
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = cudaEventElapsedTime(&out[i], v->stage_ev[i], v->stage_ev[i + 1]);
+    out[3] = 0.0f;
+    if (e == cudaSuccess && v->stage_blend_recorded) e = cudaEventElapsedTime(&out[3], v->stage_ev[3], v->stage_ev[4]);
+    return cuda_status(e);
 }
 
 int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* v, int enable) {

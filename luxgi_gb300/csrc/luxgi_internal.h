@@ -146,7 +146,7 @@ cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, 
                                int sdf_format, int compact, uint32_t* qcount, cudaStream_t st);
 cudaError_t launch_shade_batch(const TraceParams* vp, const int* starts, int n, int blocks, int light_mode,
                                int shade_variant, cudaStream_t st);
-cudaError_t launch_trace(const TraceParams& p, cudaStream_t st);
+cudaError_t launch_march(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 size_t quad_bytes(int W, int H, int D, int format);

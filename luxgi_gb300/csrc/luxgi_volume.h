@@ -49,6 +49,12 @@ struct luxgi_ddgi_volume {
     luxgi_surface_desc surf{};
     float* cell_min = nullptr;          // conservative cell minima of the full-resolution SDF
     size_t cell_min_bytes = 0;
+    // per-stage CUDA events of the last frame (luxgi_ddgi_set_stage_timing):
+    // [0] trace start, [1] march start, [2] shade start, [3] trace end,
+    // [4] probe update end
+    cudaEvent_t stage_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool stage_timing = false;
+    bool stage_blend_recorded = false;
     int4* mq = nullptr;                 // suspended-march queues (march compaction)
     uint32_t* mq_count = nullptr;
     uint32_t mqa_cap = 0, mqb_cap = 0;

@@ -365,7 +365,7 @@ static cudaError_t launch_march_variant(const TraceParams& p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
+cudaError_t launch_march(const TraceParams& p, cudaStream_t st) {
     const int64_t total = p.work;
     if (total <= 0) return cudaSuccess;
     if (p.march_variant >= 6) {
@@ -395,7 +395,7 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         note_launch();
-        return launch_shade(p, st);
+        return cudaSuccess;
     }
     // variants: 1 plain layout, 64 registers (4 blocks of 256 per SM);
     // 2 plain layout, no register bound; 3 quad-packed mip; 4 quad-packed
@@ -410,8 +410,7 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t st) {
         case 5: e = h ? launch_march_variant<__half, 4, kQuad, kPair>(p, st) : launch_march_variant<float, 4, kQuad, kPair>(p, st); break;
         default: e = h ? launch_march_variant<__half, 4, kPlain, kPlain>(p, st) : launch_march_variant<float, 4, kPlain, kPlain>(p, st); break;
     }
-    if (e != cudaSuccess) return e;
-    return launch_shade(p, st);
+    return e;
 }
 
 template <typename SdfT, int TPB, int MINB, int QMIP, int QTEX>

@@ -89,6 +89,15 @@ class DDGIVolume:
     def set_debug_rays(self, on: bool = True) -> None:
         N.check(N.ddgi().luxgi_ddgi_set_debug_rays(self._h, 1 if on else 0), "set_debug_rays")
 
+    def set_stage_timing(self, on: bool = True) -> None:
+        N.check(N.ddgi().luxgi_ddgi_set_stage_timing(self._h, 1 if on else 0), "set_stage_timing")
+
+    def stage_times(self) -> dict:
+        """Milliseconds of the last frame's stages (waits for them)."""
+        out = (ctypes.c_float * 4)()
+        N.check(N.ddgi().luxgi_ddgi_stage_times(self._h, out), "stage_times")
+        return {"setup": out[0], "march": out[1], "shade": out[2], "blend": out[3]}
+
     def trace(self, rot, stream=None) -> None:
         r = N.floats(np.asarray(rot, dtype=np.float32).ravel())
         N.check(N.ddgi().luxgi_ddgi_trace(self._h, r, _stream(stream)), "trace")
