@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--shade-variant", type=int, default=None, help="override the volume's shade variant (1,2,4,8)")
     ap.add_argument("--ray-order", type=int, default=None, help="override the volume's ray order (0, 1)")
     ap.add_argument("--march-budget", type=int, default=None, help="override the volume's march budget (-1 one pass)")
+    ap.add_argument("--shade-order", type=int, default=None, help="override the volume's shading order (0, 1)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serve200: length of the timed Poisson run")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serve200: requests per second, all sessions")
     ap.add_argument("--serve-budget-gb", type=float, default=120.0, help="serve200: device-memory budget")
@@ -124,14 +125,20 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def traffic_from_profile(workload: str, kernel: str):
-    """DRAM bytes per launch of `kernel` from a committed ncu summary, if any."""
+def traffic_from_profile(workload: str, kernel: str, work_items: int):
+    """DRAM bytes of one launch of `kernel` on `workload`, from the committed
+    ncu capture summary (profiles/traffic.json): bytes per work item of the
+    captured case times this launch's work items (the capture runs a smaller
+    case of the same scene; traffic grows with the rays marched)."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     try:
         d = json.loads(p.read_text())
-        return d.get(workload, {}).get(kernel)
+        e = d.get(workload, {}).get(kernel)
+        if not e:
+            return None
+        return int(e["dram_bytes_per_item"] * work_items)
     except Exception:
         return None
 
@@ -206,6 +213,8 @@ def run_ours(args, rank: int, world: int):
         w = replace(w, volume=replace(w.volume, ray_order=args.ray_order))
     if args.march_budget is not None:
         w = replace(w, volume=replace(w.volume, march_budget=args.march_budget))
+    if args.shade_order is not None:
+        w = replace(w, volume=replace(w.volume, shade_order=args.shade_order))
     v = w.volume
     P, R = v.probes, v.rays_per_probe
     host = HostScene(w.scene)
@@ -241,12 +250,16 @@ def run_ours(args, rank: int, world: int):
         hits = (info[..., 1] >= 0).sum().item()
         steps_total += s
         fine_total += fine
-        march_bytes.append((s * 8 + fine * 8 + hits * 48) * esz + P * R * out_b)
+        # SDFCommon.glsl reads per step 8 mip taps, per full-resolution sample
+        # 8 taps, per hit 6 x 8 normal taps; the march writes a 20-byte record
+        march_bytes.append((s * 8 + fine * 8 + hits * 48) * esz + P * R * 20)
     vol.set_debug_rays(False)
     torch.cuda.synchronize()
 
     flush = torch.empty(256 << 20, dtype=torch.int8, device=dev_t)
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    vol.set_stage_timing(True)          # CUDA events between the stages, on the launching stream
+    stages = []
     clocks = Clocks(local)
     launches0 = N.ddgi().luxgi_launch_count()
     if world > 1:
@@ -262,8 +275,10 @@ def run_ours(args, rank: int, world: int):
         vol.probe_update(stream)
         ev[k][2].record(stream)
         vol.end_frame()
+        stages.append(vol.stage_times())   # waits for this frame (outside its events)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
+    vol.set_stage_timing(False)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
@@ -313,14 +328,16 @@ def run_ours(args, rank: int, world: int):
 
     pk = peaks()
     avg_trace_ms = sum(t_trace) / K
+    stage_avg = {k: sum(s[k] for s in stages) / K for k in ("setup", "march", "shade", "blend")}
     avg_bytes = sum(march_bytes) / K
-    achieved = avg_bytes / (avg_trace_ms / 1e3) / 1e9
-    traffic = traffic_from_profile(w.name, "trace_kernel")
-    roofline = {"kernel": "trace_kernel (ray gen + SDF march + hit shading)", "bound": "hbm",
+    achieved = avg_bytes / (stage_avg["march"] / 1e3) / 1e9
+    traffic = traffic_from_profile(w.name, "march_kernel", P * R)
+    roofline = {"kernel": "march_kernel (global-SDF sphere tracing)", "bound": "hbm",
                 "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_source": pk["source"],
                 "traffic": traffic, "algorithmic_bytes_per_launch": int(avg_bytes),
-                "avg_launch_ms": round(avg_trace_ms, 4), "avg_march_steps_per_ray": round(steps_total / (K * P * R), 2),
+                "avg_launch_ms": round(stage_avg["march"], 4),
+                "avg_march_steps_per_ray": round(steps_total / (K * P * R), 2),
                 "avg_fine_samples_per_ray": round(fine_total / (K * P * R), 2)}
     if rank != 0:
         return
@@ -337,7 +354,8 @@ def run_ours(args, rank: int, world: int):
                    "light_mode": "per-hit bounce" if v.light_mode else "light cache",
                    "blend": "tensor" if v.blend else "fp32 simt", "storage": "fp16" if v.storage else "fp32",
                    "parallelism": f"replicas{world}", "l2": "256 MB flush between frames (outside the events)"},
-        "stage_ms": {"trace": round(avg_trace_ms, 4), "blend": round(sum(t_blend) / K, 4)},
+        "stage_ms": {"trace": round(avg_trace_ms, 4), "blend": round(sum(t_blend) / K, 4),
+                     **{k: round(x, 4) for k, x in stage_avg.items()}},
         "wall_s": round(wall, 4),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
         "irradiance_rel_err_vs_fp64": err, "clocks": clk,

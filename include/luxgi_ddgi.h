@@ -203,9 +203,15 @@ typedef struct luxgi_ddgi_volume_desc {
                                       runs every ray for at most this many
                                       steps, queues the unfinished ones and
                                       resumes them with full warps (twice,
-                                      then to the end); 0 (default) or -1 one
-                                      pass.  Per-ray variants 1-5.           */
-    int32_t reserved[4];
+                                      then to the end); 0 default (= 8); -1
+                                      one pass.  Per-ray variants 1-5.       */
+    int32_t shade_order;           /* tuning, results identical: 0 default
+                                      (= 1); 1 bin the hits by their surface-
+                                      cache chunk first (histogram, scan,
+                                      scatter) so a warp shades nearby hits;
+                                      -1 shade in march order.  Per-ray march
+                                      variants 1-5.                          */
+    int32_t reserved[3];
 } luxgi_ddgi_volume_desc;
 
 /* Device views of a volume's probe atlases. */

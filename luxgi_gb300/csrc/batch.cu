@@ -167,6 +167,9 @@ void plan_fill(const Plan& P, const float* rots, uint8_t* host) {
         tp[i].qa_cap = P.qa_cap;
         tp[i].qb_cap = P.qb_cap;
         tp[i].vol = i;
+        tp[i].bin_count = nullptr;      // batched launches shade in march order
+        tp[i].bin_key = nullptr;
+        tp[i].shade_seq = nullptr;
         volume_blend_params(v, bp[i]);
         if (P.tc) {
             TcBlendParams t;
@@ -644,10 +647,10 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
             consider(c);
         }
     }
-    for (int mb : {0, 6, 8, 12}) {
+    for (int mb : {-1, 6, 8, 12}) {
         luxgi_ddgi_batch_tuning c = best;
         c.march_budget = mb;
-        const int cur = best.march_budget < 0 ? 0 : best.march_budget;
+        const int cur = best.march_budget == 0 ? 8 : best.march_budget;
         if (mb != cur) consider(c);
     }
     for (int sv : {1, 2, 4}) {

@@ -59,7 +59,8 @@ void free_volume(luxgi_ddgi_volume* v) {
     void* ptrs[] = {v->irr[0], v->irr[1], v->dist[0], v->dist[1], v->dirs_trace, v->dirs_blend, v->rays, v->info,
                     v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
                     v->status, v->hit_t, v->hit_c, v->w2l, v->shade_chunks, v->shade_culled, v->shade_scratch,
-                    v->sdf_quad, v->mip_quad, v->mq, v->mq_count, v->cell_min};
+                    v->sdf_quad, v->mip_quad, v->mq, v->mq_count, v->cell_min, v->shade_bins, v->shade_key,
+                    v->shade_order};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -105,7 +106,7 @@ int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int c
     if (d.march_budget < 0 || mv >= 6) return 0;
     // queue entries hold 32-bit work indices and 16-bit step totals
     if (work >= (int64_t(1) << 32) || int64_t(cascades) * d.max_steps >= 65536) return 0;
-    return d.march_budget == 0 ? 0 : d.march_budget;   // default: one pass
+    return d.march_budget == 0 ? 8 : d.march_budget;   // default: 8 steps, then compacted passes
 }
 
 uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,
@@ -264,6 +265,10 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.qa_cap = v->mqa_cap;
     p.qb_cap = v->mqb_cap;
     p.vol = 0;
+    const bool sorted = v->shade_bins && d.shade_order >= 0 && d.march_variant < 6;
+    p.bin_count = sorted ? v->shade_bins : nullptr;
+    p.bin_key = sorted ? v->shade_key : nullptr;
+    p.shade_seq = sorted ? v->shade_order : nullptr;
     p.div_x = make_fastdiv(uint32_t(d.uniform.probe_counts[0]));
     p.div_xy = make_fastdiv(uint32_t(d.uniform.probe_counts[0]) * uint32_t(d.uniform.probe_counts[1]));
 }
@@ -336,6 +341,21 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
         v->mqa_cap = ca;
         v->mqb_cap = cb;
     }
+    if (!v->shade_bins && v->desc.shade_order >= 0 && v->desc.march_variant < 6 && work < (int64_t(1) << 32)) {
+        // shading-order buffers, made on the first trace that needs them
+        cudaError_t e = dmalloc(&v->shade_bins, sizeof(uint32_t) * 2 * kShadeBins);
+        if (e == cudaSuccess) e = dmalloc(&v->shade_key, sizeof(uint32_t) * size_t(work));
+        if (e == cudaSuccess) e = dmalloc(&v->shade_order, sizeof(uint32_t) * size_t(work));
+        if (e != cudaSuccess) {
+            void* ptrs[] = {v->shade_bins, v->shade_key, v->shade_order};
+            for (void* q : ptrs)
+                if (q) cudaFree(q);
+            v->shade_bins = nullptr;
+            v->shade_key = nullptr;
+            v->shade_order = nullptr;
+            return cuda_status(e);
+        }
+    }
     TraceParams p;
     volume_trace_params(v, rot, p);
     BlendParams b;
@@ -349,11 +369,16 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     int s = e == cudaSuccess ? volume_prepare(v, st) : cuda_status(e);
     if (s == LUXGI_OK) {
         mark(1);
-        s = cuda_status(launch_march(p, st));
+        cudaError_t em = p.bin_count ? cudaMemsetAsync(p.bin_count, 0, sizeof(uint32_t) * kShadeBins, st)
+                                     : cudaSuccess;
+        if (em == cudaSuccess) em = launch_march(p, st);
+        s = cuda_status(em);
     }
     if (s == LUXGI_OK) {
         mark(2);
-        s = cuda_status(launch_shade(p, st));
+        cudaError_t es = p.bin_count ? launch_shade_sort(p, st) : cudaSuccess;
+        if (es == cudaSuccess) es = launch_shade(p, st);
+        s = cuda_status(es);
         mark(3);
     }
     nvtxRangePop();
@@ -470,6 +495,7 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->march_variant < 0 || desc->march_variant > 9) return LUXGI_EINVAL;
     if (desc->ray_order != 0 && desc->ray_order != 1) return LUXGI_EINVAL;
     if (desc->march_budget < -1) return LUXGI_EINVAL;
+    if (desc->shade_order < -1 || desc->shade_order > 1) return LUXGI_EINVAL;
     if (desc->shade_variant != 0 && desc->shade_variant != 1 && desc->shade_variant != 2 &&
         desc->shade_variant != 4 && desc->shade_variant != 8)
         return LUXGI_EINVAL;

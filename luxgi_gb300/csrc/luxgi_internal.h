@@ -49,7 +49,17 @@ struct TraceParams {
     uint32_t qa_cap, qb_cap;
     int budget1, budget2;
     int vol;                 // this volume's index in a batched launch (queue entries)
+    // shading order by hit chunk (shade_order 1): the march counts its hits
+    // per bin and records each work item's bin; a scan and a scatter give
+    // `shade_seq`, the work items bin by bin, which the shade kernel walks.
+    uint32_t* bin_count;     // [2][kShadeBins]: per-bin counts, then the scatter cursors
+    uint32_t* bin_key;       // [work] bin of each work item
+    uint32_t* shade_seq;     // [work] work items sorted by bin
 };
+
+// Shading bins: the 40^3 surface-cache chunks of the hits, then one bin for
+// misses, rays inside geometry and padding.
+constexpr int kShadeBins = 40 * 40 * 40 + 1;
 
 constexpr int kProbeTile = 256;
 
@@ -148,6 +158,8 @@ cudaError_t launch_shade_batch(const TraceParams* vp, const int* starts, int n, 
                                int shade_variant, cudaStream_t st);
 cudaError_t launch_march(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
+// Scan of the shading bins and scatter of the work items into `shade_seq`.
+cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 size_t quad_bytes(int W, int H, int D, int format);
 size_t cell_min_bytes(int W, int H, int D);

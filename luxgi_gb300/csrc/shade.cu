@@ -86,9 +86,63 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
 
 template <int MODE, int UNROLL>
 __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= p.work) return;
+    shade_ray<MODE, UNROLL>(p, p.shade_seq ? int64_t(__ldg(p.shade_seq + i)) : i);
+}
+
+// ------------------------------------------------------ shading order
+// Exclusive scan of the bin counts into the scatter cursors: one block,
+// each thread a contiguous run of bins.
+constexpr int kScanThreads = 1024;
+
+__global__ void __launch_bounds__(kScanThreads) bin_scan_kernel(const uint32_t* __restrict__ count,
+                                                               uint32_t* __restrict__ cursor, int nb) {
+    __shared__ uint32_t part[kScanThreads];
+    const int per = (nb + kScanThreads - 1) / kScanThreads;
+    const int b0 = int(threadIdx.x) * per, b1 = min(b0 + per, nb);
+    uint32_t s = 0;
+    for (int b = b0; b < b1; ++b) s += count[b];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < kScanThreads; off <<= 1) {
+        const uint32_t v = int(threadIdx.x) >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+    for (int b = b0; b < b1; ++b) {
+        cursor[b] = run;
+        run += count[b];
+    }
+}
+
+// Work items into `order` bin by bin (order within a bin is arbitrary; each
+// item is shaded the same wherever it lands).
+__global__ void __launch_bounds__(256) bin_scatter_kernel(const uint32_t* __restrict__ key, uint32_t* __restrict__ cursor,
+                                                          uint32_t* __restrict__ order, int64_t work) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (idx >= p.work) return;
-    shade_ray<MODE, UNROLL>(p, idx);
+    if (idx >= work) return;
+    const uint32_t k = __ldg(key + idx);
+    const unsigned act = __activemask();
+    const unsigned same = __match_any_sync(act, k);
+    const int lane = int(threadIdx.x) & 31;
+    const int leader = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cursor + k, uint32_t(__popc(same)));
+    base = __shfl_sync(same, base, leader);
+    const uint32_t pos = base + uint32_t(__popc(same & ((1u << lane) - 1u)));
+    if (pos < work) order[pos] = uint32_t(idx);   // the counts cover every work item once
+}
+
+cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st) {
+    if (p.work <= 0) return cudaSuccess;
+    uint32_t* cursor = p.bin_count + kShadeBins;
+    bin_scan_kernel<<<1, kScanThreads, 0, st>>>(p.bin_count, cursor, kShadeBins);
+    bin_scatter_kernel<<<unsigned((p.work + 255) / 256), 256, 0, st>>>(p.bin_key, cursor, p.shade_seq, p.work);
+    note_launch(2);
+    return cudaGetLastError();
 }
 
 // Batched over many volumes (128 rays a block), parameters staged in

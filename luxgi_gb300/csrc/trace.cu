@@ -62,7 +62,29 @@ cudaError_t launch_raygen_batch(const TraceParams* vp, const int* starts, int n,
 // with the same ray index, so a warp marches 32 parallel rays from
 // neighbouring probes through nearby SDF texels.  The march is the whole
 // kernel (no shading code): small, low register count, high occupancy.
-__device__ __forceinline__ void write_march(const TraceParams& p, int probe, int ray, const MarchHit& hit) {
+// Counts work item idx into shading bin `key` (one atomic per group of
+// converged lanes with the same bin) and records its bin.
+__device__ __forceinline__ void record_bin(const TraceParams& p, int64_t idx, uint32_t key) {
+    const unsigned act = __activemask();
+    const unsigned same = __match_any_sync(act, key);
+    if ((int(threadIdx.x) & 31) == __ffs(same) - 1) atomicAdd(p.bin_count + key, uint32_t(__popc(same)));
+    p.bin_key[idx] = key;
+}
+
+// Shading bin of a march result: the surface-cache chunk of the hit point
+// (the chunk grid of sampleGlobalSurfaceAtlas), or the last bin.
+__device__ __forceinline__ uint32_t shade_bin(const TraceParams& p, int cls, f3 origin, f3 dir, float time) {
+    if (cls < 0) return kShadeBins - 1;
+    const f3 hp = add3(origin, mul3(dir, time));
+    const float cs = p.surf.data.chunk_size;
+    const int cx = imn(imx(int(floorf(hp.x / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const int cy = imn(imx(int(floorf(hp.y / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const int cz = imn(imx(int(floorf(hp.z / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    return uint32_t((cz * kChunksRes + cy) * kChunksRes + cx);
+}
+
+__device__ __forceinline__ void write_march(const TraceParams& p, int64_t idx, int probe, int ray, f3 origin, f3 dir,
+                                            const MarchHit& hit) {
     int cls = -1;                                          // miss
     if (hit.time >= 0.0f) {
         // GISDFRays.comp:93: a hit at the probe from inside a surface
@@ -72,6 +94,7 @@ __device__ __forceinline__ void write_march(const TraceParams& p, int probe, int
     p.hit_t[o] = make_float4(hit.time, hit.normal.x, hit.normal.y, hit.normal.z);
     p.hit_c[o] = cls;
     if (p.info) p.info[o] = make_int4(hit.steps, hit.time >= 0.0f ? hit.cascade : -1, hit.fine, 0);
+    if (p.bin_count) record_bin(p, idx, shade_bin(p, cls, origin, dir, hit.time));
 }
 
 // Suspended-march queue entry: (work item, volume, cascade | in-cascade << 7
@@ -128,6 +151,7 @@ __device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
     march_state_init(m);
     MarchHit hit;
     bool done = true;
+    if (!valid && p.bin_count) record_bin(p, idx, kShadeBins - 1);   // padding of the last probe tile
     if (valid) {
         const float4 d4 = __ldg(p.dirs + ray);
         const f3 dir{d4.x, d4.y, d4.z};
@@ -136,7 +160,7 @@ __device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
                                            p.budget1 > 0 ? p.budget1 : 0x7FFFFFFF, hit);
         if (p.budget1 > 0 && enqueue_march(p.qa, p.qcount, p.qa_cap, !done, idx, p.vol, m)) return;
         if (!done) march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m, 0x7FFFFFFF, hit);
-        write_march(p, probe, ray, hit);
+        write_march(p, idx, probe, ray, origin, dir, hit);
     }
 }
 
@@ -165,7 +189,7 @@ __device__ __forceinline__ void march_resume(const TraceParams& p0, const TraceP
                                                 FINAL ? 0x7FFFFFFF : p.budget2, hit);
         if (!FINAL && enqueue_march(p0.qb, p0.qcount + 1, p0.qb_cap, !done, idx, vol, m)) continue;
         if (!done) march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m, 0x7FFFFFFF, hit);
-        write_march(p, probe, ray, hit);
+        write_march(p, idx, probe, ray, origin, dir, hit);
     }
 }
 

@@ -57,6 +57,7 @@ class VolumeSpec:
     shade_variant: int = 0
     ray_order: int = 0
     march_budget: int = 0
+    shade_order: int = 0
 
     @property
     def probes(self) -> int:
@@ -97,6 +98,7 @@ class VolumeSpec:
         d.shade_variant = self.shade_variant
         d.ray_order = self.ray_order
         d.march_budget = self.march_budget
+        d.shade_order = self.shade_order
         return d
 
 

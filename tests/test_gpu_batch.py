@@ -179,6 +179,6 @@ def test_batch_launch_count(cuda, blend):
     batch.update(_rots(3, 2))
     torch.cuda.synchronize()
     per_frame = lib.luxgi_launch_count() - c0
-    # raygen, weights, march, shade + blend: 2 FP32 launches, or 2 per volume
-    # (the default march is one pass)
-    assert per_frame == 4 + (2 if blend == N.BLEND_FP32 else 2 * 3)
+    # raygen, weights, march (three passes: the default compacts after 8
+    # steps), shade + blend: 2 FP32 launches, or 2 per volume
+    assert per_frame == 6 + (2 if blend == N.BLEND_FP32 else 2 * 3)
