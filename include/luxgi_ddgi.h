@@ -203,14 +203,17 @@ typedef struct luxgi_ddgi_volume_desc {
                                       runs every ray for at most this many
                                       steps, queues the unfinished ones and
                                       resumes them with full warps (twice,
-                                      then to the end); 0 default (= 8); -1
-                                      one pass.  Per-ray variants 1-5.       */
-    int32_t shade_order;           /* tuning, results identical: 0 default
-                                      (= 1); 1 bin the hits by their surface-
-                                      cache chunk first (histogram, scan,
-                                      scatter) so a warp shades nearby hits;
-                                      -1 shade in march order.  Per-ray march
-                                      variants 1-5.                          */
+                                      then to the end); 0 default (8 when the
+                                      volume has >= 2^20 probe-rays, else one
+                                      pass); -1 one pass.  Per-ray variants
+                                      1-5.                                   */
+    int32_t shade_order;           /* tuning, results identical: 1 bin the
+                                      hits by their surface-cache chunk first
+                                      (histogram, scan, scatter) so a warp
+                                      shades nearby hits; -1 shade in march
+                                      order; 0 default (1 when the volume has
+                                      >= 2^20 probe-rays, else -1).  Per-ray
+                                      march variants 1-5.                    */
     int32_t reserved[3];
 } luxgi_ddgi_volume_desc;
 
@@ -310,7 +313,9 @@ typedef struct luxgi_ddgi_batch_tuning {
                                 tile (x 4 texels): 1, 2 or 4                 */
     int32_t use_graph;       /* 1 capture + replay a CUDA graph, 0 launch     */
     int32_t march_budget;    /* as luxgi_ddgi_volume_desc.march_budget        */
-    int32_t reserved[2];
+    int32_t shade_order;     /* 1 shade in bin order (bins shared by the
+                                batch's volumes), 0 or -1 march order        */
+    int32_t reserved[1];
     float frame_ms;          /* frame time measured by the autotuner, else 0  */
 } luxgi_ddgi_batch_tuning;
 

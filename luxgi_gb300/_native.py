@@ -94,8 +94,8 @@ class Rays(ctypes.Structure):
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("march_variant", c_int32), ("march_threads", c_int32), ("shade_variant", c_int32),
-                ("blend_probes", c_int32), ("use_graph", c_int32), ("march_budget", c_int32), ("reserved", c_int32 * 2),
-                ("frame_ms", c_float)]
+                ("blend_probes", c_int32), ("use_graph", c_int32), ("march_budget", c_int32), ("shade_order", c_int32),
+                ("reserved", c_int32 * 1), ("frame_ms", c_float)]
 
 
 class ServerDesc(ctypes.Structure):

@@ -46,7 +46,7 @@ bool tuning_valid(const luxgi_ddgi_batch_tuning& t) {
     return t.march_variant >= 1 && t.march_variant <= 5 && (t.march_threads == 128 || t.march_threads == 256) &&
            (t.shade_variant == 1 || t.shade_variant == 2 || t.shade_variant == 4 || t.shade_variant == 8) &&
            (t.blend_probes == 1 || t.blend_probes == 2 || t.blend_probes == 4) && (t.use_graph == 0 || t.use_graph == 1) &&
-           t.march_budget >= -1;
+           t.march_budget >= -1 && t.shade_order >= -1 && t.shade_order <= 1;
 }
 
 luxgi_ddgi_batch_tuning default_tuning() {
@@ -61,18 +61,32 @@ luxgi_ddgi_batch_tuning default_tuning() {
     return t;
 }
 
-size_t plan_queue_bytes(const Plan& P) {
+static size_t queue_bytes(const Plan& P) {
     return P.budget > 0 ? sizeof(int4) * 2 * (size_t(P.qa_cap) + P.qb_cap) + 16 : 0;
 }
 
-void plan_set_queues(Plan& P, void* dev) {
-    if (P.budget <= 0 || !dev) {
-        P.q = nullptr;
-        P.qcount = nullptr;
-        return;
+size_t plan_aux_bytes(const Plan& P) {
+    size_t b = queue_bytes(P);
+    if (P.sorted) b += sizeof(uint32_t) * (2 * size_t(kBatchShadeBins) + 2 * size_t(P.work)) + 16;
+    return b;
+}
+
+void plan_set_aux(Plan& P, void* dev) {
+    P.q = nullptr;
+    P.qcount = nullptr;
+    P.sbins = P.skeys = P.sseq = nullptr;
+    if (!dev) return;
+    uint8_t* base = static_cast<uint8_t*>(dev);
+    if (P.budget > 0) {
+        P.q = reinterpret_cast<int4*>(base);
+        P.qcount = reinterpret_cast<uint32_t*>(P.q + 2 * (size_t(P.qa_cap) + P.qb_cap));
+        base += queue_bytes(P);
     }
-    P.q = static_cast<int4*>(dev);
-    P.qcount = reinterpret_cast<uint32_t*>(P.q + 2 * (size_t(P.qa_cap) + P.qb_cap));
+    if (P.sorted) {
+        P.sbins = reinterpret_cast<uint32_t*>(base);
+        P.skeys = P.sbins + 2 * size_t(kBatchShadeBins);
+        P.sseq = P.skeys + size_t(P.work);
+    }
 }
 
 // Gives every volume the plan's march and shade variant (the packed SDF
@@ -114,7 +128,7 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         volume_blend_params(v, b);
         const int64_t PR = trace_work(v->P, v->R, (v->desc.ray_order == 1 && v->desc.march_variant < 6) ? 1 : 0);
         luxgi_ddgi_volume_desc vd = v->desc;
-        vd.march_budget = t.march_budget;
+        vd.march_budget = t.march_budget == 0 ? 8 : t.march_budget;
         P.budget = std::min(P.budget, march_budget_for(vd, PR, int(v->sdf.data.cascades_count)));
         P.work += PR;
         int64_t cnt[kNumStages];
@@ -124,6 +138,7 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         cnt[kShade] = (PR + 127) / 128;
         cnt[kBlendI] = P.tc ? 0 : blend_blocks(b, false, t.blend_probes);
         cnt[kBlendD] = P.tc ? 0 : blend_blocks(b, true, t.blend_probes);
+        cnt[kWork] = PR;
         for (int s = 0; s < kNumStages; ++s) {
             P.starts[size_t(s) * (n + 1) + i] = int(acc[s]);
             acc[s] += cnt[s];
@@ -145,10 +160,13 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
     // the batch's queue entries hold 32-bit work indices per volume; the
     // counters hold the whole batch's
     if (P.work >= (int64_t(1) << 32)) P.budget = 0;
+    if (t.march_budget == 0 && P.work < kLargeWork) P.budget = 0;   // default: large batches only
     if (P.budget > 0) {
         P.qa_cap = march_qa_cap(P.work);
         P.qb_cap = march_qb_cap(P.work);
     }
+    // batch-wide work indices are ints in the work-offset table (INT_MAX checked above)
+    P.sorted = t.shade_order == 1 && t.march_variant < 6;
     return LUXGI_OK;
 }
 
@@ -167,9 +185,11 @@ void plan_fill(const Plan& P, const float* rots, uint8_t* host) {
         tp[i].qa_cap = P.qa_cap;
         tp[i].qb_cap = P.qb_cap;
         tp[i].vol = i;
-        tp[i].bin_count = nullptr;      // batched launches shade in march order
-        tp[i].bin_key = nullptr;
+        // shading bins shared by the batch; keys at the volume's batch-wide offset
+        tp[i].bin_count = P.sbins;
+        tp[i].bin_key = P.sbins ? P.skeys + P.starts[size_t(kWork) * (P.n + 1) + i] : nullptr;
         tp[i].shade_seq = nullptr;
+        tp[i].bin_mask = P.sbins ? uint32_t(kBatchShadeBins - 1) : 0u;
         volume_blend_params(v, bp[i]);
         if (P.tc) {
             TcBlendParams t;
@@ -213,11 +233,19 @@ cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cud
     const int n = P.n, n1 = P.n + 1;
     cudaError_t e = launch_raygen_batch(tp, d_starts + kRaygen * n1, n, P.blocks[kRaygen], st);
     if (e == cudaSuccess) e = launch_weights_batch(bp, d_starts + kWeights * n1, n, P.blocks[kWeights], st);
+    if (e == cudaSuccess && P.sbins)
+        e = cudaMemsetAsync(P.sbins, 0, sizeof(uint32_t) * kBatchShadeBins, st);
     if (e == cudaSuccess)
         e = launch_march_batch(tp, d_starts + kMarch * n1, n, P.blocks[kMarch], P.t.march_variant,
                                P.t.march_threads, P.sdf_format, P.q ? 1 : 0, P.qcount, st);
-    if (e == cudaSuccess)
+    if (P.sbins) {
+        if (e == cudaSuccess) e = launch_bin_sort(P.sbins, kBatchShadeBins, P.skeys, P.sseq, P.work, st);
+        if (e == cudaSuccess)
+            e = launch_shade_batch_sorted(tp, d_starts + kWork * n1, n, P.sseq, P.work, P.light_mode,
+                                          P.t.shade_variant, st);
+    } else if (e == cudaSuccess) {
         e = launch_shade_batch(tp, d_starts + kShade * n1, n, P.blocks[kShade], P.light_mode, P.t.shade_variant, st);
+    }
     if (e != cudaSuccess) return e;
     if (!P.tc)
         return launch_blend_batch(bp, d_starts + kBlendI * n1, P.blocks[kBlendI], P.smem_i, d_starts + kBlendD * n1,
@@ -268,6 +296,7 @@ int run_group(luxgi_ddgi_volume* const* vols, int n, const float* rots, cudaStre
     t.march_variant = vols[0]->desc.march_variant;
     t.shade_variant = vols[0]->desc.shade_variant;
     t.march_budget = vols[0]->desc.march_budget;
+    t.shade_order = vols[0]->desc.shade_order;
     t.use_graph = 0;
     Plan P;
     int s = plan_build(P, vols, n, t);
@@ -277,9 +306,9 @@ int run_group(luxgi_ddgi_volume* const* vols, int n, const float* rots, cudaStre
     std::vector<uint8_t> host(P.arg_bytes + P.starts.size() * sizeof(int));
     const size_t qoff = align16(host.size());
     uint8_t* dev = nullptr;
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&dev), qoff + plan_queue_bytes(P), st);
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&dev), qoff + plan_aux_bytes(P), st);
     if (e != cudaSuccess) return cuda_status(e);
-    plan_set_queues(P, dev + qoff);
+    plan_set_aux(P, dev + qoff);
     plan_fill(P, rots, host.data());
     std::memcpy(host.data() + P.arg_bytes, P.starts.data(), P.starts.size() * sizeof(int));
     // pageable source: the copy has taken the bytes when the call returns
@@ -358,7 +387,7 @@ int replan(luxgi_ddgi_batch* b, const luxgi_ddgi_batch_tuning& t) {
     if (s != LUXGI_OK) return s;
     s = plan_build(b->plan, vols.data(), int(vols.size()), t);
     if (s != LUXGI_OK) return s;
-    const size_t qb = plan_queue_bytes(b->plan);
+    const size_t qb = plan_aux_bytes(b->plan);
     if (qb > b->dev_q_cap) {
         if (b->dev_q) cudaFree(b->dev_q);
         b->dev_q = nullptr;
@@ -367,7 +396,7 @@ int replan(luxgi_ddgi_batch* b, const luxgi_ddgi_batch_tuning& t) {
         if (e != cudaSuccess) return cuda_status(e);
         b->dev_q_cap = qb;
     }
-    plan_set_queues(b->plan, b->dev_q);
+    plan_set_aux(b->plan, b->dev_q);
     const Plan& P = b->plan;
     if (P.arg_bytes > b->host_cap) {
         for (int k = 0; k < 2; ++k) {
@@ -564,6 +593,7 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* 
                 const luxgi_ddgi_volume* c = vols[j];
                 if (done[j] || !c->bound || c->desc.march_variant != mv ||
                     c->desc.shade_variant != a->desc.shade_variant || c->desc.march_budget != a->desc.march_budget ||
+                    c->desc.shade_order != a->desc.shade_order ||
                     c->desc.storage != a->desc.storage ||
                     c->desc.light_mode != a->desc.light_mode || c->tc != a->tc || c->sdf.format != a->sdf.format ||
                     c->device != a->device)
@@ -652,6 +682,11 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
         c.march_budget = mb;
         const int cur = best.march_budget == 0 ? 8 : best.march_budget;
         if (mb != cur) consider(c);
+    }
+    {
+        luxgi_ddgi_batch_tuning c = best;
+        c.shade_order = best.shade_order == 1 ? -1 : 1;
+        consider(c);
     }
     for (int sv : {1, 2, 4}) {
         luxgi_ddgi_batch_tuning c = best;

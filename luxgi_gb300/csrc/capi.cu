@@ -101,12 +101,20 @@ size_t atlas_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 2 
 
 }  // namespace
 
+bool luxgi::shade_binned(const luxgi_ddgi_volume_desc& d, int64_t work) {
+    if (d.march_variant >= 6 || work >= (int64_t(1) << 32) || d.shade_order < 0) return false;
+    return d.shade_order == 1 || work >= kLargeWork;     // default: large launches
+}
+
 int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int cascades) {
     const int mv = d.march_variant == 0 ? 4 : d.march_variant;
     if (d.march_budget < 0 || mv >= 6) return 0;
     // queue entries hold 32-bit work indices and 16-bit step totals
     if (work >= (int64_t(1) << 32) || int64_t(cascades) * d.max_steps >= 65536) return 0;
-    return d.march_budget == 0 ? 8 : d.march_budget;   // default: 8 steps, then compacted passes
+    // default: compacted passes after 8 steps for large launches; small ones
+    // cannot amortise the two extra passes
+    if (d.march_budget == 0) return work >= kLargeWork ? 8 : 0;
+    return d.march_budget;
 }
 
 uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,
@@ -265,7 +273,7 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.qa_cap = v->mqa_cap;
     p.qb_cap = v->mqb_cap;
     p.vol = 0;
-    const bool sorted = v->shade_bins && d.shade_order >= 0 && d.march_variant < 6;
+    const bool sorted = v->shade_bins && shade_binned(d, p.work);
     p.bin_count = sorted ? v->shade_bins : nullptr;
     p.bin_key = sorted ? v->shade_key : nullptr;
     p.shade_seq = sorted ? v->shade_order : nullptr;
@@ -341,7 +349,7 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
         v->mqa_cap = ca;
         v->mqb_cap = cb;
     }
-    if (!v->shade_bins && v->desc.shade_order >= 0 && v->desc.march_variant < 6 && work < (int64_t(1) << 32)) {
+    if (!v->shade_bins && shade_binned(v->desc, work)) {
         // shading-order buffers, made on the first trace that needs them
         cudaError_t e = dmalloc(&v->shade_bins, sizeof(uint32_t) * 2 * kShadeBins);
         if (e == cudaSuccess) e = dmalloc(&v->shade_key, sizeof(uint32_t) * size_t(work));

@@ -8,7 +8,9 @@
 
 namespace luxgi {
 
-enum Stage { kRaygen, kWeights, kMarch, kShade, kBlendI, kBlendD, kNumStages };
+// block-offset tables of the batched launches; kWork holds each volume's
+// first batch-wide march work index instead
+enum Stage { kRaygen, kWeights, kMarch, kShade, kBlendI, kBlendD, kWork, kNumStages };
 
 // What a set of volumes needs to run one frame as batched launches.
 struct Plan {
@@ -27,14 +29,19 @@ struct Plan {
     int budget = 0;
     int64_t work = 0;                   // march work items of all volumes
     uint32_t qa_cap = 0, qb_cap = 0;
-    int4* q = nullptr;                  // device queues + counters (plan_set_queues)
+    int4* q = nullptr;                  // device queues + counters (plan_set_aux)
     uint32_t* qcount = nullptr;
+    // shading in bin order over the whole batch (sorted false: march order)
+    bool sorted = false;
+    uint32_t* sbins = nullptr;          // [2][kBatchShadeBins]
+    uint32_t* skeys = nullptr;          // [work] bin of each batch-wide work item
+    uint32_t* sseq = nullptr;           // [work] batch-wide work items by bin
 };
 
-// Device bytes of the plan's march queues and counters (0 without compaction),
-// and binding them to a device region of that size (16-byte aligned).
-size_t plan_queue_bytes(const Plan& P);
-void plan_set_queues(Plan& P, void* dev);
+// Device bytes of the plan's march queues and shading-order arrays, and
+// binding them to a device region of that size (16-byte aligned).
+size_t plan_aux_bytes(const Plan& P);
+void plan_set_aux(Plan& P, void* dev);
 
 int compat_check(luxgi_ddgi_volume* const* vols, int n);
 bool tuning_valid(const luxgi_ddgi_batch_tuning& t);

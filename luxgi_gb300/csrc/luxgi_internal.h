@@ -55,11 +55,14 @@ struct TraceParams {
     uint32_t* bin_count;     // [2][kShadeBins]: per-bin counts, then the scatter cursors
     uint32_t* bin_key;       // [work] bin of each work item
     uint32_t* shade_seq;     // [work] work items sorted by bin
+    uint32_t bin_mask;       // batched launches: bins shared by the volumes, key
+                             // (vol * kShadeBins + chunk) & bin_mask; 0 alone
 };
 
 // Shading bins: the 40^3 surface-cache chunks of the hits, then one bin for
 // misses, rays inside geometry and padding.
 constexpr int kShadeBins = 40 * 40 * 40 + 1;
+constexpr int kBatchShadeBins = 1 << 17;
 
 constexpr int kProbeTile = 256;
 
@@ -160,6 +163,13 @@ cudaError_t launch_march(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
 // Scan of the shading bins and scatter of the work items into `shade_seq`.
 cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st);
+// The same over raw arrays: bins [2][nb] (counts, cursors), keys and seq [work].
+cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint32_t* keys, uint32_t* seq, int64_t work,
+                            cudaStream_t st);
+// Batched shading in bin order: seq holds batch-wide work indices; work_off
+// [n + 1] the first batch-wide index of each volume.
+cudaError_t launch_shade_batch_sorted(const TraceParams* vp, const int* work_off, int n, const uint32_t* seq,
+                                      int64_t work, int light_mode, int shade_variant, cudaStream_t st);
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 size_t quad_bytes(int W, int H, int D, int format);
 size_t cell_min_bytes(int W, int H, int D);

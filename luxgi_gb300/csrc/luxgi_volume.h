@@ -80,6 +80,11 @@ int volume_alloc_packs(luxgi_ddgi_volume* v);
 // `work` items and whose march variant / budget / step cap are those of d;
 // 0 when the march runs in one pass.
 int march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int cascades);
+// Launches of at least this many march work items take the compacted march
+// and the binned shading by default.
+constexpr int64_t kLargeWork = int64_t(1) << 20;
+// Whether a volume's hits are shaded in bin order (shade_order and size).
+bool shade_binned(const luxgi_ddgi_volume_desc& d, int64_t work);
 // Device bytes a volume of description d allocates once bound to the scene
 // (luxgi_ddgi_create + luxgi_ddgi_bind_scene; debug ray records excluded).
 uint64_t volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,

@@ -122,6 +122,7 @@ luxgi_ddgi_batch_tuning server_tuning(const luxgi_server_desc& d) {
     if (d.tuning.shade_variant) t.shade_variant = d.tuning.shade_variant;
     if (d.tuning.blend_probes) t.blend_probes = d.tuning.blend_probes;
     t.march_budget = d.tuning.march_budget;
+    t.shade_order = d.tuning.shade_order;
     t.use_graph = 0;
     return t;
 }
@@ -280,7 +281,7 @@ int cuda_launch(luxgi_server* S, Slot& sl, const std::vector<Session*>& members)
     if (s != LUXGI_OK) return s;
     const size_t sb = P.starts.size() * sizeof(int);
     const size_t qoff = (P.arg_bytes + sb + 15) & ~size_t(15);
-    const size_t need = qoff + plan_queue_bytes(P);
+    const size_t need = qoff + plan_aux_bytes(P);
     if (need > sl.cap) {
         if (sl.host) cudaFreeHost(sl.host);
         if (sl.dev) cudaFree(sl.dev);
@@ -295,7 +296,7 @@ int cuda_launch(luxgi_server* S, Slot& sl, const std::vector<Session*>& members)
     }
     s = prepare_all(P, sl.st);
     if (s != LUXGI_OK) return s;
-    plan_set_queues(P, sl.dev + qoff);
+    plan_set_aux(P, sl.dev + qoff);
     plan_fill(P, rots.data(), sl.host);
     std::memcpy(sl.host + P.arg_bytes, P.starts.data(), sb);
     cudaError_t e = cudaMemcpyAsync(sl.dev, sl.host, P.arg_bytes + sb, cudaMemcpyHostToDevice, sl.st);

@@ -136,12 +136,49 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(const uint32_t* __rest
     if (pos < work) order[pos] = uint32_t(idx);   // the counts cover every work item once
 }
 
-cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st) {
-    if (p.work <= 0) return cudaSuccess;
-    uint32_t* cursor = p.bin_count + kShadeBins;
-    bin_scan_kernel<<<1, kScanThreads, 0, st>>>(p.bin_count, cursor, kShadeBins);
-    bin_scatter_kernel<<<unsigned((p.work + 255) / 256), 256, 0, st>>>(p.bin_key, cursor, p.shade_seq, p.work);
+cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint32_t* keys, uint32_t* seq, int64_t work,
+                            cudaStream_t st) {
+    if (work <= 0) return cudaSuccess;
+    uint32_t* cursor = bins + nb;
+    bin_scan_kernel<<<1, kScanThreads, 0, st>>>(bins, cursor, nb);
+    bin_scatter_kernel<<<unsigned((work + 255) / 256), 256, 0, st>>>(keys, cursor, seq, work);
     note_launch(2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st) {
+    return launch_bin_sort(p.bin_count, kShadeBins, p.bin_key, p.shade_seq, p.work, st);
+}
+
+// Batched shading in bin order: neighbouring threads may belong to
+// different volumes, so each reads its volume's parameter block from
+// device memory (cached) instead of a per-block shared copy.
+template <int MODE, int UNROLL>
+__global__ void __launch_bounds__(128)
+    shade_batch_sorted_kernel(const TraceParams* __restrict__ vp, const int* __restrict__ work_off, int n,
+                              const uint32_t* __restrict__ seq, int64_t work) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= work) return;
+    const int g = int(__ldg(seq + i));
+    const int v = batch_volume(work_off, n, g);
+    shade_ray<MODE, UNROLL>(vp[v], int64_t(g - __ldg(work_off + v)));
+}
+
+cudaError_t launch_shade_batch_sorted(const TraceParams* vp, const int* work_off, int n, const uint32_t* seq,
+                                      int64_t work, int light_mode, int shade_variant, cudaStream_t st) {
+    if (work <= 0) return cudaSuccess;
+    const unsigned b = unsigned((work + 127) / 128);
+    if (light_mode == LUXGI_LIGHT_PER_HIT) {
+        switch (shade_variant) {
+            case 2: shade_batch_sorted_kernel<LUXGI_LIGHT_PER_HIT, 2><<<b, 128, 0, st>>>(vp, work_off, n, seq, work); break;
+            case 4: shade_batch_sorted_kernel<LUXGI_LIGHT_PER_HIT, 4><<<b, 128, 0, st>>>(vp, work_off, n, seq, work); break;
+            case 8: shade_batch_sorted_kernel<LUXGI_LIGHT_PER_HIT, 8><<<b, 128, 0, st>>>(vp, work_off, n, seq, work); break;
+            default: shade_batch_sorted_kernel<LUXGI_LIGHT_PER_HIT, 1><<<b, 128, 0, st>>>(vp, work_off, n, seq, work); break;
+        }
+    } else {
+        shade_batch_sorted_kernel<LUXGI_LIGHT_CACHE, 1><<<b, 128, 0, st>>>(vp, work_off, n, seq, work);
+    }
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -201,7 +201,7 @@ class DDGIBatch:
     @staticmethod
     def default_tuning() -> dict:
         return {"march_variant": 4, "march_threads": 256, "shade_variant": 1, "blend_probes": 2, "use_graph": 1,
-                "march_budget": 0}
+                "march_budget": 0, "shade_order": 0}
 
     def update(self, rots, stream=None) -> None:
         r = np.ascontiguousarray(np.asarray(rots, dtype=np.float32).reshape(len(self.volumes), 9))
@@ -231,7 +231,7 @@ class DDGIBatch:
     def _as_dict(t) -> dict:
         return {"march_variant": t.march_variant, "march_threads": t.march_threads, "shade_variant": t.shade_variant,
                 "blend_probes": t.blend_probes, "use_graph": t.use_graph, "march_budget": t.march_budget,
-                "frame_ms": t.frame_ms}
+                "shade_order": t.shade_order, "frame_ms": t.frame_ms}
 
     def close(self) -> None:
         h = getattr(self, "_h", None)

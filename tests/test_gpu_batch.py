@@ -72,10 +72,10 @@ def _assert_same(alone, batched, exact=True):
 
 
 @pytest.mark.parametrize("blend", [N.BLEND_FP32, N.BLEND_TENSOR])
-@pytest.mark.parametrize("use_graph", [1, 0])
-def test_batch_equals_single(cuda, blend, use_graph):
+@pytest.mark.parametrize("use_graph,shade_order,march_budget", [(1, 0, 0), (0, 0, 0), (1, -1, -1), (0, 1, 3)])
+def test_batch_equals_single(cuda, blend, use_graph, shade_order, march_budget):
     _, alone, batched = _pairs(blend)
-    batch = DDGIBatch(batched, {"use_graph": use_graph})
+    batch = DDGIBatch(batched, {"use_graph": use_graph, "shade_order": shade_order, "march_budget": march_budget})
     n = len(alone)
     for f in range(3):
         rots = _rots(n, f)
@@ -179,6 +179,6 @@ def test_batch_launch_count(cuda, blend):
     batch.update(_rots(3, 2))
     torch.cuda.synchronize()
     per_frame = lib.luxgi_launch_count() - c0
-    # raygen, weights, march (three passes: the default compacts after 8
-    # steps), shade + blend: 2 FP32 launches, or 2 per volume
-    assert per_frame == 6 + (2 if blend == N.BLEND_FP32 else 2 * 3)
+    # raygen, weights, march (one pass: small batches do not compact by
+    # default), shade (march order) + blend: 2 FP32 launches, or 2 per volume
+    assert per_frame == 4 + (2 if blend == N.BLEND_FP32 else 2 * 3)
