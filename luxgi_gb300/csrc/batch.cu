@@ -166,7 +166,7 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         P.qb_cap = march_qb_cap(P.work);
     }
     // batch-wide work indices are ints in the work-offset table (INT_MAX checked above)
-    P.sorted = t.shade_order == 1 && t.march_variant < 6;
+    P.sorted = t.shade_order == 1 && t.march_variant < 6 && n <= kBatchShadeBins / 2;
     return LUXGI_OK;
 }
 
@@ -189,7 +189,10 @@ void plan_fill(const Plan& P, const float* rots, uint8_t* host) {
         tp[i].bin_count = P.sbins;
         tp[i].bin_key = P.sbins ? P.skeys + P.starts[size_t(kWork) * (P.n + 1) + i] : nullptr;
         tp[i].shade_seq = nullptr;
-        tp[i].bin_mask = P.sbins ? uint32_t(kBatchShadeBins - 1) : 0u;
+        // each volume its own run of bins, so the shading order groups volumes
+        const uint32_t span = uint32_t(std::max(2, kBatchShadeBins / P.n));
+        tp[i].bin_base = P.sbins ? uint32_t(i) * span : 0u;
+        tp[i].bin_span = span;
         volume_blend_params(v, bp[i]);
         if (P.tc) {
             TcBlendParams t;
@@ -239,7 +242,8 @@ cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cud
         e = launch_march_batch(tp, d_starts + kMarch * n1, n, P.blocks[kMarch], P.t.march_variant,
                                P.t.march_threads, P.sdf_format, P.q ? 1 : 0, P.qcount, st);
     if (P.sbins) {
-        if (e == cudaSuccess) e = launch_bin_sort(P.sbins, kBatchShadeBins, P.skeys, P.sseq, P.work, st);
+        const int nb = std::max(2, kBatchShadeBins / n) * n;
+        if (e == cudaSuccess) e = launch_bin_sort(P.sbins, nb, P.skeys, P.sseq, P.work, st);
         if (e == cudaSuccess)
             e = launch_shade_batch_sorted(tp, d_starts + kWork * n1, n, P.sseq, P.work, P.light_mode,
                                           P.t.shade_variant, st);

@@ -277,6 +277,8 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.bin_count = sorted ? v->shade_bins : nullptr;
     p.bin_key = sorted ? v->shade_key : nullptr;
     p.shade_seq = sorted ? v->shade_order : nullptr;
+    p.bin_base = 0;
+    p.bin_span = kShadeBins;
     p.div_x = make_fastdiv(uint32_t(d.uniform.probe_counts[0]));
     p.div_xy = make_fastdiv(uint32_t(d.uniform.probe_counts[0]) * uint32_t(d.uniform.probe_counts[1]));
 }

@@ -55,8 +55,8 @@ struct TraceParams {
     uint32_t* bin_count;     // [2][kShadeBins]: per-bin counts, then the scatter cursors
     uint32_t* bin_key;       // [work] bin of each work item
     uint32_t* shade_seq;     // [work] work items sorted by bin
-    uint32_t bin_mask;       // batched launches: bins shared by the volumes, key
-                             // (vol * kShadeBins + chunk) & bin_mask; 0 alone
+    uint32_t bin_base;       // this volume's bins: bin_base + (chunk mod bin_span),
+    uint32_t bin_span;       // the last one for misses (alone: 0, kShadeBins)
 };
 
 // Shading bins: the 40^3 surface-cache chunks of the hits, then one bin for

@@ -150,18 +150,41 @@ cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st) {
     return launch_bin_sort(p.bin_count, kShadeBins, p.bin_key, p.shade_seq, p.work, st);
 }
 
-// Batched shading in bin order: neighbouring threads may belong to
-// different volumes, so each reads its volume's parameter block from
-// device memory (cached) instead of a per-block shared copy.
+// Batched shading in bin order.  Every volume owns a contiguous run of
+// bins, so the order groups the volumes and a block's 128 work items come
+// from the volumes between those of its first and last item: up to
+// kStagedVolumes of them are staged in shared memory, more are read from
+// device memory.
+constexpr int kStagedVolumes = 4;
+
 template <int MODE, int UNROLL>
 __global__ void __launch_bounds__(128)
     shade_batch_sorted_kernel(const TraceParams* __restrict__ vp, const int* __restrict__ work_off, int n,
                               const uint32_t* __restrict__ seq, int64_t work) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    constexpr int kWords = int(sizeof(TraceParams) / 4);
+    __shared__ __align__(16) uint32_t sp[kStagedVolumes][kWords];
+    __shared__ int vrange[2];
+    const int64_t i0 = int64_t(blockIdx.x) * blockDim.x;
+    if (threadIdx.x == 0) {
+        const int64_t last = min(i0 + int64_t(blockDim.x) - 1, work - 1);
+        vrange[0] = batch_volume(work_off, n, int(__ldg(seq + i0)));
+        vrange[1] = batch_volume(work_off, n, int(__ldg(seq + last)));
+    }
+    __syncthreads();
+    const int vlo = vrange[0], vhi = vrange[1];
+    const bool staged = vhi - vlo < kStagedVolumes;
+    if (staged) {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(vp + vlo);
+        for (int k = threadIdx.x; k < (vhi - vlo + 1) * kWords; k += blockDim.x) sp[k / kWords][k % kWords] = __ldg(src + k);
+    }
+    __syncthreads();
+    const int64_t i = i0 + threadIdx.x;
     if (i >= work) return;
     const int g = int(__ldg(seq + i));
     const int v = batch_volume(work_off, n, g);
-    shade_ray<MODE, UNROLL>(vp[v], int64_t(g - __ldg(work_off + v)));
+    const int64_t idx = int64_t(g - __ldg(work_off + v));
+    if (staged) shade_ray<MODE, UNROLL>(*reinterpret_cast<const TraceParams*>(sp[v - vlo]), idx);
+    else shade_ray<MODE, UNROLL>(vp[v], idx);
 }
 
 cudaError_t launch_shade_batch_sorted(const TraceParams* vp, const int* work_off, int n, const uint32_t* seq,

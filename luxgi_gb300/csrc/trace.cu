@@ -74,14 +74,14 @@ __device__ __forceinline__ void record_bin(const TraceParams& p, int64_t idx, ui
 // Shading bin of a march result: the surface-cache chunk of the hit point
 // (the chunk grid of sampleGlobalSurfaceAtlas), or the last bin.
 __device__ __forceinline__ uint32_t shade_bin(const TraceParams& p, int cls, f3 origin, f3 dir, float time) {
-    if (cls < 0) return p.bin_mask ? p.bin_mask : kShadeBins - 1;
+    if (cls < 0) return p.bin_base + p.bin_span - 1;
     const f3 hp = add3(origin, mul3(dir, time));
     const float cs = p.surf.data.chunk_size;
     const int cx = imn(imx(int(floorf(hp.x / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
     const int cy = imn(imx(int(floorf(hp.y / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
     const int cz = imn(imx(int(floorf(hp.z / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
     const uint32_t key = uint32_t((cz * kChunksRes + cy) * kChunksRes + cx);
-    return p.bin_mask ? (uint32_t(p.vol) * kShadeBins + key) & p.bin_mask : key;
+    return p.bin_base + (p.bin_span == uint32_t(kShadeBins) ? key : key % p.bin_span);
 }
 
 __device__ __forceinline__ void write_march(const TraceParams& p, int64_t idx, int probe, int ray, f3 origin, f3 dir,
@@ -152,7 +152,7 @@ __device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
     march_state_init(m);
     MarchHit hit;
     bool done = true;
-    if (!valid && p.bin_count) record_bin(p, idx, p.bin_mask ? p.bin_mask : kShadeBins - 1);   // tile padding
+    if (!valid && p.bin_count) record_bin(p, idx, p.bin_base + p.bin_span - 1);   // tile padding
     if (valid) {
         const float4 d4 = __ldg(p.dirs + ray);
         const f3 dir{d4.x, d4.y, d4.z};
