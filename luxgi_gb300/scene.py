@@ -171,6 +171,10 @@ def scaled(w: Workload, probe_counts=None, rays=None, sdf_resolution=None, atlas
 # the case ncu captures are taken on (a few hundred MB on the device).
 PRODUCTION_PROFILE = scaled(PRODUCTION, probe_counts=(16, 8, 16), name="production_16x8x16_r256_sdf256")
 WORKLOADS[PRODUCTION_PROFILE.name] = PRODUCTION_PROFILE
+# The precision scene at 32x16x32 probes: the case tensor-core blend
+# captures are taken on.
+PRECISION_PROFILE = scaled(PRECISION, probe_counts=(32, 16, 32), name="precision_32x16x32_r256_sdf256h")
+WORKLOADS[PRECISION_PROFILE.name] = PRECISION_PROFILE
 
 
 # Batching form: many volumes of uneven size, each with its own scene.  Grid
