@@ -12,7 +12,8 @@
 // D accumulates in TMEM (FP32).  One CTA per SM, persistent over M tiles:
 //   warp 0      TMA producer (cp.async.bulk.tensor, 128B swizzle, 16 KB stages)
 //   warp 1      TMEM allocator + single-thread tcgen05.mma issuer
-//   warps 2..5  epilogue: tcgen05.ld, normalise, gamma, hysteresis, store
+//   warps 2..9  epilogue: tcgen05.ld, normalise, gamma, hysteresis, store
+//               (two warps per TMEM lane quadrant, each half the columns)
 //               with the border mirrors
 // The accumulator is double buffered in TMEM so the epilogue of one tile
 // overlaps the MMAs of the next.  Every mbarrier wait is bounded by a clock
@@ -33,7 +34,8 @@ namespace {
 constexpr int kStages = 5;
 constexpr int kKBlock = 64;                 // halves per 128-byte swizzle row
 constexpr int kStageBytes = 128 * 128;      // 128 rows x 128 bytes
-constexpr int kThreads = 192;
+constexpr int kThreads = 320;
+constexpr int kEpilogueThreads = kThreads - 64;
 constexpr long long kWaitCycles = 4000000000LL;   // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -203,8 +205,8 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         mbar_init(bfull, 1);
         mbar_init(&tfull[0], 1);
         mbar_init(&tfull[1], 1);
-        mbar_init(&tempty[0], 128);
-        mbar_init(&tempty[1], 128);
+        mbar_init(&tempty[0], kEpilogueThreads);
+        mbar_init(&tempty[1], kEpilogueThreads);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -287,6 +289,11 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         // ------------------------------------------------ epilogue
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
         const int row = q * 32 + lane;          // accumulator row = (probe, channel)
+        const int half = (warp - 2) >> 2;       // which half of the columns / texels
+        const int chunks = g.N / 16;
+        const int c_begin = half ? (chunks + 1) / 2 * 16 : 0;
+        const int c_end = half ? g.N : (chunks + 1) / 2 * 16;
+        const int t_begin = half ? g.T / 2 : 0, t_end = half ? g.T : g.T / 2;
         const luxgi_ddgi_uniform& u = g.u;
         const int XY = u.probe_counts[0] * u.probe_counts[1];
         const int n = g.side;
@@ -305,7 +312,7 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
             const int c = row % g.rows_per_probe;
             const bool live = p < g.P && (DIST || c < 3);
             const int cx = p % XY, cy = p / XY;
-            for (int c0 = 0; c0 < g.N; c0 += 16) {
+            for (int c0 = c_begin; c0 < c_end; c0 += 16) {
                 float v[16];
                 tmem_ld16(tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * g.N + c0), v);
                 if (!live) continue;
@@ -315,7 +322,7 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                     if (t >= g.T) break;
                     const int tx = t % n, ty = t / n;
                     float x = v[j] * __ldg(g.norm + t);
-                    if (!DIST) x = powf(x, ig);
+                    if (!DIST) x = __powf(x, ig);   // within the tensor path's 2e-3
                     const size_t ti = (size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2)) * g.nc + c;
                     if (!g.first) x = x * (1.0f - h) + ld_atlas<AT>(g.prev, ti) * h;
                     store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, tx, ty, c, x);
@@ -323,7 +330,8 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
             }
             if (!DIST && p < g.P && c == 3) {
                 // alpha = 1 (ProbeUpdate.glsl:279) for every texel of the cell
-                for (int t = 0; t < g.T; ++t) store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, t % n, t / n, 3, 1.0f);
+                for (int t = t_begin; t < t_end; ++t)
+                    store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, t % n, t / n, 3, 1.0f);
             }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);

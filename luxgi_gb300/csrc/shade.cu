@@ -92,29 +92,44 @@ __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
 }
 
 // ------------------------------------------------------ shading order
-// Exclusive scan of the bin counts into the scatter cursors: one block,
-// each thread a contiguous run of bins.
+// Exclusive scan of the bin counts into the scatter cursors: one block
+// walks the bins in tiles of kScanThreads (coalesced loads), each tile
+// scanned with warp shuffles and carried into the next.
 constexpr int kScanThreads = 1024;
 
 __global__ void __launch_bounds__(kScanThreads) bin_scan_kernel(const uint32_t* __restrict__ count,
                                                                uint32_t* __restrict__ cursor, int nb) {
-    __shared__ uint32_t part[kScanThreads];
-    const int per = (nb + kScanThreads - 1) / kScanThreads;
-    const int b0 = int(threadIdx.x) * per, b1 = min(b0 + per, nb);
-    uint32_t s = 0;
-    for (int b = b0; b < b1; ++b) s += count[b];
-    part[threadIdx.x] = s;
+    __shared__ uint32_t warp_sum[kScanThreads / 32];
+    __shared__ uint32_t carry;
+    const int lane = int(threadIdx.x) & 31, warp = int(threadIdx.x) >> 5;
+    if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (int off = 1; off < kScanThreads; off <<= 1) {
-        const uint32_t v = int(threadIdx.x) >= off ? part[threadIdx.x - off] : 0u;
+    for (int base = 0; base < nb; base += kScanThreads) {
+        const int b = base + int(threadIdx.x);
+        const uint32_t v = b < nb ? __ldg(count + b) : 0u;
+        uint32_t x = v;                                   // inclusive scan within the warp
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) warp_sum[warp] = x;
         __syncthreads();
-        part[threadIdx.x] += v;
+        if (warp == 0) {                                  // scan of the warp totals
+            uint32_t w = warp_sum[lane];
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += y;
+            }
+            warp_sum[lane] = w;
+        }
         __syncthreads();
-    }
-    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
-    for (int b = b0; b < b1; ++b) {
-        cursor[b] = run;
-        run += count[b];
+        const uint32_t before = carry + (warp ? warp_sum[warp - 1] : 0u);
+        if (b < nb) cursor[b] = before + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sum[kScanThreads / 32 - 1];
+        __syncthreads();
     }
 }
 
