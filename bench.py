@@ -292,39 +292,70 @@ def run_ours(args, rank: int, world: int):
         t_frame = float(t.item())
     value = world * P * R * K / (t_frame / 1e3)
 
-    # e2e through the C ABI with host buffers
+    # e2e through the C ABI with host buffers: every frame uploads its
+    # direct-light atlas from pinned memory and reads both probe atlases
+    # back.  Uploads and readbacks run on two more streams, overlapped with
+    # the neighbouring frames' compute: frame k's upload lands in a device staging buffer
+    # (two, alternating) and is moved into the bound atlas on the compute
+    # stream; frame k's readback runs while frame k + 1 computes, and frame
+    # k + 2 (which overwrites that ping-pong atlas) waits for it.
     e2e = None
     if not args.no_e2e:
-        direct_h = torch.from_numpy(host.direct.view(np.int16)).pin_memory()
+        direct_h = [torch.from_numpy(host.direct.view(np.int16)).pin_memory() for _ in range(2)]
+        stage = [torch.empty_like(dev.direct) for _ in range(2)]
         irr, dist = vol.atlases()
-        irr_h = torch.empty(irr.shape, dtype=irr.dtype).pin_memory()
-        dist_h = torch.empty(dist.shape, dtype=dist.dtype).pin_memory()
-        erots = [frame_rotation(seed + 1000, f) for f in range(K)]
-        for f in range(2):
-            dev.direct.copy_(direct_h, non_blocking=True)
-            vol.update(erots[f])
-            irr, dist = vol.atlases()
-            irr_h.copy_(irr, non_blocking=True)
-            dist_h.copy_(dist, non_blocking=True)
+        irr_h = [torch.empty(irr.shape, dtype=irr.dtype).pin_memory() for _ in range(2)]
+        dist_h = [torch.empty(dist.shape, dtype=dist.dtype).pin_memory() for _ in range(2)]
+        erots = [frame_rotation(seed + 1000, f) for f in range(K + 2)]
+        up = torch.cuda.Stream(device=dev_t)
+        down = torch.cuda.Stream(device=dev_t)
+
+        def e2e_run(frames):
+            up_done = [None, None]        # staging k % 2 filled
+            stage_free = [None, None]     # staging k % 2 consumed by its frame
+            back_done = [None, None]      # readback of the atlas slot k % 2 finished
+            for k in frames:
+                b = k % 2
+                with torch.cuda.stream(up):
+                    if stage_free[b] is not None:
+                        up.wait_event(stage_free[b])
+                    stage[b].copy_(direct_h[b], non_blocking=True)
+                    up_done[b] = torch.cuda.Event()
+                    up_done[b].record(up)
+                stream.wait_event(up_done[b])
+                if back_done[b] is not None:
+                    stream.wait_event(back_done[b])
+                with torch.cuda.stream(stream):
+                    dev.direct.copy_(stage[b], non_blocking=True)
+                stage_free[b] = torch.cuda.Event()
+                stage_free[b].record(stream)
+                vol.update(erots[k], stream)
+                done = torch.cuda.Event()
+                done.record(stream)
+                irr, dist = vol.atlases()
+                with torch.cuda.stream(down):
+                    down.wait_event(done)
+                    irr_h[b].copy_(irr, non_blocking=True)
+                    dist_h[b].copy_(dist, non_blocking=True)
+                    back_done[b] = torch.cuda.Event()
+                    back_done[b].record(down)
             torch.cuda.synchronize()
+
+        e2e_run(range(2))
         if world > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
-        for k in range(K):
-            dev.direct.copy_(direct_h, non_blocking=True)
-            vol.update(erots[k])
-            irr, dist = vol.atlases()
-            irr_h.copy_(irr, non_blocking=True)
-            dist_h.copy_(dist, non_blocking=True)
-            torch.cuda.synchronize()
+        e2e_run(range(2, K + 2))
         te = time.perf_counter() - t0
         if world > 1:
             t = torch.tensor([te], device=dev_t)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             te = float(t.item())
         e2e = {"value": world * P * R * K / te, "unit": "probe-rays/s",
-               "h2d_bytes_per_step": int(direct_h.numel() * 2 + 36),
-               "d2h_bytes_per_step": int(irr_h.numel() * irr_h.element_size() + dist_h.numel() * dist_h.element_size())}
+               "h2d_bytes_per_step": int(direct_h[0].numel() * 2 + 36),
+               "d2h_bytes_per_step": int(irr_h[0].numel() * irr_h[0].element_size() +
+                                         dist_h[0].numel() * dist_h[0].element_size()),
+               "overlap": "uploads and readbacks on two more streams, overlapped with the neighbouring frames"}
 
     pk = peaks()
     avg_trace_ms = sum(t_trace) / K
@@ -444,30 +475,42 @@ def run_batch(args, rank: int, world: int):
     seq_value = world * pr * K / (seq_ms / 1e3)
 
     # e2e: rotations from the host, every volume's atlases read back to
-    # pinned host memory each frame
+    # pinned host memory each frame; the readback of frame k runs on a
+    # second stream while frame k + 1 computes, and frame k + 2 (which
+    # overwrites those ping-pong atlases) waits for it
     e2e = None
     if not args.no_e2e:
         views = [v.atlases() for v in vols]
-        hosts = [(torch.empty(i.shape, dtype=i.dtype).pin_memory(), torch.empty(d.shape, dtype=d.dtype).pin_memory())
-                 for i, d in views]
+        hosts = [[(torch.empty(i.shape, dtype=i.dtype).pin_memory(), torch.empty(d.shape, dtype=d.dtype).pin_memory())
+                  for i, d in views] for _ in range(2)]
+        copy = torch.cuda.Stream(device=dev_t)
 
-        def e2e_step(f):
-            batch.update(rots[f], stream)
-            for v, (ih, dh) in zip(vols, hosts):
-                i, d = v.atlases()
-                ih.copy_(i, non_blocking=True)
-                dh.copy_(d, non_blocking=True)
+        def e2e_run(frames):
+            back_done = [None, None]
+            for f in frames:
+                b = f % 2
+                if back_done[b] is not None:
+                    stream.wait_event(back_done[b])
+                batch.update(rots[f], stream)
+                done = torch.cuda.Event()
+                done.record(stream)
+                cur = [v.atlases() for v in vols]
+                with torch.cuda.stream(copy):
+                    copy.wait_event(done)
+                    for (i, d), (ih, dh) in zip(cur, hosts[b]):
+                        ih.copy_(i, non_blocking=True)
+                        dh.copy_(d, non_blocking=True)
+                    back_done[b] = torch.cuda.Event()
+                    back_done[b].record(copy)
             torch.cuda.synchronize()
 
-        for f in range(2):
-            e2e_step(f)
+        e2e_run(range(2))
         if world > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
-        for f in range(W, W + K):
-            e2e_step(f)
+        e2e_run(range(W, W + K))
         te = time.perf_counter() - t0
-        d2h = sum(ih.numel() * ih.element_size() + dh.numel() * dh.element_size() for ih, dh in hosts)
+        d2h = sum(ih.numel() * ih.element_size() + dh.numel() * dh.element_size() for ih, dh in hosts[0])
         e2e = {"value": world * pr * K / te, "unit": "probe-rays/s", "h2d_bytes_per_step": 36 * n,
                "d2h_bytes_per_step": int(d2h)}
     if rank != 0:
