@@ -535,6 +535,147 @@ def run_batch(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------- surface lighting
+def run_surface(args, rank: int, world: int):
+    """Surface-cache lighting form: the production scene (2048^2 atlas, 612
+    tiles of 80^2 texels), the sun plus seeded point and spot lights, every
+    object redrawn (the GI refresh frame of the reference's schedule).  A
+    step is one luxgi_surface_light pass: emissive copy, then per light the
+    SDF shadow march and the BRDF for every footprint texel the light's
+    tile selection covers.  The metric is texel-light evaluations/s."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import oracle
+    from luxgi_gb300 import DeviceScene, HostScene, _native as N
+    from luxgi_gb300.scene import PRODUCTION
+    from luxgi_gb300.surface import SurfaceLighting, light_array, scene_lights, select_tiles
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev_t = torch.device("cuda", local)
+    nl = int(args.workload.rsplit("_l", 1)[1]) if "_l" in args.workload else 4
+    w = PRODUCTION
+    host = HostScene(w.scene)
+    dev = DeviceScene(host, w.volume.light_mode, device=f"cuda:{local}")
+    lights = scene_lights(host, nl, seed=7)
+    tiles, masks = select_tiles(host, range(host.num_objects), lights)
+    tl = (N.SurfaceTile * host.num_tiles).from_buffer_copy(host.tiles.tobytes())
+    res = host.atlas
+    sizes = np.array([(round(tl[int(t)].extends[2] * res) + 1) * (round(tl[int(t)].extends[3] * res) + 1)
+                      for t in tiles], dtype=np.int64)
+    texels = int(sizes.sum())
+    evals = int(sum(int(sz) * bin(int(m)).count("1") for sz, m in zip(sizes, masks)))
+    cam = tuple(host.surface_data.camera_pos)
+    pass_ = SurfaceLighting(dev)
+    K, W = args.steps, args.warmup
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.int8, device=dev_t)
+    t_dev = torch.as_tensor(tiles.view(np.int32)).to(dev_t)
+    m_dev = torch.as_tensor(masks.view(np.int32)).to(dev_t)
+    arr = light_array(lights)
+    d = N.SurfaceLighting()
+    d.lights = ctypes.cast(arr, ctypes.c_void_p)
+    d.num_lights = len(lights)
+    d.num_tiles = int(tiles.size)
+    d.tiles = t_dev.data_ptr()
+    d.light_masks = m_dev.data_ptr()
+    d.camera_pos[:] = list(cam)
+    d.shadow_bias = pass_.shadow_bias
+    d.copy_emissive = 1
+    d.max_steps = pass_.max_steps
+    lib = N.ddgi()
+
+    def step():
+        N.check(lib.luxgi_surface_light(ctypes.byref(dev.sdf_desc), ctypes.byref(dev.surface_desc), ctypes.byref(d),
+                                        dev.direct.data_ptr(), stream.cuda_stream), "surface_light")
+
+    for _ in range(W):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = Clocks(local)
+    launches0 = lib.luxgi_launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks.start()
+    torch.cuda.synchronize()
+    for e0, e1 in ev:
+        flush.zero_()
+        e0.record(stream)
+        step()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = lib.luxgi_launch_count() - launches0
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    if world > 1:
+        t = torch.tensor([ms], device=dev_t)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * evals * K / (ms / 1e3)
+
+    # e2e: the light records and tile lists from host memory each step (the
+    # reference uploads them as uniforms and vertex buffers per draw), the
+    # lit atlas read back to pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        out_h = torch.empty(dev.direct.shape, dtype=dev.direct.dtype).pin_memory()
+        t_h = torch.from_numpy(tiles.view(np.int32).copy()).pin_memory()
+        m_h = torch.from_numpy(masks.view(np.int32).copy()).pin_memory()
+
+        def e2e_step():
+            t_dev.copy_(t_h, non_blocking=True)
+            m_dev.copy_(m_h, non_blocking=True)
+            step()
+            out_h.copy_(dev.direct, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(K):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        e2e = {"value": world * evals * K / te, "unit": "texel-light evaluations/s",
+               "h2d_bytes_per_step": int(tiles.nbytes + masks.nbytes + 64 * len(lights)),
+               "d2h_bytes_per_step": int(out_h.numel() * out_h.element_size())}
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        inp = oracle.HostInputs(host, w.volume.light_mode, mip=dev.mip.cpu().numpy(),
+                                chunks=dev.chunks.cpu().numpy().view(np.uint32),
+                                culled=dev.culled.cpu().numpy().view(np.uint32))
+        n = 4
+        while True:
+            t0 = time.perf_counter()
+            oracle.surface_light(inp, lights, tiles[:n], masks[:n], cam)
+            el = time.perf_counter() - t0
+            if el * 4 > args.cpu_seconds or n >= tiles.size:
+                break
+            n = min(int(tiles.size), max(n * 2, int(n * args.cpu_seconds / 2 / max(el, 1e-3))))
+        ev_n = int(sum(int(sz) * bin(int(m)).count("1") for sz, m in zip(sizes[:n], masks[:n])))
+        cpu = {"value": ev_n / el, "unit": "texel-light evaluations/s", "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"{n} of {tiles.size} tiles, {ev_n} texel-light evaluations (oracle FP32, {el:.2f} s)"}
+    line = {
+        "metric": "surface-cache texel-light evaluations/s (emissive copy + SDF-shadowed BRDF per light)",
+        "value": round(value, 1), "unit": "texel-light evaluations/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": round(ms / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 shading and march, fp16 atlas", "data": "synthetic (seeded analytic scene)",
+        "config": {"workload": f"surface_light_production_atlas{res}_l{len(lights)}", "tiles": int(tiles.size),
+                   "texels": texels, "texel_light_evaluations": evals, "lights": [int(L.type) for L in lights],
+                   "shadow_max_steps": pass_.max_steps, "parallelism": f"replicas{world}",
+                   "l2": "256 MB flush between passes (outside the events)"},
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------------- serve
 def run_serve(args, rank: int, world: int):
     """Serving form: sessions with batching-form volumes and scenes, Poisson
@@ -653,6 +794,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload.startswith("batch"):
         run_batch(args, rank, world)
+    elif args.workload.startswith("surface_light"):
+        run_surface(args, rank, world)
     elif args.workload.startswith("serve"):
         run_serve(args, rank, world)
     else:

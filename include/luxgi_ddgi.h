@@ -167,6 +167,12 @@ typedef struct luxgi_surface_desc {
                                                    .frag:114)                 */
     const float*                gbuffer1;       /* device float4: oct normal.xy,
                                                    world.yz (:115)            */
+    const uint8_t*              pbr;            /* device RGBA8 UNORM res^2
+                                                   (SurfaceGBufferPRB): r
+                                                   metallic, g roughness; NULL
+                                                   = metallic 0, roughness 1  */
+    const uint16_t*             emissive;       /* device RGBA16F res^2
+                                                   (SurfaceEmissive), or NULL */
 } luxgi_surface_desc;
 
 /* Volume configuration: DDGIUniform plus the IrradianceVolume fields the
@@ -366,10 +372,13 @@ int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* vol, int enable);
 int luxgi_ddgi_load_atlases(luxgi_ddgi_volume* vol, const void* irradiance_host,
                             const void* distance_host, int32_t frames, void* stream);
 
-/* Mode A infinite bounce (SDFAtlasIndirectLight.frag:44-67): for every
- * surface-atlas texel covered by a tile, light_cache = direct_light +
- * intensity * min(albedo,0.9)/pi * sampleIrradiance(prev atlases).  When
- * infinite bounce is off or no frame is done yet it copies direct_light. */
+/* Mode A infinite bounce (SDFAtlasIndirectLight.frag:44-67) over the
+ * raster footprint of every tile (see luxgi_surface_light): light_cache =
+ * direct_light + intensity * (a - a * metallic)/pi * sampleIrradiance(prev
+ * atlases), a = min(albedo, 0.9), albedo, normal, position and metallic
+ * sampled bilinearly at the fragment's atlas coordinate.  Texels outside
+ * every tile keep their light_cache value.  When infinite bounce is off or
+ * no frame is done yet the footprint gets direct_light unchanged. */
 int luxgi_ddgi_inject_indirect(luxgi_ddgi_volume* vol, void* stream);
 
 /* sampleIrradiance (DDGICommon.glsl:163-233) for n points against the
@@ -411,6 +420,68 @@ int luxgi_sdf_build_mip_noalloc(const luxgi_sdf_desc* sdf, void* mip, void* stre
  * when the lists do not fit (chunks that do not fit stay empty). */
 int luxgi_surface_cull(const luxgi_surface_desc* surface, uint32_t* chunks,
                        uint32_t* culled, uint32_t capacity, void* stream);
+
+/* Light (Common/Light.glsl:19-28, std140), 64 bytes. */
+typedef struct luxgi_light {
+    float color[4];                /* rgb                                     */
+    float position[4];             /* xyz: point and spot lights              */
+    float direction[4];            /* xyz, unit: directional and spot lights  */
+    float intensity;
+    float radius;                  /* attenuation radius (point, spot)        */
+    float type;                    /* luxgi_light_type, a float as in GLSL    */
+    float angle;                   /* spot: cut-off cosine is 1 - angle       */
+} luxgi_light;
+
+enum luxgi_light_type {            /* Light.glsl:13-15 */
+    LUXGI_LIGHT_DIRECTIONAL = 0,
+    LUXGI_LIGHT_SPOT        = 1,
+    LUXGI_LIGHT_POINT       = 2
+};
+#define LUXGI_MAX_LIGHTS 32        /* MAX_LIGHTS, Light.glsl:30 */
+
+/* One surface-cache lighting pass: the CopyEmissive draw followed by one
+ * SDFDeferredLight draw per light (GlobalSurfaceAtlas.cpp:886-996), over a
+ * list of tiles.  A tile covers the atlas pixels [x, x + w] x [y, y + h],
+ * (x, y, w, h) = round(extends * resolution): the tile quad of addTiles2
+ * (GlobalSurfaceAtlas.cpp:554-574) spans w + 1 pixels, the TileBuffer
+ * extends holding the width less one texel of padding (:272-279).  The
+ * fragment at pixel (x + i, y + j) samples every surface texture bilinearly
+ * with REPEAT (the textures' default sampler, RHI/Definitions.h:152-159)
+ * at atlasUV = ((i + 0.5) / (w + 1), (j + 0.5) / (h + 1)) * extends.zw +
+ * extends.xy. */
+typedef struct luxgi_surface_lighting {
+    const luxgi_light* lights;     /* HOST, num_lights entries (copied into
+                                      the launch's parameters)                */
+    int32_t         num_lights;    /* 0 .. LUXGI_MAX_LIGHTS                   */
+    int32_t         num_tiles;     /* entries of tiles and light_masks        */
+    const uint32_t* tiles;         /* device: tile addresses, 1 .. surface
+                                      num_tiles - 1, each at most once (others
+                                      are skipped)                            */
+    const uint32_t* light_masks;   /* device: bit l set = light l draws tile k
+                                      (the per-light tile selection of
+                                      GlobalSurfaceAtlas.cpp:912-944); NULL =
+                                      every light draws every tile            */
+    float           camera_pos[3]; /* UniformBufferObject.cameraPos.xyz       */
+    float           shadow_bias;   /* cameraPos.w = GlobalSurface::shadowBias
+                                      (1 in the reference)                    */
+    int32_t         copy_emissive; /* 1: the footprint first gets the sampled
+                                      surface emissive (alpha 1 where the
+                                      surface has none); 0: lights add onto
+                                      `out` as it is                          */
+    int32_t         max_steps;     /* shadow march step cap per cascade; 250
+                                      in the reference (SDFCommon.glsl:143)   */
+    int32_t         reserved[2];
+} luxgi_surface_lighting;
+
+/* SDF-shadowed direct lighting of the surface cache: per footprint pixel,
+ * for each light of its tile in index order, `out` (device RGBA16F res^2)
+ * += (BRDF * radiance * cos * shadow * attenuation, 1), rounded to FP16
+ * after each light like the additive blend into a 16-bit target
+ * (SDFDeferredLight.frag:41-129, Raytraced/BRDF.glsl:65-81).  The shadow is
+ * a global-SDF march towards the light from position + normal * bias with
+ * start bias 2 voxels and no hit normal (SDFDeferredLight.frag:95-118). */
+int luxgi_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surface,
+                        const luxgi_surface_lighting* lighting, void* out, void* stream);
 
 /* ------------------------------------------------------------ misc */
 const char* luxgi_strerror(int status);

@@ -79,6 +79,9 @@ typedef struct luxgi_scene_view {
     const luxgi_scene_primitive* primitives;   /* spheres/boxes, then walls  */
     float                       sun_direction[3];
     float                       sun_color[3];
+    const uint8_t*              pbr;           /* RGBA8 res^2: metallic,
+                                                  roughness, 0, 1            */
+    const uint16_t*             emissive;      /* RGBA16F res^2              */
 } luxgi_scene_view;
 
 typedef struct luxgi_scene luxgi_scene;

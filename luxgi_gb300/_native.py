@@ -26,6 +26,10 @@ STORAGE_FP32 = 0
 STORAGE_FP16 = 1
 LIGHT_CACHE = 0
 LIGHT_PER_HIT = 1
+LIGHT_DIRECTIONAL = 0
+LIGHT_SPOT = 1
+LIGHT_POINT = 2
+MAX_LIGHTS = 32
 BLEND_FP32 = 0
 BLEND_TENSOR = 1
 
@@ -71,7 +75,18 @@ class SurfaceDesc(ctypes.Structure):
     _fields_ = [("data", SurfaceData), ("num_objects", c_int32), ("num_tiles", c_int32), ("objects", c_void_p),
                 ("tiles", c_void_p), ("chunks", c_void_p), ("culled_objects", c_void_p), ("light_cache", c_void_p),
                 ("depth", c_void_p), ("direct_light", c_void_p), ("albedo", c_void_p), ("gbuffer0", c_void_p),
-                ("gbuffer1", c_void_p)]
+                ("gbuffer1", c_void_p), ("pbr", c_void_p), ("emissive", c_void_p)]
+
+
+class Light(ctypes.Structure):
+    _fields_ = [("color", c_float * 4), ("position", c_float * 4), ("direction", c_float * 4), ("intensity", c_float),
+                ("radius", c_float), ("type", c_float), ("angle", c_float)]
+
+
+class SurfaceLighting(ctypes.Structure):
+    _fields_ = [("lights", c_void_p), ("num_lights", c_int32), ("num_tiles", c_int32), ("tiles", c_void_p),
+                ("light_masks", c_void_p), ("camera_pos", c_float * 3), ("shadow_bias", c_float),
+                ("copy_emissive", c_int32), ("max_steps", c_int32), ("reserved", c_int32 * 2)]
 
 
 class VolumeDesc(ctypes.Structure):
@@ -138,7 +153,8 @@ class SceneView(ctypes.Structure):
                 ("surface_data", SurfaceData), ("num_objects", c_int32), ("num_tiles", c_int32), ("objects", c_void_p),
                 ("tiles", c_void_p), ("atlas_resolution", c_int32), ("direct_light", c_void_p), ("depth", c_void_p),
                 ("albedo", c_void_p), ("gbuffer0", c_void_p), ("gbuffer1", c_void_p), ("num_primitives", c_int32),
-                ("primitives", c_void_p), ("sun_direction", c_float * 3), ("sun_color", c_float * 3)]
+                ("primitives", c_void_p), ("sun_direction", c_float * 3), ("sun_color", c_float * 3),
+                ("pbr", c_void_p), ("emissive", c_void_p)]
 
 
 assert ctypes.sizeof(DDGIUniform) == 96
@@ -146,6 +162,8 @@ assert ctypes.sizeof(SdfData) == 96
 assert ctypes.sizeof(SurfaceData) == 32
 assert ctypes.sizeof(SurfaceObject) == 128
 assert ctypes.sizeof(SurfaceTile) == 96
+assert ctypes.sizeof(Light) == 64
+assert ctypes.sizeof(SurfaceLighting) == 64
 
 # (name, restype, argtypes) of every exported entry point, as declared in
 # include/luxgi_ddgi.h
@@ -180,6 +198,8 @@ DDGI_API = [
     ("luxgi_sdf_build_mip", c_int, [POINTER(SdfDesc), c_void_p, c_void_p, c_void_p]),
     ("luxgi_sdf_build_mip_noalloc", c_int, [POINTER(SdfDesc), c_void_p, c_void_p]),
     ("luxgi_surface_cull", c_int, [POINTER(SurfaceDesc), c_void_p, c_void_p, c_uint32, c_void_p]),
+    ("luxgi_surface_light", c_int, [POINTER(SdfDesc), POINTER(SurfaceDesc), POINTER(SurfaceLighting), c_void_p,
+                                    c_void_p]),
     ("luxgi_strerror", ctypes.c_char_p, [c_int]),
     ("luxgi_launch_count", c_uint64, []),
 ]

@@ -24,11 +24,12 @@ OBJ = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose FP32 arithmetic must match the CPU restatement bit
 # for bit are built without FMA contraction
-NO_FMAD = {"trace.cu", "setup.cu"}
+NO_FMAD = {"trace.cu", "setup.cu", "surface.cu"}
 # shading is compared with the restatement by tolerance: approximate
 # division and square root
 FAST_DIV = {"shade.cu"}
-CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "capi.cu", "batch.cu", "server.cu"]
+CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "surface.cu", "capi.cu", "batch.cu",
+                "server.cu"]
 
 
 def nvcc() -> str:

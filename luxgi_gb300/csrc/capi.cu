@@ -754,7 +754,7 @@ int luxgi_ddgi_inject_indirect(luxgi_ddgi_volume* v, void* stream) {
     A.storage = v->desc.storage;
     const int bounce = (v->desc.infinite_bounce && v->frames != 0) ? 1 : 0;
     return cuda_status(launch_inject(v->desc.uniform, surface_view(s, LUXGI_LIGHT_CACHE), s.gbuffer0, s.gbuffer1,
-                                     reinterpret_cast<const __half*>(s.direct_light),
+                                     s.pbr, reinterpret_cast<const __half*>(s.direct_light),
                                      static_cast<__half*>(s.light_cache), A, s.num_tiles, v->desc.intensity, bounce,
                                      static_cast<cudaStream_t>(stream)));
 }
@@ -795,6 +795,24 @@ int luxgi_surface_cull(const luxgi_surface_desc* s, uint32_t* chunks, uint32_t* 
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_status(e);
     return status ? LUXGI_ENOMEM : LUXGI_OK;
+}
+
+int luxgi_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s, const luxgi_surface_lighting* L,
+                        void* out, void* stream) {
+    if (!sdf || !s || !L || !out) return LUXGI_EINVAL;
+    if (L->num_lights < 0 || L->num_lights > LUXGI_MAX_LIGHTS || (L->num_lights > 0 && !L->lights)) return LUXGI_EINVAL;
+    if (L->num_tiles < 0 || L->num_tiles > 65535 || (L->num_tiles > 0 && !L->tiles)) return LUXGI_EINVAL;
+    if (!(L->shadow_bias >= 0.0f) || L->max_steps < 1) return LUXGI_EINVAL;
+    if (!s->tiles || !s->gbuffer0 || !s->gbuffer1 || s->data.resolution < 1) return LUXGI_EINVAL;
+    if (L->num_lights > 0 && (!sdf->sdf || !sdf->mip || sdf->data.cascades_count < 1)) return LUXGI_EINVAL;
+    if (sdf->format != LUXGI_STORAGE_FP32 && sdf->format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    for (int i = 0; i < L->num_lights; ++i) {
+        const float t = L->lights[i].type;
+        if (t != float(LUXGI_LIGHT_DIRECTIONAL) && t != float(LUXGI_LIGHT_SPOT) && t != float(LUXGI_LIGHT_POINT))
+            return LUXGI_EINVAL;
+    }
+    return cuda_status(launch_surface_light(sdf_view(*sdf), *s, *L, static_cast<__half*>(out),
+                                            static_cast<cudaStream_t>(stream)));
 }
 
 }  // extern "C"

@@ -328,16 +328,17 @@ __device__ __forceinline__ void march_state_init(MarchState& m) {
     m.fine = 0;
 }
 
-// tracyGlobalSDF (SDFCommon.glsl:98-194) with stepScale 1, start bias 0,
-// hit normal requested (GISDFRays.comp:79-87), run for at most `budget`
-// steps: returns true with `hit` filled when the march ended (hit, or every
-// cascade left), false when the budget ran out first (m holds the state to
-// resume from).  Resuming performs exactly the arithmetic of an unbroken
-// march.  QMIP / QTEX select the layouts (VolLayout) read for the mip /
-// full-resolution volume.
-template <typename T, int QMIP = kPlain, int QTEX = kPlain>
+// tracyGlobalSDF (SDFCommon.glsl:98-194) with stepScale 1, run for at most
+// `budget` steps: returns true with `hit` filled when the march ended (hit,
+// or every cascade left), false when the budget ran out first (m holds the
+// state to resume from).  Resuming performs exactly the arithmetic of an
+// unbroken march.  QMIP / QTEX select the layouts (VolLayout) read for the
+// mip / full-resolution volume.  The probe rays use start bias 0 and want
+// the hit normal (GISDFRays.comp:79-87); the surface-cache shadow rays start
+// 2 voxels along and skip it (SDFDeferredLight.frag:104-111).
+template <typename T, int QMIP = kPlain, int QTEX = kPlain, bool NORMAL = true>
 __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps,
-                                          MarchState& m, int budget, MarchHit& hit) {
+                                          MarchState& m, int budget, MarchHit& hit, float start_bias = 0.0f) {
     const int C = s.C;
     const int TW = s.res * C, MW = s.mres * C;
     const float tmax = mn(trace_max, s.data.cascade_pos_distance[C - 1][3] * 2.0f);
@@ -353,7 +354,7 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
                     cz = s.data.cascade_pos_distance[cascade][2], cw = s.data.cascade_pos_distance[cascade][3];
         const float voxel = s.data.cascade_voxel_size[cascade];
         const float voxel_half = voxel * 0.5f;
-        const f3 wpos = add3(origin, mul3(dir, voxel * 0.0f));
+        const f3 wpos = add3(origin, mul3(dir, voxel * start_bias));
         if (!m.in_cascade) {
             // lineHitAABB (SDFCommon.glsl:84-95)
             const f3 d = sub3(end, wpos);
@@ -407,7 +408,10 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
                 hit.time = mx(t + sd - thick, 0.0f);
                 hit.cascade = cascade;
                 hit.sdf = sd;
-                hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, tu, uy, uz, 1.0f / s.data.resolution);
+                if (NORMAL)
+                    hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, tu, uy, uz, 1.0f / s.data.resolution);
+                else
+                    hit.normal = f3{0.0f, 0.0f, 0.0f};
                 hit.steps = m.steps + step;
                 hit.fine = m.fine;
                 return true;

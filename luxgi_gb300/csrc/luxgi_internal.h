@@ -194,8 +194,10 @@ cudaError_t launch_blend_batch(const BlendParams* vp, const int* starts_irr, int
                                int storage, cudaStream_t st);
 cudaError_t launch_border(const luxgi_ddgi_uniform& u, void* irr, void* dist, int storage, cudaStream_t st);
 cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const float* gb0, const float* gb1,
-                          const __half* direct, __half* light, const AtlasView& A, int num_tiles, float intensity,
-                          int bounce, cudaStream_t st);
+                          const uint8_t* pbr, const __half* direct, __half* light, const AtlasView& A, int num_tiles,
+                          float intensity, int bounce, cudaStream_t st);
+cudaError_t launch_surface_light(const SdfView& sdf, const luxgi_surface_desc& s, const luxgi_surface_lighting& L,
+                                 __half* out, cudaStream_t st);
 cudaError_t launch_sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, const float* pos,
                                      const float* nrm, const float* wo, float* out, int n, cudaStream_t st);
 cudaError_t launch_mip(const luxgi_sdf_desc& s, void* mip, void* tmp, cudaStream_t st);

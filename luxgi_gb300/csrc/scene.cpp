@@ -145,6 +145,8 @@ struct luxgi_scene {
     std::vector<float> depth;
     std::vector<uint8_t> albedo;
     std::vector<float> gb0, gb1;
+    std::vector<uint8_t> pbr;                   // RGBA8: metallic, roughness, 0, 1
+    std::vector<uint16_t> emissive;             // RGBA16F
     std::vector<luxgi_scene_primitive> prims;   // spheres/boxes then walls
     int n_solid = 0;                            // spheres + boxes
     float wall_half_inner = 0.0f;
@@ -241,6 +243,22 @@ int build_surface(luxgi_scene& s) {
     s.albedo.assign(texels * 4, 0);
     s.gb0.assign(texels * 4, 0.0f);
     s.gb1.assign(texels * 4, 0.0f);
+    s.pbr.assign(texels * 4, 0);
+    s.emissive.assign(texels * 4, 0);
+    for (size_t i = 0; i < texels; ++i) s.emissive[i * 4 + 3] = luxgi_float_to_half(1.0f);   // R11G11B10 reads a = 1
+    // materials from a stream of their own, so that the geometry and albedo
+    // draws stay those of scenes built without them: solids get metallic in
+    // [0, 0.6) and roughness in [0.25, 1); every seventh solid (3, 10, ...)
+    // emits 1.5 x its albedo; walls are rough dielectrics
+    Rng mrng(s.cfg.seed ^ 0x6D6174657269616Cull);
+    std::vector<float> metal(size_t(nobj), 0.0f), rough(size_t(nobj), 0.9f), emit(size_t(nobj), 0.0f);
+    for (int o = 0; o < nobj; ++o) {
+        const float m = mrng.uniform(0.0f, 0.6f), r = mrng.uniform(0.25f, 1.0f);
+        if (s.prims[size_t(o)].kind == 2) continue;
+        metal[size_t(o)] = m;
+        rough[size_t(o)] = r;
+        if (o % 7 == 3) emit[size_t(o)] = 1.5f;
+    }
 
     s.objects.assign(size_t(nobj), luxgi_surface_object{});
     s.tiles.assign(size_t(ntiles + 1), luxgi_surface_tile{});   // slot 0 = no tile
@@ -313,6 +331,12 @@ int build_surface(luxgi_scene& s) {
                         alb[q] = float(a8) / 255.0f;
                     }
                     s.albedo[ti * 4 + 3] = 255;
+                    s.pbr[ti * 4 + 0] = uint8_t(std::lround(metal[size_t(o)] * 255.0f));
+                    s.pbr[ti * 4 + 1] = uint8_t(std::lround(rough[size_t(o)] * 255.0f));
+                    s.pbr[ti * 4 + 3] = 255;
+                    for (int q = 0; q < 3; ++q)
+                        s.emissive[ti * 4 + size_t(q)] = luxgi_float_to_half(alb[q] * emit[size_t(o)]);
+                    s.emissive[ti * 4 + 3] = luxgi_float_to_half(1.0f);
                     float ndl = std::max(dot(nrm, s.sun), 0.0f);
                     float sc[3] = {s.sun_color.x, s.sun_color.y, s.sun_color.z};
                     for (int q = 0; q < 3; ++q)
@@ -435,6 +459,8 @@ extern "C" int luxgi_scene_view_get(const luxgi_scene* s, luxgi_scene_view* v) {
     v->primitives = s->prims.data();
     v->sun_direction[0] = s->sun.x; v->sun_direction[1] = s->sun.y; v->sun_direction[2] = s->sun.z;
     v->sun_color[0] = s->sun_color.x; v->sun_color[1] = s->sun_color.y; v->sun_color[2] = s->sun_color.z;
+    v->pbr = s->pbr.data();
+    v->emissive = s->emissive.data();
     return LUXGI_OK;
 }
 

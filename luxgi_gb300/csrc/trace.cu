@@ -1,7 +1,7 @@
-// Ray generation, SDF sphere tracing and hit shading (GISDFRays.comp), the
-// mode-A light-cache injection (SDFAtlasIndirectLight.frag) and batched
-// sampleIrradiance.  Built with -fmad=false: the march must reproduce the
-// FP32 CPU restatement bit for bit.
+// Ray generation and SDF sphere tracing (GISDFRays.comp), their batched
+// launches, and sampleIrradiance for caller points.  Built with
+// -fmad=false: the march must reproduce the FP32 CPU restatement bit for
+// bit.
 #include <algorithm>
 
 #include <cuda_fp16.h>
@@ -607,64 +607,6 @@ cudaError_t launch_pair_pack(const void* src, int W, int H, int D, int format, v
         pair_pack_kernel<__half><<<blocks, 256, 0, st>>>(static_cast<const __half*>(src), W, H, D, static_cast<__half2*>(dst));
     else
         pair_pack_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(src), W, H, D, static_cast<float2*>(dst));
-    note_launch();
-    return cudaGetLastError();
-}
-
-// --------------------------------------------------------------- inject
-// SDFAtlasIndirectLight.frag:44-67 over every texel of every tile rect
-// (the raster pass draws each tile's (w-1) x (h-1) viewport): the light
-// cache becomes direct light plus intensity * min(albedo, 0.9)/pi *
-// sampleIrradiance(previous atlases).  One block row per tile.
-__global__ void inject_kernel(const luxgi_ddgi_uniform u, const SurfaceView s, const float* __restrict__ gb0,
-                              const float* __restrict__ gb1, const __half* __restrict__ direct,
-                              __half* __restrict__ light, const AtlasView A, float intensity, int bounce) {
-    const int t = blockIdx.y + 1;                 // tile slot 0 is "no tile"
-    const luxgi_surface_tile* tl = s.tiles + t;
-    const int res = int(s.data.resolution);
-    const int x0 = int(lrintf(__ldg(&tl->extends[0]) * float(res)));
-    const int y0 = int(lrintf(__ldg(&tl->extends[1]) * float(res)));
-    const int w = int(lrintf(__ldg(&tl->extends[2]) * float(res)));
-    const int h = int(lrintf(__ldg(&tl->extends[3]) * float(res)));
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < w * h; k += gridDim.x * blockDim.x) {
-        const int i = k % w, j = k / w;
-        const size_t ti = size_t(y0 + j) * res + (x0 + i);
-        float add[3] = {0.0f, 0.0f, 0.0f};
-        if (bounce) {
-            const float4 g0 = __ldg(reinterpret_cast<const float4*>(gb0) + ti);
-            const float4 g1 = __ldg(reinterpret_cast<const float4*>(gb1) + ti);
-            // octohedralToDirection (Math.glsl:27-33)
-            f3 v{g1.x, g1.y, 1.0f - fabsf(g1.x) - fabsf(g1.y)};
-            if (v.z < 0.0f) {
-                const float nx = (1.0f - fabsf(v.y)) * (v.x >= 0.0f ? 1.0f : -1.0f);
-                const float ny = (1.0f - fabsf(v.x)) * (v.y >= 0.0f ? 1.0f : -1.0f);
-                v.x = nx; v.y = ny;
-            }
-            const f3 n = norm3(v);
-            const f3 wp{g0.w, g1.z, g1.w};
-            const f3 cam{s.data.camera_pos[0], s.data.camera_pos[1], s.data.camera_pos[2]};
-            const f3 wo = norm3(sub3(cam, wp));
-            const f3 e = sample_irradiance(u, A, wp, n, wo);
-            const float alb[3] = {mn(g0.x, 0.9f), mn(g0.y, 0.9f), mn(g0.z, 0.9f)};
-            const float ev[3] = {e.x, e.y, e.z};
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float diff = (alb[c] - alb[c] * 0.0f) / kPi;
-                add[c] = intensity * diff * ev[c];
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) light[ti * 4 + c] = __float2half_rn(__half2float(direct[ti * 4 + c]) + add[c]);
-        light[ti * 4 + 3] = direct[ti * 4 + 3];
-    }
-}
-
-cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const float* gb0, const float* gb1,
-                          const __half* direct, __half* light, const AtlasView& A, int num_tiles, float intensity,
-                          int bounce, cudaStream_t st) {
-    if (num_tiles <= 1) return cudaSuccess;
-    dim3 grid(8, unsigned(num_tiles - 1));
-    inject_kernel<<<grid, 256, 0, st>>>(u, s, gb0, gb1, direct, light, A, intensity, bounce);
     note_launch();
     return cudaGetLastError();
 }

@@ -255,6 +255,8 @@ class HostScene:
         self.albedo = np.frombuffer(ctypes.string_at(v.albedo, A * A * 4), dtype=np.uint8).copy()
         self.gbuffer0 = np.frombuffer(ctypes.string_at(v.gbuffer0, A * A * 16), dtype=np.float32).copy()
         self.gbuffer1 = np.frombuffer(ctypes.string_at(v.gbuffer1, A * A * 16), dtype=np.float32).copy()
+        self.pbr = np.frombuffer(ctypes.string_at(v.pbr, A * A * 4), dtype=np.uint8).copy()
+        self.emissive = np.frombuffer(ctypes.string_at(v.emissive, A * A * 8), dtype=np.uint16).copy()
         prims = (N.ScenePrimitive * v.num_primitives).from_address(v.primitives)
         self.primitives = [(p.kind, tuple(p.center), tuple(p.half_extent), tuple(p.albedo)) for p in prims]
         self.sun_direction = tuple(v.sun_direction)
@@ -314,6 +316,8 @@ class DeviceScene:
         self.albedo = torch.from_numpy(host.albedo).to(dev)
         self.gbuffer0 = torch.from_numpy(host.gbuffer0).to(dev)
         self.gbuffer1 = torch.from_numpy(host.gbuffer1).to(dev)
+        self.pbr = torch.from_numpy(host.pbr).to(dev)
+        self.emissive = torch.from_numpy(host.emissive.view(np.int16)).to(dev)
         cap = host.cull_capacity()
         self.capacity = cap
         self.chunks = torch.zeros(40 * 40 * 40, dtype=torch.int32, device=dev)
@@ -334,10 +338,12 @@ class DeviceScene:
         self.surface_desc.albedo = self.albedo.data_ptr()
         self.surface_desc.gbuffer0 = self.gbuffer0.data_ptr()
         self.surface_desc.gbuffer1 = self.gbuffer1.data_ptr()
+        self.surface_desc.pbr = self.pbr.data_ptr()
+        self.surface_desc.emissive = self.emissive.data_ptr()
         N.check(lib.luxgi_surface_cull(ctypes.byref(self.surface_desc), self.chunks.data_ptr(),
                                        self.culled.data_ptr(), cap, stream), "surface_cull")
 
     def nbytes(self) -> int:
         ts = [self.sdf, self.mip, self.mip_tmp, self.objects, self.tiles, self.depth, self.direct, self.light_cache,
-              self.albedo, self.gbuffer0, self.gbuffer1, self.chunks, self.culled]
+              self.albedo, self.gbuffer0, self.gbuffer1, self.pbr, self.emissive, self.chunks, self.culled]
         return sum(t.numel() * t.element_size() for t in ts)

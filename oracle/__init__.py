@@ -62,6 +62,8 @@ def lib() -> ctypes.CDLL:
             "oracle_cull": (c_int, [vp, vp, vp, c_uint32]),
             "oracle_inject": (c_int, [vp, vp, vp, vp, c_int, c_int, vp]),
             "oracle_sample_irradiance": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int, c_int]),
+            "oracle_surface_light": (c_int, [vp, vp, vp, c_int, vp, vp, c_int, vp, c_float, c_int, c_int, c_int,
+                                             vp, vp]),
             "oracle_texel_dirs": (c_int, [c_int, c_int, vp]),
             "oracle_oct_encode": (c_int, [vp, c_int, vp]),
         }
@@ -161,6 +163,8 @@ class HostInputs:
         self.surface_desc.albedo = host.albedo.ctypes.data
         self.surface_desc.gbuffer0 = host.gbuffer0.ctypes.data
         self.surface_desc.gbuffer1 = host.gbuffer1.ctypes.data
+        self.surface_desc.pbr = host.pbr.ctypes.data
+        self.surface_desc.emissive = host.emissive.ctypes.data
 
 
 def build_mip(sdf_desc, sdf_float: np.ndarray) -> np.ndarray:
@@ -221,14 +225,39 @@ def border(uniform, irr: np.ndarray | None, dist: np.ndarray | None) -> None:
     lib().oracle_border(ctypes.byref(uniform), _p(irr), _p(dist))
 
 
-def inject(vdesc, inputs: HostInputs, irr, dist, frames: int, precision: int = 0) -> np.ndarray:
-    res = inputs.surface_desc.data.resolution
-    out = np.zeros(res * res * 4, dtype=np.uint16)
+def inject(vdesc, inputs: HostInputs, irr, dist, frames: int, precision: int = 0, base=None) -> np.ndarray:
+    """SDFAtlasIndirectLight over every tile footprint; texels outside the
+    footprints keep `base` (default: the inputs' current light cache)."""
+    out = np.array(inputs.light_cache if base is None else base, dtype=np.uint16, copy=True)
     i = np.ascontiguousarray(irr, dtype=np.float32)
     d = np.ascontiguousarray(dist, dtype=np.float32)
     lib().oracle_inject(ctypes.byref(vdesc), ctypes.byref(inputs.surface_desc), _p(i), _p(d), frames, precision,
                         _p(out))
     return out
+
+
+def surface_light(inputs: HostInputs, lights, tiles, masks=None, camera=(0.0, 0.0, 0.0), shadow_bias: float = 1.0,
+                  copy_emissive: bool = True, max_steps: int = 250, precision: int = 0, out=None,
+                  want_shadow: bool = False):
+    """CopyEmissive + SDFDeferredLight per light over `tiles` (tile
+    addresses).  lights: sequence of luxgi_light; masks: u32 per tile
+    (None = every light).  Returns the RGBA16F atlas (u16 bits) and, with
+    want_shadow, a u32 per texel with bit l set where light l was blocked."""
+    from luxgi_gb300 import _native as N
+
+    res = inputs.surface_desc.data.resolution
+    o = np.array(inputs.host.direct if out is None else out, dtype=np.uint16, copy=True)
+    t = np.ascontiguousarray(tiles, dtype=np.uint32)
+    m = None if masks is None else np.ascontiguousarray(masks, dtype=np.uint32)
+    sh = np.zeros(res * res, dtype=np.uint32) if want_shadow else None
+    cam = (c_float * 3)(*camera)
+    arr = (N.Light * max(1, len(lights)))(*lights)
+    st = lib().oracle_surface_light(ctypes.byref(inputs.sdf_desc), ctypes.byref(inputs.surface_desc),
+                                    ctypes.cast(arr, c_void_p), len(lights), _p(t), _p(m), t.size, cam,
+                                    float(shadow_bias), int(copy_emissive), int(max_steps), precision, _p(o), _p(sh))
+    if st != 0:
+        raise RuntimeError(f"oracle_surface_light status {st}")
+    return (o, sh) if want_shadow else o
 
 
 def sample_irradiance(uniform, irr, dist, pos, nrm, wo, precision: int = 0) -> np.ndarray:
@@ -290,6 +319,8 @@ def ref_lib():
             "ref_cull": (c_int, [vp, vp, vp, c_uint32]),
             "ref_sample_irradiance": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int]),
             "ref_ray_dirs": (c_int, [vp, c_int, vp]),
+            "ref_surface_light": (c_int, [vp, vp, vp, c_int, vp, vp, c_int, vp, c_float, c_int, vp]),
+            "ref_inject": (c_int, [vp, vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -343,6 +374,32 @@ def ref_mip(sdf_desc, sdf_float: np.ndarray) -> np.ndarray:
     out = np.zeros(m * C * m * m, dtype=np.float32)
     ref_lib().ref_mip(ctypes.byref(sdf_desc), _p(s), _p(out))
     return out
+
+
+def ref_surface_light(inputs: HostInputs, lights, tiles, masks=None, camera=(0.0, 0.0, 0.0),
+                      shadow_bias: float = 1.0, copy_emissive: bool = True, out=None) -> np.ndarray:
+    """CopyEmissive + SDFDeferredLight through the reference's compiled
+    functions (250-step shadow march), RGBA16F bits."""
+    o = np.array(inputs.host.direct if out is None else out, dtype=np.uint16, copy=True)
+    from luxgi_gb300 import _native as N
+
+    t = np.ascontiguousarray(tiles, dtype=np.uint32)
+    m = None if masks is None else np.ascontiguousarray(masks, dtype=np.uint32)
+    cam = (c_float * 3)(*camera)
+    arr = (N.Light * max(1, len(lights)))(*lights)
+    ref_lib().ref_surface_light(ctypes.byref(inputs.sdf_desc), ctypes.byref(inputs.surface_desc),
+                                ctypes.cast(arr, c_void_p), len(lights), _p(t), _p(m), t.size, cam,
+                                float(shadow_bias), int(copy_emissive), _p(o))
+    return o
+
+
+def ref_inject(vdesc, inputs: HostInputs, irr, dist, base=None) -> np.ndarray:
+    """SDFAtlasIndirectLight through the reference's compiled functions."""
+    o = np.array(inputs.light_cache if base is None else base, dtype=np.uint16, copy=True)
+    i = np.ascontiguousarray(irr, dtype=np.float32)
+    d = np.ascontiguousarray(dist, dtype=np.float32)
+    ref_lib().ref_inject(ctypes.byref(vdesc), ctypes.byref(inputs.surface_desc), _p(i), _p(d), _p(o))
+    return o
 
 
 def ref_cull(surface_desc, capacity: int):

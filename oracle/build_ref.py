@@ -11,13 +11,17 @@ Compiled from the sources where they lie under the reference checkout:
     Code/Maple/src/Shaders/SDF/SDFCommon.glsl (+ ObjectRasterizeData.glsl,
         GlobalSDFData.glsl, GlobalSDFHit.glsl, GlobalSDFTrace.glsl)
     Code/Maple/src/Shaders/SDF/AtlasCommon.glsl
+    Code/Maple/src/Shaders/Raytraced/BRDF.glsl (+ Raytraced/Common.glsl)
+    Code/Maple/src/Shaders/Common/Light.glsl
 The only change made to the text is mechanical: GLSL `out T x` / `inout T x`
 parameters become C++ references `T& x` (everything else -- swizzles,
 built-ins, samplers, `in` -- is supplied by oracle/glsl_compat.h).  The
 rewritten text goes to a temporary directory that is deleted after the
 compile; nothing of the reference source is kept in the repository tree.
 The shader entry points (GISDFRays.comp main, ProbeUpdate.glsl main,
-GlobalSDFMipmap.comp main, SDFCulling.comp main) use Vulkan resource
+GlobalSDFMipmap.comp main, SDFCulling.comp main, SDFDeferredLight.frag
+main and fetchLight, CopyEmissive.frag main, SDFAtlasIndirectLight.frag
+main) use Vulkan resource
 declarations that do not compile as C++, so oracle/ref_harness.cpp restates
 those bodies around the compiled library functions.
 
@@ -38,7 +42,8 @@ OUT = HERE / "_ref"
 LIB = OUT / "libref.so"
 SHADERS = ["DDGI/DDGICommon.glsl", "Common/Math.glsl", "Raytraced/Random.glsl", "SDF/SDFCommon.glsl",
            "SDF/ObjectRasterizeData.glsl", "SDF/GlobalSDFData.glsl", "SDF/GlobalSDFHit.glsl",
-           "SDF/GlobalSDFTrace.glsl", "SDF/AtlasCommon.glsl"]
+           "SDF/GlobalSDFTrace.glsl", "SDF/AtlasCommon.glsl", "Raytraced/Common.glsl", "Raytraced/BRDF.glsl",
+           "Common/Light.glsl"]
 
 
 def reference_root(arg: str | None = None) -> Path:

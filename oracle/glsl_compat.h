@@ -230,6 +230,8 @@ inline float dot(const vec4& a, const vec4& b) {
 inline vec3 cross(const vec3& a, const vec3& b) {
     return vec3(a.e[1] * b.e[2] - a.e[2] * b.e[1], a.e[2] * b.e[0] - a.e[0] * b.e[2], a.e[0] * b.e[1] - a.e[1] * b.e[0]);
 }
+// reflect(I, N) = I - 2 dot(N, I) N
+inline vec3 reflect(const vec3& i, const vec3& n) { return i - (2.0f * dot(n, i)) * n; }
 inline float length(const vec2& v) { return glslc::f_sqrt(dot(v, v)); }
 inline float length(const vec3& v) { return glslc::f_sqrt(dot(v, v)); }
 inline float length(const ivec3& v) { return length(vec3(v)); }

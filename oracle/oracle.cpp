@@ -304,10 +304,13 @@ template <typename R> V3<R> cascade_texture_uv(const luxgi_sdf_data& d, int casc
     return {(R(cascade) + cuv.x) / R(d.cascades_count), cuv.y, cuv.z};
 }
 
-// tracyGlobalSDF (SDFCommon.glsl:98-194); stepScale = 1, start bias 0,
-// needsHitNormal = true, minDistance = 0 as GISDFRays.comp:79-87 sets them.
+// tracyGlobalSDF (SDFCommon.glsl:98-194) with stepScale = 1.  The probe
+// rays use start bias 0 and want the hit normal (GISDFRays.comp:79-87); the
+// surface-cache shadow rays start 2 voxels along and skip the normal
+// (SDFDeferredLight.frag:104-111).
 template <typename R> Hit<R> trace_sdf(const luxgi_sdf_data& d, const Vol& tex, const Vol& mip,
-                                       V3<R> origin, V3<R> dir, R trace_max, int max_steps) {
+                                       V3<R> origin, V3<R> dir, R trace_max, int max_steps,
+                                       R start_bias = R(0), bool want_normal = true) {
     Hit<R> hit;
     const int C = int(d.cascades_count);
     R tmax = std::min(trace_max, R(d.cascade_pos_distance[C - 1][3]) * R(2));
@@ -320,7 +323,7 @@ template <typename R> Hit<R> trace_sdf(const luxgi_sdf_data& d, const Vol& tex, 
         R cw = R(d.cascade_pos_distance[cascade][3]);
         R voxel = R(d.cascade_voxel_size[cascade]);
         R voxel_half = voxel * R(0.5);
-        V3<R> wpos = add(origin, mul(dir, voxel * R(0)));
+        V3<R> wpos = add(origin, mul(dir, voxel * start_bias));
         V2<R> is = line_hit_aabb(wpos, end, v3(cpos.x - cw, cpos.y - cw, cpos.z - cw), v3(cpos.x + cw, cpos.y + cw, cpos.z + cw));
         is.x = is.x * tmax;
         is.y = is.y * tmax;
@@ -347,6 +350,7 @@ template <typename R> Hit<R> trace_sdf(const luxgi_sdf_data& d, const Vol& tex, 
                 hit.time = std::max(t + sd - thick, R(0));
                 hit.cascade = cascade;
                 hit.sdf = sd;
+                if (!want_normal) break;
                 R off = R(1) / R(d.resolution);
                 R xp = sample3d(tex, v3(uv.x + off, uv.y, uv.z));
                 R xn = sample3d(tex, v3(uv.x - off, uv.y, uv.z));
@@ -714,6 +718,170 @@ void mip_pass(const std::vector<float>& src, int src_w, int src_res, int src_off
             }
 }
 
+// ------------------------------------------------ surface-cache raster passes
+// The tile quads of addTiles2 (Engine/DDGI/GlobalSurfaceAtlas.cpp:554-574)
+// cover the pixels [x, x + w] x [y, y + h], (x, y, w, h) = round(extends *
+// res): the TileBuffer extends hold the tile size less one texel of padding
+// (:272-279) while the quad spans the whole tile.  The fragment at pixel
+// (x + i, y + j) has inTileUV = ((i + 0.5) / (w + 1), (j + 0.5) / (h + 1))
+// and samples the surface textures at atlasUV = inTileUV * extends.zw +
+// extends.xy (SDFDeferredLight.frag:82, SDFAtlasIndirectLight.frag:55,
+// CopyEmissive.frag:25) with their default LINEAR + REPEAT sampler
+// (RHI/Definitions.h:152-159).
+struct Footprint {
+    int x0, y0, w, h;   // w, h: pixels of the quad
+};
+inline Footprint footprint(const luxgi_surface_tile& tl, int res) {
+    Footprint f;
+    f.x0 = int(std::lround(tl.extends[0] * float(res)));
+    f.y0 = int(std::lround(tl.extends[1] * float(res)));
+    f.w = int(std::lround(tl.extends[2] * float(res))) + 1;
+    f.h = int(std::lround(tl.extends[3] * float(res))) + 1;
+    return f;
+}
+template <typename R> V2<R> fragment_uv(const luxgi_surface_tile& tl, const Footprint& f, int i, int j) {
+    const R tu = (R(i) + R(0.5)) / R(f.w), tv = (R(j) + R(0.5)) / R(f.h);
+    return {tu * R(tl.extends[2]) + R(tl.extends[0]), tv * R(tl.extends[3]) + R(tl.extends[1])};
+}
+
+// The surface G-buffer at a fragment: albedo, world position and normal
+// (SDFDeferredLight.frag:83-87), metallic and roughness (:120-121; no PBR
+// texture reads as metallic 0, roughness 1).
+template <typename R> struct SurfaceFragment {
+    V3<R> albedo, pos, normal;
+    R metallic, roughness;
+};
+struct SurfaceTextures {
+    Tex2 g0, g1, pbr, emissive;
+    bool has_pbr = false, has_emissive = false;
+    explicit SurfaceTextures(const luxgi_surface_desc* s) {
+        const int res = int(s->data.resolution);
+        g0.f32 = s->gbuffer0; g0.W = res; g0.H = res; g0.C = 4;
+        g1.f32 = s->gbuffer1; g1.W = res; g1.H = res; g1.C = 4;
+        pbr.u8 = s->pbr; pbr.W = res; pbr.H = res; pbr.C = 4;
+        emissive.f16 = s->emissive; emissive.W = res; emissive.H = res; emissive.C = 4;
+        has_pbr = s->pbr != nullptr;
+        has_emissive = s->emissive != nullptr;
+    }
+};
+template <typename R> SurfaceFragment<R> surface_fragment(const SurfaceTextures& T, V2<R> uv) {
+    SurfaceFragment<R> f;
+    f.albedo = {bilinear_repeat(T.g0, uv, 0), bilinear_repeat(T.g0, uv, 1), bilinear_repeat(T.g0, uv, 2)};
+    const R wx = bilinear_repeat(T.g0, uv, 3);
+    const V2<R> oct{bilinear_repeat(T.g1, uv, 0), bilinear_repeat(T.g1, uv, 1)};
+    f.pos = {wx, bilinear_repeat(T.g1, uv, 2), bilinear_repeat(T.g1, uv, 3)};
+    f.normal = oct_decode(oct);                  // octohedralToDirection, Math.glsl:26-32
+    f.metallic = T.has_pbr ? bilinear_repeat(T.pbr, uv, 0) : R(0);
+    f.roughness = T.has_pbr ? bilinear_repeat(T.pbr, uv, 1) : R(1);
+    return f;
+}
+
+inline uint16_t f2h_bits(float v) {
+    _Float16 h = _Float16(v);
+    uint16_t b;
+    std::memcpy(&b, &h, 2);
+    return b;
+}
+
+// Raytraced/BRDF.glsl:14-41 and :65-81 (Cook-Torrance: GGX distribution,
+// Schlick-GGX geometry with k = (r + 1)^2 / 8, Schlick Fresnel).
+template <typename R> R ndf_ggx(R cos_lh, R roughness) {
+    const R alpha = roughness * roughness;
+    const R alpha_sq = alpha * alpha;
+    const R denom = (cos_lh * cos_lh) * (alpha_sq - R(1)) + R(1);
+    return alpha_sq / (pi_r<R>() * denom * denom);
+}
+template <typename R> R ga_schlick_g1(R cos_theta, R k) { return cos_theta / (cos_theta * (R(1) - k) + k); }
+template <typename R> R ga_schlick_ggx(R cos_li, R n_dot_v, R roughness) {
+    const R r = roughness + R(1);
+    const R k = (r * r) / R(8);
+    return ga_schlick_g1(cos_li, k) * ga_schlick_g1(n_dot_v, k);
+}
+template <typename R> V3<R> brdf(V3<R> albedo, V3<R> n, R roughness, R metallic, V3<R> view, V3<R> half_v, V3<R> l) {
+    const V3<R> f0{mixr(R(0.04f), albedo.x, metallic), mixr(R(0.04f), albedo.y, metallic),
+                   mixr(R(0.04f), albedo.z, metallic)};
+    const R cos_li = std::max(R(0), dot(n, l));
+    const R cos_lh = std::max(R(0), dot(n, half_v));
+    const R n_dot_v = std::max(R(0), dot(n, view));
+    const R fw = std::pow(clampr(R(1) - std::max(dot(half_v, view), R(0)), R(0), R(1)), R(5));
+    const V3<R> F{f0.x + (R(1) - f0.x) * fw, f0.y + (R(1) - f0.y) * fw, f0.z + (R(1) - f0.z) * fw};
+    const R D = ndf_ggx(cos_lh, roughness);
+    const R G = ga_schlick_ggx(cos_li, n_dot_v, roughness);
+    const R den = std::max(R(0.00001f), R(4) * cos_li * n_dot_v);
+    const R km = R(1) - metallic;
+    const R Fv[3] = {F.x, F.y, F.z}, av[3] = {albedo.x, albedo.y, albedo.z};
+    R out[3];
+    for (int c = 0; c < 3; ++c) {
+        const R kd = (R(1) - Fv[c]) * km;
+        const R diffuse = kd * av[c] / pi_r<R>();
+        const R specular = (Fv[c] * D * G) / den;
+        out[c] = diffuse + specular;
+    }
+    return {out[0], out[1], out[2]};
+}
+
+// fetchLight (SDFDeferredLight.frag:41-76): direction to the light, trace
+// distance and attenuation.  Types other than directional, spot and point
+// leave the outputs unset in the shader; the entry point rejects them.
+template <typename R> void fetch_light(const luxgi_light& L, V3<R> wp, V3<R>& wi, R& tmax, R& atten) {
+    const R WORLD = R(60000.0f);
+    if (L.type == 0.0f) {
+        wi = {-R(L.direction[0]), -R(L.direction[1]), -R(L.direction[2])};
+        tmax = WORLD;
+        atten = R(1);
+    } else if (L.type == 2.0f) {
+        const V3<R> d = sub(V3<R>{R(L.position[0]), R(L.position[1]), R(L.position[2])}, wp);
+        const R dist = length(d);
+        wi = normalize(d);
+        atten = R(L.radius) / (std::pow(dist, R(2)) + R(1));
+        tmax = dist;
+    } else {
+        const V3<R> lv = sub(V3<R>{R(L.position[0]), R(L.position[1]), R(L.position[2])}, wp);
+        const R cutoff = R(1) - R(L.angle);
+        wi = normalize(lv);
+        const R dist = length(lv);
+        const R theta = dot(wi, V3<R>{R(L.direction[0]), R(L.direction[1]), R(L.direction[2])});
+        const R eps = cutoff - cutoff * R(0.9f);
+        R a = (theta - cutoff) / eps;
+        a = a * (R(L.radius) / (std::pow(dist, R(2)) + R(1)));
+        atten = clampr(a, R(0), R(1));
+        tmax = dist;
+    }
+}
+
+// SDFDeferredLight.frag:79-129 for one fragment and one light: the light's
+// contribution (rgb) to the light cache.  `shadowed` reports the SDF shadow.
+template <typename R> V3<R> direct_light(const luxgi_sdf_desc* sdf, const Vol& tex, const Vol& mip,
+                                         const SurfaceFragment<R>& f, const luxgi_light& L, const float cam[3],
+                                         float shadow_bias, int max_steps, bool* shadowed) {
+    V3<R> wi{R(0), R(0), R(0)};
+    R dist = R(60000.0f), atten = R(1);
+    fetch_light<R>(L, f.pos, wi, dist, atten);
+    R shadow = R(1);
+    const R sb = R(shadow_bias);
+    const R nol = dot(f.normal, wi);
+    const R bias = R(2) * sb * clampr(R(1) - nol, R(0), R(1)) + sb;
+    if (nol > R(0)) {
+        if (atten > R(0)) {
+            const V3<R> origin = add(f.pos, mul(f.normal, sb));
+            const Hit<R> hit = trace_sdf<R>(sdf->data, tex, mip, origin, wi, dist - bias, max_steps, R(2), false);
+            shadow = hit.time >= R(0) ? R(0) : R(1);
+        }
+    } else {
+        shadow = R(0);
+    }
+    *shadowed = shadow == R(0);
+    const V3<R> c{R(cam[0]), R(cam[1]), R(cam[2])};
+    const V3<R> view = normalize(sub(c, f.pos));
+    const R intensity = std::pow(R(L.intensity), R(1.4f)) + R(0.1f);
+    const V3<R> lrad{R(L.color[0]) * intensity, R(L.color[1]) * intensity, R(L.color[2]) * intensity};
+    const V3<R> lh = normalize(add(wi, view));
+    const R cos_li = std::max(R(0), dot(f.normal, wi));
+    const V3<R> b = brdf<R>(f.albedo, f.normal, f.roughness, f.metallic, view, lh, wi);
+    const R s = cos_li * shadow * atten;
+    return {b.x * lrad.x * s, b.y * lrad.y * s, b.z * lrad.z * s};
+}
+
 }  // namespace
 
 // ===================================================================== C API
@@ -913,72 +1081,115 @@ int oracle_cull(const luxgi_surface_desc* s, uint32_t* chunks, uint32_t* culled,
     return used > capacity ? LUXGI_ENOMEM : 0;
 }
 
-// SDFAtlasIndirectLight.frag:44-67 over every texel of every tile rect;
-// light_out RGBA16F [res^2] (starts as a copy of direct_light).
+// SDFAtlasIndirectLight.frag:44-67 over the footprint of every tile;
+// light_out RGBA16F [res^2] holds the light cache on entry (texels outside
+// every footprint keep it).
 int oracle_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* s, const float* irr, const float* dist,
                   int frames, int precision, uint16_t* light_out) {
     const int res = int(s->data.resolution);
-    std::memcpy(light_out, s->direct_light, size_t(res) * res * 4 * sizeof(uint16_t));
-    if (!vd->infinite_bounce || frames == 0) return 0;
+    const bool bounce = vd->infinite_bounce && frames != 0;
     Atlases A;
     const luxgi_ddgi_uniform& u = vd->uniform;
     A.irr.f32 = irr; A.irr.W = u.irradiance_width; A.irr.H = u.irradiance_height; A.irr.C = 4;
     A.dist.f32 = dist; A.dist.W = u.depth_width; A.dist.H = u.depth_height; A.dist.C = 2;
+    const SurfaceTextures T(s);
     for (int t = 1; t < s->num_tiles; ++t) {
         const luxgi_surface_tile& tl = s->tiles[t];
-        int x0 = int(std::lround(tl.extends[0] * res)), y0 = int(std::lround(tl.extends[1] * res));
-        int w = int(std::lround(tl.extends[2] * res)), h = int(std::lround(tl.extends[3] * res));
+        const Footprint fp = footprint(tl, res);
 #pragma omp parallel for
-        for (int j = 0; j < h; ++j)
-            for (int i = 0; i < w; ++i) {
-                size_t ti = size_t(y0 + j) * size_t(res) + size_t(x0 + i);
-                const float* g0 = s->gbuffer0 + ti * 4;
-                const float* g1 = s->gbuffer1 + ti * 4;
-                float add[3];
-                if (precision == 1) {
-                    using R = double;
-                    // octohedralToDirection (Math.glsl:27-33)
-                    V3<R> v{R(g1[0]), R(g1[1]), R(1) - std::fabs(R(g1[0])) - std::fabs(R(g1[1]))};
-                    if (v.z < R(0)) {
-                        R nx = (R(1) - std::fabs(v.y)) * (v.x >= R(0) ? R(1) : R(-1));
-                        R ny = (R(1) - std::fabs(v.x)) * (v.y >= R(0) ? R(1) : R(-1));
-                        v.x = nx; v.y = ny;
-                    }
-                    V3<R> n = normalize(v);
-                    V3<R> wp{R(g0[3]), R(g1[2]), R(g1[3])};
-                    V3<R> cam{R(s->data.camera_pos[0]), R(s->data.camera_pos[1]), R(s->data.camera_pos[2])};
-                    V3<R> wo = normalize(sub(cam, wp));
-                    V3<R> e = sample_irradiance<R>(u, A, wp, n, wo);
-                    for (int k = 0; k < 3; ++k) {
-                        R alb = std::min(R(g0[k]), R(0.9f));
-                        R diff = (alb - alb * R(0)) / pi_r<R>();
-                        add[k] = float(R(vd->intensity) * diff * (k == 0 ? e.x : k == 1 ? e.y : e.z));
-                    }
+        for (int j = 0; j < fp.h; ++j)
+            for (int i = 0; i < fp.w; ++i) {
+                const size_t ti = size_t(fp.y0 + j) * size_t(res) + size_t(fp.x0 + i);
+                float add[3] = {0.0f, 0.0f, 0.0f};
+                if (bounce) {
+                    auto shade = [&](auto zero) {
+                        using R = decltype(zero);
+                        const SurfaceFragment<R> f = surface_fragment<R>(T, fragment_uv<R>(tl, fp, i, j));
+                        const V3<R> cam{R(s->data.camera_pos[0]), R(s->data.camera_pos[1]), R(s->data.camera_pos[2])};
+                        const V3<R> wo = normalize(sub(cam, f.pos));
+                        const V3<R> e = sample_irradiance<R>(u, A, f.pos, f.normal, wo);
+                        const R alb[3] = {std::min(f.albedo.x, R(0.9f)), std::min(f.albedo.y, R(0.9f)),
+                                          std::min(f.albedo.z, R(0.9f))};
+                        const R ev[3] = {e.x, e.y, e.z};
+                        for (int k = 0; k < 3; ++k) {
+                            const R diff = (alb[k] - alb[k] * f.metallic) / pi_r<R>();
+                            add[k] = float(R(vd->intensity) * diff * ev[k]);
+                        }
+                    };
+                    if (precision == 1) shade(0.0);
+                    else shade(0.0f);
+                }
+                for (int k = 0; k < 3; ++k)
+                    light_out[ti * 4 + size_t(k)] = f2h_bits(h2f(s->direct_light[ti * 4 + size_t(k)]) + add[k]);
+                light_out[ti * 4 + 3] = s->direct_light[ti * 4 + 3];
+            }
+    }
+    return 0;
+}
+
+// One surface-lighting pass (the CopyEmissive draw, then one
+// SDFDeferredLight draw per light with additive blending into a 16-bit
+// target, GlobalSurfaceAtlas.cpp:886-996) over tiles[0 .. n): out RGBA16F
+// [res^2] in/out.  masks[k] bit l: light l draws tile k (NULL: all).
+// shadow_out (optional, u32 per texel) collects bit l for each light whose
+// SDF shadow test blocked the fragment.
+int oracle_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s, const luxgi_light* lights,
+                         int num_lights, const uint32_t* tiles, const uint32_t* masks, int num_tiles,
+                         const float cam[3], float shadow_bias, int copy_emissive, int max_steps, int precision,
+                         uint16_t* out, uint32_t* shadow_out) {
+    const int res = int(s->data.resolution), mres = sdf->mip_resolution, C = int(sdf->data.cascades_count);
+    Vol tex, mip;
+    tex.W = sdf->resolution * C; tex.H = sdf->resolution; tex.D = sdf->resolution;
+    mip.W = mres * C; mip.H = mres; mip.D = mres;
+    if (sdf->format == LUXGI_STORAGE_FP16) {
+        tex.f16 = static_cast<const uint16_t*>(sdf->sdf);
+        mip.f16 = static_cast<const uint16_t*>(sdf->mip);
+    } else {
+        tex.f32 = static_cast<const float*>(sdf->sdf);
+        mip.f32 = static_cast<const float*>(sdf->mip);
+    }
+    const SurfaceTextures T(s);
+    for (int k = 0; k < num_tiles; ++k) {
+        const uint32_t t = tiles[k];
+        if (t < 1 || int(t) >= s->num_tiles) return LUXGI_EINVAL;
+        const luxgi_surface_tile& tl = s->tiles[t];
+        const Footprint fp = footprint(tl, res);
+        const uint32_t mask = masks ? masks[k] : (num_lights >= 32 ? 0xFFFFFFFFu : ((1u << num_lights) - 1u));
+#pragma omp parallel for schedule(dynamic)
+        for (int j = 0; j < fp.h; ++j)
+            for (int i = 0; i < fp.w; ++i) {
+                const size_t ti = size_t(fp.y0 + j) * size_t(res) + size_t(fp.x0 + i);
+                float acc[4];
+                if (copy_emissive) {
+                    const V2<float> uv = fragment_uv<float>(tl, fp, i, j);
+                    for (int c = 0; c < 4; ++c)
+                        acc[c] = T.has_emissive ? bilinear_repeat(T.emissive, uv, c) : (c == 3 ? 1.0f : 0.0f);
+                    for (int c = 0; c < 4; ++c) acc[c] = round_half(acc[c]);
                 } else {
-                    using R = float;
-                    V3<R> v{g1[0], g1[1], 1.0f - std::fabs(g1[0]) - std::fabs(g1[1])};
-                    if (v.z < 0.0f) {
-                        R nx = (1.0f - std::fabs(v.y)) * (v.x >= 0.0f ? 1.0f : -1.0f);
-                        R ny = (1.0f - std::fabs(v.x)) * (v.y >= 0.0f ? 1.0f : -1.0f);
-                        v.x = nx; v.y = ny;
-                    }
-                    V3<R> n = normalize(v);
-                    V3<R> wp{g0[3], g1[2], g1[3]};
-                    V3<R> cam{s->data.camera_pos[0], s->data.camera_pos[1], s->data.camera_pos[2]};
-                    V3<R> wo = normalize(sub(cam, wp));
-                    V3<R> e = sample_irradiance<R>(u, A, wp, n, wo);
-                    for (int k = 0; k < 3; ++k) {
-                        R alb = std::min(g0[k], 0.9f);
-                        R diff = (alb - alb * 0.0f) / pi_r<R>();
-                        add[k] = vd->intensity * diff * (k == 0 ? e.x : k == 1 ? e.y : e.z);
-                    }
+                    for (int c = 0; c < 4; ++c) acc[c] = h2f(out[ti * 4 + size_t(c)]);
                 }
-                for (int k = 0; k < 3; ++k) {
-                    float base = h2f(s->direct_light[ti * 4 + size_t(k)]);
-                    float v = base + add[k];
-                    _Float16 hv = _Float16(v);
-                    std::memcpy(&light_out[ti * 4 + size_t(k)], &hv, 2);
+                uint32_t blocked = 0;
+                for (int l = 0; l < num_lights; ++l) {
+                    if (!(mask >> l & 1u)) continue;
+                    float d[3];
+                    bool sh = false;
+                    if (precision == 1) {
+                        const SurfaceFragment<double> f = surface_fragment<double>(T, fragment_uv<double>(tl, fp, i, j));
+                        const V3<double> v = direct_light<double>(sdf, tex, mip, f, lights[l], cam, shadow_bias,
+                                                                  max_steps, &sh);
+                        d[0] = float(v.x); d[1] = float(v.y); d[2] = float(v.z);
+                    } else {
+                        const SurfaceFragment<float> f = surface_fragment<float>(T, fragment_uv<float>(tl, fp, i, j));
+                        const V3<float> v = direct_light<float>(sdf, tex, mip, f, lights[l], cam, shadow_bias,
+                                                                max_steps, &sh);
+                        d[0] = v.x; d[1] = v.y; d[2] = v.z;
+                    }
+                    if (sh) blocked |= 1u << l;
+                    for (int c = 0; c < 3; ++c) acc[c] = round_half(acc[c] + d[c]);
+                    acc[3] = round_half(acc[3] + 1.0f);
                 }
+                for (int c = 0; c < 4; ++c) out[ti * 4 + size_t(c)] = f2h_bits(acc[c]);
+                if (shadow_out) shadow_out[ti] = blocked;
             }
     }
     return 0;

@@ -11,6 +11,11 @@
 //   ref_blend  ProbeUpdate.glsl:182-281
 //   ref_mip    GlobalSDFMipmap.comp:190-226 and GlobalDistanceField.cpp:537-573
 //   ref_cull   SDFCulling.comp:262-327 (deterministic list placement)
+//   ref_surface_light  CopyEmissive.frag:22-26, SDFDeferredLight.frag:41-129
+//                      (BRDF from Raytraced/BRDF.glsl:65-81)
+//   ref_inject SDFAtlasIndirectLight.frag:44-67
+// The two raster passes run over the pixels of the tile quads of addTiles2
+// (Engine/DDGI/GlobalSurfaceAtlas.cpp:554-574).
 // The entry-point bodies are restated because they declare Vulkan
 // resources (images, SSBOs, push constants) that do not compile as C++.
 #include "glsl_compat.h"
@@ -18,6 +23,8 @@
 #include "DDGI/DDGICommon.glsl"
 #include "SDF/SDFCommon.glsl"
 #include "SDF/AtlasCommon.glsl"
+#include "Raytraced/BRDF.glsl"
+#include "Common/Light.glsl"
 
 #include <vector>
 
@@ -28,6 +35,7 @@ static_assert(sizeof(GlobalSDFData) == sizeof(luxgi_sdf_data), "GlobalSDFData la
 static_assert(sizeof(GlobalSurfaceAtlasData) == sizeof(luxgi_surface_data), "GlobalSurfaceAtlasData layout");
 static_assert(sizeof(ObjectBuffer) == sizeof(luxgi_surface_object), "ObjectBuffer layout");
 static_assert(sizeof(TileBuffer) == sizeof(luxgi_surface_tile), "TileBuffer layout");
+static_assert(sizeof(Light) == sizeof(luxgi_light), "Light layout");
 
 namespace {
 
@@ -51,6 +59,59 @@ sampler2D tex2d(const float* f32, const uint16_t* f16, const uint8_t* u8, int W,
     s.W = W; s.H = H; s.C = C;
     s.repeat = repeat;
     return s;
+}
+
+// The pixels a tile quad of addTiles2 covers (Engine/DDGI/
+// GlobalSurfaceAtlas.cpp:554-574): tile->x .. x + width - 1, with
+// extends.z = (width - 1) / resolution (:272-279), and the fragment's
+// interpolated inTileUV at pixel centres.
+struct Quad {
+    int x, y, width, height;
+};
+Quad tile_quad(const TileBuffer& t, int res) {
+    Quad q;
+    q.x = int(__builtin_lroundf(t.extends.x * float(res)));
+    q.y = int(__builtin_lroundf(t.extends.y * float(res)));
+    q.width = int(__builtin_lroundf(t.extends.z * float(res))) + 1;
+    q.height = int(__builtin_lroundf(t.extends.w * float(res))) + 1;
+    return q;
+}
+vec2 tile_uv(const Quad& q, int i, int j) {
+    return vec2((float(i) + 0.5f) / float(q.width), (float(j) + 0.5f) / float(q.height));
+}
+float h16(uint16_t b) { _Float16 h; std::memcpy(&h, &b, 2); return float(h); }
+uint16_t to16(float f) { _Float16 h = _Float16(f); uint16_t b; std::memcpy(&b, &h, 2); return b; }
+
+// fetchLight, SDFDeferredLight.frag:41-76 (a function of the entry-point
+// file, restated here).
+void fetchLight(const Light& light, vec3 worldPos, vec3 normal, vec3& Wi, float& tmax, float& attenuation) {
+    vec3 lightDir = vec3(0, 0, 0);
+    if (light.type == LIGHT_DIRECTIONAL) {
+        lightDir = -vec3(light.direction.xyz);
+        tmax = GLOBAL_SDF_WORLD_SIZE;
+        Wi = lightDir;
+        attenuation = 1.0;
+    } else if (light.type == LIGHT_POINT) {
+        vec3 dir = vec3(light.position.xyz) - worldPos;
+        float dist = length(dir);
+        lightDir = normalize(dir);
+        attenuation = light.radius / (pow(dist, 2.0) + 1.0);
+        Wi = lightDir;
+        tmax = dist;
+    } else if (light.type == LIGHT_SPOT) {
+        vec3 L = vec3(light.position.xyz) - worldPos;
+        float cutoffAngle = 1.0f - light.angle;
+        lightDir = normalize(L);
+        float dist = length(L);
+        float theta = dot(lightDir, vec3(light.direction.xyz));
+        float epsilon = cutoffAngle - cutoffAngle * 0.9f;
+        attenuation = ((theta - cutoffAngle) / epsilon);
+        attenuation *= light.radius / (pow(dist, 2.0) + 1.0);
+        attenuation = clamp(attenuation, 0.0, 1.0);
+        Wi = lightDir;
+        tmax = dist;
+    }
+    (void)normal;
 }
 
 }  // namespace
@@ -291,6 +352,134 @@ int ref_sample_irradiance(const luxgi_ddgi_uniform* u, const float* irr, const f
         out[3 * i] = e.x;
         out[3 * i + 1] = e.y;
         out[3 * i + 2] = e.z;
+    }
+    return 0;
+}
+
+// CopyEmissive.frag main, then SDFDeferredLight.frag main (:79-129) for each
+// light whose bit is set in masks[k] (NULL: all), blended additively into
+// the RGBA16F target `out` (rounded after each draw), over tiles[0 .. n).
+// copy_emissive = 0 skips the CopyEmissive draw.
+int ref_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf, const luxgi_light* lights,
+                      int num_lights, const uint32_t* tile_ids, const uint32_t* masks, int n, const float cam[3],
+                      float shadow_bias, int copy_emissive, uint16_t* out) {
+    const GlobalSDFData sd = as<GlobalSDFData>(sdf->data);
+    const int C = int(sdf->data.cascades_count), res = sdf->resolution, mres = sdf->mip_resolution;
+    const sampler3D tex = volume(sdf->sdf, sdf->format, res * C, res, res);
+    const sampler3D mip = volume(sdf->mip, sdf->format, mres * C, mres, mres);
+    const int A = int(surf->data.resolution);
+    const sampler2D colorS = tex2d(surf->gbuffer0, nullptr, nullptr, A, A, 4, true);
+    const sampler2D normalS = tex2d(surf->gbuffer1, nullptr, nullptr, A, A, 4, true);
+    const sampler2D pbrS = tex2d(nullptr, nullptr, surf->pbr, A, A, 4, true);
+    const sampler2D emissiveS = tex2d(nullptr, surf->emissive, nullptr, A, A, 4, true);
+    const TileBuffer* tiles = reinterpret_cast<const TileBuffer*>(surf->tiles);
+    for (int k = 0; k < n; ++k) {
+        const TileBuffer tile = tiles[tile_ids[k]];
+        const Quad q = tile_quad(tile, A);
+        const uint32_t mask = masks ? masks[k] : 0xFFFFFFFFu;
+#pragma omp parallel for schedule(dynamic)
+        for (int j = 0; j < q.height; ++j)
+            for (int i = 0; i < q.width; ++i) {
+                const size_t ti = size_t(q.y + j) * size_t(A) + size_t(q.x + i);
+                const vec2 inTileUV = tile_uv(q, i, j);
+                const vec2 atlasUV = inTileUV * vec2(tile.extends.zw) + vec2(tile.extends.xy);
+                float dst[4];
+                if (copy_emissive) {
+                    const vec4 e = surf->emissive ? texture(emissiveS, atlasUV) : vec4(0, 0, 0, 1);
+                    dst[0] = h16(to16(e.x)); dst[1] = h16(to16(e.y)); dst[2] = h16(to16(e.z)); dst[3] = h16(to16(e.w));
+                } else {
+                    for (int c = 0; c < 4; ++c) dst[c] = h16(out[ti * 4 + size_t(c)]);
+                }
+                for (int l = 0; l < num_lights; ++l) {
+                    if (!(mask >> l & 1u)) continue;
+                    const Light light = as<Light>(lights[l]);
+                    vec4 albedo = texture(colorS, atlasUV);
+                    vec4 normalTex = texture(normalS, atlasUV);
+                    vec4 pbr = surf->pbr ? texture(pbrS, atlasUV) : vec4(0, 1, 0, 1);
+                    vec3 normal = octohedralToDirection(vec2(normalTex.xy));
+                    vec3 worldPos = vec3(albedo.w, normalTex.z, normalTex.w);
+                    vec3 L = vec3(0);
+                    float dist = GLOBAL_SDF_WORLD_SIZE;
+                    float atten = 1;
+                    fetchLight(light, worldPos, normal, L, dist, atten);
+                    float shadowMask = 1.0;
+                    float NoL = dot(normal, L);
+                    float shadowBias = shadow_bias;
+                    float bias = 2 * shadowBias * clamp(1 - NoL, 0, 1) + shadowBias;
+                    if (NoL > 0) {
+                        if (atten > 0) {
+                            GlobalSDFTrace trace;
+                            trace.worldPosition = worldPos + normal * shadowBias;
+                            trace.worldDirection = L;
+                            trace.minDistance = bias;
+                            trace.maxDistance = dist - bias;
+                            trace.stepScale = 1;
+                            trace.needsHitNormal = false;
+                            GlobalSDFHit hit = tracyGlobalSDF(sd, tex, mip, trace, 2);
+                            shadowMask = isHit(hit) ? 0.0 : 1;
+                        }
+                    } else {
+                        shadowMask = 0;
+                    }
+                    float metallic = pbr.r;
+                    float roughness = pbr.g;
+                    vec3 view = normalize(vec3(cam[0], cam[1], cam[2]) - worldPos);
+                    float intensity = pow(light.intensity, 1.4) + 0.1;
+                    vec3 Lradiance = vec3(light.color.xyz) * intensity;
+                    vec3 Lh = normalize(L + view);
+                    float cosLi = max(0.0, dot(normal, L));
+                    vec3 directShading = BRDF(vec3(albedo.rgb), normal, roughness, metallic, view, Lh, L) * Lradiance *
+                                         cosLi * shadowMask * atten;
+                    dst[0] = h16(to16(dst[0] + directShading.x));
+                    dst[1] = h16(to16(dst[1] + directShading.y));
+                    dst[2] = h16(to16(dst[2] + directShading.z));
+                    dst[3] = h16(to16(dst[3] + 1.0f));
+                }
+                for (int c = 0; c < 4; ++c) out[ti * 4 + size_t(c)] = to16(dst[c]);
+            }
+    }
+    return 0;
+}
+
+// SDFAtlasIndirectLight.frag main (:51-67, indirectLighting :44-48) over
+// every tile's quad: out = direct_light + the fragment's indirect light,
+// rounded to FP16 (texels outside the quads are left as they are).
+int ref_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* surf, const float* irr, const float* dist,
+               uint16_t* out) {
+    const DDGIUniform ddgi = as<DDGIUniform>(vd->uniform);
+    const int A = int(surf->data.resolution);
+    const sampler2D colorS = tex2d(surf->gbuffer0, nullptr, nullptr, A, A, 4, true);
+    const sampler2D normalS = tex2d(surf->gbuffer1, nullptr, nullptr, A, A, 4, true);
+    const sampler2D pbrS = tex2d(nullptr, nullptr, surf->pbr, A, A, 4, true);
+    const sampler2D irrS = tex2d(irr, nullptr, nullptr, ddgi.irradianceTextureWidth, ddgi.irradianceTextureHeight, 4, true);
+    const sampler2D distS = tex2d(dist, nullptr, nullptr, ddgi.depthTextureWidth, ddgi.depthTextureHeight, 2, true);
+    const TileBuffer* tiles = reinterpret_cast<const TileBuffer*>(surf->tiles);
+    const vec3 cam(surf->data.camera_pos[0], surf->data.camera_pos[1], surf->data.camera_pos[2]);
+    for (int t = 1; t < surf->num_tiles; ++t) {
+        const TileBuffer tile = tiles[t];
+        const Quad q = tile_quad(tile, A);
+#pragma omp parallel for
+        for (int j = 0; j < q.height; ++j)
+            for (int i = 0; i < q.width; ++i) {
+                const size_t ti = size_t(q.y + j) * size_t(A) + size_t(q.x + i);
+                const vec2 atlasUV = tile_uv(q, i, j) * vec2(tile.extends.zw) + vec2(tile.extends.xy);
+                SurfaceMaterial p;
+                vec4 albedo = texture(colorS, atlasUV);
+                vec4 normalTex = texture(normalS, atlasUV);
+                vec4 pbr = surf->pbr ? texture(pbrS, atlasUV) : vec4(0, 1, 0, 1);
+                p.normal = octohedralToDirection(vec2(normalTex.xy));
+                p.albedo = vec4(min(vec3(albedo.xyz), 0.9), 1);
+                p.metallic = pbr.r;
+                p.roughness = pbr.g;
+                vec3 worldPos = vec3(albedo.w, normalTex.z, normalTex.w);
+                const vec3 Wo = normalize(cam - worldPos);
+                vec3 diffuseColor = (vec3(p.albedo.rgb) - vec3(p.albedo.rgb) * p.metallic) / PI;
+                vec3 e = vd->intensity * diffuseColor * sampleIrradiance(ddgi, worldPos, p.normal, Wo, irrS, distS);
+                out[ti * 4 + 0] = to16(h16(surf->direct_light[ti * 4 + 0]) + e.x);
+                out[ti * 4 + 1] = to16(h16(surf->direct_light[ti * 4 + 1]) + e.y);
+                out[ti * 4 + 2] = to16(h16(surf->direct_light[ti * 4 + 2]) + e.z);
+                out[ti * 4 + 3] = surf->direct_light[ti * 4 + 3];
+            }
     }
     return 0;
 }

@@ -149,3 +149,56 @@ def test_sample_irradiance_matches_reference(ref):
     a = oracle.ref_sample_irradiance(u, irr, dist, pos, nrm, wo)
     b = oracle.sample_irradiance(u, irr, dist, pos, nrm, wo, precision=0)
     assert rel_err(a, b, floor=1e-2) < 1e-4
+
+
+def _f16(bits) -> np.ndarray:
+    return np.asarray(bits, dtype=np.uint16).view(np.float16).astype(np.float32)
+
+
+def _test_lights():
+    from luxgi_gb300.surface import make_light
+
+    L = [None] * 3
+    L[0] = make_light(N.LIGHT_DIRECTIONAL, (1.0, 0.95, 0.9), 2.0, direction=(0.3, -0.8, 0.5))
+    L[1] = make_light(N.LIGHT_POINT, (0.4, 0.6, 1.0), 3.0, position=(1.0, 2.0, -0.5), radius=6.0)
+    L[2] = make_light(N.LIGHT_SPOT, (1.0, 0.5, 0.2), 4.0, position=(-2.0, 3.0, 1.0), direction=(0.5, -1.0, -0.2),
+                      radius=8.0, angle=0.3)
+    return L
+
+
+@pytest.mark.parametrize("fmt,copy_emissive", [(N.STORAGE_FP32, True), (N.STORAGE_FP16, False)])
+def test_surface_light_matches_reference(ref, fmt, copy_emissive):
+    """CopyEmissive + SDFDeferredLight (three lights, random per-tile light
+    masks) against the reference's compiled BRDF, Light and tracyGlobalSDF:
+    each light's draw rounds the FP16 target once, so the two agree within
+    one rounding step per light (1e-3 relative), and no fragment's shadow
+    test differs (a flip would change its value by far more)."""
+    w = tiny_workload(sdf=32, prims=8, atlas=256, sdf_format=fmt)
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    L = _test_lights()
+    tiles = np.arange(1, host.num_tiles, dtype=np.uint32)
+    masks = np.random.default_rng(3).integers(0, 8, size=tiles.size).astype(np.uint32)
+    cam = (0.3, 0.5, -2.0)
+    a, shadow = oracle.surface_light(inp, L, tiles, masks, cam, 1.0, copy_emissive, 250, 0, want_shadow=True)
+    b = oracle.ref_surface_light(inp, L, tiles, masks, cam, 1.0, copy_emissive)
+    assert np.count_nonzero(shadow) > 1000                  # shadows are exercised
+    assert np.count_nonzero(a != host.direct) > 10000       # and the pass wrote the footprints
+    assert np.isfinite(_f16(a)).all()
+    assert rel_err(_f16(a), _f16(b)) < 3e-3
+    assert np.mean(np.abs(_f16(a) - _f16(b)) > 1e-3 * np.maximum(np.abs(_f16(b)), 1e-3)) < 1e-4
+
+
+def test_inject_matches_reference(ref):
+    """SDFAtlasIndirectLight over the tile quads against the reference's
+    compiled sampleIrradiance (metallic from the PBR atlas)."""
+    w = tiny_workload(light=N.LIGHT_CACHE, prims=8)
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    vd = w.volume.desc()
+    rots = [frame_rotation(45, f) for f in range(2)]
+    irr, dist, frames, _ = oracle.run_frames(vd, inp, rots, precision=0)
+    a = oracle.inject(vd, inp, irr, dist, frames, precision=0)
+    b = oracle.ref_inject(vd, inp, irr, dist)
+    assert np.count_nonzero(a != host.direct) > 10000
+    assert rel_err(_f16(a), _f16(b)) < 2e-3
