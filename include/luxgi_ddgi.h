@@ -367,6 +367,12 @@ int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* vol, luxgi_ddgi_rays* out);
 int luxgi_ddgi_check_status(luxgi_ddgi_volume* vol, void* stream);
 /* Record per-ray march steps / hit cascade on the next traces (test aid). */
 int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* vol, int enable);
+/* Copy the current atlases (the copy the next frame reads) to host buffers
+ * of the volume's storage type and report the frame counter; waits for the
+ * copies.  With luxgi_ddgi_load_atlases this checkpoints a volume: frames
+ * run after a load equal the frames the saved volume would have run. */
+int luxgi_ddgi_save_atlases(const luxgi_ddgi_volume* vol, void* irradiance_host, void* distance_host,
+                            int32_t* frames, void* stream);
 /* Overwrite both atlas copies from host buffers of the volume's storage type
  * and set the frame counter (atlas persistence / restore). */
 int luxgi_ddgi_load_atlases(luxgi_ddgi_volume* vol, const void* irradiance_host,
@@ -412,6 +418,113 @@ int luxgi_sdf_build_mip(const luxgi_sdf_desc* sdf, void* mip, void* tmp, void* s
  * streams) race; every scratch texel is written before it is read, so no
  * state carries over between calls.  Allocates nothing. */
 int luxgi_sdf_build_mip_noalloc(const luxgi_sdf_desc* sdf, void* mip, void* stream);
+
+/* ------------------------------------------- global SDF from objects */
+
+/* A baked mesh SDF: the MeshDistanceField component (Engine/DDGI/
+ * MeshDistanceField.h:15-26) and its FP16 volume with up to 3 mips
+ * (SDFBaker.cpp:96-205).  Texel (x, y, z) of mip m sits at
+ * x + y*w + z*w*h, (w, h, d) = max(size >> m, 1) per axis; a texel holds
+ * (distance / max_distance + 1) / 2. */
+typedef struct luxgi_mesh_sdf {
+    float           aabb_min[3];        /* padded local bounds (paddingSDFBox)  */
+    float           aabb_max[3];
+    float           local_to_uvw_add[3];/* -min / size                          */
+    float           local_to_uvw_mul[3];/* 1 / size                             */
+    float           max_distance;       /* max3(size)                           */
+    int32_t         size[3];            /* mip-0 texels                         */
+    int32_t         mip_count;          /* 1 .. 3                               */
+    int32_t         reserved;
+    const uint16_t* mips[3];            /* device FP16 volumes                  */
+} luxgi_mesh_sdf;
+
+/* One placed object: an entity with MeshRenderer, Transform and
+ * MeshDistanceField (GlobalDistanceField.cpp:672-693). */
+typedef struct luxgi_sdf_object {
+    float   world[16];                  /* Transform::getWorldMatrix, column-major */
+    int32_t mesh;                       /* index into the mesh array            */
+    int32_t reserved[3];
+} luxgi_sdf_object;
+
+/* The global SDF's parameters (GlobalDistanceFieldPublic and
+ * GlobalDistanceField, GlobalDistanceField.h:29-45 and :590-604). */
+typedef struct luxgi_sdf_build_desc {
+    float   gi_distance;                /* giDistance, 4000 in the reference    */
+    float   global_scale;               /* gloalScale, 0.1                      */
+    float   min_object_radius;          /* minObjectRadius, 10 (times the scale) */
+    int32_t resolution;                 /* voxels per cascade side, 192 (Quality::Test) */
+    int32_t cascades;                   /* 1 .. 4, 2 (Quality::Test)            */
+    int32_t format;                     /* luxgi_storage of the SDF and mip: FP16 is
+                                           the reference's R16F                 */
+    float   near_plane, far_plane;      /* copied into luxgi_sdf_data           */
+} luxgi_sdf_build_desc;
+
+/* ObjectRasterizeData (ObjectRasterizeData.glsl:8-18), 176 bytes: one per
+ * object a cascade rasterises, in object order. */
+typedef struct luxgi_sdf_raster_object {
+    float   world_to_volume[16];
+    float   volume_to_world[16];
+    float   volume_to_uvw_mul[3];
+    float   mip_offset;                 /* min(cascade, 2)                      */
+    float   volume_to_uvw_add[3];
+    float   decode_mul;                 /* max_distance                         */
+    float   volume_local_bounds_extent[3];
+    float   decode_add;                 /* -max_distance                        */
+} luxgi_sdf_raster_object;
+
+#define LUXGI_SDF_CHUNK 32              /* CONSTS_SDF_RASTERIZE_CHUNK_SIZE      */
+#define LUXGI_SDF_CHUNK_MODELS 28       /* CONSTS_SDF_RASTERIZE_MODEL_MAX_COUNT */
+
+/* A rasterised chunk: 32^3 voxels from coord * 32 of its cascade, the
+ * objects (indices into the cascade's raster objects) it lists. */
+typedef struct luxgi_sdf_chunk {
+    int32_t  coord[3];
+    int32_t  count;
+    uint32_t models[LUXGI_SDF_CHUNK_MODELS];
+} luxgi_sdf_chunk;
+
+/* Host only: the cascade layout (centres, half extents, voxel sizes) of
+ * GlobalDistanceField.cpp:590-626 and :837-841 into `out`. */
+int luxgi_sdf_cascade_layout(const luxgi_sdf_build_desc* desc, luxgi_sdf_data* out);
+
+/* Host only: the objects and chunks cascade `cascade` rasterises
+ * (GlobalDistanceField.cpp:465-535, 672-700): objects whose bounding sphere
+ * meets the cascade and is at least min_object_radius, each with the chunks
+ * its margin-grown bounds cover, at most 28 per chunk as the reference's
+ * chunk table keeps them.  `meshes` may carry null volume pointers.
+ * Writes up to the capacities and returns the counts in *num_objects_out /
+ * *num_chunks_out (LUXGI_ENOMEM when a capacity is short). */
+int luxgi_sdf_build_plan(const luxgi_sdf_build_desc* desc, const luxgi_mesh_sdf* meshes, int num_meshes,
+                         const luxgi_sdf_object* objects, int num_objects, int cascade,
+                         luxgi_sdf_raster_object* raster_out, int raster_capacity, int* num_objects_out,
+                         int32_t* object_mesh_out, luxgi_sdf_chunk* chunks_out, int chunk_capacity,
+                         int* num_chunks_out);
+
+/* The global SDF from objects (merge_sdf::system, GlobalDistanceField.cpp:
+ * 576-842, first build): every voxel of every cascade set to 1, then per
+ * cascade its chunks rasterised (SDFRasterizeModel.glsl: the minimum over
+ * the chunk's objects of distanceToModelSDF, SDFCommon.glsl:38-62, stored
+ * as clamp(d / (2 extent), -1, 1)) and its mip built (luxgi_sdf_build_mip's
+ * passes; the flood passes only when the cascade has chunks).  sdf: device
+ * (res*C) x res x res, mip (mres*C) x mres x mres, mres = res/4, tmp mres^3
+ * elements, all of desc->format.  `data_out` gets the cascade layout.  A
+ * chunk lying partly outside its cascade writes the voxels that fall inside
+ * the packed texture, as the reference's image stores do. */
+int luxgi_sdf_build(const luxgi_sdf_build_desc* desc, const luxgi_mesh_sdf* meshes, int num_meshes,
+                    const luxgi_sdf_object* objects, int num_objects, void* sdf, void* mip, void* tmp,
+                    luxgi_sdf_data* data_out, void* stream);
+
+/* Host only: the layout of a baked .sdf file (SDFBaker.cpp:158-205, cereal
+ * binary: uvec3 size, int32 mip count, then per mip a u64 byte count and the
+ * FP16 texels).  Fills size, mip_count and, per mip, the byte offset of its
+ * texels in `bytes` and their count; checks every length against n. */
+typedef struct luxgi_mesh_sdf_file {
+    int32_t  size[3];
+    int32_t  mip_count;
+    uint64_t mip_offset[3];
+    uint64_t mip_bytes[3];
+} luxgi_mesh_sdf_file;
+int luxgi_mesh_sdf_parse(const void* bytes, uint64_t n, luxgi_mesh_sdf_file* out);
 
 /* SDFCulling.comp: chunk table (40^3 u32, device) and culled-object lists
  * (device, `capacity` u32) for the objects of `surface`.  Layout is

@@ -89,6 +89,41 @@ class SurfaceLighting(ctypes.Structure):
                 ("copy_emissive", c_int32), ("max_steps", c_int32), ("reserved", c_int32 * 2)]
 
 
+class MeshSdf(ctypes.Structure):
+    _fields_ = [("aabb_min", c_float * 3), ("aabb_max", c_float * 3), ("local_to_uvw_add", c_float * 3),
+                ("local_to_uvw_mul", c_float * 3), ("max_distance", c_float), ("size", c_int32 * 3),
+                ("mip_count", c_int32), ("reserved", c_int32), ("mips", c_void_p * 3)]
+
+
+class SdfObject(ctypes.Structure):
+    _fields_ = [("world", c_float * 16), ("mesh", c_int32), ("reserved", c_int32 * 3)]
+
+
+class SdfBuildDesc(ctypes.Structure):
+    _fields_ = [("gi_distance", c_float), ("global_scale", c_float), ("min_object_radius", c_float),
+                ("resolution", c_int32), ("cascades", c_int32), ("format", c_int32), ("near_plane", c_float),
+                ("far_plane", c_float)]
+
+
+class SdfRasterObject(ctypes.Structure):
+    _fields_ = [("world_to_volume", c_float * 16), ("volume_to_world", c_float * 16), ("volume_to_uvw_mul", c_float * 3),
+                ("mip_offset", c_float), ("volume_to_uvw_add", c_float * 3), ("decode_mul", c_float),
+                ("volume_local_bounds_extent", c_float * 3), ("decode_add", c_float)]
+
+
+SDF_CHUNK = 32
+SDF_CHUNK_MODELS = 28
+
+
+class SdfChunk(ctypes.Structure):
+    _fields_ = [("coord", c_int32 * 3), ("count", c_int32), ("models", c_uint32 * SDF_CHUNK_MODELS)]
+
+
+class MeshSdfFile(ctypes.Structure):
+    _fields_ = [("size", c_int32 * 3), ("mip_count", c_int32), ("mip_offset", ctypes.c_uint64 * 3),
+                ("mip_bytes", ctypes.c_uint64 * 3)]
+
+
 class VolumeDesc(ctypes.Structure):
     _fields_ = [("uniform", DDGIUniform), ("storage", c_int32), ("light_mode", c_int32), ("blend", c_int32),
                 ("max_steps", c_int32), ("infinite_bounce", c_int32), ("intensity", c_float),
@@ -163,6 +198,10 @@ assert ctypes.sizeof(SurfaceData) == 32
 assert ctypes.sizeof(SurfaceObject) == 128
 assert ctypes.sizeof(SurfaceTile) == 96
 assert ctypes.sizeof(Light) == 64
+assert ctypes.sizeof(MeshSdf) == 96
+assert ctypes.sizeof(SdfObject) == 80
+assert ctypes.sizeof(SdfRasterObject) == 176
+assert ctypes.sizeof(SdfChunk) == 128
 assert ctypes.sizeof(SurfaceLighting) == 64
 
 # (name, restype, argtypes) of every exported entry point, as declared in
@@ -194,12 +233,19 @@ DDGI_API = [
     ("luxgi_ddgi_set_debug_rays", c_int, [c_void_p, c_int]),
     ("luxgi_ddgi_load_atlases", c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     ("luxgi_ddgi_inject_indirect", c_int, [c_void_p, c_void_p]),
+    ("luxgi_ddgi_save_atlases", c_int, [c_void_p, c_void_p, c_void_p, POINTER(c_int32), c_void_p]),
     ("luxgi_ddgi_sample_irradiance", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("luxgi_sdf_build_mip", c_int, [POINTER(SdfDesc), c_void_p, c_void_p, c_void_p]),
     ("luxgi_sdf_build_mip_noalloc", c_int, [POINTER(SdfDesc), c_void_p, c_void_p]),
     ("luxgi_surface_cull", c_int, [POINTER(SurfaceDesc), c_void_p, c_void_p, c_uint32, c_void_p]),
     ("luxgi_surface_light", c_int, [POINTER(SdfDesc), POINTER(SurfaceDesc), POINTER(SurfaceLighting), c_void_p,
                                     c_void_p]),
+    ("luxgi_sdf_cascade_layout", c_int, [POINTER(SdfBuildDesc), POINTER(SdfData)]),
+    ("luxgi_sdf_build_plan", c_int, [POINTER(SdfBuildDesc), c_void_p, c_int, c_void_p, c_int, c_int, c_void_p, c_int,
+                                     POINTER(c_int), c_void_p, c_void_p, c_int, POINTER(c_int)]),
+    ("luxgi_sdf_build", c_int, [POINTER(SdfBuildDesc), c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                POINTER(SdfData), c_void_p]),
+    ("luxgi_mesh_sdf_parse", c_int, [c_void_p, ctypes.c_uint64, POINTER(MeshSdfFile)]),
     ("luxgi_strerror", ctypes.c_char_p, [c_int]),
     ("luxgi_launch_count", c_uint64, []),
 ]

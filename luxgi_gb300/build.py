@@ -24,12 +24,12 @@ OBJ = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose FP32 arithmetic must match the CPU restatement bit
 # for bit are built without FMA contraction
-NO_FMAD = {"trace.cu", "setup.cu", "surface.cu"}
+NO_FMAD = {"trace.cu", "setup.cu", "surface.cu", "sdfbuild.cu"}
 # shading is compared with the restatement by tolerance: approximate
 # division and square root
 FAST_DIV = {"shade.cu"}
-CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "surface.cu", "capi.cu", "batch.cu",
-                "server.cu"]
+CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "surface.cu", "sdfbuild.cu", "capi.cu",
+                "batch.cu", "server.cu"]
 
 
 def nvcc() -> str:
@@ -71,7 +71,9 @@ def build_cuda(verbose: bool = False) -> Path:
             cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE),
                    "-I", str(CSRC), "-c", str(s), "-o", str(o)]
             if src in NO_FMAD:
-                cmd.insert(1, "-fmad=false")
+                # device code without FMA contraction, and the host code too
+                # (gcc contracts by default on aarch64)
+                cmd[1:1] = ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
             if src in FAST_DIV:
                 cmd[1:1] = ["-prec-div=false", "-prec-sqrt=false"]
             if verbose:

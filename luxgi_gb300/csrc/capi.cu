@@ -743,6 +743,17 @@ int luxgi_ddgi_load_atlases(luxgi_ddgi_volume* v, const void* irr, const void* d
     return LUXGI_OK;
 }
 
+int luxgi_ddgi_save_atlases(const luxgi_ddgi_volume* v, void* irr, void* dist, int32_t* frames, void* stream) {
+    if (!v || !irr || !dist) return LUXGI_EINVAL;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(irr, v->irr[v->ping_pong], v->irr_bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dist, v->dist[v->ping_pong], v->dist_bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (frames) *frames = v->frames;
+    return LUXGI_OK;
+}
+
 int luxgi_ddgi_inject_indirect(luxgi_ddgi_volume* v, void* stream) {
     if (!v) return LUXGI_EINVAL;
     if (!v->bound) return LUXGI_ENOTBOUND;

@@ -201,6 +201,7 @@ cudaError_t launch_surface_light(const SdfView& sdf, const luxgi_surface_desc& s
 cudaError_t launch_sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, const float* pos,
                                      const float* nrm, const float* wo, float* out, int n, cudaStream_t st);
 cudaError_t launch_mip(const luxgi_sdf_desc& s, void* mip, void* tmp, cudaStream_t st);
+cudaError_t launch_mip_cascade(const luxgi_sdf_desc& s, int k, bool flood, void* mip, void* tmp, cudaStream_t st);
 cudaError_t launch_cull(const luxgi_surface_data& d, const luxgi_surface_object* objects, uint32_t* chunks,
                         uint32_t* culled, uint32_t capacity, uint32_t* d_counts, uint32_t* d_status,
                         cudaStream_t st);

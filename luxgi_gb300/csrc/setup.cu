@@ -48,22 +48,39 @@ __global__ void mip_kernel(const T* __restrict__ src, int src_w, int src_res, in
     stv(dst, size_t(x + dst_off_x) + size_t(dst_w) * (size_t(y) + size_t(mres) * z), m);
 }
 
+// Cascade k's mip: the downsampling pass, then (flood) the four flood passes
+// through tmp (GlobalDistanceField.cpp:537-573, 821-835).
 template <typename T>
-static cudaError_t mip_t(const luxgi_sdf_desc& s, T* mip, T* tmp, cudaStream_t st) {
+static cudaError_t mip_cascade_t(const luxgi_sdf_desc& s, int k, bool flood, T* mip, T* tmp, cudaStream_t st) {
     const int res = s.resolution, mres = s.mip_resolution, C = int(s.data.cascades_count);
     const T* sdf = static_cast<const T*>(s.sdf);
     dim3 blk(8, 8, 4);
     dim3 grd((mres + 7) / 8, (mres + 7) / 8, (mres + 3) / 4);
-    for (int k = 0; k < C; ++k) {
-        const float maxd = s.data.cascade_pos_distance[k][3] * 2.0f;
-        mip_kernel<T><<<grd, blk, 0, st>>>(sdf, res * C, res, k * res, mip, mres * C, k * mres, mres, 4, maxd);
-        for (int i = 1; i < 5; ++i) {
-            if (i & 1) mip_kernel<T><<<grd, blk, 0, st>>>(mip, mres * C, mres, k * mres, tmp, mres, 0, mres, 1, maxd);
-            else mip_kernel<T><<<grd, blk, 0, st>>>(tmp, mres, mres, 0, mip, mres * C, k * mres, mres, 1, maxd);
-        }
-        note_launch(5);
+    const float maxd = s.data.cascade_pos_distance[k][3] * 2.0f;
+    mip_kernel<T><<<grd, blk, 0, st>>>(sdf, res * C, res, k * res, mip, mres * C, k * mres, mres, 4, maxd);
+    note_launch();
+    if (!flood) return cudaGetLastError();
+    for (int i = 1; i < 5; ++i) {
+        if (i & 1) mip_kernel<T><<<grd, blk, 0, st>>>(mip, mres * C, mres, k * mres, tmp, mres, 0, mres, 1, maxd);
+        else mip_kernel<T><<<grd, blk, 0, st>>>(tmp, mres, mres, 0, mip, mres * C, k * mres, mres, 1, maxd);
     }
+    note_launch(4);
     return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t mip_t(const luxgi_sdf_desc& s, T* mip, T* tmp, cudaStream_t st) {
+    for (int k = 0; k < int(s.data.cascades_count); ++k) {
+        const cudaError_t e = mip_cascade_t<T>(s, k, true, mip, tmp, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_mip_cascade(const luxgi_sdf_desc& s, int k, bool flood, void* mip, void* tmp, cudaStream_t st) {
+    if (s.format == LUXGI_STORAGE_FP16)
+        return mip_cascade_t<__half>(s, k, flood, static_cast<__half*>(mip), static_cast<__half*>(tmp), st);
+    return mip_cascade_t<float>(s, k, flood, static_cast<float*>(mip), static_cast<float*>(tmp), st);
 }
 
 cudaError_t launch_mip(const luxgi_sdf_desc& s, void* mip, void* tmp, cudaStream_t st) {

@@ -49,6 +49,9 @@ def _stream(stream):
     return stream.cuda_stream
 
 
+STATE_FORMAT = 1   # probe-state checkpoint files (DDGIVolume.save_state)
+
+
 def frame_rotation(seed: int, frame: int) -> np.ndarray:
     """Seeded stand-in for the reference's std::random_device rotation
     (DDGIRenderer.cpp:267-272): column-major 3x3."""
@@ -147,6 +150,35 @@ class DDGIVolume:
         dist = np.ascontiguousarray(distance)
         N.check(N.ddgi().luxgi_ddgi_load_atlases(self._h, irr.ctypes.data, dist.ctypes.data, frames, _stream(stream)),
                 "load_atlases")
+
+    def save_atlases(self, stream=None):
+        """(irradiance, distance, frames): host copies of the current atlases."""
+        a = self.atlas_info()
+        dt = np.float16 if a.storage == N.STORAGE_FP16 else np.float32
+        irr = np.empty((a.irradiance_height, a.irradiance_width, 4), dtype=dt)
+        dist = np.empty((a.depth_height, a.depth_width, 2), dtype=dt)
+        frames = ctypes.c_int32()
+        N.check(N.ddgi().luxgi_ddgi_save_atlases(self._h, irr.ctypes.data, dist.ctypes.data, ctypes.byref(frames),
+                                                 _stream(stream)), "save_atlases")
+        return irr, dist, int(frames.value)
+
+    def save_state(self, path, stream=None) -> None:
+        """A checkpoint file of the volume's probe state: the DDGIUniform,
+        storage and frame counter with both atlases (numpy .npz)."""
+        irr, dist, frames = self.save_atlases(stream)
+        np.savez(path, format=np.array([STATE_FORMAT], np.int32), uniform=np.frombuffer(bytes(self.uniform), np.uint8),
+                 storage=np.array([self.desc.storage], np.int32), frames=np.array([frames], np.int32),
+                 irradiance=irr, distance=dist)
+
+    def load_state(self, path, stream=None) -> None:
+        """Restores a checkpoint written by save_state for a volume of the
+        same layout (DDGIUniform and storage); raises ValueError otherwise."""
+        with np.load(path) as z:
+            if int(z["format"][0]) != STATE_FORMAT:
+                raise ValueError("not a probe-state checkpoint of this format")
+            if bytes(z["uniform"]) != bytes(self.uniform) or int(z["storage"][0]) != self.desc.storage:
+                raise ValueError("checkpoint of a volume with another layout")
+            self.load_atlases(z["irradiance"], z["distance"], int(z["frames"][0]), stream)
 
     def sample_irradiance(self, pos, nrm, wo, out, stream=None) -> None:
         n = pos.shape[0]

@@ -64,6 +64,8 @@ def lib() -> ctypes.CDLL:
             "oracle_sample_irradiance": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int, c_int]),
             "oracle_surface_light": (c_int, [vp, vp, vp, c_int, vp, vp, c_int, vp, c_float, c_int, c_int, c_int,
                                              vp, vp]),
+            "oracle_sdf_build": (c_int, [vp, vp, c_int, vp, c_int, vp, vp, vp]),
+            "oracle_sdf_plan": (c_int, [vp, vp, c_int, vp, c_int, c_int, vp, c_int, vp, vp, vp, c_int, vp]),
             "oracle_texel_dirs": (c_int, [c_int, c_int, vp]),
             "oracle_oct_encode": (c_int, [vp, c_int, vp]),
         }
@@ -260,6 +262,55 @@ def surface_light(inputs: HostInputs, lights, tiles, masks=None, camera=(0.0, 0.
     return (o, sh) if want_shadow else o
 
 
+def _mesh_descs(meshes):
+    """luxgi_mesh_sdf records pointing at the meshes' host volumes."""
+    from luxgi_gb300 import _native as N
+
+    keep = [[np.ascontiguousarray(v, dtype=np.uint16) for v in m.mips] for m in meshes]
+    descs = [m.desc([v.ctypes.data for v in vols]) for m, vols in zip(meshes, keep)]
+    return (N.MeshSdf * max(1, len(descs)))(*descs), keep
+
+
+def sdf_build(desc, meshes, objects):
+    """The global SDF from objects on the CPU: (sdf float [(res*C)*res*res],
+    mip float, luxgi_sdf_data).  meshes: luxgi_gb300.sdf.MeshSDF; objects:
+    (world[16], mesh) pairs."""
+    from luxgi_gb300 import _native as N
+    from luxgi_gb300.sdf import objects_array
+
+    res, C = desc.resolution, desc.cascades
+    m = res // 4
+    sdf = np.zeros(res * C * res * res, dtype=np.float32)
+    mip = np.zeros(m * C * m * m, dtype=np.float32)
+    md, keep = _mesh_descs(meshes)
+    ob = objects_array(objects)
+    data = N.SdfData()
+    st = lib().oracle_sdf_build(ctypes.byref(desc), md, len(meshes), ob, len(objects), _p(sdf), _p(mip),
+                                ctypes.byref(data))
+    if st != 0:
+        raise RuntimeError(f"oracle_sdf_build status {st}")
+    return sdf, mip, data
+
+
+def sdf_plan(desc, meshes, objects, cascade: int):
+    """(raster records, their meshes, chunks) of one cascade on the CPU."""
+    from luxgi_gb300 import _native as N
+    from luxgi_gb300.sdf import objects_array
+
+    md, keep = _mesh_descs(meshes)
+    ob = objects_array(objects)
+    cap = 4096 + 64 * len(objects)
+    recs = (N.SdfRasterObject * max(1, len(objects)))()
+    mesh = (ctypes.c_int32 * max(1, len(objects)))()
+    chunks = (N.SdfChunk * cap)()
+    nr, nc = ctypes.c_int(), ctypes.c_int()
+    st = lib().oracle_sdf_plan(ctypes.byref(desc), md, len(meshes), ob, len(objects), cascade, recs, len(objects),
+                               ctypes.byref(nr), mesh, chunks, cap, ctypes.byref(nc))
+    if st != 0:
+        raise RuntimeError(f"oracle_sdf_plan status {st}")
+    return recs[:nr.value], list(mesh[:nr.value]), chunks[:nc.value]
+
+
 def sample_irradiance(uniform, irr, dist, pos, nrm, wo, precision: int = 0) -> np.ndarray:
     i = np.ascontiguousarray(irr, dtype=np.float32)
     d = np.ascontiguousarray(dist, dtype=np.float32)
@@ -321,6 +372,7 @@ def ref_lib():
             "ref_ray_dirs": (c_int, [vp, c_int, vp]),
             "ref_surface_light": (c_int, [vp, vp, vp, c_int, vp, vp, c_int, vp, c_float, c_int, vp]),
             "ref_inject": (c_int, [vp, vp, vp, vp, vp]),
+            "ref_sdf_raster": (c_int, [vp, vp, c_int, vp, vp, vp, c_int, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -400,6 +452,20 @@ def ref_inject(vdesc, inputs: HostInputs, irr, dist, base=None) -> np.ndarray:
     d = np.ascontiguousarray(dist, dtype=np.float32)
     ref_lib().ref_inject(ctypes.byref(vdesc), ctypes.byref(inputs.surface_desc), _p(i), _p(d), _p(o))
     return o
+
+
+def ref_sdf_raster(desc, data, cascade: int, meshes, recs, rec_mesh, chunks, sdf: np.ndarray) -> np.ndarray:
+    """SDFRasterizeModel.glsl over a cascade's chunks through the reference's
+    compiled distanceToModelSDF; writes into a copy of `sdf` (float)."""
+    from luxgi_gb300 import _native as N
+
+    out = np.array(sdf, dtype=np.float32, copy=True)
+    md, keep = _mesh_descs(meshes)
+    R = (N.SdfRasterObject * max(1, len(recs)))(*recs)
+    M = (ctypes.c_int32 * max(1, len(rec_mesh)))(*rec_mesh)
+    Ch = (N.SdfChunk * max(1, len(chunks)))(*chunks)
+    ref_lib().ref_sdf_raster(ctypes.byref(desc), ctypes.byref(data), cascade, R, M, Ch, len(chunks), md, _p(out))
+    return out
 
 
 def ref_cull(surface_desc, capacity: int):

@@ -304,6 +304,11 @@ struct sampler3D {
     const float* f32 = nullptr;
     const uint16_t* f16 = nullptr;
     int W = 0, H = 0, D = 0;
+    // mip levels (FP16) with REPEAT wrap for textureLod: the mesh SDF
+    // volumes (Texture3D with their default sampler); levels == 0 = none
+    int levels = 0;
+    const uint16_t* lv[3] = {nullptr, nullptr, nullptr};
+    int lw[3] = {0, 0, 0}, lh[3] = {0, 0, 0}, ld[3] = {0, 0, 0};
     float at(int x, int y, int z) const {
         size_t i = size_t(x) + size_t(W) * (size_t(y) + size_t(H) * size_t(z));
         if (f16) { _Float16 h; std::memcpy(&h, f16 + i, 2); return float(h); }
@@ -343,7 +348,28 @@ inline vec4 texture(const sampler3D& t, const vec3& uvw) {
               (1 - a) * b * c * t.at(x0, y1, z1) + a * b * c * t.at(x1, y1, z1);
     return vec4(v, 0.0f, 0.0f, 1.0f);
 }
-inline vec4 textureLod(const sampler3D& t, const vec3& uvw, float) { return texture(t, uvw); }
+inline vec4 textureLod(const sampler3D& t, const vec3& uvw, float lod) {
+    if (t.levels == 0) return texture(t, uvw);
+    int L = int(lod);
+    L = L < 0 ? 0 : (L >= t.levels ? t.levels - 1 : L);
+    const int W = t.lw[L], H = t.lh[L], D = t.ld[L];
+    float x = uvw.e[0] * float(W) - 0.5f, y = uvw.e[1] * float(H) - 0.5f, z = uvw.e[2] * float(D) - 0.5f;
+    float fx = glslc::f_floor(x), fy = glslc::f_floor(y), fz = glslc::f_floor(z);
+    float a = x - fx, b = y - fy, c = z - fz;
+    auto wr = [](int i, int n) { int r = i % n; return r < 0 ? r + n : r; };
+    int x0 = wr(int(fx), W), x1 = wr(int(fx) + 1, W), y0 = wr(int(fy), H), y1 = wr(int(fy) + 1, H);
+    int z0 = wr(int(fz), D), z1 = wr(int(fz) + 1, D);
+    auto at = [&](int i, int j, int k) {
+        _Float16 h;
+        std::memcpy(&h, t.lv[L] + size_t(i) + size_t(W) * (size_t(j) + size_t(H) * size_t(k)), 2);
+        return float(h);
+    };
+    float v = (1 - a) * (1 - b) * (1 - c) * at(x0, y0, z0) + a * (1 - b) * (1 - c) * at(x1, y0, z0) +
+              (1 - a) * b * (1 - c) * at(x0, y1, z0) + a * b * (1 - c) * at(x1, y1, z0) +
+              (1 - a) * (1 - b) * c * at(x0, y0, z1) + a * (1 - b) * c * at(x1, y0, z1) +
+              (1 - a) * b * c * at(x0, y1, z1) + a * b * c * at(x1, y1, z1);
+    return vec4(v, 0.0f, 0.0f, 1.0f);
+}
 inline vec4 texture(const sampler2D& t, const vec2& uv) {
     float x = uv.e[0] * float(t.W) - 0.5f, y = uv.e[1] * float(t.H) - 0.5f;
     float fx = glslc::f_floor(x), fy = glslc::f_floor(y);

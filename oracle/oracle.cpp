@@ -23,6 +23,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <array>
+#include <map>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -882,6 +884,220 @@ template <typename R> V3<R> direct_light(const luxgi_sdf_desc* sdf, const Vol& t
     return {b.x * lrad.x * s, b.y * lrad.y * s, b.z * lrad.z * s};
 }
 
+// ------------------------------------------------ global SDF from objects
+// merge_sdf::system (Engine/DDGI/GlobalDistanceField.cpp:576-842, first
+// build), chunkCalculate (:465-535), getChunkId (:193-210), the cascade
+// placement (:592-626), SDFRasterizeModel.glsl:42-63 and distanceToModelSDF
+// (SDFCommon.glsl:38-62).  FP32 with glm's association of matrix-vector
+// products; matrices column-major.
+namespace sdfb {
+
+struct Mat {
+    float m[16];
+};
+struct Vec4 {
+    float x, y, z, w;
+};
+
+inline Vec4 mv(const Mat& M, float x, float y, float z, float w) {
+    const float* m = M.m;
+    return {(m[0] * x + m[4] * y) + (m[8] * z + m[12] * w), (m[1] * x + m[5] * y) + (m[9] * z + m[13] * w),
+            (m[2] * x + m[6] * y) + (m[10] * z + m[14] * w), (m[3] * x + m[7] * y) + (m[11] * z + m[15] * w)};
+}
+inline Mat mm(const Mat& A, const Mat& B) {
+    Mat r;
+    for (int c = 0; c < 4; ++c) {
+        Vec4 v = mv(A, B.m[c * 4], B.m[c * 4 + 1], B.m[c * 4 + 2], B.m[c * 4 + 3]);
+        r.m[c * 4] = v.x; r.m[c * 4 + 1] = v.y; r.m[c * 4 + 2] = v.z; r.m[c * 4 + 3] = v.w;
+    }
+    return r;
+}
+inline Mat inv(const Mat& A) {
+    M4<float> a;
+    std::memcpy(a.m, A.m, sizeof(a.m));
+    M4<float> b = inverse(a);
+    Mat r;
+    std::memcpy(r.m, b.m, sizeof(r.m));
+    return r;
+}
+inline float fmin_g(float a, float b) { return b < a ? b : a; }   // GLSL / glm min
+inline float fmax_g(float a, float b) { return a < b ? b : a; }
+
+constexpr float kScales[4] = {1.0f, 2.5f, 5.0f, 10.0f};
+
+struct Cascade {
+    float center[3], distance, voxel;
+};
+
+// cascade placement: a fixed view point on +z from math::lineHitsAABB of the
+// segment 0 -> FORWARD * 2 c0 against [-c0, c0]^3, snapped to the chunk grid
+inline Cascade cascade(const luxgi_sdf_build_desc& d, int c) {
+    const float dist = fmin_g(15000.0f, d.gi_distance) * d.global_scale;
+    const float extent = dist / kScales[d.cascades - 1];
+    const float c0 = extent * kScales[0];
+    const float inv_z = 1.0f / ((0.0f + 1.0f * (c0 * 2.0f)) - 0.0f);
+    const float inf = INFINITY;
+    const float ex_x = (c0 - 0.0f) * inf, en_x = (-c0 - 0.0f) * inf;
+    const float ex_z = (c0 - 0.0f) * inv_z, en_z = (-c0 - 0.0f) * inv_z;
+    const float far = fmin_g(fmax_g(en_x, ex_x), fmin_g(fmax_g(en_x, ex_x), fmax_g(en_z, ex_z)));
+    const float y = fmin_g(fmax_g(far, 0.0f), 1.0f);
+    const float offset = y * c0 * 0.6f;
+    const float view[3] = {0.0f * offset, 0.0f * offset, 0.0f + 1.0f * offset};
+    Cascade k;
+    k.distance = extent * kScales[c];
+    k.voxel = (k.distance * 2.0f) / float(d.resolution);
+    const float chunk = k.voxel * 32.0f;
+    for (int i = 0; i < 3; ++i) k.center[i] = std::floor(view[i] / chunk) * chunk;
+    return k;
+}
+
+struct Plan {
+    std::vector<luxgi_sdf_raster_object> recs;
+    std::vector<int> mesh;
+    std::vector<luxgi_sdf_chunk> chunks;
+};
+
+inline int plan(const luxgi_sdf_build_desc& d, const luxgi_mesh_sdf* meshes, int nm, const luxgi_sdf_object* objs,
+                int no, int c, Plan& P) {
+    const Cascade K = cascade(d, c);
+    float bmin[3], bmax[3];
+    for (int i = 0; i < 3; ++i) {
+        bmin[i] = K.center[i] - K.distance;
+        bmax[i] = K.center[i] + K.distance;
+    }
+    const float min_radius = d.min_object_radius * d.global_scale;
+    std::map<std::array<int, 3>, size_t> table;
+    for (int o = 0; o < no; ++o) {
+        const int mi = objs[o].mesh;
+        if (mi < 0 || mi >= nm) return LUXGI_EINVAL;
+        const luxgi_mesh_sdf& m = meshes[mi];
+        Mat W;
+        std::memcpy(W.m, objs[o].world, sizeof(W.m));
+        // sdf.aabb.transform(world) (Math/BoundingBox.cpp:10-22)
+        const float cen[3] = {(m.aabb_max[0] + m.aabb_min[0]) * 0.5f, (m.aabb_max[1] + m.aabb_min[1]) * 0.5f,
+                              (m.aabb_max[2] + m.aabb_min[2]) * 0.5f};
+        const Vec4 nc = mv(W, cen[0], cen[1], cen[2], 1.0f);
+        const float oe[3] = {(m.aabb_max[0] - m.aabb_min[0]) * 0.5f, (m.aabb_max[1] - m.aabb_min[1]) * 0.5f,
+                             (m.aabb_max[2] - m.aabb_min[2]) * 0.5f};
+        const float* w = W.m;
+        float ne[3];
+        for (int r = 0; r < 3; ++r)
+            ne[r] = std::fabs(w[r]) * oe[0] + std::fabs(w[4 + r]) * oe[1] + std::fabs(w[8 + r] * oe[2]);
+        const float ncv[3] = {nc.x, nc.y, nc.z};
+        float omin[3], omax[3];
+        for (int i = 0; i < 3; ++i) {
+            omin[i] = ncv[i] - ne[i];
+            omax[i] = ncv[i] + ne[i];
+        }
+        // BoundingSphere(box), BoundingBox::intersectsWithSphere
+        float sc[3], q[3], dd[3];
+        for (int i = 0; i < 3; ++i) {
+            sc[i] = (omax[i] + omin[i]) * 0.5f;
+            dd[i] = omax[i] - omin[i];
+        }
+        const float radius = std::sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) / 2.0f;
+        for (int i = 0; i < 3; ++i) q[i] = sc[i] - fmin_g(fmax_g(sc[i], bmin[i]), bmax[i]);
+        const float d2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        if (!(d2 <= radius * radius && radius >= min_radius)) continue;
+        // getChunkId, unclamped as in the reference
+        const float margin = K.voxel * 4.0f, chunk = K.voxel * 32.0f;
+        int cmin[3], cmax[3];
+        for (int i = 0; i < 3; ++i) {
+            const float base = bmin[i] + 0.1f;
+            cmin[i] = int(((omin[i] - margin) - base) / chunk);
+            cmax[i] = int(((omax[i] + margin) - base) / chunk);
+        }
+        // ObjectRasterizeData
+        Mat T;
+        for (int i = 0; i < 16; ++i) T.m[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+        T.m[12] = -cen[0];
+        T.m[13] = -cen[1];
+        T.m[14] = -cen[2];
+        const Mat w2v = mm(inv(W), T);
+        const Mat v2w = inv(w2v);
+        luxgi_sdf_raster_object r{};
+        std::memcpy(r.world_to_volume, w2v.m, sizeof(w2v.m));
+        std::memcpy(r.volume_to_world, v2w.m, sizeof(v2w.m));
+        for (int i = 0; i < 3; ++i) {
+            r.volume_to_uvw_mul[i] = m.local_to_uvw_mul[i];
+            r.volume_to_uvw_add[i] = m.local_to_uvw_add[i] + cen[i] * m.local_to_uvw_mul[i];
+            r.volume_local_bounds_extent[i] = (m.aabb_max[i] - m.aabb_min[i]) / 2.0f;
+        }
+        r.mip_offset = float(std::min(c, 2));
+        r.decode_mul = m.max_distance;
+        r.decode_add = -m.max_distance;
+        const uint32_t id = uint32_t(P.recs.size());
+        P.recs.push_back(r);
+        P.mesh.push_back(mi);
+        for (int z = cmin[2]; z <= cmax[2]; ++z)
+            for (int y = cmin[1]; y <= cmax[1]; ++y)
+                for (int x = cmin[0]; x <= cmax[0]; ++x) {
+                    auto it = table.find({x, y, z});
+                    if (it == table.end()) {
+                        luxgi_sdf_chunk ck{};
+                        ck.coord[0] = x; ck.coord[1] = y; ck.coord[2] = z;
+                        it = table.emplace(std::array<int, 3>{x, y, z}, P.chunks.size()).first;
+                        P.chunks.push_back(ck);
+                    }
+                    luxgi_sdf_chunk& ck = P.chunks[it->second];
+                    // a full layer-0 entry is overwritten by the (empty) next
+                    // layer before the object is appended (:516-523)
+                    if (ck.count == 28) ck.count = 0;
+                    ck.models[ck.count++] = id;
+                }
+    }
+    return 0;
+}
+
+// textureLod on a mesh SDF level: trilinear, REPEAT
+inline float sample_level(const uint16_t* v, int W, int H, int D, float u, float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+    const float a = x - fx, b = y - fy, c = z - fz;
+    auto wr = [](int i, int n) { int r = i % n; return r < 0 ? r + n : r; };
+    const int x0 = wr(int(fx), W), x1 = wr(int(fx) + 1, W), y0 = wr(int(fy), H), y1 = wr(int(fy) + 1, H);
+    const int z0 = wr(int(fz), D), z1 = wr(int(fz) + 1, D);
+    auto at = [&](int i, int j, int k) { return h2f(v[size_t(i) + size_t(W) * (size_t(j) + size_t(H) * size_t(k))]); };
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float c00 = at(x0, y0, z0) * ia + at(x1, y0, z0) * a, c10 = at(x0, y1, z0) * ia + at(x1, y1, z0) * a;
+    const float c01 = at(x0, y0, z1) * ia + at(x1, y0, z1) * a, c11 = at(x0, y1, z1) * ia + at(x1, y1, z1) * a;
+    const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
+inline void xf(const float* m, const float p[3], float o[3]) {
+    o[0] = (m[0] * p[0] + m[4] * p[1]) + (m[8] * p[2] + m[12]);
+    o[1] = (m[1] * p[0] + m[5] * p[1]) + (m[9] * p[2] + m[13]);
+    o[2] = (m[2] * p[0] + m[6] * p[1]) + (m[10] * p[2] + m[14]);
+}
+
+// distanceToModelSDF (SDFCommon.glsl:38-62)
+inline float distance_to_model(float min_distance, const luxgi_sdf_raster_object& r, const uint16_t* vol, int W,
+                               int H, int D, const float wp[3]) {
+    float vp[3], uvw[3], vc[3], wc[3];
+    xf(r.world_to_volume, wp, vp);
+    for (int i = 0; i < 3; ++i) {
+        uvw[i] = vp[i] * r.volume_to_uvw_mul[i] + r.volume_to_uvw_add[i];
+        const float e = r.volume_local_bounds_extent[i];
+        vc[i] = fmin_g(fmax_g(vp[i], -e), e);
+    }
+    xf(r.volume_to_world, vc, wc);
+    const float q[3] = {wp[0] - wc[0], wp[1] - wc[1], wp[2] - wc[2]};
+    float dtv = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+    if (dtv < 0.01f) {
+        const float s[3] = {vp[0] - vc[0], vp[1] - vc[1], vp[2] - vc[2]};
+        dtv = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    }
+    dtv = fmax_g(dtv, 0.0f);
+    if (min_distance <= dtv) return dtv;
+    const float vd = (sample_level(vol, W, H, D, uvw[0], uvw[1], uvw[2]) * 2.0f - 1.0f) * r.decode_mul;
+    float result = combine(vd, dtv);
+    if (dtv > 0.0f) result = fmax_g(dtv, result);
+    return result;
+}
+
+}  // namespace sdfb
+
 }  // namespace
 
 // ===================================================================== C API
@@ -1240,6 +1456,99 @@ int oracle_oct_encode(const float* dirs, int n, float* out) {
         V2<double> o = oct_encode(V3<double>{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]});
         out[2 * i] = float(o.x); out[2 * i + 1] = float(o.y);
     }
+    return 0;
+}
+
+// The global SDF from objects (first build): every voxel 1, then per
+// cascade its chunks rasterised and its mip built (flood passes only when
+// the cascade has chunks).  Mesh volumes are host FP16 arrays.  sdf_out
+// (res*C) x res x res and mip_out (mres*C) x mres^2 as float; fp16 rounds
+// every stored value to half as the R16F textures do.
+int oracle_sdf_build(const luxgi_sdf_build_desc* d, const luxgi_mesh_sdf* meshes, int nm,
+                     const luxgi_sdf_object* objs, int no, float* sdf_out, float* mip_out, luxgi_sdf_data* data_out) {
+    const int res = d->resolution, C = d->cascades, mres = res / 4;
+    const bool fp16 = d->format == LUXGI_STORAGE_FP16;
+    const int TW = res * C;
+    std::vector<float> sdf(size_t(TW) * res * res, 1.0f);
+    std::vector<float> mip(size_t(mres) * C * mres * mres, 1.0f), tmp(size_t(mres) * mres * mres, 1.0f);
+    luxgi_sdf_data data{};
+    for (int c = 0; c < C; ++c) {
+        sdfb::Plan P;
+        const int st = sdfb::plan(*d, meshes, nm, objs, no, c, P);
+        if (st != 0) return st;
+        const sdfb::Cascade K = sdfb::cascade(*d, c);
+        data.cascade_pos_distance[c][0] = K.center[0];
+        data.cascade_pos_distance[c][1] = K.center[1];
+        data.cascade_pos_distance[c][2] = K.center[2];
+        data.cascade_pos_distance[c][3] = K.distance;
+        data.cascade_voxel_size[c] = K.voxel;
+        const float maxd = K.distance * 2.0f;
+        float mul[3], add[3];
+        for (int i = 0; i < 3; ++i) {
+            const float lo = K.center[i] - K.distance, hi = K.center[i] + K.distance;
+            mul[i] = (hi - lo) / float(res);
+            add[i] = lo + K.voxel * 0.5f;
+        }
+        const int level = std::min(c, 2);
+#pragma omp parallel for schedule(dynamic)
+        for (int k = 0; k < int(P.chunks.size()); ++k) {
+            const luxgi_sdf_chunk& ck = P.chunks[size_t(k)];
+            for (int lz = 0; lz < 32; ++lz)
+                for (int ly = 0; ly < 32; ++ly)
+                    for (int lx = 0; lx < 32; ++lx) {
+                        const int vx = ck.coord[0] * 32 + lx, vy = ck.coord[1] * 32 + ly, vz = ck.coord[2] * 32 + lz;
+                        const int gx = vx + c * res;
+                        if (gx < 0 || gx >= TW || vy < 0 || vy >= res || vz < 0 || vz >= res) continue;
+                        const float wp[3] = {float(vx) * mul[0] + add[0], float(vy) * mul[1] + add[1],
+                                             float(vz) * mul[2] + add[2]};
+                        float md = maxd;
+                        for (int i = 0; i < ck.count; ++i) {
+                            const uint32_t id = ck.models[i];
+                            const luxgi_mesh_sdf& m = meshes[P.mesh[id]];
+                            const int L = std::min(level, m.mip_count - 1);
+                            const int W = std::max(m.size[0] >> L, 1), H = std::max(m.size[1] >> L, 1),
+                                      D = std::max(m.size[2] >> L, 1);
+                            const float od = sdfb::distance_to_model(md, P.recs[id], m.mips[L], W, H, D, wp);
+                            md = sdfb::fmin_g(md, od);
+                        }
+                        float v = sdfb::fmin_g(sdfb::fmax_g(md / maxd, -1.0f), 1.0f);
+                        if (fp16) v = round_half(v);
+                        sdf[size_t(gx) + size_t(TW) * (size_t(vy) + size_t(res) * size_t(vz))] = v;
+                    }
+        }
+        mip_pass(sdf, TW, res, c * res, mip, mres * C, c * mres, mres, 4, maxd, fp16);
+        if (!P.chunks.empty())
+            for (int i = 1; i < 5; ++i) {
+                if (i & 1) mip_pass(mip, mres * C, mres, c * mres, tmp, mres, 0, mres, 1, maxd, fp16);
+                else mip_pass(tmp, mres, mres, 0, mip, mres * C, c * mres, mres, 1, maxd, fp16);
+            }
+    }
+    data.cascades_count = uint32_t(C);
+    data.resolution = float(res);
+    data.near_plane = d->near_plane;
+    data.far_plane = d->far_plane;
+    std::memcpy(sdf_out, sdf.data(), sdf.size() * sizeof(float));
+    std::memcpy(mip_out, mip.data(), mip.size() * sizeof(float));
+    if (data_out) *data_out = data;
+    return 0;
+}
+
+// The plan of one cascade: records, their meshes and chunks (capacities as
+// luxgi_sdf_build_plan).
+int oracle_sdf_plan(const luxgi_sdf_build_desc* d, const luxgi_mesh_sdf* meshes, int nm, const luxgi_sdf_object* objs,
+                    int no, int cascade, luxgi_sdf_raster_object* recs, int rec_cap, int* n_recs, int32_t* rec_mesh,
+                    luxgi_sdf_chunk* chunks, int chunk_cap, int* n_chunks) {
+    sdfb::Plan P;
+    const int st = sdfb::plan(*d, meshes, nm, objs, no, cascade, P);
+    if (st != 0) return st;
+    *n_recs = int(P.recs.size());
+    *n_chunks = int(P.chunks.size());
+    if (int(P.recs.size()) > rec_cap || int(P.chunks.size()) > chunk_cap) return LUXGI_ENOMEM;
+    for (size_t i = 0; i < P.recs.size(); ++i) {
+        recs[i] = P.recs[i];
+        rec_mesh[i] = P.mesh[i];
+    }
+    for (size_t i = 0; i < P.chunks.size(); ++i) chunks[i] = P.chunks[i];
     return 0;
 }
 

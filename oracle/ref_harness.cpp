@@ -14,6 +14,8 @@
 //   ref_surface_light  CopyEmissive.frag:22-26, SDFDeferredLight.frag:41-129
 //                      (BRDF from Raytraced/BRDF.glsl:65-81)
 //   ref_inject SDFAtlasIndirectLight.frag:44-67
+//   ref_sdf_raster SDFRasterizeModel.glsl:42-63 (distanceToModelSDF,
+//              SDFCommon.glsl:38-62) over a cascade's chunks
 // The two raster passes run over the pixels of the tile quads of addTiles2
 // (Engine/DDGI/GlobalSurfaceAtlas.cpp:554-574).
 // The entry-point bodies are restated because they declare Vulkan
@@ -36,6 +38,7 @@ static_assert(sizeof(GlobalSurfaceAtlasData) == sizeof(luxgi_surface_data), "Glo
 static_assert(sizeof(ObjectBuffer) == sizeof(luxgi_surface_object), "ObjectBuffer layout");
 static_assert(sizeof(TileBuffer) == sizeof(luxgi_surface_tile), "TileBuffer layout");
 static_assert(sizeof(Light) == sizeof(luxgi_light), "Light layout");
+static_assert(sizeof(ObjectRasterizeData) == sizeof(luxgi_sdf_raster_object), "ObjectRasterizeData layout");
 
 namespace {
 
@@ -480,6 +483,59 @@ int ref_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* surf,
                 out[ti * 4 + 2] = to16(h16(surf->direct_light[ti * 4 + 2]) + e.z);
                 out[ti * 4 + 3] = surf->direct_light[ti * 4 + 3];
             }
+    }
+    return 0;
+}
+
+// SDFRasterizeModel.glsl main without READ_DISTANCE (:42-63) for every
+// voxel of the given chunks of cascade `cascade`: the ubo (cascadeCoordTo
+// PosMul / Add, maxDistance) as GlobalDistanceField.cpp:755-760 fills it,
+// the records and mesh volumes as the plan binds them.  sdf (float,
+// (res*C) x res x res) is written where the voxel lands in the texture.
+int ref_sdf_raster(const luxgi_sdf_build_desc* d, const luxgi_sdf_data* data, int cascade,
+                   const luxgi_sdf_raster_object* recs, const int32_t* rec_mesh, const luxgi_sdf_chunk* chunks,
+                   int n_chunks, const luxgi_mesh_sdf* meshes, float* sdf) {
+    const int res = d->resolution, C = d->cascades;
+    const float cd = data->cascade_pos_distance[cascade][3], voxel = data->cascade_voxel_size[cascade];
+    vec3 center(data->cascade_pos_distance[cascade][0], data->cascade_pos_distance[cascade][1],
+                data->cascade_pos_distance[cascade][2]);
+    const vec3 bmin = center - cd, bmax = center + cd;
+    const vec3 cascadeCoordToPosMul = (bmax - bmin) / float(res);
+    const vec3 cascadeCoordToPosAdd = bmin + voxel * 0.5f;
+    const float maxDistance = cd * 2.0f;
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < n_chunks; ++k) {
+        const luxgi_sdf_chunk& ch = chunks[k];
+        std::vector<sampler3D> tex(size_t(ch.count));
+        for (int i = 0; i < ch.count; ++i) {
+            const luxgi_mesh_sdf& m = meshes[rec_mesh[ch.models[i]]];
+            sampler3D& t = tex[size_t(i)];
+            t.levels = m.mip_count;
+            for (int L = 0; L < m.mip_count; ++L) {
+                t.lv[L] = m.mips[L];
+                t.lw[L] = m.size[0] >> L > 0 ? m.size[0] >> L : 1;
+                t.lh[L] = m.size[1] >> L > 0 ? m.size[1] >> L : 1;
+                t.ld[L] = m.size[2] >> L > 0 ? m.size[2] >> L : 1;
+            }
+        }
+        for (int lz = 0; lz < 32; ++lz)
+            for (int ly = 0; ly < 32; ++ly)
+                for (int lx = 0; lx < 32; ++lx) {
+                    ivec3 voxelCoord = ivec3(ch.coord[0] * 32, ch.coord[1] * 32, ch.coord[2] * 32) + ivec3(lx, ly, lz);
+                    vec3 voxelWorldPos = vec3(voxelCoord) * cascadeCoordToPosMul + cascadeCoordToPosAdd;
+                    voxelCoord.x += cascade * res;
+                    float minDistance = maxDistance;
+                    for (int i = 0; i < ch.count; ++i) {
+                        const ObjectRasterizeData objectData = as<ObjectRasterizeData>(recs[ch.models[i]]);
+                        float objectDistance = distanceToModelSDF(minDistance, objectData, tex[size_t(i)], voxelWorldPos);
+                        minDistance = min(minDistance, objectDistance);
+                    }
+                    const float v = clamp(minDistance / maxDistance, -1, 1);
+                    if (voxelCoord.x < 0 || voxelCoord.x >= res * C || voxelCoord.y < 0 || voxelCoord.y >= res ||
+                        voxelCoord.z < 0 || voxelCoord.z >= res)
+                        continue;
+                    sdf[size_t(voxelCoord.x) + size_t(res * C) * (size_t(voxelCoord.y) + size_t(res) * size_t(voxelCoord.z))] = v;
+                }
     }
     return 0;
 }

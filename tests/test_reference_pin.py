@@ -202,3 +202,27 @@ def test_inject_matches_reference(ref):
     b = oracle.ref_inject(vd, inp, irr, dist)
     assert np.count_nonzero(a != host.direct) > 10000
     assert rel_err(_f16(a), _f16(b)) < 2e-3
+
+
+@pytest.mark.parametrize("cascades,res", [(2, 64), (3, 32)])
+def test_sdf_raster_matches_reference(ref, cascades, res):
+    """The global SDF from placed mesh SDFs: the oracle's voxels against
+    SDFRasterizeModel.glsl's main around the reference's compiled
+    distanceToModelSDF / combineDistanceToSDF, cascade after cascade on the
+    same plan (objects scattered beyond cascade 0, so chunks reach past
+    it): within 2 ulps."""
+    from luxgi_gb300.sdf import MeshSDF, box_distance, build_desc, sphere_distance, trs
+
+    meshes = [MeshSDF.bake(box_distance((2.0, 1.0, 1.5)), (-2, -1, -1.5), (2, 1, 1.5), (24, 16, 20)),
+              MeshSDF.bake(sphere_distance(1.2), (-1.2,) * 3, (1.2,) * 3, (16, 16, 16), mip_count=2)]
+    rng = np.random.default_rng(cascades)
+    objs = [(trs(rng.uniform(-90, 90, 3), rng.normal(size=3), rng.uniform(0, 6),
+                 (1, 1, 1) if i % 2 else rng.uniform(0.5, 3, 3)), i % 2) for i in range(40)]
+    d = build_desc(resolution=res, cascades=cascades, storage=N.STORAGE_FP32, global_scale=0.05)
+    sdf, _, data = oracle.sdf_build(d, meshes, objs)
+    b = np.ones_like(sdf)
+    for c in range(cascades):
+        recs, mesh, chunks = oracle.sdf_plan(d, meshes, objs, c)
+        b = oracle.ref_sdf_raster(d, data, c, meshes, recs, mesh, chunks, b)
+    assert (sdf < 1.0).mean() > 0.5
+    assert np.max(np.abs(sdf - b)) <= 2.4e-7
