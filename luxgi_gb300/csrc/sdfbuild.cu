@@ -6,8 +6,8 @@
 // The host plans each cascade the way the reference's system does -- object
 // selection, ObjectRasterizeData records and the 32^3-voxel chunk table with
 // at most 28 objects a chunk -- and the device rasterises: one block per
-// chunk, one thread per voxel column step, the chunk's records and mesh
-// volumes staged in shared memory.  Cascade by cascade: rasterise, then that
+// chunk plane, one thread per voxel, the chunk's records and mesh volumes
+// staged in shared memory.  Cascade by cascade: rasterise, then that
 // cascade's mip, as the reference orders its dispatches.
 //
 // Built with -fmad=false (and the host part without contraction): the
@@ -368,7 +368,9 @@ __global__ void fill_kernel(__half* h, float* f, size_t n) {
 }
 
 // SDFRasterizeModel.glsl main (no READ_DISTANCE: the reference's chunks
-// never reach a second layer) for every voxel of one chunk per block
+// never reach a second layer) for one z plane (32 x 32 voxels) of one chunk
+// per block: blockIdx.x = chunk, blockIdx.y = plane, so that the coarse
+// cascades' few chunks still fill the GPU
 template <typename T>
 __global__ void __launch_bounds__(256) sdf_raster_kernel(const luxgi_sdf_chunk* __restrict__ chunks,
                                                          const luxgi_sdf_raster_object* __restrict__ recs,
@@ -389,8 +391,9 @@ __global__ void __launch_bounds__(256) sdf_raster_kernel(const luxgi_sdf_chunk* 
     const int ox = __ldg(&ch->coord[0]) * LUXGI_SDF_CHUNK, oy = __ldg(&ch->coord[1]) * LUXGI_SDF_CHUNK,
               oz = __ldg(&ch->coord[2]) * LUXGI_SDF_CHUNK;
     const int TW = p.res * p.C;
-    for (int v = threadIdx.x; v < LUXGI_SDF_CHUNK * LUXGI_SDF_CHUNK * LUXGI_SDF_CHUNK; v += blockDim.x) {
-        const int vx = ox + (v & 31), vy = oy + ((v >> 5) & 31), vz = oz + (v >> 10);
+    const int vz = oz + int(blockIdx.y);
+    for (int v = threadIdx.x; v < LUXGI_SDF_CHUNK * LUXGI_SDF_CHUNK; v += blockDim.x) {
+        const int vx = ox + (v & 31), vy = oy + (v >> 5);
         const int gx = vx + p.cascade * p.res;
         // image stores outside the packed texture are discarded; x past the
         // cascade lands in its neighbour, as in the reference
@@ -480,12 +483,9 @@ int luxgi_sdf_build(const luxgi_sdf_build_desc* d, const luxgi_mesh_sdf* meshes,
     note_launch();
     cudaError_t e = cudaGetLastError();
     std::vector<CascadePlan> plans(static_cast<size_t>(C));
-    size_t max_chunks = 0, max_recs = 0;
     for (int c = 0; c < C && e == cudaSuccess; ++c) {
         const int s = plan_cascade(*d, meshes, nm, objs, no, c, plans[size_t(c)]);
         if (s != LUXGI_OK) return s;
-        max_chunks = std::max(max_chunks, plans[size_t(c)].chunks.size());
-        max_recs = std::max(max_recs, plans[size_t(c)].records.size());
     }
     // one device staging area for every cascade's lists (cascades run in
     // stream order, each after its lists' upload)
@@ -552,7 +552,7 @@ int luxgi_sdf_build(const luxgi_sdf_build_desc* d, const luxgi_mesh_sdf* meshes,
             const auto* ck = reinterpret_cast<const luxgi_sdf_chunk*>(base + chunk_off[size_t(c)]);
             const auto* rc = reinterpret_cast<const luxgi_sdf_raster_object*>(base + rec_off[size_t(c)]);
             const auto* rm = reinterpret_cast<const RasterMesh*>(base + mesh_off[size_t(c)]);
-            const unsigned grid = unsigned(pl.chunks.size());
+            const dim3 grid(unsigned(pl.chunks.size()), LUXGI_SDF_CHUNK);
             if (h) sdf_raster_kernel<__half><<<grid, 256, 0, st>>>(ck, rc, rm, p, as_t<__half>(sdf));
             else sdf_raster_kernel<float><<<grid, 256, 0, st>>>(ck, rc, rm, p, as_t<float>(sdf));
             note_launch();
