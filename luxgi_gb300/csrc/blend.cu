@@ -194,17 +194,190 @@ __host__ __device__ __forceinline__ BlendShape blend_shape(int T, int PP) {
     return s;
 }
 
-__host__ __device__ __forceinline__ size_t blend_smem_bytes(int T, int PP, bool depth) {
+// FP32 rays take the pipelined path: chunks of kPipeChunk rays, two buffers,
+// the next chunk's weights and rays copied with cp.async while the current
+// chunk's FMAs run (the same shared memory as one 32-ray buffer).
+constexpr int kPipeChunk = 16;
+
+__host__ __device__ __forceinline__ size_t blend_smem_bytes(int T, int PP, bool depth, bool pipelined) {
     const BlendShape s = blend_shape(T, PP);
-    return sizeof(float) * kRayChunk * (s.TG * kTexelTile) + size_t(depth ? 8 : 16) * kRayChunk * s.PB;
+    const int Tp = s.TG * kTexelTile;
+    if (pipelined)
+        return 2 * sizeof(float) * kPipeChunk * Tp +
+               (depth ? 2 * sizeof(float) * kPipeChunk * s.PB + sizeof(float2) * kPipeChunk * s.PB
+                      : 2 * sizeof(float4) * kPipeChunk * s.PB);
+    return sizeof(float) * kRayChunk * Tp + size_t(depth ? 8 : 16) * kRayChunk * s.PB;
 }
+
+// cp.async of 16 (or 4) bytes global -> shared; src_bytes 0 fills zeros
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
+    const unsigned d = unsigned(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, int src_bytes) {
+    const unsigned d = unsigned(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 template <bool DEPTH> struct RayVal;
 template <> struct RayVal<false> { using type = float4; };
 template <> struct RayVal<true> { using type = float2; };
 
+// The epilogue of a block: normalise, gamma, hysteresis, store + border
+// mirrors (ProbeUpdate.glsl:105-152, BorderUpdate.glsl:136-156).
+template <int DEPTH, typename AT, int PP, int NC_ACC>
+__device__ __forceinline__ void blend_epilogue(const BlendParams& p, int p0, int tg, int pg, int T, int n, int W,
+                                               float (&acc)[PP][kTexelTile][NC_ACC]) {
+    const luxgi_ddgi_uniform& u = p.u;
+    const int XY = u.probe_counts[0] * u.probe_counts[1];
+    const float* nrm = DEPTH ? p.n_dist : p.n_irr;
+    const void* prev = DEPTH ? p.prev_dist : p.prev_irr;
+    void* out = DEPTH ? p.out_dist : p.out_irr;
+    constexpr int NC = DEPTH ? 2 : 4;
+    const float h = u.hysteresis;
+    const float ig = 1.0f / u.ddgi_gamma;
+#pragma unroll
+    for (int j = 0; j < PP; ++j) {
+        const int pr = p0 + pg * PP + j;
+        if (pr >= p.P) continue;
+        const int cx = pr % XY, cy = pr / XY;
+#pragma unroll
+        for (int k = 0; k < kTexelTile; ++k) {
+            const int t = tg * kTexelTile + k;
+            if (t >= T) continue;
+            const int tx = t % n, ty = t / n;
+            const float s = __ldg(nrm + t);
+            float v[4];
+            v[0] = acc[j][k][0] * s;
+            v[1] = acc[j][k][1] * s;
+            v[2] = DEPTH ? 0.0f : acc[j][k][NC_ACC - 1] * s;
+            v[3] = 1.0f;
+            if (!DEPTH) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) v[c] = powf(v[c], ig);
+            }
+            const size_t base = (size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2)) * NC;
+            const int nch = DEPTH ? 2 : 3;
+            for (int c = 0; c < nch; ++c) {
+                float x = v[c];
+                if (!p.first) x = x * (1.0f - h) + AtlasIO<AT>::ld(prev, base + c) * h;
+                v[c] = AtlasIO<AT>::rnd(x);
+            }
+            store_texel<AT, NC>(out, W, n, cx, cy, tx, ty, v);
+        }
+    }
+}
+
+// FP32 rays: the chunk loop with cp.async double buffering.  Chunk c+1's
+// weight rows and rays (rgb+distance float4s, or the distances alone) are in
+// flight while chunk c's FMAs run; the distance blend turns the raw
+// distances into (d, d^2) in shared memory once a chunk has landed.  The
+// accumulation order per accumulator is the single-buffer kernel's.
+template <int DEPTH, typename AT, int PP>
+__device__ __forceinline__ void blend_block_pipelined(const BlendParams& p, int block, float* smem) {
+    using RV = typename RayVal<DEPTH != 0>::type;
+    constexpr int NC_ACC = DEPTH ? 2 : 3;
+    constexpr int KC = kPipeChunk;
+    const luxgi_ddgi_uniform& u = p.u;
+    const int n = DEPTH ? u.depth_probe_side : u.irradiance_probe_side;
+    const int T = n * n;
+    const int W = DEPTH ? u.depth_width : u.irradiance_width;
+    const int R = p.R;
+    const BlendShape sh = blend_shape(T, PP);
+    const int Tp = sh.TG * kTexelTile;
+    const int PB = sh.PB;
+    const int p0 = block * PB;
+    float* Ws = smem;                                               // [2][KC][Tp]
+    float* rbuf = smem + 2 * KC * Tp;                               // irr: float4 [2][KC][PB]; dist: float [2][KC][PB]
+    RV* Rd = reinterpret_cast<RV*>(rbuf + 2 * KC * PB);             // dist only: float2 [KC][PB]
+    const float* Wg = DEPTH ? p.w_dist : p.w_irr;                   // [R][Tp]
+    const float4* rays = static_cast<const float4*>(p.rays);
+    const int tg = int(threadIdx.x) % sh.TG, pg = int(threadIdx.x) / sh.TG;
+    const bool active = pg < sh.PG;
+    float acc[PP][kTexelTile][NC_ACC];
+#pragma unroll
+    for (int j = 0; j < PP; ++j)
+#pragma unroll
+        for (int k = 0; k < kTexelTile; ++k)
+#pragma unroll
+            for (int c = 0; c < NC_ACC; ++c) acc[j][k][c] = 0.0f;
+    const int nchunks = (R + KC - 1) / KC;
+    auto issue = [&](int c) {
+        const int r0 = c * KC, kc = min(KC, R - r0), b = c & 1;
+        const float4* src = reinterpret_cast<const float4*>(Wg + size_t(r0) * Tp);
+        float4* dst = reinterpret_cast<float4*>(Ws + b * KC * Tp);
+        for (int i = threadIdx.x; i < kc * Tp / 4; i += blockDim.x) cp_async16(dst + i, src + i, 16);
+        for (int i = threadIdx.x; i < PB * kc; i += blockDim.x) {
+            const int pb = i / kc, r = i % kc;
+            const int pr = p0 + pb;
+            const bool ok = pr < p.P;
+            const float4* g = rays + (ok ? size_t(pr) * R + r0 + r : 0);
+            if constexpr (DEPTH)
+                cp_async4(rbuf + b * KC * PB + r * PB + pb, reinterpret_cast<const float*>(g) + 3, ok ? 4 : 0);
+            else
+                cp_async16(reinterpret_cast<float4*>(rbuf) + b * KC * PB + r * PB + pb, g, ok ? 16 : 0);
+        }
+        cp_async_commit();
+    };
+    issue(0);
+    for (int c = 0; c < nchunks; ++c) {
+        const int kc = min(KC, R - c * KC), b = c & 1;
+        if (c + 1 < nchunks) {
+            issue(c + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const RV* rs;
+        if constexpr (DEPTH) {
+            const float* raw = rbuf + b * KC * PB;
+            for (int i = threadIdx.x; i < PB * kc; i += blockDim.x) {
+                const int pb = i / kc, r = i % kc;
+                const bool ok = p0 + pb < p.P;
+                float d = mn(u.max_distance, raw[r * PB + pb] - 0.01f);
+                if (d == -1.0f) d = u.max_distance;
+                Rd[r * PB + pb] = ok ? make_float2(d, d * d) : make_float2(0.0f, 0.0f);
+            }
+            __syncthreads();
+            rs = Rd;
+        } else {
+            rs = reinterpret_cast<const RV*>(rbuf) + b * KC * PB;
+        }
+        if (active) {
+            const float* wrow = Ws + b * KC * Tp + tg * kTexelTile;
+            const RV* rrow = rs + pg * PP;
+#pragma unroll 2
+            for (int r = 0; r < kc; ++r) {
+                const float4 w4 = *reinterpret_cast<const float4*>(wrow + r * Tp);
+                const float w[kTexelTile] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                for (int j = 0; j < PP; ++j) {
+                    const RV v = rrow[r * PB + j];
+#pragma unroll
+                    for (int k = 0; k < kTexelTile; ++k) {
+                        acc[j][k][0] = fmaf(v.x, w[k], acc[j][k][0]);
+                        acc[j][k][1] = fmaf(v.y, w[k], acc[j][k][1]);
+                        if constexpr (!DEPTH) acc[j][k][2] = fmaf(v.z, w[k], acc[j][k][2]);
+                    }
+                }
+            }
+        }
+        // the buffer just read is the target of the copies issued next
+        __syncthreads();
+    }
+    if (!active) return;
+    blend_epilogue<DEPTH, AT, PP, NC_ACC>(p, p0, tg, pg, T, n, W, acc);
+}
+
 template <int DEPTH, typename RT, typename AT, int PP>
 __device__ __forceinline__ void blend_block(const BlendParams& p, int block, float* smem) {
+    if constexpr (sizeof(RT) == 16) {
+        blend_block_pipelined<DEPTH, AT, PP>(p, block, smem);
+        return;
+    }
     using RV = typename RayVal<DEPTH != 0>::type;
     constexpr int NC_ACC = DEPTH ? 2 : 3;
     const luxgi_ddgi_uniform& u = p.u;
@@ -281,44 +454,7 @@ __device__ __forceinline__ void blend_block(const BlendParams& p, int block, flo
         __syncthreads();
     }
     if (!active) return;
-    // epilogue: normalise, gamma, hysteresis, store + border mirrors
-    const int XY = u.probe_counts[0] * u.probe_counts[1];
-    const float* nrm = DEPTH ? p.n_dist : p.n_irr;
-    const void* prev = DEPTH ? p.prev_dist : p.prev_irr;
-    void* out = DEPTH ? p.out_dist : p.out_irr;
-    constexpr int NC = DEPTH ? 2 : 4;
-    const float h = u.hysteresis;
-    const float ig = 1.0f / u.ddgi_gamma;
-#pragma unroll
-    for (int j = 0; j < PP; ++j) {
-        const int pr = p0 + pg * PP + j;
-        if (pr >= p.P) continue;
-        const int cx = pr % XY, cy = pr / XY;
-#pragma unroll
-        for (int k = 0; k < kTexelTile; ++k) {
-            const int t = tg * kTexelTile + k;
-            if (t >= T) continue;
-            const int tx = t % n, ty = t / n;
-            const float s = __ldg(nrm + t);
-            float v[4];
-            v[0] = acc[j][k][0] * s;
-            v[1] = acc[j][k][1] * s;
-            v[2] = DEPTH ? 0.0f : acc[j][k][NC_ACC - 1] * s;
-            v[3] = 1.0f;
-            if (!DEPTH) {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) v[c] = powf(v[c], ig);
-            }
-            const size_t base = (size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2)) * NC;
-            const int nch = DEPTH ? 2 : 3;
-            for (int c = 0; c < nch; ++c) {
-                float x = v[c];
-                if (!p.first) x = x * (1.0f - h) + AtlasIO<AT>::ld(prev, base + c) * h;
-                v[c] = AtlasIO<AT>::rnd(x);
-            }
-            store_texel<AT, NC>(out, W, n, cx, cy, tx, ty, v);
-        }
-    }
+    blend_epilogue<DEPTH, AT, PP, NC_ACC>(p, p0, tg, pg, T, n, W, acc);
 }
 
 template <int DEPTH, typename RT, typename AT, int PP>
@@ -352,7 +488,7 @@ int blend_blocks(const BlendParams& p, bool depth, int pp) {
 
 size_t blend_smem(const BlendParams& p, bool depth, int pp) {
     const int side = blend_side(p, depth);
-    return blend_smem_bytes(side * side, pp, depth);
+    return blend_smem_bytes(side * side, pp, depth, p.storage != LUXGI_STORAGE_FP16);
 }
 
 // Probes per thread of a single-volume launch: the largest tile that still
