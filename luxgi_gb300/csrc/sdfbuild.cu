@@ -6,7 +6,7 @@
 // The host plans each cascade the way the reference's system does -- object
 // selection, ObjectRasterizeData records and the 32^3-voxel chunk table with
 // at most 28 objects a chunk -- and the device rasterises: one block per
-// chunk plane, one thread per voxel, the chunk's records and mesh volumes
+// plane (or 8-row band) of a chunk, the chunk's records and mesh volumes
 // staged in shared memory.  Cascade by cascade: rasterise, then that
 // cascade's mip, as the reference orders its dispatches.
 //
@@ -293,6 +293,9 @@ void layout_data(const luxgi_sdf_build_desc& d, luxgi_sdf_data& out) {
 struct RasterMesh {
     const __half* vol;   // the level sampled in this cascade
     int w, h, d;
+    // a world-space sphere around the object's volume box: centre (the
+    // volume origin) and a radius bounding every box point's distance
+    float cx, cy, cz, radius;
 };
 
 struct RasterParams {
@@ -368,9 +371,11 @@ __global__ void fill_kernel(__half* h, float* f, size_t n) {
 }
 
 // SDFRasterizeModel.glsl main (no READ_DISTANCE: the reference's chunks
-// never reach a second layer) for one z plane (32 x 32 voxels) of one chunk
-// per block: blockIdx.x = chunk, blockIdx.y = plane, so that the coarse
-// cascades' few chunks still fill the GPU
+// never reach a second layer): blockIdx.x = chunk, blockIdx.y = z plane,
+// blockIdx.z = band of 32 / gridDim.z rows of the plane.  Cascades with
+// many chunks take whole planes (4 voxels a thread, the records staged
+// once a plane); the coarse cascades' few chunks take 8-row bands so that
+// they still fill the GPU.
 template <typename T>
 __global__ void __launch_bounds__(256) sdf_raster_kernel(const luxgi_sdf_chunk* __restrict__ chunks,
                                                          const luxgi_sdf_raster_object* __restrict__ recs,
@@ -392,8 +397,9 @@ __global__ void __launch_bounds__(256) sdf_raster_kernel(const luxgi_sdf_chunk* 
               oz = __ldg(&ch->coord[2]) * LUXGI_SDF_CHUNK;
     const int TW = p.res * p.C;
     const int vz = oz + int(blockIdx.y);
-    for (int v = threadIdx.x; v < LUXGI_SDF_CHUNK * LUXGI_SDF_CHUNK; v += blockDim.x) {
-        const int vx = ox + (v & 31), vy = oy + (v >> 5);
+    const int rows = LUXGI_SDF_CHUNK / int(gridDim.z);
+    for (int v = threadIdx.x; v < LUXGI_SDF_CHUNK * rows; v += blockDim.x) {
+        const int vx = ox + (v & 31), vy = oy + int(blockIdx.z) * rows + (v >> 5);
         const int gx = vx + p.cascade * p.res;
         // image stores outside the packed texture are discarded; x past the
         // cascade lands in its neighbour, as in the reference
@@ -401,7 +407,16 @@ __global__ void __launch_bounds__(256) sdf_raster_kernel(const luxgi_sdf_chunk* 
         const f3 wp{float(vx) * p.mul[0] + p.add[0], float(vy) * p.mul[1] + p.add[1], float(vz) * p.mul[2] + p.add[2]};
         float md = p.max_dist;
         for (int k = 0; k < n; ++k) {
-            const float od = distance_to_model(md, srec[k], smesh[k], wp);
+            // an object whose box is certainly farther than max(md, 0.01)
+            // (distanceToModelSDF's world-space branch) returns a distance
+            // >= md, which leaves md unchanged: skip it.  The margin covers
+            // the rounding of the transforms.
+            const RasterMesh& m = smesh[k];
+            const float dx = wp.x - m.cx, dy = wp.y - m.cy, dz = wp.z - m.cz;
+            const float dc = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float lim = mx(md, 0.01f);
+            if (dc - m.radius > lim + 1e-4f * (dc + m.radius + lim) + 1e-3f) continue;
+            const float od = distance_to_model(md, srec[k], m, wp);
             md = mn(md, od);
         }
         store_sdf<T>(out, size_t(gx) + size_t(TW) * (size_t(vy) + size_t(p.res) * size_t(vz)),
@@ -470,6 +485,10 @@ int luxgi_sdf_build(const luxgi_sdf_build_desc* d, const luxgi_mesh_sdf* meshes,
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int res = d->resolution, C = d->cascades;
+    int ordinal = 0, sms = 0;
+    cudaGetDevice(&ordinal);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ordinal);
+    if (sms <= 0) sms = 1;
     luxgi_sdf_desc sd{};
     layout_data(*d, sd.data);
     sd.format = d->format;
@@ -526,6 +545,18 @@ int luxgi_sdf_build(const luxgi_sdf_build_desc* d, const luxgi_mesh_sdf* meshes,
             rm.w = std::max(m.size[0] >> L, 1);
             rm.h = std::max(m.size[1] >> L, 1);
             rm.d = std::max(m.size[2] >> L, 1);
+            const luxgi_sdf_raster_object& r = pl.records[i];
+            const float* v2w = r.volume_to_world;
+            rm.cx = v2w[12];
+            rm.cy = v2w[13];
+            rm.cz = v2w[14];
+            double rad = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                const double cn = std::sqrt(double(v2w[a * 4]) * v2w[a * 4] + double(v2w[a * 4 + 1]) * v2w[a * 4 + 1] +
+                                            double(v2w[a * 4 + 2]) * v2w[a * 4 + 2]);
+                rad += cn * double(r.volume_local_bounds_extent[a]);
+            }
+            rm.radius = float(rad * 1.0001);
             std::memcpy(host.data() + off, &rm, sizeof(rm));
             off += sizeof(rm);
         }
@@ -552,7 +583,9 @@ int luxgi_sdf_build(const luxgi_sdf_build_desc* d, const luxgi_mesh_sdf* meshes,
             const auto* ck = reinterpret_cast<const luxgi_sdf_chunk*>(base + chunk_off[size_t(c)]);
             const auto* rc = reinterpret_cast<const luxgi_sdf_raster_object*>(base + rec_off[size_t(c)]);
             const auto* rm = reinterpret_cast<const RasterMesh*>(base + mesh_off[size_t(c)]);
-            const dim3 grid(unsigned(pl.chunks.size()), LUXGI_SDF_CHUNK);
+            // whole planes once there are 8 blocks an SM, else 8-row bands
+            const unsigned bands = pl.chunks.size() * LUXGI_SDF_CHUNK >= size_t(sms) * 8 ? 1u : 4u;
+            const dim3 grid(unsigned(pl.chunks.size()), LUXGI_SDF_CHUNK, bands);
             if (h) sdf_raster_kernel<__half><<<grid, 256, 0, st>>>(ck, rc, rm, p, as_t<__half>(sdf));
             else sdf_raster_kernel<float><<<grid, 256, 0, st>>>(ck, rc, rm, p, as_t<float>(sdf));
             note_launch();

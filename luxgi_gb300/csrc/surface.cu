@@ -14,6 +14,8 @@
 //
 // Compiled without FMA contraction: the shadow march then takes exactly the
 // oracle's steps and the blocked / lit decision of every fragment matches.
+#include <cmath>
+
 #include "luxgi_internal.h"
 
 #include "luxgi_common.cuh"
@@ -162,7 +164,10 @@ __device__ __forceinline__ f3 brdf(f3 albedo, f3 n, float roughness, float metal
     const float cos_li = mx(0.0f, dot3(n, l));
     const float cos_lh = mx(0.0f, dot3(n, half_v));
     const float n_dot_v = mx(0.0f, dot3(n, view));
-    const float fw = powf(clampf(1.0f - mx(dot3(half_v, view), 0.0f), 0.0f, 1.0f), 5.0f);
+    // pow(x, 5) of fresnelSchlick as (x^2)^2 x: within 3 ulps of the exact power
+    const float fx = clampf(1.0f - mx(dot3(half_v, view), 0.0f), 0.0f, 1.0f);
+    const float fx2 = fx * fx;
+    const float fw = fx2 * fx2 * fx;
     const float alpha = roughness * roughness;
     const float alpha_sq = alpha * alpha;
     const float denom = (cos_lh * cos_lh) * (alpha_sq - 1.0f) + 1.0f;
@@ -185,6 +190,9 @@ __device__ __forceinline__ f3 brdf(f3 albedo, f3 n, float roughness, float metal
     return f3{out[0], out[1], out[2]};
 }
 
+// The launch's copy of the lights; color[3] (unused by the shader) carries
+// the per-light radiance factor pow(intensity, 1.4) + 0.1
+// (SDFDeferredLight.frag:124), evaluated once on the host.
 struct LightSet {
     luxgi_light l[LUXGI_MAX_LIGHTS];
 };
@@ -203,7 +211,7 @@ __device__ __forceinline__ f3 direct_light(const SdfView& sdf, const Fragment& f
         const f3 d = sub3(f3{L.position[0], L.position[1], L.position[2]}, f.pos);
         dist = len3(d);
         wi = norm3(d);
-        atten = L.radius / (powf(dist, 2.0f) + 1.0f);
+        atten = L.radius / (dist * dist + 1.0f);
     } else {
         const f3 lv = sub3(f3{L.position[0], L.position[1], L.position[2]}, f.pos);
         const float cutoff = 1.0f - L.angle;
@@ -212,7 +220,7 @@ __device__ __forceinline__ f3 direct_light(const SdfView& sdf, const Fragment& f
         const float theta = dot3(wi, f3{L.direction[0], L.direction[1], L.direction[2]});
         const float eps = cutoff - cutoff * 0.9f;
         float a = (theta - cutoff) / eps;
-        a = a * (L.radius / (powf(dist, 2.0f) + 1.0f));
+        a = a * (L.radius / (dist * dist + 1.0f));
         atten = clampf(a, 0.0f, 1.0f);
     }
     // SDF shadow (:95-118)
@@ -233,7 +241,7 @@ __device__ __forceinline__ f3 direct_light(const SdfView& sdf, const Fragment& f
     }
     // shading (:120-128)
     const f3 view = norm3(sub3(cam, f.pos));
-    const float intensity = powf(L.intensity, 1.4f) + 0.1f;
+    const float intensity = L.color[3];
     const f3 lrad{L.color[0] * intensity, L.color[1] * intensity, L.color[2] * intensity};
     const f3 lh = norm3(add3(wi, view));
     const float cos_li = mx(0.0f, dot3(f.normal, wi));
@@ -355,7 +363,10 @@ cudaError_t launch_surface_light(const SdfView& sdf, const luxgi_surface_desc& s
     p.copy_emissive = L.copy_emissive;
     p.max_steps = L.max_steps;
     LightSet ls;
-    for (int i = 0; i < LUXGI_MAX_LIGHTS; ++i) ls.l[i] = i < L.num_lights ? L.lights[i] : luxgi_light{};
+    for (int i = 0; i < LUXGI_MAX_LIGHTS; ++i) {
+        ls.l[i] = i < L.num_lights ? L.lights[i] : luxgi_light{};
+        ls.l[i].color[3] = std::pow(ls.l[i].intensity, 1.4f) + 0.1f;
+    }
     // a tile of the reference's atlas is at most 128 x 128 pixels: 8 blocks of
     // 128 threads give every thread ~16 pixels there and one on an 32 x 32 tile
     const dim3 grid(8, unsigned(L.num_tiles));
