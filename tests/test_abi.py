@@ -179,3 +179,19 @@ def test_fastdiv_formula_exact():
             n &= (1 << 32) - 1
             q = (((n * m) >> 32) + n) >> l
             assert q == n // d, (d, n)
+
+
+@pytest.mark.parametrize("header", ["luxgi_ddgi.h", "luxgi_serve.h", "luxgi_scene.h"])
+def test_headers_are_plain_c(header, tmp_path):
+    """The boundary is a C ABI: each header compiles as C99 on its own, and
+    a C translation unit that calls every declared entry point links
+    against the library (the binding a C, cgo or FFI caller would make)."""
+    src = tmp_path / "use.c"
+    names = sorted(_declared(ROOT / "include" / header))
+    body = "\n".join(f"    (void)&{n};" for n in names)
+    src.write_text(f'#include "{header}"\nint main(void) {{\n{body}\n    return 0;\n}}\n')
+    lib = "luxgi_scene" if header == "luxgi_scene.h" else "luxgi_ddgi"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o",
+                        str(tmp_path / "use"), "-L", str(N.LIB_DIR), f"-l{lib}", f"-Wl,-rpath,{N.LIB_DIR}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -71,10 +71,11 @@ def _close(g, o, lights=3):
     assert np.mean(np.abs(a - b) > 1e-3 * np.maximum(np.abs(b), 1e-3)) < 1e-4
 
 
-@pytest.mark.parametrize("fmt", [N.STORAGE_FP32, N.STORAGE_FP16])
+@pytest.mark.parametrize("fmt,cascades", [(N.STORAGE_FP32, 1), (N.STORAGE_FP16, 1), (N.STORAGE_FP16, 2)])
 @pytest.mark.parametrize("copy_emissive,random_masks", [(True, True), (False, False), (True, False)])
-def test_surface_light_matches_oracle(cuda, fmt, copy_emissive, random_masks):
-    w = tiny_workload(sdf=32, prims=8, atlas=256, sdf_format=fmt)
+def test_surface_light_matches_oracle(cuda, fmt, cascades, copy_emissive, random_masks):
+    w = tiny_workload(sdf=32, prims=8, atlas=256, sdf_format=fmt, cascades=cascades,
+                      room=10.0 if cascades == 1 else 24.0)
     host, dev, inp = _setup(w)
     lights = _lights()
     tiles = np.arange(1, host.num_tiles, dtype=np.uint32)
