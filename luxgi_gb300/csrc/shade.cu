@@ -92,44 +92,64 @@ __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
 }
 
 // ------------------------------------------------------ shading order
-// Exclusive scan of the bin counts into the scatter cursors: one block
-// walks the bins in tiles of kScanThreads (coalesced loads), each tile
-// scanned with warp shuffles and carried into the next.
+// Exclusive scan of the bin counts into the scatter cursors, one block of
+// 32 warps: warp w owns a contiguous segment of the bins.  Pass 1 sums each
+// segment (32-bin coalesced slices, four loads in flight per lane), warp 0
+// scans the 32 segment totals, pass 2 rescans each segment from its base
+// (warp shuffles, the slices' loads again issued four ahead).
 constexpr int kScanThreads = 1024;
+constexpr int kScanWarps = kScanThreads / 32;
 
 __global__ void __launch_bounds__(kScanThreads) bin_scan_kernel(const uint32_t* __restrict__ count,
                                                                uint32_t* __restrict__ cursor, int nb) {
-    __shared__ uint32_t warp_sum[kScanThreads / 32];
-    __shared__ uint32_t carry;
+    __shared__ uint32_t seg_base[kScanWarps];
     const int lane = int(threadIdx.x) & 31, warp = int(threadIdx.x) >> 5;
-    if (threadIdx.x == 0) carry = 0;
+    const int seg = ((nb + kScanWarps - 1) / kScanWarps + 31) & ~31;
+    const int b0 = warp * seg, b1 = min(b0 + seg, nb);
+    uint32_t total = 0;
+    for (int b = b0; b < b1; b += 4 * 32) {
+        uint32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = b + k * 32 + lane;
+            v[k] = (b + k * 32 < b1 && i < b1) ? __ldg(count + i) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) total += __reduce_add_sync(0xffffffffu, v[k]);
+    }
+    if (lane == 0) seg_base[warp] = total;
     __syncthreads();
-    for (int base = 0; base < nb; base += kScanThreads) {
-        const int b = base + int(threadIdx.x);
-        const uint32_t v = b < nb ? __ldg(count + b) : 0u;
-        uint32_t x = v;                                   // inclusive scan within the warp
+    if (warp == 0) {
+        const uint32_t t = seg_base[lane];
+        uint32_t x = t;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
             if (lane >= off) x += y;
         }
-        if (lane == 31) warp_sum[warp] = x;
-        __syncthreads();
-        if (warp == 0) {                                  // scan of the warp totals
-            uint32_t w = warp_sum[lane];
+        seg_base[lane] = x - t;
+    }
+    __syncthreads();
+    uint32_t running = seg_base[warp];
+    for (int b = b0; b < b1; b += 4 * 32) {
+        uint32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = b + k * 32 + lane;
+            v[k] = i < b1 ? __ldg(count + i) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            uint32_t x = v[k];                              // inclusive scan of the slice
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
-                if (lane >= off) w += y;
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+                if (lane >= off) x += y;
             }
-            warp_sum[lane] = w;
+            const int i = b + k * 32 + lane;
+            if (i < b1) cursor[i] = running + x - v[k];
+            running += __shfl_sync(0xffffffffu, x, 31);
         }
-        __syncthreads();
-        const uint32_t before = carry + (warp ? warp_sum[warp - 1] : 0u);
-        if (b < nb) cursor[b] = before + x - v;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += warp_sum[kScanThreads / 32 - 1];
-        __syncthreads();
     }
 }
 
