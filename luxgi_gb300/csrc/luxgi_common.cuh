@@ -726,6 +726,31 @@ __device__ __forceinline__ void bilinear_repeat_v(const void* p, int storage, in
     }
 }
 
+// bilinear_repeat_v for the probe-cell lookups of sampleIrradiance: every
+// tap there lies inside the atlas, at least one texel from its edge (a cell
+// interior starts 2 texels into its (n+2)-texel cell, the atlas has a
+// 1-texel pad: the taps of a cell span [o + 1, o + n + 2] of the (n+2) XY + 2
+// texels), so REPEAT never wraps and a clamp that never binds guards the
+// index arithmetic in its place.  Same arithmetic as bilinear_repeat_v.
+template <int NC>
+__device__ __forceinline__ void bilinear_cell_v(const void* p, int storage, int W, int H, float u, float v, float* out) {
+    const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    const int i0 = imn(imx(int(fx), 0), W - 2), j0 = imn(imx(int(fy), 0), H - 2);
+    const int i1 = i0 + 1, j1 = j0 + 1;
+    float t00[NC], t10[NC], t01[NC], t11[NC];
+    atlas_texel<NC>(p, storage, size_t(j0) * W + i0, t00);
+    atlas_texel<NC>(p, storage, size_t(j0) * W + i1, t10);
+    atlas_texel<NC>(p, storage, size_t(j1) * W + i0, t01);
+    atlas_texel<NC>(p, storage, size_t(j1) * W + i1, t11);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const float r0 = t00[c] * (1.0f - a) + t10[c] * a, r1 = t01[c] * (1.0f - a) + t11[c] * a;
+        out[c] = r0 * (1.0f - b) + r1 * b;
+    }
+}
+
 __device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
 
 // textureCoordFromDirection (DDGICommon.glsl:141-158), split into its
@@ -825,7 +850,7 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         }
         const float dist = len3(ptp);
         float mm[2];
-        bilinear_repeat_v<2>(A.dist, A.storage, u.depth_width, u.depth_height, tu, tv, mm);
+        bilinear_cell_v<2>(A.dist, A.storage, u.depth_width, u.depth_height, tu, tv, mm);
         const float mean = mm[0];
         const float mean2 = mm[1];
         const float variance = fabsf(mean * mean - mean2);
@@ -837,7 +862,7 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         cell_texel_origin(cell_x, cell_y, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny, tu,
                           tv);
         float ir[4];
-        bilinear_repeat_v<4>(A.irr, A.storage, u.irradiance_width, u.irradiance_height, tu, tv, ir);
+        bilinear_cell_v<4>(A.irr, A.storage, u.irradiance_width, u.irradiance_height, tu, tv, ir);
         const f3 pir{pow_decode(ir[0], ge), pow_decode(ir[1], ge), pow_decode(ir[2], ge)};
         const float crush = 0.2f;
         if (weight < crush) weight = weight * (weight * weight * (1.0f / (crush * crush)));
