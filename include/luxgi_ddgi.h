@@ -394,6 +394,16 @@ int luxgi_ddgi_sample_irradiance(const luxgi_ddgi_volume* vol, const float* pos,
                                  const float* nrm, const float* wo, float* out,
                                  int n, void* stream);
 
+/* sample_probe::system + SampleProbe.comp:36-60 (DDGIRenderer.cpp:466-500):
+ * the indirect-lighting image of a screen G-buffer from the volume's
+ * current atlases.  depth: device R32F width x height (1 = background);
+ * normal: device, normal_channels (2..4) floats a pixel, the first two the
+ * octahedral normal; view_proj_inv: inverse(projView), column-major (host);
+ * out: device RGBA16F, (irradiance, 1), or 0 at background pixels. */
+int luxgi_ddgi_sample_probe_image(const luxgi_ddgi_volume* vol, const float* depth, const float* normal,
+                                  int normal_channels, int width, int height, const float camera_pos[3],
+                                  const float view_proj_inv[16], void* out, void* stream);
+
 /* ------------------------------------------------------- scene set-up */
 
 /* GlobalSDFMipmap.comp + 4 flood passes (GlobalDistanceField.cpp:537-573,

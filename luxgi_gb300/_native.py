@@ -234,6 +234,8 @@ DDGI_API = [
     ("luxgi_ddgi_load_atlases", c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     ("luxgi_ddgi_inject_indirect", c_int, [c_void_p, c_void_p]),
     ("luxgi_ddgi_save_atlases", c_int, [c_void_p, c_void_p, c_void_p, POINTER(c_int32), c_void_p]),
+    ("luxgi_ddgi_sample_probe_image", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, POINTER(c_float),
+                                              POINTER(c_float), c_void_p, c_void_p]),
     ("luxgi_ddgi_sample_irradiance", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("luxgi_sdf_build_mip", c_int, [POINTER(SdfDesc), c_void_p, c_void_p, c_void_p]),
     ("luxgi_sdf_build_mip_noalloc", c_int, [POINTER(SdfDesc), c_void_p, c_void_p]),

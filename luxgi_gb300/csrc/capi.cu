@@ -781,6 +781,20 @@ int luxgi_ddgi_sample_irradiance(const luxgi_ddgi_volume* v, const float* pos, c
                                                 static_cast<cudaStream_t>(stream)));
 }
 
+int luxgi_ddgi_sample_probe_image(const luxgi_ddgi_volume* v, const float* depth, const float* normal,
+                                  int normal_channels, int width, int height, const float camera_pos[3],
+                                  const float view_proj_inv[16], void* out, void* stream) {
+    if (!v || width < 0 || height < 0 || !camera_pos || !view_proj_inv) return LUXGI_EINVAL;
+    if (normal_channels < 2 || normal_channels > 4) return LUXGI_EINVAL;
+    if (width > 0 && height > 0 && (!depth || !normal || !out)) return LUXGI_EINVAL;
+    AtlasView A;
+    A.irr = v->irr[v->ping_pong];
+    A.dist = v->dist[v->ping_pong];
+    A.storage = v->desc.storage;
+    return cuda_status(launch_sample_probe(v->desc.uniform, A, depth, normal, normal_channels, width, height,
+                                           camera_pos, view_proj_inv, out, static_cast<cudaStream_t>(stream)));
+}
+
 int luxgi_sdf_build_mip(const luxgi_sdf_desc* sdf, void* mip, void* tmp, void* stream) {
     if (!sdf || !mip || !tmp || !sdf->sdf) return LUXGI_EINVAL;
     const int C = int(sdf->data.cascades_count);

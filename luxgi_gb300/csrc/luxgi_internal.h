@@ -200,6 +200,12 @@ cudaError_t launch_surface_light(const SdfView& sdf, const luxgi_surface_desc& s
                                  __half* out, cudaStream_t st);
 cudaError_t launch_sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, const float* pos,
                                      const float* nrm, const float* wo, float* out, int n, cudaStream_t st);
+struct Mat4 {
+    float m[16];   // column-major
+};
+cudaError_t launch_sample_probe(const luxgi_ddgi_uniform& u, const AtlasView& A, const float* depth,
+                                const float* normal, int nch, int W, int H, const float cam[3], const float vpi[16],
+                                void* out, cudaStream_t st);
 cudaError_t launch_mip(const luxgi_sdf_desc& s, void* mip, void* tmp, cudaStream_t st);
 cudaError_t launch_mip_cascade(const luxgi_sdf_desc& s, int k, bool flood, void* mip, void* tmp, cudaStream_t st);
 cudaError_t launch_cull(const luxgi_surface_data& d, const luxgi_surface_object* objects, uint32_t* chunks,

@@ -634,4 +634,59 @@ cudaError_t launch_sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasVie
     return cudaGetLastError();
 }
 
+// SampleProbe.comp:36-60: one thread per pixel of a screen G-buffer.  The
+// world position comes back from the depth through the inverse
+// view-projection (worldPositionFromDepth, Common/Math.glsl:35-42), the
+// normal from the octahedral normal target (octohedralToDirection,
+// Math.glsl:26-32); background pixels (depth 1) get 0.
+__global__ void sample_probe_kernel(const luxgi_ddgi_uniform u, const AtlasView A, const float* __restrict__ depth,
+                                    const float* __restrict__ normal, int nch, int W, int H, const float3 cam,
+                                    const Mat4 vpi, __half* __restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t i = size_t(y) * W + x;
+    const float d = __ldg(depth + i);
+    float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (d != 1.0f) {
+        const float tx = (float(x) + 0.5f) / float(W), ty = (float(y) + 0.5f) / float(H);
+        const float sx = tx * 2.0f - 1.0f, sy = ty * 2.0f - 1.0f;
+        const float* m = vpi.m;
+        const float wx = (m[0] * sx + m[4] * sy) + (m[8] * d + m[12]);
+        const float wy = (m[1] * sx + m[5] * sy) + (m[9] * d + m[13]);
+        const float wz = (m[2] * sx + m[6] * sy) + (m[10] * d + m[14]);
+        const float ww = (m[3] * sx + m[7] * sy) + (m[11] * d + m[15]);
+        const f3 P{wx / ww, wy / ww, wz / ww};
+        const float ex = __ldg(normal + i * nch), ey = __ldg(normal + i * nch + 1);
+        f3 v{ex, ey, 1.0f - fabsf(ex) - fabsf(ey)};
+        if (v.z < 0.0f) {
+            const float nx = (1.0f - fabsf(v.y)) * sign_nz(v.x);
+            const float ny = (1.0f - fabsf(v.x)) * sign_nz(v.y);
+            v.x = nx;
+            v.y = ny;
+        }
+        const f3 N = norm3(v);
+        const f3 Wo = norm3(sub3(f3{cam.x, cam.y, cam.z}, P));
+        const f3 e = sample_irradiance(u, A, P, N, Wo);
+        o = make_float4(e.x, e.y, e.z, 1.0f);
+    }
+    const __half2 a = __floats2half2_rn(o.x, o.y), b = __floats2half2_rn(o.z, o.w);
+    uint2 raw;
+    raw.x = *reinterpret_cast<const uint32_t*>(&a);
+    raw.y = *reinterpret_cast<const uint32_t*>(&b);
+    reinterpret_cast<uint2*>(out)[i] = raw;
+}
+
+cudaError_t launch_sample_probe(const luxgi_ddgi_uniform& u, const AtlasView& A, const float* depth,
+                                const float* normal, int nch, int W, int H, const float cam[3], const float vpi[16],
+                                void* out, cudaStream_t st) {
+    if (W <= 0 || H <= 0) return cudaSuccess;
+    Mat4 m;
+    for (int k = 0; k < 16; ++k) m.m[k] = vpi[k];
+    const dim3 blk(32, 8), grd(unsigned((W + 31) / 32), unsigned((H + 7) / 8));
+    sample_probe_kernel<<<grd, blk, 0, st>>>(u, A, depth, normal, nch, W, H, make_float3(cam[0], cam[1], cam[2]), m,
+                                             static_cast<__half*>(out));
+    note_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace luxgi

@@ -151,6 +151,22 @@ class DDGIVolume:
         N.check(N.ddgi().luxgi_ddgi_load_atlases(self._h, irr.ctypes.data, dist.ctypes.data, frames, _stream(stream)),
                 "load_atlases")
 
+    def sample_probe_image(self, depth, normal, camera_pos, view_proj_inv, out=None, stream=None):
+        """SampleProbe.comp over a screen G-buffer: depth (H, W) float32 and
+        normal (H, W, C) float32 device tensors, C >= 2 with the octahedral
+        normal first; returns the (H, W, 4) float16 indirect-lighting image."""
+        import torch
+
+        H, W = depth.shape
+        nch = normal.shape[-1]
+        if out is None:
+            out = torch.empty((H, W, 4), dtype=torch.float16, device=depth.device)
+        cam = (ctypes.c_float * 3)(*[float(c) for c in camera_pos])
+        vpi = (ctypes.c_float * 16)(*[float(c) for c in np.asarray(view_proj_inv, np.float32).reshape(-1)])
+        N.check(N.ddgi().luxgi_ddgi_sample_probe_image(self._h, depth.data_ptr(), normal.data_ptr(), nch, W, H, cam,
+                                                       vpi, out.data_ptr(), _stream(stream)), "sample_probe_image")
+        return out
+
     def save_atlases(self, stream=None):
         """(irradiance, distance, frames): host copies of the current atlases."""
         a = self.atlas_info()

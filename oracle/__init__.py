@@ -65,6 +65,7 @@ def lib() -> ctypes.CDLL:
             "oracle_surface_light": (c_int, [vp, vp, vp, c_int, vp, vp, c_int, vp, c_float, c_int, c_int, c_int,
                                              vp, vp]),
             "oracle_sdf_build": (c_int, [vp, vp, c_int, vp, c_int, vp, vp, vp]),
+            "oracle_sample_probe_image": (c_int, [vp, vp, vp, vp, vp, c_int, c_int, c_int, vp, vp, vp]),
             "oracle_sdf_plan": (c_int, [vp, vp, c_int, vp, c_int, c_int, vp, c_int, vp, vp, vp, c_int, vp]),
             "oracle_texel_dirs": (c_int, [c_int, c_int, vp]),
             "oracle_oct_encode": (c_int, [vp, c_int, vp]),
@@ -311,6 +312,23 @@ def sdf_plan(desc, meshes, objects, cascade: int):
     return recs[:nr.value], list(mesh[:nr.value]), chunks[:nc.value]
 
 
+def sample_probe_image(uniform, irr, dist, depth, normal, camera, view_proj_inv) -> np.ndarray:
+    """SampleProbe.comp over a G-buffer: depth (H, W) float32, normal (H, W, C)
+    float32; returns the (H, W, 4) RGBA16F image as uint16 bits."""
+    H, W = depth.shape
+    nch = normal.shape[-1]
+    out = np.zeros((H, W, 4), dtype=np.uint16)
+    i = np.ascontiguousarray(irr, dtype=np.float32)
+    d = np.ascontiguousarray(dist, dtype=np.float32)
+    dp = np.ascontiguousarray(depth, dtype=np.float32)
+    nm = np.ascontiguousarray(normal, dtype=np.float32)
+    cam = np.ascontiguousarray(camera, dtype=np.float32)
+    vpi = np.ascontiguousarray(view_proj_inv, dtype=np.float32).reshape(-1)
+    lib().oracle_sample_probe_image(ctypes.byref(uniform), _p(i), _p(d), _p(dp), _p(nm), nch, W, H, _p(cam), _p(vpi),
+                                    _p(out))
+    return out
+
+
 def sample_irradiance(uniform, irr, dist, pos, nrm, wo, precision: int = 0) -> np.ndarray:
     i = np.ascontiguousarray(irr, dtype=np.float32)
     d = np.ascontiguousarray(dist, dtype=np.float32)
@@ -373,6 +391,7 @@ def ref_lib():
             "ref_surface_light": (c_int, [vp, vp, vp, c_int, vp, vp, c_int, vp, c_float, c_int, vp]),
             "ref_inject": (c_int, [vp, vp, vp, vp, vp]),
             "ref_sdf_raster": (c_int, [vp, vp, c_int, vp, vp, vp, c_int, vp, vp]),
+            "ref_sample_probe_image": (c_int, [vp, vp, vp, vp, vp, c_int, c_int, c_int, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -465,6 +484,17 @@ def ref_sdf_raster(desc, data, cascade: int, meshes, recs, rec_mesh, chunks, sdf
     M = (ctypes.c_int32 * max(1, len(rec_mesh)))(*rec_mesh)
     Ch = (N.SdfChunk * max(1, len(chunks)))(*chunks)
     ref_lib().ref_sdf_raster(ctypes.byref(desc), ctypes.byref(data), cascade, R, M, Ch, len(chunks), md, _p(out))
+    return out
+
+
+def ref_sample_probe_image(uniform, irr, dist, depth, normal, camera, view_proj_inv) -> np.ndarray:
+    """SampleProbe.comp through the reference's compiled functions: (H, W, 4) float."""
+    H, W = depth.shape
+    nch = normal.shape[-1]
+    out = np.zeros((H, W, 4), dtype=np.float32)
+    args = [np.ascontiguousarray(a, dtype=np.float32) for a in (irr, dist, depth, normal, camera, view_proj_inv)]
+    ref_lib().ref_sample_probe_image(ctypes.byref(uniform), _p(args[0]), _p(args[1]), _p(args[2]), _p(args[3]), nch,
+                                     W, H, _p(args[4]), _p(args[5].reshape(-1)), _p(out))
     return out
 
 

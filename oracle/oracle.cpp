@@ -1411,6 +1411,41 @@ int oracle_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s,
     return 0;
 }
 
+// SampleProbe.comp:36-60 over a W x H G-buffer (depth R32F, nch floats of
+// normal a pixel, octahedral xy first), float atlases; out RGBA16F bits:
+// (irradiance, 1), or 0 where depth == 1.  worldPositionFromDepth
+// (Common/Math.glsl:35-42) with glm's association of the matrix product.
+int oracle_sample_probe_image(const luxgi_ddgi_uniform* u, const float* irr, const float* dist, const float* depth,
+                              const float* normal, int nch, int W, int H, const float cam[3], const float vpi[16],
+                              uint16_t* out) {
+    Atlases A;
+    A.irr.f32 = irr; A.irr.W = u->irradiance_width; A.irr.H = u->irradiance_height; A.irr.C = 4;
+    A.dist.f32 = dist; A.dist.W = u->depth_width; A.dist.H = u->depth_height; A.dist.C = 2;
+#pragma omp parallel for
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t i = size_t(y) * W + x;
+            const float d = depth[i];
+            float o[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (d != 1.0f) {
+                const float tx = (float(x) + 0.5f) / float(W), ty = (float(y) + 0.5f) / float(H);
+                const float sx = tx * 2.0f - 1.0f, sy = ty * 2.0f - 1.0f;
+                const float* m = vpi;
+                const float wx = (m[0] * sx + m[4] * sy) + (m[8] * d + m[12]);
+                const float wy = (m[1] * sx + m[5] * sy) + (m[9] * d + m[13]);
+                const float wz = (m[2] * sx + m[6] * sy) + (m[10] * d + m[14]);
+                const float ww = (m[3] * sx + m[7] * sy) + (m[11] * d + m[15]);
+                const V3<float> P{wx / ww, wy / ww, wz / ww};
+                const V3<float> N = oct_decode(V2<float>{normal[i * nch], normal[i * nch + 1]});
+                const V3<float> Wo = normalize(sub(V3<float>{cam[0], cam[1], cam[2]}, P));
+                const V3<float> e = sample_irradiance<float>(*u, A, P, N, Wo);
+                o[0] = e.x; o[1] = e.y; o[2] = e.z; o[3] = 1.0f;
+            }
+            for (int c = 0; c < 4; ++c) out[i * 4 + size_t(c)] = f2h_bits(o[c]);
+        }
+    return 0;
+}
+
 // sampleIrradiance for n points (float3 arrays), float atlases.
 int oracle_sample_irradiance(const luxgi_ddgi_uniform* u, const float* irr, const float* dist, const float* pos,
                              const float* nrm, const float* wo, float* out, int n, int precision) {

@@ -14,6 +14,8 @@
 //   ref_surface_light  CopyEmissive.frag:22-26, SDFDeferredLight.frag:41-129
 //                      (BRDF from Raytraced/BRDF.glsl:65-81)
 //   ref_inject SDFAtlasIndirectLight.frag:44-67
+//   ref_sample_probe_image SampleProbe.comp:36-60 (worldPositionFromDepth,
+//              Common/Math.glsl:35-42)
 //   ref_sdf_raster SDFRasterizeModel.glsl:42-63 (distanceToModelSDF,
 //              SDFCommon.glsl:38-62) over a cascade's chunks
 // The two raster passes run over the pixels of the tile quads of addTiles2
@@ -537,6 +539,41 @@ int ref_sdf_raster(const luxgi_sdf_build_desc* d, const luxgi_sdf_data* data, in
                     sdf[size_t(voxelCoord.x) + size_t(res * C) * (size_t(voxelCoord.y) + size_t(res) * size_t(voxelCoord.z))] = v;
                 }
     }
+    return 0;
+}
+
+// SampleProbe.comp main (:36-60) over a W x H G-buffer: out float4 per pixel.
+int ref_sample_probe_image(const luxgi_ddgi_uniform* u, const float* irr, const float* dist, const float* depth,
+                           const float* normal, int nch, int W, int H, const float cam[3], const float vpi[16],
+                           float* out) {
+    const DDGIUniform ddgi = as<DDGIUniform>(*u);
+    const sampler2D irrS = tex2d(irr, nullptr, nullptr, ddgi.irradianceTextureWidth, ddgi.irradianceTextureHeight, 4, true);
+    const sampler2D distS = tex2d(dist, nullptr, nullptr, ddgi.depthTextureWidth, ddgi.depthTextureHeight, 2, true);
+    mat4 viewProjInv;
+    for (int c = 0; c < 4; ++c) viewProjInv[c] = vec4(vpi[4 * c], vpi[4 * c + 1], vpi[4 * c + 2], vpi[4 * c + 3]);
+    const vec3 cameraPosition(cam[0], cam[1], cam[2]);
+#pragma omp parallel for
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t i = size_t(y) * W + x;
+            const ivec2 size = ivec2(W, H);
+            const ivec2 currentCoord = ivec2(x, y);
+            const vec2 pixelCenter = vec2(currentCoord) + vec2(0.5);
+            const vec2 texCoord = pixelCenter / vec2(size);
+            float d = depth[i];
+            vec4 result(0.0f);
+            if (d != 1.0f) {
+                const vec3 P = worldPositionFromDepth(texCoord, d, viewProjInv);
+                const vec3 N = octohedralToDirection(vec2(normal[i * nch], normal[i * nch + 1]));
+                const vec3 Wo = normalize(cameraPosition - P);
+                vec3 irradiance = sampleIrradiance(ddgi, P, N, Wo, irrS, distS);
+                result = vec4(irradiance, 1.0f);
+            }
+            out[4 * i] = result.x;
+            out[4 * i + 1] = result.y;
+            out[4 * i + 2] = result.z;
+            out[4 * i + 3] = result.w;
+        }
     return 0;
 }
 

@@ -55,3 +55,54 @@ def interior_mask(uniform, depth: bool) -> np.ndarray:
     m = np.zeros((H, W), dtype=bool)
     m[1:H - 1, 1:W - 1] = True
     return m
+
+
+def synthetic_gbuffer(width, height, seed=0, camera=(0.0, 0.5, -3.0), target=(0.0, 0.0, 2.0), fov=1.0,
+                      near=0.1, far=100.0, dist_range=(1.0, 8.0), background=0.1, channels=4):
+    """A screen G-buffer for SampleProbe.comp: a perspective camera (depth
+    0..1), per-pixel view distances in dist_range, a fraction of background
+    pixels (depth 1), random octahedral normals.  Returns (depth (H, W)
+    float32, normal (H, W, channels) float32, camera float32[3],
+    inverse(proj * view) float32[16] column-major)."""
+    rng = np.random.default_rng(seed)
+    cam = np.asarray(camera, np.float64)
+    f = np.asarray(target, np.float64) - cam
+    f /= np.linalg.norm(f)
+    up = np.array([0.0, 1.0, 0.0])
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = s, u, -f
+    view[:3, 3] = -view[:3, :3] @ cam
+    aspect = width / height
+    t = 1.0 / np.tan(fov / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0], proj[1, 1] = t / aspect, t
+    proj[2, 2], proj[2, 3] = far / (near - far), near * far / (near - far)
+    proj[3, 2] = -1.0
+    pv = proj @ view
+    ys, xs = np.mgrid[0:height, 0:width]
+    sx = (xs + 0.5) / width * 2 - 1
+    sy = (ys + 0.5) / height * 2 - 1
+    dist = rng.uniform(dist_range[0], dist_range[1], size=(height, width))
+    # view-space point at distance `dist` along the pixel's ray
+    dv = np.stack([sx * aspect / t, sy / t, -np.ones_like(sx)], axis=-1)
+    dv /= np.linalg.norm(dv, axis=-1, keepdims=True)
+    pv_pts = dv * dist[..., None]
+    clip = pv_pts @ proj[:3, :3].T + proj[:3, 3]
+    w = pv_pts @ proj[3, :3] + proj[3, 3]
+    depth = (clip[..., 2] / w).astype(np.float32)
+    depth[rng.uniform(size=depth.shape) < background] = 1.0
+    n = rng.normal(size=(height, width, 3))
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    l1 = np.abs(n).sum(-1, keepdims=True)
+    o = n[..., :2] / l1
+    neg = n[..., 2] < 0
+    fx = (1 - np.abs(o[..., 1])) * np.where(o[..., 0] >= 0, 1.0, -1.0)
+    fy = (1 - np.abs(o[..., 0])) * np.where(o[..., 1] >= 0, 1.0, -1.0)
+    o[neg, 0], o[neg, 1] = fx[neg], fy[neg]
+    normal = np.zeros((height, width, channels), np.float32)
+    normal[..., :2] = o
+    vpi = np.linalg.inv(pv).T.astype(np.float32).reshape(-1)       # column-major
+    return depth, normal, cam.astype(np.float32), vpi

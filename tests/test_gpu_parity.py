@@ -253,6 +253,32 @@ def test_sample_irradiance_matches_oracle(cuda):
     assert rel_err(out.cpu().numpy(), ref, floor=1e-2) < 1e-4
 
 
+@pytest.mark.parametrize("storage,channels", [(N.STORAGE_FP32, 4), (N.STORAGE_FP16, 2)])
+def test_sample_probe_image_matches_oracle(cuda, storage, channels):
+    """SampleProbe.comp over a synthetic screen G-buffer (luxgi_ddgi_sample_probe_image)
+    against the oracle: the same RGBA16F image within one half-float
+    rounding; background pixels exactly 0."""
+    import torch
+
+    from tests._helpers import synthetic_gbuffer
+
+    w = tiny_workload(probe_counts=(4, 3, 4), rays=64, storage=storage)
+    host, dev, vol, inp = setup(w, debug=False)
+    for f in range(3):
+        vol.update(frame_rotation(28, f))
+    irr, dist = vol.atlases()
+    depth, normal, cam, vpi = synthetic_gbuffer(160, 96, seed=3, channels=channels)
+    out = vol.sample_probe_image(torch.from_numpy(depth).cuda(), torch.from_numpy(normal).cuda(), cam, vpi)
+    sync()
+    g = out.cpu().float().numpy()
+    o = oracle.sample_probe_image(vol.uniform, _np(irr), _np(dist), depth, normal, cam, vpi)
+    o = o.view(np.float16).astype(np.float32)
+    bg = depth == 1.0
+    assert (g[bg] == 0).all()
+    assert rel_err(g[~bg], o[~bg], floor=1e-2) < 1.5e-3
+    assert np.mean(g[~bg] != o[~bg]) < 0.01
+
+
 @pytest.mark.parametrize("kw", [
     dict(probe_counts=(1, 1, 1), rays=1),
     dict(probe_counts=(1, 1, 1), rays=33, irr=1, dist=2),

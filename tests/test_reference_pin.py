@@ -226,3 +226,26 @@ def test_sdf_raster_matches_reference(ref, cascades, res):
         b = oracle.ref_sdf_raster(d, data, c, meshes, recs, mesh, chunks, b)
     assert (sdf < 1.0).mean() > 0.5
     assert np.max(np.abs(sdf - b)) <= 2.4e-7
+
+
+def test_sample_probe_image_matches_reference(ref):
+    """SampleProbe.comp (worldPositionFromDepth + octohedralToDirection +
+    sampleIrradiance) over a synthetic G-buffer: the oracle's RGBA16F image
+    against the reference's compiled functions, within one half-float
+    rounding; background pixels 0."""
+    from tests._helpers import synthetic_gbuffer
+
+    w = tiny_workload(probe_counts=(4, 3, 4), rays=64)
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    rots = [frame_rotation(46, f) for f in range(3)]
+    irr, dist, _, _ = oracle.run_frames(w.volume.desc(), inp, rots, precision=0)
+    depth, normal, cam, vpi = synthetic_gbuffer(96, 64, seed=2)
+    u = w.volume.uniform()
+    a = oracle.sample_probe_image(u, irr, dist, depth, normal, cam, vpi).view(np.float16).astype(np.float32)
+    b = oracle.ref_sample_probe_image(u, irr, dist, depth, normal, cam, vpi)
+    bg = depth == 1.0
+    assert bg.any() and (~bg).any()
+    assert (a[bg] == 0).all() and (b[bg] == 0).all()
+    assert np.isfinite(a).all() and (a[~bg][:, 3] == 1).all()
+    assert rel_err(a[~bg], b[~bg], floor=1e-2) < 1.5e-3
