@@ -139,6 +139,7 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         cnt[kBlendI] = P.tc ? 0 : blend_blocks(b, false, t.blend_probes);
         cnt[kBlendD] = P.tc ? 0 : blend_blocks(b, true, t.blend_probes);
         cnt[kWork] = PR;
+        cnt[kPack] = P.tc ? (int64_t(v->P) * v->R + 255) / 256 : 0;
         for (int s = 0; s < kNumStages; ++s) {
             P.starts[size_t(s) * (n + 1) + i] = int(acc[s]);
             acc[s] += cnt[s];
@@ -250,6 +251,7 @@ cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cud
     } else if (e == cudaSuccess) {
         e = launch_shade_batch(tp, d_starts + kShade * n1, n, P.blocks[kShade], P.light_mode, P.t.shade_variant, st);
     }
+    if (e == cudaSuccess && P.tc) e = launch_tc_pack_batch(tp, d_starts + kPack * n1, n, P.blocks[kPack], st);
     if (e != cudaSuccess) return e;
     if (!P.tc)
         return launch_blend_batch(bp, d_starts + kBlendI * n1, P.blocks[kBlendI], P.smem_i, d_starts + kBlendD * n1,

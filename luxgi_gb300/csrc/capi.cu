@@ -388,6 +388,7 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
         mark(2);
         cudaError_t es = p.bin_count ? launch_shade_sort(p, st) : cudaSuccess;
         if (es == cudaSuccess) es = launch_shade(p, st);
+        if (es == cudaSuccess) es = launch_tc_pack(p, st);
         s = cuda_status(es);
         mark(3);
     }

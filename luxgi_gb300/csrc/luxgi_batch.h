@@ -10,7 +10,7 @@ namespace luxgi {
 
 // block-offset tables of the batched launches; kWork holds each volume's
 // first batch-wide march work index instead
-enum Stage { kRaygen, kWeights, kMarch, kShade, kBlendI, kBlendD, kWork, kNumStages };
+enum Stage { kRaygen, kWeights, kMarch, kShade, kBlendI, kBlendD, kWork, kPack, kNumStages };
 
 // What a set of volumes needs to run one frame as batched launches.
 struct Plan {

@@ -161,6 +161,9 @@ cudaError_t launch_shade_batch(const TraceParams* vp, const int* starts, int n, 
                                int shade_variant, cudaStream_t st);
 cudaError_t launch_march(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
+// tensor-core blend operands from the shaded rays (coalesced, after shading)
+cudaError_t launch_tc_pack(const TraceParams& p, cudaStream_t st);
+cudaError_t launch_tc_pack_batch(const TraceParams* vp, const int* starts, int n, int blocks, cudaStream_t st);
 // Scan of the shading bins and scatter of the work items into `shade_seq`.
 cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st);
 // The same over raw arrays: bins [2][nb] (counts, cursors), keys and seq [work].

@@ -5,6 +5,7 @@
 // compared with the CPU restatement by tolerance (1e-4 relative), while the
 // march, whose hit test must reproduce the restatement's branches bit for
 // bit, stays in trace.cu with IEEE arithmetic.
+#include <algorithm>
 #include <cuda_fp16.h>
 
 #include "luxgi_internal.h"
@@ -61,26 +62,6 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
         dist = __high2float(bd);
     } else {
         reinterpret_cast<float4*>(p.out)[o] = make_float4(rad.x, rad.y, rad.z, dist);
-    }
-    if (p.tc_irr) {
-        // tensor-core operands: radiance rows and the blend's per-ray depth
-        // split into FP16 hi + lo (ProbeUpdate.glsl:204-207)
-        __half* a = p.tc_irr + size_t(probe) * 4 * p.R + ray;
-        a[0] = __float2half_rn(rad.x);
-        a[p.R] = __float2half_rn(rad.y);
-        a[2 * p.R] = __float2half_rn(rad.z);
-        a[3 * p.R] = __float2half_rn(0.0f);
-        float dd = mn(p.u.max_distance, dist - 0.01f);
-        if (dd == -1.0f) dd = p.u.max_distance;
-        const float d2 = dd * dd;
-        const __half dh = __float2half_rn(dd), d2h = __float2half_rn(d2);
-        const __half dl = __float2half_rn(dd - __half2float(dh));
-        const __half d2l = __float2half_rn(d2 - __half2float(d2h));
-        __half* b = p.tc_dist + size_t(probe) * 4 * p.R;
-        b[ray] = dh;
-        b[p.R + ray] = dl;
-        b[2 * p.R + ray] = d2h;
-        b[3 * p.R + ray] = d2l;
     }
 }
 
@@ -251,6 +232,76 @@ __global__ void __launch_bounds__(128)
     const int64_t idx = int64_t(int(blockIdx.x) - __ldg(starts + v)) * 128 + threadIdx.x;
     if (idx >= p.work) return;
     shade_ray<MODE, UNROLL>(p, idx);
+}
+
+// ------------------------------------------------ tensor-core operands
+// The tensor-core blend's operands from the shaded rays: radiance rows and
+// the blend's per-ray depth split into FP16 hi + lo (ProbeUpdate.glsl:
+// 204-207), K-major [P][4][R].  One thread per (probe, ray), ray fastest, so
+// that the ray reads and the operand writes both coalesce; the shading runs
+// in hit-chunk order, where these 2-byte stores scattered one sector each.
+__device__ __forceinline__ void tc_pack_one(const TraceParams& p, int64_t local) {
+    const int probe = int(p.index32 ? fdiv(uint32_t(local), p.div_r) : uint32_t(local / p.R));
+    const int ray = int(local - int64_t(probe) * p.R);
+    const size_t o = size_t(probe) * p.R + ray;
+    float r, g, b, dist;
+    if (p.storage == LUXGI_STORAGE_FP16) {
+        const uint2 raw = __ldg(static_cast<const uint2*>(p.out) + o);
+        const __half2 rg = *reinterpret_cast<const __half2*>(&raw.x);
+        const __half2 bd = *reinterpret_cast<const __half2*>(&raw.y);
+        r = __low2float(rg); g = __high2float(rg); b = __low2float(bd); dist = __high2float(bd);
+    } else {
+        const float4 v = __ldg(static_cast<const float4*>(p.out) + o);
+        r = v.x; g = v.y; b = v.z; dist = v.w;
+    }
+    __half* a = p.tc_irr + size_t(probe) * 4 * p.R + ray;
+    a[0] = __float2half_rn(r);
+    a[p.R] = __float2half_rn(g);
+    a[2 * p.R] = __float2half_rn(b);
+    a[3 * p.R] = __float2half_rn(0.0f);
+    float dd = mn(p.u.max_distance, dist - 0.01f);
+    if (dd == -1.0f) dd = p.u.max_distance;
+    const float d2 = dd * dd;
+    const __half dh = __float2half_rn(dd), d2h = __float2half_rn(d2);
+    const __half dl = __float2half_rn(dd - __half2float(dh));
+    const __half d2l = __float2half_rn(d2 - __half2float(d2h));
+    __half* bq = p.tc_dist + size_t(probe) * 4 * p.R + ray;
+    bq[0] = dh;
+    bq[p.R] = dl;
+    bq[2 * p.R] = d2h;
+    bq[3 * p.R] = d2l;
+}
+
+__global__ void __launch_bounds__(256) tc_pack_kernel(const TraceParams p) {
+    const int64_t n = int64_t(p.P) * p.R;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        tc_pack_one(p, i);
+}
+
+// Batched: block b belongs to the volume whose block range holds it.
+__global__ void __launch_bounds__(256) tc_pack_batch_kernel(const TraceParams* __restrict__ vp,
+                                                            const int* __restrict__ starts, int n) {
+    const int v = batch_volume(starts, n, int(blockIdx.x));
+    const TraceParams& p = vp[v];
+    const int64_t local = int64_t(int(blockIdx.x) - __ldg(starts + v)) * 256 + threadIdx.x;
+    if (local >= int64_t(p.P) * p.R) return;
+    tc_pack_one(p, local);
+}
+
+cudaError_t launch_tc_pack(const TraceParams& p, cudaStream_t st) {
+    const int64_t n = int64_t(p.P) * p.R;
+    if (n <= 0 || !p.tc_irr) return cudaSuccess;
+    const unsigned blocks = unsigned(std::min<int64_t>((n + 255) / 256, 65535));
+    tc_pack_kernel<<<blocks, 256, 0, st>>>(p);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_pack_batch(const TraceParams* vp, const int* starts, int n, int blocks, cudaStream_t st) {
+    if (blocks <= 0) return cudaSuccess;
+    tc_pack_batch_kernel<<<unsigned(blocks), 256, 0, st>>>(vp, starts, n);
+    note_launch();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st) {

@@ -180,5 +180,6 @@ def test_batch_launch_count(cuda, blend):
     torch.cuda.synchronize()
     per_frame = lib.luxgi_launch_count() - c0
     # raygen, weights, march (one pass: small batches do not compact by
-    # default), shade (march order) + blend: 2 FP32 launches, or 2 per volume
-    assert per_frame == 4 + (2 if blend == N.BLEND_FP32 else 2 * 3)
+    # default), shade (march order) + blend: 2 FP32 launches, or the
+    # operand pack and 2 tensor-core launches per volume
+    assert per_frame == 4 + (2 if blend == N.BLEND_FP32 else 1 + 2 * 3)
