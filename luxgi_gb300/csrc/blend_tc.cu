@@ -316,11 +316,17 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                 float v[16];
                 tmem_ld16(tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * g.N + c0), v);
                 if (!live) continue;
+                // texel (tx, ty) of column t, stepped along the chunk instead
+                // of divided out per column
+                int ty = c0 / n, tx = c0 - ty * n;
 #pragma unroll 4
-                for (int j = 0; j < 16; ++j) {
+                for (int j = 0; j < 16; ++j, ++tx) {
                     const int t = c0 + j;
                     if (t >= g.T) break;
-                    const int tx = t % n, ty = t / n;
+                    if (tx == n) {
+                        tx = 0;
+                        ++ty;
+                    }
                     float x = v[j] * __ldg(g.norm + t);
                     if (!DIST) x = __powf(x, ig);   // within the tensor path's 2e-3
                     const size_t ti = (size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2)) * g.nc + c;
@@ -330,8 +336,14 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
             }
             if (!DIST && p < g.P && c == 3) {
                 // alpha = 1 (ProbeUpdate.glsl:279) for every texel of the cell
-                for (int t = t_begin; t < t_end; ++t)
-                    store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, t % n, t / n, 3, 1.0f);
+                int ty = t_begin / n, tx = t_begin - ty * n;
+                for (int t = t_begin; t < t_end; ++t, ++tx) {
+                    if (tx == n) {
+                        tx = 0;
+                        ++ty;
+                    }
+                    store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, tx, ty, 3, 1.0f);
+                }
             }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);
