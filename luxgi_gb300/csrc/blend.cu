@@ -145,23 +145,21 @@ template <typename AT, int NC>
 __device__ __forceinline__ void store_texel(void* atlas, int W, int n, int cx, int cy, int tx, int ty, const float* v) {
     const int ox = cx * (n + 2) + 1, oy = cy * (n + 2) + 1;   // cell origin (border corner)
     const int X = tx + 1, Y = ty + 1;                        // cell-relative interior coords
-    int dx[9], dy[9];
-    int nd = 0;
-    dx[nd] = X; dy[nd] = Y; ++nd;
-    if (Y == 1) { dx[nd] = n + 1 - X; dy[nd] = 0; ++nd; }
-    if (Y == n) { dx[nd] = n + 1 - X; dy[nd] = n + 1; ++nd; }
-    if (X == 1) { dx[nd] = 0; dy[nd] = n + 1 - Y; ++nd; }
-    if (X == n) { dx[nd] = n + 1; dy[nd] = n + 1 - Y; ++nd; }
-    // corners: (0,0)<-(n,n), (n+1,0)<-(1,n), (0,n+1)<-(n,1), (n+1,n+1)<-(1,1)
-    if (X == n && Y == n) { dx[nd] = 0; dy[nd] = 0; ++nd; }
-    if (X == 1 && Y == n) { dx[nd] = n + 1; dy[nd] = 0; ++nd; }
-    if (X == n && Y == 1) { dx[nd] = 0; dy[nd] = n + 1; ++nd; }
-    if (X == 1 && Y == 1) { dx[nd] = n + 1; dy[nd] = n + 1; ++nd; }
-    for (int k = 0; k < nd; ++k) {
-        const size_t base = (size_t(oy + dy[k]) * W + (ox + dx[k])) * NC;
+    auto put = [&](int x, int y) {
+        const size_t base = (size_t(oy + y) * W + (ox + x)) * NC;
 #pragma unroll
         for (int c = 0; c < NC; ++c) AtlasIO<AT>::st(atlas, base + c, v[c]);
-    }
+    };
+    put(X, Y);
+    if (Y == 1) put(n + 1 - X, 0);
+    if (Y == n) put(n + 1 - X, n + 1);
+    if (X == 1) put(0, n + 1 - Y);
+    if (X == n) put(n + 1, n + 1 - Y);
+    // corners: (0,0)<-(n,n), (n+1,0)<-(1,n), (0,n+1)<-(n,1), (n+1,n+1)<-(1,1)
+    if (X == n && Y == n) put(0, 0);
+    if (X == 1 && Y == n) put(n + 1, 0);
+    if (X == n && Y == 1) put(0, n + 1);
+    if (X == 1 && Y == 1) put(n + 1, n + 1);
 }
 
 // --------------------------------------------------------------- blend
