@@ -209,7 +209,7 @@ typedef struct luxgi_ddgi_volume_desc {
                                       runs every ray for at most this many
                                       steps, queues the unfinished ones and
                                       resumes them with full warps (twice,
-                                      then to the end); 0 default (8 when the
+                                      then to the end); 0 default (12 when the
                                       volume has >= 2^20 probe-rays, else one
                                       pass); -1 one pass.  Per-ray variants
                                       1-5.                                   */

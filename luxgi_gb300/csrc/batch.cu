@@ -128,7 +128,7 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         volume_blend_params(v, b);
         const int64_t PR = trace_work(v->P, v->R, (v->desc.ray_order == 1 && v->desc.march_variant < 6) ? 1 : 0);
         luxgi_ddgi_volume_desc vd = v->desc;
-        vd.march_budget = t.march_budget == 0 ? 8 : t.march_budget;
+        vd.march_budget = t.march_budget == 0 ? kDefaultMarchBudget : t.march_budget;
         P.budget = std::min(P.budget, march_budget_for(vd, PR, int(v->sdf.data.cascades_count)));
         P.work += PR;
         int64_t cnt[kNumStages];
@@ -683,10 +683,10 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
             consider(c);
         }
     }
-    for (int mb : {-1, 6, 8, 12}) {
+    for (int mb : {-1, 8, 12, 16}) {
         luxgi_ddgi_batch_tuning c = best;
         c.march_budget = mb;
-        const int cur = best.march_budget == 0 ? 8 : best.march_budget;
+        const int cur = best.march_budget == 0 ? kDefaultMarchBudget : best.march_budget;
         if (mb != cur) consider(c);
     }
     {

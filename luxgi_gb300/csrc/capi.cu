@@ -111,9 +111,10 @@ int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int c
     if (d.march_budget < 0 || mv >= 6) return 0;
     // queue entries hold 32-bit work indices and 16-bit step totals
     if (work >= (int64_t(1) << 32) || int64_t(cascades) * d.max_steps >= 65536) return 0;
-    // default: compacted passes after 8 steps for large launches; small ones
-    // cannot amortise the two extra passes
-    if (d.march_budget == 0) return work >= kLargeWork ? 8 : 0;
+    // default: compacted passes after 12 steps for large launches (8 and 16
+    // measured slower on GB300); small ones cannot amortise the two extra
+    // passes
+    if (d.march_budget == 0) return work >= kLargeWork ? kDefaultMarchBudget : 0;
     return d.march_budget;
 }
 

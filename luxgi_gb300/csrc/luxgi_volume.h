@@ -83,6 +83,9 @@ int march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int cascades
 // Launches of at least this many march work items take the compacted march
 // and the binned shading by default.
 constexpr int64_t kLargeWork = int64_t(1) << 20;
+// Steps of the first compacted march pass when the volume leaves it to the
+// library (march_budget 0).
+constexpr int kDefaultMarchBudget = 12;
 // Whether a volume's hits are shaded in bin order (shade_order and size).
 bool shade_binned(const luxgi_ddgi_volume_desc& d, int64_t work);
 // Device bytes a volume of description d allocates once bound to the scene
