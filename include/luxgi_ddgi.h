@@ -209,9 +209,10 @@ typedef struct luxgi_ddgi_volume_desc {
                                       runs every ray for at most this many
                                       steps, queues the unfinished ones and
                                       resumes them with full warps (twice,
-                                      then to the end); 0 default (12 when the
-                                      volume has >= 2^20 probe-rays, else one
-                                      pass); -1 one pass.  Per-ray variants
+                                      then to the end); 0 default (12, then 8
+                                      in the second pass, when the volume has
+                                      >= 2^20 probe-rays, else one pass); -1
+                                      one pass.  Per-ray variants
                                       1-5.                                   */
     int32_t shade_order;           /* tuning, results identical: 1 bin the
                                       hits by their surface-cache chunk first

@@ -179,7 +179,7 @@ void plan_fill(const Plan& P, const float* rots, uint8_t* host) {
         const luxgi_ddgi_volume* v = P.vols[i];
         volume_trace_params(v, rots + 9 * i, tp[i]);
         tp[i].budget1 = P.q ? P.budget : 0;
-        tp[i].budget2 = P.budget;
+        tp[i].budget2 = march_budget2(P.t.march_budget, P.budget);
         tp[i].qa = P.q;
         tp[i].qb = P.q ? P.q + 2 * size_t(P.qa_cap) : nullptr;
         tp[i].qcount = P.qcount;

@@ -111,9 +111,9 @@ int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int c
     if (d.march_budget < 0 || mv >= 6) return 0;
     // queue entries hold 32-bit work indices and 16-bit step totals
     if (work >= (int64_t(1) << 32) || int64_t(cascades) * d.max_steps >= 65536) return 0;
-    // default: compacted passes after 12 steps for large launches (8 and 16
-    // measured slower on GB300); small ones cannot amortise the two extra
-    // passes
+    // default: compacted passes after 12 steps (then 8) for large launches
+    // (first-pass budgets 8 and 16 measured slower on GB300); small ones
+    // cannot amortise the two extra passes
     if (d.march_budget == 0) return work >= kLargeWork ? kDefaultMarchBudget : 0;
     return d.march_budget;
 }
@@ -267,7 +267,7 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.div_r = make_fastdiv(uint32_t(v->R));
     const int budget = v->mq ? march_budget_for(d, p.work, int(v->sdf.data.cascades_count)) : 0;
     p.budget1 = budget;
-    p.budget2 = budget;
+    p.budget2 = march_budget2(d.march_budget, budget);
     p.qa = v->mq;
     p.qb = v->mq ? v->mq + 2 * size_t(v->mqa_cap) : nullptr;
     p.qcount = v->mq_count;

@@ -83,9 +83,14 @@ int march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int cascades
 // Launches of at least this many march work items take the compacted march
 // and the binned shading by default.
 constexpr int64_t kLargeWork = int64_t(1) << 20;
-// Steps of the first compacted march pass when the volume leaves it to the
-// library (march_budget 0).
+// Steps of the first and second compacted march passes when the volume
+// leaves them to the library (march_budget 0); a volume that sets a budget
+// runs it in both.
 constexpr int kDefaultMarchBudget = 12;
+constexpr int kDefaultMarchBudget2 = 8;
+inline int march_budget2(int requested, int budget1) {
+    return (requested == 0 && budget1 > kDefaultMarchBudget2) ? kDefaultMarchBudget2 : budget1;
+}
 // Whether a volume's hits are shaded in bin order (shade_order and size).
 bool shade_binned(const luxgi_ddgi_volume_desc& d, int64_t work);
 // Device bytes a volume of description d allocates once bound to the scene
