@@ -67,14 +67,15 @@ static size_t queue_bytes(const Plan& P) {
 
 size_t plan_aux_bytes(const Plan& P) {
     size_t b = queue_bytes(P);
-    if (P.sorted) b += sizeof(uint32_t) * (2 * size_t(kBatchShadeBins) + 2 * size_t(P.work)) + 16;
+    if (P.sorted) b += sizeof(uint32_t) * (2 * size_t(kBatchShadeBins) + 3 * size_t(P.work)) + 16;
     return b;
 }
 
 void plan_set_aux(Plan& P, void* dev) {
     P.q = nullptr;
     P.qcount = nullptr;
-    P.sbins = P.skeys = P.sseq = nullptr;
+    P.sbins = P.sseq = nullptr;
+    P.skeys = nullptr;
     if (!dev) return;
     uint8_t* base = static_cast<uint8_t*>(dev);
     if (P.budget > 0) {
@@ -84,8 +85,8 @@ void plan_set_aux(Plan& P, void* dev) {
     }
     if (P.sorted) {
         P.sbins = reinterpret_cast<uint32_t*>(base);
-        P.skeys = P.sbins + 2 * size_t(kBatchShadeBins);
-        P.sseq = P.skeys + size_t(P.work);
+        P.skeys = reinterpret_cast<uint2*>(P.sbins + 2 * size_t(kBatchShadeBins));
+        P.sseq = reinterpret_cast<uint32_t*>(P.skeys + size_t(P.work));
     }
 }
 

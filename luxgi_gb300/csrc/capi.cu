@@ -355,7 +355,7 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     if (!v->shade_bins && shade_binned(v->desc, work)) {
         // shading-order buffers, made on the first trace that needs them
         cudaError_t e = dmalloc(&v->shade_bins, sizeof(uint32_t) * 2 * kShadeBins);
-        if (e == cudaSuccess) e = dmalloc(&v->shade_key, sizeof(uint32_t) * size_t(work));
+        if (e == cudaSuccess) e = dmalloc(&v->shade_key, sizeof(uint2) * size_t(work));
         if (e == cudaSuccess) e = dmalloc(&v->shade_order, sizeof(uint32_t) * size_t(work));
         if (e != cudaSuccess) {
             void* ptrs[] = {v->shade_bins, v->shade_key, v->shade_order};

@@ -34,7 +34,7 @@ struct Plan {
     // shading in bin order over the whole batch (sorted false: march order)
     bool sorted = false;
     uint32_t* sbins = nullptr;          // [2][kBatchShadeBins]
-    uint32_t* skeys = nullptr;          // [work] bin of each batch-wide work item
+    uint2* skeys = nullptr;             // [work] (bin, rank) of each batch-wide work item
     uint32_t* sseq = nullptr;           // [work] batch-wide work items by bin
 };
 

@@ -50,10 +50,11 @@ struct TraceParams {
     int budget1, budget2;
     int vol;                 // this volume's index in a batched launch (queue entries)
     // shading order by hit chunk (shade_order 1): the march counts its hits
-    // per bin and records each work item's bin; a scan and a scatter give
-    // `shade_seq`, the work items bin by bin, which the shade kernel walks.
-    uint32_t* bin_count;     // [2][kShadeBins]: per-bin counts, then the scatter cursors
-    uint32_t* bin_key;       // [work] bin of each work item
+    // per bin and records each work item's bin and its rank there; a scan
+    // of the counts and a placement give `shade_seq`, the work items bin by
+    // bin, which the shade kernel walks.
+    uint32_t* bin_count;     // [2][kShadeBins]: per-bin counts, then the bin starts
+    uint2* bin_key;          // [work] (bin, rank within the bin) of each work item
     uint32_t* shade_seq;     // [work] work items sorted by bin
     uint32_t bin_base;       // this volume's bins: bin_base + (chunk mod bin_span),
     uint32_t bin_span;       // the last one for misses (alone: 0, kShadeBins)
@@ -164,10 +165,11 @@ cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
 // tensor-core blend operands from the shaded rays (coalesced, after shading)
 cudaError_t launch_tc_pack(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_tc_pack_batch(const TraceParams* vp, const int* starts, int n, int blocks, cudaStream_t st);
-// Scan of the shading bins and scatter of the work items into `shade_seq`.
+// Scan of the shading bins and placement of the work items into `shade_seq`.
 cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st);
-// The same over raw arrays: bins [2][nb] (counts, cursors), keys and seq [work].
-cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint32_t* keys, uint32_t* seq, int64_t work,
+// The same over raw arrays: bins [2][nb] (counts, starts), (bin, rank)
+// slots and seq [work].
+cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint2* slots, uint32_t* seq, int64_t work,
                             cudaStream_t st);
 // Batched shading in bin order: seq holds batch-wide work indices; work_off
 // [n + 1] the first batch-wide index of each volume.

@@ -56,7 +56,7 @@ struct luxgi_ddgi_volume {
     bool stage_timing = false;
     bool stage_blend_recorded = false;
     uint32_t* shade_bins = nullptr;     // shading order: [2][kShadeBins] counts + cursors
-    uint32_t* shade_key = nullptr;      // [work] bin of each work item
+    uint2* shade_key = nullptr;         // [work] (bin, rank within the bin) of each work item
     uint32_t* shade_order = nullptr;    // [work] work items by bin
     int4* mq = nullptr;                 // suspended-march queues (march compaction)
     uint32_t* mq_count = nullptr;

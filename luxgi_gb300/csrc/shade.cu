@@ -73,30 +73,31 @@ __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
 }
 
 // ------------------------------------------------------ shading order
-// Exclusive scan of the bin counts into the scatter cursors, one block of
-// 32 warps: warp w owns a contiguous segment of the bins.  Pass 1 sums each
-// segment (32-bin coalesced slices, four loads in flight per lane), warp 0
-// scans the 32 segment totals, pass 2 rescans each segment from its base
-// (warp shuffles, the slices' loads again issued four ahead).
+// Exclusive scan of the bin counts into the bin starts, one block of 32
+// warps: warp w owns a contiguous segment of the bins.  Pass 1 sums each
+// segment (32-bin coalesced slices, kScanAhead loads in flight per lane),
+// warp 0 scans the 32 segment totals, pass 2 rescans each segment from its
+// base (warp shuffles, the slices' loads again issued kScanAhead ahead).
 constexpr int kScanThreads = 1024;
 constexpr int kScanWarps = kScanThreads / 32;
+constexpr int kScanAhead = 16;
 
 __global__ void __launch_bounds__(kScanThreads) bin_scan_kernel(const uint32_t* __restrict__ count,
-                                                               uint32_t* __restrict__ cursor, int nb) {
+                                                               uint32_t* __restrict__ start, int nb) {
     __shared__ uint32_t seg_base[kScanWarps];
     const int lane = int(threadIdx.x) & 31, warp = int(threadIdx.x) >> 5;
     const int seg = ((nb + kScanWarps - 1) / kScanWarps + 31) & ~31;
     const int b0 = warp * seg, b1 = min(b0 + seg, nb);
     uint32_t total = 0;
-    for (int b = b0; b < b1; b += 4 * 32) {
-        uint32_t v[4];
+    for (int b = b0; b < b1; b += kScanAhead * 32) {
+        uint32_t v[kScanAhead];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kScanAhead; ++k) {
             const int i = b + k * 32 + lane;
             v[k] = (b + k * 32 < b1 && i < b1) ? __ldg(count + i) : 0u;
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) total += __reduce_add_sync(0xffffffffu, v[k]);
+        for (int k = 0; k < kScanAhead; ++k) total += __reduce_add_sync(0xffffffffu, v[k]);
     }
     if (lane == 0) seg_base[warp] = total;
     __syncthreads();
@@ -112,15 +113,15 @@ __global__ void __launch_bounds__(kScanThreads) bin_scan_kernel(const uint32_t* 
     }
     __syncthreads();
     uint32_t running = seg_base[warp];
-    for (int b = b0; b < b1; b += 4 * 32) {
-        uint32_t v[4];
+    for (int b = b0; b < b1; b += kScanAhead * 32) {
+        uint32_t v[kScanAhead];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kScanAhead; ++k) {
             const int i = b + k * 32 + lane;
             v[k] = i < b1 ? __ldg(count + i) : 0u;
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kScanAhead; ++k) {
             uint32_t x = v[k];                              // inclusive scan of the slice
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
@@ -128,36 +129,32 @@ __global__ void __launch_bounds__(kScanThreads) bin_scan_kernel(const uint32_t* 
                 if (lane >= off) x += y;
             }
             const int i = b + k * 32 + lane;
-            if (i < b1) cursor[i] = running + x - v[k];
+            if (i < b1) start[i] = running + x - v[k];
             running += __shfl_sync(0xffffffffu, x, 31);
         }
     }
 }
 
-// Work items into `order` bin by bin (order within a bin is arbitrary; each
-// item is shaded the same wherever it lands).
-__global__ void __launch_bounds__(256) bin_scatter_kernel(const uint32_t* __restrict__ key, uint32_t* __restrict__ cursor,
-                                                          uint32_t* __restrict__ order, int64_t work) {
+// Work items into `order` bin by bin: item idx goes to its bin's start plus
+// the rank it drew from the bin's count when the march recorded it (the
+// order within a bin is arbitrary; each item is shaded the same wherever
+// it lands).
+__global__ void __launch_bounds__(256) bin_place_kernel(const uint2* __restrict__ slot,
+                                                        const uint32_t* __restrict__ start, uint32_t* __restrict__ order,
+                                                        int64_t work) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= work) return;
-    const uint32_t k = __ldg(key + idx);
-    const unsigned act = __activemask();
-    const unsigned same = __match_any_sync(act, k);
-    const int lane = int(threadIdx.x) & 31;
-    const int leader = __ffs(same) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(cursor + k, uint32_t(__popc(same)));
-    base = __shfl_sync(same, base, leader);
-    const uint32_t pos = base + uint32_t(__popc(same & ((1u << lane) - 1u)));
+    const uint2 s = __ldg(slot + idx);
+    const uint32_t pos = __ldg(start + s.x) + s.y;
     if (pos < work) order[pos] = uint32_t(idx);   // the counts cover every work item once
 }
 
-cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint32_t* keys, uint32_t* seq, int64_t work,
+cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint2* slots, uint32_t* seq, int64_t work,
                             cudaStream_t st) {
     if (work <= 0) return cudaSuccess;
-    uint32_t* cursor = bins + nb;
-    bin_scan_kernel<<<1, kScanThreads, 0, st>>>(bins, cursor, nb);
-    bin_scatter_kernel<<<unsigned((work + 255) / 256), 256, 0, st>>>(keys, cursor, seq, work);
+    uint32_t* start = bins + nb;
+    bin_scan_kernel<<<1, kScanThreads, 0, st>>>(bins, start, nb);
+    bin_place_kernel<<<unsigned((work + 255) / 256), 256, 0, st>>>(slots, start, seq, work);
     note_launch(2);
     return cudaGetLastError();
 }

@@ -67,8 +67,12 @@ cudaError_t launch_raygen_batch(const TraceParams* vp, const int* starts, int n,
 __device__ __forceinline__ void record_bin(const TraceParams& p, int64_t idx, uint32_t key) {
     const unsigned act = __activemask();
     const unsigned same = __match_any_sync(act, key);
-    if ((int(threadIdx.x) & 31) == __ffs(same) - 1) atomicAdd(p.bin_count + key, uint32_t(__popc(same)));
-    p.bin_key[idx] = key;
+    const int lane = int(threadIdx.x) & 31;
+    const int leader = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(p.bin_count + key, uint32_t(__popc(same)));
+    base = __shfl_sync(same, base, leader);
+    p.bin_key[idx] = make_uint2(key, base + uint32_t(__popc(same & ((1u << lane) - 1u))));
 }
 
 // Shading bin of a march result: the surface-cache chunk of the hit point
