@@ -296,12 +296,13 @@ __device__ __noinline__ f3 sdf_normal(const void* tex, const void* texq, int TW,
 }
 
 struct MarchHit {
-    f3 normal;
+    f3 normal;     // filled by march_hit_normal
     float time;
     int cascade;
     int steps;
     int fine;      // full-resolution SDF samples taken (for byte accounting)
     float sdf;
+    float u, v, w; // packed texture coordinates of the hit sample
 };
 
 // Where a ray's march stands between calls of march_run: the cascade (and
@@ -334,9 +335,12 @@ __device__ __forceinline__ void march_state_init(MarchState& m) {
 // state to resume from).  Resuming performs exactly the arithmetic of an
 // unbroken march.  QMIP / QTEX select the layouts (VolLayout) read for the
 // mip / full-resolution volume.  The probe rays use start bias 0 and want
-// the hit normal (GISDFRays.comp:79-87); the surface-cache shadow rays start
-// 2 voxels along and skip it (SDFDeferredLight.frag:104-111).
-template <typename T, int QMIP = kPlain, int QTEX = kPlain, bool NORMAL = true>
+// the hit normal (GISDFRays.comp:79-87): march_hit_normal computes it once
+// the march is over, outside the step loop, so that the lanes of a warp
+// whose rays hit at different steps fetch their normal taps together.  The
+// surface-cache shadow rays start 2 voxels along and skip it
+// (SDFDeferredLight.frag:104-111).
+template <typename T, int QMIP = kPlain, int QTEX = kPlain>
 __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps,
                                           MarchState& m, int budget, MarchHit& hit, float start_bias = 0.0f) {
     const int C = s.C;
@@ -408,10 +412,10 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
                 hit.time = mx(t + sd - thick, 0.0f);
                 hit.cascade = cascade;
                 hit.sdf = sd;
-                if (NORMAL)
-                    hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, tu, uy, uz, 1.0f / s.data.resolution);
-                else
-                    hit.normal = f3{0.0f, 0.0f, 0.0f};
+                hit.normal = f3{0.0f, 0.0f, 0.0f};
+                hit.u = tu;
+                hit.v = uy;
+                hit.w = uz;
                 hit.steps = m.steps + step;
                 hit.fine = m.fine;
                 return true;
@@ -427,7 +431,17 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
     hit.sdf = 0.0f;
     hit.steps = m.steps;
     hit.fine = m.fine;
+    hit.u = hit.v = hit.w = 0.0f;
     return true;
+}
+
+// Hit normal of an ended march (SDFCommon.glsl:174-183): central
+// differences at the hit sample's texture coordinates; zero for a miss.
+template <typename T, int QTEX>
+__device__ __forceinline__ void march_hit_normal(const SdfView& s, MarchHit& hit) {
+    if (hit.time >= 0.0f)
+        hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, s.res * s.C, s.res, hit.u, hit.v, hit.w,
+                                         1.0f / s.data.resolution);
 }
 
 // The whole march in one call.
@@ -437,6 +451,7 @@ __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 di
     march_state_init(m);
     MarchHit hit;
     march_run<T, QMIP, QTEX>(s, origin, dir, trace_max, max_steps, m, 0x7FFFFFFF, hit);
+    march_hit_normal<T, QTEX>(s, hit);
     return hit;
 }
 

@@ -165,6 +165,7 @@ __device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
                                            p.budget1 > 0 ? p.budget1 : 0x7FFFFFFF, hit);
         if (p.budget1 > 0 && enqueue_march(p.qa, p.qcount, p.qa_cap, !done, idx, p.vol, m)) return;
         if (!done) march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m, 0x7FFFFFFF, hit);
+        march_hit_normal<SdfT, QTEX>(p.sdf, hit);
         write_march(p, idx, probe, ray, origin, dir, hit);
     }
 }
@@ -194,6 +195,7 @@ __device__ __forceinline__ void march_resume(const TraceParams& p0, const TraceP
                                                 FINAL ? 0x7FFFFFFF : p.budget2, hit);
         if (!FINAL && enqueue_march(p0.qb, p0.qcount + 1, p0.qb_cap, !done, idx, vol, m)) continue;
         if (!done) march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m, 0x7FFFFFFF, hit);
+        march_hit_normal<SdfT, QTEX>(p.sdf, hit);
         write_march(p, idx, probe, ray, origin, dir, hit);
     }
 }
