@@ -131,11 +131,47 @@ template <> struct AtlasIO<float> {
     __device__ static float ld(const void* p, size_t i) { return static_cast<const float*>(p)[i]; }
     __device__ static float rnd(float v) { return v; }
     __device__ static void st(void* p, size_t i, float v) { static_cast<float*>(p)[i] = v; }
+    // all NC channels of texel `texel` in one access (atlases are 16-byte aligned)
+    template <int NC> __device__ static void ld_texel(const void* p, size_t texel, float* v) {
+        if constexpr (NC == 4) {
+            const float4 q = static_cast<const float4*>(p)[texel];
+            v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+        } else {
+            const float2 q = static_cast<const float2*>(p)[texel];
+            v[0] = q.x; v[1] = q.y;
+        }
+    }
+    template <int NC> __device__ static void st_texel(void* p, size_t texel, const float* v) {
+        if constexpr (NC == 4) static_cast<float4*>(p)[texel] = make_float4(v[0], v[1], v[2], v[3]);
+        else static_cast<float2*>(p)[texel] = make_float2(v[0], v[1]);
+    }
 };
 template <> struct AtlasIO<__half> {
     __device__ static float ld(const void* p, size_t i) { return __half2float(static_cast<const __half*>(p)[i]); }
     __device__ static float rnd(float v) { return __half2float(__float2half_rn(v)); }
     __device__ static void st(void* p, size_t i, float v) { static_cast<__half*>(p)[i] = __float2half_rn(v); }
+    template <int NC> __device__ static void ld_texel(const void* p, size_t texel, float* v) {
+        if constexpr (NC == 4) {
+            const uint2 q = static_cast<const uint2*>(p)[texel];
+            const __half2 a = *reinterpret_cast<const __half2*>(&q.x);
+            const __half2 b = *reinterpret_cast<const __half2*>(&q.y);
+            v[0] = __low2float(a); v[1] = __high2float(a); v[2] = __low2float(b); v[3] = __high2float(b);
+        } else {
+            const __half2 a = static_cast<const __half2*>(p)[texel];
+            v[0] = __low2float(a); v[1] = __high2float(a);
+        }
+    }
+    template <int NC> __device__ static void st_texel(void* p, size_t texel, const float* v) {
+        if constexpr (NC == 4) {
+            const __half2 a = __floats2half2_rn(v[0], v[1]), b = __floats2half2_rn(v[2], v[3]);
+            uint2 q;
+            q.x = *reinterpret_cast<const uint32_t*>(&a);
+            q.y = *reinterpret_cast<const uint32_t*>(&b);
+            static_cast<uint2*>(p)[texel] = q;
+        } else {
+            static_cast<__half2*>(p)[texel] = __floats2half2_rn(v[0], v[1]);
+        }
+    }
 };
 
 // Writes channel values v[0..nc) of interior texel (tx, ty) of cell
@@ -145,11 +181,7 @@ template <typename AT, int NC>
 __device__ __forceinline__ void store_texel(void* atlas, int W, int n, int cx, int cy, int tx, int ty, const float* v) {
     const int ox = cx * (n + 2) + 1, oy = cy * (n + 2) + 1;   // cell origin (border corner)
     const int X = tx + 1, Y = ty + 1;                        // cell-relative interior coords
-    auto put = [&](int x, int y) {
-        const size_t base = (size_t(oy + y) * W + (ox + x)) * NC;
-#pragma unroll
-        for (int c = 0; c < NC; ++c) AtlasIO<AT>::st(atlas, base + c, v[c]);
-    };
+    auto put = [&](int x, int y) { AtlasIO<AT>::template st_texel<NC>(atlas, size_t(oy + y) * W + (ox + x), v); };
     put(X, Y);
     if (Y == 1) put(n + 1 - X, 0);
     if (Y == n) put(n + 1 - X, n + 1);
@@ -256,11 +288,14 @@ __device__ __forceinline__ void blend_epilogue(const BlendParams& p, int p0, int
 #pragma unroll
                 for (int c = 0; c < 3; ++c) v[c] = powf(v[c], ig);
             }
-            const size_t base = (size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2)) * NC;
-            const int nch = DEPTH ? 2 : 3;
+            const size_t texel = size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2);
+            constexpr int nch = DEPTH ? 2 : 3;
+            float pv[NC];
+            if (!p.first) AtlasIO<AT>::template ld_texel<NC>(prev, texel, pv);
+#pragma unroll
             for (int c = 0; c < nch; ++c) {
                 float x = v[c];
-                if (!p.first) x = x * (1.0f - h) + AtlasIO<AT>::ld(prev, base + c) * h;
+                if (!p.first) x = x * (1.0f - h) + pv[c] * h;
                 v[c] = AtlasIO<AT>::rnd(x);
             }
             store_texel<AT, NC>(out, W, n, cx, cy, tx, ty, v);
@@ -474,6 +509,17 @@ __global__ void __launch_bounds__(kBlendThreads)
     blend_block<DEPTH, RT, AT, PP>(p, int(blockIdx.x) - __ldg(starts + v), smem);
 }
 
+// Both kinds of a volume in one launch: the distance blocks first (the
+// longer ones), then the irradiance blocks, which fill the last partial
+// wave of the distance blocks instead of starting after it.
+template <typename RT, typename AT, int PPI, int PPD>
+__global__ void __launch_bounds__(kBlendThreads) blend_pair_kernel(const BlendParams p, int blocks_dist) {
+    extern __shared__ __align__(16) float smem[];
+    const int b = int(blockIdx.x);
+    if (b < blocks_dist) blend_block<1, RT, AT, PPD>(p, b, smem);
+    else blend_block<0, RT, AT, PPI>(p, b - blocks_dist, smem);
+}
+
 static int blend_side(const BlendParams& p, bool depth) {
     return depth ? p.u.depth_probe_side : p.u.irradiance_probe_side;
 }
@@ -538,11 +584,44 @@ static cudaError_t launch_kind(const void* vp, const int* starts, int n, int blo
     }
 }
 
+template <typename RT, typename AT, int PPI, int PPD>
+static cudaError_t launch_pair_pp(const BlendParams& p, int bi, int bd, size_t sm, cudaStream_t st) {
+    auto k = blend_pair_kernel<RT, AT, PPI, PPD>;
+    if (sm > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        if (e != cudaSuccess) return e;
+    }
+    k<<<bi + bd, kBlendThreads, sm, st>>>(p, bd);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// The irradiance kind has more probes per block than the distance kind at
+// equal probes per thread, so auto_pp never gives it the larger tile: the
+// pairs below are all that occur.
+template <typename RT, typename AT>
+static cudaError_t launch_pair(const BlendParams& p, int ppi, int ppd, int bi, int bd, size_t sm, cudaStream_t st) {
+    switch (ppi * 8 + ppd) {
+        case 1 * 8 + 1: return launch_pair_pp<RT, AT, 1, 1>(p, bi, bd, sm, st);
+        case 1 * 8 + 2: return launch_pair_pp<RT, AT, 1, 2>(p, bi, bd, sm, st);
+        case 1 * 8 + 4: return launch_pair_pp<RT, AT, 1, 4>(p, bi, bd, sm, st);
+        case 2 * 8 + 2: return launch_pair_pp<RT, AT, 2, 2>(p, bi, bd, sm, st);
+        case 2 * 8 + 4: return launch_pair_pp<RT, AT, 2, 4>(p, bi, bd, sm, st);
+        case 4 * 8 + 4: return launch_pair_pp<RT, AT, 4, 4>(p, bi, bd, sm, st);
+        default: return cudaErrorNotSupported;
+    }
+}
+
 cudaError_t launch_blend(const BlendParams& p, cudaStream_t st) {
     if (p.P <= 0) return cudaSuccess;
     const int ppi = auto_pp(p, false), ppd = auto_pp(p, true);
     const int bi = blend_blocks(p, false, ppi), bd = blend_blocks(p, true, ppd);
     const size_t si = blend_smem(p, false, ppi), sd = blend_smem(p, true, ppd);
+    if (ppi <= ppd) {
+        const size_t sm = si > sd ? si : sd;
+        return p.storage == LUXGI_STORAGE_FP16 ? launch_pair<uint2, __half>(p, ppi, ppd, bi, bd, sm, st)
+                                               : launch_pair<float4, float>(p, ppi, ppd, bi, bd, sm, st);
+    }
     cudaError_t e;
     if (p.storage == LUXGI_STORAGE_FP16) {
         e = launch_kind<0, uint2, __half>(&p, nullptr, 1, bi, si, ppi, false, st);
