@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--ray-order", type=int, default=None, help="override the volume's ray order (0, 1)")
     ap.add_argument("--march-budget", type=int, default=None, help="override the volume's march budget (-1 one pass)")
     ap.add_argument("--shade-order", type=int, default=None, help="override the volume's shading order (0, 1)")
+    ap.add_argument("--shade-split", type=int, default=None, help="override the volume's split shading (-1, 0, 1)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serve200: length of the timed Poisson run")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serve200: requests per second, all sessions")
     ap.add_argument("--serve-budget-gb", type=float, default=120.0, help="serve200: device-memory budget")
@@ -215,6 +216,8 @@ def run_ours(args, rank: int, world: int):
         w = replace(w, volume=replace(w.volume, march_budget=args.march_budget))
     if args.shade_order is not None:
         w = replace(w, volume=replace(w.volume, shade_order=args.shade_order))
+    if args.shade_split is not None:
+        w = replace(w, volume=replace(w.volume, shade_split=args.shade_split))
     v = w.volume
     P, R = v.probes, v.rays_per_probe
     host = HostScene(w.scene)

@@ -221,7 +221,16 @@ typedef struct luxgi_ddgi_volume_desc {
                                       order; 0 default (1 when the volume has
                                       >= 2^20 probe-rays, else -1).  Per-ray
                                       march variants 1-5.                    */
-    int32_t reserved[3];
+    int32_t shade_split;           /* tuning, results identical: 1 the rays
+                                      that end in the compacted march's first
+                                      pass are sorted and shaded on a second
+                                      stream while the resume passes run, the
+                                      others after them; -1 off; 0 default
+                                      (on when the march is compacted, the
+                                      shading binned and the volume has
+                                      < 2^24 probe-rays).  The call keeps its
+                                      stream semantics.                      */
+    int32_t reserved[2];
 } luxgi_ddgi_volume_desc;
 
 /* Device views of a volume's probe atlases. */

@@ -128,7 +128,8 @@ class VolumeDesc(ctypes.Structure):
     _fields_ = [("uniform", DDGIUniform), ("storage", c_int32), ("light_mode", c_int32), ("blend", c_int32),
                 ("max_steps", c_int32), ("infinite_bounce", c_int32), ("intensity", c_float),
                 ("sky_radiance", c_float * 3), ("march_variant", c_int32), ("shade_variant", c_int32),
-                ("ray_order", c_int32), ("march_budget", c_int32), ("shade_order", c_int32), ("reserved", c_int32 * 3)]
+                ("ray_order", c_int32), ("march_budget", c_int32), ("shade_order", c_int32), ("shade_split", c_int32),
+                ("reserved", c_int32 * 2)]
 
 
 class Atlases(ctypes.Structure):

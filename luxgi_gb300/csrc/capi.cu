@@ -60,9 +60,38 @@ void free_volume(luxgi_ddgi_volume* v) {
                     v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
                     v->status, v->hit_t, v->hit_c, v->w2l, v->shade_chunks, v->shade_culled, v->shade_scratch,
                     v->sdf_quad, v->mip_quad, v->mq, v->mq_count, v->cell_min, v->shade_bins, v->shade_key,
-                    v->shade_order};
+                    v->shade_order, v->split_bins, v->split_key, v->split_order};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (v->fork_ev) cudaEventDestroy(v->fork_ev);
+    if (v->join_ev) cudaEventDestroy(v->join_ev);
+    if (v->side) cudaStreamDestroy(v->side);
+}
+
+// Second stream, events and buffers of the split shading, made on the
+// first trace that uses it.
+int alloc_split(luxgi_ddgi_volume* v, int64_t work) {
+    if (v->side) return LUXGI_OK;
+    cudaError_t e = dmalloc(&v->split_bins, sizeof(uint32_t) * 2 * kShadeBins);
+    if (e == cudaSuccess) e = dmalloc(&v->split_key, sizeof(uint2) * size_t(work));
+    if (e == cudaSuccess) e = dmalloc(&v->split_order, sizeof(uint32_t) * size_t(v->mqa_cap));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->join_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&v->side, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        void* ptrs[] = {v->split_bins, v->split_key, v->split_order};
+        for (void* q : ptrs)
+            if (q) cudaFree(q);
+        if (v->fork_ev) cudaEventDestroy(v->fork_ev);
+        if (v->join_ev) cudaEventDestroy(v->join_ev);
+        v->split_bins = nullptr;
+        v->split_key = nullptr;
+        v->split_order = nullptr;
+        v->fork_ev = v->join_ev = nullptr;
+        v->side = nullptr;
+        return cuda_status(e);
+    }
+    return LUXGI_OK;
 }
 
 SdfView sdf_view(const luxgi_sdf_desc& s) {
@@ -378,6 +407,40 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     cudaError_t e = launch_raygen(p.rot, v->R, v->desc.storage, v->dirs_trace, v->dirs_blend, st);
     if (e == cudaSuccess) e = launch_weights(b, st);
     int s = e == cudaSuccess ? volume_prepare(v, st) : cuda_status(e);
+    const bool split =
+        s == LUXGI_OK && p.bin_count && p.budget1 > 0 && p.march_variant < 6 && shade_split(v->desc, p.work);
+    if (split) s = alloc_split(v, p.work);
+    if (s == LUXGI_OK && split) {
+        // pass 1 on st; its finishers sorted and shaded on the side stream
+        // while passes 2 and 3 run on st; the queued rays sorted and shaded
+        // on st after them; st then waits for the side stream
+        TraceParams pa = p, pb = p;
+        pa.split = 1;
+        pa.shade_part = 1;
+        pb.bin_count = v->split_bins;
+        pb.bin_key = v->split_key;
+        pb.shade_seq = v->split_order;
+        pb.shade_part = 2;
+        mark(1);
+        cudaError_t e2 = cudaMemsetAsync(pa.bin_count, 0, sizeof(uint32_t) * kShadeBins, st);
+        if (e2 == cudaSuccess) e2 = cudaMemsetAsync(pb.bin_count, 0, sizeof(uint32_t) * kShadeBins, st);
+        if (e2 == cudaSuccess) e2 = launch_march_split(pa, pb, v->fork_ev, st);
+        if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(v->side, v->fork_ev, 0);
+        if (e2 == cudaSuccess) e2 = launch_shade_sort(pa, v->side);
+        if (e2 == cudaSuccess) e2 = launch_shade(pa, v->side);
+        if (e2 == cudaSuccess) e2 = cudaEventRecord(v->join_ev, v->side);
+        if (e2 == cudaSuccess) {
+            mark(2);
+            e2 = launch_shade_sort(pb, st);
+        }
+        if (e2 == cudaSuccess) e2 = launch_shade(pb, st);
+        if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(st, v->join_ev, 0);
+        if (e2 == cudaSuccess) e2 = launch_tc_pack(p, st);
+        s = cuda_status(e2);
+        mark(3);
+        nvtxRangePop();
+        return s;
+    }
     if (s == LUXGI_OK) {
         mark(1);
         cudaError_t em = p.bin_count ? cudaMemsetAsync(p.bin_count, 0, sizeof(uint32_t) * kShadeBins, st)
@@ -507,6 +570,7 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->march_variant < 0 || desc->march_variant > 9) return LUXGI_EINVAL;
     if (desc->ray_order != 0 && desc->ray_order != 1) return LUXGI_EINVAL;
     if (desc->march_budget < -1) return LUXGI_EINVAL;
+    if (desc->shade_split < -1 || desc->shade_split > 1) return LUXGI_EINVAL;
     if (desc->shade_order < -1 || desc->shade_order > 1) return LUXGI_EINVAL;
     if (desc->shade_variant != 0 && desc->shade_variant != 1 && desc->shade_variant != 2 &&
         desc->shade_variant != 4 && desc->shade_variant != 8)

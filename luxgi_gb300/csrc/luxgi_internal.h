@@ -58,7 +58,17 @@ struct TraceParams {
     uint32_t* shade_seq;     // [work] work items sorted by bin
     uint32_t bin_base;       // this volume's bins: bin_base + (chunk mod bin_span),
     uint32_t bin_span;       // the last one for misses (alone: 0, kShadeBins)
+    // split shading (single volume, compacted march): the rays that finish
+    // in pass 1 are sorted and shaded while passes 2 and 3 run.  Pass 1
+    // marks the rays it queues with kDeferredBin; passes 2 and 3 record
+    // theirs in a second histogram and slot array.
+    int split;
+    int shade_part;          // the shade launch covers: 0 every work item,
+                             // 1 the pass-1 finishers, 2 the queued rays (qa)
 };
+
+// Slot bin of a ray that pass 1 queued when the shading is split.
+constexpr uint32_t kDeferredBin = 0xFFFFFFFFu;
 
 // Shading bins: the 40^3 surface-cache chunks of the hits, then one bin for
 // misses, rays inside geometry and padding.
@@ -161,11 +171,16 @@ cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, 
 cudaError_t launch_shade_batch(const TraceParams* vp, const int* starts, int n, int blocks, int light_mode,
                                int shade_variant, cudaStream_t st);
 cudaError_t launch_march(const TraceParams& p, cudaStream_t st);
+// The compacted march with split shading: pass 1 with p, `after_first`
+// recorded on st, passes 2 and 3 with `resume` (its own histogram and slots).
+cudaError_t launch_march_split(const TraceParams& p, const TraceParams& resume, cudaEvent_t after_first,
+                               cudaStream_t st);
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st);
 // tensor-core blend operands from the shaded rays (coalesced, after shading)
 cudaError_t launch_tc_pack(const TraceParams& p, cudaStream_t st);
 cudaError_t launch_tc_pack_batch(const TraceParams* vp, const int* starts, int n, int blocks, cudaStream_t st);
-// Scan of the shading bins and placement of the work items into `shade_seq`.
+// Scan of the shading bins and placement of the work items into `shade_seq`
+// (shade_part 2: of the queued rays, read from qa).
 cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st);
 // The same over raw arrays: bins [2][nb] (counts, starts), (bin, rank)
 // slots and seq [work].

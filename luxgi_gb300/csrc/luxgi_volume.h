@@ -61,6 +61,13 @@ struct luxgi_ddgi_volume {
     int4* mq = nullptr;                 // suspended-march queues (march compaction)
     uint32_t* mq_count = nullptr;
     uint32_t mqa_cap = 0, mqb_cap = 0;
+    // split shading: the second stream, its fork / join events, and the
+    // resumed rays' histogram [2][kShadeBins], slots [work], order [qa_cap]
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    uint32_t* split_bins = nullptr;
+    uint2* split_key = nullptr;
+    uint32_t* split_order = nullptr;
 };
 
 
@@ -93,6 +100,15 @@ inline int march_budget2(int requested, int budget1) {
 }
 // Whether a volume's hits are shaded in bin order (shade_order and size).
 bool shade_binned(const luxgi_ddgi_volume_desc& d, int64_t work);
+// Whether the shading of a binned, compacted march of `work` items is split
+// (shade_split).  By default only below 2^24 items: the split hides the
+// resume passes' latency tail, which does not grow with the ray count, while
+// the contention between the concurrent march and shading does (GB300: +1.7 %
+// at 2^22 rays, -0.7 % at 2^25).
+constexpr int64_t kSplitMaxWork = int64_t(1) << 24;
+inline bool shade_split(const luxgi_ddgi_volume_desc& d, int64_t work) {
+    return d.shade_split == 1 || (d.shade_split == 0 && work < kSplitMaxWork);
+}
 // Device bytes a volume of description d allocates once bound to the scene
 // (luxgi_ddgi_create + luxgi_ddgi_bind_scene; debug ray records excluded).
 uint64_t volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,

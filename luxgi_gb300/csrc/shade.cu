@@ -68,7 +68,14 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
 template <int MODE, int UNROLL>
 __global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= p.work) return;
+    int64_t n = p.work;
+    if (p.shade_part) {
+        // split shading: the queued rays are qa's entries (its counter may
+        // run past the capacity; rays beyond it finished in pass 1)
+        const int64_t q = min(__ldg(p.qcount), p.qa_cap);
+        n = p.shade_part == 1 ? p.work - q : q;
+    }
+    if (i >= n) return;
     shade_ray<MODE, UNROLL>(p, p.shade_seq ? int64_t(__ldg(p.shade_seq + i)) : i);
 }
 
@@ -145,8 +152,25 @@ __global__ void __launch_bounds__(256) bin_place_kernel(const uint2* __restrict_
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= work) return;
     const uint2 s = __ldg(slot + idx);
+    if (s.x == kDeferredBin) return;              // queued by pass 1, placed with the queue
     const uint32_t pos = __ldg(start + s.x) + s.y;
     if (pos < work) order[pos] = uint32_t(idx);   // the counts cover every work item once
+}
+
+// The same for the rays pass 1 queued (split shading): entry i of qa names
+// its work item, whose slot passes 2 and 3 recorded.
+__global__ void __launch_bounds__(256) bin_place_queue_kernel(const int4* __restrict__ qa,
+                                                              const uint32_t* __restrict__ qcount, uint32_t cap,
+                                                              const uint2* __restrict__ slot,
+                                                              const uint32_t* __restrict__ start,
+                                                              uint32_t* __restrict__ order) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = min(__ldg(qcount), cap);
+    if (i >= n) return;
+    const uint32_t idx = uint32_t(__ldg(qa + 2 * size_t(i)).x);
+    const uint2 s = __ldg(slot + idx);
+    const uint32_t pos = __ldg(start + s.x) + s.y;
+    if (pos < n) order[pos] = idx;
 }
 
 cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint2* slots, uint32_t* seq, int64_t work,
@@ -160,7 +184,14 @@ cudaError_t launch_bin_sort(uint32_t* bins, int nb, const uint2* slots, uint32_t
 }
 
 cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st) {
-    return launch_bin_sort(p.bin_count, kShadeBins, p.bin_key, p.shade_seq, p.work, st);
+    if (p.shade_part != 2) return launch_bin_sort(p.bin_count, kShadeBins, p.bin_key, p.shade_seq, p.work, st);
+    if (p.qa_cap == 0) return cudaSuccess;
+    uint32_t* start = p.bin_count + kShadeBins;
+    bin_scan_kernel<<<1, kScanThreads, 0, st>>>(p.bin_count, start, kShadeBins);
+    bin_place_queue_kernel<<<(p.qa_cap + 255) / 256, 256, 0, st>>>(p.qa, p.qcount, p.qa_cap, p.bin_key, start,
+                                                                  p.shade_seq);
+    note_launch(2);
+    return cudaGetLastError();
 }
 
 // Batched shading in bin order.  Every volume owns a contiguous run of
@@ -302,7 +333,7 @@ cudaError_t launch_tc_pack_batch(const TraceParams* vp, const int* starts, int n
 }
 
 cudaError_t launch_shade(const TraceParams& p, cudaStream_t st) {
-    const int64_t total = p.work;
+    const int64_t total = p.shade_part == 2 ? int64_t(p.qa_cap) : p.work;
     if (total <= 0) return cudaSuccess;
     const unsigned sblocks = unsigned((total + 127) / 128);
     if (p.light_mode == LUXGI_LIGHT_PER_HIT) {

@@ -163,7 +163,10 @@ __device__ __forceinline__ void march_ray(const TraceParams& p, int64_t idx) {
         const f3 origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
         done = march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m,
                                            p.budget1 > 0 ? p.budget1 : 0x7FFFFFFF, hit);
-        if (p.budget1 > 0 && enqueue_march(p.qa, p.qcount, p.qa_cap, !done, idx, p.vol, m)) return;
+        if (p.budget1 > 0 && enqueue_march(p.qa, p.qcount, p.qa_cap, !done, idx, p.vol, m)) {
+            if (p.split) p.bin_key[idx] = make_uint2(kDeferredBin, 0u);
+            return;
+        }
         if (!done) march_run<SdfT, QMIP, QTEX>(p.sdf, origin, dir, kWorldSize, p.max_steps, m, 0x7FFFFFFF, hit);
         march_hit_normal<SdfT, QTEX>(p.sdf, hit);
         write_march(p, idx, probe, ray, origin, dir, hit);
@@ -377,9 +380,12 @@ static unsigned resume_blocks() {
 }
 
 // One march variant: pass 1 over every work item, then (compaction) the two
-// resume passes over the queued rays.
+// resume passes over the queued rays, with the parameters `rp` (those of
+// pass 1 unless the shading is split) and `after_first` (or nullptr)
+// recorded between.
 template <typename SdfT, int MINB, int QMIP, int QTEX>
-static cudaError_t launch_march_variant(const TraceParams& p, cudaStream_t st) {
+static cudaError_t launch_march_variant(const TraceParams& p, cudaStream_t st, const TraceParams& rp,
+                                        cudaEvent_t after_first) {
     const unsigned mblocks = unsigned((p.work + 255) / 256);
     if (p.budget1 > 0) {
         const cudaError_t e = cudaMemsetAsync(p.qcount, 0, 2 * sizeof(uint32_t), st);
@@ -387,16 +393,32 @@ static cudaError_t launch_march_variant(const TraceParams& p, cudaStream_t st) {
     }
     march_kernel<SdfT, MINB, QMIP, QTEX><<<mblocks, 256, 0, st>>>(p);
     note_launch();
+    if (after_first) {
+        const cudaError_t e = cudaEventRecord(after_first, st);
+        if (e != cudaSuccess) return e;
+    }
     if (p.budget1 > 0) {
         const unsigned rb = resume_blocks();
-        march_resume_kernel<SdfT, MINB, QMIP, QTEX, false><<<rb, 256, 0, st>>>(p);
-        march_resume_kernel<SdfT, MINB, QMIP, QTEX, true><<<rb, 256, 0, st>>>(p);
+        march_resume_kernel<SdfT, MINB, QMIP, QTEX, false><<<rb, 256, 0, st>>>(rp);
+        march_resume_kernel<SdfT, MINB, QMIP, QTEX, true><<<rb, 256, 0, st>>>(rp);
         note_launch(2);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_march(const TraceParams& p, cudaStream_t st) {
+static cudaError_t launch_march_passes(const TraceParams& p, cudaStream_t st, const TraceParams& rp,
+                                       cudaEvent_t after_first);
+
+cudaError_t launch_march(const TraceParams& p, cudaStream_t st) { return launch_march_passes(p, st, p, nullptr); }
+
+cudaError_t launch_march_split(const TraceParams& p, const TraceParams& resume, cudaEvent_t after_first,
+                               cudaStream_t st) {
+    if (p.march_variant >= 6 || p.budget1 <= 0 || !after_first) return cudaErrorInvalidValue;
+    return launch_march_passes(p, st, resume, after_first);
+}
+
+static cudaError_t launch_march_passes(const TraceParams& p, cudaStream_t st, const TraceParams& rp,
+                                       cudaEvent_t after_first) {
     const int64_t total = p.work;
     if (total <= 0) return cudaSuccess;
     if (p.march_variant >= 6) {
@@ -434,12 +456,14 @@ cudaError_t launch_march(const TraceParams& p, cudaStream_t st) {
     // full-resolution volume.  All produce identical results.
     const bool h = p.sdf.format == LUXGI_STORAGE_FP16;
     cudaError_t e;
+    const TraceParams& r = rp;
+    cudaEvent_t a = after_first;
     switch (p.march_variant) {
-        case 2: e = h ? launch_march_variant<__half, 1, kPlain, kPlain>(p, st) : launch_march_variant<float, 1, kPlain, kPlain>(p, st); break;
-        case 3: e = h ? launch_march_variant<__half, 4, kQuad, kPlain>(p, st) : launch_march_variant<float, 4, kQuad, kPlain>(p, st); break;
-        case 4: e = h ? launch_march_variant<__half, 4, kQuad, kQuad>(p, st) : launch_march_variant<float, 4, kQuad, kQuad>(p, st); break;
-        case 5: e = h ? launch_march_variant<__half, 4, kQuad, kPair>(p, st) : launch_march_variant<float, 4, kQuad, kPair>(p, st); break;
-        default: e = h ? launch_march_variant<__half, 4, kPlain, kPlain>(p, st) : launch_march_variant<float, 4, kPlain, kPlain>(p, st); break;
+        case 2: e = h ? launch_march_variant<__half, 1, kPlain, kPlain>(p, st, r, a) : launch_march_variant<float, 1, kPlain, kPlain>(p, st, r, a); break;
+        case 3: e = h ? launch_march_variant<__half, 4, kQuad, kPlain>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kPlain>(p, st, r, a); break;
+        case 4: e = h ? launch_march_variant<__half, 4, kQuad, kQuad>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kQuad>(p, st, r, a); break;
+        case 5: e = h ? launch_march_variant<__half, 4, kQuad, kPair>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kPair>(p, st, r, a); break;
+        default: e = h ? launch_march_variant<__half, 4, kPlain, kPlain>(p, st, r, a) : launch_march_variant<float, 4, kPlain, kPlain>(p, st, r, a); break;
     }
     return e;
 }

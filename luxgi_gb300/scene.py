@@ -58,6 +58,7 @@ class VolumeSpec:
     ray_order: int = 0
     march_budget: int = 0
     shade_order: int = 0
+    shade_split: int = 0
 
     @property
     def probes(self) -> int:
@@ -99,6 +100,7 @@ class VolumeSpec:
         d.ray_order = self.ray_order
         d.march_budget = self.march_budget
         d.shade_order = self.shade_order
+        d.shade_split = self.shade_split
         return d
 
 

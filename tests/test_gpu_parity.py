@@ -398,16 +398,19 @@ def test_march_variants_bit_identical(cuda, fmt):
 def test_march_compaction_and_ray_order_bit_identical(cuda, fmt):
     """Suspending marches after a step budget and resuming them from the
     queues (budgets 1, 2, 8; budget 1 overflows the queues, whose rays then
-    finish in place), the tiled ray order, and shading in hit-chunk order
-    give exactly the one-pass results, and those equal the FP32 oracle."""
+    finish in place), the tiled ray order, shading in hit-chunk order, and
+    that shading split in two (the pass-1 finishers on a second stream while
+    the resume passes run, the queued rays after them) give exactly the
+    one-pass results, and those equal the FP32 oracle."""
     from dataclasses import replace
 
     base = tiny_workload(probe_counts=(7, 3, 5), rays=64, sdf=64, sdf_format=fmt, cascades=2, room=20.0, prims=10)
     outs = []
-    for mv, budget, order, sorder in ((4, -1, 0, -1), (4, 1, 0, 1), (4, 2, 0, -1), (4, 8, 0, 0), (3, 2, 1, 1),
-                                      (5, 8, 1, -1), (1, -1, 1, 0)):
+    for mv, budget, order, sorder, split in ((4, -1, 0, -1, 0), (4, 1, 0, 1, 1), (4, 1, 0, 1, -1), (4, 2, 0, -1, 0),
+                                             (4, 8, 0, 0, 0), (3, 2, 1, 1, 1), (4, 3, 1, 1, -1), (5, 8, 1, -1, 0),
+                                             (1, -1, 1, 0, 0)):
         w = replace(base, volume=replace(base.volume, march_variant=mv, march_budget=budget, ray_order=order,
-                                         shade_order=sorder))
+                                         shade_order=sorder, shade_split=split))
         host, dev, vol, inp = setup(w)
         rot = frame_rotation(51, 0)
         vol.trace(rot)
