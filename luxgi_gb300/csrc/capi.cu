@@ -241,7 +241,7 @@ int luxgi::volume_prepare(luxgi_ddgi_volume* v, cudaStream_t st) {
         if (e != cudaSuccess) return cuda_status(e);
     }
     if (v->cell_min) {
-        e = launch_cell_min(v->sdf.sdf, res * C, res, res, v->sdf.format, v->cell_min, st);
+        e = launch_cell_min(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf.data.resolution, v->cell_min, st);
         if (e != cudaSuccess) return cuda_status(e);
     }
     if (v->sdf_quad) {
@@ -265,7 +265,10 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.surf.culled = v->shade_culled;
     p.sdf.sdf_quad = v->sdf_quad;
     p.sdf.mip_quad = v->mip_quad;
-    p.sdf.cell_min = v->cell_min;
+    p.sdf.cell_near =
+        v->cell_min ? cell_bits(v->cell_min, v->sdf.resolution * int(v->sdf.data.cascades_count), v->sdf.resolution,
+                                v->sdf.resolution)
+                    : nullptr;
     p.sdf.cw = (v->sdf.resolution * int(v->sdf.data.cascades_count) + kCellSide - 1) / kCellSide;
     p.sdf.ch = (v->sdf.resolution + kCellSide - 1) / kCellSide;
     p.hit_t = v->hit_t;

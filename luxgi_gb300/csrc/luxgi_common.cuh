@@ -244,11 +244,12 @@ struct SdfView {
     const void* sdf_quad;   // packed copy of the full-resolution volume (quad or
                             // pair layout, march variants 4 / 5) or nullptr
     const void* mip_quad;   // quad-packed mip (variants 3-5) or nullptr
-    // Conservative cell minima of the full-resolution volume: cell (i, j, k)
-    // holds the minimum texel over [4i, 4i+4] x [4j, 4j+4] x [4k, 4k+4]
-    // (clamped), every texel a trilinear footprint whose lower corner lies in
-    // the cell can read.  nullptr: not built.
-    const float* cell_min;
+    // One bit per cell (i, j, k) of the full-resolution volume, 32 cells a
+    // word: set unless the minimum texel over [4i, 4i+4] x [4j, 4j+4] x
+    // [4k, 4k+4] (clamped; every texel a trilinear footprint whose lower
+    // corner lies in the cell can read) is at or above the march's skip
+    // threshold.  nullptr: not built.
+    const uint32_t* cell_near;
     int cw, ch;             // cells along x (packed cascades) and y
     int res, mres, C;
     int format;   // luxgi_storage of the sdf/mip texels
@@ -256,18 +257,20 @@ struct SdfView {
 
 constexpr int kCellSide = 4;
 
-// True when the trilinear full-resolution sample at packed texture
-// coordinates (u, v, w) is certainly >= thr: every texel it interpolates is
-// >= the cell minimum, and a convex combination of values >= m > 0 computed
-// in FP32 is >= m (1 - 2^-20); the caller's thr carries that margin.
-__device__ __forceinline__ bool fine_sample_at_least(const SdfView& s, float u, float v, float w, float thr) {
+// False when the trilinear full-resolution sample at packed texture
+// coordinates (u, v, w) is certainly >= the skip threshold 2 margin (1.001):
+// every texel it interpolates is >= the cell minimum, and a convex
+// combination of values >= m > 0 computed in FP32 is >= m (1 - 2^-20), so
+// such a sample is never used (SDFCommon.glsl:150-158).  The 32 KB a
+// cascade of bits stay in L1, unlike the cell minima they are made from.
+__device__ __forceinline__ bool fine_needed(const SdfView& s, float u, float v, float w) {
+    if (!s.cell_near) return true;
     const int W = s.res * s.C, H = s.res, D = s.res;
     const int x0 = imn(imx(int(floorf(u * float(W) - 0.5f)), 0), W - 1);
     const int y0 = imn(imx(int(floorf(v * float(H) - 0.5f)), 0), H - 1);
     const int z0 = imn(imx(int(floorf(w * float(D) - 0.5f)), 0), D - 1);
-    const float m = __ldg(s.cell_min + (size_t(z0 / kCellSide) * s.ch + size_t(y0 / kCellSide)) * s.cw +
-                          size_t(x0 / kCellSide));
-    return m >= thr;
+    const uint32_t c = uint32_t((z0 / kCellSide) * s.ch + (y0 / kCellSide)) * uint32_t(s.cw) + uint32_t(x0 / kCellSide);
+    return (__ldg(s.cell_near + (c >> 5)) >> (c & 31u)) & 1u;
 }
 
 // One GL trilinear sample of the full-resolution or mip volume, from the
@@ -348,9 +351,6 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
     const float tmax = mn(trace_max, s.data.cascade_pos_distance[C - 1][3] * 2.0f);
     const float chunk = 32.0f / s.data.resolution;
     const float margin = 4.0f / s.data.resolution;
-    // cell minimum at or above this: the full-resolution value is >= 2 margin
-    // and unused (SDFCommon.glsl:150-158), so its taps need not be read
-    const float skip_thr = (margin * 2.0f) * 1.001f;
     const f3 end = add3(origin, mul3(dir, tmax));
     for (; m.cascade < C; ++m.cascade) {
         const int cascade = m.cascade;
@@ -397,7 +397,7 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             // (one memory round trip per step) unless the cell minima show
             // their value cannot be used; it is used only where
             // SDFCommon.glsl:150-158 samples the full-resolution SDF
-            const bool need_fine = !s.cell_min || !fine_sample_at_least(s, tu, uy, uz, skip_thr);
+            const bool need_fine = fine_needed(s, tu, uy, uz);
             float sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
             const float sdt = need_fine ? sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz) : 1.0f;
             if (sd < chunk) {

@@ -193,7 +193,10 @@ cudaError_t launch_shade_batch_sorted(const TraceParams* vp, const int* work_off
 cudaError_t launch_world_to_local(const luxgi_surface_object* objs, int n, float* w2l, cudaStream_t st);
 size_t quad_bytes(int W, int H, int D, int format);
 size_t cell_min_bytes(int W, int H, int D);
-cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, float* dst, cudaStream_t st);
+// The one-bit-per-cell table that follows the cell minima in their buffer.
+const uint32_t* cell_bits(const float* cmin, int W, int H, int D);
+cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, float resolution, float* dst,
+                            cudaStream_t st);
 cudaError_t launch_quad_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);
 size_t pair_bytes(int W, int H, int D, int format);
 cudaError_t launch_pair_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);

@@ -553,12 +553,44 @@ __global__ void cell_min_kernel(const T* __restrict__ src, int W, int H, int D, 
     }
 }
 
-size_t cell_min_bytes(int W, int H, int D) {
-    return sizeof(float) * size_t((W + kCellSide - 1) / kCellSide) * ((H + kCellSide - 1) / kCellSide) *
+// One bit per cell, 32 cells a word: set where the cell minimum is below the
+// march's skip threshold, i.e. where the full-resolution taps may be used.
+// The threshold is march_run's, computed by the same expression.
+__global__ void cell_bits_kernel(const float* __restrict__ cmin, int64_t n, float resolution,
+                                 uint32_t* __restrict__ bits) {
+    const float margin = 4.0f / resolution;
+    const float thr = (margin * 2.0f) * 1.001f;
+    const int64_t words = (n + 31) / 32;
+    for (int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < words; w += int64_t(gridDim.x) * blockDim.x) {
+        uint32_t b = 0;
+        for (int k = 0; k < 32; ++k) {
+            const int64_t i = w * 32 + k;
+            if (i < n && !(cmin[i] >= thr)) b |= 1u << k;
+        }
+        bits[w] = b;
+    }
+}
+
+static int64_t cell_count(int W, int H, int D) {
+    return int64_t((W + kCellSide - 1) / kCellSide) * ((H + kCellSide - 1) / kCellSide) *
            ((D + kCellSide - 1) / kCellSide);
 }
 
-cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, float* dst, cudaStream_t st) {
+// The cell minima (FP32), then the bits, 16-byte aligned.
+static size_t cell_bits_offset(int64_t n) { return (sizeof(float) * size_t(n) + 15) / 16 * 16; }
+
+size_t cell_min_bytes(int W, int H, int D) {
+    const int64_t n = cell_count(W, H, D);
+    return cell_bits_offset(n) + sizeof(uint32_t) * size_t((n + 31) / 32);
+}
+
+const uint32_t* cell_bits(const float* cmin, int W, int H, int D) {
+    return reinterpret_cast<const uint32_t*>(reinterpret_cast<const uint8_t*>(cmin) +
+                                             cell_bits_offset(cell_count(W, H, D)));
+}
+
+cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, float resolution, float* dst,
+                            cudaStream_t st) {
     const int cw = (W + kCellSide - 1) / kCellSide, ch = (H + kCellSide - 1) / kCellSide;
     const int cd = (D + kCellSide - 1) / kCellSide;
     const int64_t n = int64_t(cw) * ch * cd;
@@ -567,7 +599,10 @@ cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, fl
         cell_min_kernel<__half><<<blocks, 256, 0, st>>>(static_cast<const __half*>(src), W, H, D, cw, ch, cd, dst);
     else
         cell_min_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(src), W, H, D, cw, ch, cd, dst);
-    note_launch();
+    const int64_t words = (n + 31) / 32;
+    cell_bits_kernel<<<unsigned(std::min<int64_t>((words + 255) / 256, 4096)), 256, 0, st>>>(
+        dst, n, resolution, const_cast<uint32_t*>(cell_bits(dst, W, H, D)));
+    note_launch(2);
     return cudaGetLastError();
 }
 
