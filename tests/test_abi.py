@@ -83,6 +83,10 @@ def test_create_rejects_bad_descriptors_before_touching_the_device():
     bad = N.VolumeDesc.from_buffer_copy(d)
     bad.uniform.rays_per_probe = 0
     assert lib.luxgi_ddgi_create(ctypes.byref(bad), ctypes.byref(h)) == N.LUXGI_EINVAL
+    for field, value in (("march_budget", -2), ("shade_split", 2), ("shade_split", -2), ("ray_order", 2)):
+        bad = N.VolumeDesc.from_buffer_copy(d)
+        setattr(bad, field, value)
+        assert lib.luxgi_ddgi_create(ctypes.byref(bad), ctypes.byref(h)) == N.LUXGI_EINVAL, field
     assert h.value is None
 
 
