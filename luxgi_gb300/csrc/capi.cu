@@ -182,6 +182,12 @@ int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
     const int C = int(sdf.data.cascades_count);
     const int mv = v->desc.march_variant;
     const int layout = mv >= 6 ? mv - 4 : mv;          // 6..9 -> 2..5
+    // the quad samplers index texels with 32-bit arithmetic
+    auto quad_texels = [](int W, int H, int D) { return uint64_t(W + 1) * uint64_t(H + 1) * uint64_t(D); };
+    if (layout >= 3 && quad_texels(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution) >> 32)
+        return LUXGI_EUNSUPPORTED;
+    if (layout == 4 && quad_texels(sdf.resolution * C, sdf.resolution, sdf.resolution) >> 32)
+        return LUXGI_EUNSUPPORTED;
     const size_t mq = (layout >= 3) ? quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution,
                                                  sdf.format) : 0;
     const size_t sq = (layout == 4)   ? quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format)

@@ -184,23 +184,33 @@ __device__ __forceinline__ void quad_vals(const uint2& q, float* o) {
     o[0] = __low2float(a); o[1] = __high2float(a); o[2] = __low2float(b); o[3] = __high2float(b);
 }
 
+// The quad-packed sample from its integer corner (ix, iy, iz) = the floors
+// of the texel coordinates and the fractions (a, b, c).  Texel indices are
+// 32-bit: the volume holds fewer than 2^32 quad texels (checked when the
+// packed copy is made).
 template <typename T>
-__device__ __forceinline__ float sample3d_quad(const typename Quad<T>::type* __restrict__ q, int W, int H, int D, float u,
-                                               float vv, float w) {
-    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
-    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
-    const float a = x - fx, b = y - fy, c = z - fz;
-    const int qx = imn(imx(int(fx), -1), W - 1) + 1, qy = imn(imx(int(fy), -1), H - 1) + 1;
-    const int z0 = imn(imx(int(fz), 0), D - 1), z1 = imn(imx(int(fz) + 1, 0), D - 1);
-    const size_t QW = size_t(W) + 1, QWH = QW * (size_t(H) + 1);
+__device__ __forceinline__ float quad_lerp(const typename Quad<T>::type* __restrict__ q, int W, int H, int D, float a,
+                                           float b, float c, int ix, int iy, int iz) {
+    const int qx = imn(imx(ix, -1), W - 1) + 1, qy = imn(imx(iy, -1), H - 1) + 1;
+    const int z0 = imn(imx(iz, 0), D - 1), z1 = imn(imx(iz + 1, 0), D - 1);
+    const uint32_t QW = uint32_t(W) + 1u, QWH = QW * (uint32_t(H) + 1u);
+    const uint32_t row = uint32_t(qy) * QW + uint32_t(qx);
     float p0[4], p1[4];
-    quad_vals(__ldg(q + size_t(z0) * QWH + size_t(qy) * QW + qx), p0);
-    quad_vals(__ldg(q + size_t(z1) * QWH + size_t(qy) * QW + qx), p1);
+    quad_vals(__ldg(q + (uint32_t(z0) * QWH + row)), p0);
+    quad_vals(__ldg(q + (uint32_t(z1) * QWH + row)), p1);
     const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
     const float c00 = p0[0] * ia + p0[1] * a, c10 = p0[2] * ia + p0[3] * a;
     const float c01 = p1[0] * ia + p1[1] * a, c11 = p1[2] * ia + p1[3] * a;
     const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
     return c0 * ic + c1 * c;
+}
+
+template <typename T>
+__device__ __forceinline__ float sample3d_quad(const typename Quad<T>::type* __restrict__ q, int W, int H, int D, float u,
+                                               float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    return quad_lerp<T>(q, W, H, D, x - fx, y - fy, z - fz, int(fx), int(fy), int(fz));
 }
 
 // Pair-packed volume: texel (x, y, z) for x in [-1, W-1] holds
@@ -263,14 +273,20 @@ constexpr int kCellSide = 4;
 // combination of values >= m > 0 computed in FP32 is >= m (1 - 2^-20), so
 // such a sample is never used (SDFCommon.glsl:150-158).  The 32 KB a
 // cascade of bits stay in L1, unlike the cell minima they are made from.
-__device__ __forceinline__ bool fine_needed(const SdfView& s, float u, float v, float w) {
+// The same from the floors (ix, iy, iz) of the full-resolution texel
+// coordinates u W - 0.5 ...
+__device__ __forceinline__ bool fine_needed_at(const SdfView& s, int ix, int iy, int iz) {
     if (!s.cell_near) return true;
     const int W = s.res * s.C, H = s.res, D = s.res;
-    const int x0 = imn(imx(int(floorf(u * float(W) - 0.5f)), 0), W - 1);
-    const int y0 = imn(imx(int(floorf(v * float(H) - 0.5f)), 0), H - 1);
-    const int z0 = imn(imx(int(floorf(w * float(D) - 0.5f)), 0), D - 1);
+    const int x0 = imn(imx(ix, 0), W - 1), y0 = imn(imx(iy, 0), H - 1), z0 = imn(imx(iz, 0), D - 1);
     const uint32_t c = uint32_t((z0 / kCellSide) * s.ch + (y0 / kCellSide)) * uint32_t(s.cw) + uint32_t(x0 / kCellSide);
     return (__ldg(s.cell_near + (c >> 5)) >> (c & 31u)) & 1u;
+}
+
+__device__ __forceinline__ bool fine_needed(const SdfView& s, float u, float v, float w) {
+    const int W = s.res * s.C, H = s.res, D = s.res;
+    return fine_needed_at(s, int(floorf(u * float(W) - 0.5f)), int(floorf(v * float(H) - 0.5f)),
+                          int(floorf(w * float(D) - 0.5f)));
 }
 
 // One GL trilinear sample of the full-resolution or mip volume, from the
@@ -397,9 +413,23 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             // (one memory round trip per step) unless the cell minima show
             // their value cannot be used; it is used only where
             // SDFCommon.glsl:150-158 samples the full-resolution SDF
-            const bool need_fine = fine_needed(s, tu, uy, uz);
-            float sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
-            const float sdt = need_fine ? sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz) : 1.0f;
+            float sd, sdt;
+            if (QTEX == kQuad) {
+                // the cell test and the quad sample share the floors of the
+                // full-resolution texel coordinates
+                const float fx = tu * float(TW) - 0.5f, fy = uy * float(s.res) - 0.5f, fz = uz * float(s.res) - 0.5f;
+                const float lx = floorf(fx), ly = floorf(fy), lz = floorf(fz);
+                const int ix = int(lx), iy = int(ly), iz = int(lz);
+                const bool need_fine = fine_needed_at(s, ix, iy, iz);
+                sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
+                sdt = need_fine ? quad_lerp<T>(static_cast<const typename Quad<T>::type*>(s.sdf_quad), TW, s.res,
+                                               s.res, fx - lx, fy - ly, fz - lz, ix, iy, iz)
+                                : 1.0f;
+            } else {
+                const bool need_fine = fine_needed(s, tu, uy, uz);
+                sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
+                sdt = need_fine ? sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz) : 1.0f;
+            }
             if (sd < chunk) {
                 ++m.fine;
                 if (sdt < margin * 2.0f) sd = sdt;
