@@ -205,6 +205,34 @@ __device__ __forceinline__ float quad_lerp(const typename Quad<T>::type* __restr
     return c0 * ic + c1 * c;
 }
 
+// quad_lerp for coordinates u, v, w in [0, 1] (or NaN): the floors of u W -
+// 0.5 ... then lie in [-1, W - 1] (a NaN converts to 0), so the x and y
+// clamps of quad_lerp never bind and only the z planes are clamped.  Same
+// texels, same arithmetic.
+template <typename T>
+__device__ __forceinline__ float quad_lerp_unit(const typename Quad<T>::type* __restrict__ q, int W, int H, int D,
+                                                float a, float b, float c, int ix, int iy, int iz) {
+    const int z0 = imx(iz, 0), z1 = imn(iz + 1, D - 1);
+    const uint32_t QW = uint32_t(W) + 1u, QWH = QW * (uint32_t(H) + 1u);
+    const uint32_t row = uint32_t(iy + 1) * QW + uint32_t(ix + 1);
+    float p0[4], p1[4];
+    quad_vals(__ldg(q + (uint32_t(z0) * QWH + row)), p0);
+    quad_vals(__ldg(q + (uint32_t(z1) * QWH + row)), p1);
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float c00 = p0[0] * ia + p0[1] * a, c10 = p0[2] * ia + p0[3] * a;
+    const float c01 = p1[0] * ia + p1[1] * a, c11 = p1[2] * ia + p1[3] * a;
+    const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
+template <typename T>
+__device__ __forceinline__ float sample3d_quad_unit(const typename Quad<T>::type* __restrict__ q, int W, int H, int D,
+                                                    float u, float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    return quad_lerp_unit<T>(q, W, H, D, x - fx, y - fy, z - fz, int(fx), int(fy), int(fz));
+}
+
 template <typename T>
 __device__ __forceinline__ float sample3d_quad(const typename Quad<T>::type* __restrict__ q, int W, int H, int D, float u,
                                                float vv, float w) {
@@ -274,12 +302,12 @@ constexpr int kCellSide = 4;
 // such a sample is never used (SDFCommon.glsl:150-158).  The 32 KB a
 // cascade of bits stay in L1, unlike the cell minima they are made from.
 // The same from the floors (ix, iy, iz) of the full-resolution texel
-// coordinates u W - 0.5 ...
+// coordinates u W - 0.5 ... of coordinates in [0, 1] (or NaN): the floors
+// lie in [-1, W - 1] (NaN converts to 0), so only the lower clamp binds.
 __device__ __forceinline__ bool fine_needed_at(const SdfView& s, int ix, int iy, int iz) {
     if (!s.cell_near) return true;
-    const int W = s.res * s.C, H = s.res, D = s.res;
-    const int x0 = imn(imx(ix, 0), W - 1), y0 = imn(imx(iy, 0), H - 1), z0 = imn(imx(iz, 0), D - 1);
-    const uint32_t c = uint32_t((z0 / kCellSide) * s.ch + (y0 / kCellSide)) * uint32_t(s.cw) + uint32_t(x0 / kCellSide);
+    const uint32_t x0 = uint32_t(imx(ix, 0)), y0 = uint32_t(imx(iy, 0)), z0 = uint32_t(imx(iz, 0));
+    const uint32_t c = ((z0 / kCellSide) * uint32_t(s.ch) + (y0 / kCellSide)) * uint32_t(s.cw) + x0 / kCellSide;
     return (__ldg(s.cell_near + (c >> 5)) >> (c & 31u)) & 1u;
 }
 
@@ -421,9 +449,14 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
                 const float lx = floorf(fx), ly = floorf(fy), lz = floorf(fz);
                 const int ix = int(lx), iy = int(ly), iz = int(lz);
                 const bool need_fine = fine_needed_at(s, ix, iy, iz);
-                sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
-                sdt = need_fine ? quad_lerp<T>(static_cast<const typename Quad<T>::type*>(s.sdf_quad), TW, s.res,
-                                               s.res, fx - lx, fy - ly, fz - lz, ix, iy, iz)
+                // tu, uy, uz lie in [0, 1] (clamped above; tu = (cascade + ux) / C)
+                if (QMIP == kQuad)
+                    sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
+                                               s.mres, tu, uy, uz);
+                else
+                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
+                sdt = need_fine ? quad_lerp_unit<T>(static_cast<const typename Quad<T>::type*>(s.sdf_quad), TW, s.res,
+                                                    s.res, fx - lx, fy - ly, fz - lz, ix, iy, iz)
                                 : 1.0f;
             } else {
                 const bool need_fine = fine_needed(s, tu, uy, uz);
