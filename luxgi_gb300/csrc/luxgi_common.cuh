@@ -835,8 +835,14 @@ __device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1
 // direction part (octEncode of the normalised direction, scaled to texture
 // units) and its probe part (the cell's top-left corner); tex_coord_from_dir
 // adds them exactly as the shader does.
+__device__ __forceinline__ void oct_texel_offset_unit(f3 d, int W, int H, int side, float& nx, float& ny);
+
 __device__ __forceinline__ void oct_texel_offset(f3 dir, int W, int H, int side, float& nx, float& ny) {
-    const f3 d = norm3(dir);
+    oct_texel_offset_unit(norm3(dir), W, H, side, nx, ny);
+}
+
+// oct_texel_offset of a direction that is already unit length.
+__device__ __forceinline__ void oct_texel_offset_unit(f3 d, int W, int H, int side, float& nx, float& ny) {
     const float l1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
     const float inv = 1.0f / l1;
     float ox = d.x * inv, oy = d.y * inv;
@@ -884,7 +890,9 @@ __device__ __forceinline__ float pow_decode(float x, float e) {
 // sampleIrradiance (DDGICommon.glsl:163-233).  The normal-bias vector and
 // the octahedral coordinate of N are the same for the 8 cage probes and are
 // computed once.
-template <int UNROLL = 1>
+// FAST (hit shading, compared by tolerance): the probe-to-point direction is
+// normalised once and the distance taken from the same reciprocal root.
+template <int UNROLL = 1, bool FAST = false>
 __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, f3 P, f3 N, f3 Wo) {
     const f3 start{u.start_position[0], u.start_position[1], u.start_position[2]};
     const f3 stp{u.step[0], u.step[1], u.step[2]};
@@ -919,14 +927,24 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         // probe index g0 + g1 X + g2 X Y sits in atlas cell (g0 + g1 X, g2)
         const int cell_x = g[0] + g[1] * cnt[0], cell_y = g[2];
         const f3 ptp = add3(sub3(P, ppos), vb);
-        const f3 dir = norm3(mul3(ptp, -1.0f));
-        float tu, tv;
-        {
+        float tu, tv, dist;
+        if (FAST) {
+            // textureCoordFromDirection(-normalize(-ptp)) normalises ptp once
+            // more; here the unit vector and the distance share one
+            // reciprocal square root
+            const float d2 = dot3(ptp, ptp);
+            const float rl = rsqrtf(d2);
+            float ox, oy;
+            oct_texel_offset_unit(mul3(ptp, rl), u.depth_width, u.depth_height, u.depth_probe_side, ox, oy);
+            cell_texel_origin(cell_x, cell_y, u.depth_width, u.depth_height, u.depth_probe_side, ox, oy, tu, tv);
+            dist = d2 * rl;
+        } else {
+            const f3 dir = norm3(mul3(ptp, -1.0f));
             float ox, oy;
             oct_texel_offset(mul3(dir, -1.0f), u.depth_width, u.depth_height, u.depth_probe_side, ox, oy);
             cell_texel_origin(cell_x, cell_y, u.depth_width, u.depth_height, u.depth_probe_side, ox, oy, tu, tv);
+            dist = len3(ptp);
         }
-        const float dist = len3(ptp);
         float mm[2];
         bilinear_cell_v<2>(A.dist, A.storage, u.depth_width, u.depth_height, tu, tv, mm);
         const float mean = mm[0];

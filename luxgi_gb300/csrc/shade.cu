@@ -41,7 +41,7 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
             sample_surface<true>(p.surf, hp, nrm, thr, s0, s1);
             rad = s0;
             if (p.bounce) {
-                const f3 e = sample_irradiance<UNROLL>(p.u, p.prev, hp, nrm, mul3(dir, -1.0f));
+                const f3 e = sample_irradiance<UNROLL, true>(p.u, p.prev, hp, nrm, mul3(dir, -1.0f));
                 const f3 diff{s1.x / kPi, s1.y / kPi, s1.z / kPi};
                 rad = add3(rad, mulv3(mul3(diff, p.intensity), e));
             }
