@@ -424,13 +424,12 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
         const ExactDiv div_md = exact_div(md), div_c = exact_div(float(C)), div_voxel = exact_div(voxel);
         float t = m.t;
         int step = m.step;
-        for (; step < max_steps && t < m.is_y; ++step) {
-            if (budget <= 0) {
-                m.t = t;
-                m.step = step;
-                return false;
-            }
-            --budget;
+        // steps this call may take in the cascade: up to the cap, and no
+        // more than the budget (a march that would step past the budget is
+        // suspended where it stands)
+        const int room = max_steps - step;
+        const int last = step + (budget < room ? budget : room);
+        for (; step < last && t < m.is_y; ++step) {
             const f3 sp = add3(wpos, mul3(dir, t));
             // getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
             const float ux = clampf(xdiv(sp.x - cx, div_md) + 0.5f, 0.0f, 1.0f);
@@ -485,6 +484,13 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             }
             t = t + mx(sd * 1.0f, voxel);
         }
+        if (step < max_steps && t < m.is_y) {
+            // the budget ran out first
+            m.t = t;
+            m.step = step;
+            return false;
+        }
+        budget -= step - m.step;
         m.steps += step;
         m.in_cascade = 0;
     }
