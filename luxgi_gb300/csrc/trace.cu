@@ -204,7 +204,7 @@ __device__ __forceinline__ void march_resume(const TraceParams& p0, const TraceP
 }
 
 template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX>
-__global__ void __launch_bounds__(256, MIN_BLOCKS) march_kernel(const TraceParams p) {
+__global__ void __launch_bounds__(128, MIN_BLOCKS * 2) march_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= p.work) return;
     march_ray<SdfT, QMIP, QTEX>(p, idx);
@@ -386,12 +386,12 @@ static unsigned resume_blocks() {
 template <typename SdfT, int MINB, int QMIP, int QTEX>
 static cudaError_t launch_march_variant(const TraceParams& p, cudaStream_t st, const TraceParams& rp,
                                         cudaEvent_t after_first) {
-    const unsigned mblocks = unsigned((p.work + 255) / 256);
+    const unsigned mblocks = unsigned((p.work + 127) / 128);
     if (p.budget1 > 0) {
         const cudaError_t e = cudaMemsetAsync(p.qcount, 0, 2 * sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
     }
-    march_kernel<SdfT, MINB, QMIP, QTEX><<<mblocks, 256, 0, st>>>(p);
+    march_kernel<SdfT, MINB, QMIP, QTEX><<<mblocks, 128, 0, st>>>(p);
     note_launch();
     if (after_first) {
         const cudaError_t e = cudaEventRecord(after_first, st);
