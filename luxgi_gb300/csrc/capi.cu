@@ -94,6 +94,13 @@ int alloc_split(luxgi_ddgi_volume* v, int64_t work) {
     return LUXGI_OK;
 }
 
+// The march samples the SDF with 32-bit texel indices: fewer than 2^32
+// texels in the packed volume.
+bool sdf_texels_fit(const luxgi_sdf_desc& s) {
+    const uint64_t r = uint64_t(s.resolution > 0 ? s.resolution : 0);
+    return r * uint64_t(s.data.cascades_count) * r * r < (uint64_t(1) << 32);
+}
+
 SdfView sdf_view(const luxgi_sdf_desc& s) {
     SdfView v{};
     v.data = s.data;
@@ -659,6 +666,7 @@ int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const
     if (C < 1 || C > 4 || sdf->resolution < 4 || sdf->mip_resolution < 1 || !sdf->sdf || !sdf->mip) return LUXGI_EINVAL;
     if (sdf->resolution != int(sdf->data.resolution)) return LUXGI_EINVAL;
     if (sdf->format != LUXGI_STORAGE_FP32 && sdf->format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    if (!sdf_texels_fit(*sdf)) return LUXGI_EUNSUPPORTED;
     if (!surf->objects || !surf->tiles || !surf->chunks || !surf->culled_objects || !surf->depth) return LUXGI_EINVAL;
     if (surf->data.resolution == 0) return LUXGI_EINVAL;
     if (v->desc.light_mode == LUXGI_LIGHT_PER_HIT && (!surf->direct_light || !surf->albedo)) return LUXGI_EINVAL;
@@ -906,6 +914,7 @@ int luxgi_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s, 
     if (!s->tiles || !s->gbuffer0 || !s->gbuffer1 || s->data.resolution < 1) return LUXGI_EINVAL;
     if (L->num_lights > 0 && (!sdf->sdf || !sdf->mip || sdf->data.cascades_count < 1)) return LUXGI_EINVAL;
     if (sdf->format != LUXGI_STORAGE_FP32 && sdf->format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    if (L->num_lights > 0 && !sdf_texels_fit(*sdf)) return LUXGI_EUNSUPPORTED;
     for (int i = 0; i < L->num_lights; ++i) {
         const float t = L->lights[i].type;
         if (t != float(LUXGI_LIGHT_DIRECTIONAL) && t != float(LUXGI_LIGHT_SPOT) && t != float(LUXGI_LIGHT_POINT))

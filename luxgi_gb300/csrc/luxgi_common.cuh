@@ -168,6 +168,34 @@ __device__ __forceinline__ float sample3d(const T* __restrict__ v, int W, int H,
     return c0 * ic + c1 * c;
 }
 
+// sample3d for coordinates u, v, w in [0, 1] (or NaN): the floors of u W -
+// 0.5 ... lie in [-1, W - 1] (a NaN converts to 0), so each corner index
+// needs one side of its clamp, and texel indices are 32-bit (volumes of
+// fewer than 2^32 texels, checked when the SDF is bound).  Same texels,
+// same arithmetic.
+template <typename T>
+__device__ __forceinline__ float sample3d_unit(const T* __restrict__ v, int W, int H, int D, float u, float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    const float a = x - fx, b = y - fy, c = z - fz;
+    const int ix = int(fx), iy = int(fy), iz = int(fz);
+    const uint32_t x0 = uint32_t(imx(ix, 0)), x1 = uint32_t(imn(ix + 1, W - 1));
+    const uint32_t y0 = uint32_t(imx(iy, 0)), y1 = uint32_t(imn(iy + 1, H - 1));
+    const uint32_t z0 = uint32_t(imx(iz, 0)), z1 = uint32_t(imn(iz + 1, D - 1));
+    const uint32_t Wu = uint32_t(W), WH = Wu * uint32_t(H);
+    const uint32_t r00 = y0 * Wu + z0 * WH, r10 = y1 * Wu + z0 * WH;
+    const uint32_t r01 = y0 * Wu + z1 * WH, r11 = y1 * Wu + z1 * WH;
+    const float t000 = load_val(v, r00 + x0), t100 = load_val(v, r00 + x1);
+    const float t010 = load_val(v, r10 + x0), t110 = load_val(v, r10 + x1);
+    const float t001 = load_val(v, r01 + x0), t101 = load_val(v, r01 + x1);
+    const float t011 = load_val(v, r11 + x0), t111 = load_val(v, r11 + x1);
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float c00 = t000 * ia + t100 * a, c10 = t010 * ia + t110 * a;
+    const float c01 = t001 * ia + t101 * a, c11 = t011 * ia + t111 * a;
+    const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
 // Quad-packed volume: texel (x, y, z) for x in [-1, W-1], y in [-1, H-1]
 // holds (v[x, y], v[x+1, y], v[x, y+1], v[x+1, y+1]) of plane z with the
 // indices clamped to the volume, at [z][y + 1][x + 1] of a (W+1) x (H+1) x D
@@ -459,8 +487,19 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
                                 : 1.0f;
             } else {
                 const bool need_fine = fine_needed(s, tu, uy, uz);
-                sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
-                sdt = need_fine ? sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz) : 1.0f;
+                if (QMIP == kPlain)
+                    sd = sample3d_unit<T>(static_cast<const T*>(s.mip), MW, s.mres, s.mres, tu, uy, uz);
+                else if (QMIP == kQuad)
+                    sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
+                                               s.mres, tu, uy, uz);
+                else
+                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
+                if (!need_fine)
+                    sdt = 1.0f;
+                else if (QTEX == kPlain)
+                    sdt = sample3d_unit<T>(static_cast<const T*>(s.sdf), TW, s.res, s.res, tu, uy, uz);
+                else
+                    sdt = sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz);
             }
             if (sd < chunk) {
                 ++m.fine;
