@@ -3,22 +3,31 @@
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                 [--workload NAME]
 
-A step is one frame of the probe update over the whole volume: ray
-generation, SDF march, hit shading, irradiance + distance blend with the
-border copy.  The metric is probe-rays/s = probes x rays x frames / time.
+A frame is one probe update of the whole volume: ray generation, SDF march,
+hit shading, irradiance + distance blend with the border copy.  A step is
+the workload's 16-frame update sequence.  The metric is probe-rays/s =
+probes x rays x frames / time.
 
   value        device-resident inputs, CUDA events around each frame on the
                launching stream; a 256 MB L2 flush runs between frames
                (outside the events)
   e2e          the same frames through the C ABI with host buffers: each
-               step uploads the frame's direct-light atlas from pinned host
-               memory, updates, and reads both probe atlases back
-  roofline     the trace kernel: algorithmic SDF bytes (mip + full-res
+               frame uploads its direct-light atlas from pinned host memory,
+               updates, and reads both probe atlases back
+  roofline     the march kernel: algorithmic SDF bytes (mip + full-res
                trilinear taps actually taken + normal taps, counted per ray
                in an untimed debug pass of the same frames) per launch over
                its event time, against the measured HBM copy bandwidth
   cpu_baseline the CPU oracle (FP32, OpenMP, all host threads) on a bounded
-               sample of probes of the same workload
+               sample of the same workload
+  atlas_rel_err_vs_fp64
+               per atlas (irradiance, distance), frames 0-2: the GPU's
+               atlases against the FP64 oracle's trace + blend of a seeded
+               probe sample, fed the GPU's previous atlases
+  the benchmark spec   the batched (48 uneven volumes, one launch per stage, graph,
+               autotuned) and served (Poisson arrivals, memory-budget
+               admission) forms on the same GPU, and the batched form's
+               probe-rays/s over the plain form's `value`
 
 --impl reference times that CPU restatement of the reference shaders alone
 (the reference itself is a Windows Vulkan renderer with no CPU path and no
@@ -61,6 +70,10 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serve200: length of the timed Poisson run")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serve200: requests per second, all sessions")
     ap.add_argument("--serve-budget-gb", type=float, default=120.0, help="serve200: device-memory budget")
+    ap.add_argument("--frames-per-step", type=int, default=16, help="frames of the volume in one step")
+    ap.add_argument("--no-north-star", action="store_true", help="skip the batched and served forms")
+    ap.add_argument("--ns-serve-seconds", type=float, default=8.0,
+                    help="north-star leg: length of the timed serving run")
     return ap.parse_args()
 
 
@@ -81,7 +94,7 @@ class Clocks:
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -145,11 +158,8 @@ def traffic_from_profile(workload: str, kernel: str, work_items: int):
 
 
 # ------------------------------------------------------------- CPU oracle leg
-def cpu_baseline(w, host, rot, seconds: float, gpu_frame0=None):
-    """FP32 oracle trace + blend on a bounded sample of probes, all threads.
-    Also the FP64 irradiance error of the GPU frame-0 atlases on a sample."""
-    import numpy as np
-
+def cpu_baseline(w, host, rot, seconds: float):
+    """FP32 oracle trace + blend on a bounded sample of probes, all threads."""
     import oracle
 
     vd = w.volume.desc()
@@ -168,29 +178,69 @@ def cpu_baseline(w, host, rot, seconds: float, gpu_frame0=None):
         if elapsed * 4 > seconds or n >= P:
             break
         n = min(P, max(n * 2, int(n * seconds / 2 / max(elapsed, 1e-3))))
-    out = {"value": n * R / elapsed, "unit": "probe-rays/s", "cores": threads, "kind": "port",
-           "sample": f"{n} probes x {R} rays x 1 frame of {w.name} (oracle FP32 trace + blend, {elapsed:.2f} s)"}
-    err = None
-    if gpu_frame0 is not None:
-        gi, _ = gpu_frame0
-        m = min(P, 64)
-        r64, _ = oracle.trace(vd, inp, rot, 0, precision=1, probes=(0, m), want_info=False)
-        d64 = oracle.ray_dirs(rot, R, 1)
-        i64, _ = oracle.blend(vd, d64, r64, first=True, precision=1, border=True, probes=(0, m))
-        u = vd.uniform
-        n_ = u.irradiance_probe_side
-        XY = u.probe_counts[0] * u.probe_counts[1]
-        errs = []
-        for p in range(m):
-            cx, cy = p % XY, p // XY
-            ys = slice(cy * (n_ + 2) + 2, cy * (n_ + 2) + 2 + n_)
-            xs = slice(cx * (n_ + 2) + 2, cx * (n_ + 2) + 2 + n_)
-            a, b = gi[ys, xs, :3].astype(np.float64), i64[ys, xs, :3].astype(np.float64)
-            errs.append(np.abs(a - b) / np.maximum(np.abs(b), 1e-3))
-        e = np.concatenate([x.ravel() for x in errs])
-        err = {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)), "median": float(np.median(e)),
-               "probes": m, "frame": 0}
-    return out, err
+    return {"value": n * R / elapsed, "unit": "probe-rays/s", "cores": threads, "kind": "port",
+            "sample": f"{n} probes x {R} rays x 1 frame of {w.name} (oracle FP32 trace + blend, {elapsed:.2f} s)"}
+
+
+def atlas_error_vs_fp64(w, host, snaps, ranges=8, length=128):
+    """Relative error (|gpu - fp64| / max(|fp64|, 1e-3)) of each atlas, over
+    the cells (interior + border texels) of a seeded sample of probes, for
+    every frame in `snaps` = [(rot, frame, prev (irr, dist) or None, cur
+    (irr, dist))].  The FP64 oracle traces and blends the sample itself,
+    fed the GPU's previous atlases (the bounce source and the hysteresis
+    history), so each frame is checked on its own inputs."""
+    import numpy as np
+
+    import oracle
+
+    vd = w.volume.desc()
+    inp = oracle.HostInputs(host, w.volume.light_mode)
+    u = vd.uniform
+    R = u.rays_per_probe
+    P = w.volume.probes
+    length = min(length, P)
+    rng = np.random.default_rng(0xE44)
+    slots = P // length
+    picks = sorted(rng.choice(slots, size=min(ranges, slots), replace=False))
+    spans = [(int(k) * length, int(k) * length + length) for k in picks]
+    XY = u.probe_counts[0] * u.probe_counts[1]
+    errs = {"irradiance": [], "distance": []}
+    for rot, f, prev, cur in snaps:
+        pi, pd = (None, None) if prev is None else prev
+        for p0, p1 in spans:
+            r64, _ = oracle.trace(vd, inp, rot, f, pi, pd, precision=1, probes=(p0, p1), want_info=False)
+            i64, d64 = oracle.blend(vd, oracle.ray_dirs(rot, R, 1), r64, pi, pd, first=(f == 0), precision=1,
+                                    probes=(p0, p1))
+            for key, got, ref, n in (("irradiance", cur[0], i64, u.irradiance_probe_side),
+                                     ("distance", cur[1], d64, u.depth_probe_side)):
+                for p in range(p0, p1):
+                    cx, cy = p % XY, p // XY
+                    ys = slice(1 + cy * (n + 2), 1 + (cy + 1) * (n + 2))
+                    xs = slice(1 + cx * (n + 2), 1 + (cx + 1) * (n + 2))
+                    a = got[ys, xs].astype(np.float64)
+                    b = ref[ys, xs].astype(np.float64)
+                    errs[key].append((np.abs(a - b) / np.maximum(np.abs(b), 1e-3)).ravel())
+    out = {}
+    for key, parts in errs.items():
+        e = np.concatenate(parts)
+        out[key] = {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)), "median": float(np.median(e))}
+    out["probes"] = len(spans) * length
+    out["frames"] = [f for _, f, _, _ in snaps]
+    out["bound"] = 2e-3
+    out["within_bound"] = bool(max(out["irradiance"]["max"], out["distance"]["max"]) <= 2e-3)
+    return out
+
+
+def workload_config(w, world: int, frames_per_step: int) -> dict:
+    """The `config` of a single-volume workload's line (both arms)."""
+    v, sc = w.volume, w.scene
+    return {"workload": w.name, "probes": v.probes, "rays_per_probe": v.rays_per_probe,
+            "probe_counts": list(v.probe_counts), "frames_per_step": frames_per_step,
+            "sdf": f"{sc.sdf_resolution}^3 {'fp16' if sc.sdf_format else 'fp32'}", "primitives": sc.num_primitives,
+            "atlas": sc.atlas_resolution, "octahedral_sides": [v.irradiance_side, v.depth_side],
+            "max_steps": v.max_steps, "light_mode": "per-hit bounce" if v.light_mode else "light cache",
+            "blend": "tensor" if v.blend else "fp32 simt", "storage": "fp16" if v.storage else "fp32",
+            "parallelism": f"replicas{world}", "l2": "256 MB flush between frames (outside the events)"}
 
 
 # ------------------------------------------------------------------- ours
@@ -199,68 +249,66 @@ def run_ours(args, rank: int, world: int):
     import torch
 
     from luxgi_gb300 import DDGIVolume, DeviceScene, HostScene, WORKLOADS, frame_rotation, _native as N
+    from dataclasses import replace
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev_t = torch.device("cuda", local)
     w = WORKLOADS[args.workload]
-    from dataclasses import replace
-
-    if args.march_variant is not None:
-        w = replace(w, volume=replace(w.volume, march_variant=args.march_variant))
-    if args.shade_variant is not None:
-        w = replace(w, volume=replace(w.volume, shade_variant=args.shade_variant))
-    if args.ray_order is not None:
-        w = replace(w, volume=replace(w.volume, ray_order=args.ray_order))
-    if args.march_budget is not None:
-        w = replace(w, volume=replace(w.volume, march_budget=args.march_budget))
-    if args.shade_order is not None:
-        w = replace(w, volume=replace(w.volume, shade_order=args.shade_order))
-    if args.shade_split is not None:
-        w = replace(w, volume=replace(w.volume, shade_split=args.shade_split))
+    for key in ("march_variant", "shade_variant", "ray_order", "march_budget", "shade_order", "shade_split"):
+        val = getattr(args, key)
+        if val is not None:
+            w = replace(w, volume=replace(w.volume, **{key: val}))
     v = w.volume
     P, R = v.probes, v.rays_per_probe
+    F = max(1, args.frames_per_step)
     host = HostScene(w.scene)
     dev = DeviceScene(host, v.light_mode, device=f"cuda:{local}")
     vol = DDGIVolume(v)
     vol.bind_scene(dev)
     seed = 0x5EED + rank
     K, W = args.steps, args.warmup
-    rots = [frame_rotation(seed, f) for f in range(W + K)]
+    nf = (W + K) * F
+    rots = [frame_rotation(seed, f) for f in range(nf)]
     stream = torch.cuda.current_stream()
 
-    # frame 0 (first warm-up frame), kept for the FP64 error check
-    vol.update(rots[0])
-    torch.cuda.synchronize()
-    irr0 = vol.atlases()[0].float().cpu().numpy()
-    for f in range(1, W):
+    # warm-up frames; the first three are kept (previous and new atlases) for
+    # the per-atlas error against the FP64 oracle
+    snaps = []
+    prev = None
+    for f in range(W * F):
         vol.update(rots[f])
+        if f < 3:
+            torch.cuda.synchronize()
+            cur = tuple(a.float().cpu().numpy() for a in vol.atlases())
+            snaps.append((rots[f], f, prev, cur))
+            prev = cur
     torch.cuda.synchronize()
 
     # exact algorithmic bytes of the timed traces (untimed debug pass; the
     # march does not depend on the atlases, so counts equal the timed ones)
     vol.set_debug_rays(True)
     esz = 2 if host.sdf_format == N.STORAGE_FP16 else 4
-    out_b = 8 if v.storage == N.STORAGE_FP16 else 16
     march_bytes = []
     steps_total = 0
     fine_total = 0
-    for f in range(W, W + K):
+    for f in range(W * F, nf):
         vol.trace(rots[f])
         info = vol.rays()[2]
-        s = info[..., 0].to(torch.int64).sum().item()
+        st = info[..., 0].to(torch.int64).sum().item()
         fine = info[..., 2].to(torch.int64).sum().item()
         hits = (info[..., 1] >= 0).sum().item()
-        steps_total += s
+        steps_total += st
         fine_total += fine
         # SDFCommon.glsl reads per step 8 mip taps, per full-resolution sample
         # 8 taps, per hit 6 x 8 normal taps; the march writes a 20-byte record
-        march_bytes.append((s * 8 + fine * 8 + hits * 48) * esz + P * R * 20)
+        march_bytes.append((st * 8 + fine * 8 + hits * 48) * esz + P * R * 20)
     vol.set_debug_rays(False)
     torch.cuda.synchronize()
 
     flush = torch.empty(256 << 20, dtype=torch.int8, device=dev_t)
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    n_t = K * F
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(n_t)]
     vol.set_stage_timing(True)          # CUDA events between the stages, on the launching stream
     stages = []
     clocks = Clocks(local)
@@ -270,10 +318,10 @@ def run_ours(args, rank: int, world: int):
     torch.cuda.synchronize()
     clocks.start()
     t_wall = time.perf_counter()
-    for k in range(K):
+    for k in range(n_t):
         flush.zero_()
         ev[k][0].record(stream)
-        vol.trace(rots[W + k], stream)
+        vol.trace(rots[W * F + k], stream)
         ev[k][1].record(stream)
         vol.probe_update(stream)
         ev[k][2].record(stream)
@@ -286,14 +334,14 @@ def run_ours(args, rank: int, world: int):
         torch.distributed.barrier()
     clk = clocks.stop()
     launches = N.ddgi().luxgi_launch_count() - launches0
-    t_trace = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
-    t_blend = [ev[k][1].elapsed_time(ev[k][2]) for k in range(K)]
-    t_frame = sum(t_trace) + sum(t_blend)          # ms, flush excluded
+    t_trace = [ev[k][0].elapsed_time(ev[k][1]) for k in range(n_t)]
+    t_blend = [ev[k][1].elapsed_time(ev[k][2]) for k in range(n_t)]
+    t_all = sum(t_trace) + sum(t_blend)          # ms, flush excluded
     if world > 1:
-        t = torch.tensor([t_frame], device=dev_t)
+        t = torch.tensor([t_all], device=dev_t)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_frame = float(t.item())
-    value = world * P * R * K / (t_frame / 1e3)
+        t_all = float(t.item())
+    value = world * P * R * n_t / (t_all / 1e3)
 
     # e2e through the C ABI with host buffers: every frame uploads its
     # direct-light atlas from pinned memory and reads both probe atlases
@@ -309,7 +357,7 @@ def run_ours(args, rank: int, world: int):
         irr, dist = vol.atlases()
         irr_h = [torch.empty(irr.shape, dtype=irr.dtype).pin_memory() for _ in range(2)]
         dist_h = [torch.empty(dist.shape, dtype=dist.dtype).pin_memory() for _ in range(2)]
-        erots = [frame_rotation(seed + 1000, f) for f in range(K + 2)]
+        erots = [frame_rotation(seed + 1000, f) for f in range(n_t + 2)]
         up = torch.cuda.Stream(device=dev_t)
         down = torch.cuda.Stream(device=dev_t)
 
@@ -348,22 +396,22 @@ def run_ours(args, rank: int, world: int):
         if world > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
-        e2e_run(range(2, K + 2))
+        e2e_run(range(2, n_t + 2))
         te = time.perf_counter() - t0
         if world > 1:
             t = torch.tensor([te], device=dev_t)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             te = float(t.item())
-        e2e = {"value": world * P * R * K / te, "unit": "probe-rays/s",
-               "h2d_bytes_per_step": int(direct_h[0].numel() * 2 + 36),
-               "d2h_bytes_per_step": int(irr_h[0].numel() * irr_h[0].element_size() +
-                                         dist_h[0].numel() * dist_h[0].element_size()),
+        e2e = {"value": world * P * R * n_t / te, "unit": "probe-rays/s",
+               "h2d_bytes_per_step": F * int(direct_h[0].numel() * 2 + 36),
+               "d2h_bytes_per_step": F * int(irr_h[0].numel() * irr_h[0].element_size() +
+                                             dist_h[0].numel() * dist_h[0].element_size()),
                "overlap": "uploads and readbacks on two more streams, overlapped with the neighbouring frames"}
 
     pk = peaks()
-    avg_trace_ms = sum(t_trace) / K
-    stage_avg = {k: sum(s[k] for s in stages) / K for k in ("setup", "march", "shade", "blend")}
-    avg_bytes = sum(march_bytes) / K
+    avg_trace_ms = sum(t_trace) / n_t
+    stage_avg = {k: sum(s[k] for s in stages) / n_t for k in ("setup", "march", "shade", "blend")}
+    avg_bytes = sum(march_bytes) / n_t
     achieved = avg_bytes / (stage_avg["march"] / 1e3) / 1e9
     traffic = traffic_from_profile(w.name, "march_kernel", P * R)
     roofline = {"kernel": "march_kernel (global-SDF sphere tracing)", "bound": "hbm",
@@ -371,63 +419,58 @@ def run_ours(args, rank: int, world: int):
                 "frac": round(achieved / pk["hbm_gbs"], 4), "peak_source": pk["source"],
                 "traffic": traffic, "algorithmic_bytes_per_launch": int(avg_bytes),
                 "avg_launch_ms": round(stage_avg["march"], 4),
-                "avg_march_steps_per_ray": round(steps_total / (K * P * R), 2),
-                "avg_fine_samples_per_ray": round(fine_total / (K * P * R), 2)}
+                "avg_march_steps_per_ray": round(steps_total / (n_t * P * R), 2),
+                "avg_fine_samples_per_ray": round(fine_total / (n_t * P * R), 2)}
+    ns = None
+    if not args.no_north_star and world == 1:
+        # the batched and served forms on the same GPU (one process: the
+        # scaling run's ranks time the plain form only)
+        del vol, dev, flush
+        torch.cuda.empty_cache()
+        ns = north_star_leg(args, value)
     if rank != 0:
         return
     cpu, err = (None, None)
     if not args.no_cpu:
-        cpu, err = cpu_baseline(w, host, rots[0], args.cpu_seconds, gpu_frame0=(irr0, None))
+        cpu = cpu_baseline(w, host, rots[0], args.cpu_seconds)
+        if snaps:
+            err = atlas_error_vs_fp64(w, host, snaps)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "probe-rays/s", "n_gpus": world, "steps": K,
-        "warmup": W, "ms_per_step": round(t_frame / K, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded analytic scene)",
-        "config": {"workload": w.name, "probes": P, "rays_per_probe": R, "probe_counts": list(v.probe_counts),
-                   "sdf": f"{host.res}^3 {'fp16' if host.sdf_format else 'fp32'}", "atlas": host.atlas,
-                   "octahedral_sides": [v.irradiance_side, v.depth_side], "max_steps": v.max_steps,
-                   "light_mode": "per-hit bounce" if v.light_mode else "light cache",
-                   "blend": "tensor" if v.blend else "fp32 simt", "storage": "fp16" if v.storage else "fp32",
-                   "parallelism": f"replicas{world}", "l2": "256 MB flush between frames (outside the events)"},
-        "stage_ms": {"trace": round(avg_trace_ms, 4), "blend": round(sum(t_blend) / K, 4),
+        "warmup": W, "ms_per_step": round(t_all / K, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp16 sdf, fp32 march" if host.sdf_format else "fp32",
+        "data": "synthetic (seeded analytic scene)",
+        "config": workload_config(w, world, F),
+        "ms_per_frame": round(t_all / n_t, 4),
+        "stage_ms": {"trace": round(avg_trace_ms, 4), "blend": round(sum(t_blend) / n_t, 4),
                      **{k: round(x, 4) for k, x in stage_avg.items()}},
         "wall_s": round(wall, 4),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
-        "irradiance_rel_err_vs_fp64": err, "clocks": clk,
+        "atlas_rel_err_vs_fp64": err, "north_star": ns, "clocks": clk,
     }
     print(json.dumps(line), flush=True)
 
 
 # ----------------------------------------------------------------- batch
-def run_batch(args, rank: int, world: int):
-    """Batching form: 48 uneven volumes, each with its own FP16 SDF scene,
-    tensor-core blend.  `value` is the batched, graph-replayed, autotuned
-    form; `sequential` the same volumes as 48 plain luxgi_ddgi_update calls
-    per frame on the same GPU."""
+def measure_batch(ws, hosts, K: int, W: int, world: int, e2e_on: bool = True, seed: int = 0x5EED) -> dict:
+    """The batching form over workloads `ws` (scenes `hosts`): `value` is
+    the batched, graph-replayed, autotuned form; `sequential` the same
+    volumes as plain luxgi_ddgi_update calls per frame on the same GPU."""
     import numpy as np
     import torch
 
-    from luxgi_gb300 import DDGIBatch, DDGIVolume, DeviceScene, HostScene, frame_rotation, _native as N
-    from luxgi_gb300.scene import batch_workloads
+    from luxgi_gb300 import DDGIBatch, DDGIVolume, DeviceScene, frame_rotation, _native as N
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dev_t = torch.device("cuda", local)
-    count = int(args.workload[len("batch"):] or 48)
-    t0 = time.perf_counter()
-    ws = batch_workloads(count)
+    dev_t = torch.device("cuda", torch.cuda.current_device())
     vols, scenes = [], []
-    for w in ws:
-        host = HostScene(w.scene)
-        dev = DeviceScene(host, w.volume.light_mode, device=f"cuda:{local}")
+    for w, host in zip(ws, hosts):
+        dev = DeviceScene(host, w.volume.light_mode, device=str(dev_t))
         v = DDGIVolume(w.volume)
         v.bind_scene(dev)
-        scenes.append((host, dev))
+        scenes.append(dev)
         vols.append(v)
-    setup_s = time.perf_counter() - t0
     n = len(vols)
     pr = sum(w.volume.probes * w.volume.rays_per_probe for w in ws)
-    K, W = args.steps, args.warmup
-    seed = 0x5EED + rank
     rots = [np.stack([frame_rotation(seed + i, f) for i in range(n)]) for f in range(W + K)]
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.int8, device=dev_t)
@@ -468,7 +511,8 @@ def run_batch(args, rank: int, world: int):
 
     for f in range(W):
         batch_step(f)
-    clocks = Clocks(local)
+    dev_index = torch.cuda.current_device()
+    clocks = Clocks(dev_index)
     launches0 = N.ddgi().luxgi_launch_count()
     clocks.start()
     b_ms = timed(batch_step, range(W, W + K))
@@ -482,10 +526,10 @@ def run_batch(args, rank: int, world: int):
     # second stream while frame k + 1 computes, and frame k + 2 (which
     # overwrites those ping-pong atlases) waits for it
     e2e = None
-    if not args.no_e2e:
+    if e2e_on:
         views = [v.atlases() for v in vols]
-        hosts = [[(torch.empty(i.shape, dtype=i.dtype).pin_memory(), torch.empty(d.shape, dtype=d.dtype).pin_memory())
-                  for i, d in views] for _ in range(2)]
+        hb = [[(torch.empty(i.shape, dtype=i.dtype).pin_memory(), torch.empty(d.shape, dtype=d.dtype).pin_memory())
+               for i, d in views] for _ in range(2)]
         copy = torch.cuda.Stream(device=dev_t)
 
         def e2e_run(frames):
@@ -500,7 +544,7 @@ def run_batch(args, rank: int, world: int):
                 cur = [v.atlases() for v in vols]
                 with torch.cuda.stream(copy):
                     copy.wait_event(done)
-                    for (i, d), (ih, dh) in zip(cur, hosts[b]):
+                    for (i, d), (ih, dh) in zip(cur, hb[b]):
                         ih.copy_(i, non_blocking=True)
                         dh.copy_(d, non_blocking=True)
                     back_done[b] = torch.cuda.Event()
@@ -513,29 +557,94 @@ def run_batch(args, rank: int, world: int):
         t0 = time.perf_counter()
         e2e_run(range(W, W + K))
         te = time.perf_counter() - t0
-        d2h = sum(ih.numel() * ih.element_size() + dh.numel() * dh.element_size() for ih, dh in hosts[0])
+        d2h = sum(ih.numel() * ih.element_size() + dh.numel() * dh.element_size() for ih, dh in hb[0])
         e2e = {"value": world * pr * K / te, "unit": "probe-rays/s", "h2d_bytes_per_step": 36 * n,
                "d2h_bytes_per_step": int(d2h)}
+    out = {"value": value, "ms_per_step": b_ms / K, "probe_rays_per_frame": pr, "volumes": n,
+           "sequential": {"value": round(seq_value, 1), "ms_per_step": round(seq_ms / K, 4),
+                          "what": f"{n} luxgi_ddgi_update calls per frame, same volumes and GPU"},
+           "speedup_vs_sequential": round(value / seq_value, 3), "autotune": tuning,
+           "autotune_s": round(tune_s, 2), "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    batch.close()
+    for v in vols:
+        v.close()
+    del scenes, flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def batch_config(ws, world: int) -> dict:
+    return {"workload": f"batch{len(ws)}_uneven_fp16sdf_tensorblend", "volumes": len(ws),
+            "probe_rays_per_frame": sum(w.volume.probes * w.volume.rays_per_probe for w in ws),
+            "probes": sum(w.volume.probes for w in ws),
+            "rays_per_probe": sorted({w.volume.rays_per_probe for w in ws}),
+            "sdf": sorted({w.scene.sdf_resolution for w in ws}),
+            "atlas": sorted({w.scene.atlas_resolution for w in ws}), "parallelism": f"replicas{world}",
+            "l2": "256 MB flush between frames (outside the events)"}
+
+
+def run_batch(args, rank: int, world: int):
+    """Batching form: 48 uneven volumes, each with its own FP16 SDF scene,
+    tensor-core blend."""
+    import torch
+
+    from luxgi_gb300 import HostScene
+    from luxgi_gb300.scene import batch_workloads
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    count = int(args.workload[len("batch"):] or 48)
+    t0 = time.perf_counter()
+    ws = batch_workloads(count)
+    hosts = [HostScene(w.scene) for w in ws]
+    setup_s = time.perf_counter() - t0
+    b = measure_batch(ws, hosts, args.steps, args.warmup, world, not args.no_e2e, seed=0x5EED + rank)
     if rank != 0:
         return
     line = {
-        "metric": METRIC, "value": round(value, 1), "unit": "probe-rays/s", "n_gpus": world, "steps": K,
-        "warmup": W, "ms_per_step": round(b_ms / K, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 march, fp16 tensor-core blend operands, fp32 accumulate",
-        "data": "synthetic (seeded analytic scenes, one per volume)",
-        "config": {"workload": f"batch{n}_uneven_fp16sdf_tensorblend", "volumes": n, "probe_rays_per_frame": pr,
-                   "probes": sum(w.volume.probes for w in ws),
-                   "rays_per_probe": sorted({w.volume.rays_per_probe for w in ws}),
-                   "sdf": sorted({w.scene.sdf_resolution for w in ws}),
-                   "atlas": sorted({w.scene.atlas_resolution for w in ws}), "parallelism": f"replicas{world}",
-                   "l2": "256 MB flush between frames (outside the events)"},
-        "sequential": {"value": round(seq_value, 1), "ms_per_step": round(seq_ms / K, 4),
-                       "what": f"{n} luxgi_ddgi_update calls per frame, same volumes and GPU"},
-        "speedup_vs_sequential": round(value / seq_value, 3),
-        "autotune": tuning, "autotune_s": round(tune_s, 2), "setup_s": round(setup_s, 2),
-        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        "metric": METRIC, "value": round(b["value"], 1), "unit": "probe-rays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(b["ms_per_step"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 march, fp16 tensor-core blend operands, fp32 accumulate",
+        "data": "synthetic (seeded analytic scenes, one per volume)", "config": batch_config(ws, world),
+        **{k: b[k] for k in ("sequential", "speedup_vs_sequential", "autotune", "autotune_s", "e2e",
+                             "gpu_launches", "clocks")},
+        "setup_s": round(setup_s, 2),
     }
     print(json.dumps(line), flush=True)
+
+
+def north_star_leg(args, plain_value: float) -> dict:
+    """The forms the benchmark spec's target compares with the plain FP32
+    single-volume form (`plain_value`): the batched form of 48 uneven
+    volumes (FP16 SDFs, tensor-core blend) and a served run of 200 sessions
+    over the same 48 workloads (session i runs workload i mod 48, with its
+    own resident copy of the scene and atlases), Poisson arrivals at
+    --serve-rate under a --serve-budget-gb budget."""
+    from luxgi_gb300 import HostScene
+    from luxgi_gb300.scene import batch_workloads
+
+    t0 = time.perf_counter()
+    ws = batch_workloads(48)
+    hosts = [HostScene(w.scene) for w in ws]
+    setup_s = time.perf_counter() - t0
+    b = measure_batch(ws, hosts, max(args.steps, 10), 3, 1, e2e_on=True)
+    sw = [ws[i % len(ws)] for i in range(200)]
+    sh = [hosts[i % len(ws)] for i in range(200)]
+    s = measure_serve(sw, sh, args.serve_rate, args.ns_serve_seconds, args.serve_budget_gb, warm_seconds=2.0)
+    return {
+        "batched": {"value": round(b["value"], 1), "unit": "probe-rays/s", "config": batch_config(ws, 1),
+                    "ms_per_frame": round(b["ms_per_step"], 4), "frames": max(args.steps, 10),
+                    **{k: b[k] for k in ("sequential", "speedup_vs_sequential", "autotune", "e2e", "gpu_launches",
+                                         "clocks")}},
+        "served": {**s, "config": {"sessions": 200, "workloads": f"the {len(ws)} batched workloads, session i runs "
+                                   f"workload i mod {len(ws)} with its own resident scene and atlases",
+                                   "rate_per_s": args.serve_rate, "seconds": args.ns_serve_seconds,
+                                   "budget_gb": args.serve_budget_gb}},
+        "ratio_batched_vs_plain": round(b["value"] / plain_value, 4),
+        "target_ratio": 3.0,
+        "setup_s": round(setup_s, 2),
+    }
 
 
 # ------------------------------------------------------- surface lighting
@@ -807,25 +916,18 @@ def run_sdf_build(args, rank: int, world: int):
 
 
 # ----------------------------------------------------------------- serve
-def run_serve(args, rank: int, world: int):
-    """Serving form: sessions with batching-form volumes and scenes, Poisson
-    arrivals, admission by a device-memory budget with LRU eviction.
-    `value` is the probe-rays/s the server completed over the run (submit of
-    the first request to completion of the last); latency per request is
-    submit to completion seen by the host."""
+def measure_serve(ws, hosts, rate: float, seconds: float, budget_gb: float, warm_seconds: float = 3.0,
+                  seed: int = 0x5EED) -> dict:
+    """Sessions (one per workload) behind a server with a device-memory
+    budget, Poisson arrivals at `rate` over all sessions for `seconds`.
+    `value` is the probe-rays/s the server completed (submit of the first
+    request to completion of the last); latency is submit to completion
+    seen by the host."""
     import torch
 
-    from luxgi_gb300 import HostScene, Server
-    from luxgi_gb300.scene import batch_workloads
+    from luxgi_gb300 import Server
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    count = int(args.workload[len("serve"):] or 200)
-    t0 = time.perf_counter()
-    ws = batch_workloads(count, seed=0xC0FFEE + 5)
-    hosts = [HostScene(w.scene) for w in ws]
-    gen_s = time.perf_counter() - t0
-    budget = int(args.serve_budget_gb * (1 << 30))
+    budget = int(budget_gb * (1 << 30))
     srv = Server(budget, max_group=64, max_inflight=3)
     ids = [srv.add_session(w.volume, h) for w, h in zip(ws, hosts)]
     t0 = time.perf_counter()
@@ -835,65 +937,91 @@ def run_serve(args, rank: int, world: int):
         except Exception:
             break                        # budget full: the rest are admitted on demand
     admit_s = time.perf_counter() - t0
-    # warm-up: every session's first frame, untimed
-    srv.run_poisson(ids, rate=args.serve_rate, seconds=min(3.0, args.serve_seconds), seed=0x5EED + rank)
+    # warm-up: every session's first frames, untimed
+    srv.run_poisson(ids, rate=rate, seconds=min(warm_seconds, seconds), seed=seed)
     srv.stats(reset=True)
-    clocks = Clocks(local)
+    clocks = Clocks(torch.cuda.current_device())
     clocks.start()
-    srv.run_poisson(ids, rate=args.serve_rate, seconds=args.serve_seconds, seed=0x5EED + 1 + rank)
+    srv.run_poisson(ids, rate=rate, seconds=seconds, seed=seed + 1)
     clk = clocks.stop()
     st = srv.stats()
     srv.close()
+    value = st["probe_rays"] / st["wall_s"] if st["wall_s"] > 0 else 0.0
+    return {"value": round(value, 1), "unit": "probe-rays/s",
+            "latency_ms": {"p50": round(st["latency_ms_p50"], 3), "p95": round(st["latency_ms_p95"], 3),
+                           "p99": round(st["latency_ms_p99"], 3), "mean": round(st["latency_ms_mean"], 3),
+                           "max": round(st["latency_ms_max"], 3)},
+            "served": {k: st[k] for k in ("submitted", "completed", "admissions", "evictions", "rejected", "groups",
+                                          "max_overlap", "resident_sessions", "peak_resident_bytes")},
+            "mean_group": round(st["mean_group"], 2), "wall_s": round(st["wall_s"], 3),
+            "admission_s": round(admit_s, 2), "clocks": clk}
+
+
+def run_serve(args, rank: int, world: int):
+    """Serving form: sessions with batching-form volumes and scenes, Poisson
+    arrivals, admission by a device-memory budget with LRU eviction."""
+    import torch
+
+    from luxgi_gb300 import HostScene
+    from luxgi_gb300.scene import batch_workloads
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    count = int(args.workload[len("serve"):] or 200)
+    t0 = time.perf_counter()
+    ws = batch_workloads(count, seed=0xC0FFEE + 5)
+    hosts = [HostScene(w.scene) for w in ws]
+    gen_s = time.perf_counter() - t0
+    s = measure_serve(ws, hosts, args.serve_rate, args.serve_seconds, args.serve_budget_gb, seed=0x5EED + rank)
     if rank != 0:
         return
-    value = st["probe_rays"] / st["wall_s"] if st["wall_s"] > 0 else 0.0
     line = {
-        "metric": METRIC, "value": round(value * world, 1), "unit": "probe-rays/s", "n_gpus": world,
-        "steps": int(st["completed"]), "warmup": 0, "ms_per_step": round(st["latency_ms_mean"], 4),
+        "metric": METRIC, "value": round(s["value"] * world, 1), "unit": "probe-rays/s", "n_gpus": world,
+        "steps": int(s["served"]["completed"]), "warmup": 0, "ms_per_step": s["latency_ms"]["mean"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32 march, fp16 tensor-core blend operands, fp32 accumulate",
         "data": "synthetic (seeded analytic scenes, one per session)",
         "config": {"workload": f"serve{count}_poisson{int(args.serve_rate)}_budget{args.serve_budget_gb:g}GB",
                    "sessions": count, "rate_per_s": args.serve_rate, "seconds": args.serve_seconds,
-                   "budget_bytes": budget, "max_group": 64, "streams": 3, "parallelism": f"replicas{world}"},
-        "latency_ms": {"p50": round(st["latency_ms_p50"], 3), "p95": round(st["latency_ms_p95"], 3),
-                       "p99": round(st["latency_ms_p99"], 3), "mean": round(st["latency_ms_mean"], 3),
-                       "max": round(st["latency_ms_max"], 3)},
-        "served": {k: st[k] for k in ("submitted", "completed", "admissions", "evictions", "rejected", "groups",
-                                      "max_overlap", "resident_sessions", "peak_resident_bytes")},
-        "mean_group": round(st["mean_group"], 2), "wall_s": round(st["wall_s"], 3),
-        "setup_s": {"scenes": round(gen_s, 2), "admission": round(admit_s, 2)},
-        "e2e": {"value": round(value * world, 1), "unit": "probe-rays/s", "h2d_bytes_per_step": 36,
+                   "budget_bytes": int(args.serve_budget_gb * (1 << 30)), "max_group": 64, "streams": 3,
+                   "parallelism": f"replicas{world}"},
+        "latency_ms": s["latency_ms"], "served": s["served"], "mean_group": s["mean_group"], "wall_s": s["wall_s"],
+        "setup_s": {"scenes": round(gen_s, 2), "admission": s["admission_s"]},
+        "e2e": {"value": round(s["value"] * world, 1), "unit": "probe-rays/s", "h2d_bytes_per_step": 36,
                 "d2h_bytes_per_step": 0},
-        "clocks": clk,
+        "clocks": s["clocks"],
     }
     print(json.dumps(line), flush=True)
 
 
 # -------------------------------------------------------------- reference
 def run_reference(args, rank: int, world: int):
+    """The CPU restatement of the reference shaders on the host cores, on
+    the GPU arm's workload: each step is one whole frame of the volume
+    (every probe and ray; trace with the per-hit bounce from the arm's own
+    previous frame, blend, border), a bounded sample of the GPU arm's
+    16-frame step.  Loads only the oracle and the scene generator."""
     if rank != 0:
         return
     import oracle
-    from luxgi_gb300 import HostScene, WORKLOADS, frame_rotation
+    from luxgi_gb300.scene import HostScene, WORKLOADS
 
     w = WORKLOADS[args.workload]
     v = w.volume
     host = HostScene(w.scene)
-    vd = v.desc()
+    vd = v.desc(derive=oracle.derive_uniform)
     inp = oracle.HostInputs(host, v.light_mode)
     R = v.rays_per_probe
-    # a step is 1,024 probes from the middle of the volume (two 32x16 slices
-    # of the production grid): enough work for every host thread, a bounded
-    # sample of the frame
-    n = min(v.probes, 1024)
-    p0 = (v.probes - n) // 2
-    rng = (p0, p0 + n)
-    rots = [frame_rotation(0x5EED, f) for f in range(args.warmup + args.steps)]
+    fp16 = v.storage == 1
+    rots = [oracle.frame_rotation(0x5EED, f) for f in range(args.warmup + args.steps)]
+    state = {"irr": None, "dist": None, "frames": 0}
 
     def step(rot):
-        rays, _ = oracle.trace(vd, inp, rot, 0, precision=0, probes=rng, want_info=False)
-        oracle.blend(vd, oracle.ray_dirs(rot, R, 0), rays, first=True, precision=0, border=False, probes=rng)
+        f = state["frames"]
+        rays, _ = oracle.trace(vd, inp, rot, f, state["irr"], state["dist"], precision=0, want_info=False)
+        state["irr"], state["dist"] = oracle.blend(vd, oracle.ray_dirs(rot, R, 0, fp16), rays, state["irr"],
+                                                   state["dist"], first=(f == 0), precision=0)
+        state["frames"] = f + 1
 
     for f in range(args.warmup):
         step(rots[f])
@@ -901,15 +1029,15 @@ def run_reference(args, rank: int, world: int):
     for k in range(args.steps):
         step(rots[args.warmup + k])
     dt = time.perf_counter() - t0
-    value = n * R * args.steps / dt
+    value = v.probes * R * args.steps / dt
     cores = oracle.num_threads()
-    sample = (f"probes {rng[0]}-{rng[1] - 1} x {R} rays per step of {w.name} "
-              "(CPU restatement of the reference shaders, FP32 trace + blend)")
+    sample = (f"one whole frame per step ({v.probes} probes x {R} rays, per-hit bounce from the previous frame, "
+              f"blend and border) of {w.name}, of the GPU arm's {args.frames_per_step}-frame steps; "
+              "CPU restatement of the reference shaders, FP32")
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "probe-rays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic (seeded analytic scene)",
-            "config": {"workload": w.name, "probes": v.probes, "rays_per_probe": R, "parallelism": "cpu"},
+            "data": "synthetic (seeded analytic scene)", "config": workload_config(w, world, args.frames_per_step),
             "cpu_baseline": {"value": round(value, 1), "unit": "probe-rays/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 1), "unit": "probe-rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

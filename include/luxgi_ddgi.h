@@ -69,6 +69,24 @@ enum luxgi_light_mode {
                                   atlases and add albedo/pi * E_prev(hit)
                                   (Raytraced/Lighting.glsl:79-84)              */
 };
+enum luxgi_color_format {      /* the surface cache's colour textures       */
+    LUXGI_COLOR_RGBA16F    = 0,  /* 4 x FP16, 8 bytes a texel                  */
+    LUXGI_COLOR_R11G11B10F = 1   /* packed unsigned floats, 4 bytes a texel:
+                                    R bits 0-10 and G bits 11-21 (5-bit
+                                    exponent, 6-bit mantissa), B bits 22-31
+                                    (5-bit exponent, 5-bit mantissa), bias 15,
+                                    no sign; alpha reads as 1.  The engine's
+                                    SurfaceEmissive and SurfaceLightCache
+                                    (TextureFormat::R11G11B10,
+                                    GlobalSurfaceAtlas.cpp:410-411)           */
+};
+enum luxgi_gbuffer_format {     /* the surface cache's G-buffers              */
+    LUXGI_GBUFFER_RGBA32F = 0,   /* float4 a texel                             */
+    LUXGI_GBUFFER_RGBA16F = 1    /* 4 x FP16 a texel: the engine's
+                                    SurfaceGBuffer-Color / -Normal
+                                    (TextureFormat::RGBA16,
+                                    GlobalSurfaceAtlas.cpp:407-408)           */
+};
 enum luxgi_blend {
     LUXGI_BLEND_FP32   = 0,    /* FP32 SIMT contraction                        */
     LUXGI_BLEND_TENSOR = 1     /* tcgen05 FP16 operands, FP32 accumulation;
@@ -148,7 +166,10 @@ typedef struct luxgi_sdf_desc {
     const void* mip;               /* device, (mres*C) x mres x mres          */
 } luxgi_sdf_desc;
 
-/* The surface cache (GlobalSurfacePublic, GlobalSurfaceAtlas.h:31-44). */
+/* The surface cache (GlobalSurfacePublic, GlobalSurfaceAtlas.h:31-44).
+ * The colour textures (light_cache, direct_light, emissive) are all of
+ * `light_format`, the G-buffers of `gbuffer_format`; the engine's own
+ * textures are R11G11B10F and RGBA16F (GlobalSurfaceAtlas.cpp:407-411). */
 typedef struct luxgi_surface_desc {
     luxgi_surface_data          data;
     int32_t                     num_objects;
@@ -157,22 +178,27 @@ typedef struct luxgi_surface_desc {
     const luxgi_surface_tile*   tiles;          /* device                     */
     const uint32_t*             chunks;         /* device, 40^3 u32           */
     const uint32_t*             culled_objects; /* device, [0] = used words   */
-    void*                       light_cache;    /* device RGBA16F res^2 (mode A
+    void*                       light_cache;    /* device res^2 (mode A
                                                    sampled; written by inject) */
     const float*                depth;          /* device R32F res^2, 1 = empty*/
-    const uint16_t*             direct_light;   /* device RGBA16F res^2       */
+    const void*                 direct_light;   /* device res^2               */
     const uint8_t*              albedo;         /* device RGBA8 UNORM res^2   */
-    const float*                gbuffer0;       /* device float4: albedo.rgb,
+    const void*                 gbuffer0;       /* device res^2: albedo.rgb,
                                                    world.x (SDFDeferredColor
                                                    .frag:114)                 */
-    const float*                gbuffer1;       /* device float4: oct normal.xy,
+    const void*                 gbuffer1;       /* device res^2: oct normal.xy,
                                                    world.yz (:115)            */
     const uint8_t*              pbr;            /* device RGBA8 UNORM res^2
                                                    (SurfaceGBufferPRB): r
                                                    metallic, g roughness; NULL
                                                    = metallic 0, roughness 1  */
-    const uint16_t*             emissive;       /* device RGBA16F res^2
+    const void*                 emissive;       /* device res^2
                                                    (SurfaceEmissive), or NULL */
+    int32_t                     light_format;   /* luxgi_color_format of
+                                                   light_cache, direct_light,
+                                                   emissive and the lit atlas
+                                                   of luxgi_surface_light     */
+    int32_t                     gbuffer_format; /* luxgi_gbuffer_format       */
 } luxgi_surface_desc;
 
 /* Volume configuration: DDGIUniform plus the IrradianceVolume fields the
@@ -375,6 +401,18 @@ int luxgi_ddgi_get_rays(const luxgi_ddgi_volume* vol, luxgi_ddgi_rays* out);
  * LUXGI_ETIMEOUT (and clears the word) when a bounded device-side wait of
  * the tensor-core blend gave up since the last check, else LUXGI_OK. */
 int luxgi_ddgi_check_status(luxgi_ddgi_volume* vol, void* stream);
+/* Test aid for the bounded device waits of the tensor-core blend (no
+ * reference counterpart).  wait_cycles > 0 bounds each of its mbarrier waits
+ * at that many SM clock cycles on this volume's later probe updates (0
+ * restores the default, about 2 s).  withhold != 0 makes the next probe
+ * update -- that one only -- skip one operand load in its first CTA, so the
+ * matrix-multiply issuer's wait for it runs out: the kernel then stops
+ * issuing work, drains the loads and multiplies it issued, frees its tensor
+ * memory, returns, and raises the volume's status word, which
+ * luxgi_ddgi_check_status reports as LUXGI_ETIMEOUT.  That frame's atlases
+ * are incomplete; the device and the volume stay usable.  LUXGI_EUNSUPPORTED
+ * for a volume without the tensor-core blend. */
+int luxgi_ddgi_set_blend_wait_test(luxgi_ddgi_volume* vol, int64_t wait_cycles, int withhold);
 /* Record per-ray march steps / hit cascade on the next traces (test aid). */
 int luxgi_ddgi_set_debug_rays(luxgi_ddgi_volume* vol, int enable);
 /* Copy the current atlases (the copy the next frame reads) to host buffers
@@ -391,7 +429,9 @@ int luxgi_ddgi_load_atlases(luxgi_ddgi_volume* vol, const void* irradiance_host,
 /* Mode A infinite bounce (SDFAtlasIndirectLight.frag:44-67) over the
  * raster footprint of every tile (see luxgi_surface_light): light_cache =
  * direct_light + intensity * (a - a * metallic)/pi * sampleIrradiance(prev
- * atlases), a = min(albedo, 0.9), albedo, normal, position and metallic
+ * atlases), rounded to the light format (direct_light and light_cache may be
+ * the same texture, as the engine's additive draw into SurfaceLightCache
+ * is), a = min(albedo, 0.9), albedo, normal, position and metallic
  * sampled bilinearly at the fragment's atlas coordinate.  Texels outside
  * every tile keep their light_cache value.  When infinite bounce is off or
  * no frame is done yet the footprint gets direct_light unchanged. */
@@ -607,12 +647,15 @@ typedef struct luxgi_surface_lighting {
 } luxgi_surface_lighting;
 
 /* SDF-shadowed direct lighting of the surface cache: per footprint pixel,
- * for each light of its tile in index order, `out` (device RGBA16F res^2)
- * += (BRDF * radiance * cos * shadow * attenuation, 1), rounded to FP16
- * after each light like the additive blend into a 16-bit target
- * (SDFDeferredLight.frag:41-129, Raytraced/BRDF.glsl:65-81).  The shadow is
- * a global-SDF march towards the light from position + normal * bias with
- * start bias 2 voxels and no hit normal (SDFDeferredLight.frag:95-118). */
+ * for each light of its tile in index order, `out` (device res^2 of the
+ * surface's light_format) += (BRDF * radiance * cos * shadow * attenuation,
+ * 1), rounded to the target's format after each light like the additive
+ * blend into the render target: FP16 per channel (RGBA16F) or the 11/11/10-
+ * bit unsigned floats, nearest even, negative to 0 (R11G11B10F, no alpha)
+ * (SDFDeferredLight.frag:41-129, Raytraced/BRDF.glsl:65-81).  The emissive
+ * copy rounds the same way.  The shadow is a global-SDF march towards the
+ * light from position + normal * bias with start bias 2 voxels and no hit
+ * normal (SDFDeferredLight.frag:95-118). */
 int luxgi_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surface,
                         const luxgi_surface_lighting* lighting, void* out, void* stream);
 

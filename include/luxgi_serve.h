@@ -55,7 +55,10 @@ typedef struct luxgi_server_desc {
     double   sim_rate;             /* SIM: modelled probe-rays per second
                                       (0 = 1e9)                               */
     double   sim_admit_s;          /* SIM: modelled admission time (s)        */
-    int32_t  reserved[4];
+    float    sim_evict_s;          /* SIM: modelled eviction copy (s, <= 60),
+                                      run with the server's lock released as
+                                      the device copy is                      */
+    int32_t  reserved[3];
 } luxgi_server_desc;
 
 /* A session's scene, HOST memory owned by the caller (valid until the

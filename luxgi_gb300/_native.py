@@ -32,6 +32,10 @@ LIGHT_POINT = 2
 MAX_LIGHTS = 32
 BLEND_FP32 = 0
 BLEND_TENSOR = 1
+COLOR_RGBA16F = 0
+COLOR_R11G11B10F = 1
+GBUFFER_RGBA32F = 0
+GBUFFER_RGBA16F = 1
 
 
 class DDGIUniform(ctypes.Structure):
@@ -75,7 +79,8 @@ class SurfaceDesc(ctypes.Structure):
     _fields_ = [("data", SurfaceData), ("num_objects", c_int32), ("num_tiles", c_int32), ("objects", c_void_p),
                 ("tiles", c_void_p), ("chunks", c_void_p), ("culled_objects", c_void_p), ("light_cache", c_void_p),
                 ("depth", c_void_p), ("direct_light", c_void_p), ("albedo", c_void_p), ("gbuffer0", c_void_p),
-                ("gbuffer1", c_void_p), ("pbr", c_void_p), ("emissive", c_void_p)]
+                ("gbuffer1", c_void_p), ("pbr", c_void_p), ("emissive", c_void_p), ("light_format", c_int32),
+                ("gbuffer_format", c_int32)]
 
 
 class Light(ctypes.Structure):
@@ -152,7 +157,7 @@ class BatchTuning(ctypes.Structure):
 class ServerDesc(ctypes.Structure):
     _fields_ = [("memory_budget", c_uint64), ("executor", c_int32), ("max_group", c_int32),
                 ("max_inflight", c_int32), ("reserved0", c_int32), ("tuning", BatchTuning), ("sim_rate", ctypes.c_double),
-                ("sim_admit_s", ctypes.c_double), ("reserved", c_int32 * 4)]
+                ("sim_admit_s", ctypes.c_double), ("sim_evict_s", c_float), ("reserved", c_int32 * 3)]
 
 
 class SessionScene(ctypes.Structure):
@@ -232,6 +237,7 @@ DDGI_API = [
     ("luxgi_ddgi_get_rays", c_int, [c_void_p, POINTER(Rays)]),
     ("luxgi_ddgi_check_status", c_int, [c_void_p, c_void_p]),
     ("luxgi_ddgi_set_debug_rays", c_int, [c_void_p, c_int]),
+    ("luxgi_ddgi_set_blend_wait_test", c_int, [c_void_p, c_int64, c_int]),
     ("luxgi_ddgi_load_atlases", c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     ("luxgi_ddgi_inject_indirect", c_int, [c_void_p, c_void_p]),
     ("luxgi_ddgi_save_atlases", c_int, [c_void_p, c_void_p, c_void_p, POINTER(c_int32), c_void_p]),

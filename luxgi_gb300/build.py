@@ -28,6 +28,9 @@ NO_FMAD = {"trace.cu", "setup.cu", "surface.cu", "sdfbuild.cu"}
 # shading is compared with the restatement by tolerance: approximate
 # division and square root
 FAST_DIV = {"shade.cu"}
+# host code built without FMA contraction, so that its results (the seeded
+# frame rotations) are the same on x86 and aarch64 hosts
+HOST_NO_CONTRACT = {"capi.cu"}
 CUDA_SOURCES = ["trace.cu", "shade.cu", "blend.cu", "blend_tc.cu", "setup.cu", "surface.cu", "sdfbuild.cu", "capi.cu",
                 "batch.cu", "server.cu"]
 
@@ -74,6 +77,8 @@ def build_cuda(verbose: bool = False) -> Path:
                 # device code without FMA contraction, and the host code too
                 # (gcc contracts by default on aarch64)
                 cmd[1:1] = ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
+            if src in HOST_NO_CONTRACT:
+                cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
             if src in FAST_DIV:
                 cmd[1:1] = ["-prec-div=false", "-prec-sqrt=false"]
             if verbose:

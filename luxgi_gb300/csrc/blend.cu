@@ -3,9 +3,9 @@
 //
 // Every probe of a volume traces the same R directions in a frame (one
 // rotation per frame, DDGIRenderer.cpp:267-272), so the texel x ray weights
-//   irradiance  W[t][r] = max(0, D_t . dir_r)                 (ProbeUpdate.glsl:219)
-//   distance    W[t][r] = pow(max(0, D_t . dir_r), sharpness) (ProbeUpdate.glsl:217)
-// (zeroed below 1e-8, ProbeUpdate.glsl:222) and the normalisers
+//   irradiance  W[t][r] = max(0, D_t . dir_r)                 (ProbeUpdate.glsl:90)
+//   distance    W[t][r] = pow(max(0, D_t . dir_r), sharpness) (ProbeUpdate.glsl:88)
+// (zeroed below 1e-8, ProbeUpdate.glsl:93) and the normalisers
 // 1 / (2 sum_r W[t][r]) are shared by all probes.  The blend is then
 //   out[p][t][c] = n[t] * sum_r W[t][r] * ray[p][r][c]
 // followed by the gamma encode, the hysteresis mix and the store; the

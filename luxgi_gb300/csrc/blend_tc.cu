@@ -67,11 +67,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait: false when the clock budget ran out or another role gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, long long budget) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > budget) {
             *abort_flag = 1;
             return false;
         }
@@ -156,6 +156,8 @@ struct TcArgs {
     int kb_b;                             // K blocks of B (ceil(R / 64))
     int lo_offset;                        // column of the lo half in A (distance), 0 otherwise
     int tiles;
+    long long wait_cycles;                // bound of every mbarrier wait, SM clock cycles
+    int withhold;                         // test aid: block 0 skips the first A load of its first tile
 };
 
 // Writes one channel of interior texel (tx, ty) of cell (cx, cy) and its
@@ -191,8 +193,10 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
     uint64_t* bfull = bars + 2 * kStages;        // [1]
     uint64_t* tfull = bars + 2 * kStages + 1;    // [2]
     uint64_t* tempty = bars + 2 * kStages + 3;   // [2]
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 5);
+    uint64_t* mdrain = bars + 2 * kStages + 5;   // [1] MMAs issued before an abort
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 6);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const long long budget = g.wait_cycles > 0 ? g.wait_cycles : kWaitCycles;
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const uint32_t tmem_cols = (2 * g.N <= 32) ? 32 : (2 * g.N <= 64) ? 64 : (2 * g.N <= 128) ? 128 : (2 * g.N <= 256) ? 256 : 512;
@@ -207,6 +211,7 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         mbar_init(&tfull[1], 1);
         mbar_init(&tempty[0], kEpilogueThreads);
         mbar_init(&tempty[1], kEpilogueThreads);
+        mbar_init(mdrain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -220,6 +225,9 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     const uint32_t idesc = idesc_f16(128, g.N);
+    // phase of the last A load issued into each stage (producer thread)
+    uint32_t pending[kStages];
+    for (int s = 0; s < kStages; ++s) pending[s] = 0xFFFFFFFFu;
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
@@ -228,13 +236,17 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
             for (int kb = 0; kb < g.kb_b; ++kb) tma_load_2d(smem_b + kb * b_block_bytes, &map_b, bfull, kb * kKBlock, 0);
             int stage = 0;
             uint32_t phase = 0;
-            uint32_t pending[kStages];
-            for (int s = 0; s < kStages; ++s) pending[s] = 0xFFFFFFFFu;
             bool ok = true;
             for (int tile = blockIdx.x; tile < g.tiles && ok; tile += gridDim.x) {
                 for (int kb = 0; kb < g.kb_a && ok; ++kb) {
-                    ok = mbar_wait(&empty[stage], phase ^ 1u, abort_flag);
+                    ok = mbar_wait(&empty[stage], phase ^ 1u, abort_flag, budget);
                     if (!ok) break;
+                    if (g.withhold && blockIdx.x == 0 && tile == 0 && kb == 0) {
+                        // test aid: this stage's load is never issued, so the
+                        // MMA issuer's bounded wait on it runs out
+                        if (++stage == kStages) { stage = 0; phase ^= 1u; }
+                        continue;
+                    }
                     const int x = (kb < g.kb_b) ? kb * kKBlock : g.lo_offset + (kb - g.kb_b) * kKBlock;
                     mbar_expect_tx(&full[stage], kStageBytes);
                     tma_load_2d(smem_a + stage * kStageBytes, &map_a, &full[stage], x, tile * 128);
@@ -242,33 +254,23 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                     if (++stage == kStages) { stage = 0; phase ^= 1u; }
                 }
             }
-            if (!ok) {
-                // drain the loads this thread issued before giving up
-                for (int s = 0; s < kStages; ++s) {
-                    if (pending[s] == 0xFFFFFFFFu) continue;
-                    const long long t0 = clock64();
-                    while (!mbar_try_wait(&full[s], pending[s]) && clock64() - t0 < kWaitCycles) {}
-                }
-                const long long t0 = clock64();
-                while (!mbar_try_wait(bfull, 0) && clock64() - t0 < kWaitCycles) {}
-            }
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            bool ok = mbar_wait(bfull, 0, abort_flag);
+            bool ok = mbar_wait(bfull, 0, abort_flag, budget);
             int stage = 0;
             uint32_t phase = 0;
             int it = 0;
             for (int tile = blockIdx.x; tile < g.tiles && ok; tile += gridDim.x, ++it) {
                 const int acc = it & 1;
                 const uint32_t use = uint32_t(it >> 1);
-                ok = mbar_wait(&tempty[acc], (use & 1u) ^ 1u, abort_flag);
+                ok = mbar_wait(&tempty[acc], (use & 1u) ^ 1u, abort_flag, budget);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + uint32_t(acc * g.N);
                 for (int kb = 0; kb < g.kb_a && ok; ++kb) {
-                    ok = mbar_wait(&full[stage], phase, abort_flag);
+                    ok = mbar_wait(&full[stage], phase, abort_flag, budget);
                     if (!ok) break;
                     tc_fence_after();
                     const int bk = (kb < g.kb_b) ? kb : kb - g.kb_b;
@@ -305,7 +307,7 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         for (int tile = blockIdx.x; tile < g.tiles; tile += gridDim.x, ++it) {
             const int acc = it & 1;
             const uint32_t use = uint32_t(it >> 1);
-            ok = mbar_wait(&tfull[acc], use & 1u, abort_flag);
+            ok = mbar_wait(&tfull[acc], use & 1u, abort_flag, budget);
             if (!ok) break;
             tc_fence_after();
             const int p = tile * probes_per_tile + row / g.rows_per_probe;
@@ -335,7 +337,7 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                 }
             }
             if (!DIST && p < g.P && c == 3) {
-                // alpha = 1 (ProbeUpdate.glsl:279) for every texel of the cell
+                // alpha = 1 (ProbeUpdate.glsl:150) for every texel of the cell
                 int ty = t_begin / n, tx = t_begin - ty * n;
                 for (int t = t_begin; t < t_end; ++t, ++tx) {
                     if (tx == n) {
@@ -352,6 +354,27 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
     }
     tc_fence_before();
     __syncthreads();
+    if (*abort_flag) {
+        // A role gave up (every role has left its loop by now): the loads and
+        // multiplies already issued are drained, each wait bounded, before the
+        // shared memory and the tensor memory they target are released.
+        if (warp == 0 && lane == 0) {
+            for (int s = 0; s < kStages; ++s) {
+                if (pending[s] == 0xFFFFFFFFu) continue;
+                const long long t0 = clock64();
+                while (!mbar_try_wait(&full[s], pending[s]) && clock64() - t0 < budget) {}
+            }
+            const long long t0 = clock64();
+            while (!mbar_try_wait(bfull, 0) && clock64() - t0 < budget) {}
+        } else if (warp == 1 && lane == 0) {
+            // one commit tracks every multiply this thread issued
+            mma_commit(mdrain);
+            const long long t0 = clock64();
+            while (!mbar_try_wait(mdrain, 0) && clock64() - t0 < budget) {}
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
     if (warp == 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(tmem_cols));
@@ -438,6 +461,8 @@ void fill_args(const TcBlendParams& p, TcArgs& g) {
     g.status = p.status;
     const int64_t rows = int64_t(p.P) * g.rows_per_probe;
     g.tiles = int((rows + 127) / 128);
+    g.wait_cycles = p.wait_cycles > 0 ? p.wait_cycles : kWaitCycles;
+    g.withhold = p.withhold;
 }
 
 // Tensor maps, shared memory and grid of one blend kind of one volume.

@@ -94,11 +94,13 @@ int alloc_split(luxgi_ddgi_volume* v, int64_t work) {
     return LUXGI_OK;
 }
 
-// The march samples the SDF with 32-bit texel indices: fewer than 2^32
-// texels in the packed volume.
+// The march samples the SDF and its mip with 32-bit texel indices: fewer
+// than 2^32 texels in each packed volume.
 bool sdf_texels_fit(const luxgi_sdf_desc& s) {
     const uint64_t r = uint64_t(s.resolution > 0 ? s.resolution : 0);
-    return r * uint64_t(s.data.cascades_count) * r * r < (uint64_t(1) << 32);
+    const uint64_t m = uint64_t(s.mip_resolution > 0 ? s.mip_resolution : 0);
+    const uint64_t C = uint64_t(s.data.cascades_count);
+    return r * C * r * r < (uint64_t(1) << 32) && m * C * m * m < (uint64_t(1) << 32);
 }
 
 SdfView sdf_view(const luxgi_sdf_desc& s) {
@@ -122,14 +124,21 @@ SurfaceView surface_view(const luxgi_surface_desc& s, int light_mode, const floa
     v.chunks = s.chunks;
     v.culled = s.culled_objects;
     v.depth = s.depth;
+    v.color0_format = s.light_format;
     if (light_mode == LUXGI_LIGHT_PER_HIT) {
-        v.color0 = reinterpret_cast<const __half*>(s.direct_light);
+        v.color0 = s.direct_light;
         v.color1 = s.albedo;
     } else {
-        v.color0 = static_cast<const __half*>(s.light_cache);
+        v.color0 = s.light_cache;
         v.color1 = nullptr;
     }
     return v;
+}
+
+// The surface formats this build reads and writes.
+bool surface_formats_valid(const luxgi_surface_desc& s) {
+    return (s.light_format == LUXGI_COLOR_RGBA16F || s.light_format == LUXGI_COLOR_R11G11B10F) &&
+           (s.gbuffer_format == LUXGI_GBUFFER_RGBA32F || s.gbuffer_format == LUXGI_GBUFFER_RGBA16F);
 }
 
 size_t ray_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 8 : 16; }
@@ -345,6 +354,7 @@ void luxgi::volume_tc_params(const luxgi_ddgi_volume* v, TcBlendParams& p) {
     p.out_irr = v->irr[wr];
     p.out_dist = v->dist[wr];
     p.status = v->status;
+    p.wait_cycles = v->tc_wait_cycles;
     p.storage = d.storage;
     p.first = v->frames == 0;
     p.P = v->P;
@@ -482,6 +492,8 @@ int do_probe_update(luxgi_ddgi_volume* v, cudaStream_t st) {
     if (v->tc) {
         TcBlendParams p;
         volume_tc_params(v, p);
+        p.withhold = v->tc_withhold;
+        v->tc_withhold = 0;
         e = launch_tc_blend(p, st);
     } else {
         BlendParams p;
@@ -669,6 +681,7 @@ int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const
     if (!sdf_texels_fit(*sdf)) return LUXGI_EUNSUPPORTED;
     if (!surf->objects || !surf->tiles || !surf->chunks || !surf->culled_objects || !surf->depth) return LUXGI_EINVAL;
     if (surf->data.resolution == 0) return LUXGI_EINVAL;
+    if (!surface_formats_valid(*surf)) return LUXGI_EINVAL;
     if (v->desc.light_mode == LUXGI_LIGHT_PER_HIT && (!surf->direct_light || !surf->albedo)) return LUXGI_EINVAL;
     if (v->desc.light_mode == LUXGI_LIGHT_CACHE && !surf->light_cache) return LUXGI_EINVAL;
     const int nobj = int(surf->data.objects_count);
@@ -780,6 +793,14 @@ int luxgi_ddgi_check_status(luxgi_ddgi_volume* v, void* stream) {
     return e == cudaSuccess ? LUXGI_ETIMEOUT : cuda_status(e);
 }
 
+int luxgi_ddgi_set_blend_wait_test(luxgi_ddgi_volume* v, int64_t wait_cycles, int withhold) {
+    if (!v || wait_cycles < 0) return LUXGI_EINVAL;
+    if (withhold && !v->tc) return LUXGI_EUNSUPPORTED;
+    v->tc_wait_cycles = wait_cycles;
+    v->tc_withhold = withhold ? 1 : 0;
+    return LUXGI_OK;
+}
+
 int luxgi_ddgi_set_stage_timing(luxgi_ddgi_volume* v, int enable) {
     if (!v) return LUXGI_EINVAL;
     if (enable && !v->stage_ev[0]) {
@@ -848,9 +869,8 @@ int luxgi_ddgi_inject_indirect(luxgi_ddgi_volume* v, void* stream) {
     A.storage = v->desc.storage;
     const int bounce = (v->desc.infinite_bounce && v->frames != 0) ? 1 : 0;
     return cuda_status(launch_inject(v->desc.uniform, surface_view(s, LUXGI_LIGHT_CACHE), s.gbuffer0, s.gbuffer1,
-                                     s.pbr, reinterpret_cast<const __half*>(s.direct_light),
-                                     static_cast<__half*>(s.light_cache), A, s.num_tiles, v->desc.intensity, bounce,
-                                     static_cast<cudaStream_t>(stream)));
+                                     s.gbuffer_format, s.pbr, s.direct_light, s.light_cache, s.light_format, A,
+                                     s.num_tiles, v->desc.intensity, bounce, static_cast<cudaStream_t>(stream)));
 }
 
 int luxgi_ddgi_sample_irradiance(const luxgi_ddgi_volume* v, const float* pos, const float* nrm, const float* wo,
@@ -912,6 +932,7 @@ int luxgi_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s, 
     if (L->num_tiles < 0 || L->num_tiles > 65535 || (L->num_tiles > 0 && !L->tiles)) return LUXGI_EINVAL;
     if (!(L->shadow_bias >= 0.0f) || L->max_steps < 1) return LUXGI_EINVAL;
     if (!s->tiles || !s->gbuffer0 || !s->gbuffer1 || s->data.resolution < 1) return LUXGI_EINVAL;
+    if (!surface_formats_valid(*s)) return LUXGI_EINVAL;
     if (L->num_lights > 0 && (!sdf->sdf || !sdf->mip || sdf->data.cascades_count < 1)) return LUXGI_EINVAL;
     if (sdf->format != LUXGI_STORAGE_FP32 && sdf->format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
     if (L->num_lights > 0 && !sdf_texels_fit(*sdf)) return LUXGI_EUNSUPPORTED;
@@ -920,7 +941,7 @@ int luxgi_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s, 
         if (t != float(LUXGI_LIGHT_DIRECTIONAL) && t != float(LUXGI_LIGHT_SPOT) && t != float(LUXGI_LIGHT_POINT))
             return LUXGI_EINVAL;
     }
-    return cuda_status(launch_surface_light(sdf_view(*sdf), *s, *L, static_cast<__half*>(out),
+    return cuda_status(launch_surface_light(sdf_view(*sdf), *s, *L, out,
                                             static_cast<cudaStream_t>(stream)));
 }
 

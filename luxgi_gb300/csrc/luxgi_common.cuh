@@ -131,8 +131,9 @@ __device__ __forceinline__ f3 probe_location(const luxgi_ddgi_uniform& u, uint32
     const uint32_t rem = index - gz * div_xy.d;
     const uint32_t gy = fdiv(rem, div_x);
     const uint32_t gx = rem - gy * div_x.d;
-    return f3{u.step[0] * float(int(gx)) + u.start_position[0], u.step[1] * float(int(gy)) + u.start_position[1],
-              u.step[2] * float(int(gz)) + u.start_position[2]};
+    return f3{__fadd_rn(__fmul_rn(u.step[0], float(int(gx))), u.start_position[0]),
+              __fadd_rn(__fmul_rn(u.step[1], float(int(gy))), u.start_position[1]),
+              __fadd_rn(__fmul_rn(u.step[2], float(int(gz))), u.start_position[2])};
 }
 
 __device__ __forceinline__ f3 probe_location(const luxgi_ddgi_uniform& u, int index) {
@@ -564,6 +565,95 @@ __device__ __forceinline__ MarchHit march_sdf(const SdfView& s, f3 origin, f3 di
 }
 
 // ------------------------------------------------ surface atlas sampling
+// ------------------------------------------------ packed R11G11B10F colour
+// The unsigned small floats of the R11G11B10F format, written from the
+// format's definition: a 5-bit exponent with bias 15 and an M-bit mantissa
+// (M = 6 for R and G, 5 for B), no sign.  Exponent 0 holds the denormals
+// m * 2^-(14 + M), exponent 31 Inf (m = 0) or NaN.  Encoding rounds to
+// nearest, ties to even; negative values and -0 become 0, NaN stays NaN, a
+// finite value that rounds past the largest finite one becomes Inf.
+template <int M>
+__device__ __forceinline__ float ufloat_decode(uint32_t v) {
+    const uint32_t e = v >> M, m = v & ((1u << M) - 1u);
+    if (e == 0u) return float(m) * __uint_as_float(uint32_t(127 - 14 - M) << 23);   // m * 2^-(14+M), exact
+    if (e == 31u) return __uint_as_float(m ? 0x7FC00000u : 0x7F800000u);
+    return __uint_as_float(((e + 112u) << 23) | (m << (23 - M)));
+}
+template <int M>
+__device__ __forceinline__ uint32_t ufloat_encode(float x) {
+    if (x != x) return (31u << M) | ((1u << M) - 1u);
+    if (!(x > 0.0f)) return 0u;
+    const uint32_t b = __float_as_uint(x);
+    if (b >= 0x7F800000u) return 31u << M;
+    if (b < (113u << 23)) {
+        // below 2^-14: a multiple of 2^-(14+M) (the power-of-two scale is
+        // exact); a result of 2^M is the smallest normal's code
+        return uint32_t(rintf(__fmul_rn(x, __uint_as_float(uint32_t(127 + 14 + M) << 23))));
+    }
+    constexpr uint32_t sh = 23 - M;
+    const uint32_t r = (b + ((1u << (sh - 1)) - 1u) + ((b >> sh) & 1u)) >> sh;   // (exponent << M) | mantissa
+    const uint32_t e = (r >> M) - 112u;                                             // rebias 127 -> 15
+    return e >= 31u ? (31u << M) : ((e << M) | (r & ((1u << M) - 1u)));
+}
+__device__ __forceinline__ uint32_t pack_r11g11b10(float r, float g, float b) {
+    return ufloat_encode<6>(r) | (ufloat_encode<6>(g) << 11) | (ufloat_encode<5>(b) << 22);
+}
+__device__ __forceinline__ void unpack_r11g11b10(uint32_t v, float* out) {
+    out[0] = ufloat_decode<6>(v & 0x7FFu);
+    out[1] = ufloat_decode<6>((v >> 11) & 0x7FFu);
+    out[2] = ufloat_decode<5>(v >> 22);
+}
+
+// One texel of a surface colour texture (luxgi_color_format): rgba, alpha 1
+// for R11G11B10F.  color_texel_ro reads through the read-only cache.
+__device__ __forceinline__ void color_texel_ro(const void* p, int fmt, size_t texel, float* out) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        unpack_r11g11b10(__ldg(static_cast<const uint32_t*>(p) + texel), out);
+        out[3] = 1.0f;
+    } else {
+        const uint2 raw = __ldg(static_cast<const uint2*>(p) + texel);
+        const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
+        const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
+        out[0] = __low2float(a); out[1] = __high2float(a); out[2] = __low2float(b); out[3] = __high2float(b);
+    }
+}
+__device__ __forceinline__ void color_texel(const void* p, int fmt, size_t texel, float* out) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        unpack_r11g11b10(static_cast<const uint32_t*>(p)[texel], out);
+        out[3] = 1.0f;
+    } else {
+        const uint2 raw = static_cast<const uint2*>(p)[texel];
+        const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
+        const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
+        out[0] = __low2float(a); out[1] = __high2float(a); out[2] = __low2float(b); out[3] = __high2float(b);
+    }
+}
+// Stores rgba (alpha dropped for R11G11B10F), rounded to the format.
+__device__ __forceinline__ void color_store(void* p, int fmt, size_t texel, const float* v) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        static_cast<uint32_t*>(p)[texel] = pack_r11g11b10(v[0], v[1], v[2]);
+    } else {
+        const __half2 a = __floats2half2_rn(v[0], v[1]);
+        const __half2 b = __floats2half2_rn(v[2], v[3]);
+        uint2 raw;
+        raw.x = *reinterpret_cast<const uint32_t*>(&a);
+        raw.y = *reinterpret_cast<const uint32_t*>(&b);
+        static_cast<uint2*>(p)[texel] = raw;
+    }
+}
+// The value a render target of format `fmt` keeps of v (each channel).
+__device__ __forceinline__ void color_round(int fmt, float* v) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        v[0] = ufloat_decode<6>(ufloat_encode<6>(v[0]));
+        v[1] = ufloat_decode<6>(ufloat_encode<6>(v[1]));
+        v[2] = ufloat_decode<5>(ufloat_encode<5>(v[2]));
+        v[3] = 1.0f;
+    } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = __half2float(__float2half_rn(v[c]));
+    }
+}
+
 struct SurfaceView {
     luxgi_surface_data data;
     const luxgi_surface_object* objects;
@@ -571,10 +661,34 @@ struct SurfaceView {
     const luxgi_surface_tile* tiles;
     const uint32_t* chunks;
     const uint32_t* culled;
-    const __half* color0;     // light cache (mode A) or direct light (mode B), RGBA16F
+    const void* color0;       // light cache (mode A) or direct light (mode B)
+    int color0_format;        // luxgi_color_format of color0
     const uint8_t* color1;    // albedo RGBA8 (mode B)
     const float* depth;
 };
+
+// Exact FP32 arithmetic (round to nearest, never contracted into an FMA,
+// IEEE division and square root) whatever the translation unit's flags.
+// The hard cut-offs of the surface sampler (chunk of the hit point, object
+// bounding sphere, OBB margin) are computed with these, like the CPU
+// restatement computes them, so that a hit point lying within an ulp of a
+// cut-off is classified the same way; the continuous weights around them
+// may use the fast forms.
+__device__ __forceinline__ f3 mat4_mul_pt_rn(const float* m, f3 v, float w) {
+    return f3{__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], v.x), __fmul_rn(m[4], v.y)), __fmul_rn(m[8], v.z)),
+                        __fmul_rn(m[12], w)),
+              __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[1], v.x), __fmul_rn(m[5], v.y)), __fmul_rn(m[9], v.z)),
+                        __fmul_rn(m[13], w)),
+              __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[2], v.x), __fmul_rn(m[6], v.y)), __fmul_rn(m[10], v.z)),
+                        __fmul_rn(m[14], w))};
+}
+__device__ __forceinline__ float len3_rn(f3 a) {
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y)), __fmul_rn(a.z, a.z)));
+}
+// a + d * t per component, exact (the hit point of a march record)
+__device__ __forceinline__ f3 ray_point_rn(f3 a, f3 d, float t) {
+    return f3{__fadd_rn(a.x, __fmul_rn(d.x, t)), __fadd_rn(a.y, __fmul_rn(d.y, t)), __fadd_rn(a.z, __fmul_rn(d.z, t))};
+}
 
 __device__ __forceinline__ f3 mat4_mul_pt(const float* m, f3 v, float w) {
     return f3{m[0] * v.x + m[4] * v.y + m[8] * v.z + m[12] * w,
@@ -629,7 +743,7 @@ __device__ __forceinline__ void mat4_inverse(const float* A, float* out) {
 // textureGather texel indices (clamp to edge): (i0,j1),(i1,j1),(i1,j0),(i0,j0)
 struct Gather4 { int i0, i1, j0, j1; };
 __device__ __forceinline__ Gather4 gather_idx(float u, float v, int W, int H) {
-    const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
+    const float x = __fadd_rn(__fmul_rn(u, float(W)), -0.5f), y = __fadd_rn(__fmul_rn(v, float(H)), -0.5f);
     int i0 = int(floorf(x)), j0 = int(floorf(y));
     Gather4 g;
     g.i1 = imn(imx(i0 + 1, 0), W - 1);
@@ -658,15 +772,27 @@ __device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_su
     float nw = clampf(0.0f * n.x + 0.0f * n.y + 1.0f * n.z, 0.0f, 1.0f);
     nw = (nw - 0.05f) / (1.0f - 0.05f);
     if (nw <= 0.0f) return;
-    const f3 tp = mat4_mul_pt(T, local, 1.0f);
+    // The atlas coordinate (au, av) exactly: the reference takes the
+    // bilinear fractions from fract(au * res + 0.5) but the gathered texels
+    // from textureGather's own floor(au * res - 0.5), so at a texel boundary
+    // an ulp of au can pair the fractions with the neighbouring texels; au is
+    // computed like the restatement computes it (tile-space x / y, IEEE
+    // division by the bounds, no contraction), so both sides pair them alike.
+    // The depth (continuous through the visibility ramp) may round freely.
     const float bx = __ldg(&tl->object_bounds[0]), by = __ldg(&tl->object_bounds[1]), bz = __ldg(&tl->object_bounds[2]);
-    const float tdepth = tp.z / bz;
-    const float tu = clampf(tp.x / bx + 0.5f, 0.0f, 1.0f), tv = clampf(tp.y / by + 0.5f, 0.0f, 1.0f);
-    const float au = tu * __ldg(&tl->extends[2]) + __ldg(&tl->extends[0]);
-    const float av = tv * __ldg(&tl->extends[3]) + __ldg(&tl->extends[1]);
+    const float tpx = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T[0], local.x), __fmul_rn(T[4], local.y)),
+                                          __fmul_rn(T[8], local.z)), T[12]);
+    const float tpy = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T[1], local.x), __fmul_rn(T[5], local.y)),
+                                          __fmul_rn(T[9], local.z)), T[13]);
+    const float tpz = T[2] * local.x + T[6] * local.y + T[10] * local.z + T[14];
+    const float tdepth = tpz / bz;
+    const float tu = clampf(__fadd_rn(__fdiv_rn(tpx, bx), 0.5f), 0.0f, 1.0f);
+    const float tv = clampf(__fadd_rn(__fdiv_rn(tpy, by), 0.5f), 0.0f, 1.0f);
+    const float au = __fadd_rn(__fmul_rn(tu, __ldg(&tl->extends[2])), __ldg(&tl->extends[0]));
+    const float av = __fadd_rn(__fmul_rn(tv, __ldg(&tl->extends[3])), __ldg(&tl->extends[1]));
     const float res = float(S.data.resolution);
-    float bu = au * res + 0.5f; bu = bu - floorf(bu);
-    float bv = av * res + 0.5f; bv = bv - floorf(bv);
+    float bu = __fadd_rn(__fmul_rn(au, res), 0.5f); bu = bu - floorf(bu);
+    float bv = __fadd_rn(__fmul_rn(av, res), 0.5f); bv = bv - floorf(bv);
     const float bw0 = (1.0f - bu) * bv, bw1 = bu * bv, bw2 = bu * (1.0f - bv), bw3 = (1.0f - bu) * (1.0f - bv);
     const int R = int(S.data.resolution);
     const Gather4 g = gather_idx(au, av, R, R);
@@ -685,14 +811,9 @@ __device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_su
     if (sw <= 0.0f) return;
     const float w0 = bw0 * dv[0], w1 = bw1 * dv[1], w2 = bw2 * dv[2], w3 = bw3 * dv[3];
     const size_t offs[4] = {o0, o1, o2, o3};
-    float ch[4][3];
+    float ch[4][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const uint2 raw = __ldg(reinterpret_cast<const uint2*>(S.color0) + offs[i]);
-        const __half2 rg = *reinterpret_cast<const __half2*>(&raw.x);
-        const __half2 ba = *reinterpret_cast<const __half2*>(&raw.y);
-        ch[i][0] = __low2float(rg); ch[i][1] = __high2float(rg); ch[i][2] = __low2float(ba);
-    }
+    for (int i = 0; i < 4; ++i) color_texel_ro(S.color0, S.color0_format, offs[i], ch[i]);
     const f3 c0{ch[0][0] * w0 + ch[1][0] * w1 + ch[2][0] * w2 + ch[3][0] * w3,
                 ch[0][1] * w0 + ch[1][1] * w1 + ch[2][1] * w2 + ch[3][1] * w3,
                 ch[0][2] * w0 + ch[1][2] * w1 + ch[2][2] * w2 + ch[3][2] * w3};
@@ -719,9 +840,10 @@ __device__ __forceinline__ float sample_surface(const SurfaceView& S, f3 pos, f3
     out0 = acc0;
     out1 = acc1;
     const float cs = S.data.chunk_size;
-    const int cx = imn(imx(int(floorf(pos.x / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
-    const int cy = imn(imx(int(floorf(pos.y / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
-    const int cz = imn(imx(int(floorf(pos.z / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const float half_res = float(kChunksRes * 0.5f);
+    const int cx = imn(imx(int(floorf(__fadd_rn(__fdiv_rn(pos.x, cs), half_res))), 0), kChunksRes - 1);
+    const int cy = imn(imx(int(floorf(__fadd_rn(__fdiv_rn(pos.y, cs), half_res))), 0), kChunksRes - 1);
+    const int cz = imn(imx(int(floorf(__fadd_rn(__fdiv_rn(pos.z, cs), half_res))), 0), kChunksRes - 1);
     const uint32_t addr = uint32_t(cz * kChunksRes * kChunksRes + cy * kChunksRes + cx);
     uint32_t start = __ldg(S.chunks + addr);
     if (start == 0) return 0.0f;
@@ -732,7 +854,7 @@ __device__ __forceinline__ float sample_surface(const SurfaceView& S, f3 pos, f3
         const uint32_t oaddr = __ldg(S.culled + start++);
         const luxgi_surface_object* ob = S.objects + oaddr;
         const float4 bnd = __ldg(reinterpret_cast<const float4*>(ob->object_bounds));
-        if (len3(sub3(f3{bnd.x, bnd.y, bnd.z}, pos)) > bnd.w) continue;
+        if (len3_rn(sub3(f3{bnd.x, bnd.y, bnd.z}, pos)) > bnd.w) continue;
         float w2l[16];
         if (S.w2l) {
             // inverse(object.transform), computed once per scene by the same
@@ -749,9 +871,10 @@ __device__ __forceinline__ float sample_surface(const SurfaceView& S, f3 pos, f3
             for (int k = 0; k < 16; ++k) M[k] = __ldg(&ob->transform[k]);
             mat4_inverse(M, w2l);
         }
-        const f3 lp = mat4_mul_pt(w2l, pos, 1.0f);
+        const f3 lp = mat4_mul_pt_rn(w2l, pos, 1.0f);
         const float4 e = __ldg(reinterpret_cast<const float4*>(ob->extends));
-        if (fabsf(lp.x) > e.x + thr || fabsf(lp.y) > e.y + thr || fabsf(lp.z) > e.z + thr) continue;
+        if (fabsf(lp.x) > __fadd_rn(e.x, thr) || fabsf(lp.y) > __fadd_rn(e.y, thr) || fabsf(lp.z) > __fadd_rn(e.z, thr))
+            continue;
         const f3 ln = norm3(f3{w2l[0] * wn.x + w2l[4] * wn.y + w2l[8] * wn.z,
                                w2l[1] * wn.x + w2l[5] * wn.y + w2l[9] * wn.z,
                                w2l[2] * wn.x + w2l[6] * wn.y + w2l[10] * wn.z});
@@ -849,18 +972,44 @@ __device__ __forceinline__ void bilinear_repeat_v(const void* p, int storage, in
     }
 }
 
-// bilinear_repeat_v for the probe-cell lookups of sampleIrradiance: every
-// tap there lies inside the atlas, at least one texel from its edge (a cell
-// interior starts 2 texels into its (n+2)-texel cell, the atlas has a
-// 1-texel pad: the taps of a cell span [o + 1, o + n + 2] of the (n+2) XY + 2
-// texels), so REPEAT never wraps and a clamp that never binds guards the
-// index arithmetic in its place.  Same arithmetic as bilinear_repeat_v.
+
+// textureCoordFromDirection (DDGICommon.glsl:141-158) in texel units: the
+// shader forms a UV normalised by the atlas size, (cell corner + octEncode
+// offset) / W, and the sampler turns it back into texels, u * W - 0.5, which
+// FP32 resolves only to W x 6e-8 texel (2e-3 texel in a 32,770-texel-wide
+// atlas).  Here the cell corner (an integer) and the offset inside the cell
+// are kept apart: oct_cell_point gives the sample point inside the cell,
+// (octEncode(d) + 1) / 2 * side - 0.5 per axis, and bilinear_tap_v adds the
+// corner after the floor, so the bilinear fractions keep FP32's precision
+// (~1e-7 texel).  The texels and weights are those of the shader's formula
+// evaluated exactly.
+__device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
+
+__device__ __forceinline__ void oct_cell_point(f3 d, int side, float& rx, float& ry) {
+    const float l1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+    const float inv = 1.0f / l1;
+    float ox = d.x * inv, oy = d.y * inv;
+    if (d.z < 0.0f) {
+        const float tx = (1.0f - fabsf(oy)) * sign_nz(ox);
+        const float ty = (1.0f - fabsf(ox)) * sign_nz(oy);
+        ox = tx; oy = ty;
+    }
+    rx = (ox + 1.0f) * 0.5f * float(side) - 0.5f;
+    ry = (oy + 1.0f) * 0.5f * float(side) - 0.5f;
+}
+
+// Bilinear tap of NC channels at texel (x0 + rx, y0 + ry) of a W-wide atlas,
+// (x0, y0) the interior corner of a probe cell (cell * (side + 2) + 2) and
+// (rx, ry) from oct_cell_point.  rx lies in [-0.5, side - 0.5], so the four
+// texels stay inside the cell and its 1-texel border (the clamp only guards
+// a NaN direction, which converts to the cell's first texel).
 template <int NC>
-__device__ __forceinline__ void bilinear_cell_v(const void* p, int storage, int W, int H, float u, float v, float* out) {
-    const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
-    const float fx = floorf(x), fy = floorf(y);
-    const float a = x - fx, b = y - fy;
-    const int i0 = imn(imx(int(fx), 0), W - 2), j0 = imn(imx(int(fy), 0), H - 2);
+__device__ __forceinline__ void bilinear_tap_v(const void* p, int storage, int W, int side, int x0, int y0, float rx,
+                                               float ry, float* out) {
+    const float fx = fminf(fmaxf(floorf(rx), -1.0f), float(side - 1));
+    const float fy = fminf(fmaxf(floorf(ry), -1.0f), float(side - 1));
+    const float a = rx - fx, b = ry - fy;
+    const int i0 = x0 + int(fx), j0 = y0 + int(fy);
     const int i1 = i0 + 1, j1 = j0 + 1;
     float t00[NC], t10[NC], t01[NC], t11[NC];
     atlas_texel<NC>(p, storage, size_t(j0) * W + i0, t00);
@@ -872,58 +1021,6 @@ __device__ __forceinline__ void bilinear_cell_v(const void* p, int storage, int 
         const float r0 = t00[c] * (1.0f - a) + t10[c] * a, r1 = t01[c] * (1.0f - a) + t11[c] * a;
         out[c] = r0 * (1.0f - b) + r1 * b;
     }
-}
-
-__device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
-
-// textureCoordFromDirection (DDGICommon.glsl:141-158), split into its
-// direction part (octEncode of the normalised direction, scaled to texture
-// units) and its probe part (the cell's top-left corner); tex_coord_from_dir
-// adds them exactly as the shader does.
-__device__ __forceinline__ void oct_texel_offset_unit(f3 d, int W, int H, int side, float& nx, float& ny);
-
-__device__ __forceinline__ void oct_texel_offset(f3 dir, int W, int H, int side, float& nx, float& ny) {
-    oct_texel_offset_unit(norm3(dir), W, H, side, nx, ny);
-}
-
-// oct_texel_offset of a direction that is already unit length.
-__device__ __forceinline__ void oct_texel_offset_unit(f3 d, int W, int H, int side, float& nx, float& ny) {
-    const float l1 = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
-    const float inv = 1.0f / l1;
-    float ox = d.x * inv, oy = d.y * inv;
-    if (d.z < 0.0f) {
-        const float tx = (1.0f - fabsf(oy)) * sign_nz(ox);
-        const float ty = (1.0f - fabsf(ox)) * sign_nz(oy);
-        ox = tx; oy = ty;
-    }
-    const float zx = (ox + 1.0f) * 0.5f, zy = (oy + 1.0f) * 0.5f;
-    nx = (zx * float(side)) / float(W);
-    ny = (zy * float(side)) / float(H);
-}
-
-__device__ __forceinline__ void probe_texel_origin(int probe, int W, int H, int side, float nx, float ny, float& u,
-                                                   float& v) {
-    const float pwb = float(side) + 2.0f;
-    const int ppr = (W - 2) / int(pwb);
-    const float tlx = float(probe % ppr) * pwb + 2.0f, tly = float(probe / ppr) * pwb + 2.0f;
-    u = tlx / float(W) + nx;
-    v = tly / float(H) + ny;
-}
-
-// The same for a probe given by its atlas cell (cx, cy) = (probe mod X*Y,
-// probe div X*Y): the atlas holds X*Y cells per row, (W - 2) / (side + 2).
-__device__ __forceinline__ void cell_texel_origin(int cx, int cy, int W, int H, int side, float nx, float ny, float& u,
-                                                  float& v) {
-    const float pwb = float(side) + 2.0f;
-    const float tlx = float(cx) * pwb + 2.0f, tly = float(cy) * pwb + 2.0f;
-    u = tlx / float(W) + nx;
-    v = tly / float(H) + ny;
-}
-
-__device__ __forceinline__ void tex_coord_from_dir(f3 dir, int probe, int W, int H, int side, float& u, float& v) {
-    float nx, ny;
-    oct_texel_offset(dir, W, H, side, nx, ny);
-    probe_texel_origin(probe, W, H, side, nx, ny, u, v);
 }
 
 // pow(x, e) of the irradiance decode; x*x*sqrt(x) for the default gamma
@@ -952,9 +1049,11 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
     float sumw = 0.0f;
     const float ge = u.ddgi_gamma * 0.5f;
     const f3 vb = mul3(add3(N, mul3(Wo, 3.0f)), u.normal_bias);
-    float nnx, nny;
-    // textureCoordFromDirection(normalize(N), ...) (DDGICommon.glsl:213)
-    oct_texel_offset(norm3(N), u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny);
+    // textureCoordFromDirection(normalize(N), ...) (DDGICommon.glsl:213): the
+    // point inside every cage probe's irradiance cell
+    float nrx, nry;
+    oct_cell_point(norm3(N), u.irradiance_probe_side, nrx, nry);
+    const int ni = u.irradiance_probe_side, nd = u.depth_probe_side;
     // UNROLL cage probes per iteration overlap their texel fetches; the sums
     // still accumulate in probe order 0..7
 #pragma unroll UNROLL
@@ -972,26 +1071,23 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         // probe index g0 + g1 X + g2 X Y sits in atlas cell (g0 + g1 X, g2)
         const int cell_x = g[0] + g[1] * cnt[0], cell_y = g[2];
         const f3 ptp = add3(sub3(P, ppos), vb);
-        float tu, tv, dist;
+        float rx, ry, dist;
         if (FAST) {
             // textureCoordFromDirection(-normalize(-ptp)) normalises ptp once
             // more; here the unit vector and the distance share one
             // reciprocal square root
             const float d2 = dot3(ptp, ptp);
             const float rl = rsqrtf(d2);
-            float ox, oy;
-            oct_texel_offset_unit(mul3(ptp, rl), u.depth_width, u.depth_height, u.depth_probe_side, ox, oy);
-            cell_texel_origin(cell_x, cell_y, u.depth_width, u.depth_height, u.depth_probe_side, ox, oy, tu, tv);
+            oct_cell_point(mul3(ptp, rl), nd, rx, ry);
             dist = d2 * rl;
         } else {
             const f3 dir = norm3(mul3(ptp, -1.0f));
-            float ox, oy;
-            oct_texel_offset(mul3(dir, -1.0f), u.depth_width, u.depth_height, u.depth_probe_side, ox, oy);
-            cell_texel_origin(cell_x, cell_y, u.depth_width, u.depth_height, u.depth_probe_side, ox, oy, tu, tv);
+            oct_cell_point(norm3(mul3(dir, -1.0f)), nd, rx, ry);
             dist = len3(ptp);
         }
         float mm[2];
-        bilinear_cell_v<2>(A.dist, A.storage, u.depth_width, u.depth_height, tu, tv, mm);
+        bilinear_tap_v<2>(A.dist, A.storage, u.depth_width, nd, cell_x * (nd + 2) + 2, cell_y * (nd + 2) + 2, rx, ry,
+                          mm);
         const float mean = mm[0];
         const float mean2 = mm[1];
         const float variance = fabsf(mean * mean - mean2);
@@ -1000,10 +1096,9 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         cheb = mx(cheb * cheb * cheb, 0.0f);
         weight = weight * ((dist <= mean) ? 1.0f : cheb);
         weight = mx(0.000001f, weight);
-        cell_texel_origin(cell_x, cell_y, u.irradiance_width, u.irradiance_height, u.irradiance_probe_side, nnx, nny, tu,
-                          tv);
         float ir[4];
-        bilinear_cell_v<4>(A.irr, A.storage, u.irradiance_width, u.irradiance_height, tu, tv, ir);
+        bilinear_tap_v<4>(A.irr, A.storage, u.irradiance_width, ni, cell_x * (ni + 2) + 2, cell_y * (ni + 2) + 2, nrx,
+                          nry, ir);
         const f3 pir{pow_decode(ir[0], ge), pow_decode(ir[1], ge), pow_decode(ir[2], ge)};
         const float crush = 0.2f;
         if (weight < crush) weight = weight * (weight * weight * (1.0f / (crush * crush)));

@@ -216,11 +216,11 @@ cudaError_t launch_blend_batch(const BlendParams* vp, const int* starts_irr, int
                                const int* starts_dist, int blocks_dist, size_t smem_dist, int n, int pp,
                                int storage, cudaStream_t st);
 cudaError_t launch_border(const luxgi_ddgi_uniform& u, void* irr, void* dist, int storage, cudaStream_t st);
-cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const float* gb0, const float* gb1,
-                          const uint8_t* pbr, const __half* direct, __half* light, const AtlasView& A, int num_tiles,
-                          float intensity, int bounce, cudaStream_t st);
+cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const void* gb0, const void* gb1,
+                          int gbuffer_format, const uint8_t* pbr, const void* direct, void* light, int light_format,
+                          const AtlasView& A, int num_tiles, float intensity, int bounce, cudaStream_t st);
 cudaError_t launch_surface_light(const SdfView& sdf, const luxgi_surface_desc& s, const luxgi_surface_lighting& L,
-                                 __half* out, cudaStream_t st);
+                                 void* out, cudaStream_t st);
 cudaError_t launch_sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, const float* pos,
                                      const float* nrm, const float* wo, float* out, int n, cudaStream_t st);
 struct Mat4 {
@@ -251,6 +251,8 @@ struct TcBlendParams {
     void* out_dist;
     uint32_t* status;        // device word: nonzero = a bounded wait gave up
     int storage, first, P, R, Ni, Nd;
+    long long wait_cycles;   // bound of each device wait in SM cycles (0 = ~2 s)
+    int withhold;            // test aid: one operand load withheld (see blend_tc.cu)
 };
 cudaError_t launch_tc_blend(const TcBlendParams& p, cudaStream_t st);
 bool tc_blend_supported(const luxgi_ddgi_uniform& u);

@@ -16,6 +16,8 @@ struct luxgi_ddgi_volume {
     int debug_rays = 0;
     bool bound = false;
     bool tc = false;
+    long long tc_wait_cycles = 0;  // bound of the tensor-core blend's waits (0: ~2 s)
+    int tc_withhold = 0;           // test aid, one probe update: withhold one operand load
     int tc_ni = 0, tc_nd = 0;      // padded weight rows (multiples of 16)
     size_t irr_bytes = 0, dist_bytes = 0;
     void* irr[2] = {nullptr, nullptr};

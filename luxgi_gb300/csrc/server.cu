@@ -56,6 +56,9 @@ struct Session {
     uint64_t key = 0;              // launch-compatibility class
     bool resident = false;
     bool busy = false;             // a request of this session is in flight
+    bool transit = false;          // being admitted or evicted while the lock
+                                   // is released: no other thread schedules,
+                                   // evicts or admits it meanwhile
     uint64_t lru = 0;
     int32_t frames = 0;
     uint64_t submitted = 0;        // requests submitted (rotation index of run_poisson)
@@ -69,7 +72,7 @@ struct Session {
     uint32_t* d_chunks = nullptr;
     uint32_t* d_culled = nullptr;
     float* d_depth = nullptr;
-    uint16_t* d_direct = nullptr;
+    void* d_direct = nullptr;
     uint8_t* d_albedo = nullptr;
     void* d_light = nullptr;
     luxgi_sdf_desc sdf_dev{};
@@ -103,15 +106,21 @@ uint64_t cull_capacity(const luxgi_surface_desc& s) {
                                           : 1 + 40ull * 40 * 40 * (uint64_t(s.data.objects_count) + 1);
 }
 
+// bytes a texel of the scene's surface colour textures
+uint64_t color_bytes(const luxgi_session_scene& sc) {
+    return sc.surface.light_format == LUXGI_COLOR_R11G11B10F ? 4 : 8;
+}
+
 uint64_t scene_bytes(const luxgi_session_scene& sc, int light_mode) {
     const uint64_t esz = sc.sdf.format == LUXGI_STORAGE_FP16 ? 2 : 4;
     const uint64_t A2 = uint64_t(sc.atlas_resolution) * sc.atlas_resolution;
+    const uint64_t cb = color_bytes(sc);
     uint64_t b = esz * (sdf_elems(sc.sdf, false) + sdf_elems(sc.sdf, true));
     b += sizeof(luxgi_surface_object) * uint64_t(sc.surface.num_objects);
     b += sizeof(luxgi_surface_tile) * uint64_t(sc.surface.num_tiles);
     b += 4 * (40ull * 40 * 40 + cull_capacity(sc.surface));
-    b += A2 * (4 + 8 + 4);                          // depth, direct light, albedo
-    if (light_mode == LUXGI_LIGHT_CACHE) b += A2 * 8;
+    b += A2 * (4 + cb + 4);                         // depth, direct light, albedo
+    if (light_mode == LUXGI_LIGHT_CACHE) b += A2 * cb;
     return b;
 }
 
@@ -193,9 +202,10 @@ int cuda_admit(luxgi_server* S, Session& ss) {
     if (e == cudaSuccess) e = dalloc(&ss.d_chunks, 4ull * 40 * 40 * 40);
     if (e == cudaSuccess) e = dalloc(&ss.d_culled, 4 * cap);
     if (e == cudaSuccess) e = dalloc(&ss.d_depth, 4 * A2);
-    if (e == cudaSuccess) e = dalloc(&ss.d_direct, 8 * A2);
+    const uint64_t cb = color_bytes(sc);
+    if (e == cudaSuccess) e = dalloc(&ss.d_direct, cb * A2);
     if (e == cudaSuccess) e = dalloc(&ss.d_albedo, 4 * A2);
-    if (e == cudaSuccess && ss.vdesc.light_mode == LUXGI_LIGHT_CACHE) e = dalloc(&ss.d_light, 8 * A2);
+    if (e == cudaSuccess && ss.vdesc.light_mode == LUXGI_LIGHT_CACHE) e = dalloc(&ss.d_light, cb * A2);
     auto up = [&](void* dst, const void* src, uint64_t bytes) {
         if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     };
@@ -203,9 +213,9 @@ int cuda_admit(luxgi_server* S, Session& ss) {
     up(ss.d_objects, sc.surface.objects, sizeof(luxgi_surface_object) * uint64_t(sc.surface.num_objects));
     up(ss.d_tiles, sc.surface.tiles, sizeof(luxgi_surface_tile) * uint64_t(sc.surface.num_tiles));
     up(ss.d_depth, sc.surface.depth, 4 * A2);
-    up(ss.d_direct, sc.surface.direct_light, 8 * A2);
+    up(ss.d_direct, sc.surface.direct_light, cb * A2);
     up(ss.d_albedo, sc.surface.albedo, 4 * A2);
-    if (ss.d_light) up(ss.d_light, sc.surface.light_cache ? sc.surface.light_cache : sc.surface.direct_light, 8 * A2);
+    if (ss.d_light) up(ss.d_light, sc.surface.light_cache ? sc.surface.light_cache : sc.surface.direct_light, cb * A2);
     if (e != cudaSuccess) {
         free_device(ss);
         return cuda_status(e);
@@ -230,6 +240,7 @@ int cuda_admit(luxgi_server* S, Session& ss) {
     ss.surf_dev.light_cache = ss.d_light;
     ss.surf_dev.gbuffer0 = nullptr;
     ss.surf_dev.gbuffer1 = nullptr;
+    ss.surf_dev.gbuffer_format = LUXGI_GBUFFER_RGBA32F;    // G-buffers are not used by sessions
     if (s == LUXGI_OK) s = luxgi_surface_cull(&ss.surf_dev, ss.d_chunks, ss.d_culled, uint32_t(cap), st);
     luxgi_ddgi_volume_desc vd = ss.vdesc;
     vd.march_variant = S->tuning.march_variant;
@@ -310,26 +321,43 @@ int cuda_launch(luxgi_server* S, Slot& sl, const std::vector<Session*>& members)
 // ------------------------------------------------------------------ policy
 // Frees budget for `need` bytes by evicting idle resident sessions, those
 // with nothing pending first, least recently used first.  Caller holds mu.
+// The eviction copy runs with mu released; the victim is marked in transit
+// first, so that meanwhile no group is issued on it and no other caller
+// picks it again.  An eviction that fails leaves the victim resident (its
+// device state intact, its bytes still counted) and returns false.
 bool make_room(luxgi_server* S, uint64_t need, const std::vector<Session*>& keep, std::unique_lock<std::mutex>& lk) {
     while (S->resident_bytes + need > S->desc.memory_budget) {
         Session* victim = nullptr;
         for (auto& up : S->sessions) {
             Session* c = up.get();
-            if (!c->resident || c->busy) continue;
+            if (!c->resident || c->busy || c->transit) continue;
             if (std::find(keep.begin(), keep.end(), c) != keep.end()) continue;
             if (!victim || std::make_pair(!c->queue.empty(), c->lru) < std::make_pair(!victim->queue.empty(), victim->lru))
                 victim = c;
         }
         if (!victim) return false;
         int s = LUXGI_OK;
+        victim->transit = true;
         if (!S->sim) {
             lk.unlock();
             s = cuda_evict(S, *victim);
             lk.lock();
         } else {
+            if (S->desc.sim_evict_s > 0.0f) {
+                // the modelled eviction copy, with the lock released like
+                // the device copy above
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::duration<double>(S->desc.sim_evict_s));
+                lk.lock();
+            }
             victim->saved = true;
         }
-        if (s != LUXGI_OK && S->first_error == LUXGI_OK) S->first_error = s;
+        victim->transit = false;
+        S->cv_done.notify_all();
+        if (s != LUXGI_OK) {
+            if (S->first_error == LUXGI_OK) S->first_error = s;
+            return false;
+        }
         victim->resident = false;
         S->resident_bytes -= victim->bytes;
         S->resident_sessions -= 1;
@@ -385,7 +413,7 @@ void scheduler(luxgi_server* S) {
             if (sl.busy || S->stop) continue;
             std::vector<Session*> cand;
             for (auto& up : S->sessions)
-                if (!up->busy && !up->queue.empty()) cand.push_back(up.get());
+                if (!up->busy && !up->transit && !up->queue.empty()) cand.push_back(up.get());
             if (cand.empty()) break;
             std::sort(cand.begin(), cand.end(),
                       [](const Session* a, const Session* b) { return a->queue.front().ticket < b->queue.front().ticket; });
@@ -395,14 +423,19 @@ void scheduler(luxgi_server* S) {
             const size_t max_group = size_t(S->desc.max_group);
             for (Session* c : cand) {
                 if (members.size() >= max_group) break;
-                if (c->key != key) continue;
+                // (transit re-checked: admissions above release the lock, and
+                // a touch that started earlier may have claimed c meanwhile)
+                if (c->key != key || c->transit) continue;
                 if (!c->resident) {
                     if (!make_room(S, c->bytes, members, lk)) continue;   // wait for memory
                     int s = LUXGI_OK;
                     if (!S->sim) {
+                        c->transit = true;
                         lk.unlock();
                         s = cuda_admit(S, *c);
                         lk.lock();
+                        c->transit = false;
+                        S->cv_done.notify_all();
                     } else {
                         admit_s += S->desc.sim_admit_s;
                     }
@@ -472,6 +505,8 @@ int check_scene(const luxgi_session_scene* sc, int light_mode) {
         sc->sdf.mip_resolution != sc->sdf.resolution / 4 || sc->sdf.resolution != int(sc->sdf.data.resolution))
         return LUXGI_EINVAL;
     if (sc->sdf.format != LUXGI_STORAGE_FP32 && sc->sdf.format != LUXGI_STORAGE_FP16) return LUXGI_EINVAL;
+    if (sc->surface.light_format != LUXGI_COLOR_RGBA16F && sc->surface.light_format != LUXGI_COLOR_R11G11B10F)
+        return LUXGI_EINVAL;
     if (sc->surface.num_objects < 0 || sc->surface.num_tiles < 1 ||
         uint32_t(sc->surface.num_objects) != sc->surface.data.objects_count)
         return LUXGI_EINVAL;
@@ -502,7 +537,7 @@ int luxgi_server_create(const luxgi_server_desc* desc, luxgi_server** out) {
     *out = nullptr;
     if (desc->executor != LUXGI_SERVE_EXEC_CUDA && desc->executor != LUXGI_SERVE_EXEC_SIM) return LUXGI_EINVAL;
     if (desc->max_group < 0 || desc->max_inflight < 0 || desc->max_inflight > 16 || desc->sim_rate < 0.0 ||
-        desc->sim_admit_s < 0.0)
+        desc->sim_admit_s < 0.0 || !(desc->sim_evict_s >= 0.0f) || desc->sim_evict_s > 60.0f)
         return LUXGI_EINVAL;
     luxgi_server* S = new (std::nothrow) luxgi_server();
     if (!S) return LUXGI_ENOMEM;
@@ -723,22 +758,31 @@ int luxgi_server_touch(luxgi_server* S, int32_t id) {
     std::unique_lock<std::mutex> lk(S->mu);
     if (id < 0 || size_t(id) >= S->sessions.size()) return LUXGI_EINVAL;
     Session* ss = S->sessions[size_t(id)].get();
+    // a session another caller is admitting or evicting: wait for the outcome
+    S->cv_done.wait(lk, [&] { return !ss->transit; });
     if (ss->resident) return LUXGI_OK;
     if (ss->busy || !ss->queue.empty()) return LUXGI_EINVAL;
     // admission from the caller's thread: only while the scheduler is idle
     if (S->inflight != 0 || S->pending != 0) return LUXGI_EINVAL;
     if (!S->sim) cudaSetDevice(S->device);
-    if (!make_room(S, ss->bytes, {}, lk)) return LUXGI_ENOMEM;
-    int s = LUXGI_OK;
-    if (!S->sim) s = cuda_admit(S, *ss);
-    if (s != LUXGI_OK) return s;
-    ss->resident = true;
-    ss->lru = ++S->lru_clock;
-    S->resident_bytes += ss->bytes;
-    S->resident_sessions += 1;
-    S->peak_resident_bytes = std::max(S->peak_resident_bytes, S->resident_bytes);
-    S->admissions += 1;
-    return LUXGI_OK;
+    // in transit until admitted: requests submitted while make_room runs
+    // with the lock released wait for it rather than admit it twice
+    ss->transit = true;
+    const bool room = make_room(S, ss->bytes, {}, lk);
+    int s = room ? LUXGI_OK : LUXGI_ENOMEM;
+    if (room && !S->sim) s = cuda_admit(S, *ss);
+    ss->transit = false;
+    if (s == LUXGI_OK) {
+        ss->resident = true;
+        ss->lru = ++S->lru_clock;
+        S->resident_bytes += ss->bytes;
+        S->resident_sessions += 1;
+        S->peak_resident_bytes = std::max(S->peak_resident_bytes, S->resident_bytes);
+        S->admissions += 1;
+    }
+    S->cv_done.notify_all();
+    S->cv_work.notify_all();
+    return s;
 }
 
 int luxgi_server_session_atlases(luxgi_server* S, int32_t id, luxgi_ddgi_atlases* out) {

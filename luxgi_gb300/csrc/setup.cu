@@ -25,7 +25,7 @@ template <> __device__ __forceinline__ void stv<float>(float* p, size_t i, float
 template <> __device__ __forceinline__ void stv<__half>(__half* p, size_t i, float v) { p[i] = __float2half_rn(v); }
 
 // One mip voxel per thread: min over self and the 6 face neighbours of
-// combine(src[scale*v + o], |o| * maxDistance / srcRes) (GlobalSDFMipmap.comp:190-225).
+// combine(src[scale*v + o], |o| * maxDistance / srcRes) (GlobalSDFMipmap.comp:32-67).
 template <typename T>
 __global__ void mip_kernel(const T* __restrict__ src, int src_w, int src_res, int src_off_x, T* __restrict__ dst,
                            int dst_w, int dst_off_x, int mres, int scale, float max_dist) {

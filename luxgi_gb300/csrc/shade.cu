@@ -4,7 +4,10 @@
 // contraction (-prec-div=false -prec-sqrt=false -fmad=true): shading is
 // compared with the CPU restatement by tolerance (1e-4 relative), while the
 // march, whose hit test must reproduce the restatement's branches bit for
-// bit, stays in trace.cu with IEEE arithmetic.
+// bit, stays in trace.cu with IEEE arithmetic.  The hit point and the
+// surface sampler's cut-offs (chunk, bounding sphere, OBB margin) use the
+// exact *_rn forms, so every hit is sorted into the same objects and tiles
+// as in the restatement and only continuous weights carry rounding.
 #include <algorithm>
 #include <cuda_fp16.h>
 
@@ -33,7 +36,7 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
         const f3 dir{d4.x, d4.y, d4.z};
         const f3 origin = probe_location(p.u, uint32_t(probe), p.div_x, p.div_xy);
         const f3 nrm{h.y, h.z, h.w};
-        const f3 hp = add3(origin, mul3(dir, h.x));
+        const f3 hp = ray_point_rn(origin, dir, h.x);
         const float vs = p.sdf.data.cascade_voxel_size[cls];
         const float thr = vs * 1.05f;
         f3 s0, s1;

@@ -94,11 +94,13 @@ struct Fragment {
     float metallic, roughness;
 };
 
-__device__ __forceinline__ Fragment surface_fragment(const float* gb0, const float* gb1, const uint8_t* pbr, int res,
-                                                     float u, float v) {
+// gb_storage: LUXGI_STORAGE_FP32 for RGBA32F G-buffers, LUXGI_STORAGE_FP16
+// for RGBA16F ones (the texels are widened to FP32 before the filter).
+__device__ __forceinline__ Fragment surface_fragment(const void* gb0, const void* gb1, int gb_storage,
+                                                     const uint8_t* pbr, int res, float u, float v) {
     float g0[4], g1[4];
-    bilinear_repeat_v<4>(gb0, LUXGI_STORAGE_FP32, res, res, u, v, g0);
-    bilinear_repeat_v<4>(gb1, LUXGI_STORAGE_FP32, res, res, u, v, g1);
+    bilinear_repeat_v<4>(gb0, gb_storage, res, res, u, v, g0);
+    bilinear_repeat_v<4>(gb1, gb_storage, res, res, u, v, g1);
     Fragment f;
     f.albedo = f3{g0[0], g0[1], g0[2]};
     f.pos = f3{g0[3], g1[2], g1[3]};
@@ -112,17 +114,38 @@ __device__ __forceinline__ Fragment surface_fragment(const float* gb0, const flo
     return f;
 }
 
-__device__ __forceinline__ float round_half(float x) { return __half2float(__float2half_rn(x)); }
+// textureLod bilinear with REPEAT of a surface colour texture, rgba (the
+// per-channel arithmetic of bilinear_repeat; alpha 1 for R11G11B10F).
+__device__ __forceinline__ void bilinear_color_repeat(const void* p, int fmt, int W, int H, float u, float v,
+                                                      float* out) {
+    const float x = u * float(W) - 0.5f, y = v * float(H) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    const int i0 = wrap_repeat(int(fx), W), i1 = wrap_repeat(int(fx) + 1, W);
+    const int j0 = wrap_repeat(int(fy), H), j1 = wrap_repeat(int(fy) + 1, H);
+    float t00[4], t10[4], t01[4], t11[4];
+    color_texel_ro(p, fmt, size_t(j0) * W + i0, t00);
+    color_texel_ro(p, fmt, size_t(j0) * W + i1, t10);
+    color_texel_ro(p, fmt, size_t(j1) * W + i0, t01);
+    color_texel_ro(p, fmt, size_t(j1) * W + i1, t11);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float r0 = t00[c] * (1.0f - a) + t10[c] * a, r1 = t01[c] * (1.0f - a) + t11[c] * a;
+        out[c] = r0 * (1.0f - b) + r1 * b;
+    }
+}
 
 // ------------------------------------------------------------- inject
 // SDFAtlasIndirectLight.frag:44-67 over the footprint of every tile: the
 // light cache becomes direct light plus intensity * (a - a * metallic)/pi *
 // sampleIrradiance(previous atlases), a = min(albedo, 0.9).  One block row
 // per tile.
-__global__ void inject_kernel(const luxgi_ddgi_uniform u, const SurfaceView s, const float* __restrict__ gb0,
-                              const float* __restrict__ gb1, const uint8_t* __restrict__ pbr,
-                              const __half* __restrict__ direct, __half* __restrict__ light, const AtlasView A,
-                              float intensity, int bounce) {
+// `direct` and `light` may be one texture: each texel is read and written by
+// the one thread of its footprint pixel (tiles do not overlap).
+__global__ void inject_kernel(const luxgi_ddgi_uniform u, const SurfaceView s, const void* __restrict__ gb0,
+                              const void* __restrict__ gb1, int gb_storage, const uint8_t* __restrict__ pbr,
+                              const void* direct, void* light, int light_format, const AtlasView A, float intensity,
+                              int bounce) {
     const luxgi_surface_tile* tl = s.tiles + (blockIdx.y + 1);   // tile slot 0 is "no tile"
     const int res = int(s.data.resolution);
     const Footprint fp = footprint(tl, res);
@@ -136,7 +159,7 @@ __global__ void inject_kernel(const luxgi_ddgi_uniform u, const SurfaceView s, c
         if (bounce) {
             float uu, vv;
             fragment_uv(tl, fp, i, j, uu, vv);
-            const Fragment f = surface_fragment(gb0, gb1, pbr, res, uu, vv);
+            const Fragment f = surface_fragment(gb0, gb1, gb_storage, pbr, res, uu, vv);
             const f3 cam{s.data.camera_pos[0], s.data.camera_pos[1], s.data.camera_pos[2]};
             const f3 wo = norm3(sub3(cam, f.pos));
             const f3 e = sample_irradiance(u, A, f.pos, f.normal, wo);
@@ -148,9 +171,11 @@ __global__ void inject_kernel(const luxgi_ddgi_uniform u, const SurfaceView s, c
                 add[c] = intensity * diff * ev[c];
             }
         }
+        float v[4];
+        color_texel(direct, light_format, ti, v);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) light[ti * 4 + c] = __float2half_rn(__half2float(direct[ti * 4 + c]) + add[c]);
-        light[ti * 4 + 3] = direct[ti * 4 + 3];
+        for (int c = 0; c < 3; ++c) v[c] = v[c] + add[c];
+        color_store(light, light_format, ti, v);
     }
 }
 
@@ -255,13 +280,15 @@ struct LightPass {
     const luxgi_surface_tile* tiles;
     int num_surface_tiles;
     int res;
-    const float* gb0;
-    const float* gb1;
+    const void* gb0;
+    const void* gb1;
+    int gb_storage;            // LUXGI_STORAGE_FP32 / FP16 G-buffer texels
+    int light_format;          // luxgi_color_format of emissive and out
     const uint8_t* pbr;
-    const __half* emissive;
+    const void* emissive;
     const uint32_t* list;      // tile addresses
     const uint32_t* masks;     // per listed tile, or nullptr
-    __half* out;
+    void* out;
     float cam[3];
     float shadow_bias;
     int num_lights;
@@ -295,53 +322,50 @@ __global__ void __launch_bounds__(128) surface_light_kernel(const LightPass p, c
         float acc[4];
         if (p.copy_emissive) {
             if (p.emissive) {
-                bilinear_repeat_v<4>(p.emissive, LUXGI_STORAGE_FP16, p.res, p.res, uu, vv, acc);
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[c] = round_half(acc[c]);
+                bilinear_color_repeat(p.emissive, p.light_format, p.res, p.res, uu, vv, acc);
+                color_round(p.light_format, acc);
             } else {
                 acc[0] = acc[1] = acc[2] = 0.0f;
                 acc[3] = 1.0f;
             }
         } else {
-            const uint2 raw = *reinterpret_cast<const uint2*>(p.out + ti * 4);
-            const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
-            const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
-            acc[0] = __low2float(a); acc[1] = __high2float(a); acc[2] = __low2float(b); acc[3] = __high2float(b);
+            color_texel(p.out, p.light_format, ti, acc);
         }
         if (mask) {
-            const Fragment f = surface_fragment(p.gb0, p.gb1, p.pbr, p.res, uu, vv);
+            const Fragment f = surface_fragment(p.gb0, p.gb1, p.gb_storage, p.pbr, p.res, uu, vv);
             for (uint32_t m = mask; m; m &= m - 1u) {
                 const int l = __ffs(int(m)) - 1;
                 const f3 d = direct_light<T>(p.sdf, f, sl[l], cam, p.shadow_bias, p.max_steps);
-                acc[0] = round_half(acc[0] + d.x);
-                acc[1] = round_half(acc[1] + d.y);
-                acc[2] = round_half(acc[2] + d.z);
-                acc[3] = round_half(acc[3] + 1.0f);
+                acc[0] = acc[0] + d.x;
+                acc[1] = acc[1] + d.y;
+                acc[2] = acc[2] + d.z;
+                acc[3] = acc[3] + 1.0f;
+                color_round(p.light_format, acc);
             }
         }
-        const __half2 a = __floats2half2_rn(acc[0], acc[1]);
-        const __half2 b = __floats2half2_rn(acc[2], acc[3]);
-        uint2 raw;
-        raw.x = *reinterpret_cast<const uint32_t*>(&a);
-        raw.y = *reinterpret_cast<const uint32_t*>(&b);
-        *reinterpret_cast<uint2*>(p.out + ti * 4) = raw;
+        color_store(p.out, p.light_format, ti, acc);
     }
 }
 
 }  // namespace
 
-cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const float* gb0, const float* gb1,
-                          const uint8_t* pbr, const __half* direct, __half* light, const AtlasView& A, int num_tiles,
-                          float intensity, int bounce, cudaStream_t st) {
+int gbuffer_storage(int gbuffer_format) {
+    return gbuffer_format == LUXGI_GBUFFER_RGBA16F ? LUXGI_STORAGE_FP16 : LUXGI_STORAGE_FP32;
+}
+
+cudaError_t launch_inject(const luxgi_ddgi_uniform& u, const SurfaceView& s, const void* gb0, const void* gb1,
+                          int gbuffer_format, const uint8_t* pbr, const void* direct, void* light, int light_format,
+                          const AtlasView& A, int num_tiles, float intensity, int bounce, cudaStream_t st) {
     if (num_tiles <= 1) return cudaSuccess;
     dim3 grid(8, unsigned(num_tiles - 1));
-    inject_kernel<<<grid, 256, 0, st>>>(u, s, gb0, gb1, pbr, direct, light, A, intensity, bounce);
+    inject_kernel<<<grid, 256, 0, st>>>(u, s, gb0, gb1, gbuffer_storage(gbuffer_format), pbr, direct, light,
+                                        light_format, A, intensity, bounce);
     note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_surface_light(const SdfView& sdf, const luxgi_surface_desc& s, const luxgi_surface_lighting& L,
-                                 __half* out, cudaStream_t st) {
+                                 void* out, cudaStream_t st) {
     if (L.num_tiles <= 0) return cudaSuccess;
     LightPass p;
     p.sdf = sdf;
@@ -350,8 +374,10 @@ cudaError_t launch_surface_light(const SdfView& sdf, const luxgi_surface_desc& s
     p.res = int(s.data.resolution);
     p.gb0 = s.gbuffer0;
     p.gb1 = s.gbuffer1;
+    p.gb_storage = gbuffer_storage(s.gbuffer_format);
+    p.light_format = s.light_format;
     p.pbr = s.pbr;
-    p.emissive = reinterpret_cast<const __half*>(s.emissive);
+    p.emissive = s.emissive;
     p.list = L.tiles;
     p.masks = L.light_masks;
     p.out = out;

@@ -65,9 +65,11 @@ class VolumeSpec:
         x, y, z = self.probe_counts
         return x * y * z
 
-    def uniform(self) -> N.DDGIUniform:
+    def uniform(self, derive=None) -> N.DDGIUniform:
         """DDGIUniform of a grid centred on the origin, maxDistance = 1.5 x
-        spacing (DDGIRenderer.cpp:665-683)."""
+        spacing (DDGIRenderer.cpp:665-683).  The atlas sizes come from
+        luxgi_ddgi_derive_uniform, or from `derive(u)` when given (a
+        CPU-only caller that must not load the CUDA library)."""
         u = N.DDGIUniform()
         for k in range(3):
             u.start_position[k] = -0.5 * (self.probe_counts[k] - 1) * self.spacing
@@ -81,12 +83,15 @@ class VolumeSpec:
         u.irradiance_probe_side = self.irradiance_side
         u.depth_probe_side = self.depth_side
         u.rays_per_probe = self.rays_per_probe
-        N.check(N.ddgi().luxgi_ddgi_derive_uniform(ctypes.byref(u)), "derive_uniform")
+        if derive is not None:
+            derive(u)
+        else:
+            N.check(N.ddgi().luxgi_ddgi_derive_uniform(ctypes.byref(u)), "derive_uniform")
         return u
 
-    def desc(self) -> N.VolumeDesc:
+    def desc(self, derive=None) -> N.VolumeDesc:
         d = N.VolumeDesc()
-        d.uniform = self.uniform()
+        d.uniform = self.uniform(derive)
         d.storage = self.storage
         d.light_mode = self.light_mode
         d.blend = self.blend
@@ -344,6 +349,36 @@ class DeviceScene:
         self.surface_desc.emissive = self.emissive.data_ptr()
         N.check(lib.luxgi_surface_cull(ctypes.byref(self.surface_desc), self.chunks.data_ptr(),
                                        self.culled.data_ptr(), cap, stream), "surface_cull")
+
+    def set_surface_formats(self, light_format: int, gbuffer_format: int, direct, emissive, gbuffer0,
+                            gbuffer1) -> None:
+        """Re-binds the surface cache in other texture formats: the colour
+        textures (direct light; the light cache, a copy of it; emissive) in
+        `light_format` (luxgi_color_format: uint32 a texel for R11G11B10F,
+        4 x uint16 for RGBA16F) and the G-buffers in `gbuffer_format` (4 x
+        float32 or 4 x uint16 a texel), from host arrays already in those
+        formats -- the engine's own surface textures are R11G11B10F and
+        RGBA16F."""
+        import torch
+
+        def up(a):
+            a = np.ascontiguousarray(a)
+            view = {np.dtype(np.uint32): np.int32, np.dtype(np.uint16): np.int16}.get(a.dtype, a.dtype)
+            return torch.from_numpy(a.view(view)).to(self.device)
+
+        self.direct = up(direct)
+        self.light_cache = self.direct.clone()
+        self.emissive = up(emissive)
+        self.gbuffer0 = up(gbuffer0)
+        self.gbuffer1 = up(gbuffer1)
+        d = self.surface_desc
+        d.direct_light = self.direct.data_ptr()
+        d.light_cache = self.light_cache.data_ptr()
+        d.emissive = self.emissive.data_ptr()
+        d.gbuffer0 = self.gbuffer0.data_ptr()
+        d.gbuffer1 = self.gbuffer1.data_ptr()
+        d.light_format = int(light_format)
+        d.gbuffer_format = int(gbuffer_format)
 
     def nbytes(self) -> int:
         ts = [self.sdf, self.mip, self.mip_tmp, self.objects, self.tiles, self.depth, self.direct, self.light_cache,

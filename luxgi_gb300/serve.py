@@ -44,7 +44,8 @@ def session_scene(host: HostScene) -> N.SessionScene:
 
 class Server:
     def __init__(self, memory_budget: int, executor: str = "cuda", max_group: int = 64, max_inflight: int = 3,
-                 tuning: dict | None = None, sim_rate: float = 1e9, sim_admit_s: float = 0.0):
+                 tuning: dict | None = None, sim_rate: float = 1e9, sim_admit_s: float = 0.0,
+                 sim_evict_s: float = 0.0):
         d = N.ServerDesc()
         d.memory_budget = int(memory_budget)
         d.executor = N.SERVE_EXEC_SIM if executor == "sim" else N.SERVE_EXEC_CUDA
@@ -54,6 +55,7 @@ class Server:
             setattr(d.tuning, k, v)
         d.sim_rate = sim_rate
         d.sim_admit_s = sim_admit_s
+        d.sim_evict_s = sim_evict_s
         h = ctypes.c_void_p()
         N.check(N.ddgi().luxgi_server_create(ctypes.byref(d), ctypes.byref(h)), "server_create")
         self._h = h

@@ -192,7 +192,8 @@ class LightingSchedule:
 class SurfaceLighting:
     """The GPU surface-lighting pass (luxgi_surface_light) on a DeviceScene.
     `run` writes the scene's direct-light atlas unless `out` (a device
-    RGBA16F tensor of the atlas size, int16 or float16) is given."""
+    tensor of the atlas size in the surface's light format: int16 or
+    float16 x 4 for RGBA16F, int32 for R11G11B10F) is given."""
 
     def __init__(self, scene, shadow_bias: float = SHADOW_BIAS, max_steps: int = SHADOW_MAX_STEPS):
         self.scene = scene

@@ -31,7 +31,7 @@ INCLUDE = HERE.parent / "include"
 
 
 def build() -> Path:
-    deps = [SRC] + sorted(INCLUDE.glob("*.h"))
+    deps = [SRC, HERE / "packed_color.h"] + sorted(INCLUDE.glob("*.h"))
     if not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in deps):
         cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", str(SRC), "-o", str(LIB)]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -54,6 +54,10 @@ def lib() -> ctypes.CDLL:
             "oracle_set_threads": (None, [c_int]),
             "oracle_ray_dirs": (c_int, [vp, c_int, c_int, c_int, vp]),
             "oracle_rotation": (c_int, [vp, c_float, vp]),
+            "oracle_frame_rotation": (c_int, [ctypes.c_uint64, c_uint32, vp]),
+            "oracle_derive_uniform": (c_int, [vp]),
+            "oracle_pack_colors": (c_int, [vp, ctypes.c_int64, c_int, vp]),
+            "oracle_unpack_colors": (c_int, [vp, ctypes.c_int64, c_int, vp]),
             "oracle_trace": (c_int, [vp, vp, vp, vp, vp, c_int, vp, c_int, c_int, c_int, vp, vp]),
             "oracle_blend": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int, c_int, c_int, c_int, c_int]),
             "oracle_border": (c_int, [vp, vp, vp]),
@@ -104,6 +108,41 @@ def rotation(axis, angle: float) -> np.ndarray:
     return out
 
 
+def frame_rotation(seed: int, frame: int) -> np.ndarray:
+    """The synthetic workloads' seeded rotation of `frame` (column-major 3x3)."""
+    out = np.zeros(9, dtype=np.float32)
+    lib().oracle_frame_rotation(seed & (2 ** 64 - 1), frame, _p(out))
+    return out
+
+
+def pack_colors(rgba: np.ndarray, fmt: int) -> np.ndarray:
+    """Float rgba texels ([..., 4]) in a surface colour format: uint16 x 4
+    (RGBA16F) or uint32 (R11G11B10F) a texel, rounded like a render target."""
+    from luxgi_gb300 import _native as N
+
+    a = np.ascontiguousarray(rgba, dtype=np.float32).reshape(-1, 4)
+    out = np.zeros(a.shape[0] if fmt == N.COLOR_R11G11B10F else a.shape[0] * 4,
+                   dtype=np.uint32 if fmt == N.COLOR_R11G11B10F else np.uint16)
+    lib().oracle_pack_colors(_p(a), a.shape[0], fmt, _p(out))
+    return out
+
+
+def unpack_colors(texels: np.ndarray, fmt: int) -> np.ndarray:
+    """A surface colour texture's texels as float rgba [n, 4]."""
+    from luxgi_gb300 import _native as N
+
+    t = np.ascontiguousarray(texels)
+    n = t.size if fmt == N.COLOR_R11G11B10F else t.size // 4
+    out = np.zeros((n, 4), dtype=np.float32)
+    lib().oracle_unpack_colors(_p(t), n, fmt, _p(out))
+    return out
+
+
+def derive_uniform(u) -> None:
+    """Fills the atlas width/height fields of a DDGIUniform in place."""
+    lib().oracle_derive_uniform(ctypes.byref(u))
+
+
 def texel_dirs(n: int, precision: int = 0) -> np.ndarray:
     out = np.zeros((n * n, 3), dtype=np.float32)
     lib().oracle_texel_dirs(n, precision, _p(out))
@@ -127,7 +166,11 @@ class HostInputs:
     """Host-side descriptors of a scene for the oracle (numpy-backed)."""
 
     def __init__(self, host, light_mode: int, mip: np.ndarray | None = None, chunks: np.ndarray | None = None,
-                 culled: np.ndarray | None = None, light_cache: np.ndarray | None = None):
+                 culled: np.ndarray | None = None, light_cache: np.ndarray | None = None,
+                 light_format: int = 0, gbuffer_format: int = 0):
+        """light_format / gbuffer_format: the surface textures' formats; the
+        host scene's RGBA16F colours and FP32 G-buffers are converted to
+        them (see colour_textures)."""
         from luxgi_gb300 import _native as N
 
         self.host = host
@@ -159,15 +202,38 @@ class HostInputs:
         self.culled = np.ascontiguousarray(culled, dtype=np.uint32)
         self.surface_desc.chunks = self.chunks.ctypes.data
         self.surface_desc.culled_objects = self.culled.ctypes.data
-        self.light_cache = np.ascontiguousarray(host.direct.copy() if light_cache is None else light_cache)
+        tex = colour_textures(host, light_format, gbuffer_format)
+        self.direct, self.emissive, self.gbuffer0, self.gbuffer1 = tex
+        self.light_cache = np.ascontiguousarray(self.direct.copy() if light_cache is None else light_cache)
         self.surface_desc.light_cache = self.light_cache.ctypes.data
         self.surface_desc.depth = host.depth.ctypes.data
-        self.surface_desc.direct_light = host.direct.ctypes.data
+        self.surface_desc.direct_light = self.direct.ctypes.data
         self.surface_desc.albedo = host.albedo.ctypes.data
-        self.surface_desc.gbuffer0 = host.gbuffer0.ctypes.data
-        self.surface_desc.gbuffer1 = host.gbuffer1.ctypes.data
+        self.surface_desc.gbuffer0 = self.gbuffer0.ctypes.data
+        self.surface_desc.gbuffer1 = self.gbuffer1.ctypes.data
         self.surface_desc.pbr = host.pbr.ctypes.data
-        self.surface_desc.emissive = host.emissive.ctypes.data
+        self.surface_desc.emissive = self.emissive.ctypes.data
+        self.surface_desc.light_format = light_format
+        self.surface_desc.gbuffer_format = gbuffer_format
+
+
+def colour_textures(host, light_format: int = 0, gbuffer_format: int = 0):
+    """(direct light, emissive, gbuffer0, gbuffer1) of a host scene in the
+    given formats: the scene's RGBA16F colours re-encoded as R11G11B10F
+    (rounded to nearest even) or kept, its FP32 G-buffers rounded to
+    RGBA16F or kept."""
+    from luxgi_gb300 import _native as N
+
+    direct, emissive = host.direct, host.emissive
+    if light_format == N.COLOR_R11G11B10F:
+        direct = pack_colors(unpack_colors(direct, N.COLOR_RGBA16F), light_format)
+        emissive = pack_colors(unpack_colors(emissive, N.COLOR_RGBA16F), light_format)
+    g0, g1 = host.gbuffer0, host.gbuffer1
+    if gbuffer_format == N.GBUFFER_RGBA16F:
+        g0 = g0.astype(np.float16).view(np.uint16)
+        g1 = g1.astype(np.float16).view(np.uint16)
+    return (np.ascontiguousarray(direct), np.ascontiguousarray(emissive), np.ascontiguousarray(g0),
+            np.ascontiguousarray(g1))
 
 
 def build_mip(sdf_desc, sdf_float: np.ndarray) -> np.ndarray:
@@ -231,7 +297,7 @@ def border(uniform, irr: np.ndarray | None, dist: np.ndarray | None) -> None:
 def inject(vdesc, inputs: HostInputs, irr, dist, frames: int, precision: int = 0, base=None) -> np.ndarray:
     """SDFAtlasIndirectLight over every tile footprint; texels outside the
     footprints keep `base` (default: the inputs' current light cache)."""
-    out = np.array(inputs.light_cache if base is None else base, dtype=np.uint16, copy=True)
+    out = np.array(inputs.light_cache if base is None else base, copy=True)
     i = np.ascontiguousarray(irr, dtype=np.float32)
     d = np.ascontiguousarray(dist, dtype=np.float32)
     lib().oracle_inject(ctypes.byref(vdesc), ctypes.byref(inputs.surface_desc), _p(i), _p(d), frames, precision,
@@ -249,7 +315,7 @@ def surface_light(inputs: HostInputs, lights, tiles, masks=None, camera=(0.0, 0.
     from luxgi_gb300 import _native as N
 
     res = inputs.surface_desc.data.resolution
-    o = np.array(inputs.host.direct if out is None else out, dtype=np.uint16, copy=True)
+    o = np.array(inputs.direct if out is None else out, copy=True)
     t = np.ascontiguousarray(tiles, dtype=np.uint32)
     m = None if masks is None else np.ascontiguousarray(masks, dtype=np.uint32)
     sh = np.zeros(res * res, dtype=np.uint32) if want_shadow else None
@@ -451,7 +517,7 @@ def ref_surface_light(inputs: HostInputs, lights, tiles, masks=None, camera=(0.0
                       shadow_bias: float = 1.0, copy_emissive: bool = True, out=None) -> np.ndarray:
     """CopyEmissive + SDFDeferredLight through the reference's compiled
     functions (250-step shadow march), RGBA16F bits."""
-    o = np.array(inputs.host.direct if out is None else out, dtype=np.uint16, copy=True)
+    o = np.array(inputs.direct if out is None else out, copy=True)
     from luxgi_gb300 import _native as N
 
     t = np.ascontiguousarray(tiles, dtype=np.uint32)
@@ -466,7 +532,7 @@ def ref_surface_light(inputs: HostInputs, lights, tiles, masks=None, camera=(0.0
 
 def ref_inject(vdesc, inputs: HostInputs, irr, dist, base=None) -> np.ndarray:
     """SDFAtlasIndirectLight through the reference's compiled functions."""
-    o = np.array(inputs.light_cache if base is None else base, dtype=np.uint16, copy=True)
+    o = np.array(inputs.light_cache if base is None else base, copy=True)
     i = np.ascontiguousarray(irr, dtype=np.float32)
     d = np.ascontiguousarray(dist, dtype=np.float32)
     ref_lib().ref_inject(ctypes.byref(vdesc), ctypes.byref(inputs.surface_desc), _p(i), _p(d), _p(o))

@@ -25,7 +25,8 @@ main) use Vulkan resource
 declarations that do not compile as C++, so oracle/ref_harness.cpp restates
 those bodies around the compiled library functions.
 
-Usage: python oracle/build_ref.py [/path/to/reference]
+Usage: python oracle/build_ref.py /path/to/reference
+(or with the checkout in $LUXGI_REFERENCE)
 """
 from __future__ import annotations
 
@@ -46,8 +47,19 @@ SHADERS = ["DDGI/DDGICommon.glsl", "Common/Math.glsl", "Raytraced/Random.glsl", 
            "Common/Light.glsl"]
 
 
-def reference_root(arg: str | None = None) -> Path:
-    return Path(arg) if arg else Path("/root/reference")
+CHECKOUT = OUT / "checkout.txt"        # the checkout the library was built from
+
+
+def reference_root(arg: str | None = None) -> Path | None:
+    """The reference checkout: the argument, else $LUXGI_REFERENCE, else the
+    checkout the last build recorded, else None (then only a previously
+    built library, if any, is used)."""
+    import os
+
+    p = arg or os.environ.get("LUXGI_REFERENCE")
+    if not p and CHECKOUT.exists():
+        p = CHECKOUT.read_text().strip()
+    return Path(p) if p else None
 
 
 def swizzles(n: int) -> str:
@@ -75,11 +87,13 @@ def rewrite(text: str) -> str:
 
 def build(ref: Path | None = None, force: bool = False) -> Path | None:
     ref = reference_root(None if ref is None else str(ref))
-    shaders = ref / "Code/Maple/src/Shaders"
-    if not shaders.is_dir():
+    shaders = None if ref is None else ref / "Code/Maple/src/Shaders"
+    if shaders is None or not shaders.is_dir():
         return LIB if LIB.exists() else None
-    deps = [shaders / s for s in SHADERS] + [HERE / "glsl_compat.h", HERE / "ref_harness.cpp", Path(__file__)]
+    deps = [shaders / s for s in SHADERS] + [HERE / "glsl_compat.h", HERE / "packed_color.h", HERE / "ref_harness.cpp",
+                                             HERE.parent / "include" / "luxgi_ddgi.h", Path(__file__)]
     if LIB.exists() and not force and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
+        CHECKOUT.write_text(str(ref.resolve()) + "\n")
         return LIB
     OUT.mkdir(exist_ok=True)
     tmp = Path(tempfile.mkdtemp(prefix="luxgi_ref_"))
@@ -96,6 +110,7 @@ def build(ref: Path | None = None, force: bool = False) -> Path | None:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("reference build failed:\n" + r.stderr[-6000:])
+        CHECKOUT.write_text(str(ref.resolve()) + "\n")
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     return LIB

@@ -18,6 +18,8 @@
 #include <cstring>
 #include <type_traits>
 
+#include "packed_color.h"
+
 typedef unsigned int uint;
 
 #define in
@@ -319,9 +321,11 @@ struct sampler2D {
     const float* f32 = nullptr;
     const uint16_t* f16 = nullptr;
     const uint8_t* u8 = nullptr;
+    const uint32_t* r11 = nullptr;   // packed R11G11B10F (oracle/packed_color.h)
     int W = 0, H = 0, C = 4;
     bool repeat = false;
     float at(int x, int y, int ch) const {
+        if (r11) return packed_color::channel(r11[size_t(y) * size_t(W) + size_t(x)], ch);
         if (ch >= C) return ch == 3 ? 1.0f : 0.0f;
         size_t i = (size_t(y) * size_t(W) + size_t(x)) * size_t(C) + size_t(ch);
         if (f16) { _Float16 h; std::memcpy(&h, f16 + i, 2); return float(h); }

@@ -18,12 +18,14 @@
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
 // this library.
 #include "../include/luxgi_ddgi.h"
+#include "packed_color.h"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <array>
+#include <limits>
 #include <map>
 #include <vector>
 #ifdef _OPENMP
@@ -111,6 +113,27 @@ template <typename R> inline M4<R> inverse(const M4<R>& A) {
 }
 
 inline float h2f(uint16_t h) { _Float16 v; std::memcpy(&v, &h, 2); return float(v); }
+
+inline uint32_t pack_r11g11b10(const float* v) { return packed_color::pack(v); }
+inline float r11g11b10_channel(uint32_t v, int ch) { return packed_color::channel(v, ch); }
+// One texel of a surface colour texture (luxgi_color_format) into rgba.
+inline void color_load(const void* p, int fmt, size_t texel, float* out) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        const uint32_t v = static_cast<const uint32_t*>(p)[texel];
+        for (int c = 0; c < 4; ++c) out[c] = r11g11b10_channel(v, c);
+    } else {
+        for (int c = 0; c < 4; ++c) out[c] = h2f(static_cast<const uint16_t*>(p)[texel * 4 + size_t(c)]);
+    }
+}
+// The value a render target of format `fmt` keeps of v.
+inline void color_round(int fmt, float* v) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        const uint32_t q = pack_r11g11b10(v);
+        for (int c = 0; c < 4; ++c) v[c] = r11g11b10_channel(q, c);
+    } else {
+        for (int c = 0; c < 4; ++c) v[c] = float(_Float16(v[c]));
+    }
+}
 inline float round_half(float f) { return float(_Float16(f)); }
 
 // ---------------------------------------------------------- sin / cos
@@ -243,12 +266,27 @@ struct Tex2 {
     const float* f32 = nullptr;      // interleaved channels
     const uint16_t* f16 = nullptr;
     const uint8_t* u8 = nullptr;     // UNORM
+    const uint32_t* r11 = nullptr;   // packed R11G11B10F (alpha reads 1)
     int W = 0, H = 0, C = 4;
     float at(int x, int y, int ch) const {
-        size_t i = (size_t(y) * size_t(W) + size_t(x)) * size_t(C) + size_t(ch);
+        const size_t texel = size_t(y) * size_t(W) + size_t(x);
+        if (r11) return r11g11b10_channel(r11[texel], ch);
+        size_t i = texel * size_t(C) + size_t(ch);
         if (f16) return h2f(f16[i]);
         if (u8) return float(u8[i]) / 255.0f;
         return f32[i];
+    }
+    // a colour texture of luxgi_color_format `fmt`
+    void set_color(const void* p, int fmt) {
+        if (fmt == LUXGI_COLOR_R11G11B10F) r11 = static_cast<const uint32_t*>(p);
+        else f16 = static_cast<const uint16_t*>(p);
+        C = 4;
+    }
+    // a G-buffer of luxgi_gbuffer_format `fmt`
+    void set_gbuffer(const void* p, int fmt) {
+        if (fmt == LUXGI_GBUFFER_RGBA16F) f16 = static_cast<const uint16_t*>(p);
+        else f32 = static_cast<const float*>(p);
+        C = 4;
     }
 };
 // textureGather component order: (i0,j1), (i1,j1), (i1,j0), (i0,j0); clamp to edge
@@ -574,7 +612,7 @@ template <typename R> void trace_one(const TraceCtx& c, const float rot[9], int 
                 rad = s0;
                 if (c.bounce) {
                     // intensity * albedo / pi * E (Raytraced/Lighting.glsl:79-84, with the
-                    // volume intensity SDFAtlasIndirectLight.frag:74 applies)
+                    // volume intensity SDFAtlasIndirectLight.frag:47 applies)
                     V3<R> e = sample_irradiance<R>(u, c.prev, hp, hit.normal, mul(dir, R(-1)));
                     V3<R> diff{s1.x / pi_r<R>(), s1.y / pi_r<R>(), s1.z / pi_r<R>()};
                     rad = add(rad, mulv(mul(diff, R(c.vd->intensity)), e));
@@ -594,7 +632,7 @@ template <typename R> void trace_one(const TraceCtx& c, const float rot[9], int 
 }
 
 // ------------------------------------------------ ProbeUpdate.glsl
-// One probe of the irradiance or distance blend (ProbeUpdate.glsl:195-281).
+// One probe of the irradiance or distance blend (ProbeUpdate.glsl:66-152).
 // dirs: float4 [R] (already storage-rounded), rays: float4 [P][R].
 template <typename R> void blend_probe(const luxgi_ddgi_volume_desc* vd, const float* dirs, const float* rays,
                                        const float* prev, float* out, int probe, bool depth, bool first, int p0) {
@@ -689,7 +727,7 @@ void border_atlas(float* atlas, int W, int nc, int n, int cells_x, int cells_y) 
     }
 }
 
-// GlobalSDFMipmap.comp sampleSDF/main (GlobalSDFMipmap.comp:190-225) and
+// GlobalSDFMipmap.comp sampleSDF/main (GlobalSDFMipmap.comp:32-67) and
 // combineDistanceToSDF (SDFCommon.glsl:18-36).
 inline float combine(float sdf, float dist) {
     if (sdf <= 0.0f && dist <= 0.0f) return sdf;
@@ -758,10 +796,10 @@ struct SurfaceTextures {
     bool has_pbr = false, has_emissive = false;
     explicit SurfaceTextures(const luxgi_surface_desc* s) {
         const int res = int(s->data.resolution);
-        g0.f32 = s->gbuffer0; g0.W = res; g0.H = res; g0.C = 4;
-        g1.f32 = s->gbuffer1; g1.W = res; g1.H = res; g1.C = 4;
+        g0.set_gbuffer(s->gbuffer0, s->gbuffer_format); g0.W = res; g0.H = res;
+        g1.set_gbuffer(s->gbuffer1, s->gbuffer_format); g1.W = res; g1.H = res;
         pbr.u8 = s->pbr; pbr.W = res; pbr.H = res; pbr.C = 4;
-        emissive.f16 = s->emissive; emissive.W = res; emissive.H = res; emissive.C = 4;
+        emissive.set_color(s->emissive, s->light_format); emissive.W = res; emissive.H = res;
         has_pbr = s->pbr != nullptr;
         has_emissive = s->emissive != nullptr;
     }
@@ -783,6 +821,16 @@ inline uint16_t f2h_bits(float v) {
     uint16_t b;
     std::memcpy(&b, &h, 2);
     return b;
+}
+
+// Stores rgba rounded to a surface colour format (alpha dropped for
+// R11G11B10F).
+inline void color_store(void* p, int fmt, size_t texel, const float* v) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        static_cast<uint32_t*>(p)[texel] = pack_r11g11b10(v);
+    } else {
+        for (int c = 0; c < 4; ++c) static_cast<uint16_t*>(p)[texel * 4 + size_t(c)] = f2h_bits(v[c]);
+    }
 }
 
 // Raytraced/BRDF.glsl:14-41 and :65-81 (Cook-Torrance: GGX distribution,
@@ -1149,6 +1197,68 @@ int oracle_rotation(const float axis[3], float angle, float out[9]) {
     return 0;
 }
 
+// The synthetic workloads' per-frame rotation, which replaces the
+// reference's std::random_device draw (DDGIRenderer.cpp:267-272): a
+// xoshiro256** stream (Blackman & Vigna) seeded through splitmix64 from
+// seed ^ (0xD1B54A32D192ED03 * (frame + 1)); axis = normalize of three
+// U(-1, 1) draws, angle = U(0, 1) * 2pi, each draw the top 24 bits of a
+// 64-bit output; the matrix of the unit quaternion in FP32.  Restated so
+// that a CPU-only run derives the same rotations as the library.
+int oracle_frame_rotation(uint64_t seed, uint32_t frame, float out[9]) {
+    uint64_t st = seed ^ (0xD1B54A32D192ED03ull * (uint64_t(frame) + 1ull));
+    uint64_t s[4];
+    for (uint64_t& w : s) {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        w = z ^ (z >> 31);
+    }
+    auto rol = [](uint64_t v, int k) { return (v << k) | (v >> (64 - k)); };
+    auto draw = [&](float lo, float hi) {
+        const uint64_t r = rol(s[1] * 5, 7) * 9, t = s[1] << 17;
+        s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3];
+        s[2] ^= t; s[3] = rol(s[3], 45);
+        return lo + (hi - lo) * (float(r >> 40) * (1.0f / 16777216.0f));
+    };
+    float a[3];
+    for (float& c : a) c = draw(-1.0f, 1.0f);
+    const float n = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (n > 0.0f) { a[0] /= n; a[1] /= n; a[2] /= n; } else { a[0] = 0.0f; a[1] = 0.0f; a[2] = 1.0f; }
+    const float half = draw(0.0f, 1.0f) * 3.14159265f * 2.0f * 0.5f, sh = std::sin(half);
+    const float qx = a[0] * sh, qy = a[1] * sh, qz = a[2] * sh, qw = std::cos(half);
+    out[0] = 1.0f - 2.0f * (qy * qy + qz * qz); out[1] = 2.0f * (qx * qy + qw * qz); out[2] = 2.0f * (qx * qz - qw * qy);
+    out[3] = 2.0f * (qx * qy - qw * qz); out[4] = 1.0f - 2.0f * (qx * qx + qz * qz); out[5] = 2.0f * (qy * qz + qw * qx);
+    out[6] = 2.0f * (qx * qz + qw * qy); out[7] = 2.0f * (qy * qz - qw * qx); out[8] = 1.0f - 2.0f * (qx * qx + qy * qy);
+    return 0;
+}
+
+// n texels of float rgba into a surface colour format (luxgi_color_format):
+// RGBA16F (4 x u16) or R11G11B10F (u32), rounded as a render target would.
+int oracle_pack_colors(const float* rgba, int64_t n, int fmt, void* out) {
+    for (int64_t i = 0; i < n; ++i) color_store(out, fmt, size_t(i), rgba + 4 * i);
+    return 0;
+}
+// n texels of a surface colour format back to float rgba (alpha 1 for
+// R11G11B10F).
+int oracle_unpack_colors(const void* in, int64_t n, int fmt, float* rgba) {
+    for (int64_t i = 0; i < n; ++i) color_load(in, fmt, size_t(i), rgba + 4 * i);
+    return 0;
+}
+
+// Atlas sizes of DDGIRenderer.cpp:182-185: a cell of side + 2 texels per
+// probe, probes (x + y X) along the width and z along the height, plus a
+// 1-texel pad around the whole atlas.
+int oracle_derive_uniform(luxgi_ddgi_uniform* u) {
+    const int XY = u->probe_counts[0] * u->probe_counts[1], Z = u->probe_counts[2];
+    u->irradiance_width = (u->irradiance_probe_side + 2) * XY + 2;
+    u->irradiance_height = (u->irradiance_probe_side + 2) * Z + 2;
+    u->depth_width = (u->depth_probe_side + 2) * XY + 2;
+    u->depth_height = (u->depth_probe_side + 2) * Z + 2;
+    u->probe_counts[3] = 0;
+    return 0;
+}
+
 // Trace probes [p0, p1): out float4 [P][R] (rgb, distance), info int4 [P][R]
 // (steps, cascade, full-resolution samples, 0) or NULL.  sdf/surface descriptors hold HOST pointers;
 // prev_irr / prev_dist are float atlases (mode B when frames > 0).
@@ -1172,12 +1282,12 @@ int oracle_trace(const luxgi_ddgi_volume_desc* vd, const luxgi_sdf_desc* sdf, co
     c.S.d = surf;
     c.S.depth.f32 = surf->depth; c.S.depth.W = ares; c.S.depth.H = ares; c.S.depth.C = 1;
     if (vd->light_mode == LUXGI_LIGHT_PER_HIT) {
-        c.S.c0.f16 = surf->direct_light;
+        c.S.c0.set_color(surf->direct_light, surf->light_format);
         c.S.c1.u8 = surf->albedo;
         c.S.c1.W = ares; c.S.c1.H = ares; c.S.c1.C = 4;
         c.S.two = true;
     } else {
-        c.S.c0.f16 = static_cast<const uint16_t*>(surf->light_cache);
+        c.S.c0.set_color(surf->light_cache, surf->light_format);
     }
     c.S.c0.W = ares; c.S.c0.H = ares; c.S.c0.C = 4;
     c.prev.irr.f32 = prev_irr; c.prev.irr.W = u.irradiance_width; c.prev.irr.H = u.irradiance_height; c.prev.irr.C = 4;
@@ -1298,10 +1408,12 @@ int oracle_cull(const luxgi_surface_desc* s, uint32_t* chunks, uint32_t* culled,
 }
 
 // SDFAtlasIndirectLight.frag:44-67 over the footprint of every tile;
-// light_out RGBA16F [res^2] holds the light cache on entry (texels outside
-// every footprint keep it).
+// light_out [res^2] of the surface's light format holds the light cache on
+// entry (texels outside every footprint keep it); each footprint texel
+// becomes direct_light + the bounce, rounded to that format (the additive
+// draw into SurfaceLightCache).
 int oracle_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* s, const float* irr, const float* dist,
-                  int frames, int precision, uint16_t* light_out) {
+                  int frames, int precision, void* light_out) {
     const int res = int(s->data.resolution);
     const bool bounce = vd->infinite_bounce && frames != 0;
     Atlases A;
@@ -1335,24 +1447,27 @@ int oracle_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* s,
                     if (precision == 1) shade(0.0);
                     else shade(0.0f);
                 }
-                for (int k = 0; k < 3; ++k)
-                    light_out[ti * 4 + size_t(k)] = f2h_bits(h2f(s->direct_light[ti * 4 + size_t(k)]) + add[k]);
-                light_out[ti * 4 + 3] = s->direct_light[ti * 4 + 3];
+                float v[4];
+                color_load(s->direct_light, s->light_format, ti, v);
+                for (int k = 0; k < 3; ++k) v[k] = v[k] + add[k];
+                color_store(light_out, s->light_format, ti, v);
             }
     }
     return 0;
 }
 
 // One surface-lighting pass (the CopyEmissive draw, then one
-// SDFDeferredLight draw per light with additive blending into a 16-bit
-// target, GlobalSurfaceAtlas.cpp:886-996) over tiles[0 .. n): out RGBA16F
-// [res^2] in/out.  masks[k] bit l: light l draws tile k (NULL: all).
+// SDFDeferredLight draw per light with additive blending into the light
+// cache, GlobalSurfaceAtlas.cpp:886-996) over tiles[0 .. n): out [res^2] of
+// the surface's light format in/out, every draw's result rounded to that
+// format.  masks[k] bit l: light l draws tile k (NULL: all).
 // shadow_out (optional, u32 per texel) collects bit l for each light whose
 // SDF shadow test blocked the fragment.
 int oracle_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s, const luxgi_light* lights,
                          int num_lights, const uint32_t* tiles, const uint32_t* masks, int num_tiles,
                          const float cam[3], float shadow_bias, int copy_emissive, int max_steps, int precision,
-                         uint16_t* out, uint32_t* shadow_out) {
+                         void* out, uint32_t* shadow_out) {
+    const int fmt = s->light_format;
     const int res = int(s->data.resolution), mres = sdf->mip_resolution, C = int(sdf->data.cascades_count);
     Vol tex, mip;
     tex.W = sdf->resolution * C; tex.H = sdf->resolution; tex.D = sdf->resolution;
@@ -1380,9 +1495,9 @@ int oracle_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s,
                     const V2<float> uv = fragment_uv<float>(tl, fp, i, j);
                     for (int c = 0; c < 4; ++c)
                         acc[c] = T.has_emissive ? bilinear_repeat(T.emissive, uv, c) : (c == 3 ? 1.0f : 0.0f);
-                    for (int c = 0; c < 4; ++c) acc[c] = round_half(acc[c]);
+                    if (T.has_emissive) color_round(fmt, acc);
                 } else {
-                    for (int c = 0; c < 4; ++c) acc[c] = h2f(out[ti * 4 + size_t(c)]);
+                    color_load(out, fmt, ti, acc);
                 }
                 uint32_t blocked = 0;
                 for (int l = 0; l < num_lights; ++l) {
@@ -1401,10 +1516,11 @@ int oracle_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* s,
                         d[0] = v.x; d[1] = v.y; d[2] = v.z;
                     }
                     if (sh) blocked |= 1u << l;
-                    for (int c = 0; c < 3; ++c) acc[c] = round_half(acc[c] + d[c]);
-                    acc[3] = round_half(acc[3] + 1.0f);
+                    for (int c = 0; c < 3; ++c) acc[c] = acc[c] + d[c];
+                    acc[3] = acc[3] + 1.0f;
+                    color_round(fmt, acc);
                 }
-                for (int c = 0; c < 4; ++c) out[ti * 4 + size_t(c)] = f2h_bits(acc[c]);
+                color_store(out, fmt, ti, acc);
                 if (shadow_out) shadow_out[ti] = blocked;
             }
     }

@@ -8,9 +8,9 @@
 // normalizedOctCoord, getProbeId, combineDistanceToSDF, boxIntersectsSphere,
 // flattenId -- glued together the way the shader entry points do:
 //   ref_trace  GISDFRays.comp:63-128
-//   ref_blend  ProbeUpdate.glsl:182-281
-//   ref_mip    GlobalSDFMipmap.comp:190-226 and GlobalDistanceField.cpp:537-573
-//   ref_cull   SDFCulling.comp:262-327 (deterministic list placement)
+//   ref_blend  ProbeUpdate.glsl:66-152
+//   ref_mip    GlobalSDFMipmap.comp:32-67 and GlobalDistanceField.cpp:537-573
+//   ref_cull   SDFCulling.comp:36-101 (deterministic list placement)
 //   ref_surface_light  CopyEmissive.frag:22-26, SDFDeferredLight.frag:41-129
 //                      (BRDF from Raytraced/BRDF.glsl:65-81)
 //   ref_inject SDFAtlasIndirectLight.frag:44-67
@@ -64,6 +64,52 @@ sampler2D tex2d(const float* f32, const uint16_t* f16, const uint8_t* u8, int W,
     s.W = W; s.H = H; s.C = C;
     s.repeat = repeat;
     return s;
+}
+
+// A surface colour texture of luxgi_color_format `fmt` (RGBA16F, or packed
+// R11G11B10F sampled as rgb + alpha 1).
+sampler2D color_tex(const void* p, int fmt, int W, int H, bool repeat) {
+    sampler2D s = tex2d(nullptr, fmt == LUXGI_COLOR_R11G11B10F ? nullptr : static_cast<const uint16_t*>(p), nullptr,
+                        W, H, 4, repeat);
+    if (fmt == LUXGI_COLOR_R11G11B10F) s.r11 = static_cast<const uint32_t*>(p);
+    return s;
+}
+// A surface G-buffer of luxgi_gbuffer_format `fmt`.
+sampler2D gbuffer_tex(const void* p, int fmt, int W, int H) {
+    if (fmt == LUXGI_GBUFFER_RGBA16F) return tex2d(nullptr, static_cast<const uint16_t*>(p), nullptr, W, H, 4, true);
+    return tex2d(static_cast<const float*>(p), nullptr, nullptr, W, H, 4, true);
+}
+// The render target's rounding of a colour (what an RGBA16F or R11G11B10F
+// attachment stores), and its texel load and store.
+void target_round(int fmt, float* v) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        const uint32_t q = packed_color::pack(v);
+        for (int c = 0; c < 4; ++c) v[c] = packed_color::channel(q, c);
+    } else {
+        for (int c = 0; c < 4; ++c) v[c] = float(_Float16(v[c]));
+    }
+}
+void target_load(const void* p, int fmt, size_t ti, float* v) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        const uint32_t q = static_cast<const uint32_t*>(p)[ti];
+        for (int c = 0; c < 4; ++c) v[c] = packed_color::channel(q, c);
+    } else {
+        for (int c = 0; c < 4; ++c) {
+            _Float16 h;
+            std::memcpy(&h, static_cast<const uint16_t*>(p) + ti * 4 + size_t(c), 2);
+            v[c] = float(h);
+        }
+    }
+}
+void target_store(void* p, int fmt, size_t ti, const float* v) {
+    if (fmt == LUXGI_COLOR_R11G11B10F) {
+        static_cast<uint32_t*>(p)[ti] = packed_color::pack(v);
+    } else {
+        for (int c = 0; c < 4; ++c) {
+            const _Float16 h = _Float16(v[c]);
+            std::memcpy(static_cast<uint16_t*>(p) + ti * 4 + size_t(c), &h, 2);
+        }
+    }
 }
 
 // The pixels a tile quad of addTiles2 covers (Engine/DDGI/
@@ -141,8 +187,8 @@ int ref_trace(const luxgi_ddgi_volume_desc* vd, const luxgi_sdf_desc* sdf, const
     const int A = int(surf->data.resolution);
     const sampler2D depthS = tex2d(surf->depth, nullptr, nullptr, A, A, 1, false);
     const bool per_hit = vd->light_mode == LUXGI_LIGHT_PER_HIT;
-    const sampler2D colorS = per_hit ? tex2d(nullptr, surf->direct_light, nullptr, A, A, 4, false)
-                                     : tex2d(nullptr, static_cast<const uint16_t*>(surf->light_cache), nullptr, A, A, 4, false);
+    const sampler2D colorS = color_tex(per_hit ? surf->direct_light : surf->light_cache, surf->light_format, A, A,
+                                       false);
     const sampler2D albedoS = tex2d(nullptr, nullptr, surf->albedo, A, A, 4, false);
     const sampler2D irrS = tex2d(prev_irr, nullptr, nullptr, ddgi.irradianceTextureWidth, ddgi.irradianceTextureHeight, 4, true);
     const sampler2D distS = tex2d(prev_dist, nullptr, nullptr, ddgi.depthTextureWidth, ddgi.depthTextureHeight, 2, true);
@@ -363,20 +409,21 @@ int ref_sample_irradiance(const luxgi_ddgi_uniform* u, const float* irr, const f
 
 // CopyEmissive.frag main, then SDFDeferredLight.frag main (:79-129) for each
 // light whose bit is set in masks[k] (NULL: all), blended additively into
-// the RGBA16F target `out` (rounded after each draw), over tiles[0 .. n).
-// copy_emissive = 0 skips the CopyEmissive draw.
+// the target `out` of the surface's light format (rounded after each draw),
+// over tiles[0 .. n).  copy_emissive = 0 skips the CopyEmissive draw.
 int ref_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf, const luxgi_light* lights,
                       int num_lights, const uint32_t* tile_ids, const uint32_t* masks, int n, const float cam[3],
-                      float shadow_bias, int copy_emissive, uint16_t* out) {
+                      float shadow_bias, int copy_emissive, void* out) {
+    const int fmt = surf->light_format;
     const GlobalSDFData sd = as<GlobalSDFData>(sdf->data);
     const int C = int(sdf->data.cascades_count), res = sdf->resolution, mres = sdf->mip_resolution;
     const sampler3D tex = volume(sdf->sdf, sdf->format, res * C, res, res);
     const sampler3D mip = volume(sdf->mip, sdf->format, mres * C, mres, mres);
     const int A = int(surf->data.resolution);
-    const sampler2D colorS = tex2d(surf->gbuffer0, nullptr, nullptr, A, A, 4, true);
-    const sampler2D normalS = tex2d(surf->gbuffer1, nullptr, nullptr, A, A, 4, true);
+    const sampler2D colorS = gbuffer_tex(surf->gbuffer0, surf->gbuffer_format, A, A);
+    const sampler2D normalS = gbuffer_tex(surf->gbuffer1, surf->gbuffer_format, A, A);
     const sampler2D pbrS = tex2d(nullptr, nullptr, surf->pbr, A, A, 4, true);
-    const sampler2D emissiveS = tex2d(nullptr, surf->emissive, nullptr, A, A, 4, true);
+    const sampler2D emissiveS = color_tex(surf->emissive, fmt, A, A, true);
     const TileBuffer* tiles = reinterpret_cast<const TileBuffer*>(surf->tiles);
     for (int k = 0; k < n; ++k) {
         const TileBuffer tile = tiles[tile_ids[k]];
@@ -391,9 +438,10 @@ int ref_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf,
                 float dst[4];
                 if (copy_emissive) {
                     const vec4 e = surf->emissive ? texture(emissiveS, atlasUV) : vec4(0, 0, 0, 1);
-                    dst[0] = h16(to16(e.x)); dst[1] = h16(to16(e.y)); dst[2] = h16(to16(e.z)); dst[3] = h16(to16(e.w));
+                    dst[0] = e.x; dst[1] = e.y; dst[2] = e.z; dst[3] = e.w;
+                    target_round(fmt, dst);
                 } else {
-                    for (int c = 0; c < 4; ++c) dst[c] = h16(out[ti * 4 + size_t(c)]);
+                    target_load(out, fmt, ti, dst);
                 }
                 for (int l = 0; l < num_lights; ++l) {
                     if (!(mask >> l & 1u)) continue;
@@ -435,12 +483,13 @@ int ref_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf,
                     float cosLi = max(0.0, dot(normal, L));
                     vec3 directShading = BRDF(vec3(albedo.rgb), normal, roughness, metallic, view, Lh, L) * Lradiance *
                                          cosLi * shadowMask * atten;
-                    dst[0] = h16(to16(dst[0] + directShading.x));
-                    dst[1] = h16(to16(dst[1] + directShading.y));
-                    dst[2] = h16(to16(dst[2] + directShading.z));
-                    dst[3] = h16(to16(dst[3] + 1.0f));
+                    dst[0] = dst[0] + directShading.x;
+                    dst[1] = dst[1] + directShading.y;
+                    dst[2] = dst[2] + directShading.z;
+                    dst[3] = dst[3] + 1.0f;
+                    target_round(fmt, dst);
                 }
-                for (int c = 0; c < 4; ++c) out[ti * 4 + size_t(c)] = to16(dst[c]);
+                target_store(out, fmt, ti, dst);
             }
     }
     return 0;
@@ -448,13 +497,15 @@ int ref_surface_light(const luxgi_sdf_desc* sdf, const luxgi_surface_desc* surf,
 
 // SDFAtlasIndirectLight.frag main (:51-67, indirectLighting :44-48) over
 // every tile's quad: out = direct_light + the fragment's indirect light,
-// rounded to FP16 (texels outside the quads are left as they are).
+// rounded to the surface's light format, the additive draw into the light
+// cache (texels outside the quads are left as they are).
 int ref_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* surf, const float* irr, const float* dist,
-               uint16_t* out) {
+               void* out) {
     const DDGIUniform ddgi = as<DDGIUniform>(vd->uniform);
     const int A = int(surf->data.resolution);
-    const sampler2D colorS = tex2d(surf->gbuffer0, nullptr, nullptr, A, A, 4, true);
-    const sampler2D normalS = tex2d(surf->gbuffer1, nullptr, nullptr, A, A, 4, true);
+    const int fmt = surf->light_format;
+    const sampler2D colorS = gbuffer_tex(surf->gbuffer0, surf->gbuffer_format, A, A);
+    const sampler2D normalS = gbuffer_tex(surf->gbuffer1, surf->gbuffer_format, A, A);
     const sampler2D pbrS = tex2d(nullptr, nullptr, surf->pbr, A, A, 4, true);
     const sampler2D irrS = tex2d(irr, nullptr, nullptr, ddgi.irradianceTextureWidth, ddgi.irradianceTextureHeight, 4, true);
     const sampler2D distS = tex2d(dist, nullptr, nullptr, ddgi.depthTextureWidth, ddgi.depthTextureHeight, 2, true);
@@ -480,10 +531,12 @@ int ref_inject(const luxgi_ddgi_volume_desc* vd, const luxgi_surface_desc* surf,
                 const vec3 Wo = normalize(cam - worldPos);
                 vec3 diffuseColor = (vec3(p.albedo.rgb) - vec3(p.albedo.rgb) * p.metallic) / PI;
                 vec3 e = vd->intensity * diffuseColor * sampleIrradiance(ddgi, worldPos, p.normal, Wo, irrS, distS);
-                out[ti * 4 + 0] = to16(h16(surf->direct_light[ti * 4 + 0]) + e.x);
-                out[ti * 4 + 1] = to16(h16(surf->direct_light[ti * 4 + 1]) + e.y);
-                out[ti * 4 + 2] = to16(h16(surf->direct_light[ti * 4 + 2]) + e.z);
-                out[ti * 4 + 3] = surf->direct_light[ti * 4 + 3];
+                float v[4];
+                target_load(surf->direct_light, fmt, ti, v);
+                v[0] = v[0] + e.x;
+                v[1] = v[1] + e.y;
+                v[2] = v[2] + e.z;
+                target_store(out, fmt, ti, v);
             }
     }
     return 0;

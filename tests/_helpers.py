@@ -47,6 +47,34 @@ def rel_err(a: np.ndarray, b: np.ndarray, floor: float = 1e-3) -> float:
     return float(np.max(np.abs(a - b) / den)) if a.size else 0.0
 
 
+def probe_ranges(probes: int, count: int, length: int, seed: int) -> list[tuple[int, int]]:
+    """`count` disjoint seeded ranges [p0, p0 + length) of probe indices,
+    sorted (each range spans whole rows of the probe grid when `length` is a
+    multiple of the grid's x count)."""
+    slots = probes // length
+    rng = np.random.default_rng(seed)
+    picks = sorted(rng.choice(slots, size=min(count, slots), replace=False))
+    return [(int(s) * length, int(s) * length + length) for s in picks]
+
+
+def cell_errors(got: np.ndarray, ref: np.ndarray, uniform, probes, depth: bool, floor: float = 1e-3) -> np.ndarray:
+    """Relative errors (|got - ref| / max(|ref|, floor)) over the atlas cells
+    (interior and border texels, every channel) of the given probes; cell
+    of probe p at (p mod XY, p div XY), (n + 2)^2 texels from texel 1
+    (DDGICommon.glsl:94-99)."""
+    n = uniform.depth_probe_side if depth else uniform.irradiance_probe_side
+    XY = uniform.probe_counts[0] * uniform.probe_counts[1]
+    out = []
+    for p in probes:
+        cx, cy = p % XY, p // XY
+        ys = slice(1 + cy * (n + 2), 1 + (cy + 1) * (n + 2))
+        xs = slice(1 + cx * (n + 2), 1 + (cx + 1) * (n + 2))
+        a = got[ys, xs].astype(np.float64)
+        b = ref[ys, xs].astype(np.float64)
+        out.append((np.abs(a - b) / np.maximum(np.abs(b), floor)).ravel())
+    return np.concatenate(out) if out else np.zeros(0)
+
+
 def interior_mask(uniform, depth: bool) -> np.ndarray:
     """Texels that belong to a probe cell (interior + border) of the atlas."""
     n = uniform.depth_probe_side if depth else uniform.irradiance_probe_side

@@ -11,8 +11,9 @@ reference_params.json
     text: DDGIUniform / IrradianceVolume defaults (Engine/DDGI/DDGIRenderer.h),
     the octahedral sides, and the march step cap (Shaders/SDF/SDFCommon.glsl).
 
-Run from the repository root with the reference checked out at
-/root/reference:  python tests/golden/make_golden.py
+Run from the repository root with the path of a reference checkout:
+    python tests/golden/make_golden.py /path/to/reference
+(or with the checkout in $LUXGI_REFERENCE).
 """
 from __future__ import annotations
 
@@ -21,7 +22,12 @@ import re
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+import os
+
+_ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LUXGI_REFERENCE")
+if not _ref:
+    sys.exit("usage: make_golden.py /path/to/reference (or set LUXGI_REFERENCE)")
+REF = Path(_ref)
 OUT = Path(__file__).resolve().parent
 SH = REF / "Code/Maple/src/Shaders"
 ENG = REF / "Code/Maple/src/Engine"

@@ -168,3 +168,93 @@ def test_lighting_inject_and_update_chain(cuda):
     assert rel_err(gdist, od) < 2e-3
     lc = dev.light_cache.cpu().numpy().view(np.uint16)
     assert rel_err(_f16(lc), _f16(inp.light_cache), floor=1e-2) < 2e-3
+
+
+# ---------------------------------------------------------------- engine formats
+# The engine's surface textures: R11G11B10F emissive / lit atlas / light
+# cache and RGBA16F G-buffers (GlobalSurfaceAtlas.cpp:407-411).  Every draw
+# rounds the 11/11/10-bit target on both sides; the kernels and the oracle
+# make every discrete decision alike, so most codes are identical and the
+# rest lie within one code step (2^-6 relative for R and G, 2^-5 for B) per
+# draw.
+
+
+def _engine_setup(w, camera=None):
+    host, dev, _ = _setup(w, camera)
+    mip = dev.mip.cpu().numpy()
+    if host.sdf_format == N.STORAGE_FP16:
+        mip = mip.view(np.uint16)
+    inp = oracle.HostInputs(host, w.volume.light_mode, mip=mip, chunks=dev.chunks.cpu().numpy().view(np.uint32),
+                            culled=dev.culled.cpu().numpy().view(np.uint32), light_format=N.COLOR_R11G11B10F,
+                            gbuffer_format=N.GBUFFER_RGBA16F)
+    if camera is not None:
+        inp.surface_desc.data.camera_pos[:] = camera
+    dev.set_surface_formats(N.COLOR_R11G11B10F, N.GBUFFER_RGBA16F, inp.direct, inp.emissive, inp.gbuffer0,
+                            inp.gbuffer1)
+    return host, dev, inp
+
+
+def _r11_close(g, o, draws):
+    x = oracle.unpack_colors(g, N.COLOR_R11G11B10F)[:, :3]
+    y = oracle.unpack_colors(o, N.COLOR_R11G11B10F)[:, :3]
+    assert np.array_equal(np.isfinite(x), np.isfinite(y))
+    keep = np.isfinite(y).all(axis=1)
+    assert np.mean(g != o) < 2e-3
+    assert rel_err(x[keep], y[keep]) <= draws * 2.0 ** -5
+
+
+@pytest.mark.parametrize("fmt,copy_emissive", [(N.STORAGE_FP32, True), (N.STORAGE_FP16, False)])
+def test_surface_light_engine_formats_match_oracle(cuda, fmt, copy_emissive):
+    import torch
+
+    w = tiny_workload(sdf=32, prims=8, atlas=256, sdf_format=fmt)
+    host, dev, inp = _engine_setup(w)
+    lights = _lights()
+    tiles = np.arange(1, host.num_tiles, dtype=np.uint32)
+    masks = np.random.default_rng(9).integers(0, 8, size=tiles.size).astype(np.uint32)
+    cam = (0.3, 0.5, -2.0)
+    out = torch.from_numpy(inp.direct.view(np.int32).copy()).to(dev.device)
+    SurfaceLighting(dev).run(lights, tiles, masks, cam, copy_emissive, out=out)
+    torch.cuda.synchronize()
+    g = out.cpu().numpy().view(np.uint32)
+    o = oracle.surface_light(inp, lights, tiles, masks, cam, copy_emissive=copy_emissive)
+    assert np.count_nonzero(g != inp.direct) > 10000
+    _r11_close(g, o, 1 + len(lights))
+
+
+@pytest.mark.parametrize("light", [N.LIGHT_CACHE, N.LIGHT_PER_HIT])
+def test_engine_formats_chain(cuda, light):
+    """Lighting into the R11G11B10F direct-light atlas, (light-cache mode)
+    injection into the R11G11B10F light cache from RGBA16F G-buffers, and
+    the frames whose hit shading samples it: atlases within 2e-3 of the
+    oracle's, which continues from the GPU's lit atlas."""
+    import torch
+
+    w = tiny_workload(light=light, prims=8, frames=4, seed=12)
+    cam = (0.4, 0.7, -1.3)
+    host, dev, inp = _engine_setup(w, cam)
+    dev.surface_desc.data.camera_pos[:] = cam
+    vol = DDGIVolume(w.volume)
+    vol.bind_scene(dev)
+    lights = scene_lights(host, 3, seed=5)
+    tiles, masks = select_tiles(host, range(host.num_objects), lights)
+    SurfaceLighting(dev).run(lights, tiles, masks, cam)
+    o = oracle.surface_light(inp, lights, tiles, masks, cam)
+    torch.cuda.synchronize()
+    gd = dev.direct.cpu().numpy().view(np.uint32)
+    _r11_close(gd, o, 1 + len(lights))
+    inp.direct[:] = gd
+    inp.light_cache[:] = gd
+    dev.light_cache.copy_(dev.direct)
+    rots = [frame_rotation(72, f) for f in range(4)]
+    for f, r in enumerate(rots):
+        if light == N.LIGHT_CACHE and f > 0 and f % 2 == 0:
+            vol.inject_indirect()
+        vol.update(r)
+    irr, dist = vol.atlases()
+    torch.cuda.synchronize()
+    oi, od, _, _ = oracle.run_frames(vol.desc, inp, rots, precision=0, inject_every=2)
+    assert rel_err(irr.detach().cpu().float().numpy(), oi) < 2e-3
+    assert rel_err(dist.detach().cpu().float().numpy(), od) < 2e-3
+    if light == N.LIGHT_CACHE:
+        _r11_close(dev.light_cache.cpu().numpy().view(np.uint32), inp.light_cache, 1)

@@ -91,6 +91,26 @@ def test_rotation_matches_quaternion_identity():
         np.testing.assert_allclose(m @ ax, ax, atol=2e-6)      # axis is fixed
 
 
+def test_frame_rotation_and_atlas_sizes_match_the_library():
+    """The oracle's restatements of the seeded frame rotation and of the
+    atlas-size derivation equal the library's host functions (both are
+    built without FMA contraction), so a CPU-only run reproduces the
+    workload without loading the CUDA library."""
+    import ctypes
+
+    from luxgi_gb300 import _native as N
+    from luxgi_gb300.scene import PRECISION, PRODUCTION
+
+    for seed in (0, 21, 0x5EED, 2 ** 63 + 5):
+        for f in (0, 1, 7, 1000):
+            np.testing.assert_array_equal(oracle.frame_rotation(seed, f), frame_rotation(seed, f))
+    for w in (PRODUCTION, PRECISION):
+        a = w.volume.uniform()
+        b = w.volume.uniform(derive=oracle.derive_uniform)
+        assert bytes(a) == bytes(b)
+        assert ctypes.sizeof(N.DDGIUniform) == 96
+
+
 def test_oct_roundtrip_texel_centres():
     for n in (6, 8, 14, 16):
         d = oracle.texel_dirs(n, precision=1)
@@ -240,3 +260,38 @@ def test_cull_capacity_overflow_reports():
     assert cu[0] == need
     nz = ch[ch != 0]
     assert np.all(nz + cu[nz] + 1 <= need // 2)
+
+
+def test_r11g11b10f_codes_round_trip_and_round_to_nearest_even():
+    """The oracle's R11G11B10F codec against the format's definition: every
+    finite code of the 11-bit (R, G) and 10-bit (B) unsigned floats decodes
+    to m 2^-(14+M) (exponent 0) or (1 + m/2^M) 2^(e-15) and encodes back to
+    itself; halfway values round to the even mantissa; negative values
+    become 0; values past the largest finite (65024 / 64512) become Inf."""
+    from luxgi_gb300 import _native as N
+
+    R = N.COLOR_R11G11B10F
+    for M, shift, top in ((6, 0, 0x7FF), (5, 22, 0x3FF)):
+        codes = np.arange(31 << M, dtype=np.uint32)          # every finite code
+        texels = codes << shift
+        vals = oracle.unpack_colors(texels, R)[:, 0 if shift == 0 else 2]
+        e, m = codes >> M, codes & ((1 << M) - 1)
+        want = np.where(e == 0, m * 2.0 ** -(14 + M), (1 + m / 2.0 ** M) * 2.0 ** (e.astype(np.int64) - 15))
+        assert np.array_equal(vals.astype(np.float64), want)
+        rgba = np.zeros((codes.size, 4), np.float32)
+        rgba[:, 0 if shift == 0 else 2] = vals
+        back = oracle.pack_colors(rgba, R)
+        assert np.array_equal((back >> shift) & top, codes)
+    # ties to even: 1 + 1/128 lies halfway between 1 and 1 + 1/64
+    x = np.array([[1 + 1 / 128, 1 + 3 / 128, -2.0, 0], [65024 + 255, 65024 + 256, 2.0 ** -19, 0],
+                  [np.nan, np.inf, 2.0 ** -20, 0], [2.0 ** -14 - 2.0 ** -21, 0.5, 64512 + 512, 0]], np.float32)
+    got = oracle.unpack_colors(oracle.pack_colors(x, R), R)
+    np.testing.assert_array_equal(got[0, :3], [1.0, 1 + 2 / 64, 0.0])      # B: a negative value is stored as 0
+    # B's smallest denormal is 2^-19, so 2^-20 is a tie that goes to the
+    # even code 0; 2^-14 - 2^-21 is R's tie between denormal codes 63 and
+    # 64 (the smallest normal); 64512 + 512 is B's tie above its largest
+    # finite value, whose odd mantissa rounds up to Inf
+    assert got[1, 0] == 65024 and np.isinf(got[1, 1]) and got[1, 2] == 2.0 ** -19
+    assert np.isnan(got[2, 0]) and np.isinf(got[2, 1]) and got[2, 2] == 0.0
+    assert got[3, 0] == 2.0 ** -14 and got[3, 1] == 0.5 and np.isinf(got[3, 2])
+    assert (got[:, 3] == 1).all()

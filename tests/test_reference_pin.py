@@ -249,3 +249,61 @@ def test_sample_probe_image_matches_reference(ref):
     assert (a[bg] == 0).all() and (b[bg] == 0).all()
     assert np.isfinite(a).all() and (a[~bg][:, 3] == 1).all()
     assert rel_err(a[~bg], b[~bg], floor=1e-2) < 1.5e-3
+
+
+def _r11(texels) -> np.ndarray:
+    return oracle.unpack_colors(texels, N.COLOR_R11G11B10F)
+
+
+def _engine_formats_close(a, b, draws):
+    """Two R11G11B10F atlases written through `draws` rounding steps each:
+    most codes identical, the rest within one code step (2^-6 relative for R
+    and G, 2^-5 for B) per draw."""
+    x, y = _r11(a)[:, :3], _r11(b)[:, :3]
+    assert np.isfinite(x).all() and np.isfinite(y).all()
+    assert np.mean(a != b) < 2e-3
+    assert rel_err(x, y) <= draws * 2.0 ** -5
+
+
+@pytest.mark.parametrize("copy_emissive", [True, False])
+def test_surface_light_engine_formats_match_reference(ref, copy_emissive):
+    """The lighting pass on the engine's texture formats -- R11G11B10F
+    emissive and lit atlas, RGBA16F G-buffers (GlobalSurfaceAtlas.cpp:
+    407-411) -- against the reference's compiled functions, each draw's
+    result rounded to the 11/11/10-bit target by both."""
+    w = tiny_workload(sdf=32, prims=8, atlas=256)
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode, light_format=N.COLOR_R11G11B10F,
+                            gbuffer_format=N.GBUFFER_RGBA16F)
+    assert inp.direct.dtype == np.uint32 and inp.gbuffer0.dtype == np.uint16
+    L = _test_lights()
+    tiles = np.arange(1, host.num_tiles, dtype=np.uint32)
+    masks = np.random.default_rng(4).integers(0, 8, size=tiles.size).astype(np.uint32)
+    cam = (0.3, 0.5, -2.0)
+    a = oracle.surface_light(inp, L, tiles, masks, cam, 1.0, copy_emissive, 250, 0)
+    b = oracle.ref_surface_light(inp, L, tiles, masks, cam, 1.0, copy_emissive)
+    assert a.dtype == np.uint32 and np.count_nonzero(a != inp.direct) > 10000
+    _engine_formats_close(a, b, 1 + len(L))
+
+
+def test_inject_and_trace_engine_formats_match_reference(ref):
+    """Injection into an R11G11B10F light cache from RGBA16F G-buffers, and
+    the light-cache trace sampling it, against the reference's compiled
+    sampleIrradiance and sampleGlobalSurfaceAtlas."""
+    w = tiny_workload(light=N.LIGHT_CACHE, prims=8)
+    host = HostScene(w.scene)
+    inp = oracle.HostInputs(host, w.volume.light_mode, light_format=N.COLOR_R11G11B10F,
+                            gbuffer_format=N.GBUFFER_RGBA16F)
+    vd = w.volume.desc()
+    rots = [frame_rotation(47, f) for f in range(2)]
+    irr, dist, frames, _ = oracle.run_frames(vd, inp, rots, precision=0)
+    a = oracle.inject(vd, inp, irr, dist, frames, precision=0)
+    b = oracle.ref_inject(vd, inp, irr, dist)
+    assert np.count_nonzero(a != inp.direct) > 10000
+    _engine_formats_close(a, b, 1)
+    inp.light_cache[:] = a
+    rot = frame_rotation(47, 2)
+    rays, info = oracle.trace(vd, inp, rot, frames, irr, dist, precision=0)
+    rr, rinfo = oracle.ref_trace(vd, inp, rot, frames, irr, dist, dirs=oracle.ray_dirs(rot, vd.uniform.rays_per_probe))
+    assert np.array_equal(info[..., :2], rinfo)
+    assert rel_err(rays[..., :3], rr[..., :3], floor=1e-2) < 1e-5

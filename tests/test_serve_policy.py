@@ -150,3 +150,30 @@ def test_bad_arguments(scene):
     srv.close()
     with pytest.raises(N.LuxgiError):
         Server(1 << 40, executor="sim", max_inflight=99)
+
+
+def test_submit_while_touch_evicts(scene):
+    """A request for the session a touch is evicting (the eviction copy runs
+    with the server's lock released) waits for the eviction and then
+    re-admits the session; it never runs on the session mid-eviction, and
+    the victim is not evicted twice (budget: one session)."""
+    import threading
+
+    srv, (a, b), per = _server(scene, 2, 1, sim_evict_s=0.3)
+    srv.touch(a)
+    assert srv.state(a)[0]
+    t = threading.Thread(target=srv.touch, args=(b,))
+    t.start()
+    time.sleep(0.1)                       # the touch is now evicting a
+    srv.submit(a, frame_rotation(1, 0))
+    t.join()
+    srv.drain(timeout=10.0)
+    st = srv.stats()
+    assert st["completed"] == 1
+    # touch a, touch b (evicting a), then a admitted again (evicting b)
+    assert st["admissions"] == 3
+    assert st["evictions"] == 2
+    assert srv.state(a) == (True, 1)
+    assert srv.state(b)[0] is False
+    assert st["resident_sessions"] == 1 and st["resident_bytes"] == per
+    srv.close()

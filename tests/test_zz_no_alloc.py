@@ -25,10 +25,10 @@ from tests._helpers import tiny_workload
 pytestmark = pytest.mark.gpu
 
 
-def _device_sdf(fmt, seed, res):
+def _device_sdf(fmt, seed, res, cascades=1):
     import torch
 
-    host = HostScene(tiny_workload(sdf=res, sdf_format=fmt, seed=seed, prims=8).scene)
+    host = HostScene(tiny_workload(sdf=res, sdf_format=fmt, seed=seed, prims=8, cascades=cascades).scene)
     sdf = torch.from_numpy(host.sdf.view(np.int16) if fmt == N.STORAGE_FP16 else host.sdf).cuda()
     desc = N.SdfDesc()
     desc.data = host.sdf_data
@@ -58,6 +58,33 @@ def test_no_alloc_mip_matches_allocating_entry_point(fmt):
         desc.mip = ref.data_ptr()
         assert lib.luxgi_sdf_build_mip(ctypes.byref(desc), ref.data_ptr(), tmp.data_ptr(), stream) == N.LUXGI_OK
         out = torch.full((m * m * m,), -2, dtype=elem, device="cuda")
+        assert lib.luxgi_sdf_build_mip_noalloc(ctypes.byref(desc), out.data_ptr(), stream) == N.LUXGI_OK
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref)
+
+
+@pytest.mark.parametrize("fmt", [N.STORAGE_FP32, N.STORAGE_FP16])
+def test_no_alloc_mip_multi_cascade(fmt):
+    """Packed SDFs of 2 and 4 cascades (the mip of each cascade built in
+    turn through the one scratch plane), two calls in a row, equal bit for
+    bit to luxgi_sdf_build_mip."""
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    lib = N.ddgi()
+    stream = torch.cuda.current_stream().cuda_stream
+    elem = torch.int16 if fmt == N.STORAGE_FP16 else torch.float32
+    for seed, res, cascades in ((6, 128, 2), (7, 64, 4)):
+        host, sdf, desc = _device_sdf(fmt, seed, res, cascades)
+        assert host.cascades == cascades
+        m = host.mres
+        n = m * cascades * m * m
+        ref = torch.full((n,), -1, dtype=elem, device="cuda")
+        tmp = torch.zeros(m * m * m, dtype=elem, device="cuda")
+        desc.mip = ref.data_ptr()
+        assert lib.luxgi_sdf_build_mip(ctypes.byref(desc), ref.data_ptr(), tmp.data_ptr(), stream) == N.LUXGI_OK
+        out = torch.full((n,), -2, dtype=elem, device="cuda")
         assert lib.luxgi_sdf_build_mip_noalloc(ctypes.byref(desc), out.data_ptr(), stream) == N.LUXGI_OK
         torch.cuda.synchronize()
         assert torch.equal(out, ref)
