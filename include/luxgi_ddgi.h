@@ -220,7 +220,11 @@ typedef struct luxgi_ddgi_volume_desc {
                                       mip + SDF (4x SDF memory); 5 quad-packed
                                       mip + pair-packed SDF (2x SDF memory);
                                       6-9 as 2-5 with the pooled march (warps
-                                      refill finished lanes from a ray pool) */
+                                      refill finished lanes from a ray pool);
+                                      10 gather textures: one copy of the mip
+                                      and of the SDF in 2D texture arrays,
+                                      a trilinear sample two textureGathers
+                                      (1x SDF memory)                       */
     int32_t shade_variant;         /* tuning, results identical: cage probes of
                                       sampleIrradiance per loop iteration
                                       (0 default = 1; 1, 2, 4 or 8)          */

@@ -127,7 +127,7 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         const luxgi_ddgi_volume* v = vols[i];
         BlendParams b;
         volume_blend_params(v, b);
-        const int64_t PR = trace_work(v->P, v->R, (v->desc.ray_order == 1 && v->desc.march_variant < 6) ? 1 : 0);
+        const int64_t PR = trace_work(v->P, v->R, (v->desc.ray_order == 1 && !pooled_variant(v->desc.march_variant)) ? 1 : 0);
         luxgi_ddgi_volume_desc vd = v->desc;
         vd.march_budget = t.march_budget == 0 ? kDefaultMarchBudget : t.march_budget;
         P.budget = std::min(P.budget, march_budget_for(vd, PR, int(v->sdf.data.cascades_count)));

@@ -55,6 +55,87 @@ template <typename T> cudaError_t dmalloc(T** p, size_t bytes) {
     return cudaMalloc(reinterpret_cast<void**>(p), bytes);
 }
 
+using GatherTex = luxgi_ddgi_volume::GatherTex;
+
+void gather_free(GatherTex& g) {
+    if (g.tex) cudaDestroyTextureObject(g.tex);
+    if (g.arr) cudaFreeArray(g.arr);
+    g = GatherTex{};
+}
+
+// The gather texture of a W x H x D volume (march variant 10): planes of
+// (W + 2) x (H + 2) texels tiled gx to a row within the device's texture
+// gather limits, in a CUDA array made for gathers; point sampling,
+// unnormalised coordinates.  Reuses the array when the shape is unchanged.
+int gather_alloc(GatherTex& g, int W, int H, int D, int format) {
+    if (g.arr && g.W == W && g.H == H && g.D == D && g.format == format) return LUXGI_OK;
+    gather_free(g);
+    int dev = 0, maxw = 0, maxh = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxTexture2DGatherWidth, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&maxh, cudaDevAttrMaxTexture2DGatherHeight, dev);
+    if (e != cudaSuccess) return cuda_status(e);
+    const int pw = W + 2, ph = H + 2;
+    // planes a row: the largest power of two within the gather width (and
+    // no more than the planes need), so a plane's tile is a shift and a mask
+    int gx = 1;
+    while (gx * 2 * pw <= maxw && gx < D) gx *= 2;
+    const int gy = (D + gx - 1) / gx;
+    if (gx * pw > maxw || int64_t(gy) * ph > int64_t(maxh)) return LUXGI_EUNSUPPORTED;
+    const cudaChannelFormatDesc cd =
+        format == LUXGI_STORAGE_FP16 ? cudaCreateChannelDescHalf() : cudaCreateChannelDesc<float>();
+    e = cudaMallocArray(&g.arr, &cd, size_t(gx * pw), size_t(gy * ph), cudaArrayTextureGather);
+    if (e != cudaSuccess) {
+        g.arr = nullptr;
+        return e == cudaErrorMemoryAllocation ? LUXGI_ENOMEM : cuda_status(e);
+    }
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = g.arr;
+    cudaTextureDesc td{};
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    e = cudaCreateTextureObject(&g.tex, &rd, &td, nullptr);
+    if (e != cudaSuccess) {
+        g.tex = 0;
+        gather_free(g);
+        return cuda_status(e);
+    }
+    g.gx = gx;
+    g.tw = gx * pw;
+    g.th = gy * ph;
+    g.W = W;
+    g.H = H;
+    g.D = D;
+    g.format = format;
+    return LUXGI_OK;
+}
+
+// Fills a gather texture from the linear volume `src` through a staging
+// image (allocated for the copy).
+cudaError_t gather_fill(const GatherTex& g, const void* src, cudaStream_t st) {
+    const size_t esz = g.format == LUXGI_STORAGE_FP16 ? 2 : 4;
+    void* stage = nullptr;
+    cudaError_t e = cudaMallocAsync(&stage, esz * size_t(g.tw) * size_t(g.th), st);
+    if (e != cudaSuccess) return e;
+    e = launch_gather_pack(src, g.W, g.H, g.D, g.gx, g.tw, g.th, g.format, stage, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DToArrayAsync(g.arr, 0, 0, stage, esz * size_t(g.tw), esz * size_t(g.tw), size_t(g.th),
+                                     cudaMemcpyDeviceToDevice, st);
+    const cudaError_t f = cudaFreeAsync(stage, st);
+    return e != cudaSuccess ? e : f;
+}
+
+GatherVol gather_view(const GatherTex& g) {
+    GatherVol v{};
+    v.tex = g.tex;
+    v.lg = 0;
+    while ((1 << (v.lg + 1)) <= g.gx) ++v.lg;
+    return v;
+}
+
 void free_volume(luxgi_ddgi_volume* v) {
     void* ptrs[] = {v->irr[0], v->irr[1], v->dist[0], v->dist[1], v->dirs_trace, v->dirs_blend, v->rays, v->info,
                     v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
@@ -63,6 +144,8 @@ void free_volume(luxgi_ddgi_volume* v) {
                     v->shade_order, v->split_bins, v->split_key, v->split_order};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    gather_free(v->sdf_gt);
+    gather_free(v->mip_gt);
     if (v->fork_ev) cudaEventDestroy(v->fork_ev);
     if (v->join_ev) cudaEventDestroy(v->join_ev);
     if (v->side) cudaStreamDestroy(v->side);
@@ -147,13 +230,13 @@ size_t atlas_elem_bytes(int storage) { return storage == LUXGI_STORAGE_FP16 ? 2 
 }  // namespace
 
 bool luxgi::shade_binned(const luxgi_ddgi_volume_desc& d, int64_t work) {
-    if (d.march_variant >= 6 || work >= (int64_t(1) << 32) || d.shade_order < 0) return false;
+    if (pooled_variant(d.march_variant) || work >= (int64_t(1) << 32) || d.shade_order < 0) return false;
     return d.shade_order == 1 || work >= kLargeWork;     // default: large launches
 }
 
 int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int cascades) {
     const int mv = d.march_variant == 0 ? 4 : d.march_variant;
-    if (d.march_budget < 0 || mv >= 6) return 0;
+    if (d.march_budget < 0 || pooled_variant(mv)) return 0;
     // queue entries hold 32-bit work indices and 16-bit step totals
     if (work >= (int64_t(1) << 32) || int64_t(cascades) * d.max_steps >= 65536) return 0;
     // default: compacted passes after 12 steps (then 8) for large launches
@@ -183,11 +266,18 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
     b += 64 * nobj + 4 * cap + 4 * (2 * 40ull * 40 * 40 + 1);
     const int C = int(sdf.data.cascades_count);
     const int mv = d.march_variant == 0 ? 4 : d.march_variant;
-    const int layout = mv >= 6 ? mv - 4 : mv;
-    if (layout >= 3) b += quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
+    const int layout = pooled_variant(mv) ? mv - 4 : mv;
+    if (layout >= 3 && layout <= 5)
+        b += quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
     if (layout == 4) b += quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
     if (layout == 5) b += pair_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
-    if (mv < 6) b += cell_min_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution);
+    if (layout == 10) {
+        // the two gather textures: planes with a 1-texel apron
+        const uint64_t esz = sdf.format == LUXGI_STORAGE_FP16 ? 2 : 4;
+        const uint64_t r = uint64_t(sdf.resolution), m = uint64_t(sdf.mip_resolution);
+        b += esz * ((r * C + 2) * (r + 2) * r + (m * C + 2) * (m + 2) * m);
+    }
+    if (!pooled_variant(mv)) b += cell_min_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution);
     return b;
 }
 
@@ -197,15 +287,16 @@ int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
     const luxgi_sdf_desc& sdf = v->sdf;
     const int C = int(sdf.data.cascades_count);
     const int mv = v->desc.march_variant;
-    const int layout = mv >= 6 ? mv - 4 : mv;          // 6..9 -> 2..5
+    const int layout = pooled_variant(mv) ? mv - 4 : mv;   // 6..9 -> 2..5
     // the quad samplers index texels with 32-bit arithmetic
     auto quad_texels = [](int W, int H, int D) { return uint64_t(W + 1) * uint64_t(H + 1) * uint64_t(D); };
     if (layout >= 3 && quad_texels(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution) >> 32)
         return LUXGI_EUNSUPPORTED;
     if (layout == 4 && quad_texels(sdf.resolution * C, sdf.resolution, sdf.resolution) >> 32)
         return LUXGI_EUNSUPPORTED;
-    const size_t mq = (layout >= 3) ? quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution,
-                                                 sdf.format) : 0;
+    const size_t mq = (layout >= 3 && layout <= 5) ? quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution,
+                                                                sdf.mip_resolution, sdf.format)
+                                                     : 0;
     const size_t sq = (layout == 4)   ? quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format)
                       : (layout == 5) ? pair_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format)
                                       : 0;
@@ -229,8 +320,18 @@ int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
             v->sdf_quad_bytes = sq;
         }
     }
+    // gather textures for variant 10
+    if (layout == 10) {
+        int s = gather_alloc(v->sdf_gt, sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
+        if (s == LUXGI_OK)
+            s = gather_alloc(v->mip_gt, sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
+        if (s != LUXGI_OK) return s;
+    } else {
+        gather_free(v->sdf_gt);
+        gather_free(v->mip_gt);
+    }
     // cell minima for every per-ray march variant (the pooled march reads none)
-    const size_t cb = (mv >= 6) ? 0 : cell_min_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution);
+    const size_t cb = pooled_variant(mv) ? 0 : cell_min_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution);
     if (cb != v->cell_min_bytes) {
         if (v->cell_min) cudaFree(v->cell_min);
         v->cell_min = nullptr;
@@ -266,6 +367,11 @@ int luxgi::volume_prepare(luxgi_ddgi_volume* v, cudaStream_t st) {
         e = launch_cell_min(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf.data.resolution, v->cell_min, st);
         if (e != cudaSuccess) return cuda_status(e);
     }
+    if (v->sdf_gt.arr) {
+        e = gather_fill(v->sdf_gt, v->sdf.sdf, st);
+        if (e == cudaSuccess) e = gather_fill(v->mip_gt, v->sdf.mip, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
     if (v->sdf_quad) {
         e = (v->desc.march_variant == 5 || v->desc.march_variant == 9)
                 ? launch_pair_pack(v->sdf.sdf, res * C, res, res, v->sdf.format, v->sdf_quad, st)
@@ -287,6 +393,8 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.surf.culled = v->shade_culled;
     p.sdf.sdf_quad = v->sdf_quad;
     p.sdf.mip_quad = v->mip_quad;
+    p.sdf.sdf_g = gather_view(v->sdf_gt);
+    p.sdf.mip_g = gather_view(v->mip_gt);
     p.sdf.cell_near =
         v->cell_min ? cell_bits(v->cell_min, v->sdf.resolution * int(v->sdf.data.cascades_count), v->sdf.resolution,
                                 v->sdf.resolution)
@@ -314,7 +422,7 @@ void luxgi::volume_trace_params(const luxgi_ddgi_volume* v, const float rot[9], 
     p.bounce = (d.infinite_bounce && v->frames != 0) ? 1 : 0;
     p.P = v->P;
     p.R = v->R;
-    p.order = (d.ray_order == 1 && d.march_variant < 6) ? 1 : 0;
+    p.order = (d.ray_order == 1 && !pooled_variant(d.march_variant)) ? 1 : 0;
     p.work = trace_work(v->P, v->R, p.order);
     p.index32 = p.work < (int64_t(1) << 32) ? 1 : 0;
     p.div_p = make_fastdiv(uint32_t(v->P));
@@ -392,7 +500,7 @@ namespace {
 
 int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     if (!v->bound) return LUXGI_ENOTBOUND;
-    const int order = (v->desc.ray_order == 1 && v->desc.march_variant < 6) ? 1 : 0;
+    const int order = (v->desc.ray_order == 1 && !pooled_variant(v->desc.march_variant)) ? 1 : 0;
     const int64_t work = trace_work(v->P, v->R, order);
     if (!v->mq && march_budget_for(v->desc, work, int(v->sdf.data.cascades_count)) > 0) {
         // queues of the compacted march, made on the first trace that needs them
@@ -434,7 +542,8 @@ int do_trace(luxgi_ddgi_volume* v, const float rot[9], cudaStream_t st) {
     if (e == cudaSuccess) e = launch_weights(b, st);
     int s = e == cudaSuccess ? volume_prepare(v, st) : cuda_status(e);
     const bool split =
-        s == LUXGI_OK && p.bin_count && p.budget1 > 0 && p.march_variant < 6 && shade_split(v->desc, p.work);
+        s == LUXGI_OK && p.bin_count && p.budget1 > 0 && !pooled_variant(p.march_variant) &&
+        shade_split(v->desc, p.work);
     if (split) s = alloc_split(v, p.work);
     if (s == LUXGI_OK && split) {
         // pass 1 on st; its finishers sorted and shaded on the side stream
@@ -595,7 +704,7 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->light_mode != LUXGI_LIGHT_CACHE && desc->light_mode != LUXGI_LIGHT_PER_HIT) return LUXGI_EINVAL;
     if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
     if (desc->max_steps < 1) return LUXGI_EINVAL;
-    if (desc->march_variant < 0 || desc->march_variant > 9) return LUXGI_EINVAL;
+    if (desc->march_variant < 0 || desc->march_variant > 10) return LUXGI_EINVAL;
     if (desc->ray_order != 0 && desc->ray_order != 1) return LUXGI_EINVAL;
     if (desc->march_budget < -1) return LUXGI_EINVAL;
     if (desc->shade_split < -1 || desc->shade_split > 1) return LUXGI_EINVAL;

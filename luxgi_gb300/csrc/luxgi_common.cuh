@@ -301,8 +301,52 @@ __device__ __forceinline__ float sample3d_pair(const typename Pair<T>::type* __r
     return c0 * ic + c1 * c;
 }
 
+// Gather-texture volume: the z planes of a W x H x D volume tiled into one
+// 2D texture (CUDA array, block-linear), gx = 2^lg planes a row, each plane
+// (W + 2) x (H + 2) texels with a 1-texel apron that repeats its edge
+// (clamp-to-edge inside the tile).  Volume texel (x, y, z) sits at texture
+// texel (ox + x + 1, oy + y + 1), (ox, oy) = ((z mod gx) (W + 2),
+// (z div gx) (H + 2)).  One textureGather at the unnormalised point
+// (ox + ix + 2, oy + iy + 2) -- the centre of a 2x2 block, so the texture
+// unit's sub-texel rounding cannot move the footprint -- returns the four
+// texels (ix .. ix+1) x (iy .. iy+1) of plane z, clamped; a trilinear sample
+// is two gathers (planes z0, z1) and the same FP32 lerps as the eight-tap
+// form.  One copy of the volume (+1.6 % of apron at 256^2 planes) where the
+// quad-packed copy holds four.
+struct GatherVol {
+    unsigned long long tex;   // cudaTextureObject_t
+    int lg;                   // planes per texture row = 2^lg
+};
+
+template <typename T>
+__device__ __forceinline__ float gather_lerp(const GatherVol& g, int W, int H, int D, float a, float b, float c, int ix,
+                                             int iy, int iz) {
+    const int z0 = imx(iz, 0), z1 = imn(iz + 1, D - 1);
+    const int m = (1 << g.lg) - 1;
+    const int ox0 = (z0 & m) * (W + 2), oy0 = (z0 >> g.lg) * (H + 2);
+    const int ox1 = (z1 & m) * (W + 2), oy1 = (z1 >> g.lg) * (H + 2);
+    // (texel x, y) + 1 for the apron, + 1 for the block centre
+    const float4 q0 = tex2Dgather<float4>(g.tex, float(ox0 + ix + 2), float(oy0 + iy + 2), 0);
+    const float4 q1 = tex2Dgather<float4>(g.tex, float(ox1 + ix + 2), float(oy1 + iy + 2), 0);
+    // gather order (i0, j1), (i1, j1), (i1, j0), (i0, j0)
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float c00 = q0.w * ia + q0.z * a, c10 = q0.x * ia + q0.y * a;
+    const float c01 = q1.w * ia + q1.z * a, c11 = q1.x * ia + q1.y * a;
+    const float c0 = c00 * ib + c10 * b, c1 = c01 * ib + c11 * b;
+    return c0 * ic + c1 * c;
+}
+
+template <typename T>
+__device__ __forceinline__ float sample3d_gather(const GatherVol& g, int W, int H, int D, float u, float vv, float w) {
+    const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    // x and y clamped to [-1, W - 1] (a sample outside [0, 1] reads the edge)
+    const int ix = imn(imx(int(fx), -1), W - 1), iy = imn(imx(int(fy), -1), H - 1);
+    return gather_lerp<T>(g, W, H, D, x - fx, y - fy, z - fz, ix, iy, int(fz));
+}
+
 // Volume layouts a march variant reads
-enum VolLayout { kPlain = 0, kQuad = 1, kPair = 2 };
+enum VolLayout { kPlain = 0, kQuad = 1, kPair = 2, kGather = 3 };
 
 struct SdfView {
     luxgi_sdf_data data;
@@ -311,6 +355,8 @@ struct SdfView {
     const void* sdf_quad;   // packed copy of the full-resolution volume (quad or
                             // pair layout, march variants 4 / 5) or nullptr
     const void* mip_quad;   // quad-packed mip (variants 3-5) or nullptr
+    GatherVol sdf_g;        // gather textures (variant 10), tex 0 otherwise
+    GatherVol mip_g;
     // One bit per cell (i, j, k) of the full-resolution volume, 32 cells a
     // word: set unless the minimum texel over [4i, 4i+4] x [4j, 4j+4] x
     // [4k, 4k+4] (clamped; every texel a trilinear footprint whose lower
@@ -349,8 +395,9 @@ __device__ __forceinline__ bool fine_needed(const SdfView& s, float u, float v, 
 // One GL trilinear sample of the full-resolution or mip volume, from the
 // plain layout or from its quad-packed copy (same values either way).
 template <typename T, int LAYOUT>
-__device__ __forceinline__ float sample_vol(const void* plain, const void* packed, int W, int H, int D, float u, float v,
-                                            float w) {
+__device__ __forceinline__ float sample_vol(const void* plain, const void* packed, const GatherVol& g, int W, int H,
+                                            int D, float u, float v, float w) {
+    if (LAYOUT == kGather) return sample3d_gather<T>(g, W, H, D, u, v, w);
     if (LAYOUT == kQuad) return sample3d_quad<T>(static_cast<const typename Quad<T>::type*>(packed), W, H, D, u, v, w);
     if (LAYOUT == kPair) return sample3d_pair<T>(static_cast<const typename Pair<T>::type*>(packed), W, H, D, u, v, w);
     return sample3d(static_cast<const T*>(plain), W, H, D, u, v, w);
@@ -360,14 +407,14 @@ __device__ __forceinline__ float sample_vol(const void* plain, const void* packe
 // packed texture coordinates (SDFCommon.glsl:174-183).  Kept out of line so
 // the march loop's register budget does not carry its taps.
 template <typename T, int LAYOUT>
-__device__ __noinline__ f3 sdf_normal(const void* tex, const void* texq, int TW, int res, float tu, float uy, float uz,
-                                      float off) {
-    const float xp = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu + off, uy, uz);
-    const float xn = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu - off, uy, uz);
-    const float yp = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy + off, uz);
-    const float yn = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy - off, uz);
-    const float zp = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy, uz + off);
-    const float zn = sample_vol<T, LAYOUT>(tex, texq, TW, res, res, tu, uy, uz - off);
+__device__ __noinline__ f3 sdf_normal(const void* tex, const void* texq, const GatherVol g, int TW, int res, float tu,
+                                      float uy, float uz, float off) {
+    const float xp = sample_vol<T, LAYOUT>(tex, texq, g, TW, res, res, tu + off, uy, uz);
+    const float xn = sample_vol<T, LAYOUT>(tex, texq, g, TW, res, res, tu - off, uy, uz);
+    const float yp = sample_vol<T, LAYOUT>(tex, texq, g, TW, res, res, tu, uy + off, uz);
+    const float yn = sample_vol<T, LAYOUT>(tex, texq, g, TW, res, res, tu, uy - off, uz);
+    const float zp = sample_vol<T, LAYOUT>(tex, texq, g, TW, res, res, tu, uy, uz + off);
+    const float zn = sample_vol<T, LAYOUT>(tex, texq, g, TW, res, res, tu, uy, uz - off);
     return norm3(f3{xp - xn, yp - yn, zp - zn});
 }
 
@@ -470,22 +517,27 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             // their value cannot be used; it is used only where
             // SDFCommon.glsl:150-158 samples the full-resolution SDF
             float sd, sdt;
-            if (QTEX == kQuad) {
-                // the cell test and the quad sample share the floors of the
-                // full-resolution texel coordinates
+            if (QTEX == kQuad || QTEX == kGather) {
+                // the cell test and the quad / gather sample share the floors
+                // of the full-resolution texel coordinates
                 const float fx = tu * float(TW) - 0.5f, fy = uy * float(s.res) - 0.5f, fz = uz * float(s.res) - 0.5f;
                 const float lx = floorf(fx), ly = floorf(fy), lz = floorf(fz);
                 const int ix = int(lx), iy = int(ly), iz = int(lz);
                 const bool need_fine = fine_needed_at(s, ix, iy, iz);
-                // tu, uy, uz lie in [0, 1] (clamped above; tu = (cascade + ux) / C)
+                // tu, uy, uz lie in [0, 1] (clamped above; tu = (cascade + ux) / C),
+                // so ix, iy lie in [-1, W - 1] (a NaN converts to 0)
                 if (QMIP == kQuad)
                     sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
                                                s.mres, tu, uy, uz);
                 else
-                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
-                sdt = need_fine ? quad_lerp_unit<T>(static_cast<const typename Quad<T>::type*>(s.sdf_quad), TW, s.res,
-                                                    s.res, fx - lx, fy - ly, fz - lz, ix, iy, iz)
-                                : 1.0f;
+                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
+                if (!need_fine)
+                    sdt = 1.0f;
+                else if (QTEX == kGather)
+                    sdt = gather_lerp<T>(s.sdf_g, TW, s.res, s.res, fx - lx, fy - ly, fz - lz, ix, iy, iz);
+                else
+                    sdt = quad_lerp_unit<T>(static_cast<const typename Quad<T>::type*>(s.sdf_quad), TW, s.res, s.res,
+                                            fx - lx, fy - ly, fz - lz, ix, iy, iz);
             } else {
                 const bool need_fine = fine_needed(s, tu, uy, uz);
                 if (QMIP == kPlain)
@@ -494,13 +546,13 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
                     sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
                                                s.mres, tu, uy, uz);
                 else
-                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
+                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
                 if (!need_fine)
                     sdt = 1.0f;
                 else if (QTEX == kPlain)
                     sdt = sample3d_unit<T>(static_cast<const T*>(s.sdf), TW, s.res, s.res, tu, uy, uz);
                 else
-                    sdt = sample_vol<T, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz);
+                    sdt = sample_vol<T, QTEX>(s.sdf, s.sdf_quad, s.sdf_g, TW, s.res, s.res, tu, uy, uz);
             }
             if (sd < chunk) {
                 ++m.fine;
@@ -549,7 +601,7 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
 template <typename T, int QTEX>
 __device__ __forceinline__ void march_hit_normal(const SdfView& s, MarchHit& hit) {
     if (hit.time >= 0.0f)
-        hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, s.res * s.C, s.res, hit.u, hit.v, hit.w,
+        hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, s.sdf_g, s.res * s.C, s.res, hit.u, hit.v, hit.w,
                                          1.0f / s.data.resolution);
 }
 

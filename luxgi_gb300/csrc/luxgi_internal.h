@@ -10,6 +10,10 @@
 
 namespace luxgi {
 
+// March variants 6-9 are the pooled march (warps refill finished lanes
+// from a ray pool); 1-5 and 10 run one ray per thread.
+inline bool pooled_variant(int mv) { return mv >= 6 && mv <= 9; }
+
 // Count of kernel launches issued by the library (luxgi_launch_count).
 void note_launch(int n = 1);
 
@@ -198,6 +202,8 @@ const uint32_t* cell_bits(const float* cmin, int W, int H, int D);
 cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, float resolution, float* dst,
                             cudaStream_t st);
 cudaError_t launch_quad_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);
+cudaError_t launch_gather_pack(const void* src, int W, int H, int D, int gx, int tw, int th, int format, void* dst,
+                               cudaStream_t st);
 size_t pair_bytes(int W, int H, int D, int format);
 cudaError_t launch_pair_pack(const void* src, int W, int H, int D, int format, void* dst, cudaStream_t st);
 cudaError_t launch_shade_lists(const luxgi_surface_data& d, const luxgi_surface_object* objects,

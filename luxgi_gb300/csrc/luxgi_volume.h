@@ -47,6 +47,14 @@ struct luxgi_ddgi_volume {
     void* sdf_quad = nullptr;           // quad-packed copies for march variants 3, 4
     void* mip_quad = nullptr;
     size_t sdf_quad_bytes = 0, mip_quad_bytes = 0;
+    // gather textures of the full-resolution SDF and the mip (march variant
+    // 10): a 2D CUDA array each, planes tiled gx to a row
+    struct GatherTex {
+        cudaArray_t arr = nullptr;
+        cudaTextureObject_t tex = 0;
+        int gx = 0, tw = 0, th = 0, W = 0, H = 0, D = 0, format = -1;
+    };
+    GatherTex sdf_gt, mip_gt;
     luxgi_sdf_desc sdf{};
     luxgi_surface_desc surf{};
     float* cell_min = nullptr;          // conservative cell minima of the full-resolution SDF

@@ -324,8 +324,8 @@ __global__ void __launch_bounds__(256, 4) march_pool_kernel(const TraceParams p)
                     const float uy = clampf((sp.y - cy) / md + 0.5f, 0.0f, 1.0f);
                     const float uz = clampf((sp.z - cz) / md + 0.5f, 0.0f, 1.0f);
                     const float tu = (float(cascade) + ux) / float(C);
-                    float sd = sample_vol<SdfT, QMIP>(s.mip, s.mip_quad, MW, s.mres, s.mres, tu, uy, uz);
-                    const float sdt = sample_vol<SdfT, QTEX>(s.sdf, s.sdf_quad, TW, s.res, s.res, tu, uy, uz);
+                    float sd = sample_vol<SdfT, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
+                    const float sdt = sample_vol<SdfT, QTEX>(s.sdf, s.sdf_quad, s.sdf_g, TW, s.res, s.res, tu, uy, uz);
                     if (sd < chunk) {
                         ++fine;
                         if (sdt < margin * 2.0f) sd = sdt;
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(256, 4) march_pool_kernel(const TraceParams p)
                     const float thick = (voxel * 0.5f) * clampf(t / voxel, 0.0f, 1.0f);
                     if (sd < thick) {
                         const float time = mx(t + sd - thick, 0.0f);
-                        const f3 nrm = sdf_normal<SdfT, QTEX>(s.sdf, s.sdf_quad, TW, s.res, tu, uy, uz,
+                        const f3 nrm = sdf_normal<SdfT, QTEX>(s.sdf, s.sdf_quad, s.sdf_g, TW, s.res, tu, uy, uz,
                                                              1.0f / s.data.resolution);
                         steps += step;
                         finish_ray(cur, time, cascade, sd, nrm);
@@ -413,7 +413,7 @@ cudaError_t launch_march(const TraceParams& p, cudaStream_t st) { return launch_
 
 cudaError_t launch_march_split(const TraceParams& p, const TraceParams& resume, cudaEvent_t after_first,
                                cudaStream_t st) {
-    if (p.march_variant >= 6 || p.budget1 <= 0 || !after_first) return cudaErrorInvalidValue;
+    if (pooled_variant(p.march_variant) || p.budget1 <= 0 || !after_first) return cudaErrorInvalidValue;
     return launch_march_passes(p, st, resume, after_first);
 }
 
@@ -421,7 +421,7 @@ static cudaError_t launch_march_passes(const TraceParams& p, cudaStream_t st, co
                                        cudaEvent_t after_first) {
     const int64_t total = p.work;
     if (total <= 0) return cudaSuccess;
-    if (p.march_variant >= 6) {
+    if (pooled_variant(p.march_variant)) {
         // pooled march: 8 rays per lane, 8 warps per block
         constexpr int POOL = 8;
         const int64_t warps = (total + 32 * POOL - 1) / (32 * POOL);
@@ -453,6 +453,7 @@ static cudaError_t launch_march_passes(const TraceParams& p, cudaStream_t st, co
     // variants: 1 plain layout, 64 registers (4 blocks of 256 per SM);
     // 2 plain layout, no register bound; 3 quad-packed mip; 4 quad-packed
     // mip and full-resolution volume; 5 quad-packed mip, pair-packed
+    // full-resolution volume; 10 gather textures of the mip and the
     // full-resolution volume.  All produce identical results.
     const bool h = p.sdf.format == LUXGI_STORAGE_FP16;
     cudaError_t e;
@@ -463,6 +464,7 @@ static cudaError_t launch_march_passes(const TraceParams& p, cudaStream_t st, co
         case 3: e = h ? launch_march_variant<__half, 4, kQuad, kPlain>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kPlain>(p, st, r, a); break;
         case 4: e = h ? launch_march_variant<__half, 4, kQuad, kQuad>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kQuad>(p, st, r, a); break;
         case 5: e = h ? launch_march_variant<__half, 4, kQuad, kPair>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kPair>(p, st, r, a); break;
+        case 10: e = h ? launch_march_variant<__half, 4, kGather, kGather>(p, st, r, a) : launch_march_variant<float, 4, kGather, kGather>(p, st, r, a); break;
         default: e = h ? launch_march_variant<__half, 4, kPlain, kPlain>(p, st, r, a) : launch_march_variant<float, 4, kPlain, kPlain>(p, st, r, a); break;
     }
     return e;
@@ -603,6 +605,42 @@ cudaError_t launch_cell_min(const void* src, int W, int H, int D, int format, fl
     cell_bits_kernel<<<unsigned(std::min<int64_t>((words + 255) / 256, 4096)), 256, 0, st>>>(
         dst, n, resolution, const_cast<uint32_t*>(cell_bits(dst, W, H, D)));
     note_launch(2);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ gather pack
+// The gather-texture image of a W x H x D volume (GatherVol): planes of
+// (W + 2) x (H + 2) texels, gx to a row, each with a 1-texel apron that
+// repeats its edge; texels past the last plane are 0.  Written to a linear
+// staging image of tw x th elements, copied into the texture's array.
+template <typename T>
+__global__ void gather_pack_kernel(const T* __restrict__ src, int W, int H, int D, int gx, int tw, int th,
+                                   T* __restrict__ dst) {
+    const int pw = W + 2, ph = H + 2;
+    const int64_t n = int64_t(tw) * th;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const int tx = int(i % tw), ty = int(i / tw);
+        const int z = (ty / ph) * gx + tx / pw;
+        T v = T(0.0f);
+        if (z < D) {
+            const int x = imn(imx(tx % pw - 1, 0), W - 1), y = imn(imx(ty % ph - 1, 0), H - 1);
+            v = src[(size_t(z) * H + y) * W + x];
+        }
+        dst[i] = v;
+    }
+}
+
+cudaError_t launch_gather_pack(const void* src, int W, int H, int D, int gx, int tw, int th, int format, void* dst,
+                               cudaStream_t st) {
+    const int64_t n = int64_t(tw) * th;
+    const unsigned blocks = unsigned(std::min<int64_t>((n + 255) / 256, 8192));
+    if (format == LUXGI_STORAGE_FP16)
+        gather_pack_kernel<__half><<<blocks, 256, 0, st>>>(static_cast<const __half*>(src), W, H, D, gx, tw, th,
+                                                           static_cast<__half*>(dst));
+    else
+        gather_pack_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(src), W, H, D, gx, tw, th,
+                                                          static_cast<float*>(dst));
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -375,14 +375,14 @@ def test_tensor_blend_matches_fp32_blend_on_plain_small(cuda):
 
 @pytest.mark.parametrize("fmt", [N.STORAGE_FP32, N.STORAGE_FP16])
 def test_march_variants_bit_identical(cuda, fmt):
-    """Every march variant (register bound, quad-packed mip / volume) reads
-    the same texel values: per-ray results are identical and equal the FP32
-    oracle."""
+    """Every march variant (register bound, quad-packed mip / volume, gather
+    textures) reads the same texel values: per-ray results are identical and
+    equal the FP32 oracle."""
     from dataclasses import replace
 
     base = tiny_workload(probe_counts=(6, 3, 5), rays=64, sdf=64, sdf_format=fmt, cascades=2, room=20.0, prims=10)
     outs = []
-    for mv in (1, 2, 3, 4, 5, 6, 7, 8, 9):
+    for mv in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10):
         w = replace(base, volume=replace(base.volume, march_variant=mv))
         host, dev, vol, inp = setup(w)
         rot = frame_rotation(50, 0)
@@ -408,7 +408,7 @@ def test_march_compaction_and_ray_order_bit_identical(cuda, fmt):
     outs = []
     for mv, budget, order, sorder, split in ((4, -1, 0, -1, 0), (4, 1, 0, 1, 1), (4, 1, 0, 1, -1), (4, 2, 0, -1, 0),
                                              (4, 8, 0, 0, 0), (3, 2, 1, 1, 1), (4, 3, 1, 1, -1), (5, 8, 1, -1, 0),
-                                             (1, -1, 1, 0, 0)):
+                                             (1, -1, 1, 0, 0), (10, 2, 0, 1, 1), (10, -1, 1, -1, 0)):
         w = replace(base, volume=replace(base.volume, march_variant=mv, march_budget=budget, ray_order=order,
                                          shade_order=sorder, shade_split=split))
         host, dev, vol, inp = setup(w)
