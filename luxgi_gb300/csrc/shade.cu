@@ -204,8 +204,14 @@ cudaError_t launch_shade_sort(const TraceParams& p, cudaStream_t st) {
 // device memory.
 constexpr int kStagedVolumes = 4;
 
+// Resident blocks of 128 threads a SM the batched shading is compiled for
+// (8: 64 registers, 6: 80); without a bound the compiler takes 96
+// registers and the SM keeps 28 % of its warp slots busy.
+#ifndef LUXGI_SHADE_BATCH_MIN_BLOCKS
+#define LUXGI_SHADE_BATCH_MIN_BLOCKS 8
+#endif
 template <int MODE, int UNROLL>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, LUXGI_SHADE_BATCH_MIN_BLOCKS)
     shade_batch_sorted_kernel(const TraceParams* __restrict__ vp, const int* __restrict__ work_off, int n,
                               const uint32_t* __restrict__ seq, int64_t work) {
     constexpr int kWords = int(sizeof(TraceParams) / 4);
@@ -255,7 +261,7 @@ cudaError_t launch_shade_batch_sorted(const TraceParams* vp, const int* work_off
 // Batched over many volumes (128 rays a block), parameters staged in
 // shared memory once per block.
 template <int MODE, int UNROLL>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, LUXGI_SHADE_BATCH_MIN_BLOCKS)
     shade_batch_kernel(const TraceParams* __restrict__ vp, const int* __restrict__ starts, int n) {
     __shared__ __align__(16) uint32_t sp[sizeof(TraceParams) / 4];
     const int v = batch_volume(starts, n, int(blockIdx.x));
