@@ -57,6 +57,7 @@ def lib() -> ctypes.CDLL:
             "oracle_frame_rotation": (c_int, [ctypes.c_uint64, c_uint32, vp]),
             "oracle_derive_uniform": (c_int, [vp]),
             "oracle_pack_colors": (c_int, [vp, ctypes.c_int64, c_int, vp]),
+            "oracle_march_trails": (c_int, [vp, vp, vp, vp, vp, c_int, c_int, vp]),
             "oracle_unpack_colors": (c_int, [vp, ctypes.c_int64, c_int, vp]),
             "oracle_trace": (c_int, [vp, vp, vp, vp, vp, c_int, vp, c_int, c_int, c_int, vp, vp]),
             "oracle_blend": (c_int, [vp, vp, vp, vp, vp, vp, vp, c_int, c_int, c_int, c_int, c_int]),
@@ -135,6 +136,18 @@ def unpack_colors(texels: np.ndarray, fmt: int) -> np.ndarray:
     n = t.size if fmt == N.COLOR_R11G11B10F else t.size // 4
     out = np.zeros((n, 4), dtype=np.float32)
     lib().oracle_unpack_colors(_p(t), n, fmt, _p(out))
+    return out
+
+
+def march_trails(vdesc, inputs: HostInputs, rot, probes, rays, cap: int = 128) -> np.ndarray:
+    """The FP32 march's sample points of rays (probes[i], rays[i]): [n, cap,
+    4] = (u, v, w, full-resolution sampled) per step, -1 past the end."""
+    pr = np.ascontiguousarray(probes, dtype=np.int32)
+    ry = np.ascontiguousarray(rays, dtype=np.int32)
+    out = np.zeros((pr.size, cap, 4), dtype=np.float32)
+    r = np.ascontiguousarray(rot, dtype=np.float32)
+    lib().oracle_march_trails(ctypes.byref(vdesc), ctypes.byref(inputs.sdf_desc), _p(r), _p(pr), _p(ry), pr.size,
+                              cap, _p(out))
     return out
 
 

@@ -348,9 +348,16 @@ template <typename R> V3<R> cascade_texture_uv(const luxgi_sdf_data& d, int casc
 // rays use start bias 0 and want the hit normal (GISDFRays.comp:79-87); the
 // surface-cache shadow rays start 2 voxels along and skip the normal
 // (SDFDeferredLight.frag:104-111).
+// Optional record of a march's sample points: per step the packed texture
+// coordinates (u, v, w) and 1 when the full-resolution SDF was sampled.
+struct MarchTrail {
+    float* out;
+    int cap, n;
+};
+
 template <typename R> Hit<R> trace_sdf(const luxgi_sdf_data& d, const Vol& tex, const Vol& mip,
                                        V3<R> origin, V3<R> dir, R trace_max, int max_steps,
-                                       R start_bias = R(0), bool want_normal = true) {
+                                       R start_bias = R(0), bool want_normal = true, MarchTrail* trail = nullptr) {
     Hit<R> hit;
     const int C = int(d.cascades_count);
     R tmax = std::min(trace_max, R(d.cascade_pos_distance[C - 1][3]) * R(2));
@@ -377,6 +384,10 @@ template <typename R> Hit<R> trace_sdf(const luxgi_sdf_data& d, const Vol& tex, 
             R cmd;
             V3<R> uv = cascade_texture_uv(d, cascade, sp, &cmd);
             R sd = sample3d(mip, uv);
+            if (trail && trail->n < trail->cap) {
+                float* o = trail->out + 4 * trail->n++;
+                o[0] = float(uv.x); o[1] = float(uv.y); o[2] = float(uv.z); o[3] = sd < chunk ? 1.0f : 0.0f;
+            }
             if (sd < chunk) {
                 R sdt = sample3d(tex, uv);
                 ++hit.fine;
@@ -1243,6 +1254,36 @@ int oracle_pack_colors(const float* rgba, int64_t n, int fmt, void* out) {
 // R11G11B10F).
 int oracle_unpack_colors(const void* in, int64_t n, int fmt, float* rgba) {
     for (int64_t i = 0; i < n; ++i) color_load(in, fmt, size_t(i), rgba + 4 * i);
+    return 0;
+}
+
+// The FP32 march's sample points of n rays (probes[i], rays[i]) under
+// `rot`: out [n][cap][4] = (u, v, w, full-resolution sampled) per step, -1
+// past the end of a ray's march.  Analysis aid of the march's memory
+// locality (which texels a group of rays reads at each step).
+int oracle_march_trails(const luxgi_ddgi_volume_desc* vd, const luxgi_sdf_desc* sdf, const float rot[9],
+                        const int32_t* probes, const int32_t* rays, int n, int cap, float* out) {
+    const int res = sdf->resolution, mres = sdf->mip_resolution, C = int(sdf->data.cascades_count);
+    Vol tex, mip;
+    tex.W = res * C; tex.H = res; tex.D = res;
+    mip.W = mres * C; mip.H = mres; mip.D = mres;
+    if (sdf->format == LUXGI_STORAGE_FP16) {
+        tex.f16 = static_cast<const uint16_t*>(sdf->sdf);
+        mip.f16 = static_cast<const uint16_t*>(sdf->mip);
+    } else {
+        tex.f32 = static_cast<const float*>(sdf->sdf);
+        mip.f32 = static_cast<const float*>(sdf->mip);
+    }
+    const luxgi_ddgi_uniform& u = vd->uniform;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < n; ++i) {
+        float* o = out + size_t(i) * cap * 4;
+        for (int k = 0; k < cap * 4; ++k) o[k] = -1.0f;
+        MarchTrail tr{o, cap, 0};
+        const V3<float> origin = probe_location<float>(u, probes[i]);
+        const V3<float> dir = ray_direction<float>(rot, rays[i], u.rays_per_probe);
+        trace_sdf<float>(sdf->data, tex, mip, origin, dir, 60000.0f, vd->max_steps, 0.0f, false, &tr);
+    }
     return 0;
 }
 
