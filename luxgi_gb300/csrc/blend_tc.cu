@@ -12,9 +12,9 @@
 // D accumulates in TMEM (FP32).  One CTA per SM, persistent over M tiles:
 //   warp 0      TMA producer (cp.async.bulk.tensor, 128B swizzle, 16 KB stages)
 //   warp 1      TMEM allocator + single-thread tcgen05.mma issuer
-//   warps 2..9  epilogue: tcgen05.ld, normalise, gamma, hysteresis, store
-//               (two warps per TMEM lane quadrant, each half the columns)
-//               with the border mirrors
+//   warps 2..17 epilogue: tcgen05.ld, normalise, gamma, hysteresis, store
+//               (four warps per TMEM lane quadrant, each a quarter of the
+//               column chunks) with the border mirrors
 // The accumulator is double buffered in TMEM so the epilogue of one tile
 // overlaps the MMAs of the next.  Every mbarrier wait is bounded by a clock
 // budget; on expiry the kernel raises *status, stops issuing work, drains
@@ -34,7 +34,8 @@ namespace {
 constexpr int kStages = 5;
 constexpr int kKBlock = 64;                 // halves per 128-byte swizzle row
 constexpr int kStageBytes = 128 * 128;      // 128 rows x 128 bytes
-constexpr int kThreads = 320;
+constexpr int kEpilogueWarps = 16;          // 4 per TMEM lane quadrant
+constexpr int kThreads = 64 + 32 * kEpilogueWarps;
 constexpr int kEpilogueThreads = kThreads - 64;
 constexpr long long kWaitCycles = 4000000000LL;   // ~2 s at 2 GHz
 
@@ -291,11 +292,11 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         // ------------------------------------------------ epilogue
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
         const int row = q * 32 + lane;          // accumulator row = (probe, channel)
-        const int half = (warp - 2) >> 2;       // which half of the columns / texels
+        constexpr int kParts = kEpilogueWarps / 4;
+        const int part = (warp - 2) >> 2;       // which share of the column chunks / texels
         const int chunks = g.N / 16;
-        const int c_begin = half ? (chunks + 1) / 2 * 16 : 0;
-        const int c_end = half ? g.N : (chunks + 1) / 2 * 16;
-        const int t_begin = half ? g.T / 2 : 0, t_end = half ? g.T : g.T / 2;
+        const int c_begin = (chunks * part / kParts) * 16, c_end = (chunks * (part + 1) / kParts) * 16;
+        const int t_begin = g.T * part / kParts, t_end = g.T * (part + 1) / kParts;
         const luxgi_ddgi_uniform& u = g.u;
         const int XY = u.probe_counts[0] * u.probe_counts[1];
         const int n = g.side;
@@ -304,24 +305,44 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         const int probes_per_tile = 128 / g.rows_per_probe;
         int it = 0;
         bool ok = true;
+        // the previous values (hysteresis) of a 16-column chunk, loaded
+        // together: the first chunk's before the wait for the accumulator,
+        // each next chunk's while the current one is stored
+        auto load_prev = [&](int c0, int cx, int cy, int c, float* pv) {
+            int ty = c0 / n, tx = c0 - ty * n;
+#pragma unroll
+            for (int j = 0; j < 16; ++j, ++tx) {
+                if (tx == n) {
+                    tx = 0;
+                    ++ty;
+                }
+                pv[j] = (c0 + j < g.T)
+                            ? ld_atlas<AT>(g.prev, (size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2)) * g.nc + c)
+                            : 0.0f;
+            }
+        };
         for (int tile = blockIdx.x; tile < g.tiles; tile += gridDim.x, ++it) {
             const int acc = it & 1;
             const uint32_t use = uint32_t(it >> 1);
-            ok = mbar_wait(&tfull[acc], use & 1u, abort_flag, budget);
-            if (!ok) break;
-            tc_fence_after();
             const int p = tile * probes_per_tile + row / g.rows_per_probe;
             const int c = row % g.rows_per_probe;
             const bool live = p < g.P && (DIST || c < 3);
             const int cx = p % XY, cy = p / XY;
+            const bool hyst = !g.first && live;
+            float pv[16], pn[16];
+            if (hyst && c_begin < c_end) load_prev(c_begin, cx, cy, c, pv);
+            ok = mbar_wait(&tfull[acc], use & 1u, abort_flag, budget);
+            if (!ok) break;
+            tc_fence_after();
             for (int c0 = c_begin; c0 < c_end; c0 += 16) {
                 float v[16];
                 tmem_ld16(tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * g.N + c0), v);
                 if (!live) continue;
+                if (hyst && c0 + 16 < c_end) load_prev(c0 + 16, cx, cy, c, pn);
                 // texel (tx, ty) of column t, stepped along the chunk instead
                 // of divided out per column
                 int ty = c0 / n, tx = c0 - ty * n;
-#pragma unroll 4
+#pragma unroll
                 for (int j = 0; j < 16; ++j, ++tx) {
                     const int t = c0 + j;
                     if (t >= g.T) break;
@@ -331,9 +352,12 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                     }
                     float x = v[j] * __ldg(g.norm + t);
                     if (!DIST) x = __powf(x, ig);   // within the tensor path's 2e-3
-                    const size_t ti = (size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2)) * g.nc + c;
-                    if (!g.first) x = x * (1.0f - h) + ld_atlas<AT>(g.prev, ti) * h;
+                    if (!g.first) x = x * (1.0f - h) + pv[j] * h;
                     store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, tx, ty, c, x);
+                }
+                if (hyst) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) pv[j] = pn[j];
                 }
             }
             if (!DIST && p < g.P && c == 3) {
