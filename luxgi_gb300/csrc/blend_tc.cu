@@ -25,6 +25,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "atlas_io.cuh"
 #include "luxgi_internal.h"
 
 namespace luxgi {
@@ -132,19 +133,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-template <typename AT> __device__ __forceinline__ float ld_atlas(const void* p, size_t i);
-template <> __device__ __forceinline__ float ld_atlas<float>(const void* p, size_t i) {
-    return static_cast<const float*>(p)[i];
-}
-template <> __device__ __forceinline__ float ld_atlas<__half>(const void* p, size_t i) {
-    return __half2float(static_cast<const __half*>(p)[i]);
-}
-template <typename AT> __device__ __forceinline__ void st_atlas(void* p, size_t i, float v);
-template <> __device__ __forceinline__ void st_atlas<float>(void* p, size_t i, float v) { static_cast<float*>(p)[i] = v; }
-template <> __device__ __forceinline__ void st_atlas<__half>(void* p, size_t i, float v) {
-    static_cast<__half*>(p)[i] = __float2half_rn(v);
-}
-
 struct TcArgs {
     luxgi_ddgi_uniform u;
     const float* norm;        // [N] tensor-core normalisers (1 / (2 sum w_fp16))
@@ -161,23 +149,49 @@ struct TcArgs {
     int withhold;                         // test aid: block 0 skips the first A load of its first tile
 };
 
-// Writes one channel of interior texel (tx, ty) of cell (cx, cy) and its
-// border mirrors (BorderUpdate.glsl:136-156).
-template <typename AT>
-__device__ __forceinline__ void store_channel(void* atlas, int W, int nc, int n, int cx, int cy, int tx, int ty, int c,
-                                              float v) {
-    const int ox = cx * (n + 2) + 1, oy = cy * (n + 2) + 1;
-    const int X = tx + 1, Y = ty + 1;
-    auto put = [&](int x, int y) { st_atlas<AT>(atlas, (size_t(oy + y) * W + (ox + x)) * nc + c, v); };
-    put(X, Y);
-    if (Y == 1) put(n + 1 - X, 0);
-    if (Y == n) put(n + 1 - X, n + 1);
-    if (X == 1) put(0, n + 1 - Y);
-    if (X == n) put(n + 1, n + 1 - Y);
-    if (X == n && Y == n) put(0, 0);
-    if (X == 1 && Y == n) put(n + 1, 0);
-    if (X == n && Y == 1) put(0, n + 1);
-    if (X == 1 && Y == 1) put(n + 1, n + 1);
+// Lane-group transposes of the epilogue.  The lanes of one probe each hold
+// one channel over 16 accumulator columns (texels); afterwards each lane
+// holds every channel of its own texels, so that a texel is loaded (the
+// hysteresis history) and stored (with its border mirrors) in one vector
+// access instead of one scalar access per channel.
+// Irradiance, 4 lanes (r, g, b, zero row) and four 4x4 blocks: lane m ends
+// with texels 4k + m as v[4k .. 4k+3].
+__device__ __forceinline__ void transpose_quad(float* v, int lane) {
+    const bool b1 = (lane & 2) != 0, b0 = (lane & 1) != 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float* a = v + 4 * k;
+        // swap the off-diagonal 2x2 blocks with lane ^ 2 ...
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const float x = __shfl_xor_sync(0xffffffffu, b1 ? a[i] : a[i + 2], 2);
+            if (b1) a[i] = x;
+            else a[i + 2] = x;
+        }
+        // ... then transpose each 2x2 block with lane ^ 1
+        const float x0 = __shfl_xor_sync(0xffffffffu, b0 ? a[0] : a[1], 1);
+        const float x1 = __shfl_xor_sync(0xffffffffu, b0 ? a[2] : a[3], 1);
+        if (b0) {
+            a[0] = x0;
+            a[2] = x1;
+        } else {
+            a[1] = x0;
+            a[3] = x1;
+        }
+    }
+}
+
+// Distance, 2 lanes (d, d^2) and eight 2x2 blocks: lane m ends with texels
+// 2k + m as v[2k .. 2k+1].
+__device__ __forceinline__ void transpose_pair(float* v, int lane) {
+    const bool b0 = (lane & 1) != 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float* a = v + 2 * k;
+        const float x = __shfl_xor_sync(0xffffffffu, b0 ? a[0] : a[1], 1);
+        if (b0) a[0] = x;
+        else a[1] = x;
+    }
 }
 
 template <bool DIST, typename AT>
@@ -290,85 +304,88 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         }
     } else {
         // ------------------------------------------------ epilogue
+        constexpr int G = DIST ? 2 : 4;         // lanes (accumulator rows) of one probe = atlas channels
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
         const int row = q * 32 + lane;          // accumulator row = (probe, channel)
+        const int m = lane & (G - 1);           // after the transpose: texels G k + m of each chunk
         constexpr int kParts = kEpilogueWarps / 4;
-        const int part = (warp - 2) >> 2;       // which share of the column chunks / texels
+        const int part = (warp - 2) >> 2;       // which share of the column chunks
         const int chunks = g.N / 16;
         const int c_begin = (chunks * part / kParts) * 16, c_end = (chunks * (part + 1) / kParts) * 16;
-        const int t_begin = g.T * part / kParts, t_end = g.T * (part + 1) / kParts;
         const luxgi_ddgi_uniform& u = g.u;
         const int XY = u.probe_counts[0] * u.probe_counts[1];
         const int n = g.side;
         const float h = u.hysteresis;
         const float ig = 1.0f / u.ddgi_gamma;
-        const int probes_per_tile = 128 / g.rows_per_probe;
+        constexpr int probes_per_tile = 128 / G;
         int it = 0;
         bool ok = true;
-        // the previous values (hysteresis) of a 16-column chunk, loaded
-        // together: the first chunk's before the wait for the accumulator,
-        // each next chunk's while the current one is stored
-        auto load_prev = [&](int c0, int cx, int cy, int c, float* pv) {
-            int ty = c0 / n, tx = c0 - ty * n;
+        // the previous texels (hysteresis) of this lane in a 16-column chunk:
+        // the first chunk's before the wait for the accumulator, each next
+        // chunk's while the current one is stored
+        auto load_prev = [&](int c0, int cx, int cy, float* pv) {
+            int ty = (c0 + m) / n, tx = c0 + m - ty * n;
 #pragma unroll
-            for (int j = 0; j < 16; ++j, ++tx) {
-                if (tx == n) {
-                    tx = 0;
+            for (int k = 0; k < 16 / G; ++k) {
+                if (c0 + G * k + m < g.T) {
+                    AtlasIO<AT>::template ld_texel<G>(
+                        g.prev, size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2), pv + G * k);
+                }
+                tx += G;
+                while (tx >= n) {
+                    tx -= n;
                     ++ty;
                 }
-                pv[j] = (c0 + j < g.T)
-                            ? ld_atlas<AT>(g.prev, (size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2)) * g.nc + c)
-                            : 0.0f;
             }
         };
         for (int tile = blockIdx.x; tile < g.tiles; tile += gridDim.x, ++it) {
             const int acc = it & 1;
             const uint32_t use = uint32_t(it >> 1);
-            const int p = tile * probes_per_tile + row / g.rows_per_probe;
-            const int c = row % g.rows_per_probe;
-            const bool live = p < g.P && (DIST || c < 3);
+            const int p = tile * probes_per_tile + row / G;
+            const bool live = p < g.P;
             const int cx = p % XY, cy = p / XY;
             const bool hyst = !g.first && live;
             float pv[16], pn[16];
-            if (hyst && c_begin < c_end) load_prev(c_begin, cx, cy, c, pv);
+            if (hyst && c_begin < c_end) load_prev(c_begin, cx, cy, pv);
             ok = mbar_wait(&tfull[acc], use & 1u, abort_flag, budget);
             if (!ok) break;
             tc_fence_after();
             for (int c0 = c_begin; c0 < c_end; c0 += 16) {
                 float v[16];
                 tmem_ld16(tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * g.N + c0), v);
+                if (DIST) transpose_pair(v, lane);   // every lane: the shuffles span the warp
+                else transpose_quad(v, lane);
                 if (!live) continue;
-                if (hyst && c0 + 16 < c_end) load_prev(c0 + 16, cx, cy, c, pn);
-                // texel (tx, ty) of column t, stepped along the chunk instead
-                // of divided out per column
-                int ty = c0 / n, tx = c0 - ty * n;
+                if (hyst && c0 + 16 < c_end) load_prev(c0 + 16, cx, cy, pn);
+                int ty = (c0 + m) / n, tx = c0 + m - ty * n;
 #pragma unroll
-                for (int j = 0; j < 16; ++j, ++tx) {
-                    const int t = c0 + j;
-                    if (t >= g.T) break;
-                    if (tx == n) {
-                        tx = 0;
+                for (int k = 0; k < 16 / G; ++k) {
+                    const int t = c0 + G * k + m;
+                    if (t < g.T) {
+                        const float nt = __ldg(g.norm + t);
+                        float x[G];
+#pragma unroll
+                        for (int ch = 0; ch < G; ++ch) {
+                            if (!DIST && ch == 3) {
+                                x[ch] = 1.0f;   // alpha (ProbeUpdate.glsl:150)
+                                continue;
+                            }
+                            float y = v[G * k + ch] * nt;
+                            if (!DIST) y = __powf(y, ig);   // within the tensor path's 2e-3
+                            if (!g.first) y = y * (1.0f - h) + pv[G * k + ch] * h;
+                            x[ch] = y;
+                        }
+                        store_texel<AT, G>(g.out, g.W, n, cx, cy, tx, ty, x);
+                    }
+                    tx += G;
+                    while (tx >= n) {
+                        tx -= n;
                         ++ty;
                     }
-                    float x = v[j] * __ldg(g.norm + t);
-                    if (!DIST) x = __powf(x, ig);   // within the tensor path's 2e-3
-                    if (!g.first) x = x * (1.0f - h) + pv[j] * h;
-                    store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, tx, ty, c, x);
                 }
                 if (hyst) {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) pv[j] = pn[j];
-                }
-            }
-            if (!DIST && p < g.P && c == 3) {
-                // alpha = 1 (ProbeUpdate.glsl:150) for every texel of the cell
-                int ty = t_begin / n, tx = t_begin - ty * n;
-                for (int t = t_begin; t < t_end; ++t, ++tx) {
-                    if (tx == n) {
-                        tx = 0;
-                        ++ty;
-                    }
-                    store_channel<AT>(g.out, g.W, g.nc, n, cx, cy, tx, ty, 3, 1.0f);
                 }
             }
             tc_fence_before();
