@@ -22,7 +22,6 @@ using namespace luxgi;
 
 namespace luxgi {
 
-constexpr int kForkStreams = 4;   // parallel graph branches of the per-volume tensor-core blend
 
 static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
@@ -114,13 +113,15 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
     P.light_mode = vols[0]->desc.light_mode;
     P.sdf_format = vols[0]->sdf.format;
     P.tc = vols[0]->tc;
-    P.tc_bytes = tc_args_bytes();
+    P.tc_bytes = tc_job_bytes();
     P.off_trace = 0;
     P.off_blend = align16(sizeof(TraceParams) * n);
-    P.off_tc = P.off_blend + align16(sizeof(BlendParams) * n);
-    P.arg_bytes = P.off_tc + (P.tc ? align16(2 * P.tc_bytes * n) : 0);
+    // the tensor-core jobs hold tensor maps: 128-byte aligned
+    P.off_tc = (P.off_blend + align16(sizeof(BlendParams) * n) + 127) / 128 * 128;
+    P.arg_bytes = P.off_tc + (P.tc ? P.tc_bytes * n : 0);
     P.starts.assign(size_t(kNumStages) * (n + 1), 0);
     int64_t acc[kNumStages] = {};
+    std::vector<TcBlendParams> tps;
     if (P.tc) P.tcp.resize(n);
     P.budget = 1 << 30;
     for (int i = 0; i < n; ++i) {
@@ -153,8 +154,11 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
             TcBlendParams tp;
             volume_tc_params(v, tp);
             if (!tc_plan(tp, P.tcp[i])) return LUXGI_EUNSUPPORTED;
+            tps.push_back(tp);
         }
     }
+    // every volume's two blend kinds in one tensor-core launch
+    if (P.tc && !tc_launch_shape(tps.data(), P.tcp.data(), n, P.storage, P.tcl)) return LUXGI_EUNSUPPORTED;
     for (int s = 0; s < kNumStages; ++s) {
         P.starts[size_t(s) * (n + 1) + n] = int(acc[s]);
         P.blocks[s] = int(acc[s]);
@@ -199,40 +203,13 @@ void plan_fill(const Plan& P, const float* rots, uint8_t* host) {
         if (P.tc) {
             TcBlendParams t;
             volume_tc_params(v, t);
-            tc_fill_args(t, host + P.off_tc + size_t(i) * 2 * P.tc_bytes);
+            tc_fill_jobs(t, P.tcp[i], host + P.off_tc + size_t(i) * P.tc_bytes);
         }
     }
 }
 
-struct Fork {
-    cudaStream_t aux[kForkStreams] = {};
-    cudaEvent_t fork = nullptr;
-    cudaEvent_t join[kForkStreams] = {};
-};
-
-void fork_destroy(Fork& f) {
-    for (int i = 0; i < kForkStreams; ++i) {
-        if (f.aux[i]) cudaStreamDestroy(f.aux[i]);
-        if (f.join[i]) cudaEventDestroy(f.join[i]);
-        f.aux[i] = nullptr;
-        f.join[i] = nullptr;
-    }
-    if (f.fork) cudaEventDestroy(f.fork);
-    f.fork = nullptr;
-}
-
-cudaError_t fork_create(Fork& f) {
-    cudaError_t e = cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming);
-    for (int i = 0; i < kForkStreams && e == cudaSuccess; ++i) {
-        e = cudaStreamCreateWithFlags(&f.aux[i], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join[i], cudaEventDisableTiming);
-    }
-    return e;
-}
-
-// Launches one frame.  With `fork`, the per-volume tensor-core blends go
-// to parallel streams (graph branches under capture) and join back.
-cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cudaStream_t st, const Fork* fork) {
+// Launches one frame.
+cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cudaStream_t st) {
     const TraceParams* tp = reinterpret_cast<const TraceParams*>(d_args + P.off_trace);
     const BlendParams* bp = reinterpret_cast<const BlendParams*>(d_args + P.off_blend);
     const int n = P.n, n1 = P.n + 1;
@@ -257,24 +234,8 @@ cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cud
     if (!P.tc)
         return launch_blend_batch(bp, d_starts + kBlendI * n1, P.blocks[kBlendI], P.smem_i, d_starts + kBlendD * n1,
                                   P.blocks[kBlendD], P.smem_d, n, P.t.blend_probes, P.storage, st);
-    const int branches = fork ? std::min(kForkStreams, n) : 0;
-    if (branches > 1) {
-        e = cudaEventRecord(fork->fork, st);
-        for (int j = 0; j < branches && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(fork->aux[j], fork->fork, 0);
-    }
-    for (int i = 0; i < n && e == cudaSuccess; ++i) {
-        cudaStream_t s = branches > 1 ? fork->aux[i % branches] : st;
-        e = launch_tc_blend_dyn(P.tcp[i], P.storage, d_args + P.off_tc + size_t(i) * 2 * P.tc_bytes, s);
-    }
-    if (branches > 1) {
-        // join every branch (also after an error, so a capture can end)
-        for (int j = 0; j < branches; ++j) {
-            cudaError_t e2 = cudaEventRecord(fork->join[j], fork->aux[j]);
-            if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(st, fork->join[j], 0);
-            if (e == cudaSuccess) e = e2;
-        }
-    }
-    return e;
+    // every volume's irradiance and distance blends: one persistent launch
+    return launch_tc_blend_jobs(P.tcl, P.storage, d_args + P.off_tc, st);
 }
 
 int prepare_all(const Plan& P, cudaStream_t st) {
@@ -320,7 +281,7 @@ int run_group(luxgi_ddgi_volume* const* vols, int n, const float* rots, cudaStre
     std::memcpy(host.data() + P.arg_bytes, P.starts.data(), P.starts.size() * sizeof(int));
     // pageable source: the copy has taken the bytes when the call returns
     e = cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = plan_launch(P, dev, reinterpret_cast<const int*>(dev + P.arg_bytes), st, nullptr);
+    if (e == cudaSuccess) e = plan_launch(P, dev, reinterpret_cast<const int*>(dev + P.arg_bytes), st);
     const cudaError_t e2 = cudaFreeAsync(dev, st);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return cuda_status(e);
@@ -339,7 +300,6 @@ struct luxgi_ddgi_batch {
     void* dev_q = nullptr;                   // march compaction queues
     size_t dev_args_cap = 0, dev_starts_cap = 0, host_cap = 0, dev_q_cap = 0;
     cudaStream_t cap = nullptr;              // capture stream
-    Fork fork;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     uint64_t kernels_per_frame = 0;
     cudaEvent_t done[2] = {nullptr, nullptr};
@@ -380,7 +340,6 @@ void release(luxgi_ddgi_batch* b) {
     if (b->dev_starts) cudaFree(b->dev_starts);
     if (b->dev_q) cudaFree(b->dev_q);
     if (b->cap) cudaStreamDestroy(b->cap);
-    fork_destroy(b->fork);
 }
 
 // (Re)plans for tuning t: variants applied to the volumes, buffers grown,
@@ -445,7 +404,7 @@ int capture(luxgi_ddgi_batch* b, int k) {
     cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_status(e);
     cudaError_t el = cudaMemcpyAsync(b->dev_args, b->host[k], P.arg_bytes, cudaMemcpyHostToDevice, b->cap);
-    if (el == cudaSuccess) el = plan_launch(P, b->dev_args, b->dev_starts, b->cap, &b->fork);
+    if (el == cudaSuccess) el = plan_launch(P, b->dev_args, b->dev_starts, b->cap);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(b->cap, &g);
     const uint64_t captured = luxgi_launch_count() - before;
@@ -490,7 +449,7 @@ int batch_frame(luxgi_ddgi_batch* b, const float* rots, cudaStream_t st) {
         if (e == cudaSuccess) note_launch(int(b->kernels_per_frame));
     } else {
         e = cudaMemcpyAsync(b->dev_args, b->host[k], P.arg_bytes, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = plan_launch(P, b->dev_args, b->dev_starts, st, nullptr);
+        if (e == cudaSuccess) e = plan_launch(P, b->dev_args, b->dev_starts, st);
     }
     if (e == cudaSuccess) e = cudaEventRecord(b->done[k], st);
     if (e != cudaSuccess) return cuda_status(e);
@@ -630,7 +589,6 @@ int luxgi_ddgi_batch_create(luxgi_ddgi_volume* const* vols, int n, const luxgi_d
     cudaGetDevice(&b->device);
     b->plan.vols.assign(vols, vols + n);
     cudaError_t e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = fork_create(b->fork);
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&b->done[k], cudaEventDisableTiming);
     s = e == cudaSuccess ? replan(b, t) : cuda_status(e);
     if (s != LUXGI_OK) {

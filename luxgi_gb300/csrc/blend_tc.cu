@@ -9,7 +9,13 @@
 //                 (FP16 hi, FP16 residual) so the sums keep ~FP32 accuracy
 // B = weights W[t][r] in FP16, K-major, N = texels padded to 16; for the
 //     distance the same B block multiplies the hi and the lo half of A.
-// D accumulates in TMEM (FP32).  One CTA per SM, persistent over M tiles:
+// D accumulates in TMEM (FP32).  A launch runs a list of jobs, a job being
+// one blend kind of one volume (its two operand maps and its arguments):
+// both kinds of one volume, or every volume of a batch.  The jobs' 128-row
+// tiles form one list; one CTA per SM, persistent over a contiguous range
+// of it (ranges split by the bytes a tile moves), loads a job's B into
+// shared memory once and reloads it where its range crosses into the next
+// job:
 //   warp 0      TMA producer (cp.async.bulk.tensor, 128B swizzle, 16 KB stages)
 //   warp 1      TMEM allocator + single-thread tcgen05.mma issuer
 //   warps 2..17 epilogue: tcgen05.ld, normalise, gamma, hysteresis, store
@@ -17,9 +23,12 @@
 //               column chunks) with the border mirrors
 // The accumulator is double buffered in TMEM so the epilogue of one tile
 // overlaps the MMAs of the next.  Every mbarrier wait is bounded by a clock
-// budget; on expiry the kernel raises *status, stops issuing work, drains
-// what it issued and frees its TMEM.
+// budget; on expiry the kernel raises the status word of every job it had
+// tiles of, stops issuing work, drains what it issued and frees its TMEM.
+#include <algorithm>
+#include <climits>
 #include <cstring>
+#include <vector>
 
 #include <cuda.h>
 #include <cuda_fp16.h>
@@ -139,15 +148,36 @@ struct TcArgs {
     const void* prev;
     void* out;
     uint32_t* status;
+    int dist;                             // 1: distance kind, 0: irradiance
     int first, P, R, N, T, side, W, nc;   // nc: atlas channels (4 irradiance, 2 distance)
     int rows_per_probe;                   // 4 irradiance, 2 distance
     int kb_a;                             // K blocks of A per tile
     int kb_b;                             // K blocks of B (ceil(R / 64))
     int lo_offset;                        // column of the lo half in A (distance), 0 otherwise
-    int tiles;
+    int tiles;                            // 128-row tiles of this job
+    int tile0;                            // its first tile in the launch's tile list
     long long wait_cycles;                // bound of every mbarrier wait, SM clock cycles
     int withhold;                         // test aid: block 0 skips the first A load of its first tile
 };
+
+// One blend kind of one volume: its operand maps and its arguments.
+struct TcJob {
+    CUtensorMap ma;   // A, the per-ray operands: 64 x 128 boxes
+    CUtensorMap mb;   // B, the weights: 64 x N boxes
+    TcArgs g;
+};
+static_assert(alignof(TcJob) == 128 && sizeof(TcJob) % 128 == 0, "tensor maps are 128-byte aligned");
+
+// Kernel parameters: the jobs (in the parameter space for one volume, in
+// device memory for a batch) and the split of the tile list between CTAs.
+struct TcLaunchArgs {
+    TcJob local[2];
+    const TcJob* jobs;        // null: `local`
+    long long wait_cycles;
+    int njobs, nmax, b_bytes;
+    int split[kTcMaxGrid + 1];   // CTA b takes tiles [split[b], split[b + 1])
+};
+static_assert(sizeof(TcLaunchArgs) <= 4096, "kernel parameter block");
 
 // Lane-group transposes of the epilogue.  The lanes of one probe each hold
 // one channel over 16 accumulator columns (texels); afterwards each lane
@@ -194,27 +224,127 @@ __device__ __forceinline__ void transpose_pair(float* v, int lane) {
     }
 }
 
+
+// The job holding tile t, from job j onwards (jobs in tile order).
+__device__ __forceinline__ int job_from(const TcJob* J, int njobs, int j, int t) {
+    while (j + 1 < njobs && t >= J[j + 1].g.tile0) ++j;
+    return j;
+}
+
+// Epilogue of one tile for the 16 epilogue warps: tcgen05.ld, normalise,
+// gamma, hysteresis, store with the border mirrors (four warps per TMEM lane
+// quadrant, each a quarter of the column chunks).  False when the wait for
+// the accumulator gave up.
 template <bool DIST, typename AT>
-__device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CUtensorMap& map_b, const TcArgs& g) {
+__device__ __forceinline__ bool epilogue_tile(const TcArgs& g, int lt, uint32_t taddr, int q, int part, int lane,
+                                              uint64_t* tfull, uint32_t parity, volatile int* abort_flag,
+                                              long long budget) {
+    constexpr int G = DIST ? 2 : 4;         // lanes (accumulator rows) of one probe = atlas channels
+    constexpr int kParts = kEpilogueWarps / 4;
+    // the job's fields in registers (the atlas stores may alias the job list)
+    const int T = g.T, W = g.W, n = g.side;
+    const bool first = g.first != 0;
+    const float* norm = g.norm;
+    const void* prev = g.prev;
+    void* out = g.out;
+    const int XY = g.u.probe_counts[0] * g.u.probe_counts[1];
+    const float h = g.u.hysteresis;
+    const float ig = 1.0f / g.u.ddgi_gamma;
+    const int row = q * 32 + lane;          // accumulator row = (probe, channel)
+    const int m = lane & (G - 1);           // after the transpose: texels G k + m of each chunk
+    const int chunks = g.N / 16;
+    const int c_begin = (chunks * part / kParts) * 16, c_end = (chunks * (part + 1) / kParts) * 16;
+    const int p = lt * (128 / G) + row / G;
+    const bool live = p < g.P;
+    const int cx = p % XY, cy = p / XY;
+    const bool hyst = !first && live;
+    // the previous texels (hysteresis) of this lane in a 16-column chunk,
+    // the first chunk's before the wait for the accumulator (loading the
+    // next chunk's during the stores as well needs 16 more registers: the
+    // spills at the 96 a thread that 576 threads leave cost more)
+    auto load_prev = [&](int c0, float* pv) {
+        int ty = (c0 + m) / n, tx = c0 + m - ty * n;
+#pragma unroll
+        for (int k = 0; k < 16 / G; ++k) {
+            if (c0 + G * k + m < T) {
+                AtlasIO<AT>::template ld_texel<G>(prev, size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2),
+                                                  pv + G * k);
+            }
+            tx += G;
+            while (tx >= n) {
+                tx -= n;
+                ++ty;
+            }
+        }
+    };
+    float pv[16];
+    if (hyst && c_begin < c_end) load_prev(c_begin, pv);
+    if (!mbar_wait(tfull, parity, abort_flag, budget)) return false;
+    tc_fence_after();
+    for (int c0 = c_begin; c0 < c_end; c0 += 16) {
+        // the next chunks' history, in flight during the accumulator load and the transpose
+        if (hyst && c0 > c_begin) load_prev(c0, pv);
+        float v[16];
+        tmem_ld16(taddr + uint32_t(c0), v);
+        if (DIST) transpose_pair(v, lane);   // every lane: the shuffles span the warp
+        else transpose_quad(v, lane);
+        if (!live) continue;
+        int ty = (c0 + m) / n, tx = c0 + m - ty * n;
+#pragma unroll
+        for (int k = 0; k < 16 / G; ++k) {
+            const int t = c0 + G * k + m;
+            if (t < T) {
+                const float nt = __ldg(norm + t);
+                float x[G];
+#pragma unroll
+                for (int ch = 0; ch < G; ++ch) {
+                    if (!DIST && ch == 3) {
+                        x[ch] = 1.0f;   // alpha (ProbeUpdate.glsl:150)
+                        continue;
+                    }
+                    float y = v[G * k + ch] * nt;
+                    if (!DIST) y = __powf(y, ig);   // within the tensor path's 2e-3
+                    if (!first) y = y * (1.0f - h) + pv[G * k + ch] * h;
+                    x[ch] = y;
+                }
+                store_texel<AT, G>(out, W, n, cx, cy, tx, ty, x);
+            }
+            tx += G;
+            while (tx >= n) {
+                tx -= n;
+                ++ty;
+            }
+        }
+    }
+    return true;
+}
+
+template <typename AT>
+__global__ void __launch_bounds__(kThreads, 1) tc_blend_kernel(const __grid_constant__ TcLaunchArgs L) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    // 1024-byte aligned carve-out: B blocks, A stages, then barriers
+    const TcJob* J = L.jobs ? L.jobs : L.local;
+    const int njobs = L.njobs;
+    // 1024-byte aligned carve-out: B blocks (the widest job's), A stages, then barriers
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const int b_block_bytes = g.N * 128;
     uint8_t* smem_b = base;
-    uint8_t* smem_a = smem_b + g.kb_b * b_block_bytes;
+    uint8_t* smem_a = smem_b + L.b_bytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem_a + kStages * kStageBytes);
     uint64_t* full = bars;                       // [kStages]
     uint64_t* empty = bars + kStages;            // [kStages]
-    uint64_t* bfull = bars + 2 * kStages;        // [1]
-    uint64_t* tfull = bars + 2 * kStages + 1;    // [2]
-    uint64_t* tempty = bars + 2 * kStages + 3;   // [2]
-    uint64_t* mdrain = bars + 2 * kStages + 5;   // [1] MMAs issued before an abort
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 6);
+    uint64_t* bfull = bars + 2 * kStages;        // [1] B loaded
+    uint64_t* bempty = bars + 2 * kStages + 1;   // [1] the multiplies reading B done
+    uint64_t* tfull = bars + 2 * kStages + 2;    // [2]
+    uint64_t* tempty = bars + 2 * kStages + 4;   // [2]
+    uint64_t* mdrain = bars + 2 * kStages + 6;   // [1] MMAs issued before an abort
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 7);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    const long long budget = g.wait_cycles > 0 ? g.wait_cycles : kWaitCycles;
+    const long long budget = L.wait_cycles > 0 ? L.wait_cycles : kWaitCycles;
+    const int t_begin = L.split[blockIdx.x], t_end = L.split[blockIdx.x + 1];
+    const int j_begin = job_from(J, njobs, 0, t_begin);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const uint32_t tmem_cols = (2 * g.N <= 32) ? 32 : (2 * g.N <= 64) ? 64 : (2 * g.N <= 128) ? 128 : (2 * g.N <= 256) ? 256 : 512;
+    const int cols = 2 * L.nmax;
+    const uint32_t tmem_cols = (cols <= 32) ? 32 : (cols <= 64) ? 64 : (cols <= 128) ? 128 : (cols <= 256) ? 256 : 512;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -222,6 +352,7 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
             mbar_init(&empty[s], 1);
         }
         mbar_init(bfull, 1);
+        mbar_init(bempty, 1);
         mbar_init(&tfull[0], 1);
         mbar_init(&tfull[1], 1);
         mbar_init(&tempty[0], kEpilogueThreads);
@@ -239,24 +370,40 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
-    const uint32_t idesc = idesc_f16(128, g.N);
-    // phase of the last A load issued into each stage (producer thread)
+    // phase of the last A load issued into each stage, and of the last B
+    // load (producer thread)
     uint32_t pending[kStages];
     for (int s = 0; s < kStages; ++s) pending[s] = 0xFFFFFFFFu;
+    uint32_t b_pending = 0xFFFFFFFFu;
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
         if (lane == 0) {
-            mbar_expect_tx(bfull, uint32_t(g.kb_b * b_block_bytes));
-            for (int kb = 0; kb < g.kb_b; ++kb) tma_load_2d(smem_b + kb * b_block_bytes, &map_b, bfull, kb * kKBlock, 0);
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
-            for (int tile = blockIdx.x; tile < g.tiles && ok; tile += gridDim.x) {
+            int j = j_begin, jb = -1, nb = 0;
+            for (int t = t_begin; t < t_end && ok; ++t) {
+                j = job_from(J, njobs, j, t);
+                const TcArgs& g = J[j].g;
+                if (j != jb) {
+                    // the job's weights, once the multiplies of the last job are done with B
+                    if (nb > 0) {
+                        ok = mbar_wait(bempty, uint32_t(nb - 1) & 1u, abort_flag, budget);
+                        if (!ok) break;
+                    }
+                    const int bb = g.N * 128;
+                    mbar_expect_tx(bfull, uint32_t(g.kb_b * bb));
+                    for (int kb = 0; kb < g.kb_b; ++kb) tma_load_2d(smem_b + kb * bb, &J[j].mb, bfull, kb * kKBlock, 0);
+                    b_pending = uint32_t(nb) & 1u;
+                    ++nb;
+                    jb = j;
+                }
+                const int lt = t - g.tile0;
                 for (int kb = 0; kb < g.kb_a && ok; ++kb) {
                     ok = mbar_wait(&empty[stage], phase ^ 1u, abort_flag, budget);
                     if (!ok) break;
-                    if (g.withhold && blockIdx.x == 0 && tile == 0 && kb == 0) {
+                    if (g.withhold && blockIdx.x == 0 && t == t_begin && kb == 0) {
                         // test aid: this stage's load is never issued, so the
                         // MMA issuer's bounded wait on it runs out
                         if (++stage == kStages) { stage = 0; phase ^= 1u; }
@@ -264,7 +411,7 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                     }
                     const int x = (kb < g.kb_b) ? kb * kKBlock : g.lo_offset + (kb - g.kb_b) * kKBlock;
                     mbar_expect_tx(&full[stage], kStageBytes);
-                    tma_load_2d(smem_a + stage * kStageBytes, &map_a, &full[stage], x, tile * 128);
+                    tma_load_2d(smem_a + stage * kStageBytes, &J[j].ma, &full[stage], x, lt * 128);
                     pending[stage] = phase;
                     if (++stage == kStages) { stage = 0; phase ^= 1u; }
                 }
@@ -273,24 +420,35 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            bool ok = mbar_wait(bfull, 0, abort_flag, budget);
             int stage = 0;
             uint32_t phase = 0;
+            bool ok = true;
             int it = 0;
-            for (int tile = blockIdx.x; tile < g.tiles && ok; tile += gridDim.x, ++it) {
+            int j = j_begin, jb = -1, nb = 0;
+            for (int t = t_begin; t < t_end && ok; ++t, ++it) {
+                j = job_from(J, njobs, j, t);
+                const TcArgs& g = J[j].g;
+                if (j != jb) {
+                    ok = mbar_wait(bfull, uint32_t(nb) & 1u, abort_flag, budget);
+                    if (!ok) break;
+                    ++nb;
+                    jb = j;
+                }
                 const int acc = it & 1;
                 const uint32_t use = uint32_t(it >> 1);
                 ok = mbar_wait(&tempty[acc], (use & 1u) ^ 1u, abort_flag, budget);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t d_tmem = tmem_base + uint32_t(acc * g.N);
+                const uint32_t d_tmem = tmem_base + uint32_t(acc * L.nmax);
+                const uint32_t idesc = idesc_f16(128, g.N);
+                const int bb = g.N * 128;
                 for (int kb = 0; kb < g.kb_a && ok; ++kb) {
                     ok = mbar_wait(&full[stage], phase, abort_flag, budget);
                     if (!ok) break;
                     tc_fence_after();
                     const int bk = (kb < g.kb_b) ? kb : kb - g.kb_b;
                     const uint32_t a_addr = smem_u32(smem_a + stage * kStageBytes);
-                    const uint32_t b_addr = smem_u32(smem_b + bk * b_block_bytes);
+                    const uint32_t b_addr = smem_u32(smem_b + bk * bb);
 #pragma unroll
                     for (int k = 0; k < kKBlock / 16; ++k) {
                         mma_f16(d_tmem, smem_desc(a_addr + k * 32), smem_desc(b_addr + k * 32), idesc,
@@ -299,99 +457,32 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                     mma_commit(&empty[stage]);
                     if (++stage == kStages) { stage = 0; phase ^= 1u; }
                 }
-                if (ok) mma_commit(&tfull[acc]);
+                if (!ok) break;
+                mma_commit(&tfull[acc]);
+                // B is free for the next job once this job's last multiplies are done
+                if (t + 1 < t_end && t + 1 >= g.tile0 + g.tiles) mma_commit(bempty);
             }
         }
     } else {
         // ------------------------------------------------ epilogue
-        constexpr int G = DIST ? 2 : 4;         // lanes (accumulator rows) of one probe = atlas channels
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
-        const int row = q * 32 + lane;          // accumulator row = (probe, channel)
-        const int m = lane & (G - 1);           // after the transpose: texels G k + m of each chunk
-        constexpr int kParts = kEpilogueWarps / 4;
         const int part = (warp - 2) >> 2;       // which share of the column chunks
-        const int chunks = g.N / 16;
-        const int c_begin = (chunks * part / kParts) * 16, c_end = (chunks * (part + 1) / kParts) * 16;
-        const luxgi_ddgi_uniform& u = g.u;
-        const int XY = u.probe_counts[0] * u.probe_counts[1];
-        const int n = g.side;
-        const float h = u.hysteresis;
-        const float ig = 1.0f / u.ddgi_gamma;
-        constexpr int probes_per_tile = 128 / G;
         int it = 0;
-        bool ok = true;
-        // the previous texels (hysteresis) of this lane in a 16-column chunk:
-        // the first chunk's before the wait for the accumulator, each next
-        // chunk's while the current one is stored
-        auto load_prev = [&](int c0, int cx, int cy, float* pv) {
-            int ty = (c0 + m) / n, tx = c0 + m - ty * n;
-#pragma unroll
-            for (int k = 0; k < 16 / G; ++k) {
-                if (c0 + G * k + m < g.T) {
-                    AtlasIO<AT>::template ld_texel<G>(
-                        g.prev, size_t(cy * (n + 2) + ty + 2) * g.W + (cx * (n + 2) + tx + 2), pv + G * k);
-                }
-                tx += G;
-                while (tx >= n) {
-                    tx -= n;
-                    ++ty;
-                }
-            }
-        };
-        for (int tile = blockIdx.x; tile < g.tiles; tile += gridDim.x, ++it) {
+        int j = j_begin;
+        for (int t = t_begin; t < t_end; ++t, ++it) {
+            j = job_from(J, njobs, j, t);
+            const TcArgs& g = J[j].g;
             const int acc = it & 1;
-            const uint32_t use = uint32_t(it >> 1);
-            const int p = tile * probes_per_tile + row / G;
-            const bool live = p < g.P;
-            const int cx = p % XY, cy = p / XY;
-            const bool hyst = !g.first && live;
-            float pv[16], pn[16];
-            if (hyst && c_begin < c_end) load_prev(c_begin, cx, cy, pv);
-            ok = mbar_wait(&tfull[acc], use & 1u, abort_flag, budget);
+            const uint32_t parity = uint32_t(it >> 1) & 1u;
+            const uint32_t taddr = tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * L.nmax);
+            const bool ok = g.dist ? epilogue_tile<true, AT>(g, t - g.tile0, taddr, q, part, lane, &tfull[acc], parity,
+                                                             abort_flag, budget)
+                                   : epilogue_tile<false, AT>(g, t - g.tile0, taddr, q, part, lane, &tfull[acc], parity,
+                                                              abort_flag, budget);
             if (!ok) break;
-            tc_fence_after();
-            for (int c0 = c_begin; c0 < c_end; c0 += 16) {
-                float v[16];
-                tmem_ld16(tmem_base + (uint32_t(q * 32) << 16) + uint32_t(acc * g.N + c0), v);
-                if (DIST) transpose_pair(v, lane);   // every lane: the shuffles span the warp
-                else transpose_quad(v, lane);
-                if (!live) continue;
-                if (hyst && c0 + 16 < c_end) load_prev(c0 + 16, cx, cy, pn);
-                int ty = (c0 + m) / n, tx = c0 + m - ty * n;
-#pragma unroll
-                for (int k = 0; k < 16 / G; ++k) {
-                    const int t = c0 + G * k + m;
-                    if (t < g.T) {
-                        const float nt = __ldg(g.norm + t);
-                        float x[G];
-#pragma unroll
-                        for (int ch = 0; ch < G; ++ch) {
-                            if (!DIST && ch == 3) {
-                                x[ch] = 1.0f;   // alpha (ProbeUpdate.glsl:150)
-                                continue;
-                            }
-                            float y = v[G * k + ch] * nt;
-                            if (!DIST) y = __powf(y, ig);   // within the tensor path's 2e-3
-                            if (!g.first) y = y * (1.0f - h) + pv[G * k + ch] * h;
-                            x[ch] = y;
-                        }
-                        store_texel<AT, G>(g.out, g.W, n, cx, cy, tx, ty, x);
-                    }
-                    tx += G;
-                    while (tx >= n) {
-                        tx -= n;
-                        ++ty;
-                    }
-                }
-                if (hyst) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) pv[j] = pn[j];
-                }
-            }
             tc_fence_before();
             mbar_arrive(&tempty[acc]);
         }
-        (void)ok;
     }
     tc_fence_before();
     __syncthreads();
@@ -405,8 +496,10 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
                 const long long t0 = clock64();
                 while (!mbar_try_wait(&full[s], pending[s]) && clock64() - t0 < budget) {}
             }
-            const long long t0 = clock64();
-            while (!mbar_try_wait(bfull, 0) && clock64() - t0 < budget) {}
+            if (b_pending != 0xFFFFFFFFu) {
+                const long long t0 = clock64();
+                while (!mbar_try_wait(bfull, b_pending) && clock64() - t0 < budget) {}
+            }
         } else if (warp == 1 && lane == 0) {
             // one commit tracks every multiply this thread issued
             mma_commit(mdrain);
@@ -420,23 +513,11 @@ __device__ __forceinline__ void tc_blend_body(const CUtensorMap& map_a, const CU
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(tmem_cols));
     }
-    if (threadIdx.x == 0 && *abort_flag) atomicOr(g.status, 1u);
-}
-
-template <bool DIST, typename AT>
-__global__ void __launch_bounds__(kThreads, 1)
-tc_blend_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs g) {
-    tc_blend_body<DIST, AT>(map_a, map_b, g);
-}
-
-// Same kernel with the per-frame arguments (ping-pong atlases, first-frame
-// flag) read from device memory, so that a captured graph replays it frame
-// after frame while the host rewrites the arguments.
-template <bool DIST, typename AT>
-__global__ void __launch_bounds__(kThreads, 1)
-tc_blend_dyn_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                    const TcArgs* __restrict__ gd) {
-    tc_blend_body<DIST, AT>(map_a, map_b, *gd);
+    if (threadIdx.x == 0 && *abort_flag && t_begin < t_end) {
+        // every job this CTA had tiles of
+        const int j_end = job_from(J, njobs, j_begin, t_end - 1);
+        for (int j = j_begin; j <= j_end; ++j) atomicOr(J[j].g.status, 1u);
+    }
 }
 
 // ------------------------------------------------------------ host side
@@ -484,6 +565,7 @@ void fill_args(const TcBlendParams& p, TcArgs& g) {
     const luxgi_ddgi_uniform& u = p.u;
     std::memset(&g, 0, sizeof(g));
     g.u = u;
+    g.dist = DIST ? 1 : 0;
     g.first = p.first;
     g.P = p.P;
     g.R = p.R;
@@ -506,9 +588,9 @@ void fill_args(const TcBlendParams& p, TcArgs& g) {
     g.withhold = p.withhold;
 }
 
-// Tensor maps, shared memory and grid of one blend kind of one volume.
+// Tensor maps of one blend kind of one volume.
 template <bool DIST>
-bool plan_kind(const TcBlendParams& p, CUtensorMap& ma, CUtensorMap& mb, size_t& smem, int& grid) {
+bool make_maps(const TcBlendParams& p, CUtensorMap& ma, CUtensorMap& mb) {
     TcArgs g;
     fill_args<DIST>(p, g);
     const int64_t rows = int64_t(p.P) * g.rows_per_probe;
@@ -516,40 +598,46 @@ bool plan_kind(const TcBlendParams& p, CUtensorMap& ma, CUtensorMap& mb, size_t&
     if (!make_map(&ma, DIST ? static_cast<const void*>(p.a_dist) : static_cast<const void*>(p.a_irr), a_inner,
                   uint64_t(rows), kKBlock, 128))
         return false;
-    if (!make_map(&mb, DIST ? static_cast<const void*>(p.w_dist) : static_cast<const void*>(p.w_irr), uint64_t(p.R),
-                  uint64_t(g.N), kKBlock, uint32_t(g.N)))
-        return false;
-    smem = 1024 + size_t(g.kb_b) * g.N * 128 + size_t(kStages) * kStageBytes + 256;
-    grid = g.tiles < num_sms() ? g.tiles : num_sms();
-    return true;
+    return make_map(&mb, DIST ? static_cast<const void*>(p.w_dist) : static_cast<const void*>(p.w_irr),
+                    uint64_t(p.R), uint64_t(g.N), kKBlock, uint32_t(g.N));
 }
 
-template <bool DIST, typename AT>
-cudaError_t launch_one(const TcBlendParams& p, cudaStream_t st) {
-    TcArgs g;
-    fill_args<DIST>(p, g);
-    CUtensorMap ma, mb;
-    size_t smem = 0;
-    int grid = 0;
-    if (!plan_kind<DIST>(p, ma, mb, smem, grid)) return cudaErrorNotSupported;
-    auto kern = tc_blend_kernel<DIST, AT>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+void fill_job(const TcBlendParams& p, const TcPlan& plan, int k, TcJob& J) {
+    std::memset(&J, 0, sizeof(J));
+    J.ma = plan.ma[k];
+    J.mb = plan.mb[k];
+    if (k) fill_args<true>(p, J.g);
+    else fill_args<false>(p, J.g);
+    J.g.tile0 = plan.tile0[k];
+}
+
+template <typename AT>
+cudaError_t launch_kernel(const TcLaunchArgs& a, const TcLaunch& L, cudaStream_t st) {
+    auto kern = tc_blend_kernel<AT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.smem));
     if (e != cudaSuccess) return e;
-    kern<<<grid, kThreads, smem, st>>>(ma, mb, g);
+    kern<<<L.grid, kThreads, L.smem, st>>>(a);
     note_launch();
     return cudaGetLastError();
 }
 
-template <bool DIST, typename AT>
-cudaError_t launch_dyn(const TcPlan& plan, const void* d_args, cudaStream_t st) {
-    const int k = DIST ? 1 : 0;
-    auto kern = tc_blend_dyn_kernel<DIST, AT>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(plan.smem[k]));
-    if (e != cudaSuccess) return e;
-    kern<<<plan.grid[k], kThreads, plan.smem[k], st>>>(plan.ma[k], plan.mb[k],
-                                                      static_cast<const TcArgs*>(d_args) + k);
-    note_launch();
-    return cudaGetLastError();
+// One launch over the jobs: `local` (two jobs, passed as parameters) or
+// d_jobs (device memory).
+cudaError_t launch_args(const TcLaunch& L, int storage, const TcJob* local, const void* d_jobs, cudaStream_t st) {
+    if (L.grid <= 0) return cudaSuccess;
+    TcLaunchArgs a;
+    std::memset(&a, 0, sizeof(a));
+    if (local) {
+        a.local[0] = local[0];
+        a.local[1] = local[1];
+    }
+    a.jobs = local ? nullptr : static_cast<const TcJob*>(d_jobs);
+    a.wait_cycles = L.wait_cycles;
+    a.njobs = L.njobs;
+    a.nmax = L.nmax;
+    a.b_bytes = int(L.b_bytes);
+    std::memcpy(a.split, L.split, sizeof(a.split));
+    return storage == LUXGI_STORAGE_FP16 ? launch_kernel<__half>(a, L, st) : launch_kernel<float>(a, L, st);
 }
 
 }  // namespace
@@ -566,44 +654,89 @@ bool tc_blend_supported(const luxgi_ddgi_uniform& u) {
     return smem <= 227 * 1024 && encode_fn() != nullptr;
 }
 
-size_t tc_args_bytes() { return sizeof(TcArgs); }
-
-void tc_fill_args(const TcBlendParams& p, void* out) {
-    TcArgs* g = static_cast<TcArgs*>(out);
-    fill_args<false>(p, g[0]);
-    fill_args<true>(p, g[1]);
-}
-
 bool tc_plan(const TcBlendParams& p, TcPlan& plan) {
     if (p.P <= 0 || !tc_blend_supported(p.u)) return false;
-    return plan_kind<false>(p, plan.ma[0], plan.mb[0], plan.smem[0], plan.grid[0]) &&
-           plan_kind<true>(p, plan.ma[1], plan.mb[1], plan.smem[1], plan.grid[1]);
+    plan.tile0[0] = plan.tile0[1] = 0;
+    return make_maps<false>(p, plan.ma[0], plan.mb[0]) && make_maps<true>(p, plan.ma[1], plan.mb[1]);
 }
 
-cudaError_t launch_tc_blend_dyn(const TcPlan& plan, int storage, const void* d_args, cudaStream_t st) {
-    cudaError_t e;
-    if (storage == LUXGI_STORAGE_FP16) {
-        e = launch_dyn<false, __half>(plan, d_args, st);
-        if (e == cudaSuccess) e = launch_dyn<true, __half>(plan, d_args, st);
-    } else {
-        e = launch_dyn<false, float>(plan, d_args, st);
-        if (e == cudaSuccess) e = launch_dyn<true, float>(plan, d_args, st);
+bool tc_launch_shape(const TcBlendParams* ps, TcPlan* plans, int n, int storage, TcLaunch& L) {
+    L = TcLaunch();
+    if (n <= 0) return true;
+    L.njobs = 2 * n;
+    std::vector<int64_t> cost(size_t(L.njobs)), tiles(size_t(L.njobs));
+    const int64_t texel_bytes = storage == LUXGI_STORAGE_FP16 ? 2 : 4;
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        for (int k = 0; k < 2; ++k) {
+            TcArgs g;
+            if (k) fill_args<true>(ps[i], g);
+            else fill_args<false>(ps[i], g);
+            const size_t jk = size_t(2 * i + k);
+            plans[i].tile0[k] = int(total);
+            tiles[jk] = g.tiles;
+            total += g.tiles;
+            if (total > INT_MAX) return false;
+            L.nmax = std::max(L.nmax, g.N);
+            L.b_bytes = std::max(L.b_bytes, size_t(g.kb_b) * size_t(g.N) * 128);
+            // bytes a tile moves: its A operand, the history read and the
+            // texels written with their borders
+            const int64_t cell = int64_t(g.side + 2) * (g.side + 2) * g.nc * texel_bytes;
+            cost[jk] = int64_t(g.kb_a) * kStageBytes + 2 * int64_t(128 / g.rows_per_probe) * cell;
+            L.wait_cycles = (jk == 0) ? g.wait_cycles : std::min(L.wait_cycles, g.wait_cycles);
+        }
     }
-    return e;
+    L.total = int(total);
+    L.grid = int(std::min<int64_t>(total, std::min(num_sms(), kTcMaxGrid)));
+    L.smem = 1024 + L.b_bytes + size_t(kStages) * kStageBytes + 256;
+    if (L.smem > 227 * 1024) return false;
+    // CTA b starts at the first tile whose cost prefix reaches b / grid of the total
+    int64_t C = 0;
+    for (int j = 0; j < L.njobs; ++j) C += cost[size_t(j)] * tiles[size_t(j)];
+    int j = 0;
+    int64_t before = 0;
+    for (int b = 0; b <= L.grid; ++b) {
+        const int64_t target = L.grid > 0 ? C * b / L.grid : 0;
+        while (j < L.njobs && before + cost[size_t(j)] * tiles[size_t(j)] < target) {
+            before += cost[size_t(j)] * tiles[size_t(j)];
+            ++j;
+        }
+        if (j == L.njobs) {
+            L.split[b] = L.total;
+        } else {
+            const int64_t c = cost[size_t(j)];
+            const int64_t i = std::min<int64_t>((target - before + c - 1) / c, tiles[size_t(j)]);
+            const int tile0 = plans[j / 2].tile0[j % 2];
+            L.split[b] = int(tile0 + i);
+        }
+    }
+    L.split[L.grid] = L.total;
+    return true;
+}
+
+size_t tc_job_bytes() { return 2 * sizeof(TcJob); }
+
+void tc_fill_jobs(const TcBlendParams& p, const TcPlan& plan, void* out) {
+    TcJob J[2];
+    fill_job(p, plan, 0, J[0]);
+    fill_job(p, plan, 1, J[1]);
+    std::memcpy(out, J, sizeof(J));
+}
+
+cudaError_t launch_tc_blend_jobs(const TcLaunch& L, int storage, const void* d_jobs, cudaStream_t st) {
+    return launch_args(L, storage, nullptr, d_jobs, st);
 }
 
 cudaError_t launch_tc_blend(const TcBlendParams& p, cudaStream_t st) {
     if (p.P <= 0) return cudaSuccess;
     if (!tc_blend_supported(p.u)) return cudaErrorNotSupported;
-    cudaError_t e;
-    if (p.storage == LUXGI_STORAGE_FP16) {
-        e = launch_one<false, __half>(p, st);
-        if (e == cudaSuccess) e = launch_one<true, __half>(p, st);
-    } else {
-        e = launch_one<false, float>(p, st);
-        if (e == cudaSuccess) e = launch_one<true, float>(p, st);
-    }
-    return e;
+    TcPlan plan;
+    TcLaunch L;
+    if (!tc_plan(p, plan) || !tc_launch_shape(&p, &plan, 1, p.storage, L)) return cudaErrorNotSupported;
+    TcJob J[2];
+    fill_job(p, plan, 0, J[0]);
+    fill_job(p, plan, 1, J[1]);
+    return launch_args(L, p.storage, J, nullptr, st);
 }
 
 }  // namespace luxgi

@@ -19,12 +19,14 @@ struct Plan {
     int n = 0;
     int storage = 0, light_mode = 0, sdf_format = 0;
     bool tc = false;
-    // per-frame argument block: TraceParams[n], BlendParams[n], 2 x TcArgs[n]
+    // per-frame argument block: TraceParams[n], BlendParams[n], then the
+    // tensor-core jobs (tc_bytes a volume, 128-byte aligned)
     size_t off_trace = 0, off_blend = 0, off_tc = 0, tc_bytes = 0, arg_bytes = 0;
     std::vector<int> starts;            // [kNumStages][n + 1] block offsets
     int blocks[kNumStages] = {};
     size_t smem_i = 0, smem_d = 0;      // dynamic shared memory of the FP32 blend
     std::vector<TcPlan> tcp;            // tensor-core blend maps, one per volume
+    TcLaunch tcl;                       // the one tensor-core blend launch of the frame
     // march compaction shared by the plan's volumes (budget 0: one pass)
     int budget = 0;
     int64_t work = 0;                   // march work items of all volumes
@@ -51,9 +53,8 @@ int apply_variants(luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_batch
 int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_batch_tuning& t);
 // Per-frame arguments of every volume in its current state (P.arg_bytes).
 void plan_fill(const Plan& P, const float* rots, uint8_t* host);
-struct Fork;
 // One frame: d_args holds plan_fill's block, d_starts the plan's tables.
-cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cudaStream_t st, const Fork* fork);
+cudaError_t plan_launch(const Plan& P, uint8_t* d_args, const int* d_starts, cudaStream_t st);
 int prepare_all(const Plan& P, cudaStream_t st);
 void end_frame_all(const Plan& P);
 

@@ -241,8 +241,11 @@ cudaError_t launch_cull(const luxgi_surface_data& d, const luxgi_surface_object*
                         uint32_t* culled, uint32_t capacity, uint32_t* d_counts, uint32_t* d_status,
                         cudaStream_t st);
 
-// Tensor-core blend (tcgen05).  Returns cudaErrorNotSupported when the
-// shape is outside what the kernel handles.
+// Tensor-core blend (tcgen05).  One launch runs a list of jobs, a job
+// being one blend kind (irradiance or distance) of one volume: both kinds of
+// one volume (launch_tc_blend), or of every volume of a batch
+// (launch_tc_blend_jobs).  Returns cudaErrorNotSupported when a shape is
+// outside what the kernel handles.
 struct TcBlendParams {
     luxgi_ddgi_uniform u;
     const __half* a_irr;     // [P*4][R]
@@ -263,18 +266,29 @@ struct TcBlendParams {
 cudaError_t launch_tc_blend(const TcBlendParams& p, cudaStream_t st);
 bool tc_blend_supported(const luxgi_ddgi_uniform& u);
 
-// Graph-replayable form: tensor maps, shared memory and grids fixed per
-// volume (index 0 irradiance, 1 distance); the per-frame kernel arguments
-// (two blocks of tc_args_bytes(), filled by tc_fill_args) live in device
-// memory at d_args.
+// Graph-replayable batched form.  The tensor maps of a volume's two jobs
+// (index 0 irradiance, 1 distance) and their place in the launch's tile
+// list are fixed per plan; the jobs themselves (maps + per-frame
+// arguments, tc_job_bytes() per volume, filled by tc_fill_jobs) live in
+// device memory, 128-byte aligned, volume after volume.
 struct TcPlan {
     CUtensorMap ma[2], mb[2];
-    size_t smem[2];
-    int grid[2];
+    int tile0[2];            // first tile of each job in the launch's tile list
+};
+constexpr int kTcMaxGrid = 256;
+// Shape of one launch: shared memory, grid, the widest job (TMEM columns)
+// and the split of the tile list between the CTAs (by estimated cost).
+struct TcLaunch {
+    size_t smem = 0, b_bytes = 0;
+    int grid = 0, njobs = 0, nmax = 0, total = 0;
+    long long wait_cycles = 0;
+    int split[kTcMaxGrid + 1] = {};
 };
 bool tc_plan(const TcBlendParams& p, TcPlan& plan);
-size_t tc_args_bytes();
-void tc_fill_args(const TcBlendParams& p, void* out);
-cudaError_t launch_tc_blend_dyn(const TcPlan& plan, int storage, const void* d_args, cudaStream_t st);
+// Places the n volumes' jobs in one tile list (plans[i].tile0) and sizes the launch.
+bool tc_launch_shape(const TcBlendParams* ps, TcPlan* plans, int n, int storage, TcLaunch& L);
+size_t tc_job_bytes();
+void tc_fill_jobs(const TcBlendParams& p, const TcPlan& plan, void* out);
+cudaError_t launch_tc_blend_jobs(const TcLaunch& L, int storage, const void* d_jobs, cudaStream_t st);
 
 }  // namespace luxgi

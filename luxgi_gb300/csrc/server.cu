@@ -311,7 +311,7 @@ int cuda_launch(luxgi_server* S, Slot& sl, const std::vector<Session*>& members)
     plan_fill(P, rots.data(), sl.host);
     std::memcpy(sl.host + P.arg_bytes, P.starts.data(), sb);
     cudaError_t e = cudaMemcpyAsync(sl.dev, sl.host, P.arg_bytes + sb, cudaMemcpyHostToDevice, sl.st);
-    if (e == cudaSuccess) e = plan_launch(P, sl.dev, reinterpret_cast<const int*>(sl.dev + P.arg_bytes), sl.st, nullptr);
+    if (e == cudaSuccess) e = plan_launch(P, sl.dev, reinterpret_cast<const int*>(sl.dev + P.arg_bytes), sl.st);
     if (e == cudaSuccess) e = cudaEventRecord(sl.ev, sl.st);
     if (e != cudaSuccess) return cuda_status(e);
     end_frame_all(P);

@@ -181,5 +181,5 @@ def test_batch_launch_count(cuda, blend):
     per_frame = lib.luxgi_launch_count() - c0
     # raygen, weights, march (one pass: small batches do not compact by
     # default), shade (march order) + blend: 2 FP32 launches, or the
-    # operand pack and 2 tensor-core launches per volume
-    assert per_frame == 4 + (2 if blend == N.BLEND_FP32 else 1 + 2 * 3)
+    # operand pack and one tensor-core launch for every volume's two kinds
+    assert per_frame == 4 + (2 if blend == N.BLEND_FP32 else 1 + 1)
