@@ -130,16 +130,14 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 struct TcArgs {
@@ -180,16 +178,17 @@ struct TcLaunchArgs {
 static_assert(sizeof(TcLaunchArgs) <= 4096, "kernel parameter block");
 
 // Lane-group transposes of the epilogue.  The lanes of one probe each hold
-// one channel over 16 accumulator columns (texels); afterwards each lane
+// one channel over C accumulator columns (texels); afterwards each lane
 // holds every channel of its own texels, so that a texel is loaded (the
 // hysteresis history) and stored (with its border mirrors) in one vector
 // access instead of one scalar access per channel.
-// Irradiance, 4 lanes (r, g, b, zero row) and four 4x4 blocks: lane m ends
+// Irradiance, 4 lanes (r, g, b, zero row) and C / 4 4x4 blocks: lane m ends
 // with texels 4k + m as v[4k .. 4k+3].
+template <int C>
 __device__ __forceinline__ void transpose_quad(float* v, int lane) {
     const bool b1 = (lane & 2) != 0, b0 = (lane & 1) != 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < C / 4; ++k) {
         float* a = v + 4 * k;
         // swap the off-diagonal 2x2 blocks with lane ^ 2 ...
 #pragma unroll
@@ -211,12 +210,13 @@ __device__ __forceinline__ void transpose_quad(float* v, int lane) {
     }
 }
 
-// Distance, 2 lanes (d, d^2) and eight 2x2 blocks: lane m ends with texels
+// Distance, 2 lanes (d, d^2) and C / 2 2x2 blocks: lane m ends with texels
 // 2k + m as v[2k .. 2k+1].
+template <int C>
 __device__ __forceinline__ void transpose_pair(float* v, int lane) {
     const bool b0 = (lane & 1) != 0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < C / 2; ++k) {
         float* a = v + 2 * k;
         const float x = __shfl_xor_sync(0xffffffffu, b0 ? a[0] : a[1], 1);
         if (b0) a[0] = x;
@@ -258,14 +258,17 @@ __device__ __forceinline__ bool epilogue_tile(const TcArgs& g, int lt, uint32_t 
     const bool live = p < g.P;
     const int cx = p % XY, cy = p / XY;
     const bool hyst = !first && live;
-    // the previous texels (hysteresis) of this lane in a 16-column chunk,
-    // the first chunk's before the wait for the accumulator (loading the
-    // next chunk's during the stores as well needs 16 more registers: the
-    // spills at the 96 a thread that 576 threads leave cost more)
+    // the columns go in 8-wide chunks; the previous texels (hysteresis) of
+    // this lane in a chunk are loaded one chunk ahead: the first chunk's
+    // before the wait for the accumulator, each next chunk's while the
+    // current one is stored (8-wide chunks keep the accumulator values, the
+    // history and the history in flight within the 96 registers a thread
+    // that 576 threads leave)
+    constexpr int CW = 8;
     auto load_prev = [&](int c0, float* pv) {
         int ty = (c0 + m) / n, tx = c0 + m - ty * n;
 #pragma unroll
-        for (int k = 0; k < 16 / G; ++k) {
+        for (int k = 0; k < CW / G; ++k) {
             if (c0 + G * k + m < T) {
                 AtlasIO<AT>::template ld_texel<G>(prev, size_t(cy * (n + 2) + ty + 2) * W + (cx * (n + 2) + tx + 2),
                                                   pv + G * k);
@@ -277,21 +280,20 @@ __device__ __forceinline__ bool epilogue_tile(const TcArgs& g, int lt, uint32_t 
             }
         }
     };
-    float pv[16];
+    float pv[CW], pn[CW];
     if (hyst && c_begin < c_end) load_prev(c_begin, pv);
     if (!mbar_wait(tfull, parity, abort_flag, budget)) return false;
     tc_fence_after();
-    for (int c0 = c_begin; c0 < c_end; c0 += 16) {
-        // the next chunks' history, in flight during the accumulator load and the transpose
-        if (hyst && c0 > c_begin) load_prev(c0, pv);
-        float v[16];
-        tmem_ld16(taddr + uint32_t(c0), v);
-        if (DIST) transpose_pair(v, lane);   // every lane: the shuffles span the warp
-        else transpose_quad(v, lane);
+    for (int c0 = c_begin; c0 < c_end; c0 += CW) {
+        float v[CW];
+        tmem_ld8(taddr + uint32_t(c0), v);
+        if (DIST) transpose_pair<CW>(v, lane);   // every lane: the shuffles span the warp
+        else transpose_quad<CW>(v, lane);
         if (!live) continue;
+        if (hyst && c0 + CW < c_end) load_prev(c0 + CW, pn);
         int ty = (c0 + m) / n, tx = c0 + m - ty * n;
 #pragma unroll
-        for (int k = 0; k < 16 / G; ++k) {
+        for (int k = 0; k < CW / G; ++k) {
             const int t = c0 + G * k + m;
             if (t < T) {
                 const float nt = __ldg(norm + t);
@@ -314,6 +316,10 @@ __device__ __forceinline__ bool epilogue_tile(const TcArgs& g, int lt, uint32_t 
                 tx -= n;
                 ++ty;
             }
+        }
+        if (hyst) {
+#pragma unroll
+            for (int j = 0; j < CW; ++j) pv[j] = pn[j];
         }
     }
     return true;
