@@ -72,6 +72,10 @@ def parse():
     ap.add_argument("--serve-budget-gb", type=float, default=120.0, help="serve200: device-memory budget")
     ap.add_argument("--frames-per-step", type=int, default=16, help="frames of the volume in one step")
     ap.add_argument("--no-north-star", action="store_true", help="skip the batched and served forms")
+    ap.add_argument("--batch-tuning", default=None,
+                    help="batch48: a fixed tuning (JSON object of luxgi_ddgi_batch_tuning fields) instead of the autotuner")
+    ap.add_argument("--no-sequential", action="store_true",
+                    help="batch48: skip the one-volume-at-a-time comparison")
     ap.add_argument("--ns-serve-seconds", type=float, default=8.0,
                     help="north-star leg: length of the timed serving run")
     return ap.parse_args()
@@ -452,10 +456,12 @@ def run_ours(args, rank: int, world: int):
 
 
 # ----------------------------------------------------------------- batch
-def measure_batch(ws, hosts, K: int, W: int, world: int, e2e_on: bool = True, seed: int = 0x5EED) -> dict:
+def measure_batch(ws, hosts, K: int, W: int, world: int, e2e_on: bool = True, seed: int = 0x5EED,
+                  tuning: dict | None = None, sequential: bool = True) -> dict:
     """The batching form over workloads `ws` (scenes `hosts`): `value` is
-    the batched, graph-replayed, autotuned form; `sequential` the same
-    volumes as plain luxgi_ddgi_update calls per frame on the same GPU."""
+    the batched, graph-replayed form, autotuned unless `tuning` is given;
+    `sequential` the same volumes as plain luxgi_ddgi_update calls per frame
+    on the same GPU (skipped when `sequential` is false)."""
     import numpy as np
     import torch
 
@@ -497,13 +503,18 @@ def measure_batch(ws, hosts, K: int, W: int, world: int, e2e_on: bool = True, se
         for v, r in zip(vols, rots[f]):
             v.update(r, stream)
 
-    for f in range(W):
-        seq_step(f)
-    seq_ms = timed(seq_step, range(W, W + K))
+    seq_ms = None
+    if sequential:
+        for f in range(W):
+            seq_step(f)
+        seq_ms = timed(seq_step, range(W, W + K))
 
-    batch = DDGIBatch(vols)
     t0 = time.perf_counter()
-    tuning = batch.autotune(frames=3)
+    if tuning is None:
+        batch = DDGIBatch(vols)
+        tuning = batch.autotune(frames=3)
+    else:
+        batch = DDGIBatch(vols, tuning)
     tune_s = time.perf_counter() - t0
 
     def batch_step(f):
@@ -519,7 +530,7 @@ def measure_batch(ws, hosts, K: int, W: int, world: int, e2e_on: bool = True, se
     clk = clocks.stop()
     launches = N.ddgi().luxgi_launch_count() - launches0
     value = world * pr * K / (b_ms / 1e3)
-    seq_value = world * pr * K / (seq_ms / 1e3)
+    seq_value = world * pr * K / (seq_ms / 1e3) if seq_ms is not None else None
 
     # e2e: rotations from the host, every volume's atlases read back to
     # pinned host memory each frame; the readback of frame k runs on a
@@ -561,9 +572,10 @@ def measure_batch(ws, hosts, K: int, W: int, world: int, e2e_on: bool = True, se
         e2e = {"value": world * pr * K / te, "unit": "probe-rays/s", "h2d_bytes_per_step": 36 * n,
                "d2h_bytes_per_step": int(d2h)}
     out = {"value": value, "ms_per_step": b_ms / K, "probe_rays_per_frame": pr, "volumes": n,
-           "sequential": {"value": round(seq_value, 1), "ms_per_step": round(seq_ms / K, 4),
-                          "what": f"{n} luxgi_ddgi_update calls per frame, same volumes and GPU"},
-           "speedup_vs_sequential": round(value / seq_value, 3), "autotune": tuning,
+           "sequential": None if seq_value is None else {
+               "value": round(seq_value, 1), "ms_per_step": round(seq_ms / K, 4),
+               "what": f"{n} luxgi_ddgi_update calls per frame, same volumes and GPU"},
+           "speedup_vs_sequential": None if seq_value is None else round(value / seq_value, 3), "autotune": tuning,
            "autotune_s": round(tune_s, 2), "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
     batch.close()
     for v in vols:
@@ -598,7 +610,9 @@ def run_batch(args, rank: int, world: int):
     ws = batch_workloads(count)
     hosts = [HostScene(w.scene) for w in ws]
     setup_s = time.perf_counter() - t0
-    b = measure_batch(ws, hosts, args.steps, args.warmup, world, not args.no_e2e, seed=0x5EED + rank)
+    tuning = json.loads(args.batch_tuning) if args.batch_tuning else None
+    b = measure_batch(ws, hosts, args.steps, args.warmup, world, not args.no_e2e, seed=0x5EED + rank, tuning=tuning,
+                      sequential=not args.no_sequential)
     if rank != 0:
         return
     line = {
