@@ -1054,15 +1054,31 @@ __device__ __forceinline__ void oct_cell_point(f3 d, int side, float& rx, float&
 // (x0, y0) the interior corner of a probe cell (cell * (side + 2) + 2) and
 // (rx, ry) from oct_cell_point.  rx lies in [-0.5, side - 0.5], so the four
 // texels stay inside the cell and its 1-texel border (the clamp only guards
-// a NaN direction, which converts to the cell's first texel).
-template <int NC>
-__device__ __forceinline__ void bilinear_tap_v(const void* p, int storage, int W, int side, int x0, int y0, float rx,
-                                               float ry, float* out) {
+// a NaN direction, which converts to the cell's first texel).  tap_frac
+// splits the point into its texel corner and fractions, which a direction
+// shared by several cells (sampleIrradiance's normal) computes once.
+struct TapFrac {
+    int ix, iy;   // texel corner relative to the cell's interior corner
+    float a, b;   // fractions
+};
+
+__device__ __forceinline__ TapFrac tap_frac(int side, float rx, float ry) {
     const float fx = fminf(fmaxf(floorf(rx), -1.0f), float(side - 1));
     const float fy = fminf(fmaxf(floorf(ry), -1.0f), float(side - 1));
-    const float a = rx - fx, b = ry - fy;
-    const int i0 = x0 + int(fx), j0 = y0 + int(fy);
+    TapFrac f;
+    f.ix = int(fx);
+    f.iy = int(fy);
+    f.a = rx - fx;
+    f.b = ry - fy;
+    return f;
+}
+
+template <int NC>
+__device__ __forceinline__ void bilinear_at_v(const void* p, int storage, int W, int x0, int y0, const TapFrac& f,
+                                              float* out) {
+    const int i0 = x0 + f.ix, j0 = y0 + f.iy;
     const int i1 = i0 + 1, j1 = j0 + 1;
+    const float a = f.a, b = f.b;
     float t00[NC], t10[NC], t01[NC], t11[NC];
     atlas_texel<NC>(p, storage, size_t(j0) * W + i0, t00);
     atlas_texel<NC>(p, storage, size_t(j0) * W + i1, t10);
@@ -1075,6 +1091,12 @@ __device__ __forceinline__ void bilinear_tap_v(const void* p, int storage, int W
     }
 }
 
+template <int NC>
+__device__ __forceinline__ void bilinear_tap_v(const void* p, int storage, int W, int side, int x0, int y0, float rx,
+                                               float ry, float* out) {
+    bilinear_at_v<NC>(p, storage, W, x0, y0, tap_frac(side, rx, ry), out);
+}
+
 // pow(x, e) of the irradiance decode; x*x*sqrt(x) for the default gamma
 // (e = 2.5), within 1.5 ulp of powf
 __device__ __forceinline__ float pow_decode(float x, float e) {
@@ -1082,8 +1104,8 @@ __device__ __forceinline__ float pow_decode(float x, float e) {
 }
 
 // sampleIrradiance (DDGICommon.glsl:163-233).  The normal-bias vector and
-// the octahedral coordinate of N are the same for the 8 cage probes and are
-// computed once.
+// the octahedral coordinate of N (its texel corner and fractions in every
+// irradiance cell) are the same for the 8 cage probes and are computed once.
 // FAST (hit shading, compared by tolerance): the probe-to-point direction is
 // normalised once and the distance taken from the same reciprocal root.
 template <int UNROLL = 1, bool FAST = false>
@@ -1105,6 +1127,7 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
     // point inside every cage probe's irradiance cell
     float nrx, nry;
     oct_cell_point(norm3(N), u.irradiance_probe_side, nrx, nry);
+    const TapFrac nf = tap_frac(u.irradiance_probe_side, nrx, nry);
     const int ni = u.irradiance_probe_side, nd = u.depth_probe_side;
     // UNROLL cage probes per iteration overlap their texel fetches; the sums
     // still accumulate in probe order 0..7
@@ -1149,8 +1172,7 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         weight = weight * ((dist <= mean) ? 1.0f : cheb);
         weight = mx(0.000001f, weight);
         float ir[4];
-        bilinear_tap_v<4>(A.irr, A.storage, u.irradiance_width, ni, cell_x * (ni + 2) + 2, cell_y * (ni + 2) + 2, nrx,
-                          nry, ir);
+        bilinear_at_v<4>(A.irr, A.storage, u.irradiance_width, cell_x * (ni + 2) + 2, cell_y * (ni + 2) + 2, nf, ir);
         const f3 pir{pow_decode(ir[0], ge), pow_decode(ir[1], ge), pow_decode(ir[2], ge)};
         const float crush = 0.2f;
         if (weight < crush) weight = weight * (weight * weight * (1.0f / (crush * crush)));
