@@ -343,12 +343,13 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n,
  * A fixed set of volumes (uneven probe grids and ray counts) updated
  * together, frame after frame: raygen, weights, march, shade and the FP32
  * blend are each one launch over all volumes (blocks find their volume by
- * a block-offset table); the tensor-core blend is one launch pair per
- * volume on parallel graph branches.  The frame is captured once as a CUDA
- * graph and replayed; the per-frame arguments (rotations, ping-pong
- * atlases, first-frame and bounce flags) are written to pinned host memory
- * and copied in by the graph.  Results equal luxgi_ddgi_update of each
- * volume alone.  No reference counterpart. */
+ * a block-offset table); the tensor-core blend is one persistent launch
+ * over every volume's irradiance and distance jobs.  The frame is
+ * captured once as a CUDA graph and replayed; the per-frame arguments
+ * (rotations, ping-pong atlases, first-frame and bounce flags) are
+ * written to pinned host memory and copied in by the graph.  Results
+ * equal luxgi_ddgi_update of each volume alone.  No reference
+ * counterpart. */
 typedef struct luxgi_ddgi_batch luxgi_ddgi_batch;
 
 typedef struct luxgi_ddgi_batch_tuning {
