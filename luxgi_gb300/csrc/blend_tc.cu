@@ -154,7 +154,8 @@ struct TcArgs {
     int lo_offset;                        // column of the lo half in A (distance), 0 otherwise
     int tiles;                            // 128-row tiles of this job
     int tile0;                            // its first tile in the launch's tile list
-    long long wait_cycles;                // bound of every mbarrier wait, SM clock cycles
+    long long wait_cycles;                // this job's bound of an mbarrier wait, SM clock cycles (a launch
+                                          // takes the smallest of its jobs')
     int withhold;                         // test aid: block 0 skips the first A load of its first tile
 };
 

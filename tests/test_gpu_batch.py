@@ -17,7 +17,7 @@ import pytest
 from luxgi_gb300 import _native as N
 from luxgi_gb300.ddgi import DDGIBatch, DDGIVolume, frame_rotation, update_batch
 from luxgi_gb300.scene import DeviceScene, HostScene, batch_workloads
-from tests._helpers import rel_err
+from tests._helpers import rel_err, tiny_workload
 
 pytestmark = pytest.mark.gpu
 
@@ -83,6 +83,36 @@ def test_batch_equals_single(cuda, blend, use_graph, shade_order, march_budget):
             v.update(r)
         batch.update(rots)
         _assert_same(alone, batched)
+
+
+def test_tensor_blend_jobs_spanning_ctas(cuda):
+    """Three volumes of 2,048 probes with 64, 192 and 128 rays: the batch's
+    one tensor-core launch holds 288 tiles for at most one CTA per SM, so
+    CTAs' tile ranges cross from one job into the next and reload the
+    weights (of another ray count, a smaller B than the widest job's) after
+    the last multiply of the previous job.  Alone, each volume's 96 tiles
+    give each CTA one tile.  Every volume's atlases equal its own update."""
+    ws = [tiny_workload(probe_counts=(16, 8, 16), spacing=0.6, rays=r, blend=N.BLEND_TENSOR, seed=40 + i, steps=32)
+          for i, r in enumerate((64, 192, 128))]
+    scenes, alone, batched = [], [], []
+    for w in ws:
+        host = HostScene(w.scene)
+        dev = DeviceScene(host, w.volume.light_mode)
+        a, b = DDGIVolume(w.volume), DDGIVolume(w.volume)
+        a.bind_scene(dev)
+        b.bind_scene(dev)
+        scenes.append((host, dev))
+        alone.append(a)
+        batched.append(b)
+    batch = DDGIBatch(batched)
+    for f in range(3):
+        rots = _rots(len(ws), f)
+        for v, r in zip(alone, rots):
+            v.update(r)
+        batch.update(rots)
+        for v in alone + batched:
+            v.check_status()
+    _assert_same(alone, batched)
 
 
 def test_batch_fp16_storage_and_tuning_knobs(cuda):
