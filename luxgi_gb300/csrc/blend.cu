@@ -18,11 +18,6 @@
 
 namespace luxgi {
 
-// Texels per thread of the FP32 blend tile; the FP32 weight rows are stored
-// ray-major, [R][Tp] with Tp = T rounded up to whole tiles (padding zero).
-constexpr int kTexelTile = 4;
-
-__host__ __device__ __forceinline__ int blend_row_pitch(int T) { return (T + kTexelTile - 1) / kTexelTile * kTexelTile; }
 
 // ------------------------------------------------------------- weights
 // One block per texel row, threads over rays: octDecode(normalizedOctCoord)
@@ -159,7 +154,10 @@ __host__ __device__ __forceinline__ BlendShape blend_shape(int T, int PP) {
 // FP32 rays take the pipelined path: chunks of kPipeChunk rays, two buffers,
 // the next chunk's weights and rays copied with cp.async while the current
 // chunk's FMAs run (the same shared memory as one 32-ray buffer).
-constexpr int kPipeChunk = 16;
+#ifndef LUXGI_BLEND_PIPE_CHUNK
+#define LUXGI_BLEND_PIPE_CHUNK 16
+#endif
+constexpr int kPipeChunk = LUXGI_BLEND_PIPE_CHUNK;
 
 __host__ __device__ __forceinline__ size_t blend_smem_bytes(int T, int PP, bool depth, bool pipelined) {
     const BlendShape s = blend_shape(T, PP);
@@ -316,8 +314,15 @@ __device__ __forceinline__ void blend_block_pipelined(const BlendParams& p, int 
             const RV* rrow = rs + pg * PP;
 #pragma unroll 2
             for (int r = 0; r < kc; ++r) {
-                const float4 w4 = *reinterpret_cast<const float4*>(wrow + r * Tp);
-                const float w[kTexelTile] = {w4.x, w4.y, w4.z, w4.w};
+                float w[kTexelTile];
+#pragma unroll
+                for (int q = 0; q < kTexelTile / 4; ++q) {
+                    const float4 w4 = *reinterpret_cast<const float4*>(wrow + r * Tp + 4 * q);
+                    w[4 * q] = w4.x;
+                    w[4 * q + 1] = w4.y;
+                    w[4 * q + 2] = w4.z;
+                    w[4 * q + 3] = w4.w;
+                }
 #pragma unroll
                 for (int j = 0; j < PP; ++j) {
                     const RV v = rrow[r * PB + j];
@@ -402,8 +407,15 @@ __device__ __forceinline__ void blend_block(const BlendParams& p, int block, flo
             const RV* rrow = Rs + pg * PP;
 #pragma unroll 2
             for (int r = 0; r < kc; ++r) {
-                const float4 w4 = *reinterpret_cast<const float4*>(wrow + r * Tp);
-                const float w[kTexelTile] = {w4.x, w4.y, w4.z, w4.w};
+                float w[kTexelTile];
+#pragma unroll
+                for (int q = 0; q < kTexelTile / 4; ++q) {
+                    const float4 w4 = *reinterpret_cast<const float4*>(wrow + r * Tp + 4 * q);
+                    w[4 * q] = w4.x;
+                    w[4 * q + 1] = w4.y;
+                    w[4 * q + 2] = w4.z;
+                    w[4 * q + 3] = w4.w;
+                }
 #pragma unroll
                 for (int j = 0; j < PP; ++j) {
                     const RV v = rrow[r * PB + j];

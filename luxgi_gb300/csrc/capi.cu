@@ -257,7 +257,7 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
     const uint64_t ae = atlas_elem_bytes(d.storage);
     uint64_t b = 2 * (uint64_t(u.irradiance_width) * u.irradiance_height * 4 * ae +
                       uint64_t(u.depth_width) * u.depth_height * 2 * ae);
-    b += 2 * 16 * R + PR * ray_elem_bytes(d.storage) + 4 * ((Ti + 3) / 4 * 4 + (Td + 3) / 4 * 4) * R + 8 * (Ti + Td) + 16 +
+    b += 2 * 16 * R + PR * ray_elem_bytes(d.storage) + 4 * uint64_t(blend_row_pitch(int(Ti)) + blend_row_pitch(int(Td))) * R + 8 * (Ti + Td) + 16 +
          PR * (16 + 4);
     if (d.blend == LUXGI_BLEND_TENSOR) b += PR * 16 + 2 * ((Ti + 15) / 16 * 16 + (Td + 15) / 16 * 16) * R;
     const uint64_t nobj = surf.data.objects_count;
@@ -741,8 +741,8 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (e == cudaSuccess) e = dmalloc(&v->dirs_blend, sizeof(float4) * v->R);
     if (e == cudaSuccess) e = dmalloc(&v->rays, PR * ray_elem_bytes(desc->storage));
     // FP32 weights: ray-major rows padded to whole texel tiles, padding zero
-    const size_t wi_bytes = sizeof(float) * size_t((v->Ti + 3) / 4 * 4) * v->R;
-    const size_t wd_bytes = sizeof(float) * size_t((v->Td + 3) / 4 * 4) * v->R;
+    const size_t wi_bytes = sizeof(float) * size_t(blend_row_pitch(v->Ti)) * v->R;
+    const size_t wd_bytes = sizeof(float) * size_t(blend_row_pitch(v->Td)) * v->R;
     if (e == cudaSuccess) e = dmalloc(&v->w_irr, wi_bytes);
     if (e == cudaSuccess) e = dmalloc(&v->w_dist, wd_bytes);
     if (e == cudaSuccess) e = cudaMemset(v->w_irr, 0, wi_bytes);

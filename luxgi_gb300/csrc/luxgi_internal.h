@@ -14,6 +14,14 @@ namespace luxgi {
 // from a ray pool); 1-5 and 10 run one ray per thread.
 inline bool pooled_variant(int mv) { return mv >= 6 && mv <= 9; }
 
+// Texels per thread of the FP32 blend tile; the FP32 weight rows are stored
+// ray-major, [R][Tp] with Tp = T rounded up to whole tiles (padding zero).
+#ifndef LUXGI_BLEND_TEXEL_TILE
+#define LUXGI_BLEND_TEXEL_TILE 4
+#endif
+constexpr int kTexelTile = LUXGI_BLEND_TEXEL_TILE;   // a multiple of 4
+__host__ __device__ inline int blend_row_pitch(int T) { return (T + kTexelTile - 1) / kTexelTile * kTexelTile; }
+
 // Count of kernel launches issued by the library (luxgi_launch_count).
 void note_launch(int n = 1);
 
@@ -124,8 +132,8 @@ struct BlendParams {
     const void* prev_dist;
     void* out_irr;
     void* out_dist;
-    float* w_irr;            // [R][Ti rounded up to 4] cut weights, ray-major
-    float* w_dist;           // [R][Td rounded up to 4]
+    float* w_irr;            // [R][blend_row_pitch(Ti)] cut weights, ray-major
+    float* w_dist;           // [R][blend_row_pitch(Td)]
     float* n_irr;            // [Ti] 1/(2 sum w) or 1 (then the tensor-core normalisers)
     float* n_dist;           // [Td]
     __half* tcw_irr;         // [tc_ni][R] FP16 tensor-core weights, or nullptr
