@@ -1020,6 +1020,10 @@ def run_reference(args, rank: int, world: int):
     import oracle
     from luxgi_gb300.scene import HostScene, WORKLOADS
 
+    if world > 1:
+        # torchrun sets OMP_NUM_THREADS=1 for every rank; rank 0 alone runs
+        # here and takes every host core
+        oracle.set_threads(os.cpu_count() or 1)
     w = WORKLOADS[args.workload]
     v = w.volume
     host = HostScene(w.scene)
