@@ -435,7 +435,8 @@ def run_ours(args, rank: int, world: int):
     if rank != 0:
         return
     cpu, err = (None, None)
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
+        # the CPU baseline and the FP64 error check: rank 0 at N = 1 only
         cpu = cpu_baseline(w, host, rots[0], args.cpu_seconds)
         if snaps:
             err = atlas_error_vs_fp64(w, host, snaps)
@@ -773,7 +774,7 @@ def run_surface(args, rank: int, world: int):
     if rank != 0:
         return
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         inp = oracle.HostInputs(host, w.volume.light_mode, mip=dev.mip.cpu().numpy(),
                                 chunks=dev.chunks.cpu().numpy().view(np.uint32),
                                 culled=dev.culled.cpu().numpy().view(np.uint32))
@@ -910,7 +911,7 @@ def run_sdf_build(args, rank: int, world: int):
     if rank != 0:
         return
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         t0 = time.perf_counter()
         oracle.sdf_build(d, meshes, objs)
         el = time.perf_counter() - t0
