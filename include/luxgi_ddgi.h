@@ -214,7 +214,10 @@ typedef struct luxgi_ddgi_volume_desc {
     float   intensity;             /* IrradianceVolume::intensity             */
     float   sky_radiance[3];       /* constant sky for misses                 */
     int32_t march_variant;         /* tuning, results identical, speed differs:
-                                      0 default (= 4); 1 plain SDF layout,
+                                      0 default, settled at bind: 10 for an
+                                      FP32 SDF (4 where its planes exceed
+                                      the texture gather limits), 4 for an
+                                      FP16 SDF; 1 plain SDF layout,
                                       64-register march; 2 plain, no register
                                       bound; 3 quad-packed mip; 4 quad-packed
                                       mip + SDF (4x SDF memory); 5 quad-packed

@@ -67,21 +67,33 @@ void gather_free(GatherTex& g) {
 // (W + 2) x (H + 2) texels tiled gx to a row within the device's texture
 // gather limits, in a CUDA array made for gathers; point sampling,
 // unnormalised coordinates.  Reuses the array when the shape is unchanged.
-int gather_alloc(GatherTex& g, int W, int H, int D, int format) {
-    if (g.arr && g.W == W && g.H == H && g.D == D && g.format == format) return LUXGI_OK;
-    gather_free(g);
+// Planes a row of the gather texture of a W x H x D volume: the largest
+// power of two within the device's gather width (and no more than the
+// planes need), so a plane's tile is a shift and a mask; 0 when the tiled
+// planes exceed the gather limits, -1 when the limits cannot be read.
+int gather_planes_per_row(int W, int H, int D) {
     int dev = 0, maxw = 0, maxh = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxTexture2DGatherWidth, dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&maxh, cudaDevAttrMaxTexture2DGatherHeight, dev);
-    if (e != cudaSuccess) return cuda_status(e);
+    if (e != cudaSuccess) return -1;
     const int pw = W + 2, ph = H + 2;
-    // planes a row: the largest power of two within the gather width (and
-    // no more than the planes need), so a plane's tile is a shift and a mask
     int gx = 1;
     while (gx * 2 * pw <= maxw && gx < D) gx *= 2;
     const int gy = (D + gx - 1) / gx;
-    if (gx * pw > maxw || int64_t(gy) * ph > int64_t(maxh)) return LUXGI_EUNSUPPORTED;
+    if (gx * pw > maxw || int64_t(gy) * ph > int64_t(maxh)) return 0;
+    return gx;
+}
+
+int gather_alloc(GatherTex& g, int W, int H, int D, int format) {
+    if (g.arr && g.W == W && g.H == H && g.D == D && g.format == format) return LUXGI_OK;
+    gather_free(g);
+    const int gx = gather_planes_per_row(W, H, D);
+    if (gx < 0) return LUXGI_ECUDA;
+    if (gx == 0) return LUXGI_EUNSUPPORTED;
+    const int pw = W + 2, ph = H + 2;
+    const int gy = (D + gx - 1) / gx;
+    cudaError_t e;
     const cudaChannelFormatDesc cd =
         format == LUXGI_STORAGE_FP16 ? cudaCreateChannelDescHalf() : cudaCreateChannelDesc<float>();
     e = cudaMallocArray(&g.arr, &cd, size_t(gx * pw), size_t(gy * ph), cudaArrayTextureGather);
@@ -246,6 +258,18 @@ int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int c
     return d.march_budget;
 }
 
+int luxgi::default_march_variant(const luxgi_sdf_desc& sdf) {
+    // FP32 SDFs: the gather textures (one copy; production march 0.847 ->
+    // 0.812 ms against the quad-packed copies).  FP16 SDFs: the quad-packed
+    // copies (precision config 0.789 ms against 0.794 ms with gathers).
+    if (sdf.format != LUXGI_STORAGE_FP32) return 4;
+    const int C = int(sdf.data.cascades_count);
+    if (gather_planes_per_row(sdf.resolution * C, sdf.resolution, sdf.resolution) <= 0 ||
+        gather_planes_per_row(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution) <= 0)
+        return 4;
+    return 10;
+}
+
 uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi_sdf_desc& sdf,
                                     const luxgi_surface_desc& surf) {
     // mirrors the allocations of luxgi_ddgi_create and luxgi_ddgi_bind_scene
@@ -265,7 +289,7 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
     if (cap == 0) cap = 1 + 40ull * 40 * 40 * (nobj + 1);
     b += 64 * nobj + 4 * cap + 4 * (2 * 40ull * 40 * 40 + 1);
     const int C = int(sdf.data.cascades_count);
-    const int mv = d.march_variant == 0 ? 4 : d.march_variant;
+    const int mv = d.march_variant == 0 ? default_march_variant(sdf) : d.march_variant;
     const int layout = pooled_variant(mv) ? mv - 4 : mv;
     if (layout >= 3 && layout <= 5)
         b += quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
@@ -716,8 +740,12 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     luxgi_ddgi_volume* v = new (std::nothrow) luxgi_ddgi_volume();
     if (!v) return LUXGI_ENOMEM;
     v->desc = *desc;
-    // defaults: the variants measured fastest on the production workload
-    if (v->desc.march_variant == 0) v->desc.march_variant = 4;
+    // defaults: the variants measured fastest on the production workload;
+    // the march variant is settled when the SDF (its format) is bound
+    if (v->desc.march_variant == 0) {
+        v->auto_variant = true;
+        v->desc.march_variant = 4;
+    }
     if (v->desc.shade_variant == 0) v->desc.shade_variant = 1;
     cudaGetDevice(&v->device);
     const luxgi_ddgi_uniform& u = desc->uniform;
@@ -821,7 +849,12 @@ int luxgi_ddgi_bind_scene(luxgi_ddgi_volume* v, const luxgi_sdf_desc* sdf, const
     }
     v->sdf = *sdf;
     v->surf = *surf;
-    const int st = volume_alloc_packs(v);
+    if (v->auto_variant) v->desc.march_variant = default_march_variant(*sdf);
+    int st = volume_alloc_packs(v);
+    if (st == LUXGI_EUNSUPPORTED && v->auto_variant && v->desc.march_variant != 4) {
+        v->desc.march_variant = 4;
+        st = volume_alloc_packs(v);
+    }
     if (st != LUXGI_OK) return st;
     v->w2l_dirty = true;
     v->bound = true;

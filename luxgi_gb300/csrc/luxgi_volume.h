@@ -16,6 +16,7 @@ struct luxgi_ddgi_volume {
     int debug_rays = 0;
     bool bound = false;
     bool tc = false;
+    bool auto_variant = false;     // march variant left to the library: chosen at bind by the SDF format
     long long tc_wait_cycles = 0;  // bound of the tensor-core blend's waits (0: ~2 s)
     int tc_withhold = 0;           // test aid, one probe update: withhold one operand load
     int tc_ni = 0, tc_nd = 0;      // padded weight rows (multiples of 16)
@@ -93,6 +94,10 @@ void volume_blend_params(const luxgi_ddgi_volume* v, BlendParams& p);
 void volume_tc_params(const luxgi_ddgi_volume* v, TcBlendParams& p);
 // (Re)allocates the packed SDF copies the volume's march variant reads.
 int volume_alloc_packs(luxgi_ddgi_volume* v);
+// The march variant a volume that leaves it to the library (march_variant
+// 0) runs over this SDF: the gather textures (10) for an FP32 SDF whose
+// planes fit the device's gather limits, else the quad-packed copies (4).
+int default_march_variant(const luxgi_sdf_desc& sdf);
 // Steps of the first march pass with compaction for a volume whose work is
 // `work` items and whose march variant / budget / step cap are those of d;
 // 0 when the march runs in one pass.
