@@ -336,13 +336,18 @@ __device__ __forceinline__ float gather_lerp(const GatherVol& g, int W, int H, i
     return c0 * ic + c1 * c;
 }
 
+// A sample anywhere (the hit normal's taps reach one texel past [0, 1]):
+// the corner clamped to [-1, W - 1] per axis, so that the x and y taps read
+// the apron (the edge value) and the planes z0 = max(iz, 0), z1 = min(iz + 1,
+// D - 1) are those of the two-sided clamp; the fractions stay those of the
+// unclamped corner, as in sample3d (equal taps then mix to the same value).
 template <typename T>
 __device__ __forceinline__ float sample3d_gather(const GatherVol& g, int W, int H, int D, float u, float vv, float w) {
     const float x = u * float(W) - 0.5f, y = vv * float(H) - 0.5f, z = w * float(D) - 0.5f;
     const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
-    // x and y clamped to [-1, W - 1] (a sample outside [0, 1] reads the edge)
     const int ix = imn(imx(int(fx), -1), W - 1), iy = imn(imx(int(fy), -1), H - 1);
-    return gather_lerp<T>(g, W, H, D, x - fx, y - fy, z - fz, ix, iy, int(fz));
+    const int iz = imn(imx(int(fz), -1), D - 1);
+    return gather_lerp<T>(g, W, H, D, x - fx, y - fy, z - fz, ix, iy, iz);
 }
 
 // Volume layouts a march variant reads

@@ -287,8 +287,15 @@ def test_sample_probe_image_matches_oracle(cuda, storage, channels):
     dict(probe_counts=(4, 2, 2), rays=40, sdf_format=N.STORAGE_FP16, storage=N.STORAGE_FP16),
     dict(probe_counts=(3, 3, 3), rays=32, spacing=9.0),       # probes outside the room: misses
 ])
-def test_edge_shapes(cuda, kw):
+@pytest.mark.parametrize("mv", [0, 4, 10])
+def test_edge_shapes(cuda, kw, mv):
+    """Degenerate and small shapes, with the default march variant and
+    with the quad-packed (4) and gather-texture (10) samplers, whose hit
+    normals sample one texel past the cascade's edges."""
+    from dataclasses import replace
+
     w = tiny_workload(**kw)
+    w = replace(w, volume=replace(w.volume, march_variant=mv))
     host, dev, vol, inp = setup(w)
     rots = [frame_rotation(28, f) for f in range(3)]
     prev = None
