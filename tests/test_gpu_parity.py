@@ -364,6 +364,37 @@ def test_tensor_blend_vs_fp64(cuda, sides, rays):
         prev = (gi, gd)
 
 
+def test_tensor_blend_fp16_storage_vs_fp64(cuda):
+    """The tensor-core blend writing FP16 atlases (its half-precision
+    history loads and stores): within the tensor-core bound plus one FP16
+    rounding step (2^-10) of the FP64 blend, which rounds its stored values
+    to FP16 the same way and weights the rays by their FP16-stored
+    directions (the reference's RGBA16F direction-distance texture)."""
+    w = tiny_workload(probe_counts=(7, 3, 5), rays=128, irr=6, dist=14, blend=N.BLEND_TENSOR,
+                      storage=N.STORAGE_FP16)
+    host, dev, vol, inp = setup(w, debug=False)
+    u = vol.uniform
+    prev = None
+    for f in range(3):
+        r = frame_rotation(33, f)
+        vol.trace(r)
+        _, rad, _ = vol.rays()
+        sync()
+        rays_np = _np(rad)
+        vol.probe_update()
+        vol.end_frame()
+        vol.check_status()
+        irr, dist = vol.atlases()
+        sync()
+        pi, pd = (None, None) if prev is None else prev
+        ref = oracle.blend(vol.desc, oracle.ray_dirs(r, u.rays_per_probe, 1, True), rays_np, pi, pd, first=(f == 0),
+                           precision=1)
+        gi, gd = _np(irr), _np(dist)
+        assert rel_err(gi, ref[0]) < 2e-3 + 2.0 ** -10, (f, rel_err(gi, ref[0]))
+        assert rel_err(gd, ref[1]) < 2e-3 + 2.0 ** -10, (f, rel_err(gd, ref[1]))
+        prev = (gi, gd)
+
+
 def test_tensor_blend_matches_fp32_blend_on_plain_small(cuda):
     from dataclasses import replace
 
