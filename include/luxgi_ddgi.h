@@ -246,14 +246,14 @@ typedef struct luxgi_ddgi_volume_desc {
                                       in the second pass, when the volume has
                                       >= 2^20 probe-rays, else one pass); -1
                                       one pass.  Per-ray variants
-                                      1-5.                                   */
+                                      1-5 and 10.                            */
     int32_t shade_order;           /* tuning, results identical: 1 bin the
                                       hits by their surface-cache chunk first
                                       (histogram, scan, scatter) so a warp
                                       shades nearby hits; -1 shade in march
                                       order; 0 default (1 when the volume has
                                       >= 2^20 probe-rays, else -1).  Per-ray
-                                      march variants 1-5.                    */
+                                      march variants 1-5 and 10.             */
     int32_t shade_split;           /* tuning, results identical: 1 the rays
                                       that end in the compacted march's first
                                       pass are sorted and shaded on a second
@@ -333,7 +333,7 @@ int luxgi_ddgi_update(luxgi_ddgi_volume* vol, const float rot[9], void* stream);
 
 /* Many volumes, one frame each.  rots = n consecutive column-major 3x3
  * matrices (host).  Volumes that share storage, light mode, blend kind, SDF
- * format and a per-ray march variant (1-5) run together, one launch per
+ * format and a per-ray march variant (1-5, 10) run together, one launch per
  * stage for the group; the rest run one after another.  A volume may appear
  * once.  The reference dispatches every volume separately
  * (DDGIRenderer.cpp:217-464); this call replaces a loop over those
@@ -356,7 +356,7 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n,
 typedef struct luxgi_ddgi_batch luxgi_ddgi_batch;
 
 typedef struct luxgi_ddgi_batch_tuning {
-    int32_t march_variant;   /* 1-5, as luxgi_ddgi_volume_desc.march_variant  */
+    int32_t march_variant;   /* 1-5 or 10, as luxgi_ddgi_volume_desc.march_variant */
     int32_t march_threads;   /* rays per march block: 128 or 256              */
     int32_t shade_variant;   /* 1, 2, 4 or 8                                  */
     int32_t blend_probes;    /* probes per thread of the FP32-blend register

@@ -42,7 +42,8 @@ int compat_check(luxgi_ddgi_volume* const* vols, int n) {
 }
 
 bool tuning_valid(const luxgi_ddgi_batch_tuning& t) {
-    return t.march_variant >= 1 && t.march_variant <= 5 && (t.march_threads == 128 || t.march_threads == 256) &&
+    return ((t.march_variant >= 1 && t.march_variant <= 5) || t.march_variant == 10) &&
+           (t.march_threads == 128 || t.march_threads == 256) &&
            (t.shade_variant == 1 || t.shade_variant == 2 || t.shade_variant == 4 || t.shade_variant == 8) &&
            (t.blend_probes == 1 || t.blend_probes == 2 || t.blend_probes == 4) && (t.use_graph == 0 || t.use_graph == 1) &&
            t.march_budget >= -1 && t.shade_order >= -1 && t.shade_order <= 1;
@@ -172,7 +173,7 @@ int plan_build(Plan& P, luxgi_ddgi_volume* const* vols, int n, const luxgi_ddgi_
         P.qb_cap = march_qb_cap(P.work);
     }
     // batch-wide work indices are ints in the work-offset table (INT_MAX checked above)
-    P.sorted = t.shade_order == 1 && t.march_variant < 6 && n <= kBatchShadeBins / 2;
+    P.sorted = t.shade_order == 1 && !pooled_variant(t.march_variant) && n <= kBatchShadeBins / 2;
     return LUXGI_OK;
 }
 
@@ -544,8 +545,9 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* 
             if (vols[j] == vols[i]) return LUXGI_EINVAL;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // group volumes that can share launches; the pooled march variants and
-    // lone volumes take the single-volume path
+    // group volumes that can share launches (per-ray march variants 1-5
+    // and 10); the pooled march variants and lone volumes take the
+    // single-volume path
     std::vector<bool> done(size_t(n), false);
     for (int i = 0; i < n; ++i) {
         if (done[i]) continue;
@@ -554,7 +556,7 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* 
         std::vector<float> grots(rots + 9 * i, rots + 9 * i + 9);
         done[i] = true;
         const int mv = a->desc.march_variant;
-        if (a->bound && mv >= 1 && mv <= 5) {
+        if (a->bound && ((mv >= 1 && mv <= 5) || mv == 10)) {
             for (int j = i + 1; j < n; ++j) {
                 const luxgi_ddgi_volume* c = vols[j];
                 if (done[j] || !c->bound || c->desc.march_variant != mv ||
@@ -633,7 +635,7 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
     // coordinate descent: march variant x rays per block, then the march
     // compaction budget, then shade variant, then the FP32 blend's probes
     // per thread
-    for (int mv = 1; mv <= 5; ++mv) {
+    for (int mv : {1, 2, 3, 4, 5, 10}) {
         for (int tpb : {128, 256}) {
             luxgi_ddgi_batch_tuning c = best;
             c.march_variant = mv;

@@ -494,6 +494,7 @@ static void march_batch_variant(int variant, unsigned blocks, const TraceParams*
         case 3: march_batch_launch<SdfT, TPB, MINB, kQuad, kPlain>(blocks, vp, starts, n, compact, st); break;
         case 4: march_batch_launch<SdfT, TPB, MINB, kQuad, kQuad>(blocks, vp, starts, n, compact, st); break;
         case 5: march_batch_launch<SdfT, TPB, MINB, kQuad, kPair>(blocks, vp, starts, n, compact, st); break;
+        case 10: march_batch_launch<SdfT, TPB, MINB, kGather, kGather>(blocks, vp, starts, n, compact, st); break;
         default: march_batch_launch<SdfT, TPB, MINB, kPlain, kPlain>(blocks, vp, starts, n, compact, st); break;
     }
 }
@@ -501,7 +502,8 @@ static void march_batch_variant(int variant, unsigned blocks, const TraceParams*
 cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, int blocks, int variant, int tpb,
                                int sdf_format, int compact, uint32_t* qcount, cudaStream_t st) {
     if (blocks <= 0) return cudaSuccess;
-    if (variant < 1 || variant > 5 || (tpb != 128 && tpb != 256)) return cudaErrorInvalidValue;
+    if ((variant < 1 || variant > 5) && variant != 10) return cudaErrorInvalidValue;
+    if (tpb != 128 && tpb != 256) return cudaErrorInvalidValue;
     if (compact) {
         const cudaError_t e = cudaMemsetAsync(qcount, 0, 2 * sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;

@@ -147,6 +147,21 @@ def test_batch_fp16_storage_and_tuning_knobs(cuda):
     _assert_same(alone, batched)
 
 
+@pytest.mark.parametrize("tpb", [128, 256])
+def test_batch_gather_texture_march(cuda, tpb):
+    """The batched march over the gather textures (variant 10): every volume
+    equals its own update (march records exact)."""
+    _, alone, batched = _pairs(N.BLEND_FP32, n=4, seed=15)
+    batch = DDGIBatch(batched, {"march_variant": 10, "march_threads": tpb})
+    assert batch.tuning["march_variant"] == 10
+    for f in range(2):
+        rots = _rots(len(alone), f)
+        for v, r in zip(alone, rots):
+            v.update(r)
+        batch.update(rots)
+    _assert_same(alone, batched)
+
+
 def test_update_batch_groups_and_falls_back(cuda):
     _, alone, batched = _pairs(N.BLEND_FP32, n=4, seed=13)
     _, alone16, batched16 = _pairs(N.BLEND_FP32, storage=N.STORAGE_FP16, n=2, seed=14)
