@@ -24,7 +24,8 @@ probes x rays x frames / time.
                per atlas (irradiance, distance), frames 0-2: the GPU's
                atlases against the FP64 oracle's trace + blend of a seeded
                probe sample, fed the GPU's previous atlases
-  the benchmark spec   the batched (48 uneven volumes, one launch per stage, graph,
+  batched_served
+               the batched (48 uneven volumes, one launch per stage, graph,
                autotuned) and served (Poisson arrivals, memory-budget
                admission) forms on the same GPU, and the batched form's
                probe-rays/s over the plain form's `value`
@@ -71,13 +72,13 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serve200: requests per second, all sessions")
     ap.add_argument("--serve-budget-gb", type=float, default=120.0, help="serve200: device-memory budget")
     ap.add_argument("--frames-per-step", type=int, default=16, help="frames of the volume in one step")
-    ap.add_argument("--no-north-star", action="store_true", help="skip the batched and served forms")
+    ap.add_argument("--no-batched-served", action="store_true", help="skip the batched and served forms")
     ap.add_argument("--batch-tuning", default=None,
                     help="batch48: a fixed tuning (JSON object of luxgi_ddgi_batch_tuning fields) instead of the autotuner")
     ap.add_argument("--no-sequential", action="store_true",
                     help="batch48: skip the one-volume-at-a-time comparison")
     ap.add_argument("--ns-serve-seconds", type=float, default=8.0,
-                    help="north-star leg: length of the timed serving run")
+                    help="batched/served leg: length of the timed serving run")
     return ap.parse_args()
 
 
@@ -426,12 +427,12 @@ def run_ours(args, rank: int, world: int):
                 "avg_march_steps_per_ray": round(steps_total / (n_t * P * R), 2),
                 "avg_fine_samples_per_ray": round(fine_total / (n_t * P * R), 2)}
     ns = None
-    if not args.no_north_star and world == 1:
+    if not args.no_batched_served and world == 1:
         # the batched and served forms on the same GPU (one process: the
         # scaling run's ranks time the plain form only)
         del vol, dev, flush
         torch.cuda.empty_cache()
-        ns = north_star_leg(args, value)
+        ns = batched_served_leg(args, value)
     if rank != 0:
         return
     cpu, err = (None, None)
@@ -451,7 +452,7 @@ def run_ours(args, rank: int, world: int):
                      **{k: round(x, 4) for k, x in stage_avg.items()}},
         "wall_s": round(wall, 4),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
-        "atlas_rel_err_vs_fp64": err, "north_star": ns, "clocks": clk,
+        "atlas_rel_err_vs_fp64": err, "batched_served": ns, "clocks": clk,
     }
     print(json.dumps(line), flush=True)
 
@@ -629,8 +630,8 @@ def run_batch(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
-def north_star_leg(args, plain_value: float) -> dict:
-    """The forms the benchmark spec's target compares with the plain FP32
+def batched_served_leg(args, plain_value: float) -> dict:
+    """The batched and served forms, compared with the plain FP32
     single-volume form (`plain_value`): the batched form of 48 uneven
     volumes (FP16 SDFs, tensor-core blend) and a served run of 200 sessions
     over the same 48 workloads (session i runs workload i mod 48, with its
