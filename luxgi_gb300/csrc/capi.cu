@@ -230,7 +230,7 @@ SurfaceView surface_view(const luxgi_surface_desc& s, int light_mode, const floa
     return v;
 }
 
-// The surface formats this build reads and writes.
+// The surface formats the library reads and writes.
 bool surface_formats_valid(const luxgi_surface_desc& s) {
     return (s.light_format == LUXGI_COLOR_RGBA16F || s.light_format == LUXGI_COLOR_R11G11B10F) &&
            (s.gbuffer_format == LUXGI_GBUFFER_RGBA32F || s.gbuffer_format == LUXGI_GBUFFER_RGBA16F);
@@ -261,7 +261,8 @@ int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int c
 int luxgi::default_march_variant(const luxgi_sdf_desc& sdf) {
     // FP32 SDFs: the gather textures (one copy; production march 0.847 ->
     // 0.812 ms against the quad-packed copies).  FP16 SDFs: the quad-packed
-    // copies (precision config 0.789 ms against 0.794 ms with gathers).
+    // copies (16,384 probes over a 256^3 FP16 SDF: 0.789 ms against 0.794 ms
+    // with gathers).
     if (sdf.format != LUXGI_STORAGE_FP32) return 4;
     const int C = int(sdf.data.cascades_count);
     if (gather_planes_per_row(sdf.resolution * C, sdf.resolution, sdf.resolution) <= 0 ||
