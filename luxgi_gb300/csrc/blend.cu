@@ -11,6 +11,8 @@
 // followed by the gamma encode, the hysteresis mix and the store; the
 // border copy is fused into the store (each interior texel writes its
 // border mirrors too).
+#include <algorithm>
+
 #include <cuda_fp16.h>
 
 #include "atlas_io.cuh"
@@ -556,8 +558,179 @@ static cudaError_t launch_pair(const BlendParams& p, int ppi, int ppd, int bi, i
     }
 }
 
+// ------------------------------------------------ sparse distance blend
+// The distance weights are pow(cos, sharpness) cut below 1e-8: with the
+// default sharpness of 50 a texel takes ~15 % of the rays and a group of
+// four consecutive texels (one register tile) ~26 % (66 of 256).  Every
+// probe of a frame shares the directions, so the rays that carry weight for
+// a group are the same for all probes: ray_list_kernel lists them once a
+// frame, and the distance blend walks only those, in ascending order.  The
+// rays left out add fmaf(v, 0, acc) = acc in the dense blend (distances are
+// finite), so the sums are those of the dense blend, bit for bit.
+constexpr int kListThreads = 256;
+
+// One block per 4-texel group of the distance atlas: the rays whose cut
+// weight is nonzero for any of the group's texels, ascending, with the four
+// weights (a block-wide stream compaction, kListThreads rays at a time).
+__global__ void __launch_bounds__(kListThreads) ray_list_kernel(const BlendParams p) {
+    __shared__ int wsum[kListThreads / 32 + 1];
+    const int n = p.u.depth_probe_side;
+    const int Tp = blend_row_pitch(n * n);
+    const int g = int(blockIdx.x);
+    const int warp = int(threadIdx.x) / 32, lane = int(threadIdx.x) & 31;
+    const int R = p.R;
+    const float4* W4 = reinterpret_cast<const float4*>(p.w_dist);   // [R][Tp / 4]
+    int base = 0;
+    for (int r0 = 0; r0 < R; r0 += kListThreads) {
+        const int r = r0 + int(threadIdx.x);
+        float4 w = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (r < R) w = __ldg(W4 + size_t(r) * (Tp / 4) + g);
+        const bool nz = w.x != 0.0f || w.y != 0.0f || w.z != 0.0f || w.w != 0.0f;
+        const unsigned m = __ballot_sync(0xffffffffu, nz);
+        if (lane == 0) wsum[warp] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int k = 0; k < kListThreads / 32; ++k) {
+                const int c = wsum[k];
+                wsum[k] = s;
+                s += c;
+            }
+            wsum[kListThreads / 32] = s;
+        }
+        __syncthreads();
+        if (nz) {
+            const int i = base + wsum[warp] + __popc(m & ((1u << lane) - 1u));
+            p.sp_ray[size_t(g) * R + i] = r;
+            p.sp_w[size_t(g) * R + i] = w;
+        }
+        base += wsum[kListThreads / 32];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) p.sp_count[g] = base;
+}
+
+// The distance blend over the listed rays: a block takes 32 probes (a lane
+// each) and every texel group (a warp each in turn).  The probes' clamped
+// distances are staged in shared memory ray-major, [R][33] (the odd pitch
+// keeps the transposing stores free of bank conflicts).  A warp copies its
+// group's list to shared memory 32 entries at a time; each lane then reads
+// the entry (a broadcast) and its probe's distance of that ray (conflict
+// free), squares it as the dense blend does, and accumulates its four
+// texels.
+constexpr int kSparseWarps = 8;
+constexpr int kSparsePitch = 33;
+
+static_assert(32 * kSparseWarps == kBlendThreads, "the sparse and dense blocks share a launch");
+
+template <typename RT, typename AT>
+__device__ __forceinline__ void blend_dist_sparse_block(const BlendParams& p, int block, float* dsm) {
+    // dsm: [R][kSparsePitch]
+    __shared__ float4 lw[kSparseWarps][32];
+    __shared__ int lr[kSparseWarps][32];
+    const luxgi_ddgi_uniform& u = p.u;
+    const int n = u.depth_probe_side, T = n * n, W = u.depth_width;
+    const int TG = blend_row_pitch(T) / 4;
+    const int R = p.R;
+    const int p0 = block * 32;
+    for (int i = int(threadIdx.x); i < 32 * R; i += int(blockDim.x)) {
+        const int pb = i / R, r = i - pb * R;
+        const int pr = p0 + pb;
+        float d = 0.0f;
+        if (pr < p.P) {
+            const size_t o = size_t(pr) * R + r;
+            float raw;
+            if (sizeof(RT) == 16) {
+                raw = __ldg(reinterpret_cast<const float*>(static_cast<const float4*>(p.rays) + o) + 3);
+            } else {
+                const uint2 q = __ldg(static_cast<const uint2*>(p.rays) + o);
+                raw = __high2float(*reinterpret_cast<const __half2*>(&q.y));
+            }
+            d = mn(u.max_distance, raw - 0.01f);
+            if (d == -1.0f) d = u.max_distance;
+        }
+        dsm[r * kSparsePitch + pb] = d;
+    }
+    __syncthreads();
+    const int warp = int(threadIdx.x) / 32, lane = int(threadIdx.x) & 31;
+    for (int g = warp; g < TG; g += kSparseWarps) {
+        float acc[1][kTexelTile][2];
+#pragma unroll
+        for (int k = 0; k < kTexelTile; ++k) acc[0][k][0] = acc[0][k][1] = 0.0f;
+        const int cnt = __ldg(p.sp_count + g);
+        const int* rl = p.sp_ray + size_t(g) * R;
+        const float4* wl = p.sp_w + size_t(g) * R;
+        for (int c0 = 0; c0 < cnt; c0 += 32) {
+            if (c0 + lane < cnt) {
+                lr[warp][lane] = __ldg(rl + c0 + lane);
+                lw[warp][lane] = __ldg(wl + c0 + lane);
+            }
+            __syncwarp();
+            const int m = min(32, cnt - c0);
+#pragma unroll 4
+            for (int j = 0; j < m; ++j) {
+                const int r = lr[warp][j];
+                const float4 w4 = lw[warp][j];
+                const float d = dsm[r * kSparsePitch + lane];
+                const float d2 = d * d;
+                const float w[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    acc[0][k][0] = fmaf(d, w[k], acc[0][k][0]);
+                    acc[0][k][1] = fmaf(d2, w[k], acc[0][k][1]);
+                }
+            }
+            __syncwarp();
+        }
+        blend_epilogue<1, AT, 1, 2>(p, p0, g, lane, T, n, W, acc);
+    }
+}
+
+// Both kinds in one launch: the sparse distance blocks first, then the
+// dense irradiance blocks, which fill the distance blocks' last wave.
+template <typename RT, typename AT, int PPI>
+__global__ void __launch_bounds__(kBlendThreads) blend_sparse_pair_kernel(const BlendParams p, int blocks_dist) {
+    extern __shared__ __align__(16) float smem[];
+    const int b = int(blockIdx.x);
+    if (b < blocks_dist) blend_dist_sparse_block<RT, AT>(p, b, smem);
+    else blend_block<0, RT, AT, PPI>(p, b - blocks_dist, smem);
+}
+
+template <typename RT, typename AT, int PPI>
+static cudaError_t launch_sparse_pair_pp(const BlendParams& p, int bi, int bd, size_t sm, cudaStream_t st) {
+    auto k = blend_sparse_pair_kernel<RT, AT, PPI>;
+    if (sm > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+        if (e != cudaSuccess) return e;
+    }
+    k<<<bi + bd, kBlendThreads, sm, st>>>(p, bd);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <typename RT, typename AT>
+static cudaError_t launch_sparse_pair(const BlendParams& p, int ppi, int bi, int bd, size_t sm, cudaStream_t st) {
+    switch (ppi) {
+        case 1: return launch_sparse_pair_pp<RT, AT, 1>(p, bi, bd, sm, st);
+        case 2: return launch_sparse_pair_pp<RT, AT, 2>(p, bi, bd, sm, st);
+        case 4: return launch_sparse_pair_pp<RT, AT, 4>(p, bi, bd, sm, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_blend(const BlendParams& p, cudaStream_t st) {
     if (p.P <= 0) return cudaSuccess;
+    if (kTexelTile == 4 && p.sp_count && p.R <= kSparseMaxRays) {
+        // the distance kind over the listed rays and the irradiance kind, one launch
+        const int TG = blend_row_pitch(p.u.depth_probe_side * p.u.depth_probe_side) / 4;
+        ray_list_kernel<<<TG, kListThreads, 0, st>>>(p);
+        note_launch();
+        const int ppi = auto_pp(p, false);
+        const int bi = blend_blocks(p, false, ppi), bd = (p.P + 31) / 32;
+        const size_t sm = std::max(sizeof(float) * size_t(p.R) * kSparsePitch, blend_smem(p, false, ppi));
+        return p.storage == LUXGI_STORAGE_FP16 ? launch_sparse_pair<uint2, __half>(p, ppi, bi, bd, sm, st)
+                                               : launch_sparse_pair<float4, float>(p, ppi, bi, bd, sm, st);
+    }
     const int ppi = auto_pp(p, false), ppd = auto_pp(p, true);
     const int bi = blend_blocks(p, false, ppi), bd = blend_blocks(p, true, ppd);
     const size_t si = blend_smem(p, false, ppi), sd = blend_smem(p, true, ppd);

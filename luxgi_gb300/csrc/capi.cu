@@ -153,7 +153,8 @@ void free_volume(luxgi_ddgi_volume* v) {
                     v->w_irr, v->w_dist, v->n_irr, v->n_dist, v->tc_irr, v->tc_dist, v->tcw_irr, v->tcw_dist,
                     v->status, v->hit_t, v->hit_c, v->w2l, v->shade_chunks, v->shade_culled, v->shade_scratch,
                     v->sdf_quad, v->mip_quad, v->mq, v->mq_count, v->cell_min, v->shade_bins, v->shade_key,
-                    v->shade_order, v->split_bins, v->split_key, v->split_order};
+                    v->shade_order, v->split_bins, v->split_key, v->split_order, v->sp_count, v->sp_ray,
+                    v->sp_w};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     gather_free(v->sdf_gt);
@@ -285,6 +286,7 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
     b += 2 * 16 * R + PR * ray_elem_bytes(d.storage) + 4 * uint64_t(blend_row_pitch(int(Ti)) + blend_row_pitch(int(Td))) * R + 8 * (Ti + Td) + 16 +
          PR * (16 + 4);
     if (d.blend == LUXGI_BLEND_TENSOR) b += PR * 16 + 2 * ((Ti + 15) / 16 * 16 + (Td + 15) / 16 * 16) * R;
+    else if (R <= uint64_t(kSparseMaxRays)) b += uint64_t(blend_row_pitch(int(Td)) / 4) * (4 + 20 * R);
     const uint64_t nobj = surf.data.objects_count;
     uint64_t cap = surf.data.culled_objects_capacity;
     if (cap == 0) cap = 1 + 40ull * 40 * 40 * (nobj + 1);
@@ -519,6 +521,9 @@ void luxgi::volume_blend_params(const luxgi_ddgi_volume* v, BlendParams& p) {
     p.first = v->frames == 0;
     p.P = v->P;
     p.R = v->R;
+    p.sp_count = v->sp_count;
+    p.sp_ray = v->sp_ray;
+    p.sp_w = v->sp_w;
 }
 
 namespace {
@@ -781,6 +786,14 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (e == cudaSuccess) e = dmalloc(&v->status, sizeof(uint32_t) * 4);
     if (e == cudaSuccess) e = dmalloc(&v->hit_t, sizeof(float4) * PR);
     if (e == cudaSuccess) e = dmalloc(&v->hit_c, sizeof(int) * PR);
+    if (!v->tc && v->R <= kSparseMaxRays) {
+        // the sparse distance blend's ray lists: per 4-texel group, up to R
+        // ray indices and their weights
+        const size_t groups = size_t(blend_row_pitch(v->Td) / 4);
+        if (e == cudaSuccess) e = dmalloc(&v->sp_count, sizeof(int) * groups);
+        if (e == cudaSuccess) e = dmalloc(&v->sp_ray, sizeof(int) * groups * v->R);
+        if (e == cudaSuccess) e = dmalloc(&v->sp_w, sizeof(float4) * groups * v->R);
+    }
     if (v->tc) {
         if (e == cudaSuccess) e = dmalloc(&v->tc_irr, sizeof(__half) * PR * 4);
         if (e == cudaSuccess) e = dmalloc(&v->tc_dist, sizeof(__half) * PR * 4);

@@ -140,7 +140,16 @@ struct BlendParams {
     __half* tcw_dist;        // [tc_nd][R]
     int tc_ni, tc_nd;        // tensor-core weight rows (texels padded to 16)
     int storage, first, P, R;
+    // the distance blend's contributing rays (blend.cu, sparse distance
+    // blend), or nullptr: per 4-texel group g, sp_count[g] rays, their
+    // indices sp_ray[g * R + i] ascending and their four weights sp_w[g * R + i]
+    int* sp_count;
+    int* sp_ray;
+    float4* sp_w;
 };
+// Rays a volume may have for the sparse distance blend (its shared-memory
+// column of distances, 33 floats a ray, within a 227 KB block).
+constexpr int kSparseMaxRays = 1536;
 
 cudaError_t launch_raygen(const Rot& rot, int R, int storage, float4* dirs_trace, float4* dirs_blend,
                           cudaStream_t st);

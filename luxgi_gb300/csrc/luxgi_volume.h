@@ -31,6 +31,9 @@ struct luxgi_ddgi_volume {
     float* w_dist = nullptr;
     float* n_irr = nullptr;
     float* n_dist = nullptr;
+    int* sp_count = nullptr;           // sparse distance blend: contributing rays per texel group
+    int* sp_ray = nullptr;
+    float4* sp_w = nullptr;
     __half* tc_irr = nullptr;
     __half* tc_dist = nullptr;
     __half* tcw_irr = nullptr;
