@@ -662,16 +662,15 @@ __device__ __forceinline__ void blend_dist_sparse_block(const BlendParams& p, in
         const float4* wl = p.sp_w + size_t(g) * R;
         for (int c0 = 0; c0 < cnt; c0 += 32) {
             if (c0 + lane < cnt) {
-                lr[warp][lane] = __ldg(rl + c0 + lane);
+                lr[warp][lane] = __ldg(rl + c0 + lane) * kSparsePitch;   // the ray's row of distances
                 lw[warp][lane] = __ldg(wl + c0 + lane);
             }
             __syncwarp();
             const int m = min(32, cnt - c0);
-#pragma unroll 4
+#pragma unroll 8
             for (int j = 0; j < m; ++j) {
-                const int r = lr[warp][j];
                 const float4 w4 = lw[warp][j];
-                const float d = dsm[r * kSparsePitch + lane];
+                const float d = dsm[lr[warp][j] + lane];
                 const float d2 = d * d;
                 const float w[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
