@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_fp16.h>
 
 #include "luxgi_ddgi.h"
@@ -34,26 +35,43 @@ __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y
 __device__ __forceinline__ float len3(f3 a) { return sqrtf(dot3(a, a)); }
 __device__ __forceinline__ f3 norm3(f3 a) { float inv = 1.0f / sqrtf(dot3(a, a)); return mul3(a, inv); }
 
-// x / d for a divisor fixed over a loop.  When d is a power of two (with a
-// normal reciprocal) x * (1 / d) is the same real number as x / d and both
-// round it once, so the multiply gives the IEEE quotient bit for bit;
-// otherwise the division itself runs.
+// x / d for a divisor d > 0 fixed over a loop, bit for bit the IEEE quotient
+// RN(x / d), without a division per call.  y = RN(1 / d) is computed once.
+// q0 = RN(x y) lies within 1.5 ulp of x / d; one correction with the
+// remainder, q1 = RN(q0 + RN(x - d q0) y), brings it within 1 ulp (the
+// error left is |x - d q0| |y - 1/d|, a few 2^-24 ulp); a second, whose
+// remainder x - d q1 an FMA computes exactly, rounds to RN(x / d) by
+// Markstein's theorem (y within 1/2 ulp of 1/d, q1 within 1 ulp of x / d;
+// P. Markstein, IBM J. Res. Dev. 34(1), 1990), as long as no intermediate
+// leaves the normal range, which holds for |x| in [2^-100, 2^100] and the
+// march's divisors (cascade extents, voxel sizes, the cascade count).  The
+// remainder is kept negated (d q - x) so that x = -0 gives -0 like the
+// division.  For a power of two d both corrections add zero.
+// tests/exact_div_check.c checks the sequence against IEEE division over
+// every significand of x (both signs, several binades, signed zeros) for
+// the engine's default cascade divisors and significands at the edges.
 struct ExactDiv {
-    float d, inv;
-    bool pow2;
+    float d, y;
+    bool pow2;   // d a power of two with a normal reciprocal: x y is exact
 };
 
 __device__ __forceinline__ ExactDiv exact_div(float d) {
-    ExactDiv e;
     const uint32_t b = __float_as_uint(d);
     const uint32_t ex = (b >> 23) & 0xFFu;
-    e.d = d;
-    e.pow2 = (b & 0x7FFFFFu) == 0u && ex >= 2u && ex <= 252u;
-    e.inv = e.pow2 ? 1.0f / d : 0.0f;
-    return e;
+    return ExactDiv{d, 1.0f / d, (b & 0x7FFFFFu) == 0u && ex >= 2u && ex <= 252u};
 }
 
-__device__ __forceinline__ float xdiv(float x, const ExactDiv& e) { return e.pow2 ? x * e.inv : x / e.d; }
+// POW2: every divisor of the loop is a power of two (the corrections would
+// add zero), chosen outside the loop so the steps carry no test for it.
+template <bool POW2>
+__device__ __forceinline__ float xdiv(float x, const ExactDiv& e) {
+    float q = x * e.y;
+    if (POW2) return q;
+    float r = fmaf(e.d, q, -x);
+    q = fmaf(-r, e.y, q);
+    r = fmaf(e.d, q, -x);
+    return fmaf(-r, e.y, q);
+}
 
 // sin/cos for the Fibonacci azimuth: Cody-Waite reduction by pi/2 and Taylor
 // polynomials of degree 9 (sin) and 8 (cos) on [-pi/4, pi/4].
@@ -468,7 +486,7 @@ __device__ __forceinline__ void march_state_init(MarchState& m) {
 // whose rays hit at different steps fetch their normal taps together.  The
 // surface-cache shadow rays start 2 voxels along and skip it
 // (SDFDeferredLight.frag:104-111).
-template <typename T, int QMIP = kPlain, int QTEX = kPlain>
+template <typename T, int QMIP = kPlain, int QTEX = kPlain, bool SPLIT = true>
 __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps,
                                           MarchState& m, int budget, MarchHit& hit, float start_bias = 0.0f) {
     const int C = s.C;
@@ -510,76 +528,91 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
         // suspended where it stands)
         const int room = max_steps - step;
         const int last = step + (budget < room ? budget : room);
-        for (; step < last && t < m.is_y; ++step) {
-            const f3 sp = add3(wpos, mul3(dir, t));
-            // getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
-            const float ux = clampf(xdiv(sp.x - cx, div_md) + 0.5f, 0.0f, 1.0f);
-            const float uy = clampf(xdiv(sp.y - cy, div_md) + 0.5f, 0.0f, 1.0f);
-            const float uz = clampf(xdiv(sp.z - cz, div_md) + 0.5f, 0.0f, 1.0f);
-            const float tu = xdiv(float(cascade) + ux, div_c);
-            // the full-resolution taps are issued together with the mip taps
-            // (one memory round trip per step) unless the cell minima show
-            // their value cannot be used; it is used only where
-            // SDFCommon.glsl:150-158 samples the full-resolution SDF
-            float sd, sdt;
-            if (QTEX == kQuad || QTEX == kGather) {
-                // the cell test and the quad / gather sample share the floors
-                // of the full-resolution texel coordinates
-                const float fx = tu * float(TW) - 0.5f, fy = uy * float(s.res) - 0.5f, fz = uz * float(s.res) - 0.5f;
-                const float lx = floorf(fx), ly = floorf(fy), lz = floorf(fz);
-                const int ix = int(lx), iy = int(ly), iz = int(lz);
-                const bool need_fine = fine_needed_at(s, ix, iy, iz);
-                // tu, uy, uz lie in [0, 1] (clamped above; tu = (cascade + ux) / C),
-                // so ix, iy lie in [-1, W - 1] (a NaN converts to 0)
-                if (QMIP == kQuad)
-                    sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
-                                               s.mres, tu, uy, uz);
-                else
-                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
-                if (!need_fine)
-                    sdt = 1.0f;
-                else if (QTEX == kGather)
-                    sdt = gather_lerp<T>(s.sdf_g, TW, s.res, s.res, fx - lx, fy - ly, fz - lz, ix, iy, iz);
-                else
-                    sdt = quad_lerp_unit<T>(static_cast<const typename Quad<T>::type*>(s.sdf_quad), TW, s.res, s.res,
-                                            fx - lx, fy - ly, fz - lz, ix, iy, iz);
-            } else {
-                const bool need_fine = fine_needed(s, tu, uy, uz);
-                if (QMIP == kPlain)
-                    sd = sample3d_unit<T>(static_cast<const T*>(s.mip), MW, s.mres, s.mres, tu, uy, uz);
-                else if (QMIP == kQuad)
-                    sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
-                                               s.mres, tu, uy, uz);
-                else
-                    sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
-                if (!need_fine)
-                    sdt = 1.0f;
-                else if (QTEX == kPlain)
-                    sdt = sample3d_unit<T>(static_cast<const T*>(s.sdf), TW, s.res, s.res, tu, uy, uz);
-                else
-                    sdt = sample_vol<T, QTEX>(s.sdf, s.sdf_quad, s.sdf_g, TW, s.res, s.res, tu, uy, uz);
+        // the step loop, compiled twice (SPLIT): with multiplies alone when
+        // the cascade's divisors are all powers of two, with the corrected
+        // quotients otherwise (the choice is the cascade's, outside the
+        // loop); without SPLIT once, with the corrected quotients, for
+        // kernels whose registers cannot hold two copies without spilling
+        auto steps = [&](auto pow2) -> bool {
+            constexpr bool P2 = decltype(pow2)::value;
+            for (; step < last && t < m.is_y; ++step) {
+                const f3 sp = add3(wpos, mul3(dir, t));
+                // getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
+                const float ux = clampf(xdiv<P2>(sp.x - cx, div_md) + 0.5f, 0.0f, 1.0f);
+                const float uy = clampf(xdiv<P2>(sp.y - cy, div_md) + 0.5f, 0.0f, 1.0f);
+                const float uz = clampf(xdiv<P2>(sp.z - cz, div_md) + 0.5f, 0.0f, 1.0f);
+                const float tu = xdiv<P2>(float(cascade) + ux, div_c);
+                // the full-resolution taps are issued together with the mip taps
+                // (one memory round trip per step) unless the cell minima show
+                // their value cannot be used; it is used only where
+                // SDFCommon.glsl:150-158 samples the full-resolution SDF
+                float sd, sdt;
+                if (QTEX == kQuad || QTEX == kGather) {
+                    // the cell test and the quad / gather sample share the floors
+                    // of the full-resolution texel coordinates
+                    const float fx = tu * float(TW) - 0.5f, fy = uy * float(s.res) - 0.5f, fz = uz * float(s.res) - 0.5f;
+                    const float lx = floorf(fx), ly = floorf(fy), lz = floorf(fz);
+                    const int ix = int(lx), iy = int(ly), iz = int(lz);
+                    const bool need_fine = fine_needed_at(s, ix, iy, iz);
+                    // tu, uy, uz lie in [0, 1] (clamped above; tu = (cascade + ux) / C),
+                    // so ix, iy lie in [-1, W - 1] (a NaN converts to 0)
+                    if (QMIP == kQuad)
+                        sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
+                                                   s.mres, tu, uy, uz);
+                    else
+                        sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
+                    if (!need_fine)
+                        sdt = 1.0f;
+                    else if (QTEX == kGather)
+                        sdt = gather_lerp<T>(s.sdf_g, TW, s.res, s.res, fx - lx, fy - ly, fz - lz, ix, iy, iz);
+                    else
+                        sdt = quad_lerp_unit<T>(static_cast<const typename Quad<T>::type*>(s.sdf_quad), TW, s.res, s.res,
+                                                fx - lx, fy - ly, fz - lz, ix, iy, iz);
+                } else {
+                    const bool need_fine = fine_needed(s, tu, uy, uz);
+                    if (QMIP == kPlain)
+                        sd = sample3d_unit<T>(static_cast<const T*>(s.mip), MW, s.mres, s.mres, tu, uy, uz);
+                    else if (QMIP == kQuad)
+                        sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
+                                                   s.mres, tu, uy, uz);
+                    else
+                        sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
+                    if (!need_fine)
+                        sdt = 1.0f;
+                    else if (QTEX == kPlain)
+                        sdt = sample3d_unit<T>(static_cast<const T*>(s.sdf), TW, s.res, s.res, tu, uy, uz);
+                    else
+                        sdt = sample_vol<T, QTEX>(s.sdf, s.sdf_quad, s.sdf_g, TW, s.res, s.res, tu, uy, uz);
+                }
+                if (sd < chunk) {
+                    ++m.fine;
+                    if (sdt < margin * 2.0f) sd = sdt;
+                } else {
+                    sd = chunk;
+                }
+                sd = sd * md;
+                const float thick = voxel_half * clampf(xdiv<P2>(t, div_voxel), 0.0f, 1.0f);
+                if (sd < thick) {
+                    hit.time = mx(t + sd - thick, 0.0f);
+                    hit.cascade = cascade;
+                    hit.sdf = sd;
+                    hit.normal = f3{0.0f, 0.0f, 0.0f};
+                    hit.u = tu;
+                    hit.v = uy;
+                    hit.w = uz;
+                    hit.steps = m.steps + step;
+                    hit.fine = m.fine;
+                    return true;
+                }
+                t = t + mx(sd * 1.0f, voxel);
             }
-            if (sd < chunk) {
-                ++m.fine;
-                if (sdt < margin * 2.0f) sd = sdt;
-            } else {
-                sd = chunk;
-            }
-            sd = sd * md;
-            const float thick = voxel_half * clampf(xdiv(t, div_voxel), 0.0f, 1.0f);
-            if (sd < thick) {
-                hit.time = mx(t + sd - thick, 0.0f);
-                hit.cascade = cascade;
-                hit.sdf = sd;
-                hit.normal = f3{0.0f, 0.0f, 0.0f};
-                hit.u = tu;
-                hit.v = uy;
-                hit.w = uz;
-                hit.steps = m.steps + step;
-                hit.fine = m.fine;
+            return false;
+        };
+        if constexpr (SPLIT) {
+            if (div_md.pow2 && div_c.pow2 && div_voxel.pow2 ? steps(std::true_type{}) : steps(std::false_type{}))
                 return true;
-            }
-            t = t + mx(sd * 1.0f, voxel);
+        } else {
+            if (steps(std::false_type{})) return true;
         }
         if (step < max_steps && t < m.is_y) {
             // the budget ran out first
