@@ -1069,7 +1069,7 @@ __device__ __forceinline__ void bilinear_repeat_v(const void* p, int storage, in
 // FP32 resolves only to W x 6e-8 texel (2e-3 texel in a 32,770-texel-wide
 // atlas).  Here the cell corner (an integer) and the offset inside the cell
 // are kept apart: oct_cell_point gives the sample point inside the cell,
-// (octEncode(d) + 1) / 2 * side - 0.5 per axis, and bilinear_tap_v adds the
+// (octEncode(d) + 1) / 2 * side - 0.5 per axis, and bilinear_at_t adds the
 // corner after the floor, so the bilinear fractions keep FP32's precision
 // (~1e-7 texel).  The texels and weights are those of the shader's formula
 // evaluated exactly.
@@ -1088,13 +1088,13 @@ __device__ __forceinline__ void oct_cell_point(f3 d, int side, float& rx, float&
     ry = (oy + 1.0f) * 0.5f * float(side) - 0.5f;
 }
 
-// Bilinear tap of NC channels at texel (x0 + rx, y0 + ry) of a W-wide atlas,
-// (x0, y0) the interior corner of a probe cell (cell * (side + 2) + 2) and
-// (rx, ry) from oct_cell_point.  rx lies in [-0.5, side - 0.5], so the four
-// texels stay inside the cell and its 1-texel border (the clamp only guards
-// a NaN direction, which converts to the cell's first texel).  tap_frac
-// splits the point into its texel corner and fractions, which a direction
-// shared by several cells (sampleIrradiance's normal) computes once.
+// A bilinear tap at texel (x0 + rx, y0 + ry) of an atlas, (x0, y0) the
+// interior corner of a probe cell (cell * (side + 2) + 2) and (rx, ry) from
+// oct_cell_point.  rx lies in [-0.5, side - 0.5], so the four texels stay
+// inside the cell and its 1-texel border (the clamp only guards a NaN
+// direction, which converts to the cell's first texel).  tap_frac splits the
+// point into its texel corner and fractions, which a direction shared by
+// several cells (sampleIrradiance's normal) computes once.
 struct TapFrac {
     int ix, iy;   // texel corner relative to the cell's interior corner
     float a, b;   // fractions
@@ -1111,28 +1111,51 @@ __device__ __forceinline__ TapFrac tap_frac(int side, float rx, float ry) {
     return f;
 }
 
+// One texel's NC channels (NC = 4 irradiance, 2 distance) at p, one load.
 template <int NC>
-__device__ __forceinline__ void bilinear_at_v(const void* p, int storage, int W, int x0, int y0, const TapFrac& f,
-                                              float* out) {
-    const int i0 = x0 + f.ix, j0 = y0 + f.iy;
-    const int i1 = i0 + 1, j1 = j0 + 1;
-    const float a = f.a, b = f.b;
-    float t00[NC], t10[NC], t01[NC], t11[NC];
-    atlas_texel<NC>(p, storage, size_t(j0) * W + i0, t00);
-    atlas_texel<NC>(p, storage, size_t(j0) * W + i1, t10);
-    atlas_texel<NC>(p, storage, size_t(j1) * W + i0, t01);
-    atlas_texel<NC>(p, storage, size_t(j1) * W + i1, t11);
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-        const float r0 = t00[c] * (1.0f - a) + t10[c] * a, r1 = t01[c] * (1.0f - a) + t11[c] * a;
-        out[c] = r0 * (1.0f - b) + r1 * b;
+__device__ __forceinline__ void texel_ld(const float* p, float* out) {
+    if (NC == 4) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+        out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
+    } else {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+        out[0] = v.x; out[1] = v.y;
+    }
+}
+template <int NC>
+__device__ __forceinline__ void texel_ld(const __half* p, float* out) {
+    if (NC == 4) {
+        const uint2 raw = __ldg(reinterpret_cast<const uint2*>(p));
+        const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
+        const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
+        out[0] = __low2float(a); out[1] = __high2float(a); out[2] = __low2float(b); out[3] = __high2float(b);
+    } else {
+        const __half2 a = __ldg(reinterpret_cast<const __half2*>(p));
+        out[0] = __low2float(a); out[1] = __high2float(a);
     }
 }
 
-template <int NC>
-__device__ __forceinline__ void bilinear_tap_v(const void* p, int storage, int W, int side, int x0, int y0, float rx,
-                                               float ry, float* out) {
-    bilinear_at_v<NC>(p, storage, W, x0, y0, tap_frac(side, rx, ry), out);
+// Bilinear tap of NC channels at texel (x0 + f.ix, y0 + f.iy) .. + 1 of an
+// atlas of element ST with `row` elements a texel row.  Both texel indices
+// are >= 0 (x0, y0 >= 2, f.ix, f.iy >= -1), so the two row pointers come
+// from unsigned 32 x 64-bit products and the second texel of a row is the
+// next one: four loads off two pointers.
+template <int NC, typename ST>
+__device__ __forceinline__ void bilinear_at_t(const ST* __restrict__ base, size_t row, uint32_t x0, uint32_t y0,
+                                              const TapFrac& f, float* out) {
+    const ST* r0 = base + size_t(y0 + uint32_t(f.iy)) * row + size_t(x0 + uint32_t(f.ix)) * NC;
+    const ST* r1 = r0 + row;
+    const float a = f.a, b = f.b;
+    float t00[NC], t10[NC], t01[NC], t11[NC];
+    texel_ld<NC>(r0, t00);
+    texel_ld<NC>(r0 + NC, t10);
+    texel_ld<NC>(r1, t01);
+    texel_ld<NC>(r1 + NC, t11);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const float r0c = t00[c] * (1.0f - a) + t10[c] * a, r1c = t01[c] * (1.0f - a) + t11[c] * a;
+        out[c] = r0c * (1.0f - b) + r1c * b;
+    }
 }
 
 // pow(x, e) of the irradiance decode; x*x*sqrt(x) for the default gamma
@@ -1141,22 +1164,36 @@ __device__ __forceinline__ float pow_decode(float x, float e) {
     return (e == 2.5f) ? x * x * sqrtf(x) : powf(x, e);
 }
 
-// sampleIrradiance (DDGICommon.glsl:163-233).  The normal-bias vector and
-// the octahedral coordinate of N (its texel corner and fractions in every
-// irradiance cell) are the same for the 8 cage probes and are computed once.
+// sampleIrradiance (DDGICommon.glsl:163-233) over atlases of element ST.
+// The normal-bias vector and the octahedral coordinate of N (its texel
+// corner and fractions in every irradiance cell) are the same for the 8
+// cage probes and are computed once, and so are, per axis, the two
+// candidate grid coordinates, their positions and their trilinear weights
+// (the same expressions the shader evaluates per probe).
 // FAST (hit shading, compared by tolerance): the probe-to-point direction is
 // normalised once and the distance taken from the same reciprocal root.
-template <int UNROLL = 1, bool FAST = false>
-__device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, f3 P, f3 N, f3 Wo) {
-    const f3 start{u.start_position[0], u.start_position[1], u.start_position[2]};
-    const f3 stp{u.step[0], u.step[1], u.step[2]};
-    const int cnt[3] = {u.probe_counts[0], u.probe_counts[1], u.probe_counts[2]};
-    int base[3] = {int((P.x - start.x) / stp.x), int((P.y - start.y) / stp.y), int((P.z - start.z) / stp.z)};
+template <int UNROLL, bool FAST, typename ST>
+__device__ __forceinline__ f3 sample_irradiance_t(const luxgi_ddgi_uniform& u, const ST* __restrict__ irr,
+                                                  const ST* __restrict__ dist_atlas, f3 P, f3 N, f3 Wo) {
+    const float start[3] = {u.start_position[0], u.start_position[1], u.start_position[2]};
+    const float stp[3] = {u.step[0], u.step[1], u.step[2]};
+    const float pk[3] = {P.x, P.y, P.z};
+    float plo[3], phi[3], wlo[3], whi[3];
+    int glo[3], ghi[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) base[k] = imn(imx(base[k], 0), cnt[k] - 1);
-    const f3 bpos{stp.x * float(base[0]) + start.x, stp.y * float(base[1]) + start.y, stp.z * float(base[2]) + start.z};
-    const f3 alpha{clampf((P.x - bpos.x) / stp.x, 0.0f, 1.0f), clampf((P.y - bpos.y) / stp.y, 0.0f, 1.0f),
-                   clampf((P.z - bpos.z) / stp.z, 0.0f, 1.0f)};
+    for (int k = 0; k < 3; ++k) {
+        const int cnt = u.probe_counts[k];
+        const int base = imn(imx(int((pk[k] - start[k]) / stp[k]), 0), cnt - 1);
+        const float bpos = stp[k] * float(base) + start[k];
+        const float alpha = clampf((pk[k] - bpos) / stp[k], 0.0f, 1.0f);
+        // probe coordinate base + off, off in {0, 1}, clamped to the grid
+        glo[k] = base;
+        ghi[k] = imn(base + 1, cnt - 1);
+        plo[k] = bpos;
+        phi[k] = stp[k] * float(ghi[k]) + start[k];
+        wlo[k] = 1.0f - alpha;
+        whi[k] = alpha;
+    }
     f3 sum{0.0f, 0.0f, 0.0f};
     float sumw = 0.0f;
     const float ge = u.ddgi_gamma * 0.5f;
@@ -1167,22 +1204,22 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
     oct_cell_point(norm3(N), u.irradiance_probe_side, nrx, nry);
     const TapFrac nf = tap_frac(u.irradiance_probe_side, nrx, nry);
     const int ni = u.irradiance_probe_side, nd = u.depth_probe_side;
+    const size_t irow = size_t(u.irradiance_width) * 4, drow = size_t(u.depth_width) * 2;
+    const int cnt0 = u.probe_counts[0];
     // UNROLL cage probes per iteration overlap their texel fetches; the sums
     // still accumulate in probe order 0..7
 #pragma unroll UNROLL
     for (int i = 0; i < 8; ++i) {
-        const int off[3] = {i & 1, (i >> 1) & 1, (i >> 2) & 1};
-        int g[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) g[k] = imn(imx(base[k] + off[k], 0), cnt[k] - 1);
-        const f3 ppos{stp.x * float(g[0]) + start.x, stp.y * float(g[1]) + start.y, stp.z * float(g[2]) + start.z};
-        const f3 tri{off[0] ? alpha.x : 1.0f - alpha.x, off[1] ? alpha.y : 1.0f - alpha.y, off[2] ? alpha.z : 1.0f - alpha.z};
+        const bool ox = i & 1, oy = (i >> 1) & 1, oz = (i >> 2) & 1;
+        const int g0 = ox ? ghi[0] : glo[0], g1 = oy ? ghi[1] : glo[1], g2 = oz ? ghi[2] : glo[2];
+        const f3 ppos{ox ? phi[0] : plo[0], oy ? phi[1] : plo[1], oz ? phi[2] : plo[2]};
+        const f3 tri{ox ? whi[0] : wlo[0], oy ? whi[1] : wlo[1], oz ? whi[2] : wlo[2]};
         float weight = 1.0f;
         const f3 dtp = norm3(sub3(ppos, P));
         const float bf = mx(0.0001f, (dot3(dtp, N) + 1.0f) * 0.5f);
         weight = weight * (bf * bf + 0.2f);
         // probe index g0 + g1 X + g2 X Y sits in atlas cell (g0 + g1 X, g2)
-        const int cell_x = g[0] + g[1] * cnt[0], cell_y = g[2];
+        const uint32_t cell_x = uint32_t(g0 + g1 * cnt0), cell_y = uint32_t(g2);
         const f3 ptp = add3(sub3(P, ppos), vb);
         float rx, ry, dist;
         if (FAST) {
@@ -1199,8 +1236,8 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
             dist = len3(ptp);
         }
         float mm[2];
-        bilinear_tap_v<2>(A.dist, A.storage, u.depth_width, nd, cell_x * (nd + 2) + 2, cell_y * (nd + 2) + 2, rx, ry,
-                          mm);
+        bilinear_at_t<2>(dist_atlas, drow, cell_x * uint32_t(nd + 2) + 2u, cell_y * uint32_t(nd + 2) + 2u,
+                         tap_frac(nd, rx, ry), mm);
         const float mean = mm[0];
         const float mean2 = mm[1];
         const float variance = fabsf(mean * mean - mean2);
@@ -1210,7 +1247,7 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
         weight = weight * ((dist <= mean) ? 1.0f : cheb);
         weight = mx(0.000001f, weight);
         float ir[4];
-        bilinear_at_v<4>(A.irr, A.storage, u.irradiance_width, cell_x * (ni + 2) + 2, cell_y * (ni + 2) + 2, nf, ir);
+        bilinear_at_t<4>(irr, irow, cell_x * uint32_t(ni + 2) + 2u, cell_y * uint32_t(ni + 2) + 2u, nf, ir);
         const f3 pir{pow_decode(ir[0], ge), pow_decode(ir[1], ge), pow_decode(ir[2], ge)};
         const float crush = 0.2f;
         if (weight < crush) weight = weight * (weight * weight * (1.0f / (crush * crush)));
@@ -1221,6 +1258,16 @@ __device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, con
     f3 net{sum.x / sumw, sum.y / sumw, sum.z / sumw};
     net = mulv3(net, net);
     return mul3(net, 2.0f * kPi);
+}
+
+// sampleIrradiance over the atlases of a volume (FP32 or FP16 texels).
+template <int UNROLL = 1, bool FAST = false>
+__device__ __forceinline__ f3 sample_irradiance(const luxgi_ddgi_uniform& u, const AtlasView& A, f3 P, f3 N, f3 Wo) {
+    if (A.storage == LUXGI_STORAGE_FP16)
+        return sample_irradiance_t<UNROLL, FAST>(u, static_cast<const __half*>(A.irr),
+                                                 static_cast<const __half*>(A.dist), P, N, Wo);
+    return sample_irradiance_t<UNROLL, FAST>(u, static_cast<const float*>(A.irr), static_cast<const float*>(A.dist),
+                                             P, N, Wo);
 }
 
 }  // namespace luxgi
