@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # for bit are built without FMA contraction
 NO_FMAD = {"trace.cu", "setup.cu", "surface.cu", "sdfbuild.cu"}
 # shading is compared with the restatement by tolerance: approximate
-# division and square root
+# division and square root, denormals flushed to zero (the special-function
+# results need no denormal fix-ups; no shading quantity is near 1e-38)
 FAST_DIV = {"shade.cu"}
 # host code built without FMA contraction, so that its results (the seeded
 # frame rotations) are the same on x86 and aarch64 hosts
@@ -80,7 +81,7 @@ def build_cuda(verbose: bool = False) -> Path:
             if src in HOST_NO_CONTRACT:
                 cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
             if src in FAST_DIV:
-                cmd[1:1] = ["-prec-div=false", "-prec-sqrt=false"]
+                cmd[1:1] = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

@@ -860,7 +860,7 @@ __device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_su
     }
     const f3 n = norm3(mat4_mul_pt(T, nrm_local, 1.0f));
     float nw = clampf(0.0f * n.x + 0.0f * n.y + 1.0f * n.z, 0.0f, 1.0f);
-    nw = (nw - 0.05f) / (1.0f - 0.05f);
+    nw = (nw - 0.05f) * (1.0f / (1.0f - 0.05f));
     if (nw <= 0.0f) return;
     // The atlas coordinate (au, av) exactly: the reference takes the
     // bilinear fractions from fract(au * res + 0.5) but the gathered texels
@@ -875,7 +875,8 @@ __device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_su
     const float tpy = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T[1], local.x), __fmul_rn(T[5], local.y)),
                                           __fmul_rn(T[9], local.z)), T[13]);
     const float tpz = T[2] * local.x + T[6] * local.y + T[10] * local.z + T[14];
-    const float tdepth = tpz / bz;
+    const float ibz = 1.0f / bz;
+    const float tdepth = tpz * ibz;
     const float tu = clampf(__fadd_rn(__fdiv_rn(tpx, bx), 0.5f), 0.0f, 1.0f);
     const float tv = clampf(__fadd_rn(__fdiv_rn(tpy, by), 0.5f), 0.0f, 1.0f);
     const float au = __fadd_rn(__fmul_rn(tu, __ldg(&tl->extends[2])), __ldg(&tl->extends[0]));
@@ -889,11 +890,13 @@ __device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_su
     const size_t o0 = size_t(g.j1) * R + g.i0, o1 = size_t(g.j1) * R + g.i1;
     const size_t o2 = size_t(g.j0) * R + g.i1, o3 = size_t(g.j0) * R + g.i0;
     const float tz[4] = {__ldg(S.depth + o0), __ldg(S.depth + o1), __ldg(S.depth + o2), __ldg(S.depth + o3)};
-    const float dthr = 2.0f * thr / bz;
+    // the visibility ramp (|depth difference| - dthr) / (dthr / 2), with the
+    // reciprocals taken once a tile (shading compares by tolerance)
+    const float dthr = 2.0f * thr * ibz, idr = 1.0f / (thr * ibz);
     float dv[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        dv[i] = 1.0f - clampf((fabsf(tdepth - tz[i]) - dthr) / (0.5f * dthr), 0.0f, 1.0f);
+        dv[i] = 1.0f - clampf((fabsf(tdepth - tz[i]) - dthr) * idr, 0.0f, 1.0f);
         if (tz[i] >= 1.0f) dv[i] = 0.0f;
     }
     float sw = dv[0] * bw0 + dv[1] * bw1 + dv[2] * bw2 + dv[3] * bw3;
@@ -909,15 +912,16 @@ __device__ __forceinline__ void sample_tile(const SurfaceView& S, const luxgi_su
                 ch[0][2] * w0 + ch[1][2] * w1 + ch[2][2] * w2 + ch[3][2] * w3};
     acc0 = add3(acc0, mul3(c0, sw));
     if (TWO) {
+        // RGBA8 albedo: the bytes weighted, the 1/255 applied once
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const uchar4 a = __ldg(reinterpret_cast<const uchar4*>(S.color1) + offs[i]);
-            ch[i][0] = float(a.x) / 255.0f; ch[i][1] = float(a.y) / 255.0f; ch[i][2] = float(a.z) / 255.0f;
+            ch[i][0] = float(a.x); ch[i][1] = float(a.y); ch[i][2] = float(a.z);
         }
         const f3 c1{ch[0][0] * w0 + ch[1][0] * w1 + ch[2][0] * w2 + ch[3][0] * w3,
                     ch[0][1] * w0 + ch[1][1] * w1 + ch[2][1] * w2 + ch[3][1] * w3,
                     ch[0][2] * w0 + ch[1][2] * w1 + ch[2][2] * w2 + ch[3][2] * w3};
-        acc1 = add3(acc1, mul3(c1, sw));
+        acc1 = add3(acc1, mul3(c1, sw * (1.0f / 255.0f)));
     }
     accw = accw + sw;
 }
@@ -973,9 +977,9 @@ __device__ __forceinline__ float sample_surface(const SurfaceView& S, f3 pos, f3
             if (to != 0) sample_tile<TWO>(S, S.tiles + to, lp, ln, thr, acc0, acc1, accw);
         }
     }
-    const float den = mx(accw, 0.0001f);
-    out0 = f3{acc0.x / den, acc0.y / den, acc0.z / den};
-    out1 = f3{acc1.x / den, acc1.y / den, acc1.z / den};
+    const float iden = 1.0f / mx(accw, 0.0001f);
+    out0 = mul3(acc0, iden);
+    out1 = mul3(acc1, iden);
     return accw;
 }
 
@@ -1215,7 +1219,8 @@ __device__ __forceinline__ f3 sample_irradiance_t(const luxgi_ddgi_uniform& u, c
         const f3 ppos{ox ? phi[0] : plo[0], oy ? phi[1] : plo[1], oz ? phi[2] : plo[2]};
         const f3 tri{ox ? whi[0] : wlo[0], oy ? whi[1] : wlo[1], oz ? whi[2] : wlo[2]};
         float weight = 1.0f;
-        const f3 dtp = norm3(sub3(ppos, P));
+        const f3 pd = sub3(ppos, P);
+        const f3 dtp = FAST ? mul3(pd, rsqrtf(dot3(pd, pd))) : norm3(pd);
         const float bf = mx(0.0001f, (dot3(dtp, N) + 1.0f) * 0.5f);
         weight = weight * (bf * bf + 0.2f);
         // probe index g0 + g1 X + g2 X Y sits in atlas cell (g0 + g1 X, g2)

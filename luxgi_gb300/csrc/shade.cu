@@ -1,7 +1,8 @@
 // Hit shading of the march records (GISDFRays.comp:89-127): the
 // surface-cache sample and the per-hit infinite bounce.  This translation
-// unit builds with approximate division and square root and with FMA
-// contraction (-prec-div=false -prec-sqrt=false -fmad=true): shading is
+// unit builds with approximate division and square root, FMA contraction
+// and denormals flushed to zero (-prec-div=false -prec-sqrt=false -fmad=true
+// -ftz=true; no quantity of the shading lies near 1e-38): shading is
 // compared with the CPU restatement by tolerance (1e-4 relative), while the
 // march, whose hit test must reproduce the restatement's branches bit for
 // bit, stays in trace.cu with IEEE arithmetic.  The hit point and the
