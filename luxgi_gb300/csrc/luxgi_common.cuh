@@ -529,36 +529,59 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
         const int room = max_steps - step;
         const int last = step + (budget < room ? budget : room);
         // the step loop, compiled twice (SPLIT): with multiplies alone when
-        // the cascade's divisors are all powers of two, with the corrected
-        // quotients otherwise (the choice is the cascade's, outside the
-        // loop); without SPLIT once, with the corrected quotients, for
-        // kernels whose registers cannot hold two copies without spilling
+        // the cascade's divisors and the volume sizes are all powers of two,
+        // with the corrected quotients otherwise (the choice is the
+        // cascade's, outside the loop); without SPLIT once, with the
+        // corrected quotients, for kernels whose registers cannot hold two
+        // copies without spilling
         auto steps = [&](auto pow2) -> bool {
             constexpr bool P2 = decltype(pow2)::value;
             for (; step < last && t < m.is_y; ++step) {
                 const f3 sp = add3(wpos, mul3(dir, t));
                 // getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
-                const float ux = clampf(xdiv<P2>(sp.x - cx, div_md) + 0.5f, 0.0f, 1.0f);
-                const float uy = clampf(xdiv<P2>(sp.y - cy, div_md) + 0.5f, 0.0f, 1.0f);
-                const float uz = clampf(xdiv<P2>(sp.z - cz, div_md) + 0.5f, 0.0f, 1.0f);
-                const float tu = xdiv<P2>(float(cascade) + ux, div_c);
+                // (with a power-of-two extent the quotient is an exact
+                // scaling, so one FMA rounds like the multiply and the add)
+                const float ux = clampf(P2 ? fmaf(sp.x - cx, div_md.y, 0.5f) : xdiv<P2>(sp.x - cx, div_md) + 0.5f,
+                                        0.0f, 1.0f);
+                const float uy = clampf(P2 ? fmaf(sp.y - cy, div_md.y, 0.5f) : xdiv<P2>(sp.y - cy, div_md) + 0.5f,
+                                        0.0f, 1.0f);
+                const float uz = clampf(P2 ? fmaf(sp.z - cz, div_md.y, 0.5f) : xdiv<P2>(sp.z - cz, div_md) + 0.5f,
+                                        0.0f, 1.0f);
+                const float cu = float(cascade) + ux;
+                const float tu = xdiv<P2>(cu, div_c);
                 // the full-resolution taps are issued together with the mip taps
                 // (one memory round trip per step) unless the cell minima show
                 // their value cannot be used; it is used only where
                 // SDFCommon.glsl:150-158 samples the full-resolution SDF
                 float sd, sdt;
                 if (QTEX == kQuad || QTEX == kGather) {
+                    // texel coordinates u W - 0.5 of the full-resolution (f)
+                    // and mip (g) volumes.  With power-of-two sizes and
+                    // divisors tu W = cu res exactly (tu = cu / C, W = res C),
+                    // so one FMA rounds like the multiply and the subtraction.
+                    float fx, fy, fz, gx, gy, gz;
+                    if constexpr (P2) {
+                        const float r = float(s.res), mr = float(s.mres);
+                        fx = fmaf(cu, r, -0.5f); fy = fmaf(uy, r, -0.5f); fz = fmaf(uz, r, -0.5f);
+                        gx = fmaf(cu, mr, -0.5f); gy = fmaf(uy, mr, -0.5f); gz = fmaf(uz, mr, -0.5f);
+                    } else {
+                        fx = tu * float(TW) - 0.5f; fy = uy * float(s.res) - 0.5f; fz = uz * float(s.res) - 0.5f;
+                        gx = tu * float(MW) - 0.5f; gy = uy * float(s.mres) - 0.5f; gz = uz * float(s.mres) - 0.5f;
+                    }
                     // the cell test and the quad / gather sample share the floors
                     // of the full-resolution texel coordinates
-                    const float fx = tu * float(TW) - 0.5f, fy = uy * float(s.res) - 0.5f, fz = uz * float(s.res) - 0.5f;
                     const float lx = floorf(fx), ly = floorf(fy), lz = floorf(fz);
                     const int ix = int(lx), iy = int(ly), iz = int(lz);
                     const bool need_fine = fine_needed_at(s, ix, iy, iz);
                     // tu, uy, uz lie in [0, 1] (clamped above; tu = (cascade + ux) / C),
-                    // so ix, iy lie in [-1, W - 1] (a NaN converts to 0)
+                    // so the floors lie in [-1, W - 1] (a NaN converts to 0)
+                    const float mlx = floorf(gx), mly = floorf(gy), mlz = floorf(gz);
                     if (QMIP == kQuad)
-                        sd = sample3d_quad_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres,
-                                                   s.mres, tu, uy, uz);
+                        sd = quad_lerp_unit<T>(static_cast<const typename Quad<T>::type*>(s.mip_quad), MW, s.mres, s.mres,
+                                               gx - mlx, gy - mly, gz - mlz, int(mlx), int(mly), int(mlz));
+                    else if (QMIP == kGather)
+                        sd = gather_lerp<T>(s.mip_g, MW, s.mres, s.mres, gx - mlx, gy - mly, gz - mlz, int(mlx), int(mly),
+                                            int(mlz));
                     else
                         sd = sample_vol<T, QMIP>(s.mip, s.mip_quad, s.mip_g, MW, s.mres, s.mres, tu, uy, uz);
                     if (!need_fine)
@@ -609,8 +632,9 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             return false;
         };
         if constexpr (SPLIT) {
-            if (div_md.pow2 && div_c.pow2 && div_voxel.pow2 ? steps(std::true_type{}) : steps(std::false_type{}))
-                return true;
+            const bool pow2 = div_md.pow2 && div_c.pow2 && div_voxel.pow2 && (s.res & (s.res - 1)) == 0 &&
+                              (s.mres & (s.mres - 1)) == 0;
+            if (pow2 ? steps(std::true_type{}) : steps(std::false_type{})) return true;
         } else {
             if (steps(std::false_type{})) return true;
         }
