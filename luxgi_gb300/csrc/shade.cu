@@ -69,8 +69,11 @@ __device__ __forceinline__ void shade_ray(const TraceParams& p, int64_t idx) {
     }
 }
 
+// 8 blocks of 128 a SM (64 registers): the shading waits on its gathers, so
+// the warps of the eighth block pay for the few spilled bytes (production
+// shading 0.450 -> 0.420 ms against the 72 registers the compiler takes).
 template <int MODE, int UNROLL>
-__global__ void __launch_bounds__(128) shade_kernel(const TraceParams p) {
+__global__ void __launch_bounds__(128, 8) shade_kernel(const TraceParams p) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t n = p.work;
     if (p.shade_part) {
