@@ -87,8 +87,9 @@ struct Slot {
     // CUDA executor
     cudaStream_t st = nullptr;
     cudaEvent_t ev = nullptr;
-    uint8_t* host = nullptr;
-    uint8_t* dev = nullptr;
+    uint8_t* host = nullptr;       // pinned staging of the launch arguments
+    size_t hcap = 0;
+    uint8_t* dev = nullptr;        // device arguments and per-ray buffers
     size_t cap = 0;
     // group in flight
     std::vector<Request> reqs;
@@ -293,17 +294,29 @@ int cuda_launch(luxgi_server* S, Slot& sl, const std::vector<Session*>& members)
     const size_t sb = P.starts.size() * sizeof(int);
     const size_t qoff = (P.arg_bytes + sb + 15) & ~size_t(15);
     const size_t need = qoff + plan_aux_bytes(P);
-    if (need > sl.cap) {
+    // The slot's buffers grow geometrically.  The pinned staging holds the
+    // arguments alone (a few KB a volume); the device buffer, which also
+    // holds the per-ray buffers (hundreds of MB for a group of large
+    // volumes), is stream-ordered on the slot's stream, so growing it
+    // neither waits for the other slots' groups nor synchronises the device
+    // (a pinned allocation of that size stalled the whole server for
+    // ~0.2 s).  The slot is reused only after its previous group retired.
+    const size_t hneed = P.arg_bytes + sb;
+    if (hneed > sl.hcap) {
         if (sl.host) cudaFreeHost(sl.host);
-        if (sl.dev) cudaFree(sl.dev);
         sl.host = nullptr;
+        sl.hcap = 0;
+        const cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&sl.host), hneed * 2, cudaHostAllocDefault);
+        if (e != cudaSuccess) return cuda_status(e);
+        sl.hcap = hneed * 2;
+    }
+    if (need > sl.cap) {
+        if (sl.dev) cudaFreeAsync(sl.dev, sl.st);
         sl.dev = nullptr;
         sl.cap = 0;
-        const size_t cap = need * 2;
-        cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&sl.host), cap, cudaHostAllocDefault);
-        if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&sl.dev), cap);
+        const cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&sl.dev), need * 2, sl.st);
         if (e != cudaSuccess) return cuda_status(e);
-        sl.cap = cap;
+        sl.cap = need * 2;
     }
     s = prepare_all(P, sl.st);
     if (s != LUXGI_OK) return s;
