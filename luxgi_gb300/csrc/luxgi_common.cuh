@@ -73,6 +73,21 @@ __device__ __forceinline__ float xdiv(float x, const ExactDiv& e) {
     return fmaf(-r, e.y, q);
 }
 
+// How a march step loop forms its quotients: kStepPow2 multiplies alone
+// (every divisor a power of two), kStepExact the corrected quotient,
+// kStepSelect either per call by the divisor's flag.
+enum StepDiv { kStepExact = 0, kStepPow2 = 1, kStepSelect = 2 };
+template <int M>
+__device__ __forceinline__ float qdiv(float x, const ExactDiv& e) {
+    if (M == kStepPow2) return xdiv<true>(x, e);
+    if (M == kStepSelect) return e.pow2 ? xdiv<true>(x, e) : xdiv<false>(x, e);
+    return xdiv<false>(x, e);
+}
+// How march_run compiles its step loop: twice, a power-of-two copy and an
+// exact one, chosen per cascade (kDivSplit); once with exact quotients
+// (kDivExact); once choosing per quotient (kDivSelect).
+enum MarchDiv { kDivSplit = 0, kDivExact = 1, kDivSelect = 2 };
+
 // sin/cos for the Fibonacci azimuth: Cody-Waite reduction by pi/2 and Taylor
 // polynomials of degree 9 (sin) and 8 (cos) on [-pi/4, pi/4].
 __device__ __forceinline__ void fib_sincos(float x, float* s, float* c) {
@@ -486,7 +501,7 @@ __device__ __forceinline__ void march_state_init(MarchState& m) {
 // whose rays hit at different steps fetch their normal taps together.  The
 // surface-cache shadow rays start 2 voxels along and skip it
 // (SDFDeferredLight.frag:104-111).
-template <typename T, int QMIP = kPlain, int QTEX = kPlain, bool SPLIT = true>
+template <typename T, int QMIP = kPlain, int QTEX = kPlain, int DIV = kDivSplit>
 __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, float trace_max, int max_steps,
                                           MarchState& m, int budget, MarchHit& hit, float start_bias = 0.0f) {
     const int C = s.C;
@@ -528,27 +543,27 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
         // suspended where it stands)
         const int room = max_steps - step;
         const int last = step + (budget < room ? budget : room);
-        // the step loop, compiled twice (SPLIT): with multiplies alone when
-        // the cascade's divisors and the volume sizes are all powers of two,
-        // with the corrected quotients otherwise (the choice is the
-        // cascade's, outside the loop); without SPLIT once, with the
-        // corrected quotients, for kernels whose registers cannot hold two
-        // copies without spilling
-        auto steps = [&](auto pow2) -> bool {
-            constexpr bool P2 = decltype(pow2)::value;
+        // the step loop (MarchDiv): with kDivSplit compiled twice, with
+        // multiplies alone when the cascade's divisors and the volume sizes
+        // are all powers of two and with the corrected quotients otherwise
+        // (the choice is the cascade's, outside the loop); once for kernels
+        // whose registers cannot hold two copies without spilling
+        auto steps = [&](auto mode) -> bool {
+            constexpr int M = decltype(mode)::value;
+            constexpr bool P2 = M == kStepPow2;
             for (; step < last && t < m.is_y; ++step) {
                 const f3 sp = add3(wpos, mul3(dir, t));
                 // getGlobalSDFCascadeUV (SDFCommon.glsl:64-71)
                 // (with a power-of-two extent the quotient is an exact
                 // scaling, so one FMA rounds like the multiply and the add)
-                const float ux = clampf(P2 ? fmaf(sp.x - cx, div_md.y, 0.5f) : xdiv<P2>(sp.x - cx, div_md) + 0.5f,
+                const float ux = clampf(P2 ? fmaf(sp.x - cx, div_md.y, 0.5f) : qdiv<M>(sp.x - cx, div_md) + 0.5f,
                                         0.0f, 1.0f);
-                const float uy = clampf(P2 ? fmaf(sp.y - cy, div_md.y, 0.5f) : xdiv<P2>(sp.y - cy, div_md) + 0.5f,
+                const float uy = clampf(P2 ? fmaf(sp.y - cy, div_md.y, 0.5f) : qdiv<M>(sp.y - cy, div_md) + 0.5f,
                                         0.0f, 1.0f);
-                const float uz = clampf(P2 ? fmaf(sp.z - cz, div_md.y, 0.5f) : xdiv<P2>(sp.z - cz, div_md) + 0.5f,
+                const float uz = clampf(P2 ? fmaf(sp.z - cz, div_md.y, 0.5f) : qdiv<M>(sp.z - cz, div_md) + 0.5f,
                                         0.0f, 1.0f);
                 const float cu = float(cascade) + ux;
-                const float tu = xdiv<P2>(cu, div_c);
+                const float tu = qdiv<M>(cu, div_c);
                 // the full-resolution taps are issued together with the mip taps
                 // (one memory round trip per step) unless the cell minima show
                 // their value cannot be used; it is used only where
@@ -614,7 +629,7 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
                     sd = chunk;
                 }
                 sd = sd * md;
-                const float thick = voxel_half * clampf(xdiv<P2>(t, div_voxel), 0.0f, 1.0f);
+                const float thick = voxel_half * clampf(qdiv<M>(t, div_voxel), 0.0f, 1.0f);
                 if (sd < thick) {
                     hit.time = mx(t + sd - thick, 0.0f);
                     hit.cascade = cascade;
@@ -631,12 +646,16 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             }
             return false;
         };
-        if constexpr (SPLIT) {
+        if constexpr (DIV == kDivSplit) {
             const bool pow2 = div_md.pow2 && div_c.pow2 && div_voxel.pow2 && (s.res & (s.res - 1)) == 0 &&
                               (s.mres & (s.mres - 1)) == 0;
-            if (pow2 ? steps(std::true_type{}) : steps(std::false_type{})) return true;
+            if (pow2 ? steps(std::integral_constant<int, kStepPow2>{})
+                     : steps(std::integral_constant<int, kStepExact>{}))
+                return true;
+        } else if constexpr (DIV == kDivSelect) {
+            if (steps(std::integral_constant<int, kStepSelect>{})) return true;
         } else {
-            if (steps(std::false_type{})) return true;
+            if (steps(std::integral_constant<int, kStepExact>{})) return true;
         }
         if (step < max_steps && t < m.is_y) {
             // the budget ran out first

@@ -257,8 +257,11 @@ __device__ __forceinline__ f3 direct_light(const SdfView& sdf, const Fragment& f
             MarchState m;
             march_state_init(m);
             MarchHit hit;
-            march_run<T, kPlain, kPlain>(sdf, add3(f.pos, mul3(f.normal, sb)), wi, dist - bias, max_steps, m,
-                                                0x7FFFFFFF, hit, 2.0f);
+            // one step loop with the corrected quotients: the pass ran 1.10 ms
+            // with an IEEE division a step and 1.12 ms with the loop compiled
+            // twice (registers), 1.03 ms so
+            march_run<T, kPlain, kPlain, kDivExact>(sdf, add3(f.pos, mul3(f.normal, sb)), wi, dist - bias, max_steps,
+                                                    m, 0x7FFFFFFF, hit, 2.0f);
             shadow = hit.time >= 0.0f ? 0.0f : 1.0f;
         }
     } else {
