@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline time budget")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--march-variant", type=int, default=None, help="override the volume's march variant (0-5)")
+    ap.add_argument("--march-variant", type=int, default=None, help="override the volume's march variant (0-5, 10, 11)")
     ap.add_argument("--shade-variant", type=int, default=None, help="override the volume's shade variant (1,2,4,8)")
     ap.add_argument("--ray-order", type=int, default=None, help="override the volume's ray order (0, 1)")
     ap.add_argument("--march-budget", type=int, default=None, help="override the volume's march budget (-1 one pass)")

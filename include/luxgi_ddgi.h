@@ -215,9 +215,9 @@ typedef struct luxgi_ddgi_volume_desc {
     float   sky_radiance[3];       /* constant sky for misses                 */
     int32_t march_variant;         /* tuning, results identical, speed differs:
                                       0 default, settled at bind: 10 for an
-                                      FP32 SDF (4 where its planes exceed
-                                      the texture gather limits), 4 for an
-                                      FP16 SDF; 1 plain SDF layout,
+                                      FP32 SDF, 11 for an FP16 SDF (4 where
+                                      the SDF's planes exceed the texture
+                                      gather limits); 1 plain SDF layout,
                                       64-register march; 2 plain, no register
                                       bound; 3 quad-packed mip; 4 quad-packed
                                       mip + SDF (4x SDF memory); 5 quad-packed
@@ -227,7 +227,8 @@ typedef struct luxgi_ddgi_volume_desc {
                                       10 gather textures: one copy of the mip
                                       and of the SDF in 2D texture arrays,
                                       a trilinear sample two textureGathers
-                                      (1x SDF memory)                       */
+                                      (1x SDF memory); 11 quad-packed mip +
+                                      gather texture of the SDF             */
     int32_t shade_variant;         /* tuning, results identical: cage probes of
                                       sampleIrradiance per loop iteration
                                       (0 default = 1; 1, 2, 4 or 8)          */
@@ -246,14 +247,14 @@ typedef struct luxgi_ddgi_volume_desc {
                                       in the second pass, when the volume has
                                       >= 2^20 probe-rays, else one pass); -1
                                       one pass.  Per-ray variants
-                                      1-5 and 10.                            */
+                                      1-5, 10 and 11.                        */
     int32_t shade_order;           /* tuning, results identical: 1 bin the
                                       hits by their surface-cache chunk first
                                       (histogram, scan, scatter) so a warp
                                       shades nearby hits; -1 shade in march
                                       order; 0 default (1 when the volume has
                                       >= 2^20 probe-rays, else -1).  Per-ray
-                                      march variants 1-5 and 10.             */
+                                      march variants 1-5, 10 and 11.         */
     int32_t shade_split;           /* tuning, results identical: 1 the rays
                                       that end in the compacted march's first
                                       pass are sorted and shaded on a second
@@ -333,7 +334,7 @@ int luxgi_ddgi_update(luxgi_ddgi_volume* vol, const float rot[9], void* stream);
 
 /* Many volumes, one frame each.  rots = n consecutive column-major 3x3
  * matrices (host).  Volumes that share storage, light mode, blend kind, SDF
- * format and a per-ray march variant (1-5, 10) run together, one launch per
+ * format and a per-ray march variant (1-5, 10, 11) run together, one launch per
  * stage for the group; the rest run one after another.  A volume may appear
  * once.  The reference dispatches every volume separately
  * (DDGIRenderer.cpp:217-464); this call replaces a loop over those
@@ -356,7 +357,7 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n,
 typedef struct luxgi_ddgi_batch luxgi_ddgi_batch;
 
 typedef struct luxgi_ddgi_batch_tuning {
-    int32_t march_variant;   /* 1-5 or 10, as luxgi_ddgi_volume_desc.march_variant */
+    int32_t march_variant;   /* 1-5, 10 or 11, as luxgi_ddgi_volume_desc.march_variant */
     int32_t march_threads;   /* rays per march block: 128 or 256              */
     int32_t shade_variant;   /* 1, 2, 4 or 8                                  */
     int32_t blend_probes;    /* probes per thread of the FP32-blend register

@@ -42,7 +42,7 @@ int compat_check(luxgi_ddgi_volume* const* vols, int n) {
 }
 
 bool tuning_valid(const luxgi_ddgi_batch_tuning& t) {
-    return ((t.march_variant >= 1 && t.march_variant <= 5) || t.march_variant == 10) &&
+    return per_ray_variant(t.march_variant) &&
            (t.march_threads == 128 || t.march_threads == 256) &&
            (t.shade_variant == 1 || t.shade_variant == 2 || t.shade_variant == 4 || t.shade_variant == 8) &&
            (t.blend_probes == 1 || t.blend_probes == 2 || t.blend_probes == 4) && (t.use_graph == 0 || t.use_graph == 1) &&
@@ -545,8 +545,8 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* 
             if (vols[j] == vols[i]) return LUXGI_EINVAL;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // group volumes that can share launches (per-ray march variants 1-5
-    // and 10); the pooled march variants and lone volumes take the
+    // group volumes that can share launches (per-ray march variants 1-5,
+    // 10 and 11); the pooled march variants and lone volumes take the
     // single-volume path
     std::vector<bool> done(size_t(n), false);
     for (int i = 0; i < n; ++i) {
@@ -556,7 +556,7 @@ int luxgi_ddgi_update_batch(luxgi_ddgi_volume* const* vols, int n, const float* 
         std::vector<float> grots(rots + 9 * i, rots + 9 * i + 9);
         done[i] = true;
         const int mv = a->desc.march_variant;
-        if (a->bound && ((mv >= 1 && mv <= 5) || mv == 10)) {
+        if (a->bound && per_ray_variant(mv)) {
             for (int j = i + 1; j < n; ++j) {
                 const luxgi_ddgi_volume* c = vols[j];
                 if (done[j] || !c->bound || c->desc.march_variant != mv ||
@@ -635,7 +635,7 @@ int luxgi_ddgi_batch_autotune(luxgi_ddgi_batch* b, int frames, void* stream, lux
     // coordinate descent: march variant x rays per block, then the march
     // compaction budget, then shade variant, then the FP32 blend's probes
     // per thread
-    for (int mv : {1, 2, 3, 4, 5, 10}) {
+    for (int mv : {1, 2, 3, 4, 5, 10, 11}) {
         for (int tpb : {128, 256}) {
             luxgi_ddgi_batch_tuning c = best;
             c.march_variant = mv;

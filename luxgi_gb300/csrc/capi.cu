@@ -63,7 +63,7 @@ void gather_free(GatherTex& g) {
     g = GatherTex{};
 }
 
-// The gather texture of a W x H x D volume (march variant 10): planes of
+// The gather texture of a W x H x D volume (march variants 10, 11): planes of
 // (W + 2) x (H + 2) texels tiled gx to a row within the device's texture
 // gather limits, in a CUDA array made for gathers; point sampling,
 // unnormalised coordinates.  Reuses the array when the shape is unchanged.
@@ -260,15 +260,16 @@ int luxgi::march_budget_for(const luxgi_ddgi_volume_desc& d, int64_t work, int c
 }
 
 int luxgi::default_march_variant(const luxgi_sdf_desc& sdf) {
-    // FP32 SDFs: the gather textures (one copy; production march 0.847 ->
-    // 0.812 ms against the quad-packed copies).  FP16 SDFs: the quad-packed
-    // copies (16,384 probes over a 256^3 FP16 SDF: 0.789 ms against 0.794 ms
-    // with gathers).
-    if (sdf.format != LUXGI_STORAGE_FP32) return 4;
+    // FP32 SDFs: the gather textures of both volumes (one copy; production
+    // march 0.847 -> 0.812 ms against the quad-packed copies; the quad mip
+    // with the full-resolution gathers, variant 11, runs the same).  FP16
+    // SDFs: the quad-packed mip and the full-resolution gathers (precision
+    // scene, 131,072 probes: march 4.63 ms against 4.79 ms with both
+    // gathers and 4.88 ms with both quad copies).
     const int C = int(sdf.data.cascades_count);
-    if (gather_planes_per_row(sdf.resolution * C, sdf.resolution, sdf.resolution) <= 0 ||
-        gather_planes_per_row(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution) <= 0)
-        return 4;
+    if (gather_planes_per_row(sdf.resolution * C, sdf.resolution, sdf.resolution) <= 0) return 4;
+    if (sdf.format != LUXGI_STORAGE_FP32) return 11;
+    if (gather_planes_per_row(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution) <= 0) return 11;
     return 10;
 }
 
@@ -294,15 +295,16 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
     const int C = int(sdf.data.cascades_count);
     const int mv = d.march_variant == 0 ? default_march_variant(sdf) : d.march_variant;
     const int layout = pooled_variant(mv) ? mv - 4 : mv;
-    if (layout >= 3 && layout <= 5)
+    if (layout_mip_quad(layout))
         b += quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
     if (layout == 4) b += quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
     if (layout == 5) b += pair_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
-    if (layout == 10) {
-        // the two gather textures: planes with a 1-texel apron
+    {
+        // the gather textures: planes with a 1-texel apron
         const uint64_t esz = sdf.format == LUXGI_STORAGE_FP16 ? 2 : 4;
         const uint64_t r = uint64_t(sdf.resolution), m = uint64_t(sdf.mip_resolution);
-        b += esz * ((r * C + 2) * (r + 2) * r + (m * C + 2) * (m + 2) * m);
+        if (layout_sdf_gather(layout)) b += esz * (r * C + 2) * (r + 2) * r;
+        if (layout_mip_gather(layout)) b += esz * (m * C + 2) * (m + 2) * m;
     }
     if (!pooled_variant(mv)) b += cell_min_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution);
     return b;
@@ -310,20 +312,21 @@ uint64_t luxgi::volume_device_bytes(const luxgi_ddgi_volume_desc& d, const luxgi
 
 int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
     // quad-packed SDF copies for the march variants that read them
-    // (variants 3-5 per-ray threads, 7-9 the pooled march with the same layouts)
+    // (variants 3-5 and 11 per-ray threads, 7-9 the pooled march with the
+    // layouts of 3-5)
     const luxgi_sdf_desc& sdf = v->sdf;
     const int C = int(sdf.data.cascades_count);
     const int mv = v->desc.march_variant;
     const int layout = pooled_variant(mv) ? mv - 4 : mv;   // 6..9 -> 2..5
     // the quad samplers index texels with 32-bit arithmetic
     auto quad_texels = [](int W, int H, int D) { return uint64_t(W + 1) * uint64_t(H + 1) * uint64_t(D); };
-    if (layout >= 3 && quad_texels(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution) >> 32)
+    if (layout_mip_quad(layout) && quad_texels(sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution) >> 32)
         return LUXGI_EUNSUPPORTED;
     if (layout == 4 && quad_texels(sdf.resolution * C, sdf.resolution, sdf.resolution) >> 32)
         return LUXGI_EUNSUPPORTED;
-    const size_t mq = (layout >= 3 && layout <= 5) ? quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution,
-                                                                sdf.mip_resolution, sdf.format)
-                                                     : 0;
+    const size_t mq = layout_mip_quad(layout) ? quad_bytes(sdf.mip_resolution * C, sdf.mip_resolution,
+                                                           sdf.mip_resolution, sdf.format)
+                                              : 0;
     const size_t sq = (layout == 4)   ? quad_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format)
                       : (layout == 5) ? pair_bytes(sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format)
                                       : 0;
@@ -347,14 +350,19 @@ int luxgi::volume_alloc_packs(luxgi_ddgi_volume* v) {
             v->sdf_quad_bytes = sq;
         }
     }
-    // gather textures for variant 10
-    if (layout == 10) {
-        int s = gather_alloc(v->sdf_gt, sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
-        if (s == LUXGI_OK)
-            s = gather_alloc(v->mip_gt, sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
+    // gather textures for variants 10 (both volumes) and 11 (the
+    // full-resolution volume)
+    if (layout_sdf_gather(layout)) {
+        const int s = gather_alloc(v->sdf_gt, sdf.resolution * C, sdf.resolution, sdf.resolution, sdf.format);
         if (s != LUXGI_OK) return s;
     } else {
         gather_free(v->sdf_gt);
+    }
+    if (layout_mip_gather(layout)) {
+        const int s =
+            gather_alloc(v->mip_gt, sdf.mip_resolution * C, sdf.mip_resolution, sdf.mip_resolution, sdf.format);
+        if (s != LUXGI_OK) return s;
+    } else {
         gather_free(v->mip_gt);
     }
     // cell minima for every per-ray march variant (the pooled march reads none)
@@ -396,7 +404,10 @@ int luxgi::volume_prepare(luxgi_ddgi_volume* v, cudaStream_t st) {
     }
     if (v->sdf_gt.arr) {
         e = gather_fill(v->sdf_gt, v->sdf.sdf, st);
-        if (e == cudaSuccess) e = gather_fill(v->mip_gt, v->sdf.mip, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    if (v->mip_gt.arr) {
+        e = gather_fill(v->mip_gt, v->sdf.mip, st);
         if (e != cudaSuccess) return cuda_status(e);
     }
     if (v->sdf_quad) {
@@ -734,7 +745,7 @@ int luxgi_ddgi_create(const luxgi_ddgi_volume_desc* desc, luxgi_ddgi_volume** ou
     if (desc->light_mode != LUXGI_LIGHT_CACHE && desc->light_mode != LUXGI_LIGHT_PER_HIT) return LUXGI_EINVAL;
     if (desc->blend != LUXGI_BLEND_FP32 && desc->blend != LUXGI_BLEND_TENSOR) return LUXGI_EINVAL;
     if (desc->max_steps < 1) return LUXGI_EINVAL;
-    if (desc->march_variant < 0 || desc->march_variant > 10) return LUXGI_EINVAL;
+    if (desc->march_variant < 0 || desc->march_variant > 11) return LUXGI_EINVAL;
     if (desc->ray_order != 0 && desc->ray_order != 1) return LUXGI_EINVAL;
     if (desc->march_budget < -1) return LUXGI_EINVAL;
     if (desc->shade_split < -1 || desc->shade_split > 1) return LUXGI_EINVAL;

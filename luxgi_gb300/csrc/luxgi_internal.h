@@ -11,8 +11,15 @@
 namespace luxgi {
 
 // March variants 6-9 are the pooled march (warps refill finished lanes
-// from a ray pool); 1-5 and 10 run one ray per thread.
+// from a ray pool); 1-5, 10 and 11 run one ray per thread.
 inline bool pooled_variant(int mv) { return mv >= 6 && mv <= 9; }
+inline bool per_ray_variant(int mv) { return (mv >= 1 && mv <= 5) || mv == 10 || mv == 11; }
+// The SDF copies a march layout (variant, or a pooled variant's per-ray
+// twin) reads: the quad-packed mip (3-5, 11), the gather texture of the
+// full-resolution volume (10, 11) and of the mip (10).
+inline bool layout_mip_quad(int layout) { return (layout >= 3 && layout <= 5) || layout == 11; }
+inline bool layout_sdf_gather(int layout) { return layout == 10 || layout == 11; }
+inline bool layout_mip_gather(int layout) { return layout == 10; }
 
 // Texels per thread of the FP32 blend tile; the FP32 weight rows are stored
 // ray-major, [R][Tp] with Tp = T rounded up to whole tiles (padding zero).

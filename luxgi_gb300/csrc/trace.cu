@@ -463,7 +463,9 @@ static cudaError_t launch_march_passes(const TraceParams& p, cudaStream_t st, co
     // 2 plain layout, no register bound; 3 quad-packed mip; 4 quad-packed
     // mip and full-resolution volume; 5 quad-packed mip, pair-packed
     // full-resolution volume; 10 gather textures of the mip and the
-    // full-resolution volume.  All produce identical results.
+    // full-resolution volume; 11 quad-packed mip, gather texture of the
+    // full-resolution volume (the mip's loads on the LSU path, the fine
+    // samples on the texture path).  All produce identical results.
     const bool h = p.sdf.format == LUXGI_STORAGE_FP16;
     cudaError_t e;
     const TraceParams& r = rp;
@@ -474,6 +476,7 @@ static cudaError_t launch_march_passes(const TraceParams& p, cudaStream_t st, co
         case 4: e = h ? launch_march_variant<__half, 4, kQuad, kQuad>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kQuad>(p, st, r, a); break;
         case 5: e = h ? launch_march_variant<__half, 4, kQuad, kPair>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kPair>(p, st, r, a); break;
         case 10: e = h ? launch_march_variant<__half, 4, kGather, kGather>(p, st, r, a) : launch_march_variant<float, 4, kGather, kGather>(p, st, r, a); break;
+        case 11: e = h ? launch_march_variant<__half, 4, kQuad, kGather>(p, st, r, a) : launch_march_variant<float, 4, kQuad, kGather>(p, st, r, a); break;
         default: e = h ? launch_march_variant<__half, 4, kPlain, kPlain>(p, st, r, a) : launch_march_variant<float, 4, kPlain, kPlain>(p, st, r, a); break;
     }
     return e;
@@ -500,6 +503,7 @@ static void march_batch_variant(int variant, unsigned blocks, const TraceParams*
         case 4: march_batch_launch<SdfT, TPB, MINB, kQuad, kQuad>(blocks, vp, starts, n, compact, st); break;
         case 5: march_batch_launch<SdfT, TPB, MINB, kQuad, kPair>(blocks, vp, starts, n, compact, st); break;
         case 10: march_batch_launch<SdfT, TPB, MINB, kGather, kGather>(blocks, vp, starts, n, compact, st); break;
+        case 11: march_batch_launch<SdfT, TPB, MINB, kQuad, kGather>(blocks, vp, starts, n, compact, st); break;
         default: march_batch_launch<SdfT, TPB, MINB, kPlain, kPlain>(blocks, vp, starts, n, compact, st); break;
     }
 }
@@ -507,7 +511,7 @@ static void march_batch_variant(int variant, unsigned blocks, const TraceParams*
 cudaError_t launch_march_batch(const TraceParams* vp, const int* starts, int n, int blocks, int variant, int tpb,
                                int sdf_format, int compact, uint32_t* qcount, cudaStream_t st) {
     if (blocks <= 0) return cudaSuccess;
-    if ((variant < 1 || variant > 5) && variant != 10) return cudaErrorInvalidValue;
+    if (!per_ray_variant(variant)) return cudaErrorInvalidValue;
     if (tpb != 128 && tpb != 256) return cudaErrorInvalidValue;
     if (compact) {
         const cudaError_t e = cudaMemsetAsync(qcount, 0, 2 * sizeof(uint32_t), st);

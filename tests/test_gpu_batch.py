@@ -147,13 +147,14 @@ def test_batch_fp16_storage_and_tuning_knobs(cuda):
     _assert_same(alone, batched)
 
 
-@pytest.mark.parametrize("tpb", [128, 256])
-def test_batch_gather_texture_march(cuda, tpb):
-    """The batched march over the gather textures (variant 10): every volume
-    equals its own update (march records exact)."""
+@pytest.mark.parametrize("tpb,mv", [(128, 10), (256, 10), (128, 11), (256, 11)])
+def test_batch_gather_texture_march(cuda, tpb, mv):
+    """The batched march over the gather textures (variant 10; variant 11 the
+    quad-packed mip with the full-resolution gathers): every volume equals
+    its own update (march records exact)."""
     _, alone, batched = _pairs(N.BLEND_FP32, n=4, seed=15)
-    batch = DDGIBatch(batched, {"march_variant": 10, "march_threads": tpb})
-    assert batch.tuning["march_variant"] == 10
+    batch = DDGIBatch(batched, {"march_variant": mv, "march_threads": tpb})
+    assert batch.tuning["march_variant"] == mv
     for f in range(2):
         rots = _rots(len(alone), f)
         for v, r in zip(alone, rots):

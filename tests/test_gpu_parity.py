@@ -287,11 +287,12 @@ def test_sample_probe_image_matches_oracle(cuda, storage, channels):
     dict(probe_counts=(4, 2, 2), rays=40, sdf_format=N.STORAGE_FP16, storage=N.STORAGE_FP16),
     dict(probe_counts=(3, 3, 3), rays=32, spacing=9.0),       # probes outside the room: misses
 ])
-@pytest.mark.parametrize("mv", [0, 4, 10])
+@pytest.mark.parametrize("mv", [0, 4, 10, 11])
 def test_edge_shapes(cuda, kw, mv):
     """Degenerate and small shapes, with the default march variant and
-    with the quad-packed (4) and gather-texture (10) samplers, whose hit
-    normals sample one texel past the cascade's edges."""
+    with the quad-packed (4), gather-texture (10) and mixed (11: quad mip,
+    gather full resolution) samplers, whose hit normals sample one texel
+    past the cascade's edges."""
     from dataclasses import replace
 
     w = tiny_workload(**kw)
@@ -420,7 +421,7 @@ def test_march_variants_bit_identical(cuda, fmt):
 
     base = tiny_workload(probe_counts=(6, 3, 5), rays=64, sdf=64, sdf_format=fmt, cascades=2, room=20.0, prims=10)
     outs = []
-    for mv in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10):
+    for mv in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11):
         w = replace(base, volume=replace(base.volume, march_variant=mv))
         host, dev, vol, inp = setup(w)
         rot = frame_rotation(50, 0)
@@ -446,7 +447,8 @@ def test_march_compaction_and_ray_order_bit_identical(cuda, fmt):
     outs = []
     for mv, budget, order, sorder, split in ((4, -1, 0, -1, 0), (4, 1, 0, 1, 1), (4, 1, 0, 1, -1), (4, 2, 0, -1, 0),
                                              (4, 8, 0, 0, 0), (3, 2, 1, 1, 1), (4, 3, 1, 1, -1), (5, 8, 1, -1, 0),
-                                             (1, -1, 1, 0, 0), (10, 2, 0, 1, 1), (10, -1, 1, -1, 0)):
+                                             (1, -1, 1, 0, 0), (10, 2, 0, 1, 1), (10, -1, 1, -1, 0), (11, 2, 0, 1, 1),
+                                             (11, 1, 1, 1, -1)):
         w = replace(base, volume=replace(base.volume, march_variant=mv, march_budget=budget, ray_order=order,
                                          shade_order=sorder, shade_split=split))
         host, dev, vol, inp = setup(w)
