@@ -207,10 +207,13 @@ __device__ __forceinline__ void march_resume(const TraceParams& p0, const TraceP
 
 // Pass 1 keeps 9 blocks of 128 a SM (56 registers; 36 warps where 64
 // registers leave 32): the march waits on its taps, so more resident rays
-// pay for the few spilled bytes (production march 0.851 -> 0.841 ms).
+// pay for the few spilled bytes (production march 0.851 -> 0.841 ms).  The
+// gather textures of both volumes (variant 10) run best at 8 (64
+// registers: production march 0.800 -> 0.796 ms; variant 11 loses at 8).
 // MIN_BLOCKS 1 (variant 2) leaves the registers unbounded.
 template <typename SdfT, int MIN_BLOCKS, int QMIP, int QTEX>
-__global__ void __launch_bounds__(128, MIN_BLOCKS == 1 ? 2 : 9) march_kernel(const TraceParams p) {
+__global__ void __launch_bounds__(128, MIN_BLOCKS == 1 ? 2 : (QMIP == kGather && QTEX == kGather ? 8 : 9))
+    march_kernel(const TraceParams p) {
     const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= p.work) return;
     march_ray<SdfT, QMIP, QTEX>(p, idx);
