@@ -199,6 +199,15 @@ bool sdf_texels_fit(const luxgi_sdf_desc& s) {
     return r * C * r * r < (uint64_t(1) << 32) && m * C * m * m < (uint64_t(1) << 32);
 }
 
+// exact_div on the host: the same reciprocal (IEEE single division) and
+// power-of-two flag
+ExactDiv host_exact_div(float d) {
+    uint32_t b;
+    std::memcpy(&b, &d, sizeof(b));
+    const uint32_t ex = (b >> 23) & 0xFFu;
+    return ExactDiv{d, 1.0f / d, (b & 0x7FFFFFu) == 0u && ex >= 2u && ex <= 252u};
+}
+
 SdfView sdf_view(const luxgi_sdf_desc& s) {
     SdfView v{};
     v.data = s.data;
@@ -208,6 +217,11 @@ SdfView sdf_view(const luxgi_sdf_desc& s) {
     v.mres = s.mip_resolution;
     v.C = int(s.data.cascades_count);
     v.format = s.format;
+    for (int k = 0; k < 4; ++k) {
+        v.div_ext[k] = host_exact_div(s.data.cascade_pos_distance[k][3] * 2.0f);
+        v.div_voxel[k] = host_exact_div(s.data.cascade_voxel_size[k]);
+    }
+    v.div_count = host_exact_div(float(v.C));
     return v;
 }
 

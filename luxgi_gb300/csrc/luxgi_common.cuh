@@ -36,7 +36,8 @@ __device__ __forceinline__ float len3(f3 a) { return sqrtf(dot3(a, a)); }
 __device__ __forceinline__ f3 norm3(f3 a) { float inv = 1.0f / sqrtf(dot3(a, a)); return mul3(a, inv); }
 
 // x / d for a divisor d > 0 fixed over a loop, bit for bit the IEEE quotient
-// RN(x / d), without a division per call.  y = RN(1 / d) is computed once.
+// RN(x / d), without a division per call.  y = RN(1 / d) is computed once
+// (for the march's divisors on the host, with the SDF's view).
 // q0 = RN(x y) lies within 1.5 ulp of x / d; one correction with the
 // remainder, q1 = RN(q0 + RN(x - d q0) y), brings it within 1 ulp (the
 // error left is |x - d q0| |y - 1/d|, a few 2^-24 ulp); a second, whose
@@ -54,12 +55,6 @@ struct ExactDiv {
     float d, y;
     bool pow2;   // d a power of two with a normal reciprocal: x y is exact
 };
-
-__device__ __forceinline__ ExactDiv exact_div(float d) {
-    const uint32_t b = __float_as_uint(d);
-    const uint32_t ex = (b >> 23) & 0xFFu;
-    return ExactDiv{d, 1.0f / d, (b & 0x7FFFFFu) == 0u && ex >= 2u && ex <= 252u};
-}
 
 // POW2: every divisor of the loop is a power of two (the corrections would
 // add zero), chosen outside the loop so the steps carry no test for it.
@@ -404,6 +399,10 @@ struct SdfView {
     int cw, ch;             // cells along x (packed cascades) and y
     int res, mres, C;
     int format;   // luxgi_storage of the sdf/mip texels
+    // the march's loop-fixed divisors with their reciprocals, made once on
+    // the host (IEEE division there as here): per cascade 2 x its half
+    // extent and its voxel size, and the cascade count
+    ExactDiv div_ext[4], div_voxel[4], div_count;
 };
 
 constexpr int kCellSide = 4;
@@ -535,7 +534,7 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             m.in_cascade = 1;
         }
         const float md = cw * 2.0f;
-        const ExactDiv div_md = exact_div(md), div_c = exact_div(float(C)), div_voxel = exact_div(voxel);
+        const ExactDiv div_md = s.div_ext[cascade], div_c = s.div_count, div_voxel = s.div_voxel[cascade];
         float t = m.t;
         int step = m.step;
         // steps this call may take in the cascade: up to the cap, and no
