@@ -222,6 +222,9 @@ SdfView sdf_view(const luxgi_sdf_desc& s) {
         v.div_voxel[k] = host_exact_div(s.data.cascade_voxel_size[k]);
     }
     v.div_count = host_exact_div(float(v.C));
+    v.chunk = 32.0f / s.data.resolution;
+    v.margin = 4.0f / s.data.resolution;
+    v.texel = 1.0f / s.data.resolution;
     return v;
 }
 

@@ -403,6 +403,10 @@ struct SdfView {
     // the host (IEEE division there as here): per cascade 2 x its half
     // extent and its voxel size, and the cascade count
     ExactDiv div_ext[4], div_voxel[4], div_count;
+    // 32 / resolution, 4 / resolution and 1 / resolution (SDFCommon.glsl's
+    // chunk and margin in texture coordinates, the normal's offset), also
+    // divided once on the host
+    float chunk, margin, texel;
 };
 
 constexpr int kCellSide = 4;
@@ -506,8 +510,8 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
     const int C = s.C;
     const int TW = s.res * C, MW = s.mres * C;
     const float tmax = mn(trace_max, s.data.cascade_pos_distance[C - 1][3] * 2.0f);
-    const float chunk = 32.0f / s.data.resolution;
-    const float margin = 4.0f / s.data.resolution;
+    const float chunk = s.chunk;
+    const float margin = s.margin;
     const f3 end = add3(origin, mul3(dir, tmax));
     for (; m.cascade < C; ++m.cascade) {
         const int cascade = m.cascade;
@@ -682,7 +686,7 @@ template <typename T, int QTEX>
 __device__ __forceinline__ void march_hit_normal(const SdfView& s, MarchHit& hit) {
     if (hit.time >= 0.0f)
         hit.normal = sdf_normal<T, QTEX>(s.sdf, s.sdf_quad, s.sdf_g, s.res * s.C, s.res, hit.u, hit.v, hit.w,
-                                         1.0f / s.data.resolution);
+                                         s.texel);
 }
 
 // The whole march in one call.
