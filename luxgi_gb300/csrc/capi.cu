@@ -245,6 +245,7 @@ SurfaceView surface_view(const luxgi_surface_desc& s, int light_mode, const floa
         v.color0 = s.light_cache;
         v.color1 = nullptr;
     }
+    v.inv_chunk = s.data.chunk_size > 0.0f ? 1.0f / s.data.chunk_size : 0.0f;
     return v;
 }
 

@@ -801,6 +801,7 @@ struct SurfaceView {
     int color0_format;        // luxgi_color_format of color0
     const uint8_t* color1;    // albedo RGBA8 (mode B)
     const float* depth;
+    float inv_chunk;          // 1 / data.chunk_size (the march's shading bins)
 };
 
 // Exact FP32 arithmetic (round to nearest, never contracted into an FMA,

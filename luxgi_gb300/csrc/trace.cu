@@ -79,11 +79,13 @@ __device__ __forceinline__ void record_bin(const TraceParams& p, int64_t idx, ui
 // (the chunk grid of sampleGlobalSurfaceAtlas), or the last bin.
 __device__ __forceinline__ uint32_t shade_bin(const TraceParams& p, int cls, f3 origin, f3 dir, float time) {
     if (cls < 0) return p.bin_base + p.bin_span - 1;
+    // the bin only groups hits for the shading (any bin gives the same
+    // results), so the chunk comes from a multiply by the reciprocal
     const f3 hp = add3(origin, mul3(dir, time));
-    const float cs = p.surf.data.chunk_size;
-    const int cx = imn(imx(int(floorf(hp.x / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
-    const int cy = imn(imx(int(floorf(hp.y / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
-    const int cz = imn(imx(int(floorf(hp.z / cs + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const float ics = p.surf.inv_chunk;
+    const int cx = imn(imx(int(floorf(hp.x * ics + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const int cy = imn(imx(int(floorf(hp.y * ics + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
+    const int cz = imn(imx(int(floorf(hp.z * ics + float(kChunksRes * 0.5f))), 0), kChunksRes - 1);
     const uint32_t key = uint32_t((cz * kChunksRes + cy) * kChunksRes + cx);
     return p.bin_base + (p.bin_span == uint32_t(kShadeBins) ? key : key % p.bin_span);
 }
