@@ -56,6 +56,12 @@ struct ExactDiv {
     bool pow2;   // d a power of two with a normal reciprocal: x y is exact
 };
 
+__device__ __forceinline__ ExactDiv exact_div(float d) {
+    const uint32_t b = __float_as_uint(d);
+    const uint32_t ex = (b >> 23) & 0xFFu;
+    return ExactDiv{d, 1.0f / d, (b & 0x7FFFFFu) == 0u && ex >= 2u && ex <= 252u};
+}
+
 // POW2: every divisor of the loop is a power of two (the corrections would
 // add zero), chosen outside the loop so the steps carry no test for it.
 template <bool POW2>
@@ -538,7 +544,20 @@ __device__ __forceinline__ bool march_run(const SdfView& s, f3 origin, f3 dir, f
             m.in_cascade = 1;
         }
         const float md = cw * 2.0f;
-        const ExactDiv div_md = s.div_ext[cascade], div_c = s.div_count, div_voxel = s.div_voxel[cascade];
+        // the host's reciprocals (kDivSplit, kDivExact: parameters in the
+        // constant bank), or computed here (kDivSelect, the batched kernels,
+        // whose parameters sit in shared or global memory: batch48 4.61 ->
+        // 4.55 ms a frame against the copies)
+        ExactDiv div_md, div_c, div_voxel;
+        if constexpr (DIV == kDivSelect) {
+            div_md = exact_div(md);
+            div_c = exact_div(float(C));
+            div_voxel = exact_div(voxel);
+        } else {
+            div_md = s.div_ext[cascade];
+            div_c = s.div_count;
+            div_voxel = s.div_voxel[cascade];
+        }
         float t = m.t;
         int step = m.step;
         // steps this call may take in the cascade: up to the cap, and no
